@@ -1,0 +1,229 @@
+/*
+ * svo.h — C ABI of the GB300 sparse-voxel-octree engine.
+ *
+ * Three stages, each a stream-ordered call on one CUDA device:
+ *   svo_voxelize  triangles  -> voxel-fragment list   (replaces Voxelizer, src/Voxelizer.cpp:5-179)
+ *   svo_build     fragments  -> octree node pool      (replaces OctreeBuilder, src/OctreeBuilder.cpp:8-214,
+ *                                                       and Octree::Update, src/Octree.cpp:22-35)
+ *   svo_raycast   octree+rays -> hits                 (replaces Octree_RayMarchLeaf, shader/octree.glsl:179-340,
+ *                                                       as called by shader/octree_tracer.frag:23-37)
+ *
+ * Formats kept bit-for-bit from the reference:
+ *   fragment  uint32 x: vx | vy<<12 | (vz&0xff)<<24 ; uint32 y: (vz>>8)<<28 | rgb24   (shader/voxelizer.frag:40-42)
+ *   node word 0 = empty; bit31 = non-empty; interior: bits0-29 = word index of the first of 8 children;
+ *             leaf: 0xC0000000 | min(count,63)<<24 | B<<16 | G<<8 | R       (shader/octree_tag_node.comp:10-16,59;
+ *                                                                             shader/octree_alloc_node.comp:21)
+ *   the root's 8 children are words 0..7; a child block occupies 8 consecutive words.
+ *
+ * Differences from the reference, all deliberate and documented in the design notes:
+ *   - fragment order is deterministic (triangle order, then span order), the multiset is what is compared;
+ *   - child blocks are numbered by a prefix sum in word order (breadth-first, canonical) instead of racing atomics;
+ *   - leaf colour is the channel-wise integer mean floor(sum/n) (order independent) instead of a CAS running mean.
+ *
+ * Pointers marked (device) are CUDA device pointers; `stream` is a cudaStream_t (NULL = legacy default stream).
+ * Every call returns an svo_status; svo_last_error() gives a readable message for the calling thread.
+ */
+#ifndef SVO_H
+#define SVO_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status codes */
+typedef enum svo_status {
+	SVO_OK = 0,
+	SVO_ERR_INVALID = 1,  /* bad argument (level out of range, null pointer, misaligned buffer) */
+	SVO_ERR_CAPACITY = 2, /* an output would exceed its buffer or the format (detected; nothing written out of bounds) */
+	SVO_ERR_OOM = 3,      /* device allocation failed */
+	SVO_ERR_TIMEOUT = 4,  /* a bounded device-side wait gave up (status word set by the kernel) */
+	SVO_ERR_CUDA = 5      /* a CUDA runtime call failed */
+} svo_status;
+
+/* ------------------------------------------------------------------ limits (src/Config.hpp:18-22) */
+#define SVO_LEVEL_MIN 1u                 /* kOctreeLevelMin */
+#define SVO_LEVEL_MAX 12u                /* kOctreeLevelMax: 12-bit fragment coordinates */
+#define SVO_MAX_POOL_WORDS (1u << 30)    /* 30-bit child pointers (0x3fffffff mask) */
+#define SVO_SUBVOXEL_BITS 8u             /* fixed-point vertex snapping: 1/256 voxel */
+#define SVO_STACK_SIZE 23u               /* STACK_SIZE of the ray march (shader/octree.glsl:43) */
+#define SVO_MARCH_MAX_ITER (1u << 20)    /* march iteration bound (malformed pools only; a valid octree needs far fewer) */
+
+/* ------------------------------------------------------------------ data types */
+
+/* One input triangle, 48 bytes, 16-byte aligned.  Vertex k is v[3k..3k+2] in the unit cube [0,1]^3
+ * (the reference's [-1,1] normalised scene maps as p = (p_ref + 1) / 2, src/Scene.cpp:90-99).
+ * rgb[k] = 0x00BBGGRR colour of vertex k; the triangle's colour is floor((c0+c1+c2)/3) per channel. */
+typedef struct svo_triangle {
+	float v[9];
+	uint32_t rgb[3];
+} svo_triangle;
+
+/* A ray in octree space: the octree occupies [1,2]^3 exactly as in shader/octree.glsl:53. */
+typedef struct svo_ray {
+	float o[3];
+	float d[3];
+} svo_ray;
+
+/* Camera uniform block (shader/camera.glsl:8): position, look, side, up as vec4 (w ignored). */
+typedef struct svo_camera {
+	float pos[4];
+	float look[4];
+	float side[4];
+	float up[4];
+} svo_camera;
+
+/* Result of one ray, 32 bytes.
+ *   t        t_min when the march stopped
+ *   pos      o_pos of Octree_RayMarchLeaf (octree space, clamped to the hit cube and nudged by EPS)
+ *   node     the leaf word that was hit (0 on a miss); colour = node & 0xffffff (R low byte)
+ *   iter     loop iterations (o_iter of the reference)
+ *   voxel    leaf coordinates at the octree level (0xffff on a miss)
+ *   flags    bit0 hit; bits1-2 normal axis (0=x,1=y,2=z); bit3 normal points to -axis */
+typedef struct svo_hit {
+	float t;
+	float pos[3];
+	uint32_t node;
+	uint32_t iter;
+	uint16_t voxel[3];
+	uint16_t flags;
+} svo_hit;
+
+#define SVO_HIT_FLAG_HIT 1u
+#define SVO_HIT_NORMAL_AXIS(f) (((f) >> 1) & 3u)
+#define SVO_HIT_NORMAL_NEG 8u
+
+/* A voxel-fragment list (device memory). data holds `count` uint64 fragments: low word = fragment.x,
+ * high word = fragment.y (the reference's uvec2 layout). */
+typedef struct svo_fraglist {
+	uint64_t *data;    /* (device) */
+	uint32_t count;    /* fragments written */
+	uint32_t level;    /* octree level the fragments were voxelized at */
+	uint64_t capacity; /* fragments the buffer can hold */
+	uint32_t owned;    /* 1 if allocated by the library (freed by svo_fraglist_destroy) */
+	uint32_t reserved;
+} svo_fraglist;
+
+/* An octree node pool (device memory). */
+typedef struct svo_octree {
+	uint32_t *words;        /* (device) node words; the used range is [0, range_words) */
+	uint64_t capacity;      /* words the buffer can hold */
+	uint32_t range_words;   /* words in use = (blocks + 1) * 8 (src/OctreeBuilder.cpp:213, in words) */
+	uint32_t level;         /* octree level (resolution 2^level) */
+	uint32_t owned;         /* 1 if allocated by the library (freed by svo_octree_destroy) */
+	uint32_t reserved;
+} svo_octree;
+
+/* Per-level and per-stage counters a build reports (read back once, at the end of the build). */
+typedef struct svo_build_info {
+	uint32_t level;
+	uint32_t fragments;
+	uint32_t range_words;
+	uint32_t leaves;                     /* non-empty leaf words */
+	uint32_t level_nodes[SVO_LEVEL_MAX]; /* non-empty node words at depth 1..level */
+} svo_build_info;
+
+/* Caller-supplied device allocator.  alloc(user, bytes) returns device memory (256-byte aligned) or
+ * NULL; release(user, ptr) gives back memory the library asked for.  Buffers handed to the caller in an
+ * output (fragment list data, octree words) are never released by the library: the caller owns them
+ * (svo_fraglist.owned / svo_octree.owned = 0).  Scratch buffers are released before the call returns,
+ * after the work that uses them has been ordered on the call's stream. */
+typedef struct svo_allocator {
+	void *(*alloc)(void *user, size_t bytes);
+	void (*release)(void *user, void *ptr);
+	void *user;
+} svo_allocator;
+
+/* ------------------------------------------------------------------ library */
+const char *svo_last_error(void);
+const char *svo_version(void);
+/* Number of kernels this library launched since load (all devices); a cheap sanity counter for callers. */
+uint64_t svo_kernel_launches(void);
+
+/* ------------------------------------------------------------------ voxelize (Voxelizer) */
+
+/* Voxelizer::Create + CmdVoxelize (src/Voxelizer.cpp:5-26, 134-179): count pass, exact allocation,
+ * emit pass.  `tris` (device) holds n_tris triangles.  On success *out owns a new device buffer with
+ * exactly out->count fragments.  Blocks the calling thread once to read the fragment count, as the
+ * reference does (src/Voxelizer.cpp:151-155). */
+int svo_voxelize(const svo_triangle *tris, uint32_t n_tris, uint32_t level, svo_fraglist *out, void *stream);
+
+/* The count pass alone (src/Voxelizer.cpp:134-158, uCountOnly = 1): writes the fragment count to
+ * *count_host (blocking). */
+int svo_voxelize_count(const svo_triangle *tris, uint32_t n_tris, uint32_t level, uint64_t *count_host,
+                       void *stream);
+
+/* Count and emit into a caller buffer (no allocation, no host synchronisation): frags (device) holds
+ * `capacity` fragments; count_dev (device, 2 x uint64) receives [0] the number of fragments the
+ * triangles produce and [1] a status word (0 = complete).  Fragments beyond `capacity` are not written
+ * (count_dev[0] > capacity tells the caller to retry with a larger buffer); status != 0 means the
+ * workspace was too small for this mesh's large triangles (use svo_voxelize, which sizes it exactly).
+ * Scratch comes from `workspace` (device, 256-byte aligned) of svo_voxelize_workspace_size(n_tris) bytes. */
+size_t svo_voxelize_workspace_size(uint32_t n_tris);
+int svo_voxelize_into(const svo_triangle *tris, uint32_t n_tris, uint32_t level, uint64_t *frags, uint64_t capacity,
+                      uint64_t *count_dev, void *workspace, void *stream);
+
+/* svo_voxelize with every device allocation made through `alloc` (NULL = the library's stream-ordered
+ * pool, exactly svo_voxelize). */
+int svo_voxelize_ex(const svo_triangle *tris, uint32_t n_tris, uint32_t level, const svo_allocator *alloc,
+                    svo_fraglist *out, void *stream);
+
+void svo_fraglist_destroy(svo_fraglist *f, void *stream);
+
+/* ------------------------------------------------------------------ build (OctreeBuilder + Octree) */
+
+/* OctreeBuilder::Create + CmdBuild + GetOctreeRange + Octree::Update (src/OctreeBuilder.cpp:8-50,142-214,
+ * src/Octree.cpp:22-35).  Builds the octree of `frags` (device, count fragments at `level`).  On success
+ * *out owns a device pool of exactly out->range_words words.  Blocks once at the end to read the range,
+ * as GetOctreeRange does.  `info` (host, may be NULL) receives the per-level counters. */
+int svo_build(const uint64_t *frags, uint32_t count, uint32_t level, svo_octree *out, svo_build_info *info,
+              void *stream);
+
+/* Convenience: svo_build on a fragment list. */
+int svo_build_fraglist(const svo_fraglist *f, svo_octree *out, svo_build_info *info, void *stream);
+
+/* Build into a caller pool (no allocation, no host synchronisation).  pool (device) holds `capacity`
+ * words; `workspace` (device) holds svo_build_workspace_size(count, level, capacity) bytes; the result
+ * header (range_words, status, per-level counts: svo_build_info layout followed by a uint32 status) is
+ * written to `result_dev` (device, at least sizeof(svo_build_info) + 4 bytes). */
+size_t svo_build_workspace_size(uint32_t count, uint32_t level, uint64_t capacity);
+uint64_t svo_build_pool_bound(uint32_t count, uint32_t level);
+int svo_build_into(const uint64_t *frags, uint32_t count, uint32_t level, uint32_t *pool, uint64_t capacity,
+                   void *workspace, void *result_dev, void *stream);
+
+/* svo_build with every device allocation made through `alloc` (NULL = svo_build). */
+int svo_build_ex(const uint64_t *frags, uint32_t count, uint32_t level, const svo_allocator *alloc, svo_octree *out,
+                 svo_build_info *info, void *stream);
+
+void svo_octree_destroy(svo_octree *o, void *stream);
+
+/* ------------------------------------------------------------------ march (OctreeTracer) */
+
+/* Octree_RayMarchLeaf (shader/octree.glsl:179-340) for n rays (device) -> n hits (device).
+ * `fetches_dev` (device, may be NULL) accumulates the number of node words the march loaded. */
+int svo_raycast(const svo_octree *o, const svo_ray *rays, uint32_t n, svo_hit *hits, uint64_t *fetches_dev,
+                void *stream);
+
+/* OctreeTracer::CmdDrawPipeline (src/OctreeTracer.cpp:213-246) with shader/octree_tracer.frag:24,37:
+ * one primary ray per pixel of a width x height image, d = Camera_GenRay(ivec2(pixel) / size)
+ * (shader/camera.glsl:11-14), origin = cam->pos.  Hit of pixel (x, y) goes to hits[y * width + x]. */
+int svo_raycast_camera(const svo_octree *o, const svo_camera *cam, uint32_t width, uint32_t height, svo_hit *hits,
+                       uint64_t *fetches_dev, void *stream);
+
+/* Secondary rays for hits: o = hit pos, d = cosine-weighted direction about the hit normal
+ * (shader/diffuse.glsl:7-14, shader/util.glsl:5-9, shader/path_tracer.comp:44-47) with (u1,u2) from a
+ * counter hash of (seed, ray index).  Misses produce a ray with d = 0 that svo_raycast reports as a miss
+ * without touching the octree. */
+int svo_bounce_rays(const svo_hit *hits, uint32_t n, uint64_t seed, svo_ray *rays, void *stream);
+
+/* Host helper: Camera::fetch_uniform_data (src/Camera.cpp:77-95) for a position, yaw, pitch, fov and
+ * aspect ratio (radians; the reference's default fov is pi/3, src/Camera.hpp:17). */
+void svo_camera_from_angles(const float pos[3], float yaw, float pitch, float fov, float aspect, svo_camera *cam);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SVO_H */

@@ -1,0 +1,165 @@
+"""CPU oracle of the sparse-voxel-octree hot path — TEST INFRASTRUCTURE ONLY.
+
+A plain-C restatement (oracle/oracle.c) of the reference's voxelize / build / march logic, loaded with
+ctypes.  Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may import this package;
+the engine (sparsevoxeloctree_gb300) never does.  Its parity with the reference's own shader source is
+pinned by tests/test_oracle_pin.py against oracle/_ref (built by oracle/build_ref.py) and by the
+fixtures in tests/golden/.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+from sparsevoxeloctree_gb300.formats import CAMERA_DTYPE, HIT_DTYPE, RAY_DTYPE, TRIANGLE_DTYPE
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+
+COLOR_DET = 0
+COLOR_REF = 1
+
+
+def build(force: bool = False) -> str:
+    """Compile liboracle.so with the committed Makefile (gcc, seconds)."""
+    if force or not os.path.exists(LIB_PATH) or _stale():
+        subprocess.run(["make", "-s", "-C", HERE, "-B" if force else "liboracle.so"], check=True)
+    return LIB_PATH
+
+
+def _stale() -> bool:
+    t = os.path.getmtime(LIB_PATH)
+    for f in ("oracle.c", "oracle.h", os.path.join("..", "include", "svo.h")):
+        if os.path.getmtime(os.path.join(HERE, f)) > t:
+            return True
+    return False
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB_PATH)
+        P = ctypes.c_void_p
+        u32, u64, i32 = ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int
+        L.oracle_set_threads.argtypes = [i32]
+        L.oracle_get_threads.restype = i32
+        L.oracle_voxelize_count.argtypes = [P, u32, u32, P]
+        L.oracle_voxelize_count.restype = u64
+        L.oracle_voxelize_emit.argtypes = [P, u32, u32, P, P]
+        L.oracle_triangle_info.argtypes = [P, u32, P]
+        L.oracle_build.argtypes = [P, u64, u32, i32, P, u64, P, ctypes.POINTER(i32)]
+        L.oracle_build.restype = u64
+        L.oracle_canonicalize.argtypes = [P, u64, P]
+        L.oracle_canonicalize.restype = i32
+        L.oracle_raycast.argtypes = [P, u64, u32, P, u64, P, P]
+        L.oracle_camera_rays.argtypes = [P, u32, u32, P]
+        L.oracle_bounce_rays.argtypes = [P, u64, u64, P]
+        L.oracle_diffuse_sample.argtypes = [P, ctypes.c_float, ctypes.c_float, P]
+        _lib = L
+    return _lib
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def set_threads(n: int) -> None:
+    lib().oracle_set_threads(int(n))
+
+
+def threads() -> int:
+    return int(lib().oracle_get_threads())
+
+
+def voxelize(tris: np.ndarray, level: int, return_counts: bool = False):
+    """Fragments of `tris` (TRIANGLE_DTYPE) in canonical order, as uint64."""
+    tris = np.ascontiguousarray(tris, TRIANGLE_DTYPE)
+    n = len(tris)
+    counts = np.zeros(max(n, 1), np.uint32)
+    total = lib().oracle_voxelize_count(_ptr(tris), n, level, _ptr(counts))
+    offsets = np.zeros(n + 1, np.uint64)
+    np.cumsum(counts[:n], out=offsets[1:])
+    frags = np.zeros(max(int(total), 1), np.uint64)
+    lib().oracle_voxelize_emit(_ptr(tris), n, level, _ptr(offsets), _ptr(frags))
+    frags = frags[: int(total)]
+    return (frags, counts[:n]) if return_counts else frags
+
+
+TRI_INFO_DTYPE = np.dtype([(k, "<i4") for k in ("axis", "i0", "i1", "j0", "j1", "z0", "z1", "cols",
+                                                 "degenerate")] + [("rgb", "<u4")])
+
+
+def triangle_info(tri: np.ndarray, level: int) -> dict:
+    tri = np.ascontiguousarray(np.asarray(tri, TRIANGLE_DTYPE).reshape(1))
+    info = np.zeros(1, TRI_INFO_DTYPE)
+    lib().oracle_triangle_info(_ptr(tri), level, _ptr(info))
+    return {k: int(info[k][0]) for k in TRI_INFO_DTYPE.names}
+
+
+def pool_bound(count: int, level: int) -> int:
+    """Upper bound on the words a build can use (every fragment adds at most one node per depth)."""
+    words = 8
+    for i in range(1, level):
+        words += 8 * min(8 ** i, count)
+    return min(words, 1 << 30)
+
+
+def build_octree(frags: np.ndarray, level: int, color_mode: int = COLOR_DET, capacity: int | None = None,
+                 return_level_nodes: bool = False):
+    """Octree node pool (uint32, exactly `range` words) of a fragment list."""
+    frags = np.ascontiguousarray(frags, np.uint64)
+    cap = pool_bound(len(frags), level) if capacity is None else int(capacity)
+    pool = np.zeros(max(cap, 8), np.uint32)
+    level_nodes = np.zeros(12, np.uint32)
+    status = ctypes.c_int(0)
+    rng = lib().oracle_build(_ptr(frags), len(frags), level, color_mode, _ptr(pool), cap, _ptr(level_nodes),
+                             ctypes.byref(status))
+    if status.value != 0:
+        raise RuntimeError(f"oracle_build failed with status {status.value}")
+    pool = pool[: int(rng)].copy()
+    return (pool, level_nodes[:level].copy()) if return_level_nodes else pool
+
+
+def canonicalize(pool: np.ndarray) -> np.ndarray:
+    pool = np.ascontiguousarray(pool, np.uint32)
+    out = np.zeros_like(pool)
+    if lib().oracle_canonicalize(_ptr(pool), len(pool), _ptr(out)) != 0:
+        raise ValueError("malformed octree pool")
+    return out
+
+
+def raycast(pool: np.ndarray, level: int, rays: np.ndarray, return_fetches: bool = False):
+    pool = np.ascontiguousarray(pool, np.uint32)
+    rays = np.ascontiguousarray(rays, RAY_DTYPE)
+    hits = np.zeros(len(rays), HIT_DTYPE)
+    fetches = np.zeros(max(len(rays), 1), np.uint32)
+    lib().oracle_raycast(_ptr(pool), len(pool), level, _ptr(rays), len(rays), _ptr(hits), _ptr(fetches))
+    return (hits, fetches[: len(rays)]) if return_fetches else hits
+
+
+def camera_rays(cam: np.ndarray, width: int, height: int) -> np.ndarray:
+    cam = np.ascontiguousarray(np.asarray(cam, CAMERA_DTYPE).reshape(1))
+    rays = np.zeros(width * height, RAY_DTYPE)
+    lib().oracle_camera_rays(_ptr(cam), width, height, _ptr(rays))
+    return rays
+
+
+def bounce_rays(hits: np.ndarray, seed: int) -> np.ndarray:
+    hits = np.ascontiguousarray(hits, HIT_DTYPE)
+    rays = np.zeros(len(hits), RAY_DTYPE)
+    lib().oracle_bounce_rays(_ptr(hits), len(hits), seed & 0xFFFFFFFFFFFFFFFF, _ptr(rays))
+    return rays
+
+
+def diffuse_sample(normal, u1: float, u2: float) -> np.ndarray:
+    n = np.ascontiguousarray(normal, np.float32)
+    out = np.zeros(3, np.float32)
+    lib().oracle_diffuse_sample(_ptr(n), u1, u2, _ptr(out))
+    return out

@@ -1,0 +1,806 @@
+/*
+ * oracle.c — CPU oracle for the sparse-voxel-octree hot path.  TEST INFRASTRUCTURE ONLY (see oracle.h).
+ *
+ * Compile with -ffp-contract=off: the march and the ray/bounce generation must round every float
+ * operation separately, exactly as the CUDA kernels do (they use explicitly rounded intrinsics).
+ *
+ * Reference files cited below are paths inside AdamYuan/SparseVoxelOctree.
+ */
+#include "oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+#include <unistd.h>
+
+/* ====================================================================== threads */
+
+static int g_threads = 0;
+
+void oracle_set_threads(int n) { g_threads = n; }
+
+int oracle_get_threads(void) {
+	if (g_threads > 0)
+		return g_threads;
+	long n = sysconf(_SC_NPROCESSORS_ONLN);
+	return n > 0 ? (int)n : 1;
+}
+
+typedef void (*range_fn)(void *ctx, uint64_t begin, uint64_t end);
+
+typedef struct {
+	range_fn fn;
+	void *ctx;
+	uint64_t n, chunk;
+	uint64_t next; /* atomic */
+} pfor_job;
+
+static void *pfor_worker(void *arg) {
+	pfor_job *job = (pfor_job *)arg;
+	for (;;) {
+		uint64_t b = __atomic_fetch_add(&job->next, job->chunk, __ATOMIC_RELAXED);
+		if (b >= job->n)
+			break;
+		uint64_t e = b + job->chunk < job->n ? b + job->chunk : job->n;
+		job->fn(job->ctx, b, e);
+	}
+	return NULL;
+}
+
+/* Dynamic-chunked parallel loop over [0, n). */
+static void parallel_for(uint64_t n, uint64_t min_chunk, range_fn fn, void *ctx) {
+	if (n == 0)
+		return;
+	int nt = oracle_get_threads();
+	uint64_t chunk = n / ((uint64_t)nt * 16u);
+	if (chunk < min_chunk)
+		chunk = min_chunk;
+	if (nt <= 1 || n <= chunk) {
+		fn(ctx, 0, n);
+		return;
+	}
+	pfor_job job = {fn, ctx, n, chunk, 0};
+	pthread_t th[256];
+	if (nt > 256)
+		nt = 256;
+	for (int i = 0; i < nt - 1; ++i)
+		pthread_create(&th[i], NULL, pfor_worker, &job);
+	pfor_worker(&job);
+	for (int i = 0; i < nt - 1; ++i)
+		pthread_join(th[i], NULL);
+}
+
+/* ====================================================================== voxelize
+ *
+ * The reference rasterises each triangle with Vulkan conservative rasterisation (src/Voxelizer.cpp:92-127)
+ * or, without the extension, dilates it by half a pixel in a geometry shader
+ * (shader/voxelizer_conservative.geom:46-58) and clips to the triangle's pixel AABB in the fragment
+ * shader (shader/voxelizer.frag:17-25).  The fixed-function raster has no source, so the rule is
+ * restated here exactly, in integers:
+ *
+ *  1. every coordinate is snapped to 1/256 voxel: X = round_to_nearest_even(clamp(p,0,1) * R * 256);
+ *  2. the dominant axis of the (integer) normal picks the projection (shader/voxelizer.geom:27-36):
+ *     x if |n.x| > |n.y| and |n.x| > |n.z|, else y if |n.y| > |n.z|, else z;
+ *     projected (a, b, depth) = (y,z,x) / (z,x,y) / (x,y,z);
+ *  3. pixel (i, j) is covered when, for each of the three edges, the edge function's maximum over
+ *     the closed pixel square is >= 0 (the half-pixel dilation of the conservative geometry shader),
+ *     and i, j lie inside [floor(min)/256, floor(max)/256] of the projected vertices (gAABB,
+ *     shader/voxelizer.geom:39-40; discard test shader/voxelizer.frag:21-22);
+ *  4. depth = floor(plane depth at the pixel centre), clamped to [0, R-1] and then to the triangle's
+ *     [floor(min depth), floor(max depth)] (shader/voxelizer.frag:18-23, gDepthRange geom:41-42);
+ *  5. voxel = un-swizzled (i, j, depth) (shader/voxelizer.frag:24); packing as shader/voxelizer.frag:40-42;
+ *     colour = per-channel floor((c0 + c1 + c2) / 3) of the vertex colours;
+ *  6. triangles whose integer normal is zero produce nothing.
+ *
+ * Canonical fragment order: triangles in input order; inside a triangle, spans along the longer AABB
+ * side (rows when the AABB is at least as wide as tall, columns otherwise), spans in increasing order,
+ * pixels inside a span in increasing order.  The oracle visits every pixel of the AABB and tests it
+ * directly; the CUDA kernel computes span intervals arithmetically.
+ */
+
+typedef struct {
+	int axis, degenerate, cols;
+	int64_t a[3], b[3], c[3]; /* projected vertices, counter-clockwise in (a, b) */
+	int64_t na, nb, nc;       /* plane normal in projected order, nc > 0 */
+	int64_t ea[3], eb[3];     /* edge k: E_k(x,y) = ea*(x - a[k]) + eb*(y - b[k]) >= 0 inside */
+	int32_t i0, i1, j0, j1, z0, z1;
+	uint32_t rgb;
+} vox_setup;
+
+static int64_t snap(float p, float scale) {
+	float q = p > 0.0f ? p : 0.0f; /* also maps NaN to 0 */
+	q = q < 1.0f ? q : 1.0f;
+	return (int64_t)nearbyintf(q * scale);
+}
+
+static int64_t floor_div(int64_t a, int64_t b) { /* b > 0 */
+	int64_t q = a / b;
+	return (a % b != 0 && a < 0) ? q - 1 : q;
+}
+
+static int32_t clampi(int64_t v, int64_t lo, int64_t hi) { return (int32_t)(v < lo ? lo : (v > hi ? hi : v)); }
+
+static uint32_t tri_color(const svo_triangle *t) {
+	uint32_t out = 0;
+	for (int ch = 0; ch < 3; ++ch) {
+		uint32_t s = 0;
+		for (int k = 0; k < 3; ++k)
+			s += (t->rgb[k] >> (8 * ch)) & 0xffu;
+		out |= (s / 3u) << (8 * ch);
+	}
+	return out;
+}
+
+static void vox_triangle_setup(const svo_triangle *t, uint32_t level, vox_setup *s) {
+	const int64_t R = (int64_t)1 << level;
+	const float scale = (float)(R * 256);
+	int64_t V[3][3];
+	for (int k = 0; k < 3; ++k)
+		for (int c = 0; c < 3; ++c)
+			V[k][c] = snap(t->v[3 * k + c], scale);
+	int64_t e1[3], e2[3], n[3];
+	for (int c = 0; c < 3; ++c) {
+		e1[c] = V[1][c] - V[0][c];
+		e2[c] = V[2][c] - V[0][c];
+	}
+	n[0] = e1[1] * e2[2] - e1[2] * e2[1];
+	n[1] = e1[2] * e2[0] - e1[0] * e2[2];
+	n[2] = e1[0] * e2[1] - e1[1] * e2[0];
+	memset(s, 0, sizeof(*s));
+	s->rgb = tri_color(t);
+	if (n[0] == 0 && n[1] == 0 && n[2] == 0) {
+		s->degenerate = 1;
+		return;
+	}
+	int64_t ax = llabs(n[0]), ay = llabs(n[1]), az = llabs(n[2]);
+	int axis = (ax > ay && ax > az) ? 0 : (ay > az ? 1 : 2);
+	s->axis = axis;
+	/* (a, b, depth) component indices for each axis: yzx, zxy, xyz (shader/voxelizer.geom:15-19) */
+	static const int perm[3][3] = {{1, 2, 0}, {2, 0, 1}, {0, 1, 2}};
+	const int *p = perm[axis];
+	int order[3] = {0, 1, 2};
+	int64_t na = n[p[0]], nb = n[p[1]], nc = n[p[2]];
+	if (nc < 0) { /* make the projected triangle counter-clockwise */
+		order[1] = 2;
+		order[2] = 1;
+		na = -na;
+		nb = -nb;
+		nc = -nc;
+	}
+	for (int k = 0; k < 3; ++k) {
+		s->a[k] = V[order[k]][p[0]];
+		s->b[k] = V[order[k]][p[1]];
+		s->c[k] = V[order[k]][p[2]];
+	}
+	s->na = na;
+	s->nb = nb;
+	s->nc = nc;
+	for (int k = 0; k < 3; ++k) {
+		int q = (k + 1) % 3;
+		s->ea[k] = -(s->b[q] - s->b[k]);
+		s->eb[k] = s->a[q] - s->a[k];
+	}
+	int64_t amin = s->a[0], amax = s->a[0], bmin = s->b[0], bmax = s->b[0], cmin = s->c[0], cmax = s->c[0];
+	for (int k = 1; k < 3; ++k) {
+		amin = s->a[k] < amin ? s->a[k] : amin;
+		amax = s->a[k] > amax ? s->a[k] : amax;
+		bmin = s->b[k] < bmin ? s->b[k] : bmin;
+		bmax = s->b[k] > bmax ? s->b[k] : bmax;
+		cmin = s->c[k] < cmin ? s->c[k] : cmin;
+		cmax = s->c[k] > cmax ? s->c[k] : cmax;
+	}
+	s->i0 = clampi(amin >> 8, 0, R - 1);
+	s->i1 = clampi(amax >> 8, 0, R - 1);
+	s->j0 = clampi(bmin >> 8, 0, R - 1);
+	s->j1 = clampi(bmax >> 8, 0, R - 1);
+	s->z0 = clampi(cmin >> 8, 0, R - 1);
+	s->z1 = clampi(cmax >> 8, 0, R - 1);
+	s->cols = (s->j1 - s->j0) > (s->i1 - s->i0);
+}
+
+static int vox_covered(const vox_setup *s, int64_t i, int64_t j) {
+	for (int k = 0; k < 3; ++k) {
+		int64_t x = 256 * i + (s->ea[k] > 0 ? 256 : 0);
+		int64_t y = 256 * j + (s->eb[k] > 0 ? 256 : 0);
+		if (s->ea[k] * (x - s->a[k]) + s->eb[k] * (y - s->b[k]) < 0)
+			return 0;
+	}
+	return 1;
+}
+
+static uint64_t vox_fragment(const vox_setup *s, int64_t i, int64_t j, uint32_t level) {
+	const int64_t R = (int64_t)1 << level;
+	int64_t x = 256 * i + 128, y = 256 * j + 128;
+	int64_t num = s->c[0] * s->nc - s->na * (x - s->a[0]) - s->nb * (y - s->b[0]);
+	int64_t z = floor_div(num, 256 * s->nc);
+	z = z < 0 ? 0 : (z > R - 1 ? R - 1 : z);
+	z = z < s->z0 ? s->z0 : (z > s->z1 ? s->z1 : z);
+	uint32_t vx, vy, vz;
+	if (s->axis == 0) { /* u.zxy */
+		vx = (uint32_t)z;
+		vy = (uint32_t)i;
+		vz = (uint32_t)j;
+	} else if (s->axis == 1) { /* u.yzx */
+		vx = (uint32_t)j;
+		vy = (uint32_t)z;
+		vz = (uint32_t)i;
+	} else {
+		vx = (uint32_t)i;
+		vy = (uint32_t)j;
+		vz = (uint32_t)z;
+	}
+	uint32_t fx = vx | (vy << 12) | ((vz & 0xffu) << 24);
+	uint32_t fy = ((vz >> 8) << 28) | (s->rgb & 0xffffffu);
+	return (uint64_t)fx | ((uint64_t)fy << 32);
+}
+
+/* Visits covered pixels in canonical order; emit may be NULL (count only). */
+static uint64_t vox_walk(const vox_setup *s, uint32_t level, uint64_t *emit) {
+	if (s->degenerate)
+		return 0;
+	uint64_t n = 0;
+	if (!s->cols) {
+		for (int64_t j = s->j0; j <= s->j1; ++j)
+			for (int64_t i = s->i0; i <= s->i1; ++i)
+				if (vox_covered(s, i, j)) {
+					if (emit)
+						emit[n] = vox_fragment(s, i, j, level);
+					++n;
+				}
+	} else {
+		for (int64_t i = s->i0; i <= s->i1; ++i)
+			for (int64_t j = s->j0; j <= s->j1; ++j)
+				if (vox_covered(s, i, j)) {
+					if (emit)
+						emit[n] = vox_fragment(s, i, j, level);
+					++n;
+				}
+	}
+	return n;
+}
+
+void oracle_triangle_info(const svo_triangle *tri, uint32_t level, oracle_tri_info *info) {
+	vox_setup s;
+	vox_triangle_setup(tri, level, &s);
+	info->axis = s.axis;
+	info->i0 = s.i0;
+	info->i1 = s.i1;
+	info->j0 = s.j0;
+	info->j1 = s.j1;
+	info->z0 = s.z0;
+	info->z1 = s.z1;
+	info->cols = s.cols;
+	info->degenerate = s.degenerate;
+	info->rgb = s.rgb;
+}
+
+typedef struct {
+	const svo_triangle *tris;
+	uint32_t level;
+	uint32_t *counts;
+	const uint64_t *offsets;
+	uint64_t *frags;
+	uint64_t total; /* atomic */
+} vox_ctx;
+
+static void vox_count_range(void *p, uint64_t b, uint64_t e) {
+	vox_ctx *c = (vox_ctx *)p;
+	uint64_t sum = 0;
+	for (uint64_t t = b; t < e; ++t) {
+		vox_setup s;
+		vox_triangle_setup(&c->tris[t], c->level, &s);
+		uint64_t n = vox_walk(&s, c->level, NULL);
+		if (c->counts)
+			c->counts[t] = (uint32_t)n;
+		sum += n;
+	}
+	__atomic_fetch_add(&c->total, sum, __ATOMIC_RELAXED);
+}
+
+static void vox_emit_range(void *p, uint64_t b, uint64_t e) {
+	vox_ctx *c = (vox_ctx *)p;
+	for (uint64_t t = b; t < e; ++t) {
+		vox_setup s;
+		vox_triangle_setup(&c->tris[t], c->level, &s);
+		vox_walk(&s, c->level, c->frags + c->offsets[t]);
+	}
+}
+
+uint64_t oracle_voxelize_count(const svo_triangle *tris, uint32_t n, uint32_t level, uint32_t *counts) {
+	vox_ctx c = {tris, level, counts, NULL, NULL, 0};
+	parallel_for(n, 64, vox_count_range, &c);
+	return c.total;
+}
+
+void oracle_voxelize_emit(const svo_triangle *tris, uint32_t n, uint32_t level, const uint64_t *offsets,
+                          uint64_t *frags) {
+	vox_ctx c = {tris, level, NULL, offsets, frags, 0};
+	parallel_for(n, 64, vox_emit_range, &c);
+}
+
+/* ====================================================================== build
+ *
+ * The level loop of src/OctreeBuilder.cpp:142-210 with build info {begin = 0, num = 8}
+ * (src/OctreeBuilder.cpp:25-30):
+ *   init   zero words [begin, begin+num)                         shader/octree_init_node.comp:7-11
+ *   tag    every fragment walks from the root (TraverseOctree)   shader/octree_tag_node.comp:18-31
+ *          and marks 0x80000000, or merges its colour at a leaf   shader/octree_tag_node.comp:33-60
+ *   alloc  every marked word in [begin, begin+num) gets a block  shader/octree_alloc_node.comp:9-23
+ *   modify begin += num; num = counter*8 - begin + 8             shader/octree_modify_arg.comp:9-13
+ * Blocks are handed out in word order (one invocation at a time), which is the breadth-first canonical
+ * order the engine's prefix-sum allocation produces.
+ */
+
+typedef struct {
+	const uint64_t *frags;
+	uint32_t level;
+	uint32_t *pool;
+	uint64_t leaf_begin;
+	uint64_t *sums; /* det mode: per leaf word r, g, b, n */
+} tag_ctx;
+
+/* TraverseOctree: descend until the node pointer is 0 or the unit level is reached. */
+static uint64_t traverse(const uint32_t *pool, uint32_t level, uint64_t frag, int *is_leaf) {
+	uint32_t fx = (uint32_t)frag, fy = (uint32_t)(frag >> 32);
+	uint32_t pos[3] = {fx & 0xfffu, (fx >> 12) & 0xfffu, (fx >> 24) | ((fy >> 28) << 8)};
+	uint32_t dim = 1u << level;
+	uint32_t idx = 0, cur = 0;
+	do {
+		dim >>= 1;
+		uint32_t cx = pos[0] >= dim, cy = pos[1] >= dim, cz = pos[2] >= dim;
+		idx = cur | cx | (cy << 1) | (cz << 2);
+		cur = __atomic_load_n(&pool[idx], __ATOMIC_RELAXED) & 0x3fffffffu;
+		pos[0] -= cx * dim;
+		pos[1] -= cy * dim;
+		pos[2] -= cz * dim;
+	} while (cur != 0 && dim > 1);
+	*is_leaf = dim == 1;
+	return idx;
+}
+
+static void tag_range(void *p, uint64_t b, uint64_t e) {
+	tag_ctx *c = (tag_ctx *)p;
+	for (uint64_t f = b; f < e; ++f) {
+		int leaf;
+		uint64_t idx = traverse(c->pool, c->level, c->frags[f], &leaf);
+		if (leaf) {
+			uint32_t rgb = (uint32_t)(c->frags[f] >> 32) & 0xffffffu;
+			uint64_t *s = c->sums + 4 * (idx - c->leaf_begin);
+			__atomic_fetch_add(&s[0], rgb & 0xffu, __ATOMIC_RELAXED);
+			__atomic_fetch_add(&s[1], (rgb >> 8) & 0xffu, __ATOMIC_RELAXED);
+			__atomic_fetch_add(&s[2], (rgb >> 16) & 0xffu, __ATOMIC_RELAXED);
+			__atomic_fetch_add(&s[3], 1, __ATOMIC_RELAXED);
+		} else {
+			__atomic_store_n(&c->pool[idx], 0x80000000u, __ATOMIC_RELAXED);
+		}
+	}
+}
+
+/* The reference's leaf merge (shader/octree_tag_node.comp:47-57) applied sequentially: the CAS loop
+ * succeeds on its first retry, so each fragment folds into the running mean in list order. */
+static void tag_leaf_ref(uint32_t *word, uint32_t rgb) {
+	uint32_t prev = *word;
+	uint32_t nr = rgb & 0xffu, ng = (rgb >> 8) & 0xffu, nb = (rgb >> 16) & 0xffu;
+	if (prev == 0) {
+		*word = 0xC1000000u | (rgb & 0xffffffu);
+		return;
+	}
+	uint32_t pr = prev & 0xffu, pg = (prev >> 8) & 0xffu, pb = (prev >> 16) & 0xffu, pc = (prev >> 24) & 0x3fu;
+	uint32_t cnt = pc + 1u;
+	uint32_t r = (pr * pc + nr) / cnt, g = (pg * pc + ng) / cnt, bl = (pb * pc + nb) / cnt;
+	uint32_t w = cnt < 0x3fu ? cnt : 0x3fu;
+	*word = (w << 24) | (r & 0xffu) | ((g & 0xffu) << 8) | ((bl & 0xffu) << 16) | 0xC0000000u;
+}
+
+typedef struct {
+	uint32_t *pool;
+	uint64_t begin;
+	const uint64_t *sums;
+} fin_ctx;
+
+static void finalize_range(void *p, uint64_t b, uint64_t e) {
+	fin_ctx *c = (fin_ctx *)p;
+	for (uint64_t w = b; w < e; ++w) {
+		const uint64_t *s = c->sums + 4 * w;
+		if (s[3] == 0)
+			continue;
+		uint64_t n = s[3];
+		uint32_t r = (uint32_t)(s[0] / n), g = (uint32_t)(s[1] / n), bl = (uint32_t)(s[2] / n);
+		uint32_t cnt = n < 63 ? (uint32_t)n : 63u;
+		c->pool[c->begin + w] = 0xC0000000u | (cnt << 24) | (bl << 16) | (g << 8) | r;
+	}
+}
+
+uint64_t oracle_build(const uint64_t *frags, uint64_t count, uint32_t level, int color_mode, uint32_t *pool,
+                      uint64_t capacity, uint32_t *level_nodes, int *status) {
+	*status = SVO_OK;
+	if (level < SVO_LEVEL_MIN || level > SVO_LEVEL_MAX) {
+		*status = SVO_ERR_INVALID;
+		return 0;
+	}
+	uint64_t begin = 0, num = 8, counter = 0;
+	for (uint32_t i = 1; i <= level; ++i) {
+		if (begin + num > capacity) {
+			*status = SVO_ERR_CAPACITY;
+			return 0;
+		}
+		memset(pool + begin, 0, num * sizeof(uint32_t)); /* init */
+		if (i < level) {
+			tag_ctx c = {frags, level, pool, 0, NULL};
+			parallel_for(count, 4096, tag_range, &c);
+		} else if (color_mode == ORACLE_COLOR_REF) {
+			for (uint64_t f = 0; f < count; ++f) {
+				int leaf;
+				uint64_t idx = traverse(pool, level, frags[f], &leaf);
+				tag_leaf_ref(&pool[idx], (uint32_t)(frags[f] >> 32) & 0xffffffu);
+			}
+		} else {
+			uint64_t *sums = (uint64_t *)calloc(num * 4 + 4, sizeof(uint64_t));
+			tag_ctx c = {frags, level, pool, begin, sums};
+			parallel_for(count, 4096, tag_range, &c);
+			fin_ctx fc = {pool, begin, sums};
+			parallel_for(num, 4096, finalize_range, &fc);
+			free(sums);
+		}
+		uint64_t nodes = 0;
+		for (uint64_t w = begin; w < begin + num; ++w)
+			nodes += (pool[w] & 0x80000000u) != 0;
+		if (level_nodes)
+			level_nodes[i - 1] = (uint32_t)nodes;
+		if (i < level) { /* alloc + modify_arg */
+			for (uint64_t w = begin; w < begin + num; ++w)
+				if (pool[w] & 0x80000000u) {
+					pool[w] = (uint32_t)(((counter + 1) << 3) | 0x80000000u);
+					++counter;
+				}
+			begin += num;
+			num = counter * 8 - begin + 8;
+			if ((counter + 1) * 8 > SVO_MAX_POOL_WORDS) {
+				*status = SVO_ERR_CAPACITY;
+				return 0;
+			}
+		}
+	}
+	return (counter + 1) * 8;
+}
+
+int oracle_canonicalize(const uint32_t *pool, uint64_t range, uint32_t *out) {
+	if (range < 8 || range % 8)
+		return -1;
+	uint64_t nblocks = range / 8;
+	uint64_t *queue = (uint64_t *)malloc(nblocks * sizeof(uint64_t));
+	uint8_t *seen = (uint8_t *)calloc(nblocks, 1);
+	uint64_t head = 0, tail = 0;
+	queue[tail++] = 0;
+	seen[0] = 1;
+	int rc = 0;
+	while (head < tail) {
+		uint64_t blk = queue[head], nb = head;
+		++head;
+		for (int k = 0; k < 8; ++k) {
+			uint32_t w = pool[blk * 8 + k];
+			if ((w & 0xC0000000u) == 0x80000000u) {
+				uint64_t child = (w & 0x3fffffffu);
+				if (child % 8 || child / 8 >= nblocks || seen[child / 8]) {
+					rc = -1;
+					goto done;
+				}
+				seen[child / 8] = 1;
+				out[nb * 8 + k] = (uint32_t)(0x80000000u | (tail * 8));
+				queue[tail++] = child / 8;
+			} else {
+				out[nb * 8 + k] = w;
+			}
+		}
+	}
+	if (tail != nblocks)
+		rc = -1;
+done:
+	free(queue);
+	free(seen);
+	return rc;
+}
+
+/* ====================================================================== march
+ *
+ * Octree_RayMarchLeaf with the iteration counter (shader/octree.glsl:179-340), the variant the
+ * tracer calls (shader/octree_tracer.frag:37).  The octree occupies [1,2]^3; coordinates are mirrored
+ * so the ray direction is negative on every axis; cube positions are exact dyadic floats whose bits
+ * drive the pop (highest differing bit).  Every float operation is rounded separately.
+ */
+
+#define MARCH_EPS 3.552713678800501e-15f
+
+static inline float fmax_glsl(float x, float y) { return x < y ? y : x; }
+static inline float fmin_glsl(float x, float y) { return y < x ? y : x; }
+static inline uint32_t f2u(float f) {
+	uint32_t u;
+	memcpy(&u, &f, 4);
+	return u;
+}
+static inline float u2f(uint32_t u) {
+	float f;
+	memcpy(&f, &u, 4);
+	return f;
+}
+static inline float eps_clamp(float v) { return fabsf(v) > MARCH_EPS ? v : (v >= 0.0f ? MARCH_EPS : -MARCH_EPS); }
+
+static void march_one(const uint32_t *pool, uint64_t range, uint32_t level, const svo_ray *ray, svo_hit *hit,
+                      uint32_t *fetches) {
+	const float o[3] = {ray->o[0], ray->o[1], ray->o[2]};
+	float d[3] = {ray->d[0], ray->d[1], ray->d[2]};
+	uint32_t nfetch = 0;
+	if (d[0] == 0.0f && d[1] == 0.0f && d[2] == 0.0f) { /* ABI convention: no ray */
+		memset(hit, 0, sizeof(*hit));
+		hit->pos[0] = o[0];
+		hit->pos[1] = o[1];
+		hit->pos[2] = o[2];
+		hit->voxel[0] = hit->voxel[1] = hit->voxel[2] = 0xffffu;
+		if (fetches)
+			*fetches = 0;
+		return;
+	}
+	uint32_t stack[SVO_STACK_SIZE] = {0};
+	uint32_t iter = 0;
+	for (int k = 0; k < 3; ++k)
+		d[k] = eps_clamp(d[k]);
+
+	float coef[3], bias[3];
+	for (int k = 0; k < 3; ++k) {
+		coef[k] = 1.0f / -fabsf(d[k]);
+		bias[k] = coef[k] * o[k];
+	}
+	uint32_t oct_mask = 0;
+	for (int k = 0; k < 3; ++k)
+		if (d[k] > 0.0f) {
+			oct_mask ^= 1u << k;
+			bias[k] = 3.0f * coef[k] - bias[k];
+		}
+	float t_min = fmax_glsl(fmax_glsl(2.0f * coef[0] - bias[0], 2.0f * coef[1] - bias[1]), 2.0f * coef[2] - bias[2]);
+	float t_max = fmin_glsl(fmin_glsl(coef[0] - bias[0], coef[1] - bias[1]), coef[2] - bias[2]);
+	t_min = fmax_glsl(t_min, 0.0f);
+	float h = t_max;
+
+	uint32_t parent = 0, cur = 0, idx = 0;
+	float pos[3] = {1.0f, 1.0f, 1.0f};
+	for (int k = 0; k < 3; ++k)
+		if (1.5f * coef[k] - bias[k] > t_min) {
+			idx ^= 1u << k;
+			pos[k] = 1.5f;
+		}
+	uint32_t scale = SVO_STACK_SIZE - 1;
+	float scale_exp2 = 0.5f;
+
+	while (scale < SVO_STACK_SIZE) {
+		if (iter >= SVO_MARCH_MAX_ITER) /* bound for malformed pools; never reached on a valid octree */
+			break;
+		++iter;
+		if (cur == 0u) {
+			uint64_t w = (uint64_t)parent + (idx ^ oct_mask);
+			if (w >= range) { /* pointer outside the pool: stop as a miss */
+				scale = 0xffffffffu;
+				break;
+			}
+			cur = pool[w];
+			++nfetch;
+		}
+		float tc[3];
+		for (int k = 0; k < 3; ++k)
+			tc[k] = pos[k] * coef[k] - bias[k];
+		float tc_max = fmin_glsl(fmin_glsl(tc[0], tc[1]), tc[2]);
+
+		if ((cur & 0x80000000u) != 0 && t_min <= t_max) {
+			float half = scale_exp2 * 0.5f;
+			float t_center[3];
+			for (int k = 0; k < 3; ++k)
+				t_center[k] = half * coef[k] + tc[k];
+			if ((cur & 0x40000000u) != 0)
+				break; /* leaf */
+			if (tc_max < h) /* push */
+				stack[scale] = parent;
+			h = tc_max;
+			parent = cur & 0x3fffffffu;
+			idx = 0;
+			--scale;
+			scale_exp2 = half;
+			for (int k = 0; k < 3; ++k)
+				if (t_center[k] > t_min) {
+					idx ^= 1u << k;
+					pos[k] += scale_exp2;
+				}
+			cur = 0;
+			continue;
+		}
+		/* advance */
+		uint32_t step_mask = 0;
+		for (int k = 0; k < 3; ++k)
+			if (tc[k] <= tc_max) {
+				step_mask ^= 1u << k;
+				pos[k] -= scale_exp2;
+			}
+		t_min = tc_max;
+		idx ^= step_mask;
+		if ((idx & step_mask) != 0) { /* pop */
+			uint32_t diff = 0;
+			for (int k = 0; k < 3; ++k)
+				if (step_mask & (1u << k))
+					diff |= f2u(pos[k]) ^ f2u(pos[k] + scale_exp2);
+			scale = diff ? 31u - (uint32_t)__builtin_clz(diff) : 0xffffffffu; /* findMSB */
+			if (scale >= SVO_STACK_SIZE)
+				break;
+			scale_exp2 = u2f((scale - SVO_STACK_SIZE + 127u) << 23u);
+			parent = stack[scale];
+			uint32_t sh[3];
+			for (int k = 0; k < 3; ++k) {
+				sh[k] = f2u(pos[k]) >> scale;
+				pos[k] = u2f(sh[k] << scale);
+			}
+			idx = (sh[0] & 1u) | ((sh[1] & 1u) << 1) | ((sh[2] & 1u) << 2);
+			h = 0.0f;
+			cur = 0;
+		}
+	}
+
+	/* normal from the exit corner (shader/octree.glsl:307-317) */
+	float tc[3];
+	for (int k = 0; k < 3; ++k)
+		tc[k] = coef[k] * (pos[k] + scale_exp2) - bias[k];
+	int nax = (tc[0] > tc[1] && tc[0] > tc[2]) ? 0 : (tc[1] > tc[2] ? 1 : 2);
+	float norm[3] = {0.0f, 0.0f, 0.0f};
+	norm[nax] = -1.0f;
+	if ((oct_mask & (1u << nax)) == 0u)
+		norm[nax] = 1.0f;
+	/* undo mirroring (shader/octree.glsl:319-325) */
+	for (int k = 0; k < 3; ++k)
+		if (oct_mask & (1u << k))
+			pos[k] = 3.0f - scale_exp2 - pos[k];
+	/* o_pos (shader/octree.glsl:327-334) */
+	for (int k = 0; k < 3; ++k) {
+		float v = o[k] + t_min * d[k];
+		float lo = pos[k], hi = pos[k] + scale_exp2;
+		v = fmin_glsl(fmax_glsl(v, lo), hi);
+		if (k == nax)
+			v = norm[k] > 0.0f ? pos[k] + scale_exp2 + MARCH_EPS * 2.0f : pos[k] - MARCH_EPS;
+		hit->pos[k] = v;
+	}
+	int is_hit = scale < SVO_STACK_SIZE && t_min <= t_max;
+	hit->t = t_min;
+	hit->iter = iter;
+	hit->flags = (uint16_t)((is_hit ? SVO_HIT_FLAG_HIT : 0u) | ((uint32_t)nax << 1) |
+	                        (norm[nax] < 0.0f ? SVO_HIT_NORMAL_NEG : 0u));
+	if (is_hit) {
+		hit->node = cur;
+		float res = (float)(1u << level);
+		for (int k = 0; k < 3; ++k)
+			hit->voxel[k] = (uint16_t)(uint32_t)((pos[k] - 1.0f) * res);
+	} else {
+		hit->node = 0;
+		hit->voxel[0] = hit->voxel[1] = hit->voxel[2] = 0xffffu;
+	}
+	if (fetches)
+		*fetches = nfetch;
+}
+
+typedef struct {
+	const uint32_t *pool;
+	uint64_t range;
+	uint32_t level;
+	const svo_ray *rays;
+	svo_hit *hits;
+	uint32_t *fetches;
+} march_ctx;
+
+static void march_range(void *p, uint64_t b, uint64_t e) {
+	march_ctx *c = (march_ctx *)p;
+	for (uint64_t r = b; r < e; ++r)
+		march_one(c->pool, c->range, c->level, &c->rays[r], &c->hits[r], c->fetches ? &c->fetches[r] : NULL);
+}
+
+void oracle_raycast(const uint32_t *pool, uint64_t range, uint32_t level, const svo_ray *rays, uint64_t n,
+                    svo_hit *hits, uint32_t *fetches) {
+	march_ctx c = {pool, range, level, rays, hits, fetches};
+	parallel_for(n, 256, march_range, &c);
+}
+
+/* ====================================================================== rays */
+
+/* Camera_GenRay(coord) = normalize(look - side*(2c.x-1) - up*(2c.y-1)) (shader/camera.glsl:11-14);
+ * normalize is v / sqrt(x*x + y*y + z*z), each operation rounded. */
+void oracle_camera_rays(const svo_camera *cam, uint32_t width, uint32_t height, svo_ray *rays) {
+	for (uint32_t y = 0; y < height; ++y)
+		for (uint32_t x = 0; x < width; ++x) {
+			float cx = (float)x / (float)width, cy = (float)y / (float)height;
+			cx = cx * 2.0f - 1.0f;
+			cy = cy * 2.0f - 1.0f;
+			float v[3];
+			for (int k = 0; k < 3; ++k)
+				v[k] = (cam->look[k] - cam->side[k] * cx) - cam->up[k] * cy;
+			float len = sqrtf((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]);
+			svo_ray *r = &rays[(uint64_t)y * width + x];
+			for (int k = 0; k < 3; ++k) {
+				r->o[k] = cam->pos[k];
+				r->d[k] = v[k] / len;
+			}
+		}
+}
+
+/* Counter hash for the bounce sample: splitmix64 finaliser of seed + golden * (index + 1). */
+static uint64_t mix64(uint64_t z) {
+	z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+	z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+	return z ^ (z >> 31);
+}
+
+/* sin and cos of 2*pi*u for u in [0,1): quadrant split, then Taylor polynomials of degree 13/12 on
+ * [0, pi/2) in Horner form; every operation rounded separately so CPU and GPU agree bit for bit. */
+static void sincos_2pi(float u, float *s_out, float *c_out) {
+	float q4 = u * 4.0f;
+	int q = (int)q4;
+	float r = q4 - (float)q;
+	float a = r * 1.57079632679489662f;
+	float a2 = a * a;
+	float s = 1.0f / 6227020800.0f;
+	s = s * a2 + -1.0f / 39916800.0f;
+	s = s * a2 + 1.0f / 362880.0f;
+	s = s * a2 + -1.0f / 5040.0f;
+	s = s * a2 + 1.0f / 120.0f;
+	s = s * a2 + -1.0f / 6.0f;
+	s = s * a2 + 1.0f;
+	s = s * a;
+	float c = 1.0f / 479001600.0f;
+	c = c * a2 + -1.0f / 3628800.0f;
+	c = c * a2 + 1.0f / 40320.0f;
+	c = c * a2 + -1.0f / 720.0f;
+	c = c * a2 + 1.0f / 24.0f;
+	c = c * a2 + -0.5f;
+	c = c * a2 + 1.0f;
+	switch (q & 3) {
+	case 0: *s_out = s; *c_out = c; break;
+	case 1: *s_out = c; *c_out = -s; break;
+	case 2: *s_out = -s; *c_out = -c; break;
+	default: *s_out = -c; *c_out = s; break;
+	}
+}
+
+/* Diffuse_Sample (shader/diffuse.glsl:7-14) with AlignDirection (shader/util.glsl:5-9) for an
+ * axis-aligned normal; sin/cos from sincos_2pi. */
+void oracle_diffuse_sample(const float nrm_in[3], float u1, float u2, float out[3]) {
+	float rr = sqrtf(u1), sn, cs;
+	sincos_2pi(u2, &sn, &cs);
+	float dl[3] = {rr * cs, rr * sn, sqrtf(1.0f - u1)};
+	float nrm[3] = {nrm_in[0], nrm_in[1], nrm_in[2]};
+	float ref[3] = {0.0f, 0.0f, 0.0f};
+	if (fabsf(nrm[0]) > 0.01f)
+		ref[1] = 1.0f;
+	else
+		ref[0] = 1.0f;
+	float u[3] = {ref[1] * nrm[2] - ref[2] * nrm[1], ref[2] * nrm[0] - ref[0] * nrm[2],
+	              ref[0] * nrm[1] - ref[1] * nrm[0]};
+	float ul = sqrtf((u[0] * u[0] + u[1] * u[1]) + u[2] * u[2]);
+	for (int k = 0; k < 3; ++k)
+		u[k] = u[k] / ul;
+	float v[3] = {nrm[1] * u[2] - nrm[2] * u[1], nrm[2] * u[0] - nrm[0] * u[2], nrm[0] * u[1] - nrm[1] * u[0]};
+	for (int k = 0; k < 3; ++k)
+		out[k] = (dl[0] * u[k] + dl[1] * v[k]) + dl[2] * nrm[k];
+}
+
+void oracle_bounce_rays(const svo_hit *hits, uint64_t n, uint64_t seed, svo_ray *rays) {
+	for (uint64_t i = 0; i < n; ++i) {
+		const svo_hit *h = &hits[i];
+		svo_ray *r = &rays[i];
+		for (int k = 0; k < 3; ++k) {
+			r->o[k] = h->pos[k];
+			r->d[k] = 0.0f;
+		}
+		if (!(h->flags & SVO_HIT_FLAG_HIT))
+			continue;
+		uint64_t z = mix64(seed + 0x9E3779B97F4A7C15ull * (i + 1));
+		float u1 = (float)(uint32_t)(z >> 40) * (1.0f / 16777216.0f);
+		float u2 = (float)(uint32_t)((z >> 16) & 0xffffffu) * (1.0f / 16777216.0f);
+		int ax = SVO_HIT_NORMAL_AXIS(h->flags);
+		float nrm[3] = {0.0f, 0.0f, 0.0f};
+		nrm[ax] = (h->flags & SVO_HIT_NORMAL_NEG) ? -1.0f : 1.0f;
+		oracle_diffuse_sample(nrm, u1, u2, r->d);
+	}
+}

@@ -1,0 +1,73 @@
+/*
+ * oracle.h — CPU oracle for the sparse-voxel-octree hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference's algorithm
+ * (AdamYuan/SparseVoxelOctree) used to check the CUDA engine and to time the CPU baseline.
+ * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load it; the engine
+ * never calls it.
+ *
+ * Parity pinning: oracle/build_ref.py compiles the reference's own GLSL compute and march source
+ * through a C++ shim into oracle/_ref/ and tests/test_oracle_pin.py checks this oracle against it;
+ * tests/golden/ holds fixtures generated that way.
+ */
+#ifndef SVO_ORACLE_H
+#define SVO_ORACLE_H
+
+#include "../include/svo.h"
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Worker threads (0 = all hardware threads). */
+void oracle_set_threads(int n);
+int oracle_get_threads(void);
+
+/* ---- voxelize: conservative raster restated in fixed point (see oracle.c) ---- */
+/* Fragment count of every triangle (counts[t]); returns the total. */
+uint64_t oracle_voxelize_count(const svo_triangle *tris, uint32_t n, uint32_t level, uint32_t *counts);
+/* Writes fragments in canonical order (triangle, span, position).  `offsets` = exclusive prefix of counts
+ * (n+1 entries). */
+void oracle_voxelize_emit(const svo_triangle *tris, uint32_t n, uint32_t level, const uint64_t *offsets,
+                          uint64_t *frags);
+
+/* Per-triangle setup exposed for tests: axis, pixel AABB, depth range, span orientation. */
+typedef struct oracle_tri_info {
+	int32_t axis, i0, i1, j0, j1, z0, z1, cols, degenerate;
+	uint32_t rgb;
+} oracle_tri_info;
+void oracle_triangle_info(const svo_triangle *tri, uint32_t level, oracle_tri_info *info);
+
+/* ---- build ---- */
+#define ORACLE_COLOR_DET 0 /* channel-wise integer mean (the engine's rule) */
+#define ORACLE_COLOR_REF 1 /* the reference's CAS running mean, fragments applied in list order */
+/* Builds the octree with the reference's level loop (shader/octree_{init,tag,alloc}_node.comp,
+ * octree_modify_arg.comp driven as in src/OctreeBuilder.cpp:142-210), child blocks allocated in word
+ * order.  Writes at most `capacity` words to pool; returns the range in words, or 0 with *status set
+ * to SVO_ERR_CAPACITY if the pool is too small.  level_nodes (may be NULL) gets non-empty node counts
+ * per depth 1..level. */
+uint64_t oracle_build(const uint64_t *frags, uint64_t count, uint32_t level, int color_mode, uint32_t *pool,
+                      uint64_t capacity, uint32_t *level_nodes, int *status);
+
+/* Breadth-first renumbering of child blocks (children visited in word order); writes the canonical
+ * pool to `out` (range words).  Returns 0 on success, -1 on a malformed pool. */
+int oracle_canonicalize(const uint32_t *pool, uint64_t range, uint32_t *out);
+
+/* ---- march ---- */
+/* Octree_RayMarchLeaf (shader/octree.glsl:179-340) per ray.  fetches (may be NULL) gets per-ray node
+ * loads. */
+void oracle_raycast(const uint32_t *pool, uint64_t range, uint32_t level, const svo_ray *rays, uint64_t n,
+                    svo_hit *hits, uint32_t *fetches);
+/* Camera_GenRay (shader/camera.glsl:11-14) at ivec2(pixel)/size (shader/octree_tracer.frag:24). */
+void oracle_camera_rays(const svo_camera *cam, uint32_t width, uint32_t height, svo_ray *rays);
+/* Diffuse_Sample for one normal and sample pair (shader/diffuse.glsl:7-14, shader/util.glsl:5-9). */
+void oracle_diffuse_sample(const float nrm[3], float u1, float u2, float out[3]);
+/* Cosine bounce rays for hits (shader/diffuse.glsl:7-14 + shader/util.glsl:5-9). */
+void oracle_bounce_rays(const svo_hit *hits, uint64_t n, uint64_t seed, svo_ray *rays);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,115 @@
+"""ctypes binding of oracle/_ref/libsvo_ref.so — the reference's own shader code compiled for the CPU.
+
+TEST INFRASTRUCTURE ONLY.  The library is built by oracle/build_ref.py from the reference checkout and
+exists only where that checkout does; `available()` says whether it can be loaded.  It is used to pin
+the oracle (tests/test_oracle_pin.py) and to generate the fixtures in tests/golden/.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_ref", "libsvo_ref.so")
+REFERENCE_DIR = os.environ.get("SVO_REFERENCE", "/root/reference")
+
+_lib = None
+
+
+def build() -> bool:
+    """Build the library when the reference checkout is present; True if it is available afterwards."""
+    if os.path.isdir(os.path.join(REFERENCE_DIR, "shader")):
+        subprocess.run([sys.executable, os.path.join(HERE, "build_ref.py"), "--reference", REFERENCE_DIR],
+                       check=True, stdout=subprocess.DEVNULL)
+    return os.path.exists(LIB_PATH)
+
+
+def available() -> bool:
+    try:
+        lib()
+        return True
+    except OSError:
+        return False
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        P, u32, u64, i32, f32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int, ctypes.c_float
+        L.ref_build.argtypes = [P, u32, u32, P, u64]
+        L.ref_build.restype = u64
+        L.ref_raycast.argtypes = [P, u32, P, P, i32, P, P, P, P, P]
+        L.ref_occlude.argtypes = [P, u32, P, P, P]
+        L.ref_camera_rays.argtypes = [P, u32, u32, P]
+        L.ref_diffuse_sample.argtypes = [P, f32, f32, P]
+        L.ref_voxelize_triangle.argtypes = [P, u32, u32, i32, P, u64]
+        L.ref_voxelize_triangle.restype = u64
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def build_octree(frags: np.ndarray, level: int, capacity: int) -> np.ndarray:
+    frags = np.ascontiguousarray(frags, np.uint64)
+    pool = np.zeros(capacity, np.uint32)
+    rng = lib().ref_build(_p(frags), len(frags), level, _p(pool), capacity)
+    if rng == 0:
+        raise RuntimeError("reference build overflowed the pool")
+    return pool[:rng].copy()
+
+
+def raycast(pool: np.ndarray, o: np.ndarray, d: np.ndarray, with_iter: bool = True) -> dict:
+    pool = np.ascontiguousarray(pool, np.uint32)
+    o = np.ascontiguousarray(o, np.float32)
+    d = np.ascontiguousarray(d, np.float32)
+    n = len(o)
+    out = dict(hit=np.zeros(n, np.uint32), pos=np.zeros((n, 3), np.float32), color=np.zeros((n, 3), np.float32),
+               normal=np.zeros((n, 3), np.float32), iter=np.zeros(n, np.uint32))
+    lib().ref_raycast(_p(pool), n, _p(o), _p(d), int(with_iter), _p(out["hit"]), _p(out["pos"]), _p(out["color"]),
+                      _p(out["normal"]), _p(out["iter"]))
+    return out
+
+
+def occlude(pool: np.ndarray, o: np.ndarray, d: np.ndarray) -> np.ndarray:
+    pool = np.ascontiguousarray(pool, np.uint32)
+    o = np.ascontiguousarray(o, np.float32)
+    d = np.ascontiguousarray(d, np.float32)
+    hit = np.zeros(len(o), np.uint32)
+    lib().ref_occlude(_p(pool), len(o), _p(o), _p(d), _p(hit))
+    return hit
+
+
+def camera_dirs(cam, width: int, height: int) -> np.ndarray:
+    c = np.ascontiguousarray(np.concatenate([cam["pos"], cam["look"], cam["side"], cam["up"]]).astype(np.float32))
+    dirs = np.zeros((width * height, 3), np.float32)
+    lib().ref_camera_rays(_p(c), width, height, _p(dirs))
+    return dirs
+
+
+def diffuse_sample(normal, u1: float, u2: float) -> np.ndarray:
+    n = np.ascontiguousarray(normal, np.float32)
+    out = np.zeros(3, np.float32)
+    lib().ref_diffuse_sample(_p(n), u1, u2, _p(out))
+    return out
+
+
+def voxelize_triangle(v9_ref: np.ndarray, albedo: int, level: int, conservative_sw: bool) -> np.ndarray:
+    """Fragments of one triangle given in the reference's [-1,1] space."""
+    v = np.ascontiguousarray(v9_ref, np.float32)
+    cap = 1 << 16
+    while True:
+        out = np.zeros(cap, np.uint64)
+        n = lib().ref_voxelize_triangle(_p(v), albedo, level, int(conservative_sw), _p(out), cap)
+        if n <= cap:
+            return out[:n]
+        cap = int(n)

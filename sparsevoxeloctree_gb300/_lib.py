@@ -1,0 +1,113 @@
+"""ctypes binding of libsvo.so (the C ABI in include/svo.h).
+
+The library is the only compute path: if it cannot be loaded, every entry point raises.  There is no
+CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+from . import build as _build
+
+LIB_PATH = _build.LIB
+HEADER = os.path.join(_build.ROOT, "include", "svo.h")
+
+SVO_OK, SVO_ERR_INVALID, SVO_ERR_CAPACITY, SVO_ERR_OOM, SVO_ERR_TIMEOUT, SVO_ERR_CUDA = range(6)
+STATUS_NAMES = {0: "SVO_OK", 1: "SVO_ERR_INVALID", 2: "SVO_ERR_CAPACITY", 3: "SVO_ERR_OOM", 4: "SVO_ERR_TIMEOUT",
+                5: "SVO_ERR_CUDA"}
+
+u32, u64, i32, f32, sz = ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int, ctypes.c_float, ctypes.c_size_t
+P = ctypes.c_void_p
+
+
+class SvoError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(code, code)}: {message}")
+        self.code = code
+
+
+class Fraglist(ctypes.Structure):
+    _fields_ = [("data", P), ("count", u32), ("level", u32), ("capacity", u64), ("owned", u32), ("reserved", u32)]
+
+
+class OctreeC(ctypes.Structure):
+    _fields_ = [("words", P), ("capacity", u64), ("range_words", u32), ("level", u32), ("owned", u32),
+                ("reserved", u32)]
+
+
+class BuildInfo(ctypes.Structure):
+    _fields_ = [("level", u32), ("fragments", u32), ("range_words", u32), ("leaves", u32),
+                ("level_nodes", u32 * 12)]
+
+
+class CameraC(ctypes.Structure):
+    _fields_ = [("pos", f32 * 4), ("look", f32 * 4), ("side", f32 * 4), ("up", f32 * 4)]
+
+
+ALLOC_FN = ctypes.CFUNCTYPE(P, P, sz)
+RELEASE_FN = ctypes.CFUNCTYPE(None, P, P)
+
+
+class Allocator(ctypes.Structure):
+    _fields_ = [("alloc", ALLOC_FN), ("release", RELEASE_FN), ("user", P)]
+
+
+_SIGNATURES = {
+    "svo_last_error": ([], ctypes.c_char_p),
+    "svo_version": ([], ctypes.c_char_p),
+    "svo_kernel_launches": ([], u64),
+    "svo_voxelize": ([P, u32, u32, ctypes.POINTER(Fraglist), P], i32),
+    "svo_voxelize_ex": ([P, u32, u32, ctypes.POINTER(Allocator), ctypes.POINTER(Fraglist), P], i32),
+    "svo_voxelize_count": ([P, u32, u32, ctypes.POINTER(u64), P], i32),
+    "svo_voxelize_workspace_size": ([u32], sz),
+    "svo_voxelize_into": ([P, u32, u32, P, u64, P, P, P], i32),
+    "svo_fraglist_destroy": ([ctypes.POINTER(Fraglist), P], None),
+    "svo_build": ([P, u32, u32, ctypes.POINTER(OctreeC), ctypes.POINTER(BuildInfo), P], i32),
+    "svo_build_ex": ([P, u32, u32, ctypes.POINTER(Allocator), ctypes.POINTER(OctreeC), ctypes.POINTER(BuildInfo), P],
+                     i32),
+    "svo_build_fraglist": ([ctypes.POINTER(Fraglist), ctypes.POINTER(OctreeC), ctypes.POINTER(BuildInfo), P], i32),
+    "svo_build_workspace_size": ([u32, u32, u64], sz),
+    "svo_build_pool_bound": ([u32, u32], u64),
+    "svo_build_into": ([P, u32, u32, P, u64, P, P, P], i32),
+    "svo_octree_destroy": ([ctypes.POINTER(OctreeC), P], None),
+    "svo_raycast": ([ctypes.POINTER(OctreeC), P, u32, P, P, P], i32),
+    "svo_raycast_camera": ([ctypes.POINTER(OctreeC), ctypes.POINTER(CameraC), u32, u32, P, P, P], i32),
+    "svo_bounce_rays": ([P, u32, u64, P, P], i32),
+    "svo_camera_from_angles": ([ctypes.POINTER(f32), f32, f32, f32, f32, ctypes.POINTER(CameraC)], None),
+}
+
+_lib = None
+
+
+def declared_symbols() -> list[str]:
+    """Function names declared in include/svo.h."""
+    with open(HEADER) as f:
+        text = f.read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"^[A-Za-z_][\w\s\*]*?\b(svo_\w+)\s*\(", text, flags=re.M)
+    return sorted(set(names))
+
+
+def load(build_if_needed: bool = True):
+    """Load libsvo.so (building it first when sources are newer); raises if it cannot be loaded."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if build_if_needed and _build.needs_build():
+        _build.build()
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with python -m sparsevoxeloctree_gb300.build")
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, (args, res) in _SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = lib
+    return lib
+
+
+def check(code: int) -> None:
+    if code != SVO_OK:
+        raise SvoError(code, load().svo_last_error().decode())

@@ -1,0 +1,333 @@
+"""Host-side mirror of the reference's hot-path classes over the C ABI.
+
+Voxelizer, OctreeBuilder, Octree and OctreeTracer keep the reference's names and call shapes
+(src/Voxelizer.hpp:43-52, src/OctreeBuilder.hpp:36-43, src/Octree.hpp:18-28, src/OctreeTracer.hpp:57-70);
+`Cmd*` methods become stream-ordered calls and device memory is torch tensors (plumbing only: every
+computation is a libsvo.so kernel).  Status codes other than SVO_OK raise SvoError.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .formats import CAMERA_DTYPE, HIT_DTYPE, RAY_DTYPE, TRIANGLE_DTYPE
+
+
+def _stream(stream=None) -> ctypes.c_void_p:
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def _ptr(t: torch.Tensor | None) -> ctypes.c_void_p:
+    return ctypes.c_void_p(t.data_ptr() if t is not None else 0)
+
+
+def to_device(arr: np.ndarray, device="cuda") -> torch.Tensor:
+    """Upload a structured numpy array (triangles, rays, ...) as raw bytes."""
+    a = np.ascontiguousarray(arr)
+    return torch.from_numpy(a.view(np.uint8).reshape(-1)).to(device)
+
+
+def from_device(t: torch.Tensor, dtype: np.dtype) -> np.ndarray:
+    return t.detach().cpu().numpy().view(np.uint8).view(dtype)
+
+
+def camera_struct(cam) -> _lib.CameraC:
+    c = np.asarray(cam, CAMERA_DTYPE).reshape(())
+    out = _lib.CameraC()
+    for k in ("pos", "look", "side", "up"):
+        getattr(out, k)[:] = [float(x) for x in c[k]]
+    return out
+
+
+class TorchAllocator:
+    """Routes the engine's device allocations through torch's caching allocator (svo_allocator)."""
+
+    def __init__(self, device):
+        self.device = torch.device(device)
+        self.live: dict[int, torch.Tensor] = {}
+        self._alloc = _lib.ALLOC_FN(self._on_alloc)
+        self._release = _lib.RELEASE_FN(self._on_release)
+        self.struct = _lib.Allocator(self._alloc, self._release, None)
+
+    def _on_alloc(self, user, nbytes):
+        try:
+            t = torch.empty(int(nbytes), dtype=torch.uint8, device=self.device)
+        except RuntimeError:
+            return None
+        self.live[t.data_ptr()] = t
+        return t.data_ptr()
+
+    def _on_release(self, user, ptr):
+        self.live.pop(ptr, None)
+
+    def take(self, ptr: int) -> torch.Tensor:
+        return self.live.pop(ptr)
+
+
+# ------------------------------------------------------------------------------------------- Voxelizer
+class Voxelizer:
+    """Voxelizer (src/Voxelizer.hpp:13-53): triangles -> voxel-fragment list at a level."""
+
+    def __init__(self):
+        self.m_level = 0
+        self.m_voxel_resolution = 0
+        self.m_voxel_fragment_count = 0
+        self.m_tris: torch.Tensor | None = None
+        self.m_n_tris = 0
+        self.m_voxel_fragment_list: torch.Tensor | None = None
+        self.m_workspace: torch.Tensor | None = None
+        self.m_count_dev: torch.Tensor | None = None
+
+    @staticmethod
+    def Create(triangles, octree_level: int, stream=None) -> "Voxelizer":
+        """Voxelizer::Create (src/Voxelizer.cpp:5-26): count pass, exact allocation, then the fragment
+        list is filled (the reference records that second pass in CmdVoxelize)."""
+        v = Voxelizer()
+        if isinstance(triangles, np.ndarray):
+            triangles = to_device(np.asarray(triangles, TRIANGLE_DTYPE))
+        v.m_tris = triangles
+        v.m_n_tris = triangles.numel() // TRIANGLE_DTYPE.itemsize
+        v.m_level = int(octree_level)
+        v.m_voxel_resolution = 1 << v.m_level
+        lib = _lib.load()
+        alloc = TorchAllocator(triangles.device)
+        out = _lib.Fraglist()
+        _lib.check(lib.svo_voxelize_ex(_ptr(triangles), v.m_n_tris, v.m_level, ctypes.byref(alloc.struct),
+                                       ctypes.byref(out), _stream(stream)))
+        v.m_voxel_fragment_count = int(out.count)
+        buf = alloc.take(out.data) if out.count else torch.empty(0, dtype=torch.uint8, device=triangles.device)
+        v.m_voxel_fragment_list = buf.view(torch.int64)[: out.count]
+        return v
+
+    def CmdVoxelize(self, stream=None) -> None:
+        """Voxelizer::CmdVoxelize (src/Voxelizer.cpp:167-179): emit the fragments again into the list."""
+        lib = _lib.load()
+        if self.m_workspace is None:
+            dev = self.m_tris.device
+            self.m_workspace = torch.empty(lib.svo_voxelize_workspace_size(self.m_n_tris), dtype=torch.uint8,
+                                           device=dev)
+            self.m_count_dev = torch.zeros(2, dtype=torch.int64, device=dev)
+        _lib.check(lib.svo_voxelize_into(_ptr(self.m_tris), self.m_n_tris, self.m_level,
+                                         _ptr(self.m_voxel_fragment_list), self.m_voxel_fragment_count,
+                                         _ptr(self.m_count_dev), _ptr(self.m_workspace), _stream(stream)))
+
+    def GetLevel(self) -> int:
+        return self.m_level
+
+    def GetVoxelResolution(self) -> int:
+        return self.m_voxel_resolution
+
+    def GetVoxelFragmentCount(self) -> int:
+        return self.m_voxel_fragment_count
+
+    def GetVoxelFragmentList(self) -> torch.Tensor:
+        """Device tensor (int64 view of the uint64 fragments: low word x, high word y)."""
+        return self.m_voxel_fragment_list
+
+
+# ------------------------------------------------------------------------------------------- OctreeBuilder
+class OctreeBuilder:
+    """OctreeBuilder (src/OctreeBuilder.hpp:13-49): fragments -> node pool, level by level."""
+
+    RESULT_WORDS = ctypes.sizeof(_lib.BuildInfo) // 4 + 1
+
+    def __init__(self):
+        self.m_voxelizer: Voxelizer | None = None
+        self.m_fragments: torch.Tensor | None = None
+        self.m_count = 0
+        self.m_level = 0
+        self.m_capacity = 0
+        self.m_octree_buffer: torch.Tensor | None = None
+        self.m_workspace: torch.Tensor | None = None
+        self.m_result: torch.Tensor | None = None
+        self._info: dict | None = None
+
+    @staticmethod
+    def Create(voxelizer: Voxelizer | None = None, fragments: torch.Tensor | None = None, level: int | None = None,
+               capacity: int | None = None) -> "OctreeBuilder":
+        """OctreeBuilder::Create (src/OctreeBuilder.cpp:8-50): allocates the node pool and scratch.  The pool
+        holds the exact upper bound on the words a build of these fragments can use (the reference
+        guesses F*floor(L/3) words and writes past the buffer when the guess is short)."""
+        b = OctreeBuilder()
+        if voxelizer is not None:
+            b.m_voxelizer = voxelizer
+            fragments = voxelizer.GetVoxelFragmentList()
+            level = voxelizer.GetLevel()
+        b.m_fragments = fragments
+        b.m_count = int(fragments.numel())
+        b.m_level = int(level)
+        lib = _lib.load()
+        b.m_capacity = int(capacity) if capacity is not None else int(lib.svo_build_pool_bound(b.m_count, b.m_level))
+        dev = fragments.device
+        b.m_octree_buffer = torch.empty(max(b.m_capacity, 8), dtype=torch.int32, device=dev)
+        b.m_workspace = torch.empty(lib.svo_build_workspace_size(b.m_count, b.m_level, b.m_capacity), dtype=torch.uint8,
+                                    device=dev)
+        b.m_result = torch.zeros(OctreeBuilder.RESULT_WORDS, dtype=torch.int32, device=dev)
+        return b
+
+    def CmdBuild(self, stream=None) -> None:
+        """OctreeBuilder::CmdBuild (src/OctreeBuilder.cpp:142-210), stream-ordered, no host round trip."""
+        lib = _lib.load()
+        self._info = None
+        _lib.check(lib.svo_build_into(_ptr(self.m_fragments), self.m_count, self.m_level, _ptr(self.m_octree_buffer),
+                                      self.m_capacity, _ptr(self.m_workspace), _ptr(self.m_result), _stream(stream)))
+
+    def GetInfo(self) -> dict:
+        """Per-level counters of the last build (blocking read, like Counter::Read)."""
+        if self._info is None:
+            r = self.m_result.cpu().numpy().view(np.uint32)
+            status = int(r[-1])
+            if status & 2:
+                raise _lib.SvoError(_lib.SVO_ERR_CAPACITY, "octree pool too small for this build")
+            if status & 1:
+                raise _lib.SvoError(_lib.SVO_ERR_TIMEOUT, "a device-side wait gave up")
+            self._info = {"level": int(r[0]), "fragments": int(r[1]), "range_words": int(r[2]), "leaves": int(r[3]),
+                          "level_nodes": [int(x) for x in r[4:4 + self.m_level]]}
+        return self._info
+
+    def GetOctreeRange(self) -> int:
+        """OctreeBuilder::GetOctreeRange (src/OctreeBuilder.cpp:212-214): used bytes = (blocks + 1) * 32."""
+        return self.GetInfo()["range_words"] * 4
+
+    def GetOctree(self) -> torch.Tensor:
+        return self.m_octree_buffer
+
+    def GetLevel(self) -> int:
+        return self.m_level
+
+
+# ------------------------------------------------------------------------------------------- Octree
+class Octree:
+    """Octree (src/Octree.hpp:8-34): the node pool a tracer reads, its level and used range."""
+
+    def __init__(self):
+        self.m_buffer: torch.Tensor | None = None
+        self.m_range = 0  # bytes
+        self.m_level = 0
+
+    @staticmethod
+    def Create() -> "Octree":
+        return Octree()
+
+    def Update(self, builder: OctreeBuilder) -> None:
+        """Octree::Update (src/Octree.cpp:22-35); overflow is impossible here (exact pool bound), and a
+        failed build raises instead of being logged."""
+        self.m_range = builder.GetOctreeRange()
+        self.m_buffer = builder.GetOctree()
+        self.m_level = builder.GetLevel()
+
+    @staticmethod
+    def FromFragments(fragments: torch.Tensor, level: int, stream=None) -> "Octree":
+        """One-call build (svo_build_ex) with torch-owned memory."""
+        lib = _lib.load()
+        alloc = TorchAllocator(fragments.device)
+        out = _lib.OctreeC()
+        info = _lib.BuildInfo()
+        _lib.check(lib.svo_build_ex(_ptr(fragments), int(fragments.numel()), int(level), ctypes.byref(alloc.struct),
+                                    ctypes.byref(out), ctypes.byref(info), _stream(stream)))
+        o = Octree()
+        o.m_buffer = alloc.take(out.words).view(torch.int32)
+        o.m_range = int(out.range_words) * 4
+        o.m_level = int(level)
+        o.info = {"range_words": int(info.range_words), "leaves": int(info.leaves),
+                  "level_nodes": [int(info.level_nodes[i]) for i in range(level)]}
+        return o
+
+    def Empty(self) -> bool:
+        return self.m_buffer is None
+
+    def GetBuffer(self) -> torch.Tensor:
+        return self.m_buffer
+
+    def GetLevel(self) -> int:
+        return self.m_level
+
+    def GetRange(self) -> int:
+        return self.m_range
+
+    def words(self) -> torch.Tensor:
+        return self.m_buffer[: self.m_range // 4]
+
+    def c_struct(self) -> _lib.OctreeC:
+        return _lib.OctreeC(self.m_buffer.data_ptr(), self.m_buffer.numel(), self.m_range // 4, self.m_level, 0, 0)
+
+
+# ------------------------------------------------------------------------------------------- OctreeTracer
+class OctreeTracer:
+    """OctreeTracer (src/OctreeTracer.hpp:13-70) without the graphics pipeline: rays in, hits out in a
+    device buffer (32 B per ray, HIT_DTYPE) instead of a swapchain image."""
+
+    def __init__(self):
+        self.m_octree: Octree | None = None
+        self.m_camera = None
+        self.m_width = 0
+        self.m_height = 0
+        self.fetches: torch.Tensor | None = None
+
+    @staticmethod
+    def Create(octree: Octree, camera=None, width: int = 1280, height: int = 720) -> "OctreeTracer":
+        t = OctreeTracer()
+        t.m_octree, t.m_camera, t.m_width, t.m_height = octree, camera, int(width), int(height)
+        return t
+
+    def Resize(self, width: int, height: int) -> None:
+        self.m_width, self.m_height = int(width), int(height)
+
+    def _fetch_ptr(self, count_fetches: bool):
+        if not count_fetches:
+            return ctypes.c_void_p(0)
+        if self.fetches is None:
+            self.fetches = torch.zeros(1, dtype=torch.int64, device=self.m_octree.m_buffer.device)
+        return _ptr(self.fetches)
+
+    def CmdDrawPipeline(self, hits: torch.Tensor | None = None, stream=None, count_fetches: bool = False) -> torch.Tensor:
+        """One primary ray per pixel (shader/octree_tracer.frag:23-37); returns the hit buffer."""
+        n = self.m_width * self.m_height
+        if hits is None:
+            hits = torch.empty(n * HIT_DTYPE.itemsize, dtype=torch.uint8, device=self.m_octree.m_buffer.device)
+        cam = camera_struct(self.m_camera)
+        oc = self.m_octree.c_struct()
+        _lib.check(_lib.load().svo_raycast_camera(ctypes.byref(oc), ctypes.byref(cam), self.m_width, self.m_height,
+                                                  _ptr(hits), self._fetch_ptr(count_fetches), _stream(stream)))
+        return hits
+
+    def Trace(self, rays: torch.Tensor, hits: torch.Tensor | None = None, stream=None,
+              count_fetches: bool = False) -> torch.Tensor:
+        """Octree_RayMarchLeaf for an explicit ray buffer (RAY_DTYPE bytes on the device)."""
+        n = rays.numel() // RAY_DTYPE.itemsize
+        if hits is None:
+            hits = torch.empty(n * HIT_DTYPE.itemsize, dtype=torch.uint8, device=rays.device)
+        oc = self.m_octree.c_struct()
+        _lib.check(_lib.load().svo_raycast(ctypes.byref(oc), _ptr(rays), n, _ptr(hits), self._fetch_ptr(count_fetches),
+                                           _stream(stream)))
+        return hits
+
+    @staticmethod
+    def Bounce(hits: torch.Tensor, seed: int, rays: torch.Tensor | None = None, stream=None) -> torch.Tensor:
+        """One cosine-weighted diffuse bounce ray per hit (misses give a null ray)."""
+        n = hits.numel() // HIT_DTYPE.itemsize
+        if rays is None:
+            rays = torch.empty(n * RAY_DTYPE.itemsize, dtype=torch.uint8, device=hits.device)
+        _lib.check(_lib.load().svo_bounce_rays(_ptr(hits), n, seed & 0xFFFFFFFFFFFFFFFF, _ptr(rays), _stream(stream)))
+        return rays
+
+
+# ------------------------------------------------------------------------------------------- functional
+def voxelize(triangles, level: int, stream=None) -> torch.Tensor:
+    return Voxelizer.Create(triangles, level, stream).GetVoxelFragmentList()
+
+
+def build(fragments: torch.Tensor, level: int, stream=None) -> Octree:
+    return Octree.FromFragments(fragments, level, stream)
+
+
+def raycast(octree: Octree, rays: torch.Tensor, stream=None) -> torch.Tensor:
+    return OctreeTracer.Create(octree).Trace(rays, stream=stream)
+
+
+def hits_numpy(hits: torch.Tensor) -> np.ndarray:
+    return from_device(hits, HIT_DTYPE)

@@ -1,0 +1,427 @@
+// abi.cu — the C ABI of include/svo.h: argument checks, stream-ordered allocation, launches and the
+// few blocking readbacks the reference also performs (fragment count, octree range).
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "svo_internal.h"
+
+namespace svo {
+
+static std::atomic<uint64_t> g_launches{0};
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+static thread_local std::string g_error;
+
+static int fail(int code, const char *fmt, ...) {
+	char buf[512];
+	va_list ap;
+	va_start(ap, fmt);
+	vsnprintf(buf, sizeof(buf), fmt, ap);
+	va_end(ap);
+	g_error = buf;
+	return code;
+}
+
+static int cuda_fail(cudaError_t e, const char *what) {
+	cudaGetLastError(); // clear a sticky launch error of this thread
+	return fail(e == cudaErrorMemoryAllocation ? SVO_ERR_OOM : SVO_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define SVO_CK(call, what)                                                                                  \
+	do {                                                                                                \
+		cudaError_t e_ = (call);                                                                    \
+		if (e_ != cudaSuccess) return cuda_fail(e_, what);                                          \
+	} while (0)
+
+constexpr int kMaxDevices = 64;
+static int g_sm_count[kMaxDevices];
+static std::once_flag g_pool_once[kMaxDevices];
+
+static int current_device() {
+	int dev = 0;
+	cudaGetDevice(&dev);
+	return dev < kMaxDevices ? dev : 0;
+}
+
+int device_sm_count() {
+	const int dev = current_device();
+	if (g_sm_count[dev] == 0) {
+		int n = 0;
+		cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+		g_sm_count[dev] = n > 0 ? n : 1;
+	}
+	return g_sm_count[dev];
+}
+
+// Stream-ordered allocations come from the device's default memory pool; keeping freed memory in the
+// pool (release threshold = max) makes repeated builds allocation-free after the first one.
+static void prepare_pool() {
+	const int dev = current_device();
+	std::call_once(g_pool_once[dev], [dev] {
+		cudaMemPool_t pool;
+		if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+			uint64_t threshold = UINT64_MAX;
+			cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold);
+		}
+	});
+}
+
+template <typename T> static cudaError_t alloc_async(T **p, size_t bytes, cudaStream_t s) {
+	prepare_pool();
+	return cudaMallocAsync((void **)p, bytes ? bytes : 16, s);
+}
+
+static bool aligned(const void *p, size_t a) { return ((uintptr_t)p % a) == 0; }
+
+// Device memory from the caller's allocator, or from the stream-ordered pool when there is none.
+struct Mem {
+	const svo_allocator *a;
+	cudaStream_t s;
+	cudaError_t get(void **p, size_t bytes) {
+		if (a && a->alloc) {
+			*p = a->alloc(a->user, bytes ? bytes : 16);
+			return *p ? cudaSuccess : cudaErrorMemoryAllocation;
+		}
+		return alloc_async(p, bytes, s);
+	}
+	void put(void *p) {
+		if (!p) return;
+		if (a && a->alloc) {
+			if (a->release) a->release(a->user, p);
+		} else {
+			cudaFreeAsync(p, s);
+		}
+	}
+	uint32_t owned() const { return (a && a->alloc) ? 0u : 1u; }
+};
+
+static int check_level(uint32_t level) {
+	if (level < SVO_LEVEL_MIN || level > SVO_LEVEL_MAX)
+		return fail(SVO_ERR_INVALID, "level %u outside [%u, %u]", level, SVO_LEVEL_MIN, SVO_LEVEL_MAX);
+	return SVO_OK;
+}
+
+static int status_to_error(uint32_t status, const char *what) {
+	if (status & kStatusCapacity) return fail(SVO_ERR_CAPACITY, "%s: output exceeds its buffer or the 30-bit pointer range", what);
+	if (status & kStatusTimeout) return fail(SVO_ERR_TIMEOUT, "%s: a device-side wait gave up", what);
+	if (status & kStatusMalformed) return fail(SVO_ERR_INVALID, "%s: malformed octree pool", what);
+	return SVO_OK;
+}
+
+} // namespace svo
+
+using namespace svo;
+
+extern "C" {
+
+const char *svo_last_error(void) { return g_error.c_str(); }
+const char *svo_version(void) { return "svo-gb300 0.1 (sm_103a)"; }
+uint64_t svo_kernel_launches(void) { return g_launches.load(); }
+
+// ------------------------------------------------------------------------------------------ voxelize
+static int check_tris(const svo_triangle *tris, uint32_t n) {
+	if (n && !tris) return fail(SVO_ERR_INVALID, "null triangle buffer");
+	if (!aligned(tris, 16)) return fail(SVO_ERR_INVALID, "triangle buffer must be 16-byte aligned");
+	return SVO_OK;
+}
+
+size_t svo_voxelize_workspace_size(uint32_t n_tris) { return vox_workspace_bytes(n_tris, vox_default_unit_cap(n_tris)); }
+
+// Count pass with a workspace from `mem`; retries once with exact unit arrays when the first guess is
+// short.  On success *ws_out (still owned by the caller) holds the counted workspace.
+static int voxelize_count_pass(const svo_triangle *tris, uint32_t n_tris, uint32_t level, Mem &mem, void **ws_out,
+                               VoxWorkspace &w, uint64_t &total) {
+	uint64_t cap = vox_default_unit_cap(n_tris);
+	for (int attempt = 0; attempt < 2; ++attempt) {
+		void *ws = nullptr;
+		SVO_CK(mem.get(&ws, vox_workspace_bytes(n_tris, cap)), "voxelize workspace");
+		vox_workspace_layout(ws, n_tris, cap, w);
+		unsigned long long tot[3] = {0, 0, 0};
+		cudaError_t e = vox_launch_count(tris, n_tris, level, w, mem.s);
+		if (e == cudaSuccess) e = vox_launch_totals(w, mem.s);
+		if (e == cudaSuccess) e = cudaMemcpyAsync(tot, w.totals, sizeof(tot), cudaMemcpyDeviceToHost, mem.s);
+		if (e == cudaSuccess) e = cudaStreamSynchronize(mem.s);
+		if (e != cudaSuccess) {
+			mem.put(ws);
+			return cuda_fail(e, "voxelize count");
+		}
+		const uint32_t status = (uint32_t)tot[2];
+		if (status & kStatusUnits) {
+			mem.put(ws);
+			if (tot[1] >= 0xffffffffull) return fail(SVO_ERR_CAPACITY, "too many raster units");
+			cap = tot[1];
+			continue;
+		}
+		int rc = status_to_error(status, "voxelize count");
+		if (rc) {
+			mem.put(ws);
+			return rc;
+		}
+		*ws_out = ws;
+		total = tot[0];
+		return SVO_OK;
+	}
+	return fail(SVO_ERR_CAPACITY, "voxelize workspace retry failed");
+}
+
+int svo_voxelize_count(const svo_triangle *tris, uint32_t n_tris, uint32_t level, uint64_t *count_host,
+                       void *stream) {
+	int rc;
+	if ((rc = check_level(level)) || (rc = check_tris(tris, n_tris))) return rc;
+	if (!count_host) return fail(SVO_ERR_INVALID, "null count pointer");
+	Mem mem{nullptr, (cudaStream_t)stream};
+	void *ws = nullptr;
+	VoxWorkspace w;
+	uint64_t total = 0;
+	if ((rc = voxelize_count_pass(tris, n_tris, level, mem, &ws, w, total))) return rc;
+	mem.put(ws);
+	*count_host = total;
+	return SVO_OK;
+}
+
+int svo_voxelize_ex(const svo_triangle *tris, uint32_t n_tris, uint32_t level, const svo_allocator *alloc,
+                    svo_fraglist *out, void *stream) {
+	int rc;
+	if ((rc = check_level(level)) || (rc = check_tris(tris, n_tris))) return rc;
+	if (!out) return fail(SVO_ERR_INVALID, "null output fragment list");
+	cudaStream_t s = (cudaStream_t)stream;
+	Mem mem{alloc, s};
+	void *ws = nullptr;
+	VoxWorkspace w;
+	uint64_t total = 0;
+	if ((rc = voxelize_count_pass(tris, n_tris, level, mem, &ws, w, total))) return rc;
+	if (total > 0xffffffffull) { // the reference's fragment count is a uint32 (src/Voxelizer.hpp:33)
+		mem.put(ws);
+		return fail(SVO_ERR_CAPACITY, "%llu fragments exceed the 32-bit fragment count", (unsigned long long)total);
+	}
+	void *frags = nullptr;
+	cudaError_t e = mem.get(&frags, total * sizeof(uint64_t));
+	if (e != cudaSuccess) {
+		mem.put(ws);
+		return cuda_fail(e, "fragment list allocation");
+	}
+	e = vox_launch_emit(tris, n_tris, level, w, (uint64_t *)frags, total, s);
+	mem.put(ws);
+	if (e != cudaSuccess) {
+		mem.put(frags);
+		return cuda_fail(e, "voxelize emit");
+	}
+	out->data = (uint64_t *)frags;
+	out->count = (uint32_t)total;
+	out->level = level;
+	out->capacity = total;
+	out->owned = mem.owned();
+	out->reserved = 0;
+	return SVO_OK;
+}
+
+int svo_voxelize(const svo_triangle *tris, uint32_t n_tris, uint32_t level, svo_fraglist *out, void *stream) {
+	return svo_voxelize_ex(tris, n_tris, level, nullptr, out, stream);
+}
+
+int svo_voxelize_into(const svo_triangle *tris, uint32_t n_tris, uint32_t level, uint64_t *frags, uint64_t capacity,
+                      uint64_t *count_dev, void *workspace, void *stream) {
+	int rc;
+	if ((rc = check_level(level)) || (rc = check_tris(tris, n_tris))) return rc;
+	if (!count_dev || !workspace || (capacity && !frags)) return fail(SVO_ERR_INVALID, "null argument");
+	if (!aligned(workspace, 256)) return fail(SVO_ERR_INVALID, "workspace must be 256-byte aligned");
+	cudaStream_t s = (cudaStream_t)stream;
+	VoxWorkspace w;
+	vox_workspace_layout(workspace, n_tris, vox_default_unit_cap(n_tris), w);
+	SVO_CK(vox_launch_count(tris, n_tris, level, w, s), "voxelize count");
+	SVO_CK(vox_launch_totals(w, s), "voxelize totals");
+	SVO_CK(vox_launch_emit(tris, n_tris, level, w, frags, capacity, s), "voxelize emit");
+	// count_dev[0] = fragments, count_dev[1] = status bits (totals[2])
+	SVO_CK(cudaMemcpyAsync(count_dev, w.totals, sizeof(uint64_t), cudaMemcpyDeviceToDevice, s), "voxelize count copy");
+	SVO_CK(cudaMemcpyAsync(count_dev + 1, w.totals + 2, sizeof(uint64_t), cudaMemcpyDeviceToDevice, s),
+	       "voxelize status copy");
+	return SVO_OK;
+}
+
+void svo_fraglist_destroy(svo_fraglist *f, void *stream) {
+	if (!f) return;
+	if (f->owned && f->data) cudaFreeAsync(f->data, (cudaStream_t)stream);
+	memset(f, 0, sizeof(*f));
+}
+
+// ------------------------------------------------------------------------------------------ build
+uint64_t svo_build_pool_bound(uint32_t count, uint32_t level) { return build_pool_bound(count, level); }
+
+size_t svo_build_workspace_size(uint32_t count, uint32_t level, uint64_t capacity) {
+	return build_workspace_bytes(count, level, capacity);
+}
+
+static int check_frags(const uint64_t *frags, uint32_t count) {
+	if (count && !frags) return fail(SVO_ERR_INVALID, "null fragment buffer");
+	if (!aligned(frags, 8)) return fail(SVO_ERR_INVALID, "fragment buffer must be 8-byte aligned");
+	return SVO_OK;
+}
+
+int svo_build_ex(const uint64_t *frags, uint32_t count, uint32_t level, const svo_allocator *alloc, svo_octree *out,
+                 svo_build_info *info, void *stream) {
+	int rc;
+	if ((rc = check_level(level)) || (rc = check_frags(frags, count))) return rc;
+	if (!out) return fail(SVO_ERR_INVALID, "null output octree");
+	cudaStream_t s = (cudaStream_t)stream;
+	Mem mem{alloc, s};
+	const uint64_t capacity = build_pool_bound(count, level);
+	void *pool = nullptr;
+	SVO_CK(mem.get(&pool, capacity * sizeof(uint32_t)), "octree pool allocation");
+	void *ws = nullptr;
+	cudaError_t e = mem.get(&ws, build_workspace_bytes(count, level, capacity));
+	if (e != cudaSuccess) {
+		mem.put(pool);
+		return cuda_fail(e, "build workspace allocation");
+	}
+	BuildWorkspace w;
+	build_workspace_layout(ws, count, level, capacity, w);
+	e = build_launch(frags, count, level, (uint32_t *)pool, capacity, w, s);
+	BuildState st;
+	if (e == cudaSuccess) e = cudaMemcpyAsync(&st, w.state, sizeof(st), cudaMemcpyDeviceToHost, s);
+	if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+	mem.put(ws);
+	if (e != cudaSuccess) {
+		mem.put(pool);
+		return cuda_fail(e, "build");
+	}
+	if ((rc = status_to_error(st.status, "build"))) {
+		mem.put(pool);
+		return rc;
+	}
+	out->words = (uint32_t *)pool;
+	out->capacity = capacity;
+	out->range_words = st.range_words;
+	out->level = level;
+	out->owned = mem.owned();
+	out->reserved = 0;
+	if (info) {
+		memset(info, 0, sizeof(*info));
+		info->level = level;
+		info->fragments = count;
+		info->range_words = st.range_words;
+		info->leaves = st.leaves;
+		for (uint32_t d = 1; d <= level; ++d) info->level_nodes[d - 1] = d < level ? st.lv[d].nodes : st.leaves;
+	}
+	return SVO_OK;
+}
+
+int svo_build(const uint64_t *frags, uint32_t count, uint32_t level, svo_octree *out, svo_build_info *info,
+              void *stream) {
+	return svo_build_ex(frags, count, level, nullptr, out, info, stream);
+}
+
+int svo_build_fraglist(const svo_fraglist *f, svo_octree *out, svo_build_info *info, void *stream) {
+	if (!f) return fail(SVO_ERR_INVALID, "null fragment list");
+	return svo_build(f->data, f->count, f->level, out, info, stream);
+}
+
+int svo_build_into(const uint64_t *frags, uint32_t count, uint32_t level, uint32_t *pool, uint64_t capacity,
+                   void *workspace, void *result_dev, void *stream) {
+	int rc;
+	if ((rc = check_level(level)) || (rc = check_frags(frags, count))) return rc;
+	if (!pool || !workspace || !result_dev) return fail(SVO_ERR_INVALID, "null argument");
+	if (capacity < 8) return fail(SVO_ERR_CAPACITY, "pool smaller than the root block");
+	if (!aligned(pool, 16) || !aligned(workspace, 256) || !aligned(result_dev, 4))
+		return fail(SVO_ERR_INVALID, "pool must be 16-byte and workspace 256-byte aligned");
+	cudaStream_t s = (cudaStream_t)stream;
+	BuildWorkspace w;
+	build_workspace_layout(workspace, count, level, capacity, w);
+	SVO_CK(build_launch(frags, count, level, pool, capacity, w, s), "build");
+	SVO_CK(build_launch_export(w, level, count, result_dev, s), "build info export");
+	return SVO_OK;
+}
+
+void svo_octree_destroy(svo_octree *o, void *stream) {
+	if (!o) return;
+	if (o->owned && o->words) cudaFreeAsync(o->words, (cudaStream_t)stream);
+	memset(o, 0, sizeof(*o));
+}
+
+// ------------------------------------------------------------------------------------------ march
+static int check_octree(const svo_octree *o) {
+	if (!o || !o->words) return fail(SVO_ERR_INVALID, "null octree");
+	int rc = check_level(o->level);
+	if (rc) return rc;
+	if (o->range_words < 8 || o->range_words % 8) return fail(SVO_ERR_INVALID, "octree range must be a positive multiple of 8");
+	return SVO_OK;
+}
+
+static int raycast_common(const svo_octree *o, const svo_ray *rays, const svo_camera *cam, uint32_t width,
+                          uint32_t height, uint32_t n, svo_hit *hits, uint64_t *fetches_dev, void *stream) {
+	int rc;
+	if ((rc = check_octree(o))) return rc;
+	if (n && !hits) return fail(SVO_ERR_INVALID, "null hit buffer");
+	if (!aligned(hits, 16)) return fail(SVO_ERR_INVALID, "hit buffer must be 16-byte aligned");
+	if (!cam && n && (!rays || !aligned(rays, 8))) return fail(SVO_ERR_INVALID, "ray buffer must be 8-byte aligned");
+	cudaStream_t s = (cudaStream_t)stream;
+	uint32_t *scratch = nullptr;
+	SVO_CK(alloc_async(&scratch, 2 * sizeof(uint32_t), s), "ray ticket allocation");
+	MarchArgs a;
+	memset(&a, 0, sizeof(a));
+	a.pool = o->words;
+	a.range = o->range_words;
+	a.level = o->level;
+	a.rays = rays;
+	if (cam) a.cam = *cam;
+	a.width = width;
+	a.height = height;
+	a.n = n;
+	a.hits = hits;
+	a.ticket = scratch;
+	a.status = scratch + 1;
+	a.fetches = (unsigned long long *)fetches_dev;
+	cudaError_t e = march_launch(a, cam != nullptr, s);
+	cudaFreeAsync(scratch, s);
+	if (e != cudaSuccess) return cuda_fail(e, "raycast");
+	return SVO_OK;
+}
+
+int svo_raycast(const svo_octree *o, const svo_ray *rays, uint32_t n, svo_hit *hits, uint64_t *fetches_dev,
+                void *stream) {
+	return raycast_common(o, rays, nullptr, 0, 0, n, hits, fetches_dev, stream);
+}
+
+int svo_raycast_camera(const svo_octree *o, const svo_camera *cam, uint32_t width, uint32_t height, svo_hit *hits,
+                       uint64_t *fetches_dev, void *stream) {
+	if (!cam) return fail(SVO_ERR_INVALID, "null camera");
+	const uint64_t n = (uint64_t)width * height;
+	if (n > 0xffffffffull) return fail(SVO_ERR_INVALID, "image too large");
+	return raycast_common(o, nullptr, cam, width, height, (uint32_t)n, hits, fetches_dev, stream);
+}
+
+int svo_bounce_rays(const svo_hit *hits, uint32_t n, uint64_t seed, svo_ray *rays, void *stream) {
+	if (n && (!hits || !rays)) return fail(SVO_ERR_INVALID, "null argument");
+	SVO_CK(bounce_launch(hits, n, seed, rays, (cudaStream_t)stream), "bounce rays");
+	return SVO_OK;
+}
+
+void svo_camera_from_angles(const float pos[3], float yaw, float pitch, float fov, float aspect, svo_camera *cam) {
+	// trans = rotate(yaw about +y) * rotate(pitch about -x); look = trans*(0,0,1), side = trans*(1,0,0)
+	const float cy = cosf(yaw), sy = sinf(yaw), cp = cosf(pitch), sp = sinf(pitch);
+	const float tg = tanf(fov * 0.5f);
+	float look[3] = {sy * cp, sp, cy * cp};
+	float ll = sqrtf(look[0] * look[0] + look[1] * look[1] + look[2] * look[2]);
+	float side[3] = {cy, 0.0f, -sy};
+	float sl = sqrtf(side[0] * side[0] + side[2] * side[2]);
+	for (int k = 0; k < 3; ++k) {
+		look[k] /= ll;
+		side[k] = side[k] / sl * tg * aspect;
+	}
+	float up[3] = {look[1] * side[2] - look[2] * side[1], look[2] * side[0] - look[0] * side[2],
+	               look[0] * side[1] - look[1] * side[0]};
+	float ul = sqrtf(up[0] * up[0] + up[1] * up[1] + up[2] * up[2]);
+	for (int k = 0; k < 3; ++k) {
+		cam->pos[k] = pos[k];
+		cam->look[k] = look[k];
+		cam->side[k] = side[k];
+		cam->up[k] = up[k] / ul * tg;
+	}
+	cam->pos[3] = cam->look[3] = cam->side[3] = cam->up[3] = 1.0f;
+}
+
+} // extern "C"

@@ -1,0 +1,128 @@
+// common.cuh — device helpers shared by the voxelize, build and march kernels (sm_103a).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/svo.h"
+#include "svo_internal.h"
+
+#define SVO_DEV __device__ __forceinline__
+
+namespace svo {
+
+constexpr unsigned kFullMask = 0xffffffffu;
+
+// Iterations a tile waits for its predecessor's descriptor before giving up.  Tiles are claimed in
+// order by an atomic ticket, so the predecessor is always running or done; the bound only guards
+// against a broken invariant and is never reached in a correct run.
+constexpr uint32_t kSpinLimit = 1u << 22;
+
+// ------------------------------------------------------------------------------- warp / block scans
+SVO_DEV uint32_t lane_id() { return threadIdx.x & 31u; }
+
+template <typename T> SVO_DEV T warp_inclusive_sum(T v) {
+#pragma unroll
+	for (int d = 1; d < 32; d <<= 1) {
+		T o = __shfl_up_sync(kFullMask, v, d);
+		if ((int)lane_id() >= d) v += o;
+	}
+	return v;
+}
+
+template <typename T> SVO_DEV T warp_sum(T v) {
+#pragma unroll
+	for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(kFullMask, v, d);
+	return v;
+}
+
+// Exclusive block scan of one value per thread; returns the exclusive prefix and the block total.
+// `warp_tmp` must hold blockDim.x / 32 + 1 elements.
+template <typename T, int TPB> SVO_DEV T block_exclusive_sum(T v, T *warp_tmp, T &total) {
+	const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+	T incl = warp_inclusive_sum(v);
+	if (lane == 31) warp_tmp[warp] = incl;
+	__syncthreads();
+	if (warp == 0) {
+		T w = lane < TPB / 32 ? warp_tmp[lane] : T(0);
+		T wi = warp_inclusive_sum(w);
+		if (lane < TPB / 32) warp_tmp[lane] = wi - w;
+		if (lane == 31) warp_tmp[TPB / 32] = wi;
+	}
+	__syncthreads();
+	T r = warp_tmp[warp] + incl - v;
+	total = warp_tmp[TPB / 32];
+	__syncthreads();
+	return r;
+}
+
+// ------------------------------------------------------------------------------- decoupled look-back
+// Tile descriptor (64 bits): epoch[56..63] | flag[54..55] | value[0..53]; flag 1 = tile aggregate,
+// 2 = inclusive prefix.  A descriptor whose epoch differs from the caller's counts as unpublished, so
+// one zeroed descriptor array serves several scans (levels) of one call.
+constexpr unsigned long long kDescValueMask = (1ull << 54) - 1;
+
+SVO_DEV void desc_publish(unsigned long long *d, uint32_t epoch, uint32_t flag, unsigned long long value) {
+	unsigned long long w = ((unsigned long long)epoch << 56) | ((unsigned long long)flag << 54) | value;
+	asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(d), "l"(w) : "memory");
+}
+
+SVO_DEV unsigned long long desc_load(const unsigned long long *d) {
+	unsigned long long w;
+	asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(w) : "l"(d) : "memory");
+	return w;
+}
+
+// Called by one thread of tile `t` once its aggregate is known; returns the exclusive prefix of the
+// tile.  Waits are bounded (kSpinLimit); on timeout the status word gets kStatusTimeout.
+SVO_DEV unsigned long long tile_lookback(unsigned long long *descs, uint32_t t, uint32_t epoch,
+                                         unsigned long long aggregate, uint32_t *status) {
+	if (t == 0) {
+		desc_publish(&descs[0], epoch, 2, aggregate);
+		return 0;
+	}
+	desc_publish(&descs[t], epoch, 1, aggregate);
+	unsigned long long prefix = 0;
+	int64_t j = (int64_t)t - 1;
+	uint32_t spins = 0;
+	while (j >= 0) {
+		unsigned long long w = desc_load(&descs[j]);
+		uint32_t e = (uint32_t)(w >> 56), flag = (uint32_t)(w >> 54) & 3u;
+		if (e != epoch || flag == 0) {
+			if (++spins > kSpinLimit) {
+				atomicOr(status, kStatusTimeout);
+				break;
+			}
+			__nanosleep(20);
+			continue;
+		}
+		prefix += w & kDescValueMask;
+		if (flag == 2) break;
+		--j;
+	}
+	desc_publish(&descs[t], epoch, 2, prefix + aggregate);
+	return prefix;
+}
+
+// ------------------------------------------------------------------------------- integer helpers
+// floor(num / den) for den > 0, exact whenever the exact quotient lies in [lo - 2, hi + 2]; outside
+// that window the result lies outside [lo, hi] on the same side as the exact quotient, which is all a
+// caller that clamps to [lo, hi] needs.  A float estimate (relative error ~2^-22, quotients here stay
+// below 2^14 in magnitude) is within one of the exact floor and is corrected with one exact remainder.
+SVO_DEV int64_t floor_div_window(int64_t num, int64_t den, int32_t lo, int32_t hi) {
+	float est = floorf(__fdividef(__ll2float_rn(num), __ll2float_rn(den)));
+	est = fminf(fmaxf(est, (float)(lo - 2)), (float)(hi + 2));
+	int64_t q = (int64_t)est;
+	int64_t r = num - q * den;
+	if (r < 0)
+		q -= 1;
+	else if (r >= den)
+		q += 1;
+	return q;
+}
+
+SVO_DEV int32_t clamp_i32(int64_t v, int32_t lo, int32_t hi) {
+	return (int32_t)(v < lo ? lo : (v > hi ? hi : v));
+}
+
+} // namespace svo

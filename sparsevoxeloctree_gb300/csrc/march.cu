@@ -1,0 +1,350 @@
+// march.cu — stack-based leaf ray march over the octree (replaces Octree_RayMarchLeaf,
+// shader/octree.glsl:179-340, as called per pixel by shader/octree_tracer.frag:23-37 and per bounce by
+// shader/path_tracer.comp:35-47).
+//
+// This translation unit is compiled with -fmad=false and IEEE division/square root: every float
+// operation is rounded separately, so results are bit-identical to the oracle's scalar restatement.
+//
+// GB300 design:
+//   * persistent grid (a few blocks per SM); each warp claims batches of rays from a global ticket, so
+//     long incoherent rays do not leave the tail of the launch idle;
+//   * the traversal stack (one parent word per level, at most 12) lives in shared memory, laid out
+//     [level][thread] so a warp's accesses hit 32 distinct banks; it never touches local memory;
+//   * node words are read through the read-only path (ld.global.nc), so hot upper levels stay in L1/L2;
+//   * camera rays are generated in the kernel (no ray buffer), hits are written as two 16 B stores.
+#include "common.cuh"
+#include "svo_internal.h"
+
+namespace svo {
+
+constexpr int kMarchTPB = 128;
+constexpr uint32_t kRaysPerLane = 4; // rays a lane takes per ticket
+constexpr float kEps = 3.552713678800501e-15f; // EPS of shader/octree.glsl:44 (2^-48)
+
+SVO_DEV float max_glsl(float x, float y) { return x < y ? y : x; }
+SVO_DEV float min_glsl(float x, float y) { return y < x ? y : x; }
+SVO_DEV float eps_clamp(float v) { return fabsf(v) > kEps ? v : (v >= 0.0f ? kEps : -kEps); }
+
+struct MarchOut {
+	float t;
+	float pos[3];
+	uint32_t node, iter;
+	uint32_t voxel_lo, voxel_hi; // packed uint16 voxel[3] and flags, as in svo_hit
+};
+
+// One ray; `stack` points at this thread's column of the shared stack (stride kMarchTPB).
+SVO_DEV void march_ray(const uint32_t *__restrict__ pool, uint32_t range, uint32_t level, const float o[3],
+                       const float dir[3], uint32_t *stack, MarchOut &out, uint32_t &nfetch, uint32_t *status) {
+	nfetch = 0;
+	if (dir[0] == 0.0f && dir[1] == 0.0f && dir[2] == 0.0f) { // no ray (miss of a previous bounce)
+		out.t = 0.0f;
+		out.pos[0] = o[0], out.pos[1] = o[1], out.pos[2] = o[2];
+		out.node = 0, out.iter = 0;
+		out.voxel_lo = 0xffffffffu;
+		out.voxel_hi = 0x0000ffffu;
+		return;
+	}
+	for (uint32_t k = 0; k < level; ++k) stack[k * kMarchTPB] = 0u;
+	float d[3] = {eps_clamp(dir[0]), eps_clamp(dir[1]), eps_clamp(dir[2])};
+	float coef[3], bias[3];
+#pragma unroll
+	for (int k = 0; k < 3; ++k) {
+		coef[k] = 1.0f / -fabsf(d[k]);
+		bias[k] = coef[k] * o[k];
+	}
+	uint32_t oct_mask = 0;
+#pragma unroll
+	for (int k = 0; k < 3; ++k)
+		if (d[k] > 0.0f) {
+			oct_mask ^= 1u << k;
+			bias[k] = 3.0f * coef[k] - bias[k];
+		}
+	float t_min = max_glsl(max_glsl(2.0f * coef[0] - bias[0], 2.0f * coef[1] - bias[1]), 2.0f * coef[2] - bias[2]);
+	const float t_max = min_glsl(min_glsl(coef[0] - bias[0], coef[1] - bias[1]), coef[2] - bias[2]);
+	t_min = max_glsl(t_min, 0.0f);
+	float h = t_max;
+	uint32_t parent = 0, cur = 0, idx = 0;
+	float pos[3] = {1.0f, 1.0f, 1.0f};
+#pragma unroll
+	for (int k = 0; k < 3; ++k)
+		if (1.5f * coef[k] - bias[k] > t_min) {
+			idx ^= 1u << k;
+			pos[k] = 1.5f;
+		}
+	uint32_t scale = SVO_STACK_SIZE - 1;
+	float scale_exp2 = 0.5f;
+	uint32_t iter = 0;
+	const uint32_t min_scale = SVO_STACK_SIZE - level; // deepest scale a valid tree reaches
+
+	while (scale < SVO_STACK_SIZE) {
+		if (iter >= SVO_MARCH_MAX_ITER) break;
+		++iter;
+		if (cur == 0u) {
+			const uint32_t w = parent + (idx ^ oct_mask);
+			if (w >= range) {
+				atomicOr(status, kStatusMalformed);
+				scale = 0xffffffffu;
+				break;
+			}
+			cur = __ldg(pool + w);
+			++nfetch;
+		}
+		float tc[3];
+#pragma unroll
+		for (int k = 0; k < 3; ++k) tc[k] = pos[k] * coef[k] - bias[k];
+		const float tc_max = min_glsl(min_glsl(tc[0], tc[1]), tc[2]);
+
+		if ((cur & 0x80000000u) != 0u && t_min <= t_max) {
+			const float half = scale_exp2 * 0.5f;
+			float t_center[3];
+#pragma unroll
+			for (int k = 0; k < 3; ++k) t_center[k] = half * coef[k] + tc[k];
+			if ((cur & 0x40000000u) != 0u) break; // leaf
+			if (scale <= min_scale) {              // interior node below the leaf level: malformed pool
+				atomicOr(status, kStatusMalformed);
+				scale = 0xffffffffu;
+				break;
+			}
+			if (tc_max < h) stack[(SVO_STACK_SIZE - 1 - scale) * kMarchTPB] = parent; // push
+			h = tc_max;
+			parent = cur & 0x3fffffffu;
+			idx = 0;
+			--scale;
+			scale_exp2 = half;
+#pragma unroll
+			for (int k = 0; k < 3; ++k)
+				if (t_center[k] > t_min) {
+					idx ^= 1u << k;
+					pos[k] += scale_exp2;
+				}
+			cur = 0;
+			continue;
+		}
+		// advance
+		uint32_t step_mask = 0;
+#pragma unroll
+		for (int k = 0; k < 3; ++k)
+			if (tc[k] <= tc_max) {
+				step_mask ^= 1u << k;
+				pos[k] -= scale_exp2;
+			}
+		t_min = tc_max;
+		idx ^= step_mask;
+		if ((idx & step_mask) != 0u) { // pop
+			uint32_t diff = 0;
+#pragma unroll
+			for (int k = 0; k < 3; ++k)
+				if (step_mask & (1u << k)) diff |= __float_as_uint(pos[k]) ^ __float_as_uint(pos[k] + scale_exp2);
+			scale = diff ? 31u - (uint32_t)__clz(diff) : 0xffffffffu; // findMSB
+			if (scale >= SVO_STACK_SIZE) break;
+			scale_exp2 = __uint_as_float((scale - SVO_STACK_SIZE + 127u) << 23u);
+			parent = stack[(SVO_STACK_SIZE - 1 - scale) * kMarchTPB];
+			uint32_t sh[3];
+#pragma unroll
+			for (int k = 0; k < 3; ++k) {
+				sh[k] = __float_as_uint(pos[k]) >> scale;
+				pos[k] = __uint_as_float(sh[k] << scale);
+			}
+			idx = (sh[0] & 1u) | ((sh[1] & 1u) << 1) | ((sh[2] & 1u) << 2);
+			h = 0.0f;
+			cur = 0;
+		}
+	}
+
+	// normal from the exit corner, un-mirror, o_pos (shader/octree.glsl:307-334)
+	float tc[3];
+#pragma unroll
+	for (int k = 0; k < 3; ++k) tc[k] = coef[k] * (pos[k] + scale_exp2) - bias[k];
+	const uint32_t nax = (tc[0] > tc[1] && tc[0] > tc[2]) ? 0u : (tc[1] > tc[2] ? 1u : 2u);
+	const bool neg = (oct_mask >> nax) & 1u; // normal is -axis exactly when that axis was mirrored
+#pragma unroll
+	for (int k = 0; k < 3; ++k)
+		if (oct_mask & (1u << k)) pos[k] = 3.0f - scale_exp2 - pos[k];
+#pragma unroll
+	for (int k = 0; k < 3; ++k) {
+		float v = o[k] + t_min * d[k];
+		v = min_glsl(max_glsl(v, pos[k]), pos[k] + scale_exp2);
+		if ((uint32_t)k == nax) v = neg ? pos[k] - kEps : pos[k] + scale_exp2 + kEps * 2.0f;
+		out.pos[k] = v;
+	}
+	const bool hit = scale < SVO_STACK_SIZE && t_min <= t_max;
+	out.t = t_min;
+	out.iter = iter;
+	const uint32_t flags = (hit ? SVO_HIT_FLAG_HIT : 0u) | (nax << 1) | (neg ? SVO_HIT_NORMAL_NEG : 0u);
+	if (hit) {
+		const float res = (float)(1u << level);
+		const uint32_t vx = (uint32_t)((pos[0] - 1.0f) * res), vy = (uint32_t)((pos[1] - 1.0f) * res);
+		const uint32_t vz = (uint32_t)((pos[2] - 1.0f) * res);
+		out.node = cur;
+		out.voxel_lo = vx | (vy << 16);
+		out.voxel_hi = vz | (flags << 16);
+	} else {
+		out.node = 0;
+		out.voxel_lo = 0xffffffffu;
+		out.voxel_hi = 0xffffu | (flags << 16);
+	}
+}
+
+SVO_DEV void store_hit(svo_hit *hits, uint32_t r, const MarchOut &m) {
+	uint4 *dst = reinterpret_cast<uint4 *>(hits + r);
+	dst[0] = make_uint4(__float_as_uint(m.t), __float_as_uint(m.pos[0]), __float_as_uint(m.pos[1]),
+	                    __float_as_uint(m.pos[2]));
+	dst[1] = make_uint4(m.node, m.iter, m.voxel_lo, m.voxel_hi);
+}
+
+// Camera_GenRay(ivec2(pixel) / size) (shader/camera.glsl:11-14, shader/octree_tracer.frag:24).
+SVO_DEV void camera_ray(const svo_camera &cam, uint32_t width, uint32_t height, uint32_t r, float o[3], float d[3]) {
+	const uint32_t y = r / width, x = r - y * width;
+	float cx = (float)x / (float)width, cy = (float)y / (float)height;
+	cx = cx * 2.0f - 1.0f;
+	cy = cy * 2.0f - 1.0f;
+	float v[3];
+#pragma unroll
+	for (int k = 0; k < 3; ++k) v[k] = (cam.look[k] - cam.side[k] * cx) - cam.up[k] * cy;
+	const float len = sqrtf((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]);
+#pragma unroll
+	for (int k = 0; k < 3; ++k) {
+		o[k] = cam.pos[k];
+		d[k] = v[k] / len;
+	}
+}
+
+template <bool CAMERA>
+__global__ void __launch_bounds__(kMarchTPB) march_kernel(MarchArgs a) {
+	__shared__ uint32_t s_stack[SVO_LEVEL_MAX * kMarchTPB];
+	uint32_t *stack = s_stack + threadIdx.x;
+	const uint32_t lane = lane_id();
+	unsigned long long fetched = 0;
+	for (;;) {
+		uint32_t base = 0;
+		if (lane == 0) base = atomicAdd(a.ticket, 32u * kRaysPerLane);
+		base = __shfl_sync(kFullMask, base, 0);
+		if (base >= a.n) break;
+#pragma unroll 1
+		for (uint32_t k = 0; k < kRaysPerLane; ++k) {
+			const uint32_t r = base + k * 32u + lane;
+			if (r >= a.n) break;
+			float o[3], d[3];
+			if (CAMERA) {
+				camera_ray(a.cam, a.width, a.height, r, o, d);
+			} else {
+				const float2 *src = reinterpret_cast<const float2 *>(a.rays + r);
+				const float2 p0 = src[0], p1 = src[1], p2 = src[2];
+				o[0] = p0.x, o[1] = p0.y, o[2] = p1.x, d[0] = p1.y, d[1] = p2.x, d[2] = p2.y;
+			}
+			MarchOut m;
+			uint32_t nf;
+			march_ray(a.pool, a.range, a.level, o, d, stack, m, nf, a.status);
+			store_hit(a.hits, r, m);
+			fetched += nf;
+		}
+	}
+	if (a.fetches) {
+		fetched = warp_sum(fetched);
+		if (lane == 0) atomicAdd(a.fetches, fetched);
+	}
+}
+
+// ------------------------------------------------------------------------------------ bounce rays
+SVO_DEV uint64_t mix64(uint64_t z) {
+	z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+	z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+	return z ^ (z >> 31);
+}
+
+// sin and cos of 2*pi*u (u in [0,1)): quadrant split + Taylor polynomials of degree 13/12 on [0, pi/2),
+// each operation rounded separately (this file is built with -fmad=false).
+SVO_DEV void sincos_2pi(float u, float &s_out, float &c_out) {
+	const float q4 = u * 4.0f;
+	const int q = (int)q4;
+	const float r = q4 - (float)q;
+	const float a = r * 1.57079632679489662f;
+	const float a2 = a * a;
+	float s = 1.0f / 6227020800.0f;
+	s = s * a2 + -1.0f / 39916800.0f;
+	s = s * a2 + 1.0f / 362880.0f;
+	s = s * a2 + -1.0f / 5040.0f;
+	s = s * a2 + 1.0f / 120.0f;
+	s = s * a2 + -1.0f / 6.0f;
+	s = s * a2 + 1.0f;
+	s = s * a;
+	float c = 1.0f / 479001600.0f;
+	c = c * a2 + -1.0f / 3628800.0f;
+	c = c * a2 + 1.0f / 40320.0f;
+	c = c * a2 + -1.0f / 720.0f;
+	c = c * a2 + 1.0f / 24.0f;
+	c = c * a2 + -0.5f;
+	c = c * a2 + 1.0f;
+	switch (q & 3) {
+	case 0: s_out = s, c_out = c; break;
+	case 1: s_out = c, c_out = -s; break;
+	case 2: s_out = -s, c_out = -c; break;
+	default: s_out = -c, c_out = s; break;
+	}
+}
+
+// o = hit pos, d = Diffuse_Sample about the hit normal (shader/diffuse.glsl:7-14 with AlignDirection,
+// shader/util.glsl:5-9); misses give d = 0.
+__global__ void bounce_kernel(const svo_hit *__restrict__ hits, uint32_t n, uint64_t seed, svo_ray *__restrict__ rays) {
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		const svo_hit h = hits[i];
+		float d[3] = {0.0f, 0.0f, 0.0f};
+		if (h.flags & SVO_HIT_FLAG_HIT) {
+			const uint64_t z = mix64(seed + 0x9E3779B97F4A7C15ull * ((uint64_t)i + 1));
+			const float u1 = (float)(uint32_t)(z >> 40) * (1.0f / 16777216.0f);
+			const float u2 = (float)(uint32_t)((z >> 16) & 0xffffffu) * (1.0f / 16777216.0f);
+			const float rr = sqrtf(u1);
+			float sn, cs;
+			sincos_2pi(u2, sn, cs);
+			const float dl[3] = {rr * cs, rr * sn, sqrtf(1.0f - u1)};
+			const uint32_t ax = SVO_HIT_NORMAL_AXIS(h.flags);
+			float nrm[3] = {0.0f, 0.0f, 0.0f};
+			nrm[ax] = (h.flags & SVO_HIT_NORMAL_NEG) ? -1.0f : 1.0f;
+			float ref[3] = {0.0f, 0.0f, 0.0f};
+			if (fabsf(nrm[0]) > 0.01f)
+				ref[1] = 1.0f;
+			else
+				ref[0] = 1.0f;
+			float u[3] = {ref[1] * nrm[2] - ref[2] * nrm[1], ref[2] * nrm[0] - ref[0] * nrm[2],
+			              ref[0] * nrm[1] - ref[1] * nrm[0]};
+			const float ul = sqrtf((u[0] * u[0] + u[1] * u[1]) + u[2] * u[2]);
+#pragma unroll
+			for (int k = 0; k < 3; ++k) u[k] = u[k] / ul;
+			const float v[3] = {nrm[1] * u[2] - nrm[2] * u[1], nrm[2] * u[0] - nrm[0] * u[2],
+			                    nrm[0] * u[1] - nrm[1] * u[0]};
+#pragma unroll
+			for (int k = 0; k < 3; ++k) d[k] = (dl[0] * u[k] + dl[1] * v[k]) + dl[2] * nrm[k];
+		}
+		svo_ray r;
+		r.o[0] = h.pos[0], r.o[1] = h.pos[1], r.o[2] = h.pos[2];
+		r.d[0] = d[0], r.d[1] = d[1], r.d[2] = d[2];
+		rays[i] = r;
+	}
+}
+
+// ---------------------------------------------------------------------------------------------------
+cudaError_t march_launch(const MarchArgs &a, bool camera, cudaStream_t stream) {
+	cudaError_t e = cudaMemsetAsync(a.ticket, 0, sizeof(uint32_t), stream);
+	if (e != cudaSuccess || a.n == 0) return e;
+	const int sms = device_sm_count();
+	const uint64_t warps_needed = ((uint64_t)a.n + 32 * kRaysPerLane - 1) / (32 * kRaysPerLane);
+	const uint64_t blocks_needed = (warps_needed + kMarchTPB / 32 - 1) / (kMarchTPB / 32);
+	const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(blocks_needed, (uint64_t)sms * 12));
+	if (camera)
+		march_kernel<true><<<blocks, kMarchTPB, 0, stream>>>(a);
+	else
+		march_kernel<false><<<blocks, kMarchTPB, 0, stream>>>(a);
+	note_launch();
+	return cudaGetLastError();
+}
+
+cudaError_t bounce_launch(const svo_hit *hits, uint32_t n, uint64_t seed, svo_ray *rays, cudaStream_t stream) {
+	if (n == 0) return cudaSuccess;
+	const int sms = device_sm_count();
+	const uint32_t blocks = (uint32_t)std::min<uint64_t>(((uint64_t)n + 255) / 256, (uint64_t)sms * 8);
+	bounce_kernel<<<blocks, 256, 0, stream>>>(hits, n, seed, rays);
+	note_launch();
+	return cudaGetLastError();
+}
+
+} // namespace svo

@@ -1,0 +1,101 @@
+// svo_internal.h — declarations shared by the engine's translation units (not part of the ABI).
+#pragma once
+
+#include <algorithm>
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/svo.h"
+
+namespace svo {
+
+inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// Device status word bits (one word per call; the host turns them into svo_status codes).
+enum : uint32_t {
+	kStatusTimeout = 1u,  // a bounded look-back wait gave up
+	kStatusCapacity = 2u, // an output buffer or the 30-bit pointer range would overflow
+	kStatusMalformed = 4u // a march met a pointer outside the pool or a tree deeper than its level
+};
+
+void note_launch();      // counts kernel launches (svo_kernel_launches)
+int device_sm_count();   // SMs of the current device (cached per device)
+
+// ---------------------------------------------------------------- voxelize
+enum : uint32_t { kCtrTicketA = 0, kCtrTicketB = 1, kCtrStatus = 2, kCtrCount = 8 };
+enum : uint32_t { kStatusUnits = 8u }; // the unit arrays of the workspace are too small (caller retries)
+
+struct VoxWorkspace {
+	uint32_t n;
+	uint64_t unit_cap;             // units the unit arrays hold
+	uint64_t *small_off;           // [n+1] fragment offsets of small triangles
+	uint32_t *unit_off;            // [n+1] unit offsets of large triangles
+	unsigned long long *unit_frag; // [unit_cap+1] fragment offset of each unit inside the large region
+	unsigned long long *descs, *descs2, *descs3; // look-back descriptors of the three scans
+	size_t desc_bytes;
+	uint32_t *counters;            // tile tickets, status
+	unsigned long long *totals;    // [0] fragments, [1] units, [2] status (written by vox_launch_totals)
+};
+uint64_t vox_default_unit_cap(uint32_t n);
+size_t vox_workspace_bytes(uint32_t n, uint64_t unit_cap);
+size_t vox_workspace_layout(void *ws, uint32_t n, uint64_t unit_cap, VoxWorkspace &w);
+cudaError_t vox_launch_count(const svo_triangle *tris, uint32_t n, uint32_t level, const VoxWorkspace &w,
+                             cudaStream_t stream);
+cudaError_t vox_launch_totals(const VoxWorkspace &w, cudaStream_t stream);
+cudaError_t vox_launch_emit(const svo_triangle *tris, uint32_t n, uint32_t level, const VoxWorkspace &w,
+                            uint64_t *frags, uint64_t capacity, cudaStream_t stream);
+
+// ---------------------------------------------------------------- build
+struct LevelInfo {
+	uint32_t begin;         // first word of this depth's node range
+	uint32_t num;           // words in the range (8 per parent node)
+	uint32_t blocks_before; // child blocks allocated before this depth's alloc
+	uint32_t nodes;         // non-empty words at this depth (written by its alloc / finalize)
+};
+
+struct BuildState {
+	uint32_t status;
+	uint32_t range_words;
+	uint32_t leaves;
+	uint32_t pad;
+	uint32_t tiles[16];                 // tile tickets of each depth's alloc scan
+	LevelInfo lv[SVO_LEVEL_MAX + 2];    // lv[d] for depth d (1-based)
+};
+
+struct BuildWorkspace {
+	BuildState *state;
+	unsigned long long *descs;
+	size_t desc_count;
+	uint32_t *cache;           // per-fragment node index of the previous depth
+	unsigned long long *sums;  // leaf accumulators, 2 x u64 per leaf word
+	size_t sum_slots;
+	size_t total_bytes;
+};
+uint64_t build_pool_bound(uint32_t count, uint32_t level);
+size_t build_workspace_bytes(uint32_t count, uint32_t level, uint64_t capacity);
+void build_workspace_layout(void *ws, uint32_t count, uint32_t level, uint64_t capacity, BuildWorkspace &w);
+cudaError_t build_launch(const uint64_t *frags, uint32_t count, uint32_t level, uint32_t *pool, uint64_t capacity,
+                         const BuildWorkspace &w, cudaStream_t stream);
+// svo_build_info followed by the uint32 status word, written to device memory `out`.
+cudaError_t build_launch_export(const BuildWorkspace &w, uint32_t level, uint32_t count, void *out,
+                                cudaStream_t stream);
+
+// ---------------------------------------------------------------- march
+struct MarchArgs {
+	const uint32_t *pool;
+	uint32_t range;
+	uint32_t level;
+	const svo_ray *rays;
+	svo_camera cam;
+	uint32_t width, height;
+	uint32_t n;
+	svo_hit *hits;
+	uint32_t *ticket;             // device ray ticket (zeroed by march_launch)
+	unsigned long long *fetches;  // optional node-load total
+	uint32_t *status;             // device status word
+};
+cudaError_t march_launch(const MarchArgs &a, bool camera, cudaStream_t stream);
+cudaError_t bounce_launch(const svo_hit *hits, uint32_t n, uint64_t seed, svo_ray *rays, cudaStream_t stream);
+
+} // namespace svo

@@ -1,0 +1,440 @@
+// voxelize.cu — triangles -> voxel fragments (replaces the reference's raster voxelizer:
+// shader/voxelizer.{vert,geom,frag}, shader/voxelizer_conservative.geom, src/Voxelizer.cpp).
+//
+// Rule (identical to the oracle's restatement, see oracle/oracle.c):
+//   coordinates snapped to 1/256 voxel (round to nearest even), dominant-axis projection
+//   (shader/voxelizer.geom:27-36), a pixel is covered when each edge function's maximum over the
+//   closed pixel square is >= 0 (the half-pixel dilation of shader/voxelizer_conservative.geom:46-58)
+//   and the pixel lies in the triangle's pixel AABB (shader/voxelizer.frag:21-22); depth = floor of the
+//   plane depth at the pixel centre, clamped to [0,R-1] and the triangle's depth range
+//   (shader/voxelizer.frag:18-23); packing as shader/voxelizer.frag:40-42.
+//
+// GB300 design.  Coverage is computed per span (a row or column of the AABB, whichever makes fewer
+// spans) from three exact interval bounds: a span costs three corrected float divisions whatever its
+// length.  Triangle sizes span five orders of magnitude (a room wall covers 5e5 pixels, clutter ~10), so
+// work is balanced at two granularities:
+//   * small triangles (AABB <= kSmallArea pixels) are handled whole by one lane;
+//   * large triangles are cut into units = (span, piece of <= kPiece pixels); units are flat work items
+//     spread over the whole grid, so a wall becomes thousands of independent units.
+// Passes (all stream-ordered, sizes stay on the device):
+//   vox_classify_scan  per triangle: small -> fragment count, large -> unit count; both scanned with a
+//                      single-pass decoupled look-back (small fragment offsets, large unit offsets);
+//   vox_unit_scan      per unit: covered length, look-back scan -> fragment offset of every unit;
+//   vox_emit           small triangles by lane, then units by lane, at their offsets.
+// Fragment order is deterministic: small triangles in input order, then large triangles in input order
+// (spans, then pixels, in increasing order inside each).
+#include "common.cuh"
+#include "svo_internal.h"
+
+namespace svo {
+
+struct TriSetup {
+	int32_t valid, axis, cols;
+	int32_t u0, u1, v0, v1; // AABB in the span frame (u: inside a span, v: span index)
+	int32_t z0, z1;
+	int32_t gu[3], gv[3]; // edge k coefficients along U and V (sub-pixel units)
+	int32_t pu[3], pv[3]; // origin vertex of edge k in (U, V)
+	int64_t K, NU, NV, D; // depth numerator K - NU*u - NV*v over denominator D (> 0)
+	uint32_t rgb;
+	int32_t level;
+};
+
+SVO_DEV int32_t snap_coord(float p, float scale) {
+	float q = p > 0.0f ? p : 0.0f; // also maps NaN to 0
+	q = q < 1.0f ? q : 1.0f;
+	return __float2int_rn(q * scale);
+}
+
+SVO_DEV uint32_t mean_color(uint32_t c0, uint32_t c1, uint32_t c2) {
+	uint32_t out = 0;
+#pragma unroll
+	for (int ch = 0; ch < 3; ++ch) {
+		uint32_t s = ((c0 >> (8 * ch)) & 0xffu) + ((c1 >> (8 * ch)) & 0xffu) + ((c2 >> (8 * ch)) & 0xffu);
+		out |= (s / 3u) << (8 * ch);
+	}
+	return out;
+}
+
+SVO_DEV void tri_setup(const svo_triangle *__restrict__ tris, uint32_t t, uint32_t level, TriSetup &s) {
+	const float4 *p = reinterpret_cast<const float4 *>(tris + t);
+	float4 q0 = __ldg(p), q1 = __ldg(p + 1), q2 = __ldg(p + 2);
+	const float v[9] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x};
+	s.rgb = mean_color(__float_as_uint(q2.y), __float_as_uint(q2.z), __float_as_uint(q2.w));
+	s.level = (int32_t)level;
+	const int32_t R = 1 << level;
+	const float scale = (float)(256 << level);
+	int32_t X[3], Y[3], Z[3];
+#pragma unroll
+	for (int k = 0; k < 3; ++k) {
+		X[k] = snap_coord(v[3 * k], scale);
+		Y[k] = snap_coord(v[3 * k + 1], scale);
+		Z[k] = snap_coord(v[3 * k + 2], scale);
+	}
+	const int64_t e1x = X[1] - X[0], e1y = Y[1] - Y[0], e1z = Z[1] - Z[0];
+	const int64_t e2x = X[2] - X[0], e2y = Y[2] - Y[0], e2z = Z[2] - Z[0];
+	const int64_t nx = e1y * e2z - e1z * e2y, ny = e1z * e2x - e1x * e2z, nz = e1x * e2y - e1y * e2x;
+	s.valid = (nx | ny | nz) != 0;
+	if (!s.valid) return;
+	const int64_t ax = nx < 0 ? -nx : nx, ay = ny < 0 ? -ny : ny, az = nz < 0 ? -nz : nz;
+	const int axis = (ax > ay && ax > az) ? 0 : (ay > az ? 1 : 2);
+	s.axis = axis;
+	// projected (a, b, depth): yzx / zxy / xyz (shader/voxelizer.geom:15-19)
+	int32_t A[3], B[3], C[3];
+#pragma unroll
+	for (int k = 0; k < 3; ++k) {
+		A[k] = axis == 0 ? Y[k] : (axis == 1 ? Z[k] : X[k]);
+		B[k] = axis == 0 ? Z[k] : (axis == 1 ? X[k] : Y[k]);
+		C[k] = axis == 0 ? X[k] : (axis == 1 ? Y[k] : Z[k]);
+	}
+	int64_t na = axis == 0 ? ny : (axis == 1 ? nz : nx);
+	int64_t nb = axis == 0 ? nz : (axis == 1 ? nx : ny);
+	int64_t nc = axis == 0 ? nx : (axis == 1 ? ny : nz);
+	if (nc < 0) { // counter-clockwise in (a, b): swap vertices 1 and 2
+		int32_t t0 = A[1], t1 = B[1], t2 = C[1];
+		A[1] = A[2], B[1] = B[2], C[1] = C[2];
+		A[2] = t0, B[2] = t1, C[2] = t2;
+		na = -na, nb = -nb, nc = -nc;
+	}
+	const int32_t amin = min(A[0], min(A[1], A[2])), amax = max(A[0], max(A[1], A[2]));
+	const int32_t bmin = min(B[0], min(B[1], B[2])), bmax = max(B[0], max(B[1], B[2]));
+	const int32_t cmin = min(C[0], min(C[1], C[2])), cmax = max(C[0], max(C[1], C[2]));
+	const int32_t i0 = clamp_i32(amin >> 8, 0, R - 1), i1 = clamp_i32(amax >> 8, 0, R - 1);
+	const int32_t j0 = clamp_i32(bmin >> 8, 0, R - 1), j1 = clamp_i32(bmax >> 8, 0, R - 1);
+	s.z0 = clamp_i32(cmin >> 8, 0, R - 1);
+	s.z1 = clamp_i32(cmax >> 8, 0, R - 1);
+	const int cols = (j1 - j0) > (i1 - i0);
+	s.cols = cols;
+	s.u0 = cols ? j0 : i0;
+	s.u1 = cols ? j1 : i1;
+	s.v0 = cols ? i0 : j0;
+	s.v1 = cols ? i1 : j1;
+#pragma unroll
+	for (int k = 0; k < 3; ++k) {
+		const int q = (k + 1) % 3;
+		const int32_t ea = -(B[q] - B[k]), eb = A[q] - A[k];
+		s.gu[k] = cols ? eb : ea;
+		s.gv[k] = cols ? ea : eb;
+		s.pu[k] = cols ? B[k] : A[k];
+		s.pv[k] = cols ? A[k] : B[k];
+	}
+	// depth at the centre of pixel (i, j): floor((C0*nc - na*(256i+128-A0) - nb*(256j+128-B0)) / (256*nc))
+	const int64_t nu = cols ? nb : na, nv = cols ? na : nb;
+	const int64_t cu = cols ? B[0] : A[0], cv = cols ? A[0] : B[0];
+	s.K = (int64_t)C[0] * nc - nu * (128 - cu) - nv * (128 - cv);
+	s.NU = 256 * nu;
+	s.NV = 256 * nv;
+	s.D = 256 * nc;
+}
+
+// Covered interval [lo, hi] of span v (empty when lo > hi).
+SVO_DEV void span_interval(const TriSetup &s, int32_t v, int32_t &lo, int32_t &hi) {
+	const int32_t R = 1 << s.level;
+	lo = s.u0;
+	hi = s.u1;
+#pragma unroll
+	for (int k = 0; k < 3; ++k) {
+		const int64_t g = s.gu[k], h = s.gv[k];
+		const int64_t Ck = g * ((g > 0 ? 256 : 0) - s.pu[k]) + h * (256 * (int64_t)v + (h > 0 ? 256 : 0) - s.pv[k]);
+		// 256 * g * u + Ck >= 0
+		if (g > 0) {
+			// ceil(-Ck / (256 g)) = -floor(Ck / (256 g)); exact where the bound falls in [0, R-1]
+			const int64_t b = -floor_div_window(Ck, 256 * g, -(R - 1), 0);
+			lo = max(lo, clamp_i32(b, -1, R));
+		} else if (g < 0) {
+			const int64_t b = floor_div_window(Ck, -256 * g, 0, R - 1);
+			hi = min(hi, clamp_i32(b, -1, R));
+		} else if (Ck < 0) {
+			hi = lo - 1;
+		}
+	}
+}
+
+SVO_DEV uint64_t make_fragment(const TriSetup &s, int32_t u, int32_t v) {
+	const int32_t R = 1 << s.level;
+	const int64_t num = s.K - s.NU * u - s.NV * v;
+	int32_t z = clamp_i32(floor_div_window(num, s.D, 0, R - 1), 0, R - 1);
+	z = z < s.z0 ? s.z0 : (z > s.z1 ? s.z1 : z);
+	const uint32_t i = (uint32_t)(s.cols ? v : u), j = (uint32_t)(s.cols ? u : v), zz = (uint32_t)z;
+	// un-swizzle (shader/voxelizer.frag:24): axis 0 -> u.zxy, 1 -> u.yzx, 2 -> u.xyz
+	const uint32_t vx = s.axis == 0 ? zz : (s.axis == 1 ? j : i);
+	const uint32_t vy = s.axis == 0 ? i : (s.axis == 1 ? zz : j);
+	const uint32_t vz = s.axis == 0 ? j : (s.axis == 1 ? i : zz);
+	const uint32_t fx = vx | (vy << 12) | ((vz & 0xffu) << 24);
+	const uint32_t fy = ((vz >> 8) << 28) | (s.rgb & 0xffffffu);
+	return (uint64_t)fx | ((uint64_t)fy << 32);
+}
+
+constexpr int kSmallArea = 64;  // AABB pixels up to which one lane handles the whole triangle
+constexpr int kPiece = 256;     // pixels of a span one unit covers at most
+
+SVO_DEV bool is_large(const TriSetup &s) {
+	return s.valid && (int64_t)(s.u1 - s.u0 + 1) * (s.v1 - s.v0 + 1) > kSmallArea;
+}
+
+SVO_DEV uint32_t pieces_per_span(const TriSetup &s) { return (uint32_t)((s.u1 - s.u0) / kPiece + 1); }
+
+SVO_DEV uint32_t unit_count(const TriSetup &s) { return (uint32_t)(s.v1 - s.v0 + 1) * pieces_per_span(s); }
+
+SVO_DEV uint32_t count_serial(const TriSetup &s) {
+	uint32_t n = 0;
+	for (int32_t v = s.v0; v <= s.v1; ++v) {
+		int32_t lo, hi;
+		span_interval(s, v, lo, hi);
+		n += hi >= lo ? (uint32_t)(hi - lo + 1) : 0u;
+	}
+	return n;
+}
+
+SVO_DEV void emit_serial(const TriSetup &s, uint64_t *__restrict__ out) {
+	uint32_t k = 0;
+	for (int32_t v = s.v0; v <= s.v1; ++v) {
+		int32_t lo, hi;
+		span_interval(s, v, lo, hi);
+		for (int32_t u = lo; u <= hi; ++u) out[k++] = make_fragment(s, u, v);
+	}
+}
+
+// Unit `local` of a large triangle: its span v and the covered pixel interval [lo, hi] inside its piece.
+SVO_DEV void unit_interval(const TriSetup &s, uint32_t local, int32_t &v, int32_t &lo, int32_t &hi) {
+	const uint32_t pps = pieces_per_span(s);
+	v = s.v0 + (int32_t)(local / pps);
+	const int32_t p0 = s.u0 + (int32_t)(local % pps) * kPiece;
+	span_interval(s, v, lo, hi);
+	lo = max(lo, p0);
+	hi = min(hi, p0 + kPiece - 1);
+}
+
+// Index of the last entry of the non-decreasing array a[0..n] that is <= x (a[0] = 0 <= x).
+SVO_DEV uint32_t upper_index(const uint32_t *__restrict__ a, uint32_t n, uint32_t x) {
+	uint32_t lo = 0, hi = n; // invariant a[lo] <= x < a[hi] (a[n] > x)
+	while (hi - lo > 1) {
+		const uint32_t mid = (lo + hi) >> 1;
+		if (__ldg(a + mid) <= x)
+			lo = mid;
+		else
+			hi = mid;
+	}
+	return lo;
+}
+
+// ---------------------------------------------------------------------------------------------------
+constexpr int kTPB = 256;
+constexpr int kIPT = 2;
+constexpr int kTile = kTPB * kIPT;
+
+// Per triangle: small fragment count and large unit count, both exclusive-scanned.
+//   small_off[t] = fragments of small triangles before t; small_off[n] = small total
+//   unit_off[t]  = units of large triangles before t;    unit_off[n]  = unit total
+__global__ void __launch_bounds__(kTPB) vox_classify_scan(const svo_triangle *__restrict__ tris, uint32_t n,
+                                                          uint32_t level, VoxWorkspace w) {
+	__shared__ uint32_t s_tile;
+	__shared__ uint32_t s_cnt[kTile];
+	__shared__ uint32_t s_units[kTile];
+	__shared__ unsigned long long s_warp[kTPB / 32 + 1];
+	__shared__ unsigned long long s_prefix[2];
+	if (threadIdx.x == 0) s_tile = atomicAdd(&w.counters[kCtrTicketA], 1u);
+	__syncthreads();
+	const uint32_t tile = s_tile;
+	const uint64_t base = (uint64_t)tile * kTile;
+#pragma unroll 1
+	for (int k = 0; k < kIPT; ++k) {
+		const uint64_t t = base + (uint64_t)k * kTPB + threadIdx.x;
+		TriSetup s;
+		s.valid = 0;
+		if (t < n) tri_setup(tris, (uint32_t)t, level, s);
+		const bool large = is_large(s);
+		s_cnt[k * kTPB + threadIdx.x] = (s.valid && !large) ? count_serial(s) : 0u;
+		s_units[k * kTPB + threadIdx.x] = large ? unit_count(s) : 0u;
+	}
+	__syncthreads();
+	unsigned long long lc = 0, lu = 0;
+#pragma unroll
+	for (int k = 0; k < kIPT; ++k) {
+		lc += s_cnt[threadIdx.x * kIPT + k];
+		lu += s_units[threadIdx.x * kIPT + k];
+	}
+	unsigned long long tc, tu;
+	const unsigned long long ec = block_exclusive_sum<unsigned long long, kTPB>(lc, s_warp, tc);
+	const unsigned long long eu = block_exclusive_sum<unsigned long long, kTPB>(lu, s_warp, tu);
+	if (threadIdx.x == 0) {
+		s_prefix[0] = tile_lookback(w.descs, tile, 1u, tc, &w.counters[kCtrStatus]);
+		s_prefix[1] = tile_lookback(w.descs2, tile, 1u, tu, &w.counters[kCtrStatus]);
+	}
+	__syncthreads();
+	unsigned long long rc = s_prefix[0] + ec, ru = s_prefix[1] + eu;
+#pragma unroll
+	for (int k = 0; k < kIPT; ++k) {
+		const uint64_t t = base + (uint64_t)threadIdx.x * kIPT + k;
+		if (t < n) {
+			w.small_off[t] = rc;
+			w.unit_off[t] = (uint32_t)ru;
+		}
+		rc += s_cnt[threadIdx.x * kIPT + k];
+		ru += s_units[threadIdx.x * kIPT + k];
+	}
+	if (base + kTile >= n && base <= n && threadIdx.x == 0) {
+		w.small_off[n] = s_prefix[0] + tc;
+		const unsigned long long units = s_prefix[1] + tu;
+		w.unit_off[n] = units > 0xffffffffull ? 0xffffffffu : (uint32_t)units;
+		if (units > w.unit_cap) atomicOr(&w.counters[kCtrStatus], kStatusUnits);
+	}
+}
+
+// Per unit of a large triangle: covered length, scanned into unit_frag[u] (offset inside the large
+// region); unit_frag[units] = large total.  Persistent grid: tiles claimed in order by ticket.
+__global__ void __launch_bounds__(kTPB) vox_unit_scan(const svo_triangle *__restrict__ tris, uint32_t n,
+                                                      uint32_t level, VoxWorkspace w) {
+	__shared__ uint32_t s_tile;
+	__shared__ unsigned long long s_warp[kTPB / 32 + 1];
+	__shared__ unsigned long long s_prefix;
+	const uint32_t units = w.unit_off[n];
+	if (units > w.unit_cap) return; // the host re-runs with a workspace sized for `units`
+	const uint32_t ntiles = (units + kTile - 1) / kTile;
+	for (;;) {
+		if (threadIdx.x == 0) s_tile = atomicAdd(&w.counters[kCtrTicketB], 1u);
+		__syncthreads();
+		const uint32_t tile = s_tile;
+		__syncthreads();
+		if (tile >= ntiles) break;
+		uint32_t len[kIPT];
+		unsigned long long local = 0;
+#pragma unroll
+		for (int k = 0; k < kIPT; ++k) {
+			const uint32_t u = tile * kTile + threadIdx.x * kIPT + k;
+			len[k] = 0;
+			if (u < units) {
+				const uint32_t t = upper_index(w.unit_off, n, u);
+				TriSetup s;
+				tri_setup(tris, t, level, s);
+				int32_t v, lo, hi;
+				unit_interval(s, u - w.unit_off[t], v, lo, hi);
+				len[k] = hi >= lo ? (uint32_t)(hi - lo + 1) : 0u;
+			}
+			local += len[k];
+		}
+		unsigned long long total;
+		const unsigned long long excl = block_exclusive_sum<unsigned long long, kTPB>(local, s_warp, total);
+		if (threadIdx.x == 0) s_prefix = tile_lookback(w.descs3, tile, 1u, total, &w.counters[kCtrStatus]);
+		__syncthreads();
+		unsigned long long run = s_prefix + excl;
+#pragma unroll
+		for (int k = 0; k < kIPT; ++k) {
+			const uint32_t u = tile * kTile + threadIdx.x * kIPT + k;
+			if (u < units) w.unit_frag[u] = run;
+			run += len[k];
+		}
+		if (tile == ntiles - 1 && threadIdx.x == 0) w.unit_frag[units] = s_prefix + total;
+		__syncthreads();
+	}
+	if (ntiles == 0 && blockIdx.x == 0 && threadIdx.x == 0) w.unit_frag[0] = 0;
+}
+
+// Emission: threads [0, n) write small triangles, threads [n, n + units) write units.
+__global__ void __launch_bounds__(kTPB) vox_emit(const svo_triangle *__restrict__ tris, uint32_t n, uint32_t level,
+                                                 VoxWorkspace w, uint64_t *__restrict__ frags, uint64_t capacity) {
+	const uint32_t units = w.unit_off[n];
+	const uint64_t small_total = w.small_off[n];
+	const uint64_t items = (uint64_t)n + (units <= w.unit_cap ? units : 0u);
+	for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < items; i += (uint64_t)gridDim.x * blockDim.x) {
+		if (i < n) {
+			const uint64_t off = w.small_off[i], end = w.small_off[i + 1];
+			if (end == off || end > capacity) continue;
+			TriSetup s;
+			tri_setup(tris, (uint32_t)i, level, s);
+			if (s.valid && !is_large(s)) emit_serial(s, frags + off);
+		} else {
+			const uint32_t u = (uint32_t)(i - n);
+			const uint64_t off = small_total + w.unit_frag[u], end = small_total + w.unit_frag[u + 1];
+			if (end == off || end > capacity) continue;
+			const uint32_t t = upper_index(w.unit_off, n, u);
+			TriSetup s;
+			tri_setup(tris, t, level, s);
+			int32_t v, lo, hi;
+			unit_interval(s, u - w.unit_off[t], v, lo, hi);
+			uint64_t *out = frags + off;
+			for (int32_t x = lo; x <= hi; ++x) *out++ = make_fragment(s, x, v);
+		}
+	}
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Workspace: small_off[n+1] u64 | unit_off[n+1] u32 | unit_frag[unit_cap+1] u64 | 3 descriptor arrays |
+// counters.  unit_cap is a first guess; a larger unit total makes the count report it and the caller
+// retries with vox_workspace_bytes(n, units).
+uint64_t vox_default_unit_cap(uint32_t n) { return 2ull * n + 65536; }
+
+static size_t tiles_for(uint64_t items) { return (size_t)((items + kTile - 1) / kTile + 1); }
+
+size_t vox_workspace_bytes(uint32_t n, uint64_t unit_cap) {
+	VoxWorkspace w;
+	return vox_workspace_layout(nullptr, n, unit_cap, w);
+}
+
+size_t vox_workspace_layout(void *ws, uint32_t n, uint64_t unit_cap, VoxWorkspace &w) {
+	char *p = (char *)ws;
+	size_t off = 0;
+	auto take = [&](size_t bytes) {
+		char *q = p + off;
+		off += align_up(bytes, 256);
+		return q;
+	};
+	w.n = n;
+	w.unit_cap = unit_cap;
+	w.small_off = (uint64_t *)take(sizeof(uint64_t) * ((size_t)n + 1));
+	w.unit_off = (uint32_t *)take(sizeof(uint32_t) * ((size_t)n + 1));
+	w.unit_frag = (unsigned long long *)take(sizeof(unsigned long long) * (size_t)(unit_cap + 1));
+	const size_t t1 = tiles_for(n), t3 = tiles_for(unit_cap);
+	w.descs = (unsigned long long *)(p + off);
+	w.desc_bytes = align_up((2 * t1 + t3) * sizeof(unsigned long long), 256);
+	w.descs2 = w.descs + t1;
+	w.descs3 = w.descs + 2 * t1;
+	off += w.desc_bytes;
+	w.counters = (uint32_t *)take(kCtrCount * sizeof(uint32_t));
+	w.totals = (unsigned long long *)take(4 * sizeof(unsigned long long));
+	return off;
+}
+
+cudaError_t vox_launch_count(const svo_triangle *tris, uint32_t n, uint32_t level, const VoxWorkspace &w,
+                             cudaStream_t stream) {
+	cudaError_t e = cudaMemsetAsync(w.descs, 0, w.desc_bytes, stream);
+	if (e != cudaSuccess) return e;
+	e = cudaMemsetAsync(w.counters, 0, kCtrCount * sizeof(uint32_t), stream);
+	if (e != cudaSuccess) return e;
+	if (n == 0) {
+		e = cudaMemsetAsync(w.small_off, 0, sizeof(uint64_t), stream);
+		if (e == cudaSuccess) e = cudaMemsetAsync(w.unit_off, 0, sizeof(uint32_t), stream);
+		if (e == cudaSuccess) e = cudaMemsetAsync(w.unit_frag, 0, sizeof(unsigned long long), stream);
+		return e;
+	}
+	vox_classify_scan<<<(n + kTile - 1) / kTile, kTPB, 0, stream>>>(tris, n, level, w);
+	note_launch();
+	const int sms = device_sm_count();
+	vox_unit_scan<<<(uint32_t)sms * 4, kTPB, 0, stream>>>(tris, n, level, w);
+	note_launch();
+	return cudaGetLastError();
+}
+
+cudaError_t vox_launch_emit(const svo_triangle *tris, uint32_t n, uint32_t level, const VoxWorkspace &w,
+                            uint64_t *frags, uint64_t capacity, cudaStream_t stream) {
+	if (n == 0) return cudaSuccess;
+	const int sms = device_sm_count();
+	vox_emit<<<(uint32_t)sms * 16, kTPB, 0, stream>>>(tris, n, level, w, frags, capacity);
+	note_launch();
+	return cudaGetLastError();
+}
+
+__global__ void vox_totals(VoxWorkspace w) {
+	const uint32_t units = w.unit_off[w.n];
+	const uint32_t status = w.counters[kCtrStatus];
+	w.totals[0] = w.small_off[w.n] + ((status & kStatusUnits) ? 0ull : w.unit_frag[units]);
+	w.totals[1] = units;
+	w.totals[2] = status;
+}
+
+cudaError_t vox_launch_totals(const VoxWorkspace &w, cudaStream_t stream) {
+	vox_totals<<<1, 1, 0, stream>>>(w);
+	note_launch();
+	return cudaGetLastError();
+}
+
+} // namespace svo

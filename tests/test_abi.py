@@ -1,0 +1,62 @@
+"""The C ABI library: it loads, exports every function include/svo.h declares, and its host-side
+argument checks and helpers behave (no kernel runs here)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from sparsevoxeloctree_gb300 import _lib
+
+
+@pytest.fixture(scope="module")
+def lib():
+    return _lib.load()
+
+
+def test_exports_every_declared_symbol(lib):
+    names = _lib.declared_symbols()
+    assert len(names) >= 20
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_version_and_counters(lib):
+    assert b"sm_103a" in lib.svo_version()
+    assert lib.svo_kernel_launches() >= 0
+
+
+def test_invalid_arguments_are_rejected_before_any_launch(lib):
+    before = lib.svo_kernel_launches()
+    out = _lib.Fraglist()
+    assert lib.svo_voxelize(None, 0, 0, ctypes.byref(out), None) == _lib.SVO_ERR_INVALID
+    assert b"level" in lib.svo_last_error()
+    assert lib.svo_voxelize(None, 0, 13, ctypes.byref(out), None) == _lib.SVO_ERR_INVALID
+    assert lib.svo_voxelize(None, 5, 4, ctypes.byref(out), None) == _lib.SVO_ERR_INVALID
+    assert lib.svo_voxelize(ctypes.c_void_p(8), 5, 4, ctypes.byref(out), None) == _lib.SVO_ERR_INVALID  # misaligned
+    oc = _lib.OctreeC()
+    assert lib.svo_build(None, 0, 0, ctypes.byref(oc), None, None) == _lib.SVO_ERR_INVALID
+    assert lib.svo_build(ctypes.c_void_p(4), 3, 5, ctypes.byref(oc), None, None) == _lib.SVO_ERR_INVALID
+    assert lib.svo_raycast(ctypes.byref(oc), None, 0, None, None, None) == _lib.SVO_ERR_INVALID  # null octree
+    oc.words, oc.level, oc.range_words = 256, 5, 12  # range not a multiple of 8
+    assert lib.svo_raycast(ctypes.byref(oc), None, 0, None, None, None) == _lib.SVO_ERR_INVALID
+    assert lib.svo_build_into(ctypes.c_void_p(256), 1, 3, ctypes.c_void_p(256), 4, ctypes.c_void_p(256),
+                              ctypes.c_void_p(256), None) == _lib.SVO_ERR_CAPACITY
+    assert lib.svo_kernel_launches() == before
+
+
+def test_pool_bound_and_workspace_sizes(lib):
+    import oracle
+    for count, level in [(0, 1), (1, 1), (5, 3), (1000, 8), (38_000_000, 10), (150_000_000, 12)]:
+        assert lib.svo_build_pool_bound(count, level) == oracle.pool_bound(count, level)
+    assert lib.svo_build_workspace_size(1000, 8, lib.svo_build_pool_bound(1000, 8)) > 4000
+    assert lib.svo_voxelize_workspace_size(1000) > 8 * 1000
+
+
+def test_camera_from_angles_matches_python(lib):
+    from sparsevoxeloctree_gb300 import scenes
+    pos = (ctypes.c_float * 3)(1.5, 1.4, 1.3)
+    cam = _lib.CameraC()
+    lib.svo_camera_from_angles(pos, 0.3, -0.2, np.pi / 3, 1.5, ctypes.byref(cam))
+    ref = scenes.camera_from_angles((1.5, 1.4, 1.3), 0.3, -0.2, np.pi / 3, 1.5)
+    for k in ("pos", "look", "side", "up"):
+        assert np.allclose(np.array(getattr(cam, k)[:3]), ref[k][:3], atol=1e-6)

@@ -1,0 +1,245 @@
+"""CUDA engine vs the CPU oracle on the same seeded inputs, through the C ABI.
+
+Bar: fragments (canonical order) and octrees bit-exact; ray hits bit-exact in every field (the march is
+compiled without FMA contraction and follows the same float operations as the oracle), which is
+stricter than the >= 99.99% voxel-id / |dt| <= 1e-5 tolerance the engine promises.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from sparsevoxeloctree_gb300 import scenes
+from sparsevoxeloctree_gb300.formats import HIT_DTYPE, RAY_DTYPE, TRIANGLE_DTYPE, rays_from_arrays
+
+pytestmark = pytest.mark.gpu
+
+T_TOL = 1e-5  # |dt| bound, octree space (extent 1)
+
+
+def _api():
+    from sparsevoxeloctree_gb300 import api
+    return api
+
+
+def gpu_voxelize(tris, level):
+    api = _api()
+    v = api.Voxelizer.Create(np.asarray(tris, TRIANGLE_DTYPE), level)
+    return v.GetVoxelFragmentList().cpu().numpy().view(np.uint64)
+
+
+def gpu_build(frags, level):
+    import torch
+    api = _api()
+    t = torch.from_numpy(np.ascontiguousarray(frags).view(np.int64)).cuda()
+    o = api.Octree.FromFragments(t, level)
+    return o, o.words().cpu().numpy().view(np.uint32)
+
+
+def gpu_trace(octree, rays):
+    api = _api()
+    hits = api.OctreeTracer.Create(octree).Trace(api.to_device(np.asarray(rays, RAY_DTYPE)))
+    return api.hits_numpy(hits)
+
+
+def assert_same_fragments(got, ref):
+    """Multiset equality of fragment lists (the engine's order is deterministic but differs from the
+    oracle's triangle order: small triangles first, then large ones)."""
+    assert len(got) == len(ref)
+    assert np.array_equal(np.sort(got), np.sort(ref))
+
+
+def assert_hits_equal(h_gpu, h_ref):
+    for f in HIT_DTYPE.names:
+        a, b = h_gpu[f], h_ref[f]
+        if not np.array_equal(a, b):
+            bad = np.nonzero((a != b).reshape(len(a), -1).any(axis=1))[0]
+            raise AssertionError(f"hit field {f} differs on {len(bad)} rays, first {bad[:5]}: "
+                                 f"{h_gpu[bad[:3]]} vs {h_ref[bad[:3]]}")
+
+
+def single(v9, rgb=(0x112233, 0x445566, 0x778899)):
+    t = np.zeros(1, TRIANGLE_DTYPE)
+    t["v"] = np.asarray(v9, np.float32).reshape(1, 9)
+    t["rgb"] = rgb
+    return t
+
+
+# ------------------------------------------------------------------------------------------- voxelize
+def test_voxelize_plain_256_bit_exact(cuda):
+    s = scenes.plain_256()
+    ref = oracle.voxelize(s.tris, s.level)
+    got = gpu_voxelize(s.tris, s.level)
+    assert_same_fragments(got, ref)
+    again = gpu_voxelize(s.tris, s.level)
+    assert np.array_equal(again, got)  # run-to-run identical, order included
+
+
+@pytest.mark.parametrize("level", [1, 2, 5, 8, 12])
+def test_voxelize_random_triangles(cuda, level):
+    g = np.random.default_rng(level)
+    n = 3000
+    c = g.uniform(0, 1, size=(n, 1, 3))
+    size = np.exp(g.uniform(np.log(1e-4), np.log(0.7), size=(n, 1, 1)))
+    verts = np.clip(c + g.normal(size=(n, 3, 3)) * size, -0.05, 1.05)
+    tris = np.zeros(n, TRIANGLE_DTYPE)
+    tris["v"] = verts.reshape(n, 9).astype(np.float32)
+    tris["rgb"] = g.integers(0, 1 << 24, size=(n, 3))
+    ref = oracle.voxelize(tris, level)
+    got = gpu_voxelize(tris, level)
+    assert_same_fragments(got, ref)
+
+
+def test_voxelize_edge_cases(cuda):
+    tris = np.concatenate([
+        single([0.1, 0.1, 0.1, 0.1, 0.1, 0.1, 0.1, 0.1, 0.1]),          # a point: degenerate
+        single([0.1, 0.1, 0.1, 0.5, 0.5, 0.5, 0.9, 0.9, 0.9]),          # collinear: degenerate
+        single([0.0, 0.0, 0.5, 1.0, 0.0, 0.5, 0.0, 1.0, 0.5]),          # half the z = 0.5 plane
+        single([0.0, 0.0, 0.0, 1.0, 1.0, 1.0, 1.0, 0.0, 0.0]),          # 45 degree diagonal
+        single([np.nan, 0.2, 0.2, 0.3, np.inf, 0.2, 0.2, 0.3, -1.0]),  # non-finite / outside
+        single([0.25, 0.25, 0.25, 0.75, 0.25, 0.25, 0.25, 0.75, 0.25]),  # on voxel boundaries
+        single([0.5, 0.5, 0.5, 0.5 + 1e-7, 0.5, 0.5, 0.5, 0.5 + 1e-7, 0.5]),  # sub-voxel sliver
+    ])
+    for level in (1, 4, 10, 12):
+        assert_same_fragments(gpu_voxelize(tris, level), oracle.voxelize(tris, level))
+
+
+def test_voxelize_empty(cuda):
+    got = gpu_voxelize(np.zeros(0, TRIANGLE_DTYPE), 6)
+    assert len(got) == 0
+
+
+def test_voxelize_golden_vs_reference_shaders(cuda, golden_dir):
+    """Reference geometry+fragment shaders (conservative variant, fixture) vs the engine: equal except
+    fragments whose pixel-centre depth lies within float rounding of a voxel boundary (one voxel off)."""
+    z = np.load(f"{golden_dir}/golden_vox.npz")
+    tris = z["tris"].view(TRIANGLE_DTYPE)
+    level = int(z["level"])
+    got = gpu_voxelize(tris, level)
+    assert_same_fragments(got, oracle.voxelize(tris, level))
+    a, b = set(got.tolist()), set(z["frags"].tolist())
+    assert len(a ^ b) <= 0.002 * len(b)
+
+
+# ------------------------------------------------------------------------------------------- build
+@pytest.mark.parametrize("level", [1, 2, 3, 6, 9])
+def test_build_random_fragments(cuda, level):
+    g = np.random.default_rng(100 + level)
+    R = 1 << level
+    n = 20000
+    xyz = g.integers(0, R, size=(n, 3))
+    if level > 3:  # cluster half of them so leaves merge many fragments (count saturates at 63)
+        xyz[: n // 2] = g.integers(0, min(R, 4), size=(n // 2, 3))
+    from sparsevoxeloctree_gb300.formats import pack_fragments
+    frags = pack_fragments(xyz[:, 0], xyz[:, 1], xyz[:, 2], g.integers(0, 1 << 24, size=n))
+    ref = oracle.build_octree(frags, level)
+    _, got = gpu_build(frags, level)
+    assert np.array_equal(got, ref)
+
+
+def test_build_plain_256_bit_exact(cuda):
+    s = scenes.plain_256()
+    frags = oracle.voxelize(s.tris, s.level)
+    ref, ref_nodes = oracle.build_octree(frags, s.level, return_level_nodes=True)
+    o, got = gpu_build(frags, s.level)
+    assert np.array_equal(got, ref)
+    assert o.info["level_nodes"] == ref_nodes.tolist()
+
+
+def test_build_golden_structure(cuda, golden_dir):
+    """The reference's own tag/alloc shaders (fixture): same structure; leaf colours agree wherever the
+    running mean and the integer mean coincide (one or two fragments per leaf)."""
+    z = np.load(f"{golden_dir}/golden_build.npz")
+    frags, level, ref_pool = z["frags"], int(z["level"]), z["pool"]
+    _, got = gpu_build(frags, level)
+    assert len(got) == len(ref_pool)
+    assert np.array_equal(got & 0xC0000000, ref_pool & 0xC0000000)
+    interior = (ref_pool & 0xC0000000) == 0x80000000
+    assert np.array_equal(got[interior], ref_pool[interior])
+    leaf = (ref_pool >> 30) == 3
+    cnt = (ref_pool >> 24) & 0x3F
+    small = leaf & (cnt <= 2)
+    assert np.array_equal(got[small], ref_pool[small])
+    assert np.array_equal((got[leaf] >> 24) & 0x3F, cnt[leaf])
+
+
+def test_build_empty(cuda):
+    _, got = gpu_build(np.zeros(0, np.uint64), 7)
+    assert len(got) == 8 and not got.any()
+
+
+# ------------------------------------------------------------------------------------------- march
+def test_march_golden_vs_reference_shader(cuda, golden_dir):
+    zb = np.load(f"{golden_dir}/golden_build.npz")
+    zm = np.load(f"{golden_dir}/golden_march.npz")
+    level, pool = int(zb["level"]), zb["pool"]
+    import torch
+    api = _api()
+    o = api.Octree()
+    o.m_buffer = torch.from_numpy(pool.view(np.int32)).cuda()
+    o.m_range, o.m_level = len(pool) * 4, level
+    rays = rays_from_arrays(zm["o"], zm["d"])
+    h = gpu_trace(o, rays)
+    assert np.array_equal(h, oracle.raycast(pool, level, rays))
+    hit = (h["flags"] & 1).astype(np.uint32)
+    assert np.array_equal(hit, zm["hit"])
+    assert np.array_equal(h["iter"], zm["iter"])
+    assert np.array_equal(h["pos"], zm["pos"])
+    col = np.stack([(h["node"] >> (8 * k)) & 255 for k in range(3)], 1).astype(np.float32) / 255.0
+    m = hit == 1
+    assert np.array_equal(col[m], zm["color"][m])
+    nrm = np.zeros((len(h), 3), np.float32)
+    nrm[np.arange(len(h)), (h["flags"] >> 1) & 3] = np.where(h["flags"] & 8, -1.0, 1.0)
+    assert np.array_equal(nrm, zm["normal"])
+
+
+def test_march_camera_and_bounce_plain_256(cuda):
+    s = scenes.plain_256()
+    frags = oracle.voxelize(s.tris, s.level)
+    pool = oracle.build_octree(frags, s.level)
+    o, _ = gpu_build(frags, s.level)
+    api = _api()
+    tracer = api.OctreeTracer.Create(o, s.camera, s.width, s.height)
+    h_gpu = api.hits_numpy(tracer.CmdDrawPipeline())
+    rays = oracle.camera_rays(s.camera, s.width, s.height)
+    h_ref = oracle.raycast(pool, s.level, rays)
+    assert_hits_equal(h_gpu, h_ref)
+    # one diffuse bounce per hit
+    b_gpu = api.OctreeTracer.Bounce(api.to_device(h_gpu), seed=77)
+    b_ref = oracle.bounce_rays(h_ref, 77)
+    assert np.array_equal(api.from_device(b_gpu, RAY_DTYPE), b_ref)
+    h2 = api.hits_numpy(tracer.Trace(b_gpu))
+    assert_hits_equal(h2, oracle.raycast(pool, s.level, b_ref))
+
+
+def test_march_random_rays_many_levels(cuda):
+    g = np.random.default_rng(3)
+    for level in (1, 3, 7, 10):
+        R = 1 << level
+        n = 30000
+        from sparsevoxeloctree_gb300.formats import pack_fragments
+        xyz = g.integers(0, R, size=(n, 3))
+        frags = pack_fragments(xyz[:, 0], xyz[:, 1], xyz[:, 2], g.integers(0, 1 << 24, size=n))
+        pool = oracle.build_octree(frags, level)
+        o, _ = gpu_build(frags, level)
+        o1, d1 = scenes.random_rays(g, 20000)
+        o2, d2 = scenes.random_rays(g, 20000, inside=True)
+        rays = rays_from_arrays(np.concatenate([o1, o2]), np.concatenate([d1, d2]))
+        rays["d"][:6] = [[1, 0, 0], [0, 1, 0], [0, 0, -1], [0, 0, 0], [1e-30, 0, 1], [-1, 1e-20, 0]]
+        assert_hits_equal(gpu_trace(o, rays), oracle.raycast(pool, level, rays))
+
+
+def test_camera_golden(cuda, golden_dir):
+    """Primary-ray directions: oracle == reference Camera_GenRay (fixture); the GPU march over camera
+    rays equals the march over the oracle's explicit rays."""
+    z = np.load(f"{golden_dir}/golden_camera.npz")
+    from sparsevoxeloctree_gb300.formats import CAMERA_DTYPE
+    cam = z["cam"].view(CAMERA_DTYPE)[0]
+    w, h = int(z["width"]), int(z["height"])
+    rays = oracle.camera_rays(cam, w, h)
+    assert np.array_equal(rays["d"], z["dirs"])
+    s = scenes.plain_256()
+    frags = oracle.voxelize(s.tris, s.level)
+    o, pool = gpu_build(frags, s.level)
+    api = _api()
+    h_cam = api.hits_numpy(api.OctreeTracer.Create(o, cam, w, h).CmdDrawPipeline())
+    assert_hits_equal(h_cam, oracle.raycast(pool, s.level, rays))
