@@ -1,0 +1,386 @@
+#!/usr/bin/env python3
+"""Benchmark: the plain sparse-voxel-octree hot path (voxelize -> build -> primary-ray march) on GB300.
+
+One step = one pass of the whole path over the 2^10 room workload (262,144 triangles, 1920x1080 primary
+rays; a seeded synthetic scene standing in for the reference's OBJ scenes): count + emit the fragment
+list, build the octree level by level, march every pixel's primary ray.  `value` is the device time of a
+step with inputs already in HBM (lower is better); `e2e` is the same step through the C ABI with host
+buffers (triangle upload, the ABI's own count/range readbacks, hit download).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference] [--workload NAME]
+
+--impl reference times the CPU implementation of the same path (the oracle: a restatement pinned
+bit-exact to the reference's own shader code) on the host cores, full workload per step.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "SVO build ms & Grays/s ray march; batched/served vs plain; served p50/p99 ms"
+L2_FLUSH_BYTES = 512 << 20
+
+WORKLOADS = {
+    "room_1024": "plain voxelize+build+march at 2^10: room shell, 200 cylinders, 210,932 clutter tris "
+                 "(262,144 tris), 1920x1080 primary rays from a seeded interior camera",
+    "plain_256": "plain voxelize+build+march at 2^8: icosphere (20,480 tris) + 64 boxes, 64x64 primary rays",
+    "clusters_4096": "plain voxelize+build+march at 2^12: ~10M tris in 4 clusters, 3840x2160 primary rays",
+}
+
+
+def make_scene(name: str):
+    from sparsevoxeloctree_gb300 import scenes
+    return {"room_1024": scenes.room_1024, "plain_256": scenes.plain_256, "clusters_4096": scenes.clusters_4096}[name]()
+
+
+def load_peaks() -> dict:
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return {"hbm_gbs": float(p["hbm_gbs"]), "source": "measured"}
+    except (OSError, KeyError, ValueError):
+        return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+# ------------------------------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi samples (200 ms) of SM clock and throttle reasons while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "100", "-i", str(self.gpu)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------------------------------ engine arm
+def algorithmic_bytes(kernel: str, w: dict) -> float | None:
+    """Algorithmic bytes of one launch: units the launch processes x bytes per unit (design notes)."""
+    F, T, L, n, k = w["fragments"], w["triangles"], w["level"], w["rays"], w["fetches_per_ray"]
+    leaf_words = w["leaf_words"]
+    table = {
+        "vox_classify_scan": 48.0 * T + 12.0 * T,     # triangles in, offsets out
+        "vox_emit": 48.0 * T + 8.0 * F,               # triangles in, fragments out
+        "dense_mark": 8.0 * F,                        # the fragment list, read once
+        "build_tag": 8.0 * F,                         # one sparse level: the fragment list
+        "build_tag_leaf": 8.0 * F + 8.0 * F,          # fragments in, one 8 B accumulator update each
+        "build_finalize": 12.0 * leaf_words,          # 8 B accumulator in, 4 B leaf word out
+        "dense_write": 4.0 * (w["range_words"] - leaf_words),  # interior words out
+        "march_camera": n * (32.0 + 4.0 * k),         # hit out + node words fetched (rays made in-kernel)
+        "march_rays": n * (24.0 + 32.0 + 4.0 * k),
+    }
+    return table.get(kernel)
+
+
+def engine_arm(args, rank: int, world: int, device) -> dict:
+    import numpy as np
+    import torch
+
+    from sparsevoxeloctree_gb300 import _lib, api
+    from sparsevoxeloctree_gb300.formats import HIT_DTYPE
+
+    lib = _lib.load()
+    scene = make_scene(args.workload)
+    T = len(scene.tris)
+    n_rays = scene.n_rays
+    tris_host = torch.from_numpy(np.ascontiguousarray(scene.tris).view(np.uint8).reshape(-1)).pin_memory()
+    tris_dev = tris_host.to(device)
+    stream = torch.cuda.current_stream()
+
+    vox = api.Voxelizer.Create(tris_dev, scene.level)
+    F = vox.GetVoxelFragmentCount()
+    builder = api.OctreeBuilder.Create(vox)
+    builder.CmdBuild()
+    builder.Reserve()  # scratch sized to this scene's leaf level
+    builder.CmdBuild()
+    octree = api.Octree.Create()
+    octree.Update(builder)
+    tracer = api.OctreeTracer.Create(octree, scene.camera, scene.width, scene.height)
+    hits = tracer.CmdDrawPipeline(count_fetches=True)
+    torch.cuda.synchronize()
+    fetches = int(tracer.fetches.item())
+    info = builder.GetInfo()
+    hit_np = api.hits_numpy(hits)
+
+    def step():
+        vox.CmdVoxelize()
+        builder.CmdBuild()
+        tracer.CmdDrawPipeline(hits)
+
+    flush_buf = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=device)
+    for _ in range(args.warmup):
+        flush_buf.zero_()
+        step()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    sampler = ClockSampler(device.index if device.index is not None else 0)
+    events = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier()
+    sampler.start()
+    launches0 = lib.svo_kernel_launches()
+    lib.svo_profile_enable(1)
+    for a, b in events:
+        flush_buf.zero_()
+        a.record(stream)
+        step()
+        b.record(stream)
+    barrier()
+    launches = lib.svo_kernel_launches() - launches0
+    profile = _lib.profile_summary()
+    lib.svo_profile_enable(0)
+    clocks = sampler.stop()
+    step_ms = [a.elapsed_time(b) for a, b in events]
+    ms = float(np.mean(step_ms))
+    if world > 1:
+        t = torch.tensor([ms], device=device)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+
+    # per-stage device time from the per-kernel events
+    def stage_ms(prefixes):
+        return sum(v["ms"] for k, v in profile.items() if k.startswith(prefixes)) / args.steps
+
+    vox_ms, build_ms, march_ms = stage_ms(("vox_",)), stage_ms(("build_", "dense_")), stage_ms(("march_",))
+    leaf_words = 8 if scene.level == 1 else 8 * info["level_nodes"][scene.level - 2]
+    wl = {"fragments": F, "triangles": T, "level": scene.level, "rays": n_rays, "fetches_per_ray": fetches / n_rays,
+          "range_words": info["range_words"], "leaf_words": leaf_words}
+    peaks = load_peaks()
+    dom = max(profile.items(), key=lambda kv: kv[1]["ms"])
+    dom_name, dom_stats = dom[0], dom[1]
+    dom_launch_ms = dom_stats["ms"] / dom_stats["launches"]
+    alg = algorithmic_bytes(dom_name, wl)
+    roofline = {"kernel": dom_name, "bound": "hbm", "unit": "GB/s", "peak": peaks["hbm_gbs"],
+                "peak_source": peaks["source"], "launch_ms": dom_launch_ms,
+                "share_of_step": dom_stats["ms"] / args.steps / ms}
+    if alg is not None:
+        ach = alg / (dom_launch_ms * 1e-3) / 1e9
+        roofline.update({"achieved": ach, "frac": ach / peaks["hbm_gbs"], "algorithmic_bytes_per_launch": alg})
+    roofline["traffic"] = None  # filled from the committed ncu capture (profiles/), not measured live
+
+    stages = {
+        "voxelize_ms": vox_ms, "build_ms": build_ms, "march_ms": march_ms,
+        "svo_build_ms": vox_ms + build_ms,
+        "mfragments_per_s": F / (vox_ms * 1e-3) / 1e6 if vox_ms else None,
+        "grays_per_s": n_rays / (march_ms * 1e-3) / 1e9 if march_ms else None,
+        "voxelize_gbs": (48.0 * T + 8.0 * F) / (vox_ms * 1e-3) / 1e9 if vox_ms else None,
+        "build_gbs": (8.0 * F * scene.level + 16.0 * info["range_words"]) / (build_ms * 1e-3) / 1e9 if build_ms else None,
+        "march_gbs": n_rays * (24.0 + 32.0 + 4.0 * fetches / n_rays) / (march_ms * 1e-3) / 1e9 if march_ms else None,
+        "hit_fraction": float((hit_np["flags"] & 1).mean()), "mean_iterations": float(hit_np["iter"].mean()),
+        "node_fetches_per_ray": fetches / n_rays, "octree_words": info["range_words"], "leaves": info["leaves"],
+        "kernels": profile,
+    }
+
+    e2e = None if args.no_e2e else e2e_arm(args, scene, tris_host, device, world)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(scene, per_step=False)
+    return {"value": ms, "ms_per_step": ms, "step_ms_all": step_ms, "stages": stages, "roofline": roofline,
+            "clocks": clocks, "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": int(launches),
+            "config_extra": {"level": scene.level, "triangles": T, "fragments": F, "rays": n_rays}}
+
+
+def e2e_arm(args, scene, tris_host, device, world) -> dict:
+    """The same step through the C ABI with host buffers: upload triangles from pinned memory, svo_voxelize
+    (count pass, its blocking count readback, exact allocation, emit), svo_build (its blocking range
+    readback), svo_raycast_camera, download the hits to pinned memory."""
+    import torch
+
+    from sparsevoxeloctree_gb300 import _lib, api
+    from sparsevoxeloctree_gb300.formats import HIT_DTYPE
+
+    lib = _lib.load()
+    n = scene.n_rays
+    hits_host = torch.empty(n * HIT_DTYPE.itemsize, dtype=torch.uint8).pin_memory()
+    tris_dev = torch.empty_like(tris_host, device=device)
+    hits_dev = torch.empty(n * HIT_DTYPE.itemsize, dtype=torch.uint8, device=device)
+    cam = api.camera_struct(scene.camera)
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    T = len(scene.tris)
+
+    def one():
+        tris_dev.copy_(tris_host, non_blocking=True)
+        fl = _lib.Fraglist()
+        _lib.check(lib.svo_voxelize(ctypes.c_void_p(tris_dev.data_ptr()), T, scene.level, ctypes.byref(fl), s))
+        oc = _lib.OctreeC()
+        _lib.check(lib.svo_build_fraglist(ctypes.byref(fl), ctypes.byref(oc), None, s))
+        _lib.check(lib.svo_raycast_camera(ctypes.byref(oc), ctypes.byref(cam), scene.width, scene.height,
+                                          ctypes.c_void_p(hits_dev.data_ptr()), None, s))
+        hits_host.copy_(hits_dev, non_blocking=True)
+        lib.svo_fraglist_destroy(ctypes.byref(fl), s)
+        lib.svo_octree_destroy(ctypes.byref(oc), s)
+        torch.cuda.current_stream().synchronize()
+
+    for _ in range(args.warmup):
+        one()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        one()
+        times.append((time.perf_counter() - t0) * 1e3)
+    ms = float(statistics.mean(times))
+    if world > 1:
+        t = torch.tensor([ms], device=device)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    return {"value": ms, "unit": "ms", "h2d_bytes_per_step": int(tris_host.numel()),
+            "d2h_bytes_per_step": int(hits_host.numel()) + 8 * 3 + 256,
+            "path": "svo_voxelize -> svo_build_fraglist -> svo_raycast_camera with pinned host buffers",
+            "timing": "host wall clock per step (includes the ABI's blocking readbacks)"}
+
+
+# ------------------------------------------------------------------------------------------ CPU arms
+def cpu_baseline(scene, per_step: bool) -> dict:
+    """The oracle (CPU restatement of the reference's path) on the host cores, full workload."""
+    import oracle
+    t0 = time.perf_counter()
+    frags = oracle.voxelize(scene.tris, scene.level)
+    t1 = time.perf_counter()
+    pool = oracle.build_octree(frags, scene.level)
+    t2 = time.perf_counter()
+    rays = oracle.camera_rays(scene.camera, scene.width, scene.height)
+    oracle.raycast(pool, scene.level, rays)
+    t3 = time.perf_counter()
+    ms = (t3 - t0) * 1e3
+    return {"value": ms, "unit": "ms", "cores": oracle.threads(), "kind": "port",
+            "sample": f"full {scene.name} workload, one pass ({len(scene.tris)} tris, {len(frags)} fragments, "
+                      f"{scene.n_rays} rays)",
+            "stages_ms": {"voxelize": (t1 - t0) * 1e3, "build": (t2 - t1) * 1e3, "march": (t3 - t2) * 1e3}}
+
+
+def reference_arm(args, rank: int) -> dict | None:
+    if rank != 0:
+        return None
+    import oracle
+    scene = make_scene(args.workload)
+    for _ in range(args.warmup):
+        cpu_baseline(scene, True)
+    runs = [cpu_baseline(scene, True) for _ in range(args.steps)]
+    ms = float(statistics.mean(r["value"] for r in runs))
+    cpu = dict(runs[-1])
+    cpu["value"] = ms
+    return {"value": ms, "ms_per_step": ms, "cpu_baseline": cpu,
+            "e2e": {"value": ms, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "config_extra": {"level": scene.level, "triangles": len(scene.tris), "rays": scene.n_rays,
+                             "cores": oracle.threads()}}
+
+
+# ------------------------------------------------------------------------------------------ main
+def main() -> int:
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="room_1024")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    line = {"metric": METRIC, "unit": "ms", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "fp32+u32",
+            "data": "synthetic (seeded scene with the benchmark configuration's shapes; the reference's OBJ "
+                    "scenes are not available)"}
+    config = {"workload": f"{args.workload}: {WORKLOADS[args.workload]}",
+              "step": "voxelize (count+emit) + octree build + primary-ray march",
+              "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MiB write); fragment list and node "
+                    "pool exceed L2", "parallelism": f"replicas x{world}" if world > 1 else "single GPU"}
+
+    if args.impl == "reference":
+        res = reference_arm(args, rank)
+        if res is None:
+            return 0
+        line.update({"impl": "reference", "value": res["value"], "ms_per_step": res["ms_per_step"],
+                     "cpu_baseline": res["cpu_baseline"], "e2e": res["e2e"], "gpu_launches": 0})
+        config.update(res["config_extra"])
+        line["config"] = config
+        print(json.dumps(line), flush=True)
+        return 0
+
+    import torch
+    if world > 1:
+        torch.cuda.set_device(local_rank)
+        torch.distributed.init_process_group("nccl")
+    device = torch.device("cuda", local_rank)
+    torch.cuda.set_device(device)
+    res = engine_arm(args, rank, world, device)
+    config.update(res["config_extra"])
+    line.update({"value": res["value"], "ms_per_step": res["ms_per_step"], "config": config,
+                 "stages": res["stages"], "roofline": res["roofline"], "cpu_baseline": res["cpu_baseline"],
+                 "e2e": res["e2e"], "clocks": res["clocks"], "gpu_launches": res["gpu_launches"],
+                 "step_ms": res["step_ms_all"]})
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

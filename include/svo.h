@@ -142,6 +142,14 @@ const char *svo_version(void);
 /* Number of kernels this library launched since load (all devices); a cheap sanity counter for callers. */
 uint64_t svo_kernel_launches(void);
 
+/* Per-kernel timing (the GPU-timestamp instrument of src/LoaderThread.cpp:57-97, per kernel instead of
+ * per stage).  While enabled, every launch of this library is bracketed by two CUDA events recorded on
+ * its own stream.  svo_profile_summary synchronizes on those events and writes a JSON object
+ * {"kernel": {"launches": n, "ms": total}, ...} into buf; it returns the length it needed (excluding
+ * the terminating NUL).  Enabling clears earlier records. */
+void svo_profile_enable(int on);
+size_t svo_profile_summary(char *buf, size_t cap);
+
 /* ------------------------------------------------------------------ voxelize (Voxelizer) */
 
 /* Voxelizer::Create + CmdVoxelize (src/Voxelizer.cpp:5-26, 134-179): count pass, exact allocation,
@@ -184,14 +192,18 @@ int svo_build(const uint64_t *frags, uint32_t count, uint32_t level, svo_octree 
 /* Convenience: svo_build on a fragment list. */
 int svo_build_fraglist(const svo_fraglist *f, svo_octree *out, svo_build_info *info, void *stream);
 
-/* Build into a caller pool (no allocation, no host synchronisation).  pool (device) holds `capacity`
- * words; `workspace` (device) holds svo_build_workspace_size(count, level, capacity) bytes; the result
- * header (range_words, status, per-level counts: svo_build_info layout followed by a uint32 status) is
- * written to `result_dev` (device, at least sizeof(svo_build_info) + 4 bytes). */
-size_t svo_build_workspace_size(uint32_t count, uint32_t level, uint64_t capacity);
+/* Build into a caller pool (no allocation, no host synchronisation).  pool (device, 16-byte aligned)
+ * holds `capacity` words (svo_build_pool_bound(count, level) always suffices); `workspace` (device,
+ * 256-byte aligned) holds `workspace_bytes` bytes, at least svo_build_workspace_size(count, level,
+ * capacity, leaf_words) where leaf_words is the number of words of the deepest level (known from an
+ * earlier build of the same fragments, e.g. 8 x level_nodes[level-2] of its svo_build_info) or 0 for
+ * the worst case.  The result (svo_build_info followed by a uint32 status word, 0 = complete) is
+ * written to `result_dev` (device).  A workspace too small for the leaf level reports SVO_ERR_CAPACITY
+ * through the status word. */
+size_t svo_build_workspace_size(uint32_t count, uint32_t level, uint64_t capacity, uint64_t leaf_words);
 uint64_t svo_build_pool_bound(uint32_t count, uint32_t level);
 int svo_build_into(const uint64_t *frags, uint32_t count, uint32_t level, uint32_t *pool, uint64_t capacity,
-                   void *workspace, void *result_dev, void *stream);
+                   void *workspace, size_t workspace_bytes, void *result_dev, void *stream);
 
 /* svo_build with every device allocation made through `alloc` (NULL = svo_build). */
 int svo_build_ex(const uint64_t *frags, uint32_t count, uint32_t level, const svo_allocator *alloc, svo_octree *out,

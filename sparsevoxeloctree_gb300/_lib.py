@@ -58,6 +58,8 @@ _SIGNATURES = {
     "svo_last_error": ([], ctypes.c_char_p),
     "svo_version": ([], ctypes.c_char_p),
     "svo_kernel_launches": ([], u64),
+    "svo_profile_enable": ([i32], None),
+    "svo_profile_summary": ([ctypes.c_char_p, sz], sz),
     "svo_voxelize": ([P, u32, u32, ctypes.POINTER(Fraglist), P], i32),
     "svo_voxelize_ex": ([P, u32, u32, ctypes.POINTER(Allocator), ctypes.POINTER(Fraglist), P], i32),
     "svo_voxelize_count": ([P, u32, u32, ctypes.POINTER(u64), P], i32),
@@ -68,9 +70,9 @@ _SIGNATURES = {
     "svo_build_ex": ([P, u32, u32, ctypes.POINTER(Allocator), ctypes.POINTER(OctreeC), ctypes.POINTER(BuildInfo), P],
                      i32),
     "svo_build_fraglist": ([ctypes.POINTER(Fraglist), ctypes.POINTER(OctreeC), ctypes.POINTER(BuildInfo), P], i32),
-    "svo_build_workspace_size": ([u32, u32, u64], sz),
+    "svo_build_workspace_size": ([u32, u32, u64, u64], sz),
     "svo_build_pool_bound": ([u32, u32], u64),
-    "svo_build_into": ([P, u32, u32, P, u64, P, P, P], i32),
+    "svo_build_into": ([P, u32, u32, P, u64, P, sz, P, P], i32),
     "svo_octree_destroy": ([ctypes.POINTER(OctreeC), P], None),
     "svo_raycast": ([ctypes.POINTER(OctreeC), P, u32, P, P, P], i32),
     "svo_raycast_camera": ([ctypes.POINTER(OctreeC), ctypes.POINTER(CameraC), u32, u32, P, P, P], i32),
@@ -111,3 +113,13 @@ def load(build_if_needed: bool = True):
 def check(code: int) -> None:
     if code != SVO_OK:
         raise SvoError(code, load().svo_last_error().decode())
+
+
+def profile_summary() -> dict:
+    """Per-kernel {name: {"launches": n, "ms": total}} since svo_profile_enable(1)."""
+    import json
+    lib = load()
+    need = lib.svo_profile_summary(None, 0)
+    buf = ctypes.create_string_buffer(need + 1)
+    lib.svo_profile_summary(buf, need + 1)
+    return json.loads(buf.value.decode())

@@ -148,10 +148,12 @@ class OctreeBuilder:
 
     @staticmethod
     def Create(voxelizer: Voxelizer | None = None, fragments: torch.Tensor | None = None, level: int | None = None,
-               capacity: int | None = None) -> "OctreeBuilder":
+               capacity: int | None = None, leaf_words: int | None = None) -> "OctreeBuilder":
         """OctreeBuilder::Create (src/OctreeBuilder.cpp:8-50): allocates the node pool and scratch.  The pool
         holds the exact upper bound on the words a build of these fragments can use (the reference
-        guesses F*floor(L/3) words and writes past the buffer when the guess is short)."""
+        guesses F*floor(L/3) words and writes past the buffer when the guess is short).  Scratch covers
+        the worst-case leaf level unless `leaf_words` (from an earlier build's info) is given; Reserve()
+        shrinks it to the exact size after a first build."""
         b = OctreeBuilder()
         if voxelizer is not None:
             b.m_voxelizer = voxelizer
@@ -164,8 +166,8 @@ class OctreeBuilder:
         b.m_capacity = int(capacity) if capacity is not None else int(lib.svo_build_pool_bound(b.m_count, b.m_level))
         dev = fragments.device
         b.m_octree_buffer = torch.empty(max(b.m_capacity, 8), dtype=torch.int32, device=dev)
-        b.m_workspace = torch.empty(lib.svo_build_workspace_size(b.m_count, b.m_level, b.m_capacity), dtype=torch.uint8,
-                                    device=dev)
+        b.m_workspace = torch.empty(lib.svo_build_workspace_size(b.m_count, b.m_level, b.m_capacity,
+                                                                 int(leaf_words or 0)), dtype=torch.uint8, device=dev)
         b.m_result = torch.zeros(OctreeBuilder.RESULT_WORDS, dtype=torch.int32, device=dev)
         return b
 
@@ -174,7 +176,17 @@ class OctreeBuilder:
         lib = _lib.load()
         self._info = None
         _lib.check(lib.svo_build_into(_ptr(self.m_fragments), self.m_count, self.m_level, _ptr(self.m_octree_buffer),
-                                      self.m_capacity, _ptr(self.m_workspace), _ptr(self.m_result), _stream(stream)))
+                                      self.m_capacity, _ptr(self.m_workspace), self.m_workspace.numel(),
+                                      _ptr(self.m_result), _stream(stream)))
+
+    def Reserve(self) -> None:
+        """Shrink the scratch to the exact leaf level of the last build (blocking)."""
+        info = self.GetInfo()
+        leaf_words = 8 if self.m_level == 1 else 8 * info["level_nodes"][self.m_level - 2]
+        lib = _lib.load()
+        self.m_workspace = torch.empty(lib.svo_build_workspace_size(self.m_count, self.m_level, self.m_capacity,
+                                                                    leaf_words), dtype=torch.uint8,
+                                       device=self.m_fragments.device)
 
     def GetInfo(self) -> dict:
         """Per-level counters of the last build (blocking read, like Counter::Read)."""

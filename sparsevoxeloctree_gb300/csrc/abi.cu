@@ -7,6 +7,8 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <vector>
+#include <algorithm>
 
 #include "svo_internal.h"
 
@@ -16,6 +18,42 @@ static std::atomic<uint64_t> g_launches{0};
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 static thread_local std::string g_error;
+
+// ---------------------------------------------------------------- profiling
+struct ProfRecord {
+	const char *name;
+	cudaEvent_t begin, end;
+};
+static std::mutex g_prof_mu;
+static std::atomic<bool> g_prof_on{false};
+static std::vector<ProfRecord> g_prof;
+static std::vector<cudaEvent_t> g_prof_free;
+
+static cudaEvent_t prof_event() {
+	if (!g_prof_free.empty()) {
+		cudaEvent_t e = g_prof_free.back();
+		g_prof_free.pop_back();
+		return e;
+	}
+	cudaEvent_t e = nullptr;
+	cudaEventCreate(&e);
+	return e;
+}
+
+ProfScope::ProfScope(const char *name, cudaStream_t s) : slot(-1), stream(s) {
+	if (!g_prof_on.load(std::memory_order_relaxed)) return;
+	std::lock_guard<std::mutex> lk(g_prof_mu);
+	ProfRecord r{name, prof_event(), prof_event()};
+	cudaEventRecord(r.begin, s);
+	g_prof.push_back(r);
+	slot = (int)g_prof.size() - 1;
+}
+
+ProfScope::~ProfScope() {
+	if (slot < 0) return;
+	std::lock_guard<std::mutex> lk(g_prof_mu);
+	if (slot < (int)g_prof.size()) cudaEventRecord(g_prof[slot].end, stream);
+}
 
 static int fail(int code, const char *fmt, ...) {
 	char buf[512];
@@ -120,6 +158,49 @@ using namespace svo;
 extern "C" {
 
 const char *svo_last_error(void) { return g_error.c_str(); }
+
+void svo_profile_enable(int on) {
+	std::lock_guard<std::mutex> lk(g_prof_mu);
+	if (on) {
+		for (auto &r : g_prof) {
+			g_prof_free.push_back(r.begin);
+			g_prof_free.push_back(r.end);
+		}
+		g_prof.clear();
+	}
+	g_prof_on.store(on != 0);
+}
+
+size_t svo_profile_summary(char *buf, size_t cap) {
+	std::lock_guard<std::mutex> lk(g_prof_mu);
+	std::vector<std::pair<std::string, std::pair<int, double>>> agg;
+	for (auto &r : g_prof) {
+		cudaEventSynchronize(r.end);
+		float ms = 0.0f;
+		if (cudaEventElapsedTime(&ms, r.begin, r.end) != cudaSuccess) ms = 0.0f;
+		auto it = std::find_if(agg.begin(), agg.end(), [&](const auto &a) { return a.first == r.name; });
+		if (it == agg.end()) {
+			agg.push_back({r.name, {1, (double)ms}});
+		} else {
+			it->second.first += 1;
+			it->second.second += ms;
+		}
+	}
+	std::string out = "{";
+	for (size_t i = 0; i < agg.size(); ++i) {
+		char item[256];
+		snprintf(item, sizeof(item), "%s\"%s\": {\"launches\": %d, \"ms\": %.6f}", i ? ", " : "", agg[i].first.c_str(),
+		         agg[i].second.first, agg[i].second.second);
+		out += item;
+	}
+	out += "}";
+	if (buf && cap) {
+		const size_t n = std::min(cap - 1, out.size());
+		memcpy(buf, out.data(), n);
+		buf[n] = 0;
+	}
+	return out.size();
+}
 const char *svo_version(void) { return "svo-gb300 0.1 (sm_103a)"; }
 uint64_t svo_kernel_launches(void) { return g_launches.load(); }
 
@@ -252,14 +333,23 @@ void svo_fraglist_destroy(svo_fraglist *f, void *stream) {
 // ------------------------------------------------------------------------------------------ build
 uint64_t svo_build_pool_bound(uint32_t count, uint32_t level) { return build_pool_bound(count, level); }
 
-size_t svo_build_workspace_size(uint32_t count, uint32_t level, uint64_t capacity) {
-	return build_workspace_bytes(count, level, capacity);
+size_t svo_build_workspace_size(uint32_t count, uint32_t level, uint64_t capacity, uint64_t leaf_words) {
+	BuildWorkspace w;
+	const uint64_t slots = leaf_words ? leaf_words : build_leaf_slot_bound(count, level, capacity);
+	build_workspace_layout(nullptr, count, level, capacity, slots, w);
+	return w.total_bytes;
 }
 
 static int check_frags(const uint64_t *frags, uint32_t count) {
 	if (count && !frags) return fail(SVO_ERR_INVALID, "null fragment buffer");
 	if (!aligned(frags, 8)) return fail(SVO_ERR_INVALID, "fragment buffer must be 8-byte aligned");
 	return SVO_OK;
+}
+
+// Reads the build state back (blocking).
+static cudaError_t read_state(const BuildWorkspace &w, BuildState &st, cudaStream_t s) {
+	cudaError_t e = cudaMemcpyAsync(&st, w.state, sizeof(st), cudaMemcpyDeviceToHost, s);
+	return e == cudaSuccess ? cudaStreamSynchronize(s) : e;
 }
 
 int svo_build_ex(const uint64_t *frags, uint32_t count, uint32_t level, const svo_allocator *alloc, svo_octree *out,
@@ -270,29 +360,62 @@ int svo_build_ex(const uint64_t *frags, uint32_t count, uint32_t level, const sv
 	cudaStream_t s = (cudaStream_t)stream;
 	Mem mem{alloc, s};
 	const uint64_t capacity = build_pool_bound(count, level);
-	void *pool = nullptr;
+	void *pool = nullptr, *ws = nullptr, *acc = nullptr, *wide = nullptr;
 	SVO_CK(mem.get(&pool, capacity * sizeof(uint32_t)), "octree pool allocation");
-	void *ws = nullptr;
-	cudaError_t e = mem.get(&ws, build_workspace_bytes(count, level, capacity));
+	BuildWorkspace w;
+	build_workspace_layout(nullptr, count, level, capacity, 0, w);
+	cudaError_t e = mem.get(&ws, w.interior_bytes);
+	BuildState st;
+	auto cleanup = [&](bool keep_pool) {
+		mem.put(ws);
+		mem.put(acc);
+		mem.put(wide);
+		if (!keep_pool) mem.put(pool);
+	};
 	if (e != cudaSuccess) {
-		mem.put(pool);
+		cleanup(false);
 		return cuda_fail(e, "build workspace allocation");
 	}
-	BuildWorkspace w;
-	build_workspace_layout(ws, count, level, capacity, w);
-	e = build_launch(frags, count, level, (uint32_t *)pool, capacity, w, s);
-	BuildState st;
-	if (e == cudaSuccess) e = cudaMemcpyAsync(&st, w.state, sizeof(st), cudaMemcpyDeviceToHost, s);
-	if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-	mem.put(ws);
+	build_workspace_layout(ws, count, level, capacity, 0, w);
+	// stage 1: interior levels; the leaf range is then known exactly (as GetOctreeRange reads the
+	// counter, src/OctreeBuilder.cpp:212-214)
+	e = build_launch_interior(frags, count, level, (uint32_t *)pool, capacity, w, s);
+	if (e == cudaSuccess) e = read_state(w, st, s);
 	if (e != cudaSuccess) {
-		mem.put(pool);
-		return cuda_fail(e, "build");
+		cleanup(false);
+		return cuda_fail(e, "build interior levels");
 	}
 	if ((rc = status_to_error(st.status, "build"))) {
-		mem.put(pool);
+		cleanup(false);
 		return rc;
 	}
+	// stage 2: leaf colours with accumulators sized to the leaf range
+	const uint64_t leaf_words = st.lv[level].num;
+	w.leaf_slots = leaf_words;
+	e = mem.get(&acc, leaf_words * 8 + 16);
+	w.acc = (unsigned long long *)acc;
+	if (e == cudaSuccess) e = build_launch_leaf(frags, count, level, (uint32_t *)pool, w, false, s);
+	if (e == cudaSuccess) e = read_state(w, st, s);
+	if (e == cudaSuccess && (st.status & kStatusLeafWide)) { // a voxel with more than 257 fragments
+		e = mem.get(&wide, leaf_words * 16 + 16);
+		w.acc_wide = (unsigned long long *)wide;
+		if (e == cudaSuccess) e = build_launch_leaf(frags, count, level, (uint32_t *)pool,
+		                                            BuildWorkspace{w.state, w.descs, w.desc_count, w.dv, w.dense_words,
+		                                                           w.cache, w.interior_bytes, w.leaf_slots, nullptr,
+		                                                           w.acc_wide, w.total_bytes},
+		                                            true, s);
+		if (e == cudaSuccess) e = read_state(w, st, s);
+		st.status &= ~kStatusLeafWide;
+	}
+	if (e != cudaSuccess) {
+		cleanup(false);
+		return cuda_fail(e, "build leaf level");
+	}
+	if ((rc = status_to_error(st.status, "build"))) {
+		cleanup(false);
+		return rc;
+	}
+	cleanup(true);
 	out->words = (uint32_t *)pool;
 	out->capacity = capacity;
 	out->range_words = st.range_words;
@@ -321,17 +444,30 @@ int svo_build_fraglist(const svo_fraglist *f, svo_octree *out, svo_build_info *i
 }
 
 int svo_build_into(const uint64_t *frags, uint32_t count, uint32_t level, uint32_t *pool, uint64_t capacity,
-                   void *workspace, void *result_dev, void *stream) {
+                   void *workspace, size_t workspace_bytes, void *result_dev, void *stream) {
 	int rc;
 	if ((rc = check_level(level)) || (rc = check_frags(frags, count))) return rc;
 	if (!pool || !workspace || !result_dev) return fail(SVO_ERR_INVALID, "null argument");
 	if (capacity < 8) return fail(SVO_ERR_CAPACITY, "pool smaller than the root block");
 	if (!aligned(pool, 16) || !aligned(workspace, 256) || !aligned(result_dev, 4))
 		return fail(SVO_ERR_INVALID, "pool must be 16-byte and workspace 256-byte aligned");
-	cudaStream_t s = (cudaStream_t)stream;
 	BuildWorkspace w;
-	build_workspace_layout(workspace, count, level, capacity, w);
-	SVO_CK(build_launch(frags, count, level, pool, capacity, w, s), "build");
+	build_workspace_layout(nullptr, count, level, capacity, 0, w);
+	const size_t interior = w.interior_bytes;
+	if (workspace_bytes < interior + 2 * 256 + 24 * 8)
+		return fail(SVO_ERR_CAPACITY, "workspace of %zu bytes is below the %zu the interior levels need", workspace_bytes,
+		            interior + 2 * 256 + 24 * 8);
+	// the most leaf slots (8 B packed + 16 B wide each) whose layout fits in workspace_bytes
+	uint64_t slots = ((workspace_bytes - interior) / 24) & ~7ull;
+	for (;;) {
+		build_workspace_layout(nullptr, count, level, capacity, slots, w);
+		if (w.total_bytes <= workspace_bytes || slots < 8) break;
+		slots -= 8;
+	}
+	build_workspace_layout(workspace, count, level, capacity, slots, w);
+	cudaStream_t s = (cudaStream_t)stream;
+	SVO_CK(build_launch_interior(frags, count, level, pool, capacity, w, s), "build interior levels");
+	SVO_CK(build_launch_leaf(frags, count, level, pool, w, true, s), "build leaf level");
 	SVO_CK(build_launch_export(w, level, count, result_dev, s), "build info export");
 	return SVO_OK;
 }

@@ -331,10 +331,9 @@ cudaError_t march_launch(const MarchArgs &a, bool camera, cudaStream_t stream) {
 	const uint64_t blocks_needed = (warps_needed + kMarchTPB / 32 - 1) / (kMarchTPB / 32);
 	const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(blocks_needed, (uint64_t)sms * 12));
 	if (camera)
-		march_kernel<true><<<blocks, kMarchTPB, 0, stream>>>(a);
+		SVO_LAUNCH("march_camera", stream, march_kernel<true><<<blocks, kMarchTPB, 0, stream>>>(a););
 	else
-		march_kernel<false><<<blocks, kMarchTPB, 0, stream>>>(a);
-	note_launch();
+		SVO_LAUNCH("march_rays", stream, march_kernel<false><<<blocks, kMarchTPB, 0, stream>>>(a););
 	return cudaGetLastError();
 }
 
@@ -342,8 +341,7 @@ cudaError_t bounce_launch(const svo_hit *hits, uint32_t n, uint64_t seed, svo_ra
 	if (n == 0) return cudaSuccess;
 	const int sms = device_sm_count();
 	const uint32_t blocks = (uint32_t)std::min<uint64_t>(((uint64_t)n + 255) / 256, (uint64_t)sms * 8);
-	bounce_kernel<<<blocks, 256, 0, stream>>>(hits, n, seed, rays);
-	note_launch();
+	SVO_LAUNCH("bounce_kernel", stream, bounce_kernel<<<blocks, 256, 0, stream>>>(hits, n, seed, rays););
 	return cudaGetLastError();
 }
 

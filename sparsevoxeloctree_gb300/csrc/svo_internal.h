@@ -16,10 +16,25 @@ inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 enum : uint32_t {
 	kStatusTimeout = 1u,  // a bounded look-back wait gave up
 	kStatusCapacity = 2u, // an output buffer or the 30-bit pointer range would overflow
-	kStatusMalformed = 4u // a march met a pointer outside the pool or a tree deeper than its level
+	kStatusMalformed = 4u, // a march met a pointer outside the pool or a tree deeper than its level
+	kStatusLeafWide = 16u  // a voxel got more than 257 fragments: leaf colours need the wide accumulators
 };
 
 void note_launch();      // counts kernel launches (svo_kernel_launches)
+
+// Brackets one kernel launch with CUDA events on its stream while profiling is enabled.
+struct ProfScope {
+	ProfScope(const char *name, cudaStream_t stream);
+	~ProfScope();
+	int slot;
+	cudaStream_t stream;
+};
+#define SVO_LAUNCH(name, stream, ...)                                                                       \
+	do {                                                                                                \
+		::svo::ProfScope prof_scope_(name, stream);                                                 \
+		__VA_ARGS__;                                                                                \
+		::svo::note_launch();                                                                       \
+	} while (0)
 int device_sm_count();   // SMs of the current device (cached per device)
 
 // ---------------------------------------------------------------- voxelize
@@ -63,20 +78,41 @@ struct BuildState {
 	LevelInfo lv[SVO_LEVEL_MAX + 2];    // lv[d] for depth d (1-based)
 };
 
+constexpr uint32_t kDenseMaxDepth = 9; // deepest depth held as a dense occupancy bitmap (8^9 bits)
+
+// Dense occupancy bitmaps of depths 1..D, concatenated (level d at word off[d]), and the exclusive
+// prefix of their popcounts over the concatenation (prefix[off[D+1]] = occupied cells of depths 1..D).
+struct DenseView {
+	uint32_t *bits;
+	uint32_t *prefix;
+	uint32_t off[kDenseMaxDepth + 2];
+	uint32_t D;
+};
+
 struct BuildWorkspace {
 	BuildState *state;
 	unsigned long long *descs;
 	size_t desc_count;
-	uint32_t *cache;           // per-fragment node index of the previous depth
-	unsigned long long *sums;  // leaf accumulators, 2 x u64 per leaf word
-	size_t sum_slots;
+	DenseView dv;
+	uint32_t dense_words;
+	uint32_t *cache;                // per-fragment node index of the previous sparse depth
+	size_t interior_bytes;          // bytes up to here
+	uint64_t leaf_slots;            // leaf words the accumulators cover
+	unsigned long long *acc;        // packed leaf accumulators (8 B per leaf word)
+	unsigned long long *acc_wide;   // exact leaf accumulators (16 B per leaf word), used only on overflow
 	size_t total_bytes;
 };
 uint64_t build_pool_bound(uint32_t count, uint32_t level);
-size_t build_workspace_bytes(uint32_t count, uint32_t level, uint64_t capacity);
-void build_workspace_layout(void *ws, uint32_t count, uint32_t level, uint64_t capacity, BuildWorkspace &w);
-cudaError_t build_launch(const uint64_t *frags, uint32_t count, uint32_t level, uint32_t *pool, uint64_t capacity,
-                         const BuildWorkspace &w, cudaStream_t stream);
+uint64_t build_leaf_slot_bound(uint32_t count, uint32_t level, uint64_t capacity);
+uint32_t dense_depth(uint32_t level);
+void build_workspace_layout(void *ws, uint32_t count, uint32_t level, uint64_t capacity, uint64_t leaf_slots,
+                            BuildWorkspace &w);
+// Interior levels (dense bitmaps, then sparse tag/alloc); the leaf range ends up in state->lv[level].
+cudaError_t build_launch_interior(const uint64_t *frags, uint32_t count, uint32_t level, uint32_t *pool,
+                                  uint64_t capacity, const BuildWorkspace &w, cudaStream_t stream);
+// Leaf colours and finalize (packed accumulators; the flag-gated wide pass too when `wide`).
+cudaError_t build_launch_leaf(const uint64_t *frags, uint32_t count, uint32_t level, uint32_t *pool,
+                              const BuildWorkspace &w, bool wide, cudaStream_t stream);
 // svo_build_info followed by the uint32 status word, written to device memory `out`.
 cudaError_t build_launch_export(const BuildWorkspace &w, uint32_t level, uint32_t count, void *out,
                                 cudaStream_t stream);

@@ -406,11 +406,9 @@ cudaError_t vox_launch_count(const svo_triangle *tris, uint32_t n, uint32_t leve
 		if (e == cudaSuccess) e = cudaMemsetAsync(w.unit_frag, 0, sizeof(unsigned long long), stream);
 		return e;
 	}
-	vox_classify_scan<<<(n + kTile - 1) / kTile, kTPB, 0, stream>>>(tris, n, level, w);
-	note_launch();
+	SVO_LAUNCH("vox_classify_scan", stream, vox_classify_scan<<<(n + kTile - 1) / kTile, kTPB, 0, stream>>>(tris, n, level, w););
 	const int sms = device_sm_count();
-	vox_unit_scan<<<(uint32_t)sms * 4, kTPB, 0, stream>>>(tris, n, level, w);
-	note_launch();
+	SVO_LAUNCH("vox_unit_scan", stream, vox_unit_scan<<<(uint32_t)sms * 4, kTPB, 0, stream>>>(tris, n, level, w););
 	return cudaGetLastError();
 }
 
@@ -418,8 +416,7 @@ cudaError_t vox_launch_emit(const svo_triangle *tris, uint32_t n, uint32_t level
                             uint64_t *frags, uint64_t capacity, cudaStream_t stream) {
 	if (n == 0) return cudaSuccess;
 	const int sms = device_sm_count();
-	vox_emit<<<(uint32_t)sms * 16, kTPB, 0, stream>>>(tris, n, level, w, frags, capacity);
-	note_launch();
+	SVO_LAUNCH("vox_emit", stream, vox_emit<<<(uint32_t)sms * 16, kTPB, 0, stream>>>(tris, n, level, w, frags, capacity););
 	return cudaGetLastError();
 }
 
@@ -432,8 +429,7 @@ __global__ void vox_totals(VoxWorkspace w) {
 }
 
 cudaError_t vox_launch_totals(const VoxWorkspace &w, cudaStream_t stream) {
-	vox_totals<<<1, 1, 0, stream>>>(w);
-	note_launch();
+	SVO_LAUNCH("vox_totals", stream, vox_totals<<<1, 1, 0, stream>>>(w););
 	return cudaGetLastError();
 }
 

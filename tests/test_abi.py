@@ -39,8 +39,10 @@ def test_invalid_arguments_are_rejected_before_any_launch(lib):
     assert lib.svo_raycast(ctypes.byref(oc), None, 0, None, None, None) == _lib.SVO_ERR_INVALID  # null octree
     oc.words, oc.level, oc.range_words = 256, 5, 12  # range not a multiple of 8
     assert lib.svo_raycast(ctypes.byref(oc), None, 0, None, None, None) == _lib.SVO_ERR_INVALID
-    assert lib.svo_build_into(ctypes.c_void_p(256), 1, 3, ctypes.c_void_p(256), 4, ctypes.c_void_p(256),
+    assert lib.svo_build_into(ctypes.c_void_p(256), 1, 3, ctypes.c_void_p(256), 4, ctypes.c_void_p(256), 1 << 20,
                               ctypes.c_void_p(256), None) == _lib.SVO_ERR_CAPACITY
+    assert lib.svo_build_into(ctypes.c_void_p(256), 1, 3, ctypes.c_void_p(256), 64, ctypes.c_void_p(256), 64,
+                              ctypes.c_void_p(256), None) == _lib.SVO_ERR_CAPACITY  # workspace too small
     assert lib.svo_kernel_launches() == before
 
 
@@ -48,7 +50,8 @@ def test_pool_bound_and_workspace_sizes(lib):
     import oracle
     for count, level in [(0, 1), (1, 1), (5, 3), (1000, 8), (38_000_000, 10), (150_000_000, 12)]:
         assert lib.svo_build_pool_bound(count, level) == oracle.pool_bound(count, level)
-    assert lib.svo_build_workspace_size(1000, 8, lib.svo_build_pool_bound(1000, 8)) > 4000
+    cap = lib.svo_build_pool_bound(1000, 8)
+    assert lib.svo_build_workspace_size(1000, 8, cap, 0) > lib.svo_build_workspace_size(1000, 8, cap, 64) > 4000
     assert lib.svo_voxelize_workspace_size(1000) > 8 * 1000
 
 

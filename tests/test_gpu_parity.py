@@ -243,3 +243,72 @@ def test_camera_golden(cuda, golden_dir):
     api = _api()
     h_cam = api.hits_numpy(api.OctreeTracer.Create(o, cam, w, h).CmdDrawPipeline())
     assert_hits_equal(h_cam, oracle.raycast(pool, s.level, rays))
+
+
+# ------------------------------------------------------------------------------------------- build edge paths
+@pytest.mark.parametrize("level", [10, 11, 12])
+def test_build_deep_levels(cuda, level):
+    """Levels 11 and 12 go through the sparse tag/alloc path below the dense depth-9 bitmaps."""
+    from sparsevoxeloctree_gb300.formats import pack_fragments
+    g = np.random.default_rng(300 + level)
+    R = 1 << level
+    n = 40000
+    xyz = g.integers(0, R, size=(n, 3))
+    xyz[: n // 4] = (xyz[: n // 4] // 64) * 64 + g.integers(0, 3, size=(n // 4, 3))  # small dense clumps
+    frags = pack_fragments(xyz[:, 0], xyz[:, 1], xyz[:, 2], g.integers(0, 1 << 24, size=n))
+    ref, nodes = oracle.build_octree(frags, level, return_level_nodes=True)
+    o, got = gpu_build(frags, level)
+    assert np.array_equal(got, ref)
+    assert o.info["level_nodes"] == nodes.tolist()
+
+
+def _crowded_voxel_fragments(level, n_hot):
+    from sparsevoxeloctree_gb300.formats import pack_fragments
+    g = np.random.default_rng(7)
+    R = 1 << level
+    xyz = g.integers(0, R, size=(2000, 3))
+    hot = np.tile([[R // 3, R // 2, R // 5]], (n_hot, 1))
+    xyz = np.concatenate([xyz, hot])
+    return pack_fragments(xyz[:, 0], xyz[:, 1], xyz[:, 2], g.integers(0, 1 << 24, size=len(xyz)))
+
+
+@pytest.mark.parametrize("n_hot", [257, 258, 5000])
+def test_build_many_fragments_in_one_voxel(cuda, n_hot):
+    """More than 257 fragments in one voxel overflow the packed accumulator: the exact wide pass takes
+    over (both through svo_build_ex and through the stream-ordered svo_build_into)."""
+    import torch
+    api = _api()
+    level = 6
+    frags = _crowded_voxel_fragments(level, n_hot)
+    ref = oracle.build_octree(frags, level)
+    _, got = gpu_build(frags, level)
+    assert np.array_equal(got, ref)
+    t = torch.from_numpy(frags.view(np.int64)).cuda()
+    b = api.OctreeBuilder.Create(fragments=t, level=level)
+    b.GetOctree().fill_(-1)
+    b.CmdBuild()
+    assert b.GetOctreeRange() == 4 * len(ref)
+    assert np.array_equal(b.GetOctree()[: len(ref)].cpu().numpy().view(np.uint32), ref)
+
+
+def test_build_into_pool_too_small_reports_capacity(cuda):
+    import torch
+    from sparsevoxeloctree_gb300 import _lib
+    api = _api()
+    s = scenes.plain_256()
+    frags = oracle.voxelize(s.tris, s.level)
+    t = torch.from_numpy(frags.view(np.int64)).cuda()
+    b = api.OctreeBuilder.Create(fragments=t, level=s.level, capacity=4096)
+    b.CmdBuild()
+    with pytest.raises(_lib.SvoError) as e:
+        b.GetInfo()
+    assert e.value.code == _lib.SVO_ERR_CAPACITY
+    # the builder is still usable with a large enough pool
+    b2 = api.OctreeBuilder.Create(fragments=t, level=s.level)
+    b2.CmdBuild()
+    b2.Reserve()  # scratch shrunk to the exact leaf level
+    b2.GetOctree().fill_(-1)  # no stale words from the first build can pass the comparison
+    b2.CmdBuild()
+    ref = oracle.build_octree(frags, s.level)
+    assert b2.GetInfo()["range_words"] == len(ref)  # raises if the build reported an error
+    assert np.array_equal(b2.GetOctree()[: len(ref)].cpu().numpy().view(np.uint32), ref)
