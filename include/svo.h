@@ -180,6 +180,20 @@ int svo_voxelize_ex(const svo_triangle *tris, uint32_t n_tris, uint32_t level, c
 
 void svo_fraglist_destroy(svo_fraglist *f, void *stream);
 
+/* svo_voxelize_into for callers that cannot allocate device memory (a frame loop that forbids
+ * allocation after start-up, a thread holding an allocator lock, a fully pre-partitioned device).
+ * No counterpart in the reference.  The caller passes the triangles, the fragment buffer (`capacity`
+ * fragments) and count_dev (device, 2 x uint64: [0] fragments produced, [1] status, 0 = complete); the
+ * engine's scratch is a fixed 16 MiB array in device memory that every GPU loading this library holds
+ * until the process exits.  It takes at most 262,144 triangles (more: SVO_ERR_CAPACITY, nothing
+ * launched) whose large triangles split into at most about 1.5 million raster units (a 1024 x 1024
+ * wall is 4,096; beyond the limit count_dev[1] is non-zero and svo_voxelize must be used).  No
+ * allocation call is made.  The first call on a device looks up that array's address; make that first
+ * call before any stream capture.  All calls share the array: calls whose work overlaps on the GPU
+ * (other streams, other host threads) race and must be serialized by the caller. */
+int svo_voxelize_static(const svo_triangle *tris, uint32_t n_tris, uint32_t level, uint64_t *frags, uint64_t capacity,
+                        uint64_t *count_dev, void *stream);
+
 /* ------------------------------------------------------------------ build (OctreeBuilder + Octree) */
 
 /* OctreeBuilder::Create + CmdBuild + GetOctreeRange + Octree::Update (src/OctreeBuilder.cpp:8-50,142-214,

@@ -66,6 +66,7 @@ _SIGNATURES = {
     "svo_voxelize_workspace_size": ([u32], sz),
     "svo_voxelize_into": ([P, u32, u32, P, u64, P, P, P], i32),
     "svo_fraglist_destroy": ([ctypes.POINTER(Fraglist), P], None),
+    "svo_voxelize_static": ([P, u32, u32, P, u64, P, P], i32),
     "svo_build": ([P, u32, u32, ctypes.POINTER(OctreeC), ctypes.POINTER(BuildInfo), P], i32),
     "svo_build_ex": ([P, u32, u32, ctypes.POINTER(Allocator), ctypes.POINTER(OctreeC), ctypes.POINTER(BuildInfo), P],
                      i32),

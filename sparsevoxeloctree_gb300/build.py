@@ -26,6 +26,7 @@ UNITS = {
     "voxelize.cu": [],
     "build.cu": [],
     "march.cu": ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"],
+    "noalloc.cu": [],
 }
 HEADERS = ["common.cuh", "svo_internal.h"]
 

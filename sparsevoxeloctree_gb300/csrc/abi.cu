@@ -65,6 +65,16 @@ static int fail(int code, const char *fmt, ...) {
 	return code;
 }
 
+int svo_fail(int code, const char *fmt, ...) {
+	char buf[512];
+	va_list ap;
+	va_start(ap, fmt);
+	vsnprintf(buf, sizeof(buf), fmt, ap);
+	va_end(ap);
+	g_error = buf;
+	return code;
+}
+
 static int cuda_fail(cudaError_t e, const char *what) {
 	cudaGetLastError(); // clear a sticky launch error of this thread
 	return fail(e == cudaErrorMemoryAllocation ? SVO_ERR_OOM : SVO_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));

@@ -1,0 +1,84 @@
+// noalloc.cu — svo_voxelize_static: the voxelizer's count + emit with its scratch in a fixed device array,
+// for callers that cannot allocate device memory.
+//
+// Who needs this: code that runs where a cudaMalloc is not allowed or not safe — a renderer's frame loop
+// that forbids allocation after start-up, a host thread holding a memory-pool lock, or an embedding
+// whose device memory is fully carved up in advance.  They bring their own triangle and fragment
+// buffers; the engine's own scratch (fragment offsets, large-triangle units, scan descriptors,
+// counters) then has to live somewhere that needs no allocation call: a file-scope __device__ array
+// that the module loader places when the library is loaded and that stays resident on every GPU that
+// loads the library until the process exits.
+#include <cstring>
+#include <mutex>
+
+#include "svo_internal.h"
+
+namespace svo {
+
+// Scratch for up to kStaticMaxTris triangles: (n+1) fragment offsets (8 B), (n+1) unit offsets (4 B),
+// scan descriptors and counters; everything left over holds raster units of large triangles (8 B
+// each; a room wall at level 10 is 4,096 units, the 262,144-triangle room scene about 0.7M).
+constexpr uint32_t kStaticMaxTris = 262144;
+constexpr size_t kStaticScratchBytes = 16u << 20; // 16 MiB
+
+// Largest unit capacity whose workspace layout for n triangles fits the static scratch.
+static uint64_t static_unit_cap(uint32_t n) {
+	VoxWorkspace w;
+	const size_t fixed = vox_workspace_layout(nullptr, n, 0, w);
+	uint64_t cap = (kStaticScratchBytes - fixed) / 9;
+	while (cap > 0 && vox_workspace_layout(nullptr, n, cap, w) > kStaticScratchBytes) cap -= cap > 4096 ? 4096 : cap;
+	return cap;
+}
+
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+
+constexpr int kMaxDevices = 64;
+static void *g_scratch_addr[kMaxDevices];
+static std::mutex g_scratch_mu;
+
+// Device address of g_static_scratch on the current device, looked up once per device.
+static cudaError_t static_scratch(void **out) {
+	int dev = 0;
+	cudaError_t e = cudaGetDevice(&dev);
+	if (e != cudaSuccess) return e;
+	if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+	std::lock_guard<std::mutex> lk(g_scratch_mu);
+	if (!g_scratch_addr[dev]) {
+		void *p = nullptr;
+		e = cudaGetSymbolAddress(&p, g_static_scratch);
+		if (e != cudaSuccess) return e;
+		g_scratch_addr[dev] = p;
+	}
+	*out = g_scratch_addr[dev];
+	return cudaSuccess;
+}
+
+} // namespace svo
+
+using namespace svo;
+
+extern "C" int svo_voxelize_static(const svo_triangle *tris, uint32_t n_tris, uint32_t level, uint64_t *frags,
+                                   uint64_t capacity, uint64_t *count_dev, void *stream) {
+	if (level < SVO_LEVEL_MIN || level > SVO_LEVEL_MAX) return svo_fail(SVO_ERR_INVALID, "level %u outside [1, 12]", level);
+	if (n_tris > kStaticMaxTris)
+		return svo_fail(SVO_ERR_CAPACITY,
+		                "svo_voxelize_static handles at most %u triangles (got %u); use svo_voxelize for larger meshes",
+		                kStaticMaxTris, n_tris);
+	if ((n_tris && !tris) || ((uintptr_t)tris % 16) != 0) return svo_fail(SVO_ERR_INVALID, "triangle buffer must be 16-byte aligned");
+	if (!count_dev || (capacity && !frags)) return svo_fail(SVO_ERR_INVALID, "null argument");
+	void *scratch = nullptr;
+	cudaError_t e = static_scratch(&scratch);
+	if (e != cudaSuccess) return svo_fail(SVO_ERR_CUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+	cudaStream_t s = (cudaStream_t)stream;
+	VoxWorkspace w;
+	vox_workspace_layout(scratch, n_tris, static_unit_cap(n_tris), w);
+	// vox_launch_count clears the scan descriptors and counters the previous call left behind
+	e = vox_launch_count(tris, n_tris, level, w, s);
+	if (e == cudaSuccess) e = vox_launch_totals(w, s);
+	if (e == cudaSuccess) e = vox_launch_emit(tris, n_tris, level, w, frags, capacity, s);
+	if (e == cudaSuccess) e = cudaMemcpyAsync(count_dev, w.totals, sizeof(uint64_t), cudaMemcpyDeviceToDevice, s);
+	if (e == cudaSuccess)
+		e = cudaMemcpyAsync(count_dev + 1, w.totals + 2, sizeof(uint64_t), cudaMemcpyDeviceToDevice, s);
+	if (e != cudaSuccess) return svo_fail(SVO_ERR_CUDA, "svo_voxelize_static: %s", cudaGetErrorString(e));
+	return SVO_OK;
+}

@@ -21,6 +21,7 @@ enum : uint32_t {
 };
 
 void note_launch();      // counts kernel launches (svo_kernel_launches)
+int svo_fail(int code, const char *fmt, ...); // sets the calling thread's svo_last_error message
 
 // Brackets one kernel launch with CUDA events on its stream while profiling is enabled.
 struct ProfScope {
