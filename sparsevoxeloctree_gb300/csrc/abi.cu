@@ -505,8 +505,8 @@ static int raycast_common(const svo_octree *o, const svo_ray *rays, const svo_ca
 	if (!aligned(hits, 16)) return fail(SVO_ERR_INVALID, "hit buffer must be 16-byte aligned");
 	if (!cam && n && (!rays || !aligned(rays, 8))) return fail(SVO_ERR_INVALID, "ray buffer must be 8-byte aligned");
 	cudaStream_t s = (cudaStream_t)stream;
-	uint32_t *scratch = nullptr;
-	SVO_CK(alloc_async(&scratch, 2 * sizeof(uint32_t), s), "ray ticket allocation");
+	unsigned long long *scratch = nullptr;
+	SVO_CK(alloc_async(&scratch, 2 * sizeof(unsigned long long), s), "ray ticket allocation");
 	MarchArgs a;
 	memset(&a, 0, sizeof(a));
 	a.pool = o->words;
@@ -519,7 +519,7 @@ static int raycast_common(const svo_octree *o, const svo_ray *rays, const svo_ca
 	a.n = n;
 	a.hits = hits;
 	a.ticket = scratch;
-	a.status = scratch + 1;
+	a.status = reinterpret_cast<uint32_t *>(scratch + 1);
 	a.fetches = (unsigned long long *)fetches_dev;
 	cudaError_t e = march_launch(a, cam != nullptr, s);
 	cudaFreeAsync(scratch, s);

@@ -157,7 +157,10 @@ __global__ void __launch_bounds__(kTPB) dense_scan(DenseView dv, uint32_t total_
 		}
 		uint32_t total;
 		uint32_t run = block_exclusive_sum<uint32_t, kTPB>(local, s_warp, total);
-		if (threadIdx.x == 0) s_prefix = (uint32_t)tile_lookback(descs, tile, 15u, total, &state->status);
+		if (threadIdx.x < 32) {
+			const uint32_t p = (uint32_t)tile_lookback_warp(descs, tile, 15u, total, &state->status);
+			if (threadIdx.x == 0) s_prefix = p;
+		}
 		__syncthreads();
 		run += s_prefix;
 #pragma unroll
@@ -186,57 +189,51 @@ __global__ void dense_finish(DenseView dv, BuildState *state) {
 	}
 }
 
-// Writes the child blocks of every occupied cell of depths 0 (the root) .. D: interior words of depths
-// 1..D, and for depth D+1 zeroed words when sparse levels follow (leaf blocks are left to the finalize).
+// Writes the child blocks of every occupied cell of depths 0 (the root) .. D that has interior or
+// sparse children: interior words of depths 1..D, and zeroed words of depth D+1 when sparse levels
+// follow.  When depth D+1 is the leaf depth, depth-D cells are skipped: the leaf finalize writes those
+// blocks whole.  One bitmap word and one prefix word of the child depth serve all 8 children.
 __global__ void __launch_bounds__(kTPB) dense_write(uint32_t *__restrict__ pool, uint64_t capacity, DenseView dv,
                                                     uint32_t level, BuildState *state) {
 	const uint32_t D = dv.D;
-	const uint32_t parent_words = dv.off[D + 1]; // words of depths 1..D; item 0 = the root
 	const bool leaf_next = D + 1 == level;
+	const uint32_t last_parent_depth = leaf_next ? D - 1 : D;
+	const uint32_t parent_words = dv.off[last_parent_depth + 1]; // words of parent depths 1..last; item 0 = root
 	for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item <= parent_words; item += gridDim.x * blockDim.x) {
-		if (item == 0) { // the root block: words 0..7 are the depth-1 nodes
-			uint32_t w[8];
-#pragma unroll
-			for (int o = 0; o < 8; ++o)
-				w[o] = dense_bit(dv, 1, o) ? (0x80000000u | (8u * (1u + grank(dv, 1, o)))) : 0u;
-			uint4 *dst = reinterpret_cast<uint4 *>(pool);
-			dst[0] = make_uint4(w[0], w[1], w[2], w[3]);
-			dst[1] = make_uint4(w[4], w[5], w[6], w[7]);
-			continue;
+		uint32_t bits, e, base_m, r;
+		if (item == 0) { // the root: a single occupied cell whose block (words 0..7) holds the depth-1 nodes
+			bits = 1u, e = 0, base_m = 0, r = 0;
+		} else {
+			const uint32_t gw = item - 1; // global word of a parent depth e in 1..last
+			e = 1;
+			while (gw >= dv.off[e + 1]) ++e;
+			bits = __ldg(dv.bits + gw);
+			base_m = (gw - dv.off[e]) << 5;
+			r = __ldg(dv.prefix + gw); // grank of the first set bit of this word
 		}
-		const uint32_t gw = item - 1; // global word of a parent depth e in 1..D
-		uint32_t e = 1;
-		while (gw >= dv.off[e + 1]) ++e;
 		const uint32_t d = e + 1; // depth of the words being written
-		uint32_t bits = __ldg(dv.bits + gw);
-		if (!bits) continue;
-		const uint32_t base_m = (gw - dv.off[e]) << 5;
-		uint32_t r = __ldg(dv.prefix + gw); // grank of the first set bit of this word
 		while (bits) {
 			const uint32_t b = __ffs(bits) - 1;
 			bits &= bits - 1;
 			const uint32_t q = base_m + b; // parent cell (depth e)
-			const uint64_t blk = 8ull * (1u + r++);
+			const uint64_t blk = e == 0 ? 0ull : 8ull * (1u + r++);
 			if (blk + 8 > capacity || blk + 8 > SVO_MAX_POOL_WORDS) {
 				atomicOr(&state->status, kStatusCapacity);
 				continue;
 			}
-			if (d <= D) {
-				uint32_t w[8];
+			uint32_t w[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+			if (d <= D) { // children are interior nodes: one byte of the depth-d bitmap
+				const uint32_t cw = dv.off[d] + (q >> 2), shift = (q & 3u) * 8u;
+				const uint32_t word = __ldg(dv.bits + cw);
+				const uint32_t kids = (word >> shift) & 0xffu;
+				const uint32_t rank0 = __ldg(dv.prefix + cw) + __popc(word & ((1u << shift) - 1u));
 #pragma unroll
-				for (int o = 0; o < 8; ++o) {
-					const uint32_t m = 8u * q + o;
-					w[o] = dense_bit(dv, d, m) ? (0x80000000u | (8u * (1u + grank(dv, d, m)))) : 0u;
-				}
-				uint4 *dst = reinterpret_cast<uint4 *>(pool + blk);
-				dst[0] = make_uint4(w[0], w[1], w[2], w[3]);
-				dst[1] = make_uint4(w[4], w[5], w[6], w[7]);
-			} else if (!leaf_next) { // sparse depths follow: zero the block for their tags
-
-				uint4 *dst = reinterpret_cast<uint4 *>(pool + blk);
-				dst[0] = make_uint4(0, 0, 0, 0);
-				dst[1] = make_uint4(0, 0, 0, 0);
-			} // leaf blocks are written whole by the leaf finalize
+				for (int o = 0; o < 8; ++o)
+					if ((kids >> o) & 1u) w[o] = 0x80000000u | (8u * (1u + rank0 + __popc(kids & ((1u << o) - 1u))));
+			}
+			uint4 *dst = reinterpret_cast<uint4 *>(pool + blk);
+			dst[0] = make_uint4(w[0], w[1], w[2], w[3]);
+			dst[1] = make_uint4(w[4], w[5], w[6], w[7]);
 		}
 	}
 }
@@ -311,6 +308,65 @@ __global__ void __launch_bounds__(kTPB) build_tag(const uint64_t *__restrict__ f
 	}
 }
 
+// Leaf sweep: 4 fragments per thread, in phases so their loads and atomics overlap: fragment loads,
+// leaf-word lookups (dense ranks or the cached parent), then the four accumulator updates.
+__global__ void __launch_bounds__(kTPB) build_leaf(const uint64_t *__restrict__ frags, uint32_t n, uint32_t level,
+                                                   const uint32_t *__restrict__ pool,
+                                                   const uint32_t *__restrict__ cache,
+                                                   unsigned long long *__restrict__ acc, DenseView dv,
+                                                   BuildState *state) {
+	const uint32_t status = state->status;
+	if (status & kStatusCapacity) return;
+	const bool parent_dense = level == 1 || level - 1 <= dv.D;
+	const uint32_t leaf_begin = state->lv[level].begin, leaf_num = state->lv[level].num;
+	uint32_t *st = &state->status;
+	const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+	const uint64_t nq = (n + 3ull) / 4ull;
+	for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += stride) {
+		const uint64_t f0 = q * 4;
+		uint64_t f[4];
+		uint32_t c[4] = {0u, 0u, 0u, 0u};
+		const bool full = f0 + 4 <= n && ((uintptr_t)(frags + f0) & 15u) == 0;
+		if (full) {
+			const ulonglong2 a = __ldcs(reinterpret_cast<const ulonglong2 *>(frags + f0));
+			const ulonglong2 b = __ldcs(reinterpret_cast<const ulonglong2 *>(frags + f0 + 2));
+			f[0] = a.x, f[1] = a.y, f[2] = b.x, f[3] = b.y;
+			if (!parent_dense) {
+				const uint4 cc = __ldcs(reinterpret_cast<const uint4 *>(cache + f0));
+				c[0] = cc.x, c[1] = cc.y, c[2] = cc.z, c[3] = cc.w;
+			}
+		} else {
+#pragma unroll
+			for (int k = 0; k < 4; ++k) {
+				f[k] = f0 + k < n ? frags[f0 + k] : 0ull;
+				c[k] = (!parent_dense && f0 + k < n) ? cache[f0 + k] : 0u;
+			}
+		}
+		uint32_t slot[4];
+#pragma unroll
+		for (int k = 0; k < 4; ++k) {
+			uint32_t x, y, z;
+			frag_xyz(f[k], x, y, z);
+			const uint32_t idx = parent_dense ? dense_child_word(dv, x, y, z, level, level)
+			                                  : (__ldg(pool + c[k]) & 0x3fffffffu) + octant_at(x, y, z, 0);
+			slot[k] = f0 + k < n ? idx - leaf_begin : 0xffffffffu;
+		}
+		unsigned long long old[4];
+#pragma unroll
+		for (int k = 0; k < 4; ++k) {
+			old[k] = 0ull;
+			if (slot[k] < leaf_num) {
+				const uint32_t rgb = (uint32_t)(f[k] >> 32);
+				const unsigned long long v = (rgb & 0xffu) | ((unsigned long long)((rgb >> 8) & 0xffu) << 16) |
+				                             ((unsigned long long)((rgb >> 16) & 0xffu) << 32) | kLeafOne;
+				old[k] = atomicAdd(acc + slot[k], v);
+			}
+		}
+		if ((old[0] >> 48) >= 257ull || (old[1] >> 48) >= 257ull || (old[2] >> 48) >= 257ull || (old[3] >> 48) >= 257ull)
+			atomicOr(st, kStatusLeafWide); // a packed sum may have carried: the wide pass redoes the colours
+	}
+}
+
 // Prefix-sum allocation of child blocks for the marked words of a sparse depth (persistent grid, tiles
 // claimed in order by ticket so the look-back always waits on a running or finished tile).  The block
 // of a node is zeroed (the next depth's init) unless the next depth is the leaf depth.
@@ -356,7 +412,10 @@ __global__ void __launch_bounds__(kTPB) build_alloc(uint32_t *__restrict__ pool,
 		for (int k = 0; k < kAllocIPT; ++k) cnt += (w[k] >> 31);
 		uint32_t total;
 		const uint32_t rank0 = block_exclusive_sum<uint32_t, kTPB>(cnt, s_warp, total);
-		if (threadIdx.x == 0) s_prefix = (uint32_t)tile_lookback(descs, tile, depth, total, &state->status);
+		if (threadIdx.x < 32) {
+			const uint32_t p = (uint32_t)tile_lookback_warp(descs, tile, depth, total, &state->status);
+			if (threadIdx.x == 0) s_prefix = p;
+		}
 		__syncthreads();
 		const uint32_t prefix = s_prefix;
 		uint32_t rank = rank0;
@@ -415,21 +474,34 @@ __global__ void __launch_bounds__(kTPB) build_finalize(uint32_t *__restrict__ po
 	if (s_skip) return;
 	const LevelInfo li = state->lv[level];
 	uint32_t leaves = 0;
-	for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < li.num; k += gridDim.x * blockDim.x) {
-		uint32_t word = 0;
+	// 4 leaf words per thread (num and begin are multiples of 8: 16-byte stores, 32-byte packed loads)
+	for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < li.num / 4u; g += gridDim.x * blockDim.x) {
+		uint32_t word[4];
+#pragma unroll
+		for (int j = 0; j < 4; ++j) word[j] = 0u;
 		if (WIDE) {
-			const ulonglong2 a = reinterpret_cast<const ulonglong2 *>(acc)[k];
-			const uint32_t n = (uint32_t)(a.y >> 32);
-			if (n) word = leaf_word(n, (uint32_t)a.x, (uint32_t)(a.x >> 32), (uint32_t)a.y);
+			const ulonglong2 *a = reinterpret_cast<const ulonglong2 *>(acc) + 4u * g;
+#pragma unroll
+			for (int j = 0; j < 4; ++j) {
+				const ulonglong2 v = a[j];
+				const uint32_t n = (uint32_t)(v.y >> 32);
+				if (n) word[j] = leaf_word(n, (uint32_t)v.x, (uint32_t)(v.x >> 32), (uint32_t)v.y);
+			}
 		} else {
-			const unsigned long long a = __ldcs(acc + k);
-			const uint32_t n = (uint32_t)(a >> 48);
-			if (n)
-				word = leaf_word(n, (uint32_t)(a & 0xffffu), (uint32_t)((a >> 16) & 0xffffu),
-				                 (uint32_t)((a >> 32) & 0xffffu));
+			const ulonglong2 *a = reinterpret_cast<const ulonglong2 *>(acc) + 2u * g;
+			const ulonglong2 v0 = __ldcs(a), v1 = __ldcs(a + 1);
+			const unsigned long long v[4] = {v0.x, v0.y, v1.x, v1.y};
+#pragma unroll
+			for (int j = 0; j < 4; ++j) {
+				const uint32_t n = (uint32_t)(v[j] >> 48);
+				if (n)
+					word[j] = leaf_word(n, (uint32_t)(v[j] & 0xffffu), (uint32_t)((v[j] >> 16) & 0xffffu),
+					                    (uint32_t)((v[j] >> 32) & 0xffffu));
+			}
 		}
-		pool[li.begin + k] = word;
-		leaves += word != 0u;
+		reinterpret_cast<uint4 *>(pool + li.begin)[g] = make_uint4(word[0], word[1], word[2], word[3]);
+#pragma unroll
+		for (int j = 0; j < 4; ++j) leaves += word[j] != 0u;
 	}
 	leaves = warp_sum(leaves);
 	if (lane_id() == 0) s_warp[threadIdx.x >> 5] = leaves;
@@ -597,8 +669,7 @@ cudaError_t build_launch_leaf(const uint64_t *frags, uint32_t count, uint32_t le
 		SVO_LAUNCH("build_leaf_zero", stream,
 		           build_leaf_zero<<<(uint32_t)sms * 8, kTPB, 0, stream>>>(w.acc, w.leaf_slots, w.state, level););
 		SVO_LAUNCH("build_tag_leaf", stream,
-		           build_tag<kTagLeaf><<<tag_blocks, kTPB, 0, stream>>>(frags, count, level, level, pool, w.cache, w.acc,
-		                                                                w.dv, w.state, vec_ok););
+		           build_leaf<<<tag_blocks, kTPB, 0, stream>>>(frags, count, level, pool, w.cache, w.acc, w.dv, w.state););
 		SVO_LAUNCH("build_finalize", stream,
 		           build_finalize<false><<<(uint32_t)sms * 8, kTPB, 0, stream>>>(pool, w.acc, w.state, level););
 	}

@@ -73,34 +73,45 @@ SVO_DEV unsigned long long desc_load(const unsigned long long *d) {
 	return w;
 }
 
-// Called by one thread of tile `t` once its aggregate is known; returns the exclusive prefix of the
-// tile.  Waits are bounded (kSpinLimit); on timeout the status word gets kStatusTimeout.
-SVO_DEV unsigned long long tile_lookback(unsigned long long *descs, uint32_t t, uint32_t epoch,
-                                         unsigned long long aggregate, uint32_t *status) {
+// Decoupled look-back for tile `t` once its aggregate is known, called by all 32 lanes of one warp:
+// each step inspects the 32 nearest unexamined predecessors at once and sums their aggregates up to
+// the nearest inclusive prefix.  Returns the tile's exclusive prefix on every lane.  Waits are bounded
+// (kSpinLimit); on timeout the status word gets kStatusTimeout.
+SVO_DEV unsigned long long tile_lookback_warp(unsigned long long *descs, uint32_t t, uint32_t epoch,
+                                              unsigned long long aggregate, uint32_t *status) {
+	const uint32_t lane = lane_id();
 	if (t == 0) {
-		desc_publish(&descs[0], epoch, 2, aggregate);
+		if (lane == 0) desc_publish(&descs[0], epoch, 2, aggregate);
 		return 0;
 	}
-	desc_publish(&descs[t], epoch, 1, aggregate);
+	if (lane == 0) desc_publish(&descs[t], epoch, 1, aggregate);
 	unsigned long long prefix = 0;
-	int64_t j = (int64_t)t - 1;
+	int64_t end = (int64_t)t - 1; // window: descriptors end, end-1, ..., end-31 (lane k reads end-k)
 	uint32_t spins = 0;
-	while (j >= 0) {
-		unsigned long long w = desc_load(&descs[j]);
-		uint32_t e = (uint32_t)(w >> 56), flag = (uint32_t)(w >> 54) & 3u;
-		if (e != epoch || flag == 0) {
+	for (;;) {
+		const int64_t j = end - (int64_t)lane;
+		unsigned long long w = 0;
+		uint32_t flag = 2; // before tile 0: an inclusive prefix of 0
+		if (j >= 0) {
+			w = desc_load(&descs[j]);
+			flag = ((uint32_t)(w >> 56) == epoch) ? (uint32_t)(w >> 54) & 3u : 0u;
+		}
+		const uint32_t incl = __ballot_sync(kFullMask, flag == 2);
+		const uint32_t first = incl ? (uint32_t)(__ffs(incl) - 1) : 31u;
+		const uint32_t need = first == 31u ? kFullMask : ((2u << first) - 1u);
+		if (__ballot_sync(kFullMask, flag == 0) & need) { // a needed predecessor has not published yet
 			if (++spins > kSpinLimit) {
-				atomicOr(status, kStatusTimeout);
+				if (lane == 0) atomicOr(status, kStatusTimeout);
 				break;
 			}
 			__nanosleep(20);
 			continue;
 		}
-		prefix += w & kDescValueMask;
-		if (flag == 2) break;
-		--j;
+		prefix += warp_sum(((need >> lane) & 1u) && j >= 0 ? (w & kDescValueMask) : 0ull);
+		if (incl) break;
+		end -= 32;
 	}
-	desc_publish(&descs[t], epoch, 2, prefix + aggregate);
+	if (lane == 0) desc_publish(&descs[t], epoch, 2, prefix + aggregate);
 	return prefix;
 }
 

@@ -6,19 +6,23 @@
 // operation is rounded separately, so results are bit-identical to the oracle's scalar restatement.
 //
 // GB300 design:
-//   * persistent grid (a few blocks per SM); each warp claims batches of rays from a global ticket, so
-//     long incoherent rays do not leave the tail of the launch idle;
+//   * persistent grid; each warp claims 32 rays at a time from a global ticket (one ray per lane), so
+//     rays of very different lengths do not leave the tail of the launch idle (measured: 4 rays per lane
+//     per ticket took 1.7x longer on the 2^10 room scene);
+//   * camera rays are claimed as 8x4-pixel tiles, so a warp's lanes march neighbouring rays that share
+//     traversal paths and node words;
 //   * the traversal stack (one parent word per level, at most 12) lives in shared memory, laid out
 //     [level][thread] so a warp's accesses hit 32 distinct banks; it never touches local memory;
 //   * node words are read through the read-only path (ld.global.nc), so hot upper levels stay in L1/L2;
-//   * camera rays are generated in the kernel (no ray buffer), hits are written as two 16 B stores.
+//   * camera rays are generated in the kernel (no ray buffer), hits are written as two 16 B stores
+//     (row-major by pixel, whatever the claim order).
 #include "common.cuh"
 #include "svo_internal.h"
 
 namespace svo {
 
 constexpr int kMarchTPB = 128;
-constexpr uint32_t kRaysPerLane = 4; // rays a lane takes per ticket
+constexpr uint32_t kRaysPerLane = 1; // rays a lane takes per ticket
 constexpr float kEps = 3.552713678800501e-15f; // EPS of shader/octree.glsl:44 (2^-48)
 
 SVO_DEV float max_glsl(float x, float y) { return x < y ? y : x; }
@@ -214,20 +218,29 @@ __global__ void __launch_bounds__(kMarchTPB) march_kernel(MarchArgs a) {
 	__shared__ uint32_t s_stack[SVO_LEVEL_MAX * kMarchTPB];
 	uint32_t *stack = s_stack + threadIdx.x;
 	const uint32_t lane = lane_id();
+	// work slots: ray indices, or for camera rays 32 slots per 8x4 tile of the (padded) image
+	const uint32_t tiles_x = CAMERA ? (a.width + 7u) / 8u : 0u;
+	const uint64_t slots = CAMERA ? (uint64_t)tiles_x * ((a.height + 3u) / 4u) * 32u : (uint64_t)a.n;
 	unsigned long long fetched = 0;
 	for (;;) {
-		uint32_t base = 0;
-		if (lane == 0) base = atomicAdd(a.ticket, 32u * kRaysPerLane);
+		unsigned long long base = 0;
+		if (lane == 0) base = atomicAdd(a.ticket, (unsigned long long)(32u * kRaysPerLane));
 		base = __shfl_sync(kFullMask, base, 0);
-		if (base >= a.n) break;
+		if (base >= slots) break;
 #pragma unroll 1
 		for (uint32_t k = 0; k < kRaysPerLane; ++k) {
-			const uint32_t r = base + k * 32u + lane;
-			if (r >= a.n) break;
+			const uint64_t slot = base + k * 32u + lane;
+			if (slot >= slots) break;
 			float o[3], d[3];
-			if (CAMERA) {
+			uint32_t r;
+			if constexpr (CAMERA) {
+				const uint32_t tile = (uint32_t)(slot >> 5), in = (uint32_t)(slot & 31u);
+				const uint32_t x = (tile % tiles_x) * 8u + (in & 7u), y = (tile / tiles_x) * 4u + (in >> 3);
+				if (x >= a.width || y >= a.height) continue; // padding slot of a partial edge tile
+				r = y * a.width + x;
 				camera_ray(a.cam, a.width, a.height, r, o, d);
 			} else {
+				r = (uint32_t)slot;
 				const float2 *src = reinterpret_cast<const float2 *>(a.rays + r);
 				const float2 p0 = src[0], p1 = src[1], p2 = src[2];
 				o[0] = p0.x, o[1] = p0.y, o[2] = p1.x, d[0] = p1.y, d[1] = p2.x, d[2] = p2.y;
@@ -324,12 +337,12 @@ __global__ void bounce_kernel(const svo_hit *__restrict__ hits, uint32_t n, uint
 
 // ---------------------------------------------------------------------------------------------------
 cudaError_t march_launch(const MarchArgs &a, bool camera, cudaStream_t stream) {
-	cudaError_t e = cudaMemsetAsync(a.ticket, 0, sizeof(uint32_t), stream);
+	cudaError_t e = cudaMemsetAsync(a.ticket, 0, sizeof(unsigned long long), stream);
 	if (e != cudaSuccess || a.n == 0) return e;
 	const int sms = device_sm_count();
 	const uint64_t warps_needed = ((uint64_t)a.n + 32 * kRaysPerLane - 1) / (32 * kRaysPerLane);
 	const uint64_t blocks_needed = (warps_needed + kMarchTPB / 32 - 1) / (kMarchTPB / 32);
-	const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(blocks_needed, (uint64_t)sms * 12));
+	const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(blocks_needed, (uint64_t)sms * 16));
 	if (camera)
 		SVO_LAUNCH("march_camera", stream, march_kernel<true><<<blocks, kMarchTPB, 0, stream>>>(a););
 	else

@@ -128,7 +128,7 @@ struct MarchArgs {
 	uint32_t width, height;
 	uint32_t n;
 	svo_hit *hits;
-	uint32_t *ticket;             // device ray ticket (zeroed by march_launch)
+	unsigned long long *ticket;   // device work-slot ticket (zeroed by march_launch)
 	unsigned long long *fetches;  // optional node-load total
 	uint32_t *status;             // device status word
 };

@@ -256,9 +256,10 @@ __global__ void __launch_bounds__(kTPB) vox_classify_scan(const svo_triangle *__
 	unsigned long long tc, tu;
 	const unsigned long long ec = block_exclusive_sum<unsigned long long, kTPB>(lc, s_warp, tc);
 	const unsigned long long eu = block_exclusive_sum<unsigned long long, kTPB>(lu, s_warp, tu);
-	if (threadIdx.x == 0) {
-		s_prefix[0] = tile_lookback(w.descs, tile, 1u, tc, &w.counters[kCtrStatus]);
-		s_prefix[1] = tile_lookback(w.descs2, tile, 1u, tu, &w.counters[kCtrStatus]);
+	if (threadIdx.x < 32) {
+		const unsigned long long pc = tile_lookback_warp(w.descs, tile, 1u, tc, &w.counters[kCtrStatus]);
+		const unsigned long long pu = tile_lookback_warp(w.descs2, tile, 1u, tu, &w.counters[kCtrStatus]);
+		if (threadIdx.x == 0) s_prefix[0] = pc, s_prefix[1] = pu;
 	}
 	__syncthreads();
 	unsigned long long rc = s_prefix[0] + ec, ru = s_prefix[1] + eu;
@@ -314,7 +315,10 @@ __global__ void __launch_bounds__(kTPB) vox_unit_scan(const svo_triangle *__rest
 		}
 		unsigned long long total;
 		const unsigned long long excl = block_exclusive_sum<unsigned long long, kTPB>(local, s_warp, total);
-		if (threadIdx.x == 0) s_prefix = tile_lookback(w.descs3, tile, 1u, total, &w.counters[kCtrStatus]);
+		if (threadIdx.x < 32) {
+			const unsigned long long p = tile_lookback_warp(w.descs3, tile, 1u, total, &w.counters[kCtrStatus]);
+			if (threadIdx.x == 0) s_prefix = p;
+		}
 		__syncthreads();
 		unsigned long long run = s_prefix + excl;
 #pragma unroll

@@ -312,3 +312,22 @@ def test_build_into_pool_too_small_reports_capacity(cuda):
     ref = oracle.build_octree(frags, s.level)
     assert b2.GetInfo()["range_words"] == len(ref)  # raises if the build reported an error
     assert np.array_equal(b2.GetOctree()[: len(ref)].cpu().numpy().view(np.uint32), ref)
+
+
+@pytest.mark.parametrize("size", [(37, 23), (7, 5), (1, 1), (1921, 3), (8, 4)])
+def test_camera_image_sizes_not_multiple_of_the_tile(cuda, size):
+    """Camera rays are claimed in 8x4 tiles: edge tiles must cover every pixel exactly once."""
+    import torch
+    api = _api()
+    s = scenes.plain_256()
+    frags = oracle.voxelize(s.tris, s.level)
+    o, pool = gpu_build(frags, s.level)
+    w, h = size
+    cam = scenes.camera_from_angles((1.5, 1.5, 0.5), 0.05, 0.02, np.pi / 3, w / h)
+    n = w * h
+    hits = torch.full((n * 32 + 64,), 0xAB, dtype=torch.uint8, device="cuda")  # guard bytes after the image
+    api.OctreeTracer.Create(o, cam, w, h).CmdDrawPipeline(hits[: n * 32])
+    raw = hits.cpu().numpy()
+    assert (raw[n * 32:] == 0xAB).all()  # nothing written past the last pixel
+    got = raw[: n * 32].view(np.uint8).view(HIT_DTYPE)
+    assert_hits_equal(got, oracle.raycast(pool, s.level, oracle.camera_rays(cam, w, h)))
