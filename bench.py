@@ -168,6 +168,9 @@ def engine_arm(args, rank: int, world: int, device) -> dict:
         flush_buf.zero_()
         step()
     torch.cuda.synchronize()
+    vox.CheckEmission()  # the re-recorded voxelize pass produced every fragment
+    if builder.GetInfo()["range_words"] != info["range_words"]:
+        raise RuntimeError("re-recorded build differs from the first build")
 
     def barrier():
         if world > 1:

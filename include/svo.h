@@ -103,7 +103,7 @@ typedef struct svo_fraglist {
 	uint32_t level;    /* octree level the fragments were voxelized at */
 	uint64_t capacity; /* fragments the buffer can hold */
 	uint32_t owned;    /* 1 if allocated by the library (freed by svo_fraglist_destroy) */
-	uint32_t reserved;
+	uint32_t units;    /* raster units of the large triangles (sizes svo_voxelize_into's workspace) */
 } svo_fraglist;
 
 /* An octree node pool (device memory). */
@@ -142,6 +142,15 @@ const char *svo_version(void);
 /* Number of kernels this library launched since load (all devices); a cheap sanity counter for callers. */
 uint64_t svo_kernel_launches(void);
 
+/* Device memory and transfers for callers without the CUDA headers (C, C++, FFI bindings).  Allocation
+ * is stream-ordered (freed memory stays pooled for reuse); copies are asynchronous on `stream` except
+ * svo_download with sync = 1, which returns once the data is in host memory. */
+int svo_device_alloc(void **ptr, size_t bytes, void *stream);
+void svo_device_free(void *ptr, void *stream);
+int svo_upload(void *dst_device, const void *src_host, size_t bytes, void *stream);
+int svo_download(void *dst_host, const void *src_device, size_t bytes, int sync, void *stream);
+int svo_stream_synchronize(void *stream);
+
 /* Per-kernel timing (the GPU-timestamp instrument of src/LoaderThread.cpp:57-97, per kernel instead of
  * per stage).  While enabled, every launch of this library is bracketed by two CUDA events recorded on
  * its own stream.  svo_profile_summary synchronizes on those events and writes a JSON object
@@ -166,12 +175,14 @@ int svo_voxelize_count(const svo_triangle *tris, uint32_t n_tris, uint32_t level
 /* Count and emit into a caller buffer (no allocation, no host synchronisation): frags (device) holds
  * `capacity` fragments; count_dev (device, 2 x uint64) receives [0] the number of fragments the
  * triangles produce and [1] a status word (0 = complete).  Fragments beyond `capacity` are not written
- * (count_dev[0] > capacity tells the caller to retry with a larger buffer); status != 0 means the
- * workspace was too small for this mesh's large triangles (use svo_voxelize, which sizes it exactly).
- * Scratch comes from `workspace` (device, 256-byte aligned) of svo_voxelize_workspace_size(n_tris) bytes. */
-size_t svo_voxelize_workspace_size(uint32_t n_tris);
+ * (count_dev[0] > capacity tells the caller to retry with a larger buffer).  Scratch comes from
+ * `workspace` (device, 256-byte aligned, `workspace_bytes` long), at least
+ * svo_voxelize_workspace_size(n_tris, units) with `units` from an earlier count of the same mesh
+ * (svo_fraglist.units) or 0 for a guess; when the mesh's large triangles need more raster units than
+ * the workspace holds, their fragments are skipped and count_dev[1] is non-zero. */
+size_t svo_voxelize_workspace_size(uint32_t n_tris, uint64_t units);
 int svo_voxelize_into(const svo_triangle *tris, uint32_t n_tris, uint32_t level, uint64_t *frags, uint64_t capacity,
-                      uint64_t *count_dev, void *workspace, void *stream);
+                      uint64_t *count_dev, void *workspace, size_t workspace_bytes, void *stream);
 
 /* svo_voxelize with every device allocation made through `alloc` (NULL = the library's stream-ordered
  * pool, exactly svo_voxelize). */

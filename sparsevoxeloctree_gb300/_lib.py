@@ -29,7 +29,7 @@ class SvoError(RuntimeError):
 
 
 class Fraglist(ctypes.Structure):
-    _fields_ = [("data", P), ("count", u32), ("level", u32), ("capacity", u64), ("owned", u32), ("reserved", u32)]
+    _fields_ = [("data", P), ("count", u32), ("level", u32), ("capacity", u64), ("owned", u32), ("units", u32)]
 
 
 class OctreeC(ctypes.Structure):
@@ -58,13 +58,18 @@ _SIGNATURES = {
     "svo_last_error": ([], ctypes.c_char_p),
     "svo_version": ([], ctypes.c_char_p),
     "svo_kernel_launches": ([], u64),
+    "svo_device_alloc": ([ctypes.POINTER(P), sz, P], i32),
+    "svo_device_free": ([P, P], None),
+    "svo_upload": ([P, P, sz, P], i32),
+    "svo_download": ([P, P, sz, i32, P], i32),
+    "svo_stream_synchronize": ([P], i32),
     "svo_profile_enable": ([i32], None),
     "svo_profile_summary": ([ctypes.c_char_p, sz], sz),
     "svo_voxelize": ([P, u32, u32, ctypes.POINTER(Fraglist), P], i32),
     "svo_voxelize_ex": ([P, u32, u32, ctypes.POINTER(Allocator), ctypes.POINTER(Fraglist), P], i32),
     "svo_voxelize_count": ([P, u32, u32, ctypes.POINTER(u64), P], i32),
-    "svo_voxelize_workspace_size": ([u32], sz),
-    "svo_voxelize_into": ([P, u32, u32, P, u64, P, P, P], i32),
+    "svo_voxelize_workspace_size": ([u32, u64], sz),
+    "svo_voxelize_into": ([P, u32, u32, P, u64, P, P, sz, P], i32),
     "svo_fraglist_destroy": ([ctypes.POINTER(Fraglist), P], None),
     "svo_voxelize_static": ([P, u32, u32, P, u64, P, P], i32),
     "svo_build": ([P, u32, u32, ctypes.POINTER(OctreeC), ctypes.POINTER(BuildInfo), P], i32),

@@ -81,6 +81,7 @@ class Voxelizer:
         self.m_voxel_fragment_list: torch.Tensor | None = None
         self.m_workspace: torch.Tensor | None = None
         self.m_count_dev: torch.Tensor | None = None
+        self.m_units = 0
 
     @staticmethod
     def Create(triangles, octree_level: int, stream=None) -> "Voxelizer":
@@ -99,6 +100,7 @@ class Voxelizer:
         _lib.check(lib.svo_voxelize_ex(_ptr(triangles), v.m_n_tris, v.m_level, ctypes.byref(alloc.struct),
                                        ctypes.byref(out), _stream(stream)))
         v.m_voxel_fragment_count = int(out.count)
+        v.m_units = int(out.units)
         buf = alloc.take(out.data) if out.count else torch.empty(0, dtype=torch.uint8, device=triangles.device)
         v.m_voxel_fragment_list = buf.view(torch.int64)[: out.count]
         return v
@@ -108,12 +110,21 @@ class Voxelizer:
         lib = _lib.load()
         if self.m_workspace is None:
             dev = self.m_tris.device
-            self.m_workspace = torch.empty(lib.svo_voxelize_workspace_size(self.m_n_tris), dtype=torch.uint8,
-                                           device=dev)
+            self.m_workspace = torch.empty(lib.svo_voxelize_workspace_size(self.m_n_tris, self.m_units),
+                                           dtype=torch.uint8, device=dev)
             self.m_count_dev = torch.zeros(2, dtype=torch.int64, device=dev)
         _lib.check(lib.svo_voxelize_into(_ptr(self.m_tris), self.m_n_tris, self.m_level,
                                          _ptr(self.m_voxel_fragment_list), self.m_voxel_fragment_count,
-                                         _ptr(self.m_count_dev), _ptr(self.m_workspace), _stream(stream)))
+                                         _ptr(self.m_count_dev), _ptr(self.m_workspace), self.m_workspace.numel(),
+                                         _stream(stream)))
+
+    def CheckEmission(self) -> None:
+        """Raise unless the last CmdVoxelize produced every fragment (blocking read)."""
+        count, status = (int(x) for x in self.m_count_dev.cpu())
+        if status != 0 or count != self.m_voxel_fragment_count:
+            raise _lib.SvoError(_lib.SVO_ERR_CAPACITY,
+                                f"re-emission incomplete: {count} of {self.m_voxel_fragment_count} fragments, "
+                                f"status {status}")
 
     def GetLevel(self) -> int:
         return self.m_level

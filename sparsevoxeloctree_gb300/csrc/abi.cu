@@ -169,6 +169,34 @@ extern "C" {
 
 const char *svo_last_error(void) { return g_error.c_str(); }
 
+int svo_device_alloc(void **ptr, size_t bytes, void *stream) {
+	if (!ptr) return fail(SVO_ERR_INVALID, "null pointer");
+	SVO_CK(alloc_async(ptr, bytes, (cudaStream_t)stream), "device allocation");
+	return SVO_OK;
+}
+
+void svo_device_free(void *ptr, void *stream) {
+	if (ptr) cudaFreeAsync(ptr, (cudaStream_t)stream);
+}
+
+int svo_upload(void *dst_device, const void *src_host, size_t bytes, void *stream) {
+	if (bytes && (!dst_device || !src_host)) return fail(SVO_ERR_INVALID, "null pointer");
+	SVO_CK(cudaMemcpyAsync(dst_device, src_host, bytes, cudaMemcpyHostToDevice, (cudaStream_t)stream), "upload");
+	return SVO_OK;
+}
+
+int svo_download(void *dst_host, const void *src_device, size_t bytes, int sync, void *stream) {
+	if (bytes && (!dst_host || !src_device)) return fail(SVO_ERR_INVALID, "null pointer");
+	SVO_CK(cudaMemcpyAsync(dst_host, src_device, bytes, cudaMemcpyDeviceToHost, (cudaStream_t)stream), "download");
+	if (sync) SVO_CK(cudaStreamSynchronize((cudaStream_t)stream), "download synchronize");
+	return SVO_OK;
+}
+
+int svo_stream_synchronize(void *stream) {
+	SVO_CK(cudaStreamSynchronize((cudaStream_t)stream), "stream synchronize");
+	return SVO_OK;
+}
+
 void svo_profile_enable(int on) {
 	std::lock_guard<std::mutex> lk(g_prof_mu);
 	if (on) {
@@ -221,12 +249,14 @@ static int check_tris(const svo_triangle *tris, uint32_t n) {
 	return SVO_OK;
 }
 
-size_t svo_voxelize_workspace_size(uint32_t n_tris) { return vox_workspace_bytes(n_tris, vox_default_unit_cap(n_tris)); }
+size_t svo_voxelize_workspace_size(uint32_t n_tris, uint64_t units) {
+	return vox_workspace_bytes(n_tris, units ? units : vox_default_unit_cap(n_tris));
+}
 
 // Count pass with a workspace from `mem`; retries once with exact unit arrays when the first guess is
 // short.  On success *ws_out (still owned by the caller) holds the counted workspace.
 static int voxelize_count_pass(const svo_triangle *tris, uint32_t n_tris, uint32_t level, Mem &mem, void **ws_out,
-                               VoxWorkspace &w, uint64_t &total) {
+                               VoxWorkspace &w, uint64_t &total, uint64_t &units) {
 	uint64_t cap = vox_default_unit_cap(n_tris);
 	for (int attempt = 0; attempt < 2; ++attempt) {
 		void *ws = nullptr;
@@ -255,6 +285,7 @@ static int voxelize_count_pass(const svo_triangle *tris, uint32_t n_tris, uint32
 		}
 		*ws_out = ws;
 		total = tot[0];
+		units = tot[1];
 		return SVO_OK;
 	}
 	return fail(SVO_ERR_CAPACITY, "voxelize workspace retry failed");
@@ -268,8 +299,8 @@ int svo_voxelize_count(const svo_triangle *tris, uint32_t n_tris, uint32_t level
 	Mem mem{nullptr, (cudaStream_t)stream};
 	void *ws = nullptr;
 	VoxWorkspace w;
-	uint64_t total = 0;
-	if ((rc = voxelize_count_pass(tris, n_tris, level, mem, &ws, w, total))) return rc;
+	uint64_t total = 0, units = 0;
+	if ((rc = voxelize_count_pass(tris, n_tris, level, mem, &ws, w, total, units))) return rc;
 	mem.put(ws);
 	*count_host = total;
 	return SVO_OK;
@@ -284,8 +315,8 @@ int svo_voxelize_ex(const svo_triangle *tris, uint32_t n_tris, uint32_t level, c
 	Mem mem{alloc, s};
 	void *ws = nullptr;
 	VoxWorkspace w;
-	uint64_t total = 0;
-	if ((rc = voxelize_count_pass(tris, n_tris, level, mem, &ws, w, total))) return rc;
+	uint64_t total = 0, units = 0;
+	if ((rc = voxelize_count_pass(tris, n_tris, level, mem, &ws, w, total, units))) return rc;
 	if (total > 0xffffffffull) { // the reference's fragment count is a uint32 (src/Voxelizer.hpp:33)
 		mem.put(ws);
 		return fail(SVO_ERR_CAPACITY, "%llu fragments exceed the 32-bit fragment count", (unsigned long long)total);
@@ -307,7 +338,7 @@ int svo_voxelize_ex(const svo_triangle *tris, uint32_t n_tris, uint32_t level, c
 	out->level = level;
 	out->capacity = total;
 	out->owned = mem.owned();
-	out->reserved = 0;
+	out->units = (uint32_t)units;
 	return SVO_OK;
 }
 
@@ -316,14 +347,27 @@ int svo_voxelize(const svo_triangle *tris, uint32_t n_tris, uint32_t level, svo_
 }
 
 int svo_voxelize_into(const svo_triangle *tris, uint32_t n_tris, uint32_t level, uint64_t *frags, uint64_t capacity,
-                      uint64_t *count_dev, void *workspace, void *stream) {
+                      uint64_t *count_dev, void *workspace, size_t workspace_bytes, void *stream) {
 	int rc;
 	if ((rc = check_level(level)) || (rc = check_tris(tris, n_tris))) return rc;
 	if (!count_dev || !workspace || (capacity && !frags)) return fail(SVO_ERR_INVALID, "null argument");
 	if (!aligned(workspace, 256)) return fail(SVO_ERR_INVALID, "workspace must be 256-byte aligned");
-	cudaStream_t s = (cudaStream_t)stream;
 	VoxWorkspace w;
-	vox_workspace_layout(workspace, n_tris, vox_default_unit_cap(n_tris), w);
+	const size_t fixed = vox_workspace_layout(nullptr, n_tris, 0, w);
+	if (workspace_bytes < fixed)
+		return fail(SVO_ERR_CAPACITY, "workspace of %zu bytes is below the %zu this mesh needs", workspace_bytes, fixed);
+	// the most raster units whose layout fits in workspace_bytes (the layout grows with the capacity)
+	uint64_t lo = 0, hi = (workspace_bytes - fixed) / 8 + 1;
+	while (hi - lo > 1) {
+		const uint64_t mid = lo + (hi - lo) / 2;
+		if (vox_workspace_layout(nullptr, n_tris, mid, w) <= workspace_bytes)
+			lo = mid;
+		else
+			hi = mid;
+	}
+	const uint64_t cap = lo;
+	cudaStream_t s = (cudaStream_t)stream;
+	vox_workspace_layout(workspace, n_tris, cap, w);
 	SVO_CK(vox_launch_count(tris, n_tris, level, w, s), "voxelize count");
 	SVO_CK(vox_launch_totals(w, s), "voxelize totals");
 	SVO_CK(vox_launch_emit(tris, n_tris, level, w, frags, capacity, s), "voxelize emit");

@@ -1,0 +1,73 @@
+// Drives the C++ host classes (include/svo.hpp) through the whole path the way the reference's loader
+// thread and tracer do (src/LoaderThread.cpp:52-75, src/Application.cpp:144-152):
+//   Scene -> Voxelizer -> OctreeBuilder -> CmdBuild -> Octree::Update -> OctreeTracer::CmdDrawPipeline
+// Usage: wrapper_pipeline <triangles.bin> <level> <camera.bin (16 floats)> <width> <height> <out prefix>
+// Writes <out>.frags (uint64), <out>.pool (uint32, range words) and <out>.hits (svo_hit).
+#include <cstdio>
+#include <fstream>
+#include <iterator>
+#include <vector>
+
+#include "svo.hpp"
+
+template <typename T> static std::vector<T> read_file(const char *path) {
+	std::ifstream f(path, std::ios::binary);
+	std::vector<char> bytes((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+	std::vector<T> out(bytes.size() / sizeof(T));
+	std::memcpy(out.data(), bytes.data(), out.size() * sizeof(T));
+	return out;
+}
+
+template <typename T> static void write_file(const std::string &path, const std::vector<T> &v) {
+	std::ofstream f(path, std::ios::binary);
+	f.write(reinterpret_cast<const char *>(v.data()), (std::streamsize)(v.size() * sizeof(T)));
+}
+
+int main(int argc, char **argv) {
+	if (argc != 7) {
+		std::fprintf(stderr, "usage: %s tris level camera width height out\n", argv[0]);
+		return 2;
+	}
+	try {
+		const auto tris = read_file<svo_triangle>(argv[1]);
+		const uint32_t level = (uint32_t)std::atoi(argv[2]);
+		const auto camf = read_file<float>(argv[3]);
+		svo_camera cam;
+		std::memcpy(&cam, camf.data(), sizeof(cam));
+		const uint32_t width = (uint32_t)std::atoi(argv[4]), height = (uint32_t)std::atoi(argv[5]);
+		const std::string out = argv[6];
+
+		auto scene = svo::Scene::Create(tris);
+		auto voxelizer = svo::Voxelizer::Create(scene, level);
+		auto builder = svo::OctreeBuilder::Create(voxelizer);
+		builder->CmdBuild();
+		auto octree = svo::Octree::Create();
+		octree->Update(builder);
+		voxelizer->CmdVoxelize(); // record both passes again: same results
+		voxelizer->CheckEmission();
+		builder->CmdBuild();
+		octree->Update(builder);
+		auto tracer = svo::OctreeTracer::Create(octree, cam, width, height);
+		svo::DeviceBuffer hits(sizeof(svo_hit) * width * height, nullptr);
+		tracer->CmdDrawPipeline((svo_hit *)hits.get());
+
+		std::vector<uint64_t> frags(voxelizer->GetVoxelFragmentCount());
+		svo::Check(svo_download(frags.data(), voxelizer->GetVoxelFragmentList(), frags.size() * 8, 0, nullptr));
+		std::vector<uint32_t> pool(octree->GetRange() / 4);
+		svo::Check(svo_download(pool.data(), octree->GetBuffer(), octree->GetRange(), 0, nullptr));
+		std::vector<svo_hit> h(width * height);
+		svo::Check(svo_download(h.data(), hits.get(), h.size() * sizeof(svo_hit), 1, nullptr));
+		write_file(out + ".frags", frags);
+		write_file(out + ".pool", pool);
+		write_file(out + ".hits", h);
+		std::printf("fragments %u range %llu words levels", voxelizer->GetVoxelFragmentCount(),
+		            (unsigned long long)pool.size());
+		const svo_build_info &info = builder->GetInfo();
+		for (uint32_t d = 0; d < level; ++d) std::printf(" %u", info.level_nodes[d]);
+		std::printf("\n");
+	} catch (const svo::Error &e) {
+		std::fprintf(stderr, "%s\n", e.what());
+		return 1;
+	}
+	return 0;
+}

@@ -52,7 +52,8 @@ def test_pool_bound_and_workspace_sizes(lib):
         assert lib.svo_build_pool_bound(count, level) == oracle.pool_bound(count, level)
     cap = lib.svo_build_pool_bound(1000, 8)
     assert lib.svo_build_workspace_size(1000, 8, cap, 0) > lib.svo_build_workspace_size(1000, 8, cap, 64) > 4000
-    assert lib.svo_voxelize_workspace_size(1000) > 8 * 1000
+    assert lib.svo_voxelize_workspace_size(1000, 0) > 8 * 1000
+    assert lib.svo_voxelize_workspace_size(1000, 10**6) > lib.svo_voxelize_workspace_size(1000, 0)
 
 
 def test_camera_from_angles_matches_python(lib):

@@ -331,3 +331,18 @@ def test_camera_image_sizes_not_multiple_of_the_tile(cuda, size):
     assert (raw[n * 32:] == 0xAB).all()  # nothing written past the last pixel
     got = raw[: n * 32].view(np.uint8).view(HIT_DTYPE)
     assert_hits_equal(got, oracle.raycast(pool, s.level, oracle.camera_rays(cam, w, h)))
+
+
+def test_voxelizer_reemission_needs_exact_unit_scratch(cuda):
+    """The room scene's walls and cylinders need more raster units than the default guess: re-emission
+    (CmdVoxelize) must use the unit count from the first pass and reproduce every fragment."""
+    api = _api()
+    s = scenes.room_1024()
+    v = api.Voxelizer.Create(s.tris, s.level)
+    first = v.GetVoxelFragmentList().clone()
+    assert v.m_units > 2 * len(s.tris) + 65536  # more than the default guess
+    v.GetVoxelFragmentList().fill_(0)
+    v.CmdVoxelize()
+    v.CheckEmission()
+    import torch
+    assert torch.equal(v.GetVoxelFragmentList(), first)
