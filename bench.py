@@ -116,7 +116,6 @@ def algorithmic_bytes(kernel: str, w: dict) -> float | None:
     leaf_words = w["leaf_words"]
     table = {
         "vox_classify_scan": 48.0 * T + 12.0 * T,     # triangles in, offsets out
-        "vox_emit": 48.0 * T + 8.0 * F,               # triangles in, fragments out
         "dense_mark": 8.0 * F,                        # the fragment list, read once
         "build_tag": 8.0 * F,                         # one sparse level: the fragment list
         "build_tag_leaf": 8.0 * F + 8.0 * F,          # fragments in, one 8 B accumulator update each

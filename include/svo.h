@@ -197,8 +197,8 @@ void svo_fraglist_destroy(svo_fraglist *f, void *stream);
  * fragments) and count_dev (device, 2 x uint64: [0] fragments produced, [1] status, 0 = complete); the
  * engine's scratch is a fixed 16 MiB array in device memory that every GPU loading this library holds
  * until the process exits.  It takes at most 262,144 triangles (more: SVO_ERR_CAPACITY, nothing
- * launched) whose large triangles split into at most about 1.5 million raster units (a 1024 x 1024
- * wall is 4,096; beyond the limit count_dev[1] is non-zero and svo_voxelize must be used).  No
+ * launched) whose large triangles split into at most about 1 million raster units (1,047,808 at the
+ * triangle limit, up to 1.29 million for small meshes; a 1024 x 1024 wall is 4,096; beyond the limit count_dev[1] is non-zero and svo_voxelize must be used).  No
  * allocation call is made.  The first call on a device looks up that array's address; make that first
  * call before any stream capture.  All calls share the array: calls whose work overlaps on the GPU
  * (other streams, other host threads) race and must be serialized by the caller. */

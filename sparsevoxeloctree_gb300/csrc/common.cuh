@@ -118,13 +118,20 @@ SVO_DEV unsigned long long tile_lookback_warp(unsigned long long *descs, uint32_
 // ------------------------------------------------------------------------------- integer helpers
 // floor(num / den) for den > 0, exact whenever the exact quotient lies in [lo - 2, hi + 2]; outside
 // that window the result lies outside [lo, hi] on the same side as the exact quotient, which is all a
-// caller that clamps to [lo, hi] needs.  A float estimate (relative error ~2^-22, quotients here stay
-// below 2^14 in magnitude) is within one of the exact floor and is corrected with one exact remainder.
+// caller that clamps to [lo, hi] needs.  The estimate uses 32-bit arithmetic only (64-bit integer <->
+// float conversions run on the FP64 pipe, which is narrow on this part): num and den are shifted right
+// by the same amount until both fit 31 bits, which keeps their ratio.  Inside the window (|quotient| <
+// 2^13) den then keeps at least 17 significant bits, so the float quotient is within 0.01 of the exact
+// one; its floor is corrected by one exact int64 remainder.  (A den shifted to 0 means a quotient of
+// magnitude >= 2^30: the infinite estimate clamps to the correct side.)
 SVO_DEV int64_t floor_div_window(int64_t num, int64_t den, int32_t lo, int32_t hi) {
-	float est = floorf(__fdividef(__ll2float_rn(num), __ll2float_rn(den)));
+	const uint64_t mag = (uint64_t)(num < 0 ? -num : num) | (uint64_t)den;
+	const int sh = max(0, 33 - __clzll((long long)mag)); // bits(mag) - 31
+	const float nf = (float)(int32_t)(num >> sh), df = (float)(int32_t)(den >> sh);
+	float est = floorf(__fdividef(nf, df));
 	est = fminf(fmaxf(est, (float)(lo - 2)), (float)(hi + 2));
-	int64_t q = (int64_t)est;
-	int64_t r = num - q * den;
+	int64_t q = (int32_t)est;
+	const int64_t r = num - q * den;
 	if (r < 0)
 		q -= 1;
 	else if (r >= den)

@@ -16,8 +16,9 @@
 namespace svo {
 
 // Scratch for up to kStaticMaxTris triangles: (n+1) fragment offsets (8 B), (n+1) unit offsets (4 B),
-// scan descriptors and counters; everything left over holds raster units of large triangles (8 B
-// each; a room wall at level 10 is 4,096 units, the 262,144-triangle room scene about 0.7M).
+// scan descriptors and counters; everything left over holds raster units of large triangles (12 B
+// each; a room wall at level 10 is 4,096 units, the 262,144-triangle room scene 963,479 of the 1,047,808
+// that fit beside 262,144 triangles).
 constexpr uint32_t kStaticMaxTris = 262144;
 constexpr size_t kStaticScratchBytes = 16u << 20; // 16 MiB
 
@@ -25,7 +26,7 @@ constexpr size_t kStaticScratchBytes = 16u << 20; // 16 MiB
 static uint64_t static_unit_cap(uint32_t n) {
 	VoxWorkspace w;
 	const size_t fixed = vox_workspace_layout(nullptr, n, 0, w);
-	uint64_t cap = (kStaticScratchBytes - fixed) / 9;
+	uint64_t cap = (kStaticScratchBytes - fixed) / 13;
 	while (cap > 0 && vox_workspace_layout(nullptr, n, cap, w) > kStaticScratchBytes) cap -= cap > 4096 ? 4096 : cap;
 	return cap;
 }

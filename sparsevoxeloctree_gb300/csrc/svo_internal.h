@@ -48,6 +48,7 @@ struct VoxWorkspace {
 	uint64_t *small_off;           // [n+1] fragment offsets of small triangles
 	uint32_t *unit_off;            // [n+1] unit offsets of large triangles
 	unsigned long long *unit_frag; // [unit_cap+1] fragment offset of each unit inside the large region
+	uint32_t *unit_tri;            // [unit_cap+1] triangle of each unit
 	unsigned long long *descs, *descs2, *descs3; // look-back descriptors of the three scans
 	size_t desc_bytes;
 	uint32_t *counters;            // tile tickets, status

@@ -217,6 +217,33 @@ SVO_DEV uint32_t upper_index(const uint32_t *__restrict__ a, uint32_t n, uint32_
 	return lo;
 }
 
+// Warp-wide version for a warp-uniform x, with the invariant a[lo] <= x < a[hi]: each step probes 32
+// evenly spaced entries at once and keeps the gap the ballot points at (4 dependent loads for n = 2^18).
+SVO_DEV uint32_t warp_upper_index(const uint32_t *__restrict__ a, uint32_t lo, uint32_t hi, uint32_t x) {
+	const uint32_t lane = lane_id();
+	while (hi - lo > 1) {
+		const uint32_t step = (hi - lo + 31) / 32;
+		const uint32_t p = lo + lane * step;
+		const bool le = p < hi && __ldg(a + p) <= x;
+		const uint32_t c = __popc(__ballot_sync(kFullMask, le)); // >= 1: lane 0 probes lo
+		lo += (c - 1) * step;
+		hi = min(hi, lo + step);
+	}
+	return lo;
+}
+
+// Per-lane search inside [lo, hi) with a[lo] <= x < a[hi] (a short range that sits in L1).
+SVO_DEV uint32_t upper_index_in(const uint32_t *__restrict__ a, uint32_t lo, uint32_t hi, uint32_t x) {
+	while (hi - lo > 1) {
+		const uint32_t mid = (lo + hi) >> 1;
+		if (__ldg(a + mid) <= x)
+			lo = mid;
+		else
+			hi = mid;
+	}
+	return lo;
+}
+
 // ---------------------------------------------------------------------------------------------------
 constexpr int kTPB = 256;
 constexpr int kIPT = 2;
@@ -299,12 +326,21 @@ __global__ void __launch_bounds__(kTPB) vox_unit_scan(const svo_triangle *__rest
 		if (tile >= ntiles) break;
 		uint32_t len[kIPT];
 		unsigned long long local = 0;
+		// the warp's kIPT * 32 consecutive units lie in triangles [t_first, t_last]
+		const uint32_t u_first = tile * kTile + (threadIdx.x & ~31u) * kIPT;
+		uint32_t t_first = 0, t_end = 0;
+		if (u_first < units) {
+			const uint32_t u_last = min(u_first + 32 * kIPT - 1, units - 1);
+			t_first = warp_upper_index(w.unit_off, 0, n, u_first);
+			t_end = warp_upper_index(w.unit_off, t_first, n, u_last) + 1;
+		}
 #pragma unroll
 		for (int k = 0; k < kIPT; ++k) {
 			const uint32_t u = tile * kTile + threadIdx.x * kIPT + k;
 			len[k] = 0;
 			if (u < units) {
-				const uint32_t t = upper_index(w.unit_off, n, u);
+				const uint32_t t = upper_index_in(w.unit_off, t_first, t_end, u);
+				w.unit_tri[u] = t;
 				TriSetup s;
 				tri_setup(tris, t, level, s);
 				int32_t v, lo, hi;
@@ -333,36 +369,141 @@ __global__ void __launch_bounds__(kTPB) vox_unit_scan(const svo_triangle *__rest
 	if (ntiles == 0 && blockIdx.x == 0 && threadIdx.x == 0) w.unit_frag[0] = 0;
 }
 
-// Emission: threads [0, n) write small triangles, threads [n, n + units) write units.
+// Emission of small triangles: one lane per triangle, its fragments in order at its offset.
 __global__ void __launch_bounds__(kTPB) vox_emit(const svo_triangle *__restrict__ tris, uint32_t n, uint32_t level,
                                                  VoxWorkspace w, uint64_t *__restrict__ frags, uint64_t capacity) {
+	for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+		const uint64_t off = w.small_off[i], end = w.small_off[i + 1];
+		if (end == off || end > capacity) continue;
+		TriSetup s;
+		tri_setup(tris, (uint32_t)i, level, s);
+		if (s.valid && !is_large(s)) emit_serial(s, frags + off);
+	}
+}
+
+// Float value of num / den (den > 0, |num| <= den here) from the top 31 bits of both: 32-bit
+// conversions only; relative error a few 2^-24.
+SVO_DEV float ratio_f(int64_t num, int64_t den) {
+	const uint64_t mag = (uint64_t)(num < 0 ? -num : num) | (uint64_t)den;
+	const int sh = max(0, 33 - __clzll((long long)mag));
+	return (float)(int32_t)(num >> sh) / (float)(int32_t)(den >> sh);
+}
+
+// One unit, prepared by the lane that owns it for the lanes that write its fragments.  Fragment k of
+// the unit is pixel u = lo + k of span v with plane depth q0 + (r0 - k NU) / D, r0 = num0 - q0 D in
+// [0, D); t = fr0 - k fb approximates (r0 - k NU) / D within 1e-4 (fr0, fb: the two ratios in float),
+// so floor(t) is exact unless t lies within kDepthEps of an integer, where the exact int64 division
+// decides.  The fragment words are base | u and z placed in their packed fields.
+struct UnitRec {
+	float fr0, fb;
+	int32_t q0, lo;
+	int32_t excl, z0, z1;
+	uint32_t fields; // u shift | z shift << 8 | (u is the split z field) << 16 | (z is) << 17
+	uint32_t base_lo, base_hi;
+	int64_t num0, nu, d;
+};
+constexpr float kDepthEps = 1.0f / 1024.0f;
+
+SVO_DEV uint32_t field_of(int axis, int which) { return (uint32_t)((axis + which) % 3); } // 0 i, 1 j, 2 depth
+
+// Emission of large-triangle units, 32 consecutive units per warp.  Their fragments are contiguous in
+// the output, so the warp writes them together: lane k takes fragments k, k+32, ... of the group (each
+// store instruction covers 256 contiguous bytes), finds the unit holding its fragment and evaluates it
+// from that unit's record.
+__global__ void __launch_bounds__(kTPB, 4) vox_emit_units(const svo_triangle *__restrict__ tris, uint32_t n,
+                                                       uint32_t level, VoxWorkspace w, uint64_t *__restrict__ frags,
+                                                       uint64_t capacity) {
+	__shared__ UnitRec s_rec[kTPB];
+	__shared__ uint32_t s_incl[kTPB];
 	const uint32_t units = w.unit_off[n];
+	if (units > w.unit_cap) return; // reported by the count; nothing sensible to emit
 	const uint64_t small_total = w.small_off[n];
-	const uint64_t items = (uint64_t)n + (units <= w.unit_cap ? units : 0u);
-	for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < items; i += (uint64_t)gridDim.x * blockDim.x) {
-		if (i < n) {
-			const uint64_t off = w.small_off[i], end = w.small_off[i + 1];
-			if (end == off || end > capacity) continue;
-			TriSetup s;
-			tri_setup(tris, (uint32_t)i, level, s);
-			if (s.valid && !is_large(s)) emit_serial(s, frags + off);
-		} else {
-			const uint32_t u = (uint32_t)(i - n);
-			const uint64_t off = small_total + w.unit_frag[u], end = small_total + w.unit_frag[u + 1];
-			if (end == off || end > capacity) continue;
-			const uint32_t t = upper_index(w.unit_off, n, u);
-			TriSetup s;
-			tri_setup(tris, t, level, s);
+	const uint32_t lane = lane_id();
+	const int32_t R = 1 << level;
+	const UnitRec *warp_rec = s_rec + (threadIdx.x & ~31u);
+	const uint32_t *warp_incl = s_incl + (threadIdx.x & ~31u);
+	const uint64_t warps = (uint64_t)gridDim.x * blockDim.x / 32;
+	for (uint64_t g = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32; g * 32 < units; g += warps) {
+		const uint64_t u = g * 32 + lane;
+		uint32_t len = 0;
+		if (u < units) {
+			const uint32_t t = w.unit_tri[u];
+			TriSetup S;
+			tri_setup(tris, t, level, S);
 			int32_t v, lo, hi;
-			unit_interval(s, u - w.unit_off[t], v, lo, hi);
-			uint64_t *out = frags + off;
-			for (int32_t x = lo; x <= hi; ++x) *out++ = make_fragment(s, x, v);
+			unit_interval(S, (uint32_t)u - w.unit_off[t], v, lo, hi);
+			if (hi >= lo) {
+				len = (uint32_t)(hi - lo + 1);
+				UnitRec &rec = s_rec[threadIdx.x];
+				const int64_t num0 = S.K - S.NU * lo - S.NV * v;
+				const int64_t q0 = floor_div_window(num0, S.D, -2, R + 2);
+				rec.q0 = (int32_t)q0;
+				rec.fr0 = ratio_f(num0 - q0 * S.D, S.D);
+				rec.fb = ratio_f(S.NU, S.D);
+				rec.lo = lo;
+				rec.z0 = S.z0;
+				rec.z1 = S.z1;
+				rec.num0 = num0;
+				rec.nu = S.NU;
+				rec.d = S.D;
+				// coordinate fields: i -> (axis+1)%3, j -> (axis+2)%3, depth -> axis (0 x, 1 y, 2 z)
+				const uint32_t fi = field_of(S.axis, 1), fj = field_of(S.axis, 2), fz = field_of(S.axis, 0);
+				const uint32_t fu = S.cols ? fj : fi, fv = S.cols ? fi : fj;
+				rec.fields = (12u * fu) | ((12u * fz) << 8) | ((fu == 2u) << 16) | ((fz == 2u) << 17);
+				const uint32_t vv = (uint32_t)v;
+				rec.base_lo = vv << (12u * fv);
+				rec.base_hi = (S.rgb & 0xffffffu) | (fv == 2u ? (vv >> 8) << 28 : 0u);
+			}
 		}
+		const uint32_t incl = warp_inclusive_sum(len);
+		const uint32_t total = __shfl_sync(kFullMask, incl, 31);
+		s_incl[threadIdx.x] = incl;
+		s_rec[threadIdx.x].excl = (int32_t)(incl - len);
+		__syncwarp();
+		const uint64_t first = small_total + (uint64_t)w.unit_frag[g * 32];
+		uint64_t *out = frags + first;
+		const uint64_t room = first < capacity ? capacity - first : 0;
+		uint32_t j = 0, have = 32;
+		int32_t k = 0, q0 = 0, lo = 0, z0 = 0, z1 = 0;
+		float kf = 0.0f, fr0 = 0.0f, fb = 0.0f;
+		uint32_t ush = 0, zsh = 0, usplit = 0, zsplit = 0, base_lo = 0, base_hi = 0;
+		for (uint32_t f = lane; f < total; f += 32) {
+			while (warp_incl[j] <= f) ++j;
+			if (j != have) {
+				const UnitRec &rec = warp_rec[j];
+				k = (int32_t)(f - (uint32_t)rec.excl);
+				kf = (float)k;
+				fr0 = rec.fr0, fb = rec.fb, q0 = rec.q0, lo = rec.lo, z0 = rec.z0, z1 = rec.z1;
+				ush = rec.fields & 0xffu, zsh = (rec.fields >> 8) & 0xffu;
+				usplit = 0u - ((rec.fields >> 16) & 1u), zsplit = 0u - ((rec.fields >> 17) & 1u);
+				base_lo = rec.base_lo, base_hi = rec.base_hi;
+				have = j;
+			} else {
+				k += 32;
+				kf += 32.0f;
+			}
+			const float tf = fmaf(-kf, fb, fr0);
+			const float fl = floorf(tf);
+			const float fr = tf - fl;
+			int32_t z;
+			if (fr >= kDepthEps && fr <= 1.0f - kDepthEps) {
+				z = q0 + (int32_t)fl;
+			} else {
+				const UnitRec &rec = warp_rec[j];
+				z = (int32_t)floor_div_window(rec.num0 - (int64_t)k * rec.nu, rec.d, -2, R + 2);
+			}
+			const uint32_t zz = (uint32_t)(z < z0 ? z0 : (z > z1 ? z1 : z)), uu = (uint32_t)(lo + k);
+			const uint32_t flo = base_lo | (uu << ush) | (zz << zsh);
+			const uint32_t fhi = base_hi | (((uu >> 8) << 28) & usplit) | (((zz >> 8) << 28) & zsplit);
+			if (f < room) out[f] = (uint64_t)flo | ((uint64_t)fhi << 32);
+		}
+		__syncwarp();
 	}
 }
 
 // ---------------------------------------------------------------------------------------------------
-// Workspace: small_off[n+1] u64 | unit_off[n+1] u32 | unit_frag[unit_cap+1] u64 | 3 descriptor arrays |
+// Workspace: small_off[n+1] u64 | unit_off[n+1] u32 | unit_frag[unit_cap+1] u64 | unit_tri[unit_cap+1] u32 |
+// 3 descriptor arrays |
 // counters.  unit_cap is a first guess; a larger unit total makes the count report it and the caller
 // retries with vox_workspace_bytes(n, units).
 uint64_t vox_default_unit_cap(uint32_t n) { return 2ull * n + 65536; }
@@ -387,6 +528,7 @@ size_t vox_workspace_layout(void *ws, uint32_t n, uint64_t unit_cap, VoxWorkspac
 	w.small_off = (uint64_t *)take(sizeof(uint64_t) * ((size_t)n + 1));
 	w.unit_off = (uint32_t *)take(sizeof(uint32_t) * ((size_t)n + 1));
 	w.unit_frag = (unsigned long long *)take(sizeof(unsigned long long) * (size_t)(unit_cap + 1));
+	w.unit_tri = (uint32_t *)take(sizeof(uint32_t) * (size_t)(unit_cap + 1));
 	const size_t t1 = tiles_for(n), t3 = tiles_for(unit_cap);
 	w.descs = (unsigned long long *)(p + off);
 	w.desc_bytes = align_up((2 * t1 + t3) * sizeof(unsigned long long), 256);
@@ -421,6 +563,8 @@ cudaError_t vox_launch_emit(const svo_triangle *tris, uint32_t n, uint32_t level
 	if (n == 0) return cudaSuccess;
 	const int sms = device_sm_count();
 	SVO_LAUNCH("vox_emit", stream, vox_emit<<<(uint32_t)sms * 16, kTPB, 0, stream>>>(tris, n, level, w, frags, capacity););
+	SVO_LAUNCH("vox_emit_units", stream,
+	           vox_emit_units<<<(uint32_t)sms * 8, kTPB, 0, stream>>>(tris, n, level, w, frags, capacity););
 	return cudaGetLastError();
 }
 
