@@ -118,13 +118,31 @@ def algorithmic_bytes(kernel: str, w: dict) -> float | None:
         "vox_classify_scan": 48.0 * T + 12.0 * T,     # triangles in, offsets out
         "dense_mark": 8.0 * F,                        # the fragment list, read once
         "build_tag": 8.0 * F,                         # one sparse level: the fragment list
-        "build_tag_leaf": 8.0 * F + 8.0 * F,          # fragments in, one 8 B accumulator update each
+        "build_leaf": 8.0 * F + 8.0 * F,              # fragments in, one 8 B accumulator update each
         "build_finalize": 12.0 * leaf_words,          # 8 B accumulator in, 4 B leaf word out
         "dense_write": 4.0 * (w["range_words"] - leaf_words),  # interior words out
         "march_camera": n * (32.0 + 4.0 * k),         # hit out + node words fetched (rays made in-kernel)
         "march_rays": n * (24.0 + 32.0 + 4.0 * k),
     }
     return table.get(kernel)
+
+
+# ncu kernel names of the profile labels whose captures are committed under profiles/
+PROFILE_FILES = {"build_leaf": "build_leaf", "march_camera": "march_kernel", "vox_emit_units": "vox_emit_units"}
+
+
+def profiled_traffic(label: str, workload: str) -> dict:
+    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the kernel, from its
+    committed ncu capture on this workload (profiles/<kernel>_<workload>.md), or null without one."""
+    name = PROFILE_FILES.get(label)
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles", f"{name}_{workload}.md")
+    if name is None or not os.path.exists(path):
+        return {"traffic": None}
+    with open(path) as f:
+        for line in f:
+            if line.startswith("dram_bytes_per_launch:"):
+                return {"traffic": int(line.split(":", 1)[1]), "traffic_source": os.path.relpath(path)}
+    return {"traffic": None}
 
 
 def engine_arm(args, rank: int, world: int, device) -> dict:
@@ -218,7 +236,7 @@ def engine_arm(args, rank: int, world: int, device) -> dict:
     if alg is not None:
         ach = alg / (dom_launch_ms * 1e-3) / 1e9
         roofline.update({"achieved": ach, "frac": ach / peaks["hbm_gbs"], "algorithmic_bytes_per_launch": alg})
-    roofline["traffic"] = None  # filled from the committed ncu capture (profiles/), not measured live
+    roofline.update(profiled_traffic(dom_name, args.workload))
 
     stages = {
         "voxelize_ms": vox_ms, "build_ms": build_ms, "march_ms": march_ms,

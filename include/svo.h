@@ -81,7 +81,10 @@ typedef struct svo_camera {
  *   node     the leaf word that was hit (0 on a miss); colour = node & 0xffffff (R low byte)
  *   iter     loop iterations (o_iter of the reference)
  *   voxel    leaf coordinates at the octree level (0xffff on a miss)
- *   flags    bit0 hit; bits1-2 normal axis (0=x,1=y,2=z); bit3 normal points to -axis */
+ *   flags    bit0 hit; bits1-2 normal axis (0=x,1=y,2=z); bit3 normal points to -axis;
+ *            bit4 the march was aborted (a child pointer outside the pool's range, an interior word
+ *            below the octree level, or SVO_MARCH_MAX_ITER iterations): the pool is malformed and the
+ *            ray counts as a miss.  A pool made by svo_build never sets it. */
 typedef struct svo_hit {
 	float t;
 	float pos[3];
@@ -94,6 +97,7 @@ typedef struct svo_hit {
 #define SVO_HIT_FLAG_HIT 1u
 #define SVO_HIT_NORMAL_AXIS(f) (((f) >> 1) & 3u)
 #define SVO_HIT_NORMAL_NEG 8u
+#define SVO_HIT_FLAG_ABORTED 16u
 
 /* A voxel-fragment list (device memory). data holds `count` uint64 fragments: low word = fragment.x,
  * high word = fragment.y (the reference's uvec2 layout). */

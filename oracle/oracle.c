@@ -572,13 +572,20 @@ static void march_one(const uint32_t *pool, uint64_t range, uint32_t level, cons
 	uint32_t scale = SVO_STACK_SIZE - 1;
 	float scale_exp2 = 0.5f;
 
+	/* Malformed pools stop the ray as an aborted miss (the engine's guard; the shader has none):
+	 * a pointer outside the pool, an interior word below the octree level, or the iteration bound. */
+	int aborted = 0;
+	const uint32_t min_scale = SVO_STACK_SIZE - level;
 	while (scale < SVO_STACK_SIZE) {
-		if (iter >= SVO_MARCH_MAX_ITER) /* bound for malformed pools; never reached on a valid octree */
+		if (iter >= SVO_MARCH_MAX_ITER) { /* never reached on a valid octree */
+			aborted = 1;
 			break;
+		}
 		++iter;
 		if (cur == 0u) {
 			uint64_t w = (uint64_t)parent + (idx ^ oct_mask);
-			if (w >= range) { /* pointer outside the pool: stop as a miss */
+			if (w >= range) {
+				aborted = 1;
 				scale = 0xffffffffu;
 				break;
 			}
@@ -597,6 +604,11 @@ static void march_one(const uint32_t *pool, uint64_t range, uint32_t level, cons
 				t_center[k] = half * coef[k] + tc[k];
 			if ((cur & 0x40000000u) != 0)
 				break; /* leaf */
+			if (scale <= min_scale) { /* interior word at the leaf level */
+				aborted = 1;
+				scale = 0xffffffffu;
+				break;
+			}
 			if (tc_max < h) /* push */
 				stack[scale] = parent;
 			h = tc_max;
@@ -664,11 +676,11 @@ static void march_one(const uint32_t *pool, uint64_t range, uint32_t level, cons
 			v = norm[k] > 0.0f ? pos[k] + scale_exp2 + MARCH_EPS * 2.0f : pos[k] - MARCH_EPS;
 		hit->pos[k] = v;
 	}
-	int is_hit = scale < SVO_STACK_SIZE && t_min <= t_max;
+	int is_hit = !aborted && scale < SVO_STACK_SIZE && t_min <= t_max;
 	hit->t = t_min;
 	hit->iter = iter;
 	hit->flags = (uint16_t)((is_hit ? SVO_HIT_FLAG_HIT : 0u) | ((uint32_t)nax << 1) |
-	                        (norm[nax] < 0.0f ? SVO_HIT_NORMAL_NEG : 0u));
+	                        (norm[nax] < 0.0f ? SVO_HIT_NORMAL_NEG : 0u) | (aborted ? SVO_HIT_FLAG_ABORTED : 0u));
 	if (is_hit) {
 		hit->node = cur;
 		float res = (float)(1u << level);

@@ -668,7 +668,7 @@ cudaError_t build_launch_leaf(const uint64_t *frags, uint32_t count, uint32_t le
 	if (w.acc) {
 		SVO_LAUNCH("build_leaf_zero", stream,
 		           build_leaf_zero<<<(uint32_t)sms * 8, kTPB, 0, stream>>>(w.acc, w.leaf_slots, w.state, level););
-		SVO_LAUNCH("build_tag_leaf", stream,
+		SVO_LAUNCH("build_leaf", stream,
 		           build_leaf<<<tag_blocks, kTPB, 0, stream>>>(frags, count, level, pool, w.cache, w.acc, w.dv, w.state););
 		SVO_LAUNCH("build_finalize", stream,
 		           build_finalize<false><<<(uint32_t)sms * 8, kTPB, 0, stream>>>(pool, w.acc, w.state, level););
@@ -677,7 +677,7 @@ cudaError_t build_launch_leaf(const uint64_t *frags, uint32_t count, uint32_t le
 		// exact colours for voxels with more than 257 fragments; these launches return at once otherwise
 		SVO_LAUNCH("build_wide_zero", stream,
 		           build_wide_zero<<<(uint32_t)sms * 4, kTPB, 0, stream>>>(w.acc_wide, w.state, level););
-		SVO_LAUNCH("build_tag_leaf_wide", stream,
+		SVO_LAUNCH("build_leaf_wide", stream,
 		           build_tag<kTagLeafWide><<<tag_blocks, kTPB, 0, stream>>>(frags, count, level, level, pool, w.cache,
 		                                                                    w.acc_wide, w.dv, w.state, vec_ok););
 		SVO_LAUNCH("build_finalize_wide", stream,

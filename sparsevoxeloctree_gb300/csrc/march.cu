@@ -78,15 +78,20 @@ SVO_DEV void march_ray(const uint32_t *__restrict__ pool, uint32_t range, uint32
 	uint32_t scale = SVO_STACK_SIZE - 1;
 	float scale_exp2 = 0.5f;
 	uint32_t iter = 0;
+	bool aborted = false; // pointer outside the pool, tree deeper than its level, or iteration bound
 	const uint32_t min_scale = SVO_STACK_SIZE - level; // deepest scale a valid tree reaches
 
 	while (scale < SVO_STACK_SIZE) {
-		if (iter >= SVO_MARCH_MAX_ITER) break;
+		if (iter >= SVO_MARCH_MAX_ITER) {
+			aborted = true;
+			break;
+		}
 		++iter;
 		if (cur == 0u) {
 			const uint32_t w = parent + (idx ^ oct_mask);
 			if (w >= range) {
 				atomicOr(status, kStatusMalformed);
+				aborted = true;
 				scale = 0xffffffffu;
 				break;
 			}
@@ -106,6 +111,7 @@ SVO_DEV void march_ray(const uint32_t *__restrict__ pool, uint32_t range, uint32
 			if ((cur & 0x40000000u) != 0u) break; // leaf
 			if (scale <= min_scale) {              // interior node below the leaf level: malformed pool
 				atomicOr(status, kStatusMalformed);
+				aborted = true;
 				scale = 0xffffffffu;
 				break;
 			}
@@ -171,10 +177,11 @@ SVO_DEV void march_ray(const uint32_t *__restrict__ pool, uint32_t range, uint32
 		if ((uint32_t)k == nax) v = neg ? pos[k] - kEps : pos[k] + scale_exp2 + kEps * 2.0f;
 		out.pos[k] = v;
 	}
-	const bool hit = scale < SVO_STACK_SIZE && t_min <= t_max;
+	const bool hit = !aborted && scale < SVO_STACK_SIZE && t_min <= t_max;
 	out.t = t_min;
 	out.iter = iter;
-	const uint32_t flags = (hit ? SVO_HIT_FLAG_HIT : 0u) | (nax << 1) | (neg ? SVO_HIT_NORMAL_NEG : 0u);
+	const uint32_t flags = (hit ? SVO_HIT_FLAG_HIT : 0u) | (nax << 1) | (neg ? SVO_HIT_NORMAL_NEG : 0u) |
+	                       (aborted ? SVO_HIT_FLAG_ABORTED : 0u);
 	if (hit) {
 		const float res = (float)(1u << level);
 		const uint32_t vx = (uint32_t)((pos[0] - 1.0f) * res), vy = (uint32_t)((pos[1] - 1.0f) * res);

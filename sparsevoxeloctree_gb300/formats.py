@@ -31,6 +31,7 @@ STACK_SIZE = 23
 
 HIT_FLAG_HIT = 1
 HIT_NORMAL_NEG = 8
+HIT_FLAG_ABORTED = 16  # malformed pool: pointer outside the range, interior word below the level, or the iteration bound
 
 NODE_NONEMPTY = 0x80000000
 NODE_LEAF = 0x40000000

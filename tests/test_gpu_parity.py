@@ -228,6 +228,41 @@ def test_march_random_rays_many_levels(cuda):
         assert_hits_equal(gpu_trace(o, rays), oracle.raycast(pool, level, rays))
 
 
+def test_march_malformed_pools_are_flagged(cuda):
+    """Pools no build produces: child pointers past the range, interior words at the leaf level, a
+    cycle back to the root block.  Every read stays inside the range (checked before the load); such rays
+    end as misses with the aborted flag, identically to the oracle; rays into valid leaves still hit."""
+    import torch
+
+    from sparsevoxeloctree_gb300.formats import HIT_FLAG_ABORTED, HIT_FLAG_HIT
+    api = _api()
+    leaf = 0xC1000000 | 0x123456
+    far = 0x80000000 | 0x0FFF0000
+    cases = [
+        (3, [far] * 8),                                        # pointers past the range
+        (2, [0x80000008] * 8 + [0x80000008] * 8),              # interior word at the leaf level
+        (3, [0x80000000] * 8),                                 # cycle to the root block
+        (2, [leaf, far, 0, 0x80000008, leaf, 0, far, 0x80000008] + [leaf, 0, 0, 0, 0, 0, 0, 0x80000000]),
+    ]
+    g = np.random.default_rng(17)
+    o1, d1 = scenes.random_rays(g, 4000)
+    o2, d2 = scenes.random_rays(g, 4000, inside=True)
+    rays = rays_from_arrays(np.concatenate([o1, o2]), np.concatenate([d1, d2]))
+    aborted_total = 0
+    for level, words in cases:
+        pool = np.array(words, np.uint32)
+        o = api.Octree()
+        o.m_buffer = torch.from_numpy(pool.view(np.int32)).cuda()
+        o.m_range = 4 * len(pool)
+        o.m_level = level
+        got = gpu_trace(o, rays)
+        assert_hits_equal(got, oracle.raycast(pool, level, rays))
+        ab = (got["flags"] & HIT_FLAG_ABORTED) != 0
+        assert not np.any(ab & ((got["flags"] & HIT_FLAG_HIT) != 0))
+        aborted_total += int(ab.sum())
+    assert aborted_total > 0
+
+
 def test_camera_golden(cuda, golden_dir):
     """Primary-ray directions: oracle == reference Camera_GenRay (fixture); the GPU march over camera
     rays equals the march over the oracle's explicit rays."""
