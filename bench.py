@@ -164,7 +164,7 @@ def engine_arm(args, rank: int, world: int, device) -> dict:
     F = vox.GetVoxelFragmentCount()
     builder = api.OctreeBuilder.Create(vox)
     builder.CmdBuild()
-    builder.Reserve()  # scratch sized to this scene's leaf level
+    builder.Reserve()  # pool sized to this scene's exact range
     builder.CmdBuild()
     octree = api.Octree.Create()
     octree.Update(builder)

@@ -224,11 +224,11 @@ int svo_build_fraglist(const svo_fraglist *f, svo_octree *out, svo_build_info *i
 /* Build into a caller pool (no allocation, no host synchronisation).  pool (device, 16-byte aligned)
  * holds `capacity` words (svo_build_pool_bound(count, level) always suffices); `workspace` (device,
  * 256-byte aligned) holds `workspace_bytes` bytes, at least svo_build_workspace_size(count, level,
- * capacity, leaf_words) where leaf_words is the number of words of the deepest level (known from an
- * earlier build of the same fragments, e.g. 8 x level_nodes[level-2] of its svo_build_info) or 0 for
- * the worst case.  The result (svo_build_info followed by a uint32 status word, 0 = complete) is
- * written to `result_dev` (device).  A workspace too small for the leaf level reports SVO_ERR_CAPACITY
- * through the status word. */
+ * capacity, leaf_words) (about 12 bytes per fragment plus the dense bitmaps; `leaf_words` is accepted
+ * for compatibility and no longer changes the size: the leaf level accumulates in on-chip memory).
+ * The result (svo_build_info followed by a uint32 status word, 0 = complete) is written to
+ * `result_dev` (device).  A pool too small for the octree reports SVO_ERR_CAPACITY through the status
+ * word; a workspace below svo_build_workspace_size is rejected before any launch. */
 size_t svo_build_workspace_size(uint32_t count, uint32_t level, uint64_t capacity, uint64_t leaf_words);
 uint64_t svo_build_pool_bound(uint32_t count, uint32_t level);
 int svo_build_into(const uint64_t *frags, uint32_t count, uint32_t level, uint32_t *pool, uint64_t capacity,

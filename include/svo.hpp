@@ -142,6 +142,17 @@ public:
 		stream_ = stream;
 	}
 
+	// Shrinks the node pool to the exact range of the last build (blocking); later CmdBuild calls on the
+	// same fragments fit it exactly.
+	void Reserve(void *stream = nullptr) {
+		const uint64_t range = GetInfo().range_words;
+		const uint32_t n = voxelizer_->GetVoxelFragmentCount(), level = voxelizer_->GetLevel();
+		capacity_ = range;
+		pool_ = std::make_unique<DeviceBuffer>(capacity_ * sizeof(uint32_t), stream);
+		workspace_ = std::make_unique<DeviceBuffer>(svo_build_workspace_size(n, level, capacity_, 0), stream);
+		have_info_ = false;
+	}
+
 	// Counters of the last build (blocking read, like Counter::Read, src/Counter.cpp:23-34).
 	const svo_build_info &GetInfo() {
 		if (!have_info_) {

@@ -162,9 +162,9 @@ class OctreeBuilder:
                capacity: int | None = None, leaf_words: int | None = None) -> "OctreeBuilder":
         """OctreeBuilder::Create (src/OctreeBuilder.cpp:8-50): allocates the node pool and scratch.  The pool
         holds the exact upper bound on the words a build of these fragments can use (the reference
-        guesses F*floor(L/3) words and writes past the buffer when the guess is short).  Scratch covers
-        the worst-case leaf level unless `leaf_words` (from an earlier build's info) is given; Reserve()
-        shrinks it to the exact size after a first build."""
+        guesses F*floor(L/3) words and writes past the buffer when the guess is short); Reserve() shrinks
+        it to the exact range after a first build.  `leaf_words` is accepted for compatibility: the leaf
+        level needs no device scratch."""
         b = OctreeBuilder()
         if voxelizer is not None:
             b.m_voxelizer = voxelizer
@@ -191,13 +191,16 @@ class OctreeBuilder:
                                       _ptr(self.m_result), _stream(stream)))
 
     def Reserve(self) -> None:
-        """Shrink the scratch to the exact leaf level of the last build (blocking)."""
+        """Shrink the node pool to the exact range of the last build (blocking); later CmdBuild calls on
+        the same fragments fit it exactly."""
         info = self.GetInfo()
-        leaf_words = 8 if self.m_level == 1 else 8 * info["level_nodes"][self.m_level - 2]
         lib = _lib.load()
-        self.m_workspace = torch.empty(lib.svo_build_workspace_size(self.m_count, self.m_level, self.m_capacity,
-                                                                    leaf_words), dtype=torch.uint8,
-                                       device=self.m_fragments.device)
+        dev = self.m_fragments.device
+        self.m_capacity = int(info["range_words"])
+        self.m_octree_buffer = torch.empty(max(self.m_capacity, 8), dtype=torch.int32, device=dev)
+        self.m_workspace = torch.empty(lib.svo_build_workspace_size(self.m_count, self.m_level, self.m_capacity, 0),
+                                       dtype=torch.uint8, device=dev)
+        self._info = None
 
     def GetInfo(self) -> dict:
         """Per-level counters of the last build (blocking read, like Counter::Read)."""

@@ -388,9 +388,9 @@ void svo_fraglist_destroy(svo_fraglist *f, void *stream) {
 uint64_t svo_build_pool_bound(uint32_t count, uint32_t level) { return build_pool_bound(count, level); }
 
 size_t svo_build_workspace_size(uint32_t count, uint32_t level, uint64_t capacity, uint64_t leaf_words) {
+	(void)leaf_words; // the leaf level accumulates in shared memory: its size does not matter
 	BuildWorkspace w;
-	const uint64_t slots = leaf_words ? leaf_words : build_leaf_slot_bound(count, level, capacity);
-	build_workspace_layout(nullptr, count, level, capacity, slots, w);
+	build_workspace_layout(nullptr, count, level, capacity, w);
 	return w.total_bytes;
 }
 
@@ -414,62 +414,30 @@ int svo_build_ex(const uint64_t *frags, uint32_t count, uint32_t level, const sv
 	cudaStream_t s = (cudaStream_t)stream;
 	Mem mem{alloc, s};
 	const uint64_t capacity = build_pool_bound(count, level);
-	void *pool = nullptr, *ws = nullptr, *acc = nullptr, *wide = nullptr;
+	void *pool = nullptr, *ws = nullptr;
 	SVO_CK(mem.get(&pool, capacity * sizeof(uint32_t)), "octree pool allocation");
 	BuildWorkspace w;
-	build_workspace_layout(nullptr, count, level, capacity, 0, w);
-	cudaError_t e = mem.get(&ws, w.interior_bytes);
-	BuildState st;
-	auto cleanup = [&](bool keep_pool) {
-		mem.put(ws);
-		mem.put(acc);
-		mem.put(wide);
-		if (!keep_pool) mem.put(pool);
-	};
+	build_workspace_layout(nullptr, count, level, capacity, w);
+	cudaError_t e = mem.get(&ws, w.total_bytes);
 	if (e != cudaSuccess) {
-		cleanup(false);
+		mem.put(pool);
 		return cuda_fail(e, "build workspace allocation");
 	}
-	build_workspace_layout(ws, count, level, capacity, 0, w);
-	// stage 1: interior levels; the leaf range is then known exactly (as GetOctreeRange reads the
-	// counter, src/OctreeBuilder.cpp:212-214)
+	build_workspace_layout(ws, count, level, capacity, w);
 	e = build_launch_interior(frags, count, level, (uint32_t *)pool, capacity, w, s);
+	if (e == cudaSuccess) e = build_launch_leaf(count, level, (uint32_t *)pool, capacity, w, s);
+	// the range is read back once, as GetOctreeRange reads the counter (src/OctreeBuilder.cpp:212-214)
+	BuildState st;
 	if (e == cudaSuccess) e = read_state(w, st, s);
+	mem.put(ws);
 	if (e != cudaSuccess) {
-		cleanup(false);
-		return cuda_fail(e, "build interior levels");
+		mem.put(pool);
+		return cuda_fail(e, "build");
 	}
 	if ((rc = status_to_error(st.status, "build"))) {
-		cleanup(false);
+		mem.put(pool);
 		return rc;
 	}
-	// stage 2: leaf colours with accumulators sized to the leaf range
-	const uint64_t leaf_words = st.lv[level].num;
-	w.leaf_slots = leaf_words;
-	e = mem.get(&acc, leaf_words * 8 + 16);
-	w.acc = (unsigned long long *)acc;
-	if (e == cudaSuccess) e = build_launch_leaf(frags, count, level, (uint32_t *)pool, w, false, s);
-	if (e == cudaSuccess) e = read_state(w, st, s);
-	if (e == cudaSuccess && (st.status & kStatusLeafWide)) { // a voxel with more than 257 fragments
-		e = mem.get(&wide, leaf_words * 16 + 16);
-		w.acc_wide = (unsigned long long *)wide;
-		if (e == cudaSuccess) e = build_launch_leaf(frags, count, level, (uint32_t *)pool,
-		                                            BuildWorkspace{w.state, w.descs, w.desc_count, w.dv, w.dense_words,
-		                                                           w.cache, w.interior_bytes, w.leaf_slots, nullptr,
-		                                                           w.acc_wide, w.total_bytes},
-		                                            true, s);
-		if (e == cudaSuccess) e = read_state(w, st, s);
-		st.status &= ~kStatusLeafWide;
-	}
-	if (e != cudaSuccess) {
-		cleanup(false);
-		return cuda_fail(e, "build leaf level");
-	}
-	if ((rc = status_to_error(st.status, "build"))) {
-		cleanup(false);
-		return rc;
-	}
-	cleanup(true);
 	out->words = (uint32_t *)pool;
 	out->capacity = capacity;
 	out->range_words = st.range_words;
@@ -506,22 +474,14 @@ int svo_build_into(const uint64_t *frags, uint32_t count, uint32_t level, uint32
 	if (!aligned(pool, 16) || !aligned(workspace, 256) || !aligned(result_dev, 4))
 		return fail(SVO_ERR_INVALID, "pool must be 16-byte and workspace 256-byte aligned");
 	BuildWorkspace w;
-	build_workspace_layout(nullptr, count, level, capacity, 0, w);
-	const size_t interior = w.interior_bytes;
-	if (workspace_bytes < interior + 2 * 256 + 24 * 8)
-		return fail(SVO_ERR_CAPACITY, "workspace of %zu bytes is below the %zu the interior levels need", workspace_bytes,
-		            interior + 2 * 256 + 24 * 8);
-	// the most leaf slots (8 B packed + 16 B wide each) whose layout fits in workspace_bytes
-	uint64_t slots = ((workspace_bytes - interior) / 24) & ~7ull;
-	for (;;) {
-		build_workspace_layout(nullptr, count, level, capacity, slots, w);
-		if (w.total_bytes <= workspace_bytes || slots < 8) break;
-		slots -= 8;
-	}
-	build_workspace_layout(workspace, count, level, capacity, slots, w);
+	build_workspace_layout(nullptr, count, level, capacity, w);
+	if (workspace_bytes < w.total_bytes)
+		return fail(SVO_ERR_CAPACITY, "workspace of %zu bytes is below the %zu this build needs", workspace_bytes,
+		            w.total_bytes);
+	build_workspace_layout(workspace, count, level, capacity, w);
 	cudaStream_t s = (cudaStream_t)stream;
 	SVO_CK(build_launch_interior(frags, count, level, pool, capacity, w, s), "build interior levels");
-	SVO_CK(build_launch_leaf(frags, count, level, pool, w, true, s), "build leaf level");
+	SVO_CK(build_launch_leaf(count, level, pool, capacity, w, s), "build leaf level");
 	SVO_CK(build_launch_export(w, level, count, result_dev, s), "build info export");
 	return SVO_OK;
 }

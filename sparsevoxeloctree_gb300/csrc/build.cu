@@ -10,18 +10,21 @@
 //     0x80000000 | 8 * (1 + grank(d, m)), where grank counts occupied cells of depths 1..d-1 plus the
 //     occupied depth-d cells whose Morton code is below m (breadth-first order = Morton order per depth);
 //   * that word sits at 8 * (1 + grank(d-1, m >> 3)) + (m & 7), i.e. in its parent's child block.
-// GB300 design, in three stages:
+// GB300 design, in four stages:
 //   dense   depths 1..D (D = min(L-1, 9); 8^9 bits = 16 MB stays in L2): one sweep over the fragments sets
 //           the occupancy bits of depth D (warp-deduplicated atomicOr), coarser depths are OR-reductions of
 //           8-bit groups, one single-pass look-back scan of popcounts over all depths gives every grank,
 //           and one pass writes all interior words of depths 1..D;
+//   buckets the same sweep counts fragments per bucket of 32^3 voxels; a look-back scan and one scatter
+//           copy the fragments into bucket order (8 B per fragment), which every later sweep reads;
 //   sparse  depths D+1..L-1 (only when L > 10): the reference's tag / prefix-sum alloc per level with a
 //           per-fragment cached node index (4 B per fragment), so tag reads one parent word;
-//   leaf    one sweep: each fragment finds its leaf word and adds its colour to a packed 64-bit
-//           accumulator (r, g, b, n in 16-bit fields: one atomic per fragment); a finalize pass writes
-//           every leaf word as 0xC0000000 | min(n,63)<<24 | floor(sum/n) (the channel-wise integer mean).
-//           The packing is exact up to 257 fragments per voxel; a voxel beyond that raises a flag and a
-//           flag-gated second leaf pass redoes the colours with 2 x 64-bit accumulators per voxel.
+//   leaf    one block per bucket: the bucket's leaf blocks are contiguous in the pool, so the block
+//           accumulates their colours in shared memory (r, g, b, n in 16-bit fields, one shared atomic
+//           per fragment) and writes every leaf word, 0xC0000000 | min(n,63)<<24 | floor(sum/n) (the
+//           channel-wise integer mean), with no accumulator array in device memory.  The packing is exact
+//           up to 257 fragments per voxel; a window where a voxel exceeds that is redone with exact
+//           64-bit sums in the same block.
 // Sizes stay on the device (BuildState): no host round trip inside a stage.
 #include "common.cuh"
 #include "svo_internal.h"
@@ -33,7 +36,7 @@ constexpr int kAllocIPT = 8;
 constexpr int kAllocTile = kTPB * kAllocIPT;
 constexpr int kScanIPT = 8;
 constexpr int kScanTile = kTPB * kScanIPT;
-constexpr unsigned long long kLeafOne = 1ull << 48;
+constexpr unsigned long long kLeafOne = 1ull << 48; // count field of a packed leaf accumulator
 
 // ------------------------------------------------------------------------------------------ helpers
 SVO_DEV void frag_xyz(uint64_t f, uint32_t &x, uint32_t &y, uint32_t &z) {
@@ -89,25 +92,30 @@ __global__ void build_init(BuildState *state) {
 }
 
 // ------------------------------------------------------------------------------------------ dense stage
-// Sets the depth-D occupancy bit of every fragment.  Per warp, fragments that fall in the same bitmap
-// word are merged first (match + reduce), so one atomicOr covers them.
+// Sets the depth-D occupancy bit of every fragment and counts the fragments of every bucket.  Per warp,
+// fragments that fall in the same bitmap word (or bucket) are merged first, so one atomic covers them.
 __global__ void __launch_bounds__(kTPB) dense_mark(const uint64_t *__restrict__ frags, uint32_t n, uint32_t level,
-                                                   DenseView dv) {
+                                                   DenseView dv, uint32_t bshift, uint32_t *__restrict__ bcount) {
 	const uint32_t shift = level - dv.D;
+	const uint32_t key_shift = 3 * (bshift - shift); // the bucket key is a prefix of the depth-D Morton code
 	uint32_t *bits = dv.bits + dv.off[dv.D];
 	const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
 	for (uint64_t f = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; f < ((n + 31ull) & ~31ull); f += stride) {
-		uint32_t word = 0xffffffffu, bit = 0;
+		uint32_t word = 0xffffffffu, bit = 0, key = 0xffffffffu;
 		if (f < n) {
 			uint32_t x, y, z;
 			frag_xyz(__ldcs(frags + f), x, y, z);
 			const uint32_t m = morton(x, y, z, shift);
 			word = m >> 5;
 			bit = 1u << (m & 31);
+			key = m >> key_shift;
 		}
 		const uint32_t peers = __match_any_sync(kFullMask, word);
 		const uint32_t merged = __reduce_or_sync(peers, bit);
 		if (word != 0xffffffffu && lane_id() == (uint32_t)(__ffs(peers) - 1)) atomicOr(bits + word, merged);
+		// fragments per bucket (of 32^3 voxels), for the bucketed copy
+		const uint32_t kpeers = __match_any_sync(kFullMask, key);
+		if (key != 0xffffffffu && lane_id() == (uint32_t)(__ffs(kpeers) - 1)) atomicAdd(bcount + key, __popc(kpeers));
 	}
 }
 
@@ -191,7 +199,7 @@ __global__ void dense_finish(DenseView dv, BuildState *state) {
 
 // Writes the child blocks of every occupied cell of depths 0 (the root) .. D that has interior or
 // sparse children: interior words of depths 1..D, and zeroed words of depth D+1 when sparse levels
-// follow.  When depth D+1 is the leaf depth, depth-D cells are skipped: the leaf finalize writes those
+// follow.  When depth D+1 is the leaf depth, depth-D cells are skipped: the leaf stage writes those
 // blocks whole.  One bitmap word and one prefix word of the child depth serve all 8 children.
 __global__ void __launch_bounds__(kTPB) dense_write(uint32_t *__restrict__ pool, uint64_t capacity, DenseView dv,
                                                     uint32_t level, BuildState *state) {
@@ -238,13 +246,11 @@ __global__ void __launch_bounds__(kTPB) dense_write(uint32_t *__restrict__ pool,
 	}
 }
 
-// ------------------------------------------------------------------------------------------ tag (sparse levels, leaf)
-enum TagMode { kTagInterior = 0, kTagLeaf = 1, kTagLeafWide = 2 };
-
-template <int MODE>
+// ------------------------------------------------------------------------------------------ tag (sparse levels)
+// Marks the depth-`depth` node of every fragment (0x80000000), reading its parent through the node index
+// cached by the previous sparse depth (or the dense bitmaps when the parent depth is dense).
 SVO_DEV void tag_one(uint64_t frag, uint32_t &node, uint32_t level, uint32_t depth, bool parent_dense,
-                     const DenseView &dv, uint32_t *__restrict__ pool, unsigned long long *__restrict__ acc,
-                     uint32_t leaf_begin, uint32_t leaf_num, uint32_t *status) {
+                     const DenseView &dv, uint32_t *__restrict__ pool) {
 	uint32_t x, y, z;
 	frag_xyz(frag, x, y, z);
 	uint32_t idx;
@@ -252,120 +258,39 @@ SVO_DEV void tag_one(uint64_t frag, uint32_t &node, uint32_t level, uint32_t dep
 		idx = dense_child_word(dv, x, y, z, level, depth);
 	else
 		idx = (pool[node] & 0x3fffffffu) + octant_at(x, y, z, level - depth);
-	if (MODE == kTagInterior) {
-		if ((pool[idx] & 0x80000000u) == 0u) pool[idx] = 0x80000000u;
-		node = idx;
-	} else {
-		const uint32_t slot = idx - leaf_begin;
-		if (slot >= leaf_num) return;
-		const uint32_t rgb = (uint32_t)(frag >> 32);
-		const uint32_t r = rgb & 0xffu, g = (rgb >> 8) & 0xffu, b = (rgb >> 16) & 0xffu;
-		if (MODE == kTagLeaf) {
-			const unsigned long long v = r | ((unsigned long long)g << 16) | ((unsigned long long)b << 32) | kLeafOne;
-			const unsigned long long old = atomicAdd(acc + slot, v);
-			if ((old >> 48) >= 257ull) atomicOr(status, kStatusLeafWide); // the packed sums may have carried
-		} else {
-			atomicAdd(acc + 2 * (size_t)slot, r | ((unsigned long long)g << 32));
-			atomicAdd(acc + 2 * (size_t)slot + 1, b | (1ull << 32));
-		}
-	}
+	if ((pool[idx] & 0x80000000u) == 0u) pool[idx] = 0x80000000u;
+	node = idx;
 }
 
-template <int MODE>
 __global__ void __launch_bounds__(kTPB) build_tag(const uint64_t *__restrict__ frags, uint32_t n, uint32_t level,
                                                   uint32_t depth, uint32_t *__restrict__ pool,
-                                                  uint32_t *__restrict__ cache, unsigned long long *__restrict__ acc,
-                                                  DenseView dv, BuildState *state, int vec_ok) {
-	const uint32_t status = state->status;
-	if (status & kStatusCapacity) return;
-	if (MODE == kTagLeafWide && !(status & kStatusLeafWide)) return;
+                                                  uint32_t *__restrict__ cache, DenseView dv, BuildState *state) {
+	if (state->status & kStatusCapacity) return;
 	const bool parent_dense = depth == 1 || depth - 1 <= dv.D;
-	const bool store_cache = MODE == kTagInterior;
-	const uint32_t leaf_begin = MODE != kTagInterior ? state->lv[depth].begin : 0u;
-	const uint32_t leaf_num = MODE != kTagInterior ? state->lv[depth].num : 0u;
-	uint32_t *st = &state->status;
 	const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
 	const uint64_t nq = (n + 3ull) / 4ull;
 	for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += stride) {
 		const uint64_t f0 = q * 4;
-		if (vec_ok && f0 + 4 <= n) {
+		if (f0 + 4 <= n) { // the sorted copy is 256-byte aligned: 16-byte loads
 			const ulonglong2 a = __ldcs(reinterpret_cast<const ulonglong2 *>(frags + f0));
 			const ulonglong2 b = __ldcs(reinterpret_cast<const ulonglong2 *>(frags + f0 + 2));
 			uint4 c = make_uint4(0, 0, 0, 0);
 			if (!parent_dense) c = __ldcs(reinterpret_cast<const uint4 *>(cache + f0));
-			tag_one<MODE>(a.x, c.x, level, depth, parent_dense, dv, pool, acc, leaf_begin, leaf_num, st);
-			tag_one<MODE>(a.y, c.y, level, depth, parent_dense, dv, pool, acc, leaf_begin, leaf_num, st);
-			tag_one<MODE>(b.x, c.z, level, depth, parent_dense, dv, pool, acc, leaf_begin, leaf_num, st);
-			tag_one<MODE>(b.y, c.w, level, depth, parent_dense, dv, pool, acc, leaf_begin, leaf_num, st);
-			if (store_cache) __stcs(reinterpret_cast<uint4 *>(cache + f0), c);
+			tag_one(a.x, c.x, level, depth, parent_dense, dv, pool);
+			tag_one(a.y, c.y, level, depth, parent_dense, dv, pool);
+			tag_one(b.x, c.z, level, depth, parent_dense, dv, pool);
+			tag_one(b.y, c.w, level, depth, parent_dense, dv, pool);
+			__stcs(reinterpret_cast<uint4 *>(cache + f0), c);
 		} else {
-			for (uint64_t f = f0; f < f0 + 4 && f < n; ++f) {
+			for (uint64_t f = f0; f < n; ++f) {
 				uint32_t c = parent_dense ? 0u : cache[f];
-				tag_one<MODE>(frags[f], c, level, depth, parent_dense, dv, pool, acc, leaf_begin, leaf_num, st);
-				if (store_cache) cache[f] = c;
+				tag_one(frags[f], c, level, depth, parent_dense, dv, pool);
+				cache[f] = c;
 			}
 		}
 	}
 }
 
-// Leaf sweep: 4 fragments per thread, in phases so their loads and atomics overlap: fragment loads,
-// leaf-word lookups (dense ranks or the cached parent), then the four accumulator updates.
-__global__ void __launch_bounds__(kTPB) build_leaf(const uint64_t *__restrict__ frags, uint32_t n, uint32_t level,
-                                                   const uint32_t *__restrict__ pool,
-                                                   const uint32_t *__restrict__ cache,
-                                                   unsigned long long *__restrict__ acc, DenseView dv,
-                                                   BuildState *state) {
-	const uint32_t status = state->status;
-	if (status & kStatusCapacity) return;
-	const bool parent_dense = level == 1 || level - 1 <= dv.D;
-	const uint32_t leaf_begin = state->lv[level].begin, leaf_num = state->lv[level].num;
-	uint32_t *st = &state->status;
-	const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-	const uint64_t nq = (n + 3ull) / 4ull;
-	for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += stride) {
-		const uint64_t f0 = q * 4;
-		uint64_t f[4];
-		uint32_t c[4] = {0u, 0u, 0u, 0u};
-		const bool full = f0 + 4 <= n && ((uintptr_t)(frags + f0) & 15u) == 0;
-		if (full) {
-			const ulonglong2 a = __ldcs(reinterpret_cast<const ulonglong2 *>(frags + f0));
-			const ulonglong2 b = __ldcs(reinterpret_cast<const ulonglong2 *>(frags + f0 + 2));
-			f[0] = a.x, f[1] = a.y, f[2] = b.x, f[3] = b.y;
-			if (!parent_dense) {
-				const uint4 cc = __ldcs(reinterpret_cast<const uint4 *>(cache + f0));
-				c[0] = cc.x, c[1] = cc.y, c[2] = cc.z, c[3] = cc.w;
-			}
-		} else {
-#pragma unroll
-			for (int k = 0; k < 4; ++k) {
-				f[k] = f0 + k < n ? frags[f0 + k] : 0ull;
-				c[k] = (!parent_dense && f0 + k < n) ? cache[f0 + k] : 0u;
-			}
-		}
-		uint32_t slot[4];
-#pragma unroll
-		for (int k = 0; k < 4; ++k) {
-			uint32_t x, y, z;
-			frag_xyz(f[k], x, y, z);
-			const uint32_t idx = parent_dense ? dense_child_word(dv, x, y, z, level, level)
-			                                  : (__ldg(pool + c[k]) & 0x3fffffffu) + octant_at(x, y, z, 0);
-			slot[k] = f0 + k < n ? idx - leaf_begin : 0xffffffffu;
-		}
-		unsigned long long old[4];
-#pragma unroll
-		for (int k = 0; k < 4; ++k) {
-			old[k] = 0ull;
-			if (slot[k] < leaf_num) {
-				const uint32_t rgb = (uint32_t)(f[k] >> 32);
-				const unsigned long long v = (rgb & 0xffu) | ((unsigned long long)((rgb >> 8) & 0xffu) << 16) |
-				                             ((unsigned long long)((rgb >> 16) & 0xffu) << 32) | kLeafOne;
-				old[k] = atomicAdd(acc + slot[k], v);
-			}
-		}
-		if ((old[0] >> 48) >= 257ull || (old[1] >> 48) >= 257ull || (old[2] >> 48) >= 257ull || (old[3] >> 48) >= 257ull)
-			atomicOr(st, kStatusLeafWide); // a packed sum may have carried: the wide pass redoes the colours
-	}
-}
 
 // Prefix-sum allocation of child blocks for the marked words of a sparse depth (persistent grid, tiles
 // claimed in order by ticket so the look-back always waits on a running or finished tile).  The block
@@ -430,7 +355,7 @@ __global__ void __launch_bounds__(kTPB) build_alloc(uint32_t *__restrict__ pool,
 				continue;
 			}
 			w[k] = (uint32_t)ptr | 0x80000000u;
-			if (!next_is_leaf) { // the next depth's init; leaf blocks are written whole by the finalize
+			if (!next_is_leaf) { // the next depth's init; leaf blocks are written whole by the leaf stage
 				uint4 *child = reinterpret_cast<uint4 *>(pool + ptr);
 				child[0] = make_uint4(0, 0, 0, 0);
 				child[1] = make_uint4(0, 0, 0, 0);
@@ -453,87 +378,334 @@ __global__ void __launch_bounds__(kTPB) build_alloc(uint32_t *__restrict__ pool,
 	}
 }
 
-// ------------------------------------------------------------------------------------------ leaf finalize
-SVO_DEV uint32_t leaf_word(uint32_t n, uint32_t sr, uint32_t sg, uint32_t sb) {
-	return 0xC0000000u | (min(n, 63u) << 24) | ((sb / n) << 16) | ((sg / n) << 8) | (sr / n);
+// ------------------------------------------------------------------------------------------ buckets
+// The fragments are copied once into buckets of 32^3 voxels (Morton order of the bucket, any order
+// inside one).  All later sweeps read the bucketed copy: the sparse tag passes then touch the pool
+// region by region, and the leaf stage gives each bucket to one block, which accumulates its leaf
+// colours in shared memory.  The leaf blocks (8 words per depth L-1 node) of one bucket are contiguous
+// in the pool (breadth-first order is Morton order within a depth), so that block writes them whole.
+constexpr uint32_t kBucketVoxelBits = 5; // bucket edge: 32 voxels
+
+SVO_DEV uint32_t bucket_of(uint32_t x, uint32_t y, uint32_t z, uint32_t bshift) { return morton(x, y, z, bshift); }
+
+// Fragment counts per bucket (used when the dense stage does not run: level 1).
+__global__ void __launch_bounds__(kTPB) bucket_hist(const uint64_t *__restrict__ frags, uint32_t n, uint32_t bshift,
+                                                    uint32_t *__restrict__ bcount) {
+	const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+	for (uint64_t f = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; f < ((n + 31ull) & ~31ull); f += stride) {
+		uint32_t key = 0xffffffffu;
+		if (f < n) {
+			uint32_t x, y, z;
+			frag_xyz(frags[f], x, y, z);
+			key = bucket_of(x, y, z, bshift);
+		}
+		const uint32_t peers = __match_any_sync(kFullMask, key);
+		if (key != 0xffffffffu && lane_id() == (uint32_t)(__ffs(peers) - 1)) atomicAdd(bcount + key, __popc(peers));
+	}
 }
 
-// Writes every leaf word (empty ones as 0) from the packed accumulators; the packed pass is skipped
-// when the wide pass must redo the colours, and the wide pass only runs then.
-template <bool WIDE>
-__global__ void __launch_bounds__(kTPB) build_finalize(uint32_t *__restrict__ pool,
-                                                       const unsigned long long *__restrict__ acc, BuildState *state,
-                                                       uint32_t level) {
-	__shared__ uint32_t s_warp[kTPB / 32];
-	__shared__ uint32_t s_skip;
-	if (threadIdx.x == 0) {
-		const uint32_t st = state->status;
-		s_skip = (st & kStatusCapacity) || (WIDE ? !(st & kStatusLeafWide) : (st & kStatusLeafWide));
+// Exclusive prefix of the bucket counts (boff[nb] = total) and the list of non-empty buckets in order;
+// two single-pass look-back scans, tiles claimed in order by ticket.
+__global__ void __launch_bounds__(kTPB) bucket_scan(const uint32_t *__restrict__ bcount, uint32_t nb,
+                                                    uint32_t *__restrict__ boff, uint32_t *__restrict__ blist,
+                                                    BuildState *state, unsigned long long *descs) {
+	__shared__ uint32_t s_tile;
+	__shared__ uint32_t s_warp[kTPB / 32 + 1];
+	__shared__ uint32_t s_prefix[2];
+	if (threadIdx.x == 0) s_tile = atomicAdd(&state->tiles[1], 1u);
+	__syncthreads();
+	const uint32_t tile = s_tile;
+	const uint32_t ntiles = (nb + kScanTile - 1) / kScanTile;
+	const uint32_t b0 = tile * kScanTile + threadIdx.x * kScanIPT;
+	uint32_t c[kScanIPT], local = 0, nonempty = 0;
+#pragma unroll
+	for (int k = 0; k < kScanIPT; ++k) {
+		c[k] = b0 + k < nb ? bcount[b0 + k] : 0u;
+		local += c[k];
+		nonempty += c[k] != 0u;
+	}
+	uint32_t total, total_ne;
+	uint32_t run = block_exclusive_sum<uint32_t, kTPB>(local, s_warp, total);
+	__syncthreads();
+	uint32_t run_ne = block_exclusive_sum<uint32_t, kTPB>(nonempty, s_warp, total_ne);
+	if (threadIdx.x < 32) {
+		const uint32_t p = (uint32_t)tile_lookback_warp(descs, tile, 1u, total, &state->status);
+		const uint32_t q = (uint32_t)tile_lookback_warp(descs + ntiles, tile, 1u, total_ne, &state->status);
+		if (threadIdx.x == 0) s_prefix[0] = p, s_prefix[1] = q;
 	}
 	__syncthreads();
-	if (s_skip) return;
-	const LevelInfo li = state->lv[level];
-	uint32_t leaves = 0;
-	// 4 leaf words per thread (num and begin are multiples of 8: 16-byte stores, 32-byte packed loads)
-	for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < li.num / 4u; g += gridDim.x * blockDim.x) {
-		uint32_t word[4];
+	run += s_prefix[0];
+	run_ne += s_prefix[1];
 #pragma unroll
-		for (int j = 0; j < 4; ++j) word[j] = 0u;
-		if (WIDE) {
-			const ulonglong2 *a = reinterpret_cast<const ulonglong2 *>(acc) + 4u * g;
-#pragma unroll
-			for (int j = 0; j < 4; ++j) {
-				const ulonglong2 v = a[j];
-				const uint32_t n = (uint32_t)(v.y >> 32);
-				if (n) word[j] = leaf_word(n, (uint32_t)v.x, (uint32_t)(v.x >> 32), (uint32_t)v.y);
+	for (int k = 0; k < kScanIPT; ++k) {
+		if (b0 + k < nb) {
+			boff[b0 + k] = run;
+			if (c[k]) blist[run_ne++] = b0 + k;
+		}
+		run += c[k];
+	}
+	if (tile == ntiles - 1 && threadIdx.x == 0) {
+		boff[nb] = s_prefix[0] + total;
+		state->buckets = s_prefix[1] + total_ne;
+	}
+}
+
+// Copies every fragment into its bucket; lanes of a warp with the same bucket take one cursor step.
+// When the leaf depth's parents are dense (level <= 10), the copy holds leaf items instead of fragments:
+// the leaf word slot (from the dense bitmap of depth level-1) in the high word and the colour in the low
+// one, so the leaf stage needs no lookups.
+__global__ void __launch_bounds__(kTPB) bucket_scatter(const uint64_t *__restrict__ frags, uint32_t n,
+                                                       uint32_t bshift, const uint32_t *__restrict__ boff,
+                                                       uint32_t *__restrict__ bfill, uint64_t *__restrict__ sorted,
+                                                       bool items, DenseView dv, uint32_t level,
+                                                       const BuildState *state) {
+	const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+	const uint32_t lane = lane_id();
+	const uint32_t *pbits = items && level > 1 ? dv.bits + dv.off[level - 1] : nullptr;
+	const uint32_t *pprefix = items && level > 1 ? dv.prefix + dv.off[level - 1] : nullptr;
+	const uint32_t leaf_begin = items ? state->lv[level].begin : 0u;
+	for (uint64_t f = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; f < ((n + 31ull) & ~31ull); f += stride) {
+		uint32_t key = 0xffffffffu;
+		uint64_t out = 0;
+		if (f < n) {
+			const uint64_t frag = __ldcs(frags + f);
+			uint32_t x, y, z;
+			frag_xyz(frag, x, y, z);
+			out = frag;
+			if (pbits) { // parent cell m (depth level-1); the bucket key is its prefix
+				const uint32_t m = morton(x, y, z, 1), w = m >> 5;
+				key = m >> (3 * (bshift - 1));
+				out = ((uint64_t)(octant_at(x, y, z, 0) + 8u * (1u + __ldg(pprefix + w) +
+				                                                 __popc(__ldg(pbits + w) & ((1u << (m & 31)) - 1u))) -
+				                  leaf_begin)
+				       << 32) |
+				      ((frag >> 32) & 0xffffffu);
+			} else {
+				key = bucket_of(x, y, z, bshift);
 			}
-		} else {
-			const ulonglong2 *a = reinterpret_cast<const ulonglong2 *>(acc) + 2u * g;
-			const ulonglong2 v0 = __ldcs(a), v1 = __ldcs(a + 1);
-			const unsigned long long v[4] = {v0.x, v0.y, v1.x, v1.y};
-#pragma unroll
-			for (int j = 0; j < 4; ++j) {
-				const uint32_t n = (uint32_t)(v[j] >> 48);
-				if (n)
-					word[j] = leaf_word(n, (uint32_t)(v[j] & 0xffffu), (uint32_t)((v[j] >> 16) & 0xffffu),
-					                    (uint32_t)((v[j] >> 32) & 0xffffu));
+			if (items && !pbits) {
+				const uint32_t idx = octant_at(x, y, z, 0);
+				out = ((uint64_t)(idx - leaf_begin) << 32) | ((frag >> 32) & 0xffffffu);
 			}
 		}
-		reinterpret_cast<uint4 *>(pool + li.begin)[g] = make_uint4(word[0], word[1], word[2], word[3]);
-#pragma unroll
-		for (int j = 0; j < 4; ++j) leaves += word[j] != 0u;
-	}
-	leaves = warp_sum(leaves);
-	if (lane_id() == 0) s_warp[threadIdx.x >> 5] = leaves;
-	__syncthreads();
-	if (threadIdx.x == 0) {
-		uint32_t t = 0;
-		for (int i = 0; i < kTPB / 32; ++i) t += s_warp[i];
-		atomicAdd(&state->leaves, t);
-		if (blockIdx.x == 0) state->range_words = li.begin + li.num;
+		const uint32_t peers = __match_any_sync(kFullMask, key);
+		const uint32_t leader = __ffs(peers) - 1;
+		uint32_t base = 0;
+		if (key != 0xffffffffu && lane == leader) base = atomicAdd(bfill + key, __popc(peers));
+		base = __shfl_sync(kFullMask, base, leader);
+		if (key != 0xffffffffu) sorted[boff[key] + base + __popc(peers & ((1u << lane) - 1u))] = out;
 	}
 }
 
-// Zeroes the packed leaf accumulators of the leaf depth; a leaf range larger than the accumulator
-// array is a capacity error.
-__global__ void build_leaf_zero(unsigned long long *acc, uint64_t acc_slots, BuildState *state, uint32_t level) {
+// ------------------------------------------------------------------------------------------ leaf stage
+// Leaf word from exact 64-bit colour sums (the overflow path; integer division).
+SVO_DEV uint32_t leaf_word_wide(uint32_t n, uint64_t sr, uint64_t sg, uint64_t sb) {
+	return 0xC0000000u | (min(n, 63u) << 24) | ((uint32_t)(sb / n) << 16) | ((uint32_t)(sg / n) << 8) |
+	       (uint32_t)(sr / n);
+}
+
+// Leaf word from packed sums (1 <= n <= 257, every sum < 2^16).  floor(s / n) = trunc(s * (1/n) + 2^-10):
+// the float product is within 4e-5 of s / n, a non-integer s / n lies at least 1/257 below the next
+// integer, and an integer one is lifted clear of the truncation by the 2^-10.
+SVO_DEV uint32_t leaf_word(uint32_t n, uint32_t sr, uint32_t sg, uint32_t sb) {
+	const float inv = __frcp_rn((float)n);
+	const uint32_t r = (uint32_t)fmaf((float)sr, inv, 0.0009765625f);
+	const uint32_t g = (uint32_t)fmaf((float)sg, inv, 0.0009765625f);
+	const uint32_t b = (uint32_t)fmaf((float)sb, inv, 0.0009765625f);
+	return 0xC0000000u | (min(n, 63u) << 24) | (b << 16) | (g << 8) | r;
+}
+
+// Where the leaf stage finds the parent of a leaf: the dense bitmap of depth level-1 (its words at
+// bits/prefix) or, below the dense depths, the node index cached per fragment by the last sparse tag.
+struct LeafParent {
+	const uint32_t *bits, *prefix; // dense depth level-1 (null at level 1: the parent is the root)
+	const uint32_t *pool, *cache;  // sparse parent
+	uint32_t leaf_begin;
+};
+
+// Leaf word slot (index from the start of the leaf range) of fragment f of the bucketed copy.
+SVO_DEV uint32_t leaf_slot(uint64_t frag, uint64_t f, const LeafParent &lp) {
+	uint32_t x, y, z;
+	frag_xyz(frag, x, y, z);
+	const uint32_t oct = octant_at(x, y, z, 0);
+	uint32_t idx;
+	if (lp.cache) {
+		idx = (__ldg(lp.pool + __ldg(lp.cache + f)) & 0x3fffffffu) + oct;
+	} else if (lp.bits) { // 8 * (1 + grank(level-1, parent)) + octant
+		const uint32_t m = morton(x, y, z, 1);
+		const uint32_t w = m >> 5;
+		idx = 8u * (1u + __ldg(lp.prefix + w) + __popc(__ldg(lp.bits + w) & ((1u << (m & 31)) - 1u))) + oct;
+	} else {
+		idx = oct;
+	}
+	return idx - lp.leaf_begin;
+}
+
+constexpr uint32_t kLeafSlots = 4096;         // packed accumulators in shared memory (8 B each)
+constexpr uint32_t kWideSlots = kLeafSlots / 4; // exact accumulators (4 x 8 B each) of the overflow path
+
+// Extent of every non-empty bucket, in list order: first and last item, first and last leaf slot
+// (lo = 0xffffffff, hi = 0 when the leaf stage reduces the span over the bucket's fragments).
+//   one bucket (level <= 5): the whole leaf range;
+//   dense parents: bucket b is 4096 parent cells = 128 words of the depth level-1 bitmap, and the prefix
+//     entries at its first word and at the next bucket's give its first and last leaf block.
+__global__ void bucket_meta(const uint32_t *__restrict__ boff, const uint32_t *__restrict__ blist, uint32_t nb,
+                            DenseView dv, uint32_t level, const BuildState *state, uint4 *__restrict__ meta) {
+	const uint32_t nbuckets = state->buckets;
+	const bool items = level == 1 || level - 1 <= dv.D;
+	const uint32_t leaf_begin = state->lv[level].begin, leaf_num = state->lv[level].num;
+	const uint32_t *pprefix = items && level > 1 ? dv.prefix + dv.off[level - 1] : nullptr;
+	for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nbuckets; t += gridDim.x * blockDim.x) {
+		const uint32_t b = blist[t];
+		uint4 m = make_uint4(boff[b], boff[b + 1], 0xffffffffu, 0u);
+		if (nb == 1) {
+			m.z = 0, m.w = leaf_num - 1;
+		} else if (pprefix) {
+			const uint32_t before = leaf_begin / 8u - 1u; // occupied cells of depths below the parents
+			m.z = 8u * (pprefix[128u * b] - before);
+			m.w = 8u * (pprefix[128u * (b + 1)] - before) - 1u;
+		}
+		meta[t] = m;
+	}
+}
+
+// One bucket per block at a time, buckets taken grid-stride from the list (the next bucket's extent is
+// loaded while the block works on the current one).  For each window of kLeafSlots slots of the
+// bucket's span: zero the shared accumulators, add every item of the window, and write the window's
+// leaf words (empty slots as 0).  An accumulator is two 32-bit words, (r | g << 16) and (b | n << 16):
+// a field can carry only when a voxel has more than 257 fragments (257 x 255 = 65535), so an add that
+// sees a count of 257 or more marks the window, which is then redone exactly with 64-bit r, g, b and n
+// sums, kWideSlots slots at a time.
+//   items (dense parents): the bucketed copy holds (slot << 32 | rgb);
+//   otherwise: fragments, slots through the cached parent index, span reduced over the bucket.
+__global__ void __launch_bounds__(kTPB) build_leaf(const uint64_t *__restrict__ sorted, uint32_t level,
+                                                   uint32_t *__restrict__ pool, uint64_t capacity,
+                                                   const uint32_t *__restrict__ cache, DenseView dv,
+                                                   const uint4 *__restrict__ meta, BuildState *state) {
+	extern __shared__ unsigned long long s_acc[];
+	uint32_t *s_acc32 = reinterpret_cast<uint32_t *>(s_acc);
+	__shared__ uint32_t s_lo, s_hi, s_over, s_leaves;
 	if (state->status & kStatusCapacity) return;
-	const uint32_t num = state->lv[level].num;
-	if (num > acc_slots) {
+	const uint64_t leaf_end = (uint64_t)state->lv[level].begin + state->lv[level].num;
+	if (leaf_end > capacity || leaf_end > SVO_MAX_POOL_WORDS) { // leaf blocks of dense parents: checked here
 		if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&state->status, kStatusCapacity);
 		return;
 	}
-	ulonglong2 *a = reinterpret_cast<ulonglong2 *>(acc);
-	for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < num / 2u; k += (uint64_t)gridDim.x * blockDim.x)
-		a[k] = make_ulonglong2(0ull, 0ull);
-}
-
-// Zeroes the wide accumulators (only when a voxel overflowed the packed ones).
-__global__ void build_wide_zero(unsigned long long *acc, BuildState *state, uint32_t level) {
-	if (!(state->status & kStatusLeafWide) || (state->status & kStatusCapacity)) return;
-	const uint32_t num = state->lv[level].num;
-	for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < 2ull * num; k += (uint64_t)gridDim.x * blockDim.x)
-		acc[k] = 0ull;
+	const bool items = level == 1 || level - 1 <= dv.D;
+	const uint32_t leaf_begin = state->lv[level].begin;
+	LeafParent lp;
+	lp.bits = nullptr, lp.prefix = nullptr;
+	lp.pool = pool;
+	lp.cache = cache;
+	lp.leaf_begin = leaf_begin;
+	const uint32_t nbuckets = state->buckets;
+	if (threadIdx.x == 0) s_leaves = 0;
+	uint4 next = blockIdx.x < nbuckets ? meta[blockIdx.x] : make_uint4(0, 0, 0, 0);
+	for (uint32_t t = blockIdx.x; t < nbuckets; t += gridDim.x) {
+		const uint4 m = next;
+		if (t + gridDim.x < nbuckets) next = meta[t + gridDim.x];
+		const uint32_t f0 = m.x, f1 = m.y;
+		uint32_t span_lo = m.z & ~7u, span_hi = (m.w | 7u) + 1u;
+		if (m.z > m.w) { // span reduced over the bucket's fragments
+			if (threadIdx.x == 0) s_lo = 0xffffffffu, s_hi = 0u;
+			__syncthreads();
+			uint32_t lo = 0xffffffffu, hi = 0u;
+			for (uint32_t fb = f0 + threadIdx.x; fb < f1; fb += 4 * kTPB) {
+				uint64_t fr[4];
+#pragma unroll
+				for (int k = 0; k < 4; ++k) fr[k] = fb + k * kTPB < f1 ? sorted[fb + k * kTPB] : 0ull;
+#pragma unroll
+				for (int k = 0; k < 4; ++k)
+					if (fb + k * kTPB < f1) {
+						const uint32_t sl = leaf_slot(fr[k], fb + k * kTPB, lp);
+						lo = min(lo, sl), hi = max(hi, sl);
+					}
+			}
+			lo = __reduce_min_sync(kFullMask, lo), hi = __reduce_max_sync(kFullMask, hi);
+			if (lane_id() == 0) atomicMin(&s_lo, lo), atomicMax(&s_hi, hi);
+			__syncthreads();
+			span_lo = s_lo & ~7u, span_hi = (s_hi | 7u) + 1u;
+		}
+		for (uint32_t w0 = span_lo; w0 < span_hi; w0 += kLeafSlots) {
+			const uint32_t wn = min(kLeafSlots, span_hi - w0);
+			for (uint32_t i = threadIdx.x; i < wn; i += kTPB) s_acc[i] = 0ull;
+			if (threadIdx.x == 0) s_over = 0;
+			__syncthreads();
+			bool over = false;
+			for (uint32_t fb = f0 + threadIdx.x; fb < f1; fb += 4 * kTPB) {
+				uint64_t fr[4];
+				uint32_t sl[4], rgb[4];
+#pragma unroll
+				for (int k = 0; k < 4; ++k) fr[k] = fb + k * kTPB < f1 ? sorted[fb + k * kTPB] : 0ull;
+#pragma unroll
+				for (int k = 0; k < 4; ++k) {
+					const bool in = fb + k * kTPB < f1;
+					sl[k] = !in ? 0xffffffffu : (items ? (uint32_t)(fr[k] >> 32) : leaf_slot(fr[k], fb + k * kTPB, lp)) - w0;
+					rgb[k] = items ? (uint32_t)fr[k] : (uint32_t)(fr[k] >> 32);
+				}
+#pragma unroll
+				for (int k = 0; k < 4; ++k)
+					if (sl[k] < wn) {
+						atomicAdd(s_acc32 + 2 * sl[k], (rgb[k] & 0xffu) | (((rgb[k] >> 8) & 0xffu) << 16));
+						over |= (atomicAdd(s_acc32 + 2 * sl[k] + 1, ((rgb[k] >> 16) & 0xffu) | (1u << 16)) >> 16) >= 257u;
+					}
+			}
+			if (__any_sync(kFullMask, over) && lane_id() == 0) s_over = 1;
+			__syncthreads();
+			uint32_t leaves = 0;
+			if (!s_over) {
+				for (uint32_t i = 4 * threadIdx.x; i < wn; i += 4 * kTPB) {
+					const uint4 a = *reinterpret_cast<const uint4 *>(s_acc32 + 2 * i);
+					const uint4 c = *reinterpret_cast<const uint4 *>(s_acc32 + 2 * i + 4);
+					const uint32_t rg[4] = {a.x, a.z, c.x, c.z}, bn[4] = {a.y, a.w, c.y, c.w};
+					uint32_t word[4];
+#pragma unroll
+					for (int j = 0; j < 4; ++j) {
+						const uint32_t n = bn[j] >> 16;
+						word[j] = n ? leaf_word(n, rg[j] & 0xffffu, rg[j] >> 16, bn[j] & 0xffffu) : 0u;
+						leaves += word[j] != 0u;
+					}
+					*reinterpret_cast<uint4 *>(pool + leaf_begin + w0 + i) = make_uint4(word[0], word[1], word[2], word[3]);
+				}
+			} else {
+				// exact sums for this window, kWideSlots slots at a time
+				unsigned long long *acc4 = s_acc;
+				for (uint32_t v0 = 0; v0 < wn; v0 += kWideSlots) {
+					const uint32_t vn = min(kWideSlots, wn - v0);
+					__syncthreads();
+					for (uint32_t i = threadIdx.x; i < 4 * vn; i += kTPB) acc4[i] = 0ull;
+					__syncthreads();
+					for (uint32_t f = f0 + threadIdx.x; f < f1; f += kTPB) {
+						const uint64_t item = sorted[f];
+						const uint32_t sl = (items ? (uint32_t)(item >> 32) : leaf_slot(item, f, lp)) - w0 - v0;
+						const uint32_t c = items ? (uint32_t)item : (uint32_t)(item >> 32);
+						if (sl < vn) {
+							atomicAdd(acc4 + 4 * sl, (unsigned long long)(c & 0xffu));
+							atomicAdd(acc4 + 4 * sl + 1, (unsigned long long)((c >> 8) & 0xffu));
+							atomicAdd(acc4 + 4 * sl + 2, (unsigned long long)((c >> 16) & 0xffu));
+							atomicAdd(acc4 + 4 * sl + 3, 1ull);
+						}
+					}
+					__syncthreads();
+					for (uint32_t i = threadIdx.x; i < vn; i += kTPB) {
+						const unsigned long long n = acc4[4 * i + 3];
+						// n < 2^32 (fragment counts are 32-bit)
+						const uint32_t word = n ? leaf_word_wide((uint32_t)n, acc4[4 * i], acc4[4 * i + 1], acc4[4 * i + 2]) : 0u;
+						pool[leaf_begin + w0 + v0 + i] = word;
+						leaves += word != 0u;
+					}
+				}
+			}
+			leaves = warp_sum(leaves);
+			if (lane_id() == 0 && leaves) atomicAdd(&s_leaves, leaves);
+			__syncthreads();
+		}
+	}
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		if (s_leaves) atomicAdd(&state->leaves, s_leaves);
+		if (blockIdx.x == 0) state->range_words = leaf_end;
+	}
 }
 
 // Writes svo_build_info followed by the status word to `out` (device) from the build state.
@@ -546,7 +718,7 @@ __global__ void build_export(const BuildState *state, uint32_t level, uint32_t c
 	info->leaves = state->leaves;
 	for (uint32_t d = 1; d <= SVO_LEVEL_MAX; ++d)
 		info->level_nodes[d - 1] = d < level ? state->lv[d].nodes : (d == level ? state->leaves : 0u);
-	out[sizeof(svo_build_info) / 4] = state->status & ~kStatusLeafWide; // the wide pass resolved it
+	out[sizeof(svo_build_info) / 4] = state->status;
 }
 
 // ------------------------------------------------------------------------------------------ host side
@@ -576,19 +748,11 @@ static uint64_t max_sparse_level_words(uint32_t count, uint32_t level, uint32_t 
 	return best;
 }
 
-uint64_t build_leaf_slot_bound(uint32_t count, uint32_t level, uint64_t capacity) {
-	uint64_t per = 1;
-	for (uint32_t i = 1; i < level; ++i) per = per >= (1ull << 40) ? per : per * 8;
-	uint64_t b = 8 * (per < count ? per : (uint64_t)count);
-	if (b < 8) b = 8;
-	return b < capacity ? b : capacity;
-}
-
-// Layout: state | descriptors | dense bitmaps | dense prefix | node cache | packed leaf accumulators
-// (leaf_slots x 8 B) | wide leaf accumulators (leaf_slots x 16 B).  leaf_slots = 0 lays out the
-// interior part only (the accumulators are then placed separately by the caller).
-void build_workspace_layout(void *ws, uint32_t count, uint32_t level, uint64_t capacity, uint64_t leaf_slots,
-                            BuildWorkspace &w) {
+// Layout: state | dense-scan descriptors | dense bitmaps | dense prefix | bucket counts, offsets,
+// cursors, list and scan descriptors | bucketed fragment copy (8 B per fragment) | node cache (4 B per
+// fragment, sparse levels only).  The leaf stage needs nothing more: its accumulators live in shared
+// memory.
+void build_workspace_layout(void *ws, uint32_t count, uint32_t level, uint64_t capacity, BuildWorkspace &w) {
 	char *p = (char *)ws;
 	size_t off = 0;
 	auto take = [&](size_t bytes) {
@@ -613,11 +777,17 @@ void build_workspace_layout(void *ws, uint32_t count, uint32_t level, uint64_t c
 	w.descs = (unsigned long long *)take(w.desc_count * sizeof(unsigned long long));
 	w.dv.bits = (uint32_t *)take((size_t)o * 4 + 32);
 	w.dv.prefix = (uint32_t *)take(((size_t)o + 1) * 4);
+	w.bshift = std::min<uint32_t>(level, kBucketVoxelBits);
+	w.nb = 1u << (3 * (level - w.bshift));
+	w.bcount = (uint32_t *)take((size_t)w.nb * 4);
+	w.bfill = (uint32_t *)take((size_t)w.nb * 4);
+	w.boff = (uint32_t *)take(((size_t)w.nb + 1) * 4);
+	w.blist = (uint32_t *)take((size_t)w.nb * 4);
+	w.bmeta = (uint4 *)take((size_t)w.nb * 16);
+	w.bdesc_count = 2 * ((size_t)(w.nb + kScanTile - 1) / kScanTile + 1);
+	w.bdescs = (unsigned long long *)take(w.bdesc_count * sizeof(unsigned long long));
+	w.sorted = (uint64_t *)take((size_t)count * 8 + 32);
 	w.cache = (uint32_t *)take(level > D + 1 ? (size_t)count * 4 + 16 : 16);
-	w.interior_bytes = off;
-	w.leaf_slots = leaf_slots;
-	w.acc = leaf_slots ? (unsigned long long *)take(leaf_slots * 8 + 16) : nullptr;
-	w.acc_wide = leaf_slots ? (unsigned long long *)take(leaf_slots * 16 + 16) : nullptr;
 	w.total_bytes = off;
 }
 
@@ -630,13 +800,26 @@ cudaError_t build_launch_interior(const uint64_t *frags, uint32_t count, uint32_
                                   uint64_t capacity, const BuildWorkspace &w, cudaStream_t stream) {
 	cudaError_t e = cudaMemsetAsync(w.descs, 0, w.desc_count * sizeof(unsigned long long), stream);
 	if (e == cudaSuccess && w.dense_words) e = cudaMemsetAsync(w.dv.bits, 0, (size_t)w.dense_words * 4, stream);
+	// bucket counts and cursors are adjacent: one memset
+	if (e == cudaSuccess) e = cudaMemsetAsync(w.bcount, 0, (char *)w.boff - (char *)w.bcount, stream);
+	if (e == cudaSuccess) e = cudaMemsetAsync(w.bdescs, 0, w.bdesc_count * sizeof(unsigned long long), stream);
 	if (e != cudaSuccess) return e;
 	const int sms = device_sm_count();
 	const uint32_t D = w.dv.D;
 	SVO_LAUNCH("build_init", stream, build_init<<<1, 256, 0, stream>>>(w.state););
 	if (D >= 1) {
 		SVO_LAUNCH("dense_mark", stream,
-		           dense_mark<<<grid_for(count, kTPB, (uint32_t)sms * 16), kTPB, 0, stream>>>(frags, count, level, w.dv););
+		           dense_mark<<<grid_for(count, kTPB, (uint32_t)sms * 16), kTPB, 0, stream>>>(frags, count, level, w.dv,
+		                                                                                      w.bshift, w.bcount););
+	} else {
+		SVO_LAUNCH("bucket_hist", stream,
+		           bucket_hist<<<grid_for(count, kTPB, (uint32_t)sms * 16), kTPB, 0, stream>>>(frags, count, w.bshift,
+		                                                                                       w.bcount););
+	}
+	SVO_LAUNCH("bucket_scan", stream,
+	           bucket_scan<<<(w.nb + kScanTile - 1) / kScanTile, kTPB, 0, stream>>>(w.bcount, w.nb, w.boff, w.blist,
+	                                                                               w.state, w.bdescs););
+	if (D >= 1) {
 		for (uint32_t d = D - 1; d >= 1; --d)
 			SVO_LAUNCH("dense_reduce", stream,
 			           dense_reduce<<<grid_for(dense_words_of(d), kTPB, (uint32_t)sms * 8), kTPB, 0, stream>>>(w.dv, d););
@@ -648,41 +831,34 @@ cudaError_t build_launch_interior(const uint64_t *frags, uint32_t count, uint32_
 		           dense_write<<<grid_for((uint64_t)w.dense_words + 1, kTPB, (uint32_t)sms * 16), kTPB, 0, stream>>>(
 		               pool, capacity, w.dv, level, w.state););
 	}
-	const int vec_ok = ((uintptr_t)frags & 15u) == 0;
+	// the bucketed copy: leaf items when the leaf parents are dense (their bitmap is final now), fragments
+	// for the sparse levels otherwise
+	const bool items = level == 1 || level - 1 <= D;
+	SVO_LAUNCH("bucket_scatter", stream,
+	           bucket_scatter<<<grid_for(count, kTPB, (uint32_t)sms * 16), kTPB, 0, stream>>>(
+	               frags, count, w.bshift, w.boff, w.bfill, w.sorted, items, w.dv, level, w.state););
 	const uint32_t tag_blocks = grid_for(((uint64_t)count + 3) / 4, kTPB, (uint32_t)sms * 16);
 	for (uint32_t depth = D + 1; depth < level; ++depth) {
 		SVO_LAUNCH("build_tag", stream,
-		           build_tag<kTagInterior><<<tag_blocks, kTPB, 0, stream>>>(frags, count, level, depth, pool, w.cache,
-		                                                                    w.acc, w.dv, w.state, vec_ok););
+		           build_tag<<<tag_blocks, kTPB, 0, stream>>>(w.sorted, count, level, depth, pool, w.cache, w.dv,
+		                                                      w.state););
 		SVO_LAUNCH("build_alloc", stream,
 		           build_alloc<<<(uint32_t)sms * 4, kTPB, 0, stream>>>(pool, capacity, depth, level, w.state, w.descs););
 	}
 	return cudaGetLastError();
 }
 
-cudaError_t build_launch_leaf(const uint64_t *frags, uint32_t count, uint32_t level, uint32_t *pool,
-                              const BuildWorkspace &w, bool wide, cudaStream_t stream) {
+cudaError_t build_launch_leaf(uint32_t count, uint32_t level, uint32_t *pool, uint64_t capacity,
+                              const BuildWorkspace &w, cudaStream_t stream) {
+	(void)count;
 	const int sms = device_sm_count();
-	const int vec_ok = ((uintptr_t)frags & 15u) == 0;
-	const uint32_t tag_blocks = grid_for(((uint64_t)count + 3) / 4, kTPB, (uint32_t)sms * 16);
-	if (w.acc) {
-		SVO_LAUNCH("build_leaf_zero", stream,
-		           build_leaf_zero<<<(uint32_t)sms * 8, kTPB, 0, stream>>>(w.acc, w.leaf_slots, w.state, level););
-		SVO_LAUNCH("build_leaf", stream,
-		           build_leaf<<<tag_blocks, kTPB, 0, stream>>>(frags, count, level, pool, w.cache, w.acc, w.dv, w.state););
-		SVO_LAUNCH("build_finalize", stream,
-		           build_finalize<false><<<(uint32_t)sms * 8, kTPB, 0, stream>>>(pool, w.acc, w.state, level););
-	}
-	if (wide && w.acc_wide) {
-		// exact colours for voxels with more than 257 fragments; these launches return at once otherwise
-		SVO_LAUNCH("build_wide_zero", stream,
-		           build_wide_zero<<<(uint32_t)sms * 4, kTPB, 0, stream>>>(w.acc_wide, w.state, level););
-		SVO_LAUNCH("build_leaf_wide", stream,
-		           build_tag<kTagLeafWide><<<tag_blocks, kTPB, 0, stream>>>(frags, count, level, level, pool, w.cache,
-		                                                                    w.acc_wide, w.dv, w.state, vec_ok););
-		SVO_LAUNCH("build_finalize_wide", stream,
-		           build_finalize<true><<<(uint32_t)sms * 8, kTPB, 0, stream>>>(pool, w.acc_wide, w.state, level););
-	}
+	const size_t smem = kLeafSlots * sizeof(unsigned long long); // 32 KB: below the default dynamic limit
+	SVO_LAUNCH("bucket_meta", stream,
+	           bucket_meta<<<grid_for(w.nb, kTPB, (uint32_t)sms * 4), kTPB, 0, stream>>>(w.boff, w.blist, w.nb, w.dv, level,
+	                                                                                w.state, w.bmeta););
+	SVO_LAUNCH("build_leaf", stream,
+	           build_leaf<<<(uint32_t)sms * 6, kTPB, smem, stream>>>(w.sorted, level, pool, capacity, w.cache, w.dv,
+	                                                                  w.bmeta, w.state););
 	return cudaGetLastError();
 }
 

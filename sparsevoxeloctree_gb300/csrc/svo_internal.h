@@ -16,8 +16,7 @@ inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 enum : uint32_t {
 	kStatusTimeout = 1u,  // a bounded look-back wait gave up
 	kStatusCapacity = 2u, // an output buffer or the 30-bit pointer range would overflow
-	kStatusMalformed = 4u, // a march met a pointer outside the pool or a tree deeper than its level
-	kStatusLeafWide = 16u  // a voxel got more than 257 fragments: leaf colours need the wide accumulators
+	kStatusMalformed = 4u  // a march met a pointer outside the pool or a tree deeper than its level
 };
 
 void note_launch();      // counts kernel launches (svo_kernel_launches)
@@ -68,7 +67,7 @@ struct LevelInfo {
 	uint32_t begin;         // first word of this depth's node range
 	uint32_t num;           // words in the range (8 per parent node)
 	uint32_t blocks_before; // child blocks allocated before this depth's alloc
-	uint32_t nodes;         // non-empty words at this depth (written by its alloc / finalize)
+	uint32_t nodes;         // non-empty words at this depth (written by its alloc)
 };
 
 struct BuildState {
@@ -78,6 +77,8 @@ struct BuildState {
 	uint32_t pad;
 	uint32_t tiles[16];                 // tile tickets of each depth's alloc scan
 	LevelInfo lv[SVO_LEVEL_MAX + 2];    // lv[d] for depth d (1-based)
+	uint32_t buckets;                   // non-empty fragment buckets (bucket_scan)
+	uint32_t leaf_ticket;               // buckets claimed by the leaf stage
 };
 
 constexpr uint32_t kDenseMaxDepth = 9; // deepest depth held as a dense occupancy bitmap (8^9 bits)
@@ -97,24 +98,28 @@ struct BuildWorkspace {
 	size_t desc_count;
 	DenseView dv;
 	uint32_t dense_words;
-	uint32_t *cache;                // per-fragment node index of the previous sparse depth
-	size_t interior_bytes;          // bytes up to here
-	uint64_t leaf_slots;            // leaf words the accumulators cover
-	unsigned long long *acc;        // packed leaf accumulators (8 B per leaf word)
-	unsigned long long *acc_wide;   // exact leaf accumulators (16 B per leaf word), used only on overflow
+	uint32_t bshift;                // bucket key = Morton code of the voxel >> bshift bits per axis
+	uint32_t nb;                    // buckets (8^(level - bshift))
+	uint32_t *bcount;               // [nb] fragments per bucket
+	uint32_t *boff;                 // [nb+1] first fragment of each bucket in `sorted`
+	uint32_t *bfill;                // [nb] scatter cursors
+	uint32_t *blist;                // [nb] non-empty buckets in order
+	uint4 *bmeta;                   // [nb] per listed bucket: first/last item, first/last leaf slot
+	unsigned long long *bdescs;     // look-back descriptors of the bucket scan (2 scans)
+	size_t bdesc_count;
+	uint64_t *sorted;               // [count] the fragments, bucketed
+	uint32_t *cache;                // [count] node index of the previous sparse depth, per sorted fragment
 	size_t total_bytes;
 };
 uint64_t build_pool_bound(uint32_t count, uint32_t level);
-uint64_t build_leaf_slot_bound(uint32_t count, uint32_t level, uint64_t capacity);
 uint32_t dense_depth(uint32_t level);
-void build_workspace_layout(void *ws, uint32_t count, uint32_t level, uint64_t capacity, uint64_t leaf_slots,
-                            BuildWorkspace &w);
+void build_workspace_layout(void *ws, uint32_t count, uint32_t level, uint64_t capacity, BuildWorkspace &w);
 // Interior levels (dense bitmaps, then sparse tag/alloc); the leaf range ends up in state->lv[level].
 cudaError_t build_launch_interior(const uint64_t *frags, uint32_t count, uint32_t level, uint32_t *pool,
                                   uint64_t capacity, const BuildWorkspace &w, cudaStream_t stream);
-// Leaf colours and finalize (packed accumulators; the flag-gated wide pass too when `wide`).
-cudaError_t build_launch_leaf(const uint64_t *frags, uint32_t count, uint32_t level, uint32_t *pool,
-                              const BuildWorkspace &w, bool wide, cudaStream_t stream);
+// Leaf words of the deepest level from the bucketed fragments.
+cudaError_t build_launch_leaf(uint32_t count, uint32_t level, uint32_t *pool, uint64_t capacity,
+                              const BuildWorkspace &w, cudaStream_t stream);
 // svo_build_info followed by the uint32 status word, written to device memory `out`.
 cudaError_t build_launch_export(const BuildWorkspace &w, uint32_t level, uint32_t count, void *out,
                                 cudaStream_t stream);

@@ -45,6 +45,7 @@ int main(int argc, char **argv) {
 		octree->Update(builder);
 		voxelizer->CmdVoxelize(); // record both passes again: same results
 		voxelizer->CheckEmission();
+		builder->Reserve(); // pool shrunk to the exact range: the re-recorded build fits it
 		builder->CmdBuild();
 		octree->Update(builder);
 		auto tracer = svo::OctreeTracer::Create(octree, cam, width, height);

@@ -51,7 +51,8 @@ def test_pool_bound_and_workspace_sizes(lib):
     for count, level in [(0, 1), (1, 1), (5, 3), (1000, 8), (38_000_000, 10), (150_000_000, 12)]:
         assert lib.svo_build_pool_bound(count, level) == oracle.pool_bound(count, level)
     cap = lib.svo_build_pool_bound(1000, 8)
-    assert lib.svo_build_workspace_size(1000, 8, cap, 0) > lib.svo_build_workspace_size(1000, 8, cap, 64) > 4000
+    # the bucketed fragment copy (8 B per fragment) dominates; the leaf level needs no device scratch
+    assert lib.svo_build_workspace_size(1000, 8, cap, 0) == lib.svo_build_workspace_size(1000, 8, cap, 64) > 8000
     assert lib.svo_voxelize_workspace_size(1000, 0) > 8 * 1000
     assert lib.svo_voxelize_workspace_size(1000, 10**6) > lib.svo_voxelize_workspace_size(1000, 0)
 

@@ -307,17 +307,20 @@ def _crowded_voxel_fragments(level, n_hot):
     return pack_fragments(xyz[:, 0], xyz[:, 1], xyz[:, 2], g.integers(0, 1 << 24, size=len(xyz)))
 
 
-@pytest.mark.parametrize("n_hot", [257, 258, 5000])
+@pytest.mark.parametrize("n_hot", [257, 258, 5000, 65536, 65576])
 def test_build_many_fragments_in_one_voxel(cuda, n_hot):
     """More than 257 fragments in one voxel overflow the packed accumulator: the exact wide pass takes
-    over (both through svo_build_ex and through the stream-ordered svo_build_into)."""
+    over (both through svo_build_ex and through the stream-ordered svo_build_into).  At 65,536 and
+    65,576 fragments the voxel's count field wraps to a value below 258, so only the check that the count
+    fields add up to the fragment count catches it."""
     import torch
     api = _api()
     level = 6
     frags = _crowded_voxel_fragments(level, n_hot)
     ref = oracle.build_octree(frags, level)
-    _, got = gpu_build(frags, level)
+    o, got = gpu_build(frags, level)
     assert np.array_equal(got, ref)
+    assert o.info["leaves"] == int(np.count_nonzero((ref & 0xC0000000) == 0xC0000000))
     t = torch.from_numpy(frags.view(np.int64)).cuda()
     b = api.OctreeBuilder.Create(fragments=t, level=level)
     b.GetOctree().fill_(-1)
@@ -341,12 +344,38 @@ def test_build_into_pool_too_small_reports_capacity(cuda):
     # the builder is still usable with a large enough pool
     b2 = api.OctreeBuilder.Create(fragments=t, level=s.level)
     b2.CmdBuild()
-    b2.Reserve()  # scratch shrunk to the exact leaf level
+    b2.Reserve()  # pool shrunk to the exact range
     b2.GetOctree().fill_(-1)  # no stale words from the first build can pass the comparison
     b2.CmdBuild()
     ref = oracle.build_octree(frags, s.level)
     assert b2.GetInfo()["range_words"] == len(ref)  # raises if the build reported an error
     assert np.array_equal(b2.GetOctree()[: len(ref)].cpu().numpy().view(np.uint32), ref)
+
+
+@pytest.mark.parametrize("short_by", [8, 64])
+def test_build_into_pool_short_of_the_leaf_range(cuda, short_by):
+    """A pool that holds every interior block but not the whole leaf range: SVO_ERR_CAPACITY through the
+    status word and no word written past `capacity` (guard words behind it stay intact)."""
+    import ctypes
+
+    import torch
+    from sparsevoxeloctree_gb300 import _lib
+    lib = _lib.load()
+    s = scenes.plain_256()
+    frags = oracle.voxelize(s.tris, s.level)
+    ref = oracle.build_octree(frags, s.level)
+    cap = len(ref) - short_by
+    t = torch.from_numpy(frags.view(np.int64)).cuda()
+    pool = torch.full((cap + 4096,), 0x5A5A5A5A, dtype=torch.int32, device="cuda")
+    ws = torch.empty(lib.svo_build_workspace_size(len(frags), s.level, cap, 0), dtype=torch.uint8, device="cuda")
+    res = torch.zeros(64, dtype=torch.int32, device="cuda")
+    rc = lib.svo_build_into(ctypes.c_void_p(t.data_ptr()), len(frags), s.level, ctypes.c_void_p(pool.data_ptr()), cap,
+                            ctypes.c_void_p(ws.data_ptr()), ws.numel(), ctypes.c_void_p(res.data_ptr()), None)
+    assert rc == _lib.SVO_OK
+    torch.cuda.synchronize()
+    status = int(res.cpu().numpy().view(np.uint32)[ctypes.sizeof(_lib.BuildInfo) // 4])
+    assert status & 2  # capacity
+    assert bool((pool[cap:] == 0x5A5A5A5A).all())
 
 
 @pytest.mark.parametrize("size", [(37, 23), (7, 5), (1, 1), (1921, 3), (8, 4)])
