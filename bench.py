@@ -310,6 +310,93 @@ def e2e_arm(args, scene, tris_host, device, world) -> dict:
             "timing": "host wall clock per step (includes the ABI's blocking readbacks)"}
 
 
+# ------------------------------------------------------------------------------------------ batched build
+def batch_leg(args, device) -> dict:
+    """The batched-build workload: 64 clutter meshes (triangles log-uniform in [1e3, 5e5], levels 7..10)
+    voxelized and built (a) in one svo_batcher batch (one count pass, one readback of the counts, one
+    recorded launch sequence for emit + every build level over all meshes, one readback of the results)
+    and (b) as 64 sequential plain builds through the C ABI (svo_voxelize + svo_build_fraglist per mesh,
+    each with its own two blocking readbacks).  Triangles are resident in HBM for both; both are timed on
+    the host wall clock per whole batch, blocking readbacks included."""
+    import numpy as np
+    import torch
+
+    from sparsevoxeloctree_gb300 import _lib, api, scenes
+
+    lib = _lib.load()
+    meshes = scenes.batch_64()
+    tris = [api.to_device(t) for t, _ in meshes]
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    bb = api.BatchBuilder(use_graph=True)
+    batch = [(t, level) for t, (_, level) in zip(tris, meshes)]
+
+    def batched():
+        bb.Build(batch)
+
+    def sequential():
+        for t, (_, level) in zip(tris, meshes):
+            fl = _lib.Fraglist()
+            _lib.check(lib.svo_voxelize(ctypes.c_void_p(t.data_ptr()), t.numel() // 48, level, ctypes.byref(fl), s))
+            oc = _lib.OctreeC()
+            _lib.check(lib.svo_build_fraglist(ctypes.byref(fl), ctypes.byref(oc), None, s))
+            lib.svo_fraglist_destroy(ctypes.byref(fl), s)
+            lib.svo_octree_destroy(ctypes.byref(oc), s)
+        torch.cuda.current_stream().synchronize()
+
+    def timed(fn, reps):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        out = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            fn()
+            out.append((time.perf_counter() - t0) * 1e3)
+        return out
+
+    reps = max(3, min(args.steps, 10))
+    launches0 = lib.svo_kernel_launches()
+    b_ms = timed(batched, reps)
+    seq_ms = timed(sequential, reps)
+    F = sum(bb.GetInfo(i)["fragments"] for i in range(len(meshes)))
+    W = sum(bb.GetInfo(i)["range_words"] for i in range(len(meshes)))
+    T = sum(len(t) for t, _ in meshes)
+    # device time of one batch (count graph + build graph), profiled launches excluded: CUDA events around
+    # a Build on the current stream
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    batched()
+    ev1.record()
+    torch.cuda.synchronize()
+    dev_ms = ev0.elapsed_time(ev1)
+    # per-kernel device times of one batch, launches issued directly (no graph) with events around each
+    prof_bb = api.BatchBuilder(use_graph=False)
+    prof_bb.Build(batch)
+    torch.cuda.synchronize()
+    lib.svo_profile_enable(1)
+    prof_bb.Build(batch)
+    kernels = _lib.profile_summary()
+    lib.svo_profile_enable(0)
+    del prof_bb
+    peaks = load_peaks()
+    alg = 48.0 * T + 40.0 * F + 4.0 * W
+    bm, sm = float(np.median(b_ms)), float(np.median(seq_ms))
+    return {"workload": "batch_64: 64 clutter meshes, triangles log-uniform in [1e3, 5e5] (seeded), levels 7..10",
+            "meshes": len(meshes), "triangles": T, "fragments": F, "octree_words": W,
+            "batched_ms": bm, "sequential_plain_ms": sm, "speedup_vs_sequential": sm / bm,
+            "batched_mfragments_per_s": F / (bm * 1e-3) / 1e6,
+            "sequential_mfragments_per_s": F / (sm * 1e-3) / 1e6,
+            "batched_device_ms": dev_ms,
+            "roofline": {"bound": "hbm", "algorithmic_bytes": alg,
+                         "bytes_formula": "48 B/triangle + 40 B/fragment (8 emit, 16 two sweeps, 8 bucketed copy, "
+                                          "8 leaf sweep) + 4 B/node word",
+                         "achieved_gbs": alg / (bm * 1e-3) / 1e9, "peak": peaks["hbm_gbs"],
+                         "frac": alg / (bm * 1e-3) / 1e9 / peaks["hbm_gbs"]},
+            "graph": bb.stats(), "timing": "host wall clock per batch (median), blocking readbacks included",
+            "kernels_one_batch": kernels,
+            "reps": reps, "kernel_launches_recorded": int(lib.svo_kernel_launches() - launches0)}
+
+
 # ------------------------------------------------------------------------------------------ CPU arms
 def cpu_baseline(scene, per_step: bool) -> dict:
     """The oracle (CPU restatement of the reference's path) on the host cores, full workload."""
@@ -356,6 +443,7 @@ def main() -> int:
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="room_1024")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-build leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -390,11 +478,15 @@ def main() -> int:
     device = torch.device("cuda", local_rank)
     torch.cuda.set_device(device)
     res = engine_arm(args, rank, world, device)
+    if not args.no_batch and rank == 0:
+        res["batched"] = batch_leg(args, device)
     config.update(res["config_extra"])
     line.update({"value": res["value"], "ms_per_step": res["ms_per_step"], "config": config,
                  "stages": res["stages"], "roofline": res["roofline"], "cpu_baseline": res["cpu_baseline"],
                  "e2e": res["e2e"], "clocks": res["clocks"], "gpu_launches": res["gpu_launches"],
                  "step_ms": res["step_ms_all"]})
+    if "batched" in res:
+        line["batched"] = res["batched"]
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -148,7 +148,8 @@ uint64_t svo_kernel_launches(void);
 
 /* Device memory and transfers for callers without the CUDA headers (C, C++, FFI bindings).  Allocation
  * is stream-ordered (freed memory stays pooled for reuse); copies are asynchronous on `stream` except
- * svo_download with sync = 1, which returns once the data is in host memory. */
+ * svo_download with sync = 1, which returns once the data is in host memory.  Copies go through
+ * unified addressing, so either side may also be device memory (a device-to-device copy). */
 int svo_device_alloc(void **ptr, size_t bytes, void *stream);
 void svo_device_free(void *ptr, void *stream);
 int svo_upload(void *dst_device, const void *src_host, size_t bytes, void *stream);
@@ -239,6 +240,48 @@ int svo_build_ex(const uint64_t *frags, uint32_t count, uint32_t level, const sv
                  svo_build_info *info, void *stream);
 
 void svo_octree_destroy(svo_octree *o, void *stream);
+
+/* ------------------------------------------------------------------ batched voxelize + build */
+
+/* One mesh of a batch: its triangles (device, 16-byte aligned) and the octree level it is built at. */
+typedef struct svo_batch_mesh {
+	const svo_triangle *tris;
+	uint32_t n_tris;
+	uint32_t level;
+} svo_batch_mesh;
+
+/* A batcher builds many meshes together (the reference builds one mesh per Voxelizer::CmdVoxelize +
+ * OctreeBuilder::CmdBuild, src/Voxelizer.cpp:134-179, src/OctreeBuilder.cpp:142-210; LoaderThread
+ * drives one at a time, src/LoaderThread.cpp:43-116).  It owns device arenas that only grow (a repeated
+ * batch allocates nothing) and the CUDA graphs of its launch sequences.  Not thread-safe: one caller at
+ * a time per batcher. */
+typedef struct svo_batcher svo_batcher;
+
+int svo_batcher_create(svo_batcher **out);
+void svo_batcher_destroy(svo_batcher *b);
+
+/* Voxelizes and builds every mesh: one count pass over all triangles, one blocking readback of the
+ * per-mesh fragment counts, then the emit pass, every build level and the result export as launches
+ * that each cover all meshes (depths below level 10 of meshes finer than 2^10 run per mesh), recorded
+ * as a CUDA graph that is replayed while the batch's sizes and buffers are unchanged, and one blocking
+ * readback of the per-mesh results.  Per mesh, fragments and octree are identical to svo_voxelize +
+ * svo_build of that mesh alone.  Results are read with svo_batcher_result and stay valid until the
+ * next svo_batcher_build on this batcher or its destruction. */
+int svo_batcher_build(svo_batcher *b, const svo_batch_mesh *meshes, uint32_t n_meshes, void *stream);
+
+/* Number of meshes of the last batch. */
+uint32_t svo_batcher_meshes(const svo_batcher *b);
+
+/* Views of mesh `mesh` of the last batch (any output may be NULL): its fragment list and octree inside
+ * the batcher's shared fragment list and node pool (owned = 0: never destroy them), and its counters. */
+int svo_batcher_result(const svo_batcher *b, uint32_t mesh, svo_fraglist *frags, svo_octree *octree,
+                       svo_build_info *info);
+
+/* Graph recording on (default) or off (every launch issued directly). */
+int svo_batcher_set_graph(svo_batcher *b, int on);
+
+/* Graphs captured and replays since creation. */
+void svo_batcher_stats(const svo_batcher *b, uint64_t *graph_captures, uint64_t *graph_replays);
 
 /* ------------------------------------------------------------------ march (OctreeTracer) */
 

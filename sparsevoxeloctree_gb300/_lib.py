@@ -46,6 +46,10 @@ class CameraC(ctypes.Structure):
     _fields_ = [("pos", f32 * 4), ("look", f32 * 4), ("side", f32 * 4), ("up", f32 * 4)]
 
 
+class BatchMesh(ctypes.Structure):
+    _fields_ = [("tris", P), ("n_tris", u32), ("level", u32)]
+
+
 ALLOC_FN = ctypes.CFUNCTYPE(P, P, sz)
 RELEASE_FN = ctypes.CFUNCTYPE(None, P, P)
 
@@ -83,6 +87,13 @@ _SIGNATURES = {
     "svo_raycast": ([ctypes.POINTER(OctreeC), P, u32, P, P, P], i32),
     "svo_raycast_camera": ([ctypes.POINTER(OctreeC), ctypes.POINTER(CameraC), u32, u32, P, P, P], i32),
     "svo_bounce_rays": ([P, u32, u64, P, P], i32),
+    "svo_batcher_create": ([ctypes.POINTER(P)], i32),
+    "svo_batcher_destroy": ([P], None),
+    "svo_batcher_build": ([P, ctypes.POINTER(BatchMesh), u32, P], i32),
+    "svo_batcher_meshes": ([P], u32),
+    "svo_batcher_result": ([P, u32, ctypes.POINTER(Fraglist), ctypes.POINTER(OctreeC), ctypes.POINTER(BuildInfo)], i32),
+    "svo_batcher_set_graph": ([P, i32], i32),
+    "svo_batcher_stats": ([P, ctypes.POINTER(u64), ctypes.POINTER(u64)], None),
     "svo_camera_from_angles": ([ctypes.POINTER(f32), f32, f32, f32, f32, ctypes.POINTER(CameraC)], None),
 }
 

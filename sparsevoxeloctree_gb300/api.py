@@ -276,10 +276,24 @@ class Octree:
         return self.m_range
 
     def words(self) -> torch.Tensor:
+        if getattr(self, "_view", None) is not None:
+            return _copy_from(self._view.words, self.m_range // 4, torch.int32)
         return self.m_buffer[: self.m_range // 4]
 
     def c_struct(self) -> _lib.OctreeC:
+        if getattr(self, "_view", None) is not None:
+            return self._view
         return _lib.OctreeC(self.m_buffer.data_ptr(), self.m_buffer.numel(), self.m_range // 4, self.m_level, 0, 0)
+
+    @staticmethod
+    def FromView(view: _lib.OctreeC, owner=None) -> "Octree":
+        """An Octree over a node pool the engine owns (a batcher's shared pool): words() copies it out."""
+        o = Octree()
+        o._view = _lib.OctreeC(view.words, view.capacity, view.range_words, view.level, 0, 0)
+        o._owner = owner
+        o.m_range = int(view.range_words) * 4
+        o.m_level = int(view.level)
+        return o
 
 
 # ------------------------------------------------------------------------------------------- OctreeTracer
@@ -340,6 +354,77 @@ class OctreeTracer:
             rays = torch.empty(n * RAY_DTYPE.itemsize, dtype=torch.uint8, device=hits.device)
         _lib.check(_lib.load().svo_bounce_rays(_ptr(hits), n, seed & 0xFFFFFFFFFFFFFFFF, _ptr(rays), _stream(stream)))
         return rays
+
+
+# ------------------------------------------------------------------------------------------- batches
+def _copy_from(ptr: int, count: int, dtype: torch.dtype, device="cuda") -> torch.Tensor:
+    """Device copy of `count` elements at an engine-owned device address."""
+    out = torch.empty(count, dtype=dtype, device=device)
+    if count:
+        nbytes = count * out.element_size()
+        _lib.check(_lib.load().svo_download(_ptr(out), ctypes.c_void_p(ptr), nbytes, 1, _stream()))
+    return out
+
+
+class BatchBuilder:
+    """Many meshes voxelized and built together (svo_batcher): one count pass, one launch per stage for
+    all meshes with per-mesh offsets into a shared fragment list and node pool, the launch sequence
+    recorded as a CUDA graph and replayed for batches of the same shape.  Per mesh the result equals
+    Voxelizer.Create + OctreeBuilder.CmdBuild of that mesh alone."""
+
+    def __init__(self, use_graph: bool = True):
+        lib = _lib.load()
+        h = ctypes.c_void_p()
+        _lib.check(lib.svo_batcher_create(ctypes.byref(h)))
+        self.handle = h
+        _lib.check(lib.svo_batcher_set_graph(h, 1 if use_graph else 0))
+        self._meshes = None
+        self._keep = None
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value and _lib._lib is not None:
+            _lib._lib.svo_batcher_destroy(h)
+            self.handle = None
+
+    def Build(self, meshes, stream=None) -> None:
+        """meshes: sequence of (triangles, level), triangles a device tensor of TRIANGLE_DTYPE bytes (or a
+        numpy array, uploaded first)."""
+        tris = [to_device(np.asarray(t, TRIANGLE_DTYPE)) if isinstance(t, np.ndarray) else t for t, _ in meshes]
+        arr = (_lib.BatchMesh * len(tris))()
+        for i, (t, (_, level)) in enumerate(zip(tris, meshes)):
+            arr[i].tris = t.data_ptr() if t.numel() else 0
+            arr[i].n_tris = t.numel() // TRIANGLE_DTYPE.itemsize
+            arr[i].level = int(level)
+        self._keep = tris
+        _lib.check(_lib.load().svo_batcher_build(self.handle, arr, len(tris), _stream(stream)))
+        self._meshes = len(tris)
+
+    def __len__(self) -> int:
+        return int(_lib.load().svo_batcher_meshes(self.handle))
+
+    def result(self, i: int):
+        f, o, info = _lib.Fraglist(), _lib.OctreeC(), _lib.BuildInfo()
+        _lib.check(_lib.load().svo_batcher_result(self.handle, i, ctypes.byref(f), ctypes.byref(o), ctypes.byref(info)))
+        return f, o, info
+
+    def GetVoxelFragmentList(self, i: int) -> torch.Tensor:
+        f, _, _ = self.result(i)
+        return _copy_from(f.data or 0, int(f.count), torch.int64)
+
+    def GetOctree(self, i: int) -> Octree:
+        _, o, _ = self.result(i)
+        return Octree.FromView(o, owner=self)
+
+    def GetInfo(self, i: int) -> dict:
+        _, _, info = self.result(i)
+        return {"level": int(info.level), "fragments": int(info.fragments), "range_words": int(info.range_words),
+                "leaves": int(info.leaves), "level_nodes": [int(info.level_nodes[k]) for k in range(int(info.level))]}
+
+    def stats(self) -> dict:
+        c, r = _lib.u64(), _lib.u64()
+        _lib.load().svo_batcher_stats(self.handle, ctypes.byref(c), ctypes.byref(r))
+        return {"graph_captures": int(c.value), "graph_replays": int(r.value)}
 
 
 # ------------------------------------------------------------------------------------------- functional

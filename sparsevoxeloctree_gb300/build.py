@@ -27,6 +27,7 @@ UNITS = {
     "build.cu": [],
     "march.cu": ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"],
     "noalloc.cu": [],
+    "batch.cu": [],
 }
 HEADERS = ["common.cuh", "svo_internal.h"]
 
@@ -53,7 +54,9 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     cc = nvcc()
-    extra = extra or []
+    extra = list(extra or [])
+    if os.environ.get("SVO_CHECKED"):  # internal bounds checks (debug builds)
+        extra.append("-DSVO_CHECKED")
 
     def compile_unit(name: str) -> str:
         obj = os.path.join(BUILD, name.replace(".cu", ".o"))

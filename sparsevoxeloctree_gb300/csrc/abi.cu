@@ -42,6 +42,8 @@ static cudaEvent_t prof_event() {
 
 ProfScope::ProfScope(const char *name, cudaStream_t s) : slot(-1), stream(s) {
 	if (!g_prof_on.load(std::memory_order_relaxed)) return;
+	cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+	if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return; // graph replays are timed whole
 	std::lock_guard<std::mutex> lk(g_prof_mu);
 	ProfRecord r{name, prof_event(), prof_event()};
 	cudaEventRecord(r.begin, s);
@@ -155,6 +157,9 @@ static int check_level(uint32_t level) {
 }
 
 static int status_to_error(uint32_t status, const char *what) {
+	if (status & kStatusCheck) return fail(SVO_ERR_CUDA, "%s: internal bounds check %u failed", what, status >> 16);
+	if (status & kStatusBadFragment)
+		return fail(SVO_ERR_INVALID, "%s: fragment coordinates outside the octree level", what);
 	if (status & kStatusCapacity) return fail(SVO_ERR_CAPACITY, "%s: output exceeds its buffer or the 30-bit pointer range", what);
 	if (status & kStatusTimeout) return fail(SVO_ERR_TIMEOUT, "%s: a device-side wait gave up", what);
 	if (status & kStatusMalformed) return fail(SVO_ERR_INVALID, "%s: malformed octree pool", what);
@@ -181,13 +186,13 @@ void svo_device_free(void *ptr, void *stream) {
 
 int svo_upload(void *dst_device, const void *src_host, size_t bytes, void *stream) {
 	if (bytes && (!dst_device || !src_host)) return fail(SVO_ERR_INVALID, "null pointer");
-	SVO_CK(cudaMemcpyAsync(dst_device, src_host, bytes, cudaMemcpyHostToDevice, (cudaStream_t)stream), "upload");
+	SVO_CK(cudaMemcpyAsync(dst_device, src_host, bytes, cudaMemcpyDefault, (cudaStream_t)stream), "upload");
 	return SVO_OK;
 }
 
 int svo_download(void *dst_host, const void *src_device, size_t bytes, int sync, void *stream) {
 	if (bytes && (!dst_host || !src_device)) return fail(SVO_ERR_INVALID, "null pointer");
-	SVO_CK(cudaMemcpyAsync(dst_host, src_device, bytes, cudaMemcpyDeviceToHost, (cudaStream_t)stream), "download");
+	SVO_CK(cudaMemcpyAsync(dst_host, src_device, bytes, cudaMemcpyDefault, (cudaStream_t)stream), "download");
 	if (sync) SVO_CK(cudaStreamSynchronize((cudaStream_t)stream), "download synchronize");
 	return SVO_OK;
 }

@@ -26,6 +26,8 @@
 //           up to 257 fragments per voxel; a window where a voxel exceeds that is redone with exact
 //           64-bit sums in the same block.
 // Sizes stay on the device (BuildState): no host round trip inside a stage.
+#include <cstring>
+
 #include "common.cuh"
 #include "svo_internal.h"
 
@@ -36,7 +38,6 @@ constexpr int kAllocIPT = 8;
 constexpr int kAllocTile = kTPB * kAllocIPT;
 constexpr int kScanIPT = 8;
 constexpr int kScanTile = kTPB * kScanIPT;
-constexpr unsigned long long kLeafOne = 1ull << 48; // count field of a packed leaf accumulator
 
 // ------------------------------------------------------------------------------------------ helpers
 SVO_DEV void frag_xyz(uint64_t f, uint32_t &x, uint32_t &y, uint32_t &z) {
@@ -83,10 +84,68 @@ SVO_DEV uint32_t dense_child_word(const DenseView &dv, uint32_t x, uint32_t y, u
 	return 8u * (1u + grank(dv, depth - 1, morton(x, y, z, level - depth + 1))) + oct;
 }
 
+// ------------------------------------------------------------------------------------------ batches
+// Every stage runs over all meshes of a batch in one launch.  Work items are flat over the batch
+// (fragments, buckets, dense_write items) and find their mesh by a binary search over the [M+1] offsets;
+// a single build (B = false) takes its one mesh by value and searches nothing.
+template <typename T> SVO_DEV uint32_t mesh_search(const T *__restrict__ a, uint32_t M, T x) {
+	uint32_t lo = 0, hi = M; // a[lo] <= x < a[hi]
+	while (hi - lo > 1) {
+		const uint32_t mid = (lo + hi) >> 1;
+		if (__ldg(a + mid) <= x)
+			lo = mid;
+		else
+			hi = mid;
+	}
+	return lo;
+}
+
+template <bool B> SVO_DEV BuildMesh mesh_at(const BuildBatch &bb, uint32_t m) {
+	if constexpr (B)
+		return bb.table[m];
+	else
+		return bb.one;
+}
+
+template <bool B> SVO_DEV uint32_t batch_size(const BuildBatch &bb) { return B ? bb.M : 1u; }
+
+// Internal bounds checks, compiled in with -DSVO_CHECKED: a failed check records its id (first one
+// wins, in the batch state's pad word), sets kStatusCheck and skips the access it guards.
+#ifdef SVO_CHECKED
+SVO_DEV bool check_ok(bool ok, uint32_t id, BuildState *g) {
+	if (!ok) {
+		atomicCAS(&g->pad, 0u, id);
+		atomicOr(&g->status, kStatusCheck);
+	}
+	return ok;
+}
+#define SVO_CHECK(cond, id, g) check_ok((cond), (id), (g))
+#else
+#define SVO_CHECK(cond, id, g) true
+#endif
+
+// A fragment of a level-L octree has every coordinate below 2^L; the build skips any other (a caller's
+// malformed list) and reports it, and no later stage of the build (or batch) runs on it.
+// Conditions of the batch (or single build) state after which no later stage may trust the scans or the
+// fragment list: every stage that writes through scanned offsets skips its work and the call reports it.
+constexpr uint32_t kStatusAbort = kStatusTimeout | kStatusBadFragment;
+
+SVO_DEV bool frag_in_level(uint32_t x, uint32_t y, uint32_t z, uint32_t level) { return ((x | y | z) >> level) == 0u; }
+SVO_DEV void flag_bad_fragment(BuildState *state, BuildState *g) {
+	atomicOr(&state->status, kStatusBadFragment);
+	if (g != state) atomicOr(&g->status, kStatusBadFragment);
+}
+
 // ------------------------------------------------------------------------------------------ init
-__global__ void build_init(BuildState *state) {
+// Block m clears mesh m's state (and block 0 the batch-wide state of a batch).
+template <bool B> __global__ void build_init(BuildBatch bb, BuildState *gstate) {
+	BuildState *state = mesh_at<B>(bb, blockIdx.x).state;
 	uint32_t *s = reinterpret_cast<uint32_t *>(state);
 	for (uint32_t k = threadIdx.x; k < sizeof(BuildState) / 4; k += blockDim.x) s[k] = 0u;
+	if (B && blockIdx.x == 0) {
+		uint32_t *g = reinterpret_cast<uint32_t *>(gstate);
+		for (uint32_t k = threadIdx.x; k < sizeof(BuildState) / 4; k += blockDim.x) g[k] = 0u;
+	}
 	__syncthreads();
 	if (threadIdx.x == 0) state->lv[1] = LevelInfo{0u, 8u, 0u, 0u};
 }
@@ -94,33 +153,46 @@ __global__ void build_init(BuildState *state) {
 // ------------------------------------------------------------------------------------------ dense stage
 // Sets the depth-D occupancy bit of every fragment and counts the fragments of every bucket.  Per warp,
 // fragments that fall in the same bitmap word (or bucket) are merged first, so one atomic covers them.
-__global__ void __launch_bounds__(kTPB) dense_mark(const uint64_t *__restrict__ frags, uint32_t n, uint32_t level,
-                                                   DenseView dv, uint32_t bshift, uint32_t *__restrict__ bcount) {
-	const uint32_t shift = level - dv.D;
-	const uint32_t key_shift = 3 * (bshift - shift); // the bucket key is a prefix of the depth-D Morton code
-	uint32_t *bits = dv.bits + dv.off[dv.D];
+// Bitmap words and buckets are numbered over the whole batch, so merging never mixes meshes.
+template <bool B>
+__global__ void __launch_bounds__(kTPB) dense_mark(const uint64_t *__restrict__ frags, uint64_t n, BuildBatch bb,
+                                                   uint32_t *__restrict__ bcount) {
 	const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
 	for (uint64_t f = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; f < ((n + 31ull) & ~31ull); f += stride) {
 		uint32_t word = 0xffffffffu, bit = 0, key = 0xffffffffu;
 		if (f < n) {
+			const uint32_t mi = B ? mesh_search(bb.frag_base, bb.M, (unsigned long long)f) : 0u;
+			const BuildMesh md = mesh_at<B>(bb, mi);
 			uint32_t x, y, z;
 			frag_xyz(__ldcs(frags + f), x, y, z);
-			const uint32_t m = morton(x, y, z, shift);
-			word = m >> 5;
-			bit = 1u << (m & 31);
-			key = m >> key_shift;
+			const uint32_t D = md.dv.D;
+			if (!frag_in_level(x, y, z, md.level)) {
+				flag_bad_fragment(md.state, bb.gstate);
+			} else if (D >= 1) {
+				const uint32_t shift = md.level - D;
+				const uint32_t m = morton(x, y, z, shift);
+				word = md.mark_word + (m >> 5);
+				bit = 1u << (m & 31);
+				key = md.bucket_base + (m >> (3 * (md.bshift - shift))); // a prefix of the depth-D code
+			} else {
+				key = md.bucket_base + morton(x, y, z, md.bshift);
+			}
+			if (word != 0xffffffffu && !SVO_CHECK(word < bb.dense_total, 1u, bb.gstate)) word = 0xffffffffu, bit = 0;
+			if (key != 0xffffffffu && !SVO_CHECK(key < bb.nb_total, 2u, bb.gstate)) key = 0xffffffffu;
 		}
 		const uint32_t peers = __match_any_sync(kFullMask, word);
 		const uint32_t merged = __reduce_or_sync(peers, bit);
-		if (word != 0xffffffffu && lane_id() == (uint32_t)(__ffs(peers) - 1)) atomicOr(bits + word, merged);
-		// fragments per bucket (of 32^3 voxels), for the bucketed copy
+		if (word != 0xffffffffu && lane_id() == (uint32_t)(__ffs(peers) - 1)) atomicOr(bb.dense_bits + word, merged);
+		// fragments per bucket, for the bucketed copy
 		const uint32_t kpeers = __match_any_sync(kFullMask, key);
 		if (key != 0xffffffffu && lane_id() == (uint32_t)(__ffs(kpeers) - 1)) atomicAdd(bcount + key, __popc(kpeers));
 	}
 }
 
-// bitmap of depth d from depth d+1: bit p = (byte p of the child bitmap != 0).
-__global__ void dense_reduce(DenseView dv, uint32_t d) {
+// bitmap of depth d from depth d+1: bit p = (byte p of the child bitmap != 0).  blockIdx.y = mesh.
+template <bool B> __global__ void dense_reduce(BuildBatch bb, uint32_t d) {
+	const DenseView dv = mesh_at<B>(bb, blockIdx.y).dv;
+	if (dv.D < d + 1) return;
 	const uint32_t nbits = 1u << (3 * d);
 	const uint32_t nwords = (nbits + 31) / 32;
 	const uint8_t *child = reinterpret_cast<const uint8_t *>(dv.bits + dv.off[d + 1]);
@@ -142,58 +214,83 @@ __global__ void dense_reduce(DenseView dv, uint32_t d) {
 	}
 }
 
-// Exclusive prefix of popcounts over the concatenated bitmaps of depths 1..D; prefix[total] = total
-// occupied cells.  Persistent grid, tiles claimed in order by ticket.
-__global__ void __launch_bounds__(kTPB) dense_scan(DenseView dv, uint32_t total_words, BuildState *state,
+// Exclusive prefix of popcounts over the concatenated bitmaps of depths 1..D, segmented per mesh (a
+// mesh's region is whole tiles, the first of which starts a segment); prefix[W] = occupied cells of the
+// mesh for its region of W bitmap words (the padding words are zero).  Persistent grid, tiles claimed in
+// order by ticket.  A tile is kDenseTile words, 32 per thread read and written as 16-byte vectors: large
+// tiles keep the number of tiles in flight (and so the look-back distance) small against the work.
+constexpr int kDenseIPT = 32;
+constexpr uint32_t kDenseTile = kTPB * kDenseIPT;
+static_assert(kDenseTile == kBuildScanTile, "dense regions are padded to whole scan tiles");
+
+template <bool B>
+__global__ void __launch_bounds__(kTPB) dense_scan(BuildBatch bb, uint32_t total_words, BuildState *gstate,
                                                    unsigned long long *descs) {
 	__shared__ uint32_t s_tile;
 	__shared__ uint32_t s_warp[kTPB / 32 + 1];
 	__shared__ uint32_t s_prefix;
-	const uint32_t ntiles = (total_words + kScanTile - 1) / kScanTile;
+	const uint32_t *bits = bb.dense_bits;
+	uint32_t *prefix = bb.dense_prefix;
+	const uint32_t ntiles = total_words / kDenseTile; // regions are whole tiles
 	for (;;) {
-		if (threadIdx.x == 0) s_tile = atomicAdd(&state->tiles[0], 1u);
+		if (threadIdx.x == 0) s_tile = atomicAdd(&gstate->tiles[0], 1u);
 		__syncthreads();
 		const uint32_t tile = s_tile;
 		__syncthreads();
 		if (tile >= ntiles) break;
-		const uint32_t w0 = tile * kScanTile + threadIdx.x * kScanIPT;
-		uint32_t c[kScanIPT], local = 0;
+		const uint32_t first = tile * kDenseTile;
+		bool seg_start = tile == 0;
+		if constexpr (B) seg_start = __ldg(bb.dense_base + mesh_search(bb.dense_base, bb.M, first)) == first;
+		const uint32_t w0 = first + threadIdx.x * kDenseIPT;
+		const uint4 *src = reinterpret_cast<const uint4 *>(bits + w0);
+		uint32_t c[kDenseIPT], local = 0;
 #pragma unroll
-		for (int k = 0; k < kScanIPT; ++k) {
-			c[k] = w0 + k < total_words ? __popc(dv.bits[w0 + k]) : 0u;
-			local += c[k];
+		for (int k = 0; k < kDenseIPT / 4; ++k) {
+			const uint4 v = __ldcs(src + k);
+			c[4 * k] = __popc(v.x), c[4 * k + 1] = __popc(v.y), c[4 * k + 2] = __popc(v.z), c[4 * k + 3] = __popc(v.w);
 		}
+#pragma unroll
+		for (int k = 0; k < kDenseIPT; ++k) local += c[k];
 		uint32_t total;
 		uint32_t run = block_exclusive_sum<uint32_t, kTPB>(local, s_warp, total);
 		if (threadIdx.x < 32) {
-			const uint32_t p = (uint32_t)tile_lookback_warp(descs, tile, 15u, total, &state->status);
+			const uint32_t p = (uint32_t)tile_lookback_warp(descs, tile, 15u, total, &gstate->status, seg_start);
 			if (threadIdx.x == 0) s_prefix = p;
 		}
 		__syncthreads();
 		run += s_prefix;
+		uint4 *dst = reinterpret_cast<uint4 *>(prefix + w0);
 #pragma unroll
-		for (int k = 0; k < kScanIPT; ++k) {
-			if (w0 + k < total_words) dv.prefix[w0 + k] = run;
-			run += c[k];
+		for (int k = 0; k < kDenseIPT / 4; ++k) {
+			uint4 o;
+			o.x = run, run += c[4 * k];
+			o.y = run, run += c[4 * k + 1];
+			o.z = run, run += c[4 * k + 2];
+			o.w = run, run += c[4 * k + 3];
+			dst[k] = o;
 		}
-		if (tile == ntiles - 1 && threadIdx.x == 0) dv.prefix[total_words] = s_prefix + total;
 		__syncthreads();
 	}
 }
 
-// Level ranges of depths 1..D+1 from the scanned counts (BuildState.lv as the sparse stage keeps it).
-__global__ void dense_finish(DenseView dv, BuildState *state) {
-	if (threadIdx.x != 0) return;
-	// occupied cells of depth d: N_d = prefix[off[d+1]] - prefix[off[d]]; cells of depths < d: prefix[off[d]]
-	for (uint32_t d = 1; d <= dv.D + 1; ++d) {
-		const uint32_t before_parent = d >= 2 ? dv.prefix[dv.off[d - 1]] : 0u; // occupied cells of depths < d-1
-		const uint32_t parents = d >= 2 ? dv.prefix[dv.off[d]] - dv.prefix[dv.off[d - 1]] : 1u;
-		LevelInfo li;
-		li.begin = d == 1 ? 0u : 8u * (1u + before_parent);
-		li.num = 8u * parents;
-		li.blocks_before = d == 1 ? 0u : dv.prefix[dv.off[d]];
-		li.nodes = d <= dv.D ? dv.prefix[dv.off[d + 1]] - dv.prefix[dv.off[d]] : 0u;
-		state->lv[d] = li;
+// Level ranges of depths 1..D+1 from the scanned counts (BuildState.lv as the sparse stage keeps it);
+// one thread per mesh.
+template <bool B> __global__ void dense_finish(BuildBatch bb) {
+	for (uint32_t mi = blockIdx.x * blockDim.x + threadIdx.x; mi < batch_size<B>(bb); mi += gridDim.x * blockDim.x) {
+		const BuildMesh md = mesh_at<B>(bb, mi);
+		const DenseView &dv = md.dv;
+		if (dv.D == 0) continue;
+		// occupied cells of depth d: N_d = prefix[off[d+1]] - prefix[off[d]]; cells of depths < d: prefix[off[d]]
+		for (uint32_t d = 1; d <= dv.D + 1; ++d) {
+			const uint32_t before_parent = d >= 2 ? dv.prefix[dv.off[d - 1]] : 0u; // occupied cells of depths < d-1
+			const uint32_t parents = d >= 2 ? dv.prefix[dv.off[d]] - dv.prefix[dv.off[d - 1]] : 1u;
+			LevelInfo li;
+			li.begin = d == 1 ? 0u : 8u * (1u + before_parent);
+			li.num = 8u * parents;
+			li.blocks_before = d == 1 ? 0u : dv.prefix[dv.off[d]];
+			li.nodes = d <= dv.D ? dv.prefix[dv.off[d + 1]] - dv.prefix[dv.off[d]] : 0u;
+			md.state->lv[d] = li;
+		}
 	}
 }
 
@@ -201,18 +298,19 @@ __global__ void dense_finish(DenseView dv, BuildState *state) {
 // sparse children: interior words of depths 1..D, and zeroed words of depth D+1 when sparse levels
 // follow.  When depth D+1 is the leaf depth, depth-D cells are skipped: the leaf stage writes those
 // blocks whole.  One bitmap word and one prefix word of the child depth serve all 8 children.
-__global__ void __launch_bounds__(kTPB) dense_write(uint32_t *__restrict__ pool, uint64_t capacity, DenseView dv,
-                                                    uint32_t level, BuildState *state) {
-	const uint32_t D = dv.D;
-	const bool leaf_next = D + 1 == level;
-	const uint32_t last_parent_depth = leaf_next ? D - 1 : D;
-	const uint32_t parent_words = dv.off[last_parent_depth + 1]; // words of parent depths 1..last; item 0 = root
-	for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item <= parent_words; item += gridDim.x * blockDim.x) {
+template <bool B>
+__global__ void __launch_bounds__(kTPB) dense_write(BuildBatch bb, uint32_t total_items) {
+	for (uint32_t gitem = blockIdx.x * blockDim.x + threadIdx.x; gitem < total_items; gitem += gridDim.x * blockDim.x) {
+		const uint32_t mi = B ? mesh_search(bb.item_base, bb.M, gitem) : 0u;
+		const BuildMesh md = mesh_at<B>(bb, mi);
+		const DenseView &dv = md.dv;
+		const uint32_t item = gitem - md.item_base;
+		const uint32_t D = dv.D;
 		uint32_t bits, e, base_m, r;
 		if (item == 0) { // the root: a single occupied cell whose block (words 0..7) holds the depth-1 nodes
 			bits = 1u, e = 0, base_m = 0, r = 0;
 		} else {
-			const uint32_t gw = item - 1; // global word of a parent depth e in 1..last
+			const uint32_t gw = item - 1; // word of a parent depth e in 1..last
 			e = 1;
 			while (gw >= dv.off[e + 1]) ++e;
 			bits = __ldg(dv.bits + gw);
@@ -225,8 +323,8 @@ __global__ void __launch_bounds__(kTPB) dense_write(uint32_t *__restrict__ pool,
 			bits &= bits - 1;
 			const uint32_t q = base_m + b; // parent cell (depth e)
 			const uint64_t blk = e == 0 ? 0ull : 8ull * (1u + r++);
-			if (blk + 8 > capacity || blk + 8 > SVO_MAX_POOL_WORDS) {
-				atomicOr(&state->status, kStatusCapacity);
+			if (blk + 8 > md.capacity || blk + 8 > SVO_MAX_POOL_WORDS) {
+				atomicOr(&md.state->status, kStatusCapacity);
 				continue;
 			}
 			uint32_t w[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
@@ -239,7 +337,7 @@ __global__ void __launch_bounds__(kTPB) dense_write(uint32_t *__restrict__ pool,
 				for (int o = 0; o < 8; ++o)
 					if ((kids >> o) & 1u) w[o] = 0x80000000u | (8u * (1u + rank0 + __popc(kids & ((1u << o) - 1u))));
 			}
-			uint4 *dst = reinterpret_cast<uint4 *>(pool + blk);
+			uint4 *dst = reinterpret_cast<uint4 *>(md.pool + blk);
 			dst[0] = make_uint4(w[0], w[1], w[2], w[3]);
 			dst[1] = make_uint4(w[4], w[5], w[6], w[7]);
 		}
@@ -262,16 +360,18 @@ SVO_DEV void tag_one(uint64_t frag, uint32_t &node, uint32_t level, uint32_t dep
 	node = idx;
 }
 
+// One mesh's sparse depth (meshes of a batch with sparse depths run these one mesh at a time).
 __global__ void __launch_bounds__(kTPB) build_tag(const uint64_t *__restrict__ frags, uint32_t n, uint32_t level,
                                                   uint32_t depth, uint32_t *__restrict__ pool,
-                                                  uint32_t *__restrict__ cache, DenseView dv, BuildState *state) {
-	if (state->status & kStatusCapacity) return;
+                                                  uint32_t *__restrict__ cache, DenseView dv, BuildState *state,
+                                                  const BuildState *gstate) {
+	if ((state->status & kStatusCapacity) || (gstate->status & kStatusAbort)) return;
 	const bool parent_dense = depth == 1 || depth - 1 <= dv.D;
 	const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
 	const uint64_t nq = (n + 3ull) / 4ull;
 	for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += stride) {
 		const uint64_t f0 = q * 4;
-		if (f0 + 4 <= n) { // the sorted copy is 256-byte aligned: 16-byte loads
+		if (f0 + 4 <= n) { // the sorted copy of a mesh is 32-byte aligned: 16-byte loads
 			const ulonglong2 a = __ldcs(reinterpret_cast<const ulonglong2 *>(frags + f0));
 			const ulonglong2 b = __ldcs(reinterpret_cast<const ulonglong2 *>(frags + f0 + 2));
 			uint4 c = make_uint4(0, 0, 0, 0);
@@ -291,18 +391,19 @@ __global__ void __launch_bounds__(kTPB) build_tag(const uint64_t *__restrict__ f
 	}
 }
 
-
 // Prefix-sum allocation of child blocks for the marked words of a sparse depth (persistent grid, tiles
 // claimed in order by ticket so the look-back always waits on a running or finished tile).  The block
 // of a node is zeroed (the next depth's init) unless the next depth is the leaf depth.
 __global__ void __launch_bounds__(kTPB) build_alloc(uint32_t *__restrict__ pool, uint64_t capacity, uint32_t depth,
-                                                    uint32_t level, BuildState *state, unsigned long long *descs) {
+                                                    uint32_t level, BuildState *state, unsigned long long *descs,
+                                                    const BuildState *gstate) {
 	__shared__ uint32_t s_tile;
 	__shared__ uint32_t s_warp[kTPB / 32 + 1];
 	__shared__ uint32_t s_prefix;
 	__shared__ uint32_t s_abort;
 	// other blocks of this launch may set the capacity flag: decide once per block
-	if (threadIdx.x == 0) s_abort = atomicOr(&state->status, 0u) & kStatusCapacity;
+	if (threadIdx.x == 0)
+		s_abort = (atomicOr(&state->status, 0u) & kStatusCapacity) | (gstate->status & kStatusAbort);
 	__syncthreads();
 	if (s_abort) return;
 	const LevelInfo li = state->lv[depth];
@@ -379,30 +480,18 @@ __global__ void __launch_bounds__(kTPB) build_alloc(uint32_t *__restrict__ pool,
 }
 
 // ------------------------------------------------------------------------------------------ buckets
-// The fragments are copied once into buckets of 32^3 voxels (Morton order of the bucket, any order
+// The fragments are copied once into buckets of voxels (Morton order of the bucket, any order
 // inside one).  All later sweeps read the bucketed copy: the sparse tag passes then touch the pool
 // region by region, and the leaf stage gives each bucket to one block, which accumulates its leaf
 // colours in shared memory.  The leaf blocks (8 words per depth L-1 node) of one bucket are contiguous
 // in the pool (breadth-first order is Morton order within a depth), so that block writes them whole.
-constexpr uint32_t kBucketVoxelBits = 5; // bucket edge: 32 voxels
+// In a batch the buckets of all meshes are concatenated in mesh order, so one scan over all of them
+// places every mesh's bucketed copy after the previous mesh's.
+// Bucket edge: 32 voxels (16^3 leaf parents).  Smaller buckets bound the leaf stage's span per bucket
+// but multiply its per-bucket cost (measured on the 2^10 room scene: 16-voxel buckets took 2.5x longer).
+uint32_t bucket_shift(uint32_t level) { return std::min<uint32_t>(level, 5u); }
 
 SVO_DEV uint32_t bucket_of(uint32_t x, uint32_t y, uint32_t z, uint32_t bshift) { return morton(x, y, z, bshift); }
-
-// Fragment counts per bucket (used when the dense stage does not run: level 1).
-__global__ void __launch_bounds__(kTPB) bucket_hist(const uint64_t *__restrict__ frags, uint32_t n, uint32_t bshift,
-                                                    uint32_t *__restrict__ bcount) {
-	const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-	for (uint64_t f = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; f < ((n + 31ull) & ~31ull); f += stride) {
-		uint32_t key = 0xffffffffu;
-		if (f < n) {
-			uint32_t x, y, z;
-			frag_xyz(frags[f], x, y, z);
-			key = bucket_of(x, y, z, bshift);
-		}
-		const uint32_t peers = __match_any_sync(kFullMask, key);
-		if (key != 0xffffffffu && lane_id() == (uint32_t)(__ffs(peers) - 1)) atomicAdd(bcount + key, __popc(peers));
-	}
-}
 
 // Exclusive prefix of the bucket counts (boff[nb] = total) and the list of non-empty buckets in order;
 // two single-pass look-back scans, tiles claimed in order by ticket.
@@ -454,46 +543,61 @@ __global__ void __launch_bounds__(kTPB) bucket_scan(const uint32_t *__restrict__
 // When the leaf depth's parents are dense (level <= 10), the copy holds leaf items instead of fragments:
 // the leaf word slot (from the dense bitmap of depth level-1) in the high word and the colour in the low
 // one, so the leaf stage needs no lookups.
-__global__ void __launch_bounds__(kTPB) bucket_scatter(const uint64_t *__restrict__ frags, uint32_t n,
-                                                       uint32_t bshift, const uint32_t *__restrict__ boff,
-                                                       uint32_t *__restrict__ bfill, uint64_t *__restrict__ sorted,
-                                                       bool items, DenseView dv, uint32_t level,
-                                                       const BuildState *state) {
+template <bool B>
+__global__ void __launch_bounds__(kTPB) bucket_scatter(const uint64_t *__restrict__ frags, uint64_t n, BuildBatch bb,
+                                                       const uint32_t *__restrict__ boff, uint32_t *__restrict__ bfill,
+                                                       uint64_t *__restrict__ sorted) {
 	const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
 	const uint32_t lane = lane_id();
-	const uint32_t *pbits = items && level > 1 ? dv.bits + dv.off[level - 1] : nullptr;
-	const uint32_t *pprefix = items && level > 1 ? dv.prefix + dv.off[level - 1] : nullptr;
-	const uint32_t leaf_begin = items ? state->lv[level].begin : 0u;
 	for (uint64_t f = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; f < ((n + 31ull) & ~31ull); f += stride) {
-		uint32_t key = 0xffffffffu;
-		uint64_t out = 0;
+		uint32_t key = 0xffffffffu, pad = 0;
+		uint64_t out = 0, send = 0;
 		if (f < n) {
+			const uint32_t mi = B ? mesh_search(bb.frag_base, bb.M, (unsigned long long)f) : 0u;
+			const BuildMesh md = mesh_at<B>(bb, mi);
+			const uint32_t level = md.level;
+			const bool items = level == 1 || level - 1 <= md.dv.D;
 			const uint64_t frag = __ldcs(frags + f);
 			uint32_t x, y, z;
 			frag_xyz(frag, x, y, z);
 			out = frag;
-			if (pbits) { // parent cell m (depth level-1); the bucket key is its prefix
+			if (!frag_in_level(x, y, z, level)) {
+				// skipped (dense_mark reported it)
+			} else if (items && level > 1) { // parent cell m (depth level-1); the bucket key is its prefix
+				const uint32_t *pbits = md.dv.bits + md.parent_off;
+				const uint32_t *pprefix = md.dv.prefix + md.parent_off;
+				const uint32_t leaf_begin = md.state->lv[level].begin;
 				const uint32_t m = morton(x, y, z, 1), w = m >> 5;
-				key = m >> (3 * (bshift - 1));
+				key = m >> (3 * (md.bshift - 1));
 				out = ((uint64_t)(octant_at(x, y, z, 0) + 8u * (1u + __ldg(pprefix + w) +
 				                                                 __popc(__ldg(pbits + w) & ((1u << (m & 31)) - 1u))) -
 				                  leaf_begin)
 				       << 32) |
 				      ((frag >> 32) & 0xffffffu);
 			} else {
-				key = bucket_of(x, y, z, bshift);
+				key = bucket_of(x, y, z, md.bshift);
+				if (items) // level 1: the leaf words are the root block
+					out = ((uint64_t)octant_at(x, y, z, 0) << 32) | ((frag >> 32) & 0xffffffu);
 			}
-			if (items && !pbits) {
-				const uint32_t idx = octant_at(x, y, z, 0);
-				out = ((uint64_t)(idx - leaf_begin) << 32) | ((frag >> 32) & 0xffffffu);
+			if (key != 0xffffffffu) {
+				key += md.bucket_base;
+				if (!SVO_CHECK(key < bb.nb_total, 3u, bb.gstate)) key = 0xffffffffu;
 			}
+			pad = md.sorted_pad;
+			send = md.frag_base + md.sorted_pad + md.count;
 		}
 		const uint32_t peers = __match_any_sync(kFullMask, key);
 		const uint32_t leader = __ffs(peers) - 1;
 		uint32_t base = 0;
 		if (key != 0xffffffffu && lane == leader) base = atomicAdd(bfill + key, __popc(peers));
 		base = __shfl_sync(kFullMask, base, leader);
-		if (key != 0xffffffffu) sorted[boff[key] + base + __popc(peers & ((1u << lane) - 1u))] = out;
+		if (key != 0xffffffffu) {
+			const uint64_t at = (uint64_t)boff[key] + pad + base + __popc(peers & ((1u << lane) - 1u));
+			if (at < send) // always true after a complete bucket scan (a timed-out scan is reported)
+				sorted[at] = out;
+			else
+				SVO_CHECK(false, 4u, bb.gstate);
+		}
 	}
 }
 
@@ -515,57 +619,54 @@ SVO_DEV uint32_t leaf_word(uint32_t n, uint32_t sr, uint32_t sg, uint32_t sb) {
 	return 0xC0000000u | (min(n, 63u) << 24) | (b << 16) | (g << 8) | r;
 }
 
-// Where the leaf stage finds the parent of a leaf: the dense bitmap of depth level-1 (its words at
-// bits/prefix) or, below the dense depths, the node index cached per fragment by the last sparse tag.
-struct LeafParent {
-	const uint32_t *bits, *prefix; // dense depth level-1 (null at level 1: the parent is the root)
-	const uint32_t *pool, *cache;  // sparse parent
-	uint32_t leaf_begin;
-};
-
-// Leaf word slot (index from the start of the leaf range) of fragment f of the bucketed copy.
-SVO_DEV uint32_t leaf_slot(uint64_t frag, uint64_t f, const LeafParent &lp) {
+// Leaf word slot (index from the start of the leaf range) of fragment f of the bucketed copy, for a
+// mesh whose leaf parents are sparse: through the node index cached per fragment by the last sparse tag.
+SVO_DEV uint32_t leaf_slot(uint64_t frag, uint64_t f, const uint32_t *__restrict__ pool,
+                           const uint32_t *__restrict__ cache, uint32_t leaf_begin) {
 	uint32_t x, y, z;
 	frag_xyz(frag, x, y, z);
-	const uint32_t oct = octant_at(x, y, z, 0);
-	uint32_t idx;
-	if (lp.cache) {
-		idx = (__ldg(lp.pool + __ldg(lp.cache + f)) & 0x3fffffffu) + oct;
-	} else if (lp.bits) { // 8 * (1 + grank(level-1, parent)) + octant
-		const uint32_t m = morton(x, y, z, 1);
-		const uint32_t w = m >> 5;
-		idx = 8u * (1u + __ldg(lp.prefix + w) + __popc(__ldg(lp.bits + w) & ((1u << (m & 31)) - 1u))) + oct;
-	} else {
-		idx = oct;
-	}
-	return idx - lp.leaf_begin;
+	return (__ldg(pool + __ldg(cache + f)) & 0x3fffffffu) + octant_at(x, y, z, 0) - leaf_begin;
 }
 
 constexpr uint32_t kLeafSlots = 4096;         // packed accumulators in shared memory (8 B each)
 constexpr uint32_t kWideSlots = kLeafSlots / 4; // exact accumulators (4 x 8 B each) of the overflow path
 
 // Extent of every non-empty bucket, in list order: first and last item, first and last leaf slot
-// (lo = 0xffffffff, hi = 0 when the leaf stage reduces the span over the bucket's fragments).
+// (lo = 0xffffffff, hi = 0 when the leaf stage reduces the span over the bucket's fragments), and for
+// a batch the bucket's mesh.
 //   one bucket (level <= 5): the whole leaf range;
-//   dense parents: bucket b is 4096 parent cells = 128 words of the depth level-1 bitmap, and the prefix
-//     entries at its first word and at the next bucket's give its first and last leaf block.
-__global__ void bucket_meta(const uint32_t *__restrict__ boff, const uint32_t *__restrict__ blist, uint32_t nb,
-                            DenseView dv, uint32_t level, const BuildState *state, uint4 *__restrict__ meta) {
-	const uint32_t nbuckets = state->buckets;
-	const bool items = level == 1 || level - 1 <= dv.D;
-	const uint32_t leaf_begin = state->lv[level].begin, leaf_num = state->lv[level].num;
-	const uint32_t *pprefix = items && level > 1 ? dv.prefix + dv.off[level - 1] : nullptr;
+//   dense parents: bucket b is 8^(bshift-1) parent cells (128 words of the depth level-1 bitmap), and the
+//     prefix entries at its first word and at the next bucket's give its first and last leaf block.
+// Also writes every mesh's range (its leaf range is final once the interior levels are built).
+template <bool B>
+__global__ void bucket_meta(BuildBatch bb, const uint32_t *__restrict__ boff, const uint32_t *__restrict__ blist,
+                            const BuildState *gstate, uint4 *__restrict__ meta, uint32_t *__restrict__ bmesh) {
+	const uint32_t nbuckets = gstate->buckets;
 	for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nbuckets; t += gridDim.x * blockDim.x) {
 		const uint32_t b = blist[t];
-		uint4 m = make_uint4(boff[b], boff[b + 1], 0xffffffffu, 0u);
-		if (nb == 1) {
+		const uint32_t mi = B ? mesh_search(bb.bucket_base, bb.M, b) : 0u;
+		const BuildMesh md = mesh_at<B>(bb, mi);
+		const uint32_t level = md.level, bl = b - md.bucket_base;
+		const bool items = level == 1 || level - 1 <= md.dv.D;
+		const uint32_t leaf_begin = md.state->lv[level].begin, leaf_num = md.state->lv[level].num;
+		uint4 m = make_uint4(boff[b] + md.sorted_pad, boff[b + 1] + md.sorted_pad, 0xffffffffu, 0u);
+		if (md.nb == 1) {
 			m.z = 0, m.w = leaf_num - 1;
-		} else if (pprefix) {
+		} else if (items && level > 1) {
+			const uint32_t *pprefix = md.dv.prefix + md.dv.off[level - 1];
 			const uint32_t before = leaf_begin / 8u - 1u; // occupied cells of depths below the parents
-			m.z = 8u * (pprefix[128u * b] - before);
-			m.w = 8u * (pprefix[128u * (b + 1)] - before) - 1u;
+			const uint32_t wpb = (1u << (3 * (md.bshift - 1))) >> 5; // parent-bitmap words per bucket
+			m.z = 8u * (pprefix[wpb * bl] - before);
+			m.w = 8u * (pprefix[wpb * (bl + 1)] - before) - 1u;
 		}
+		if (!SVO_CHECK(m.y <= bb.sorted_total && m.x <= m.y, 5u, bb.gstate)) m.y = m.x;
+		if (m.z <= m.w && !SVO_CHECK(m.w < leaf_num, 6u, bb.gstate)) m.y = m.x;
 		meta[t] = m;
+		if (B) bmesh[t] = mi;
+	}
+	for (uint32_t mi = blockIdx.x * blockDim.x + threadIdx.x; mi < batch_size<B>(bb); mi += gridDim.x * blockDim.x) {
+		const BuildMesh md = mesh_at<B>(bb, mi);
+		md.state->range_words = md.state->lv[md.level].begin + md.state->lv[md.level].num;
 	}
 }
 
@@ -578,32 +679,38 @@ __global__ void bucket_meta(const uint32_t *__restrict__ boff, const uint32_t *_
 // sums, kWideSlots slots at a time.
 //   items (dense parents): the bucketed copy holds (slot << 32 | rgb);
 //   otherwise: fragments, slots through the cached parent index, span reduced over the bucket.
-__global__ void __launch_bounds__(kTPB) build_leaf(const uint64_t *__restrict__ sorted, uint32_t level,
-                                                   uint32_t *__restrict__ pool, uint64_t capacity,
-                                                   const uint32_t *__restrict__ cache, DenseView dv,
-                                                   const uint4 *__restrict__ meta, BuildState *state) {
+template <bool B>
+__global__ void __launch_bounds__(kTPB) build_leaf(const uint64_t *__restrict__ sorted, BuildBatch bb,
+                                                   const uint32_t *__restrict__ cache, const uint4 *__restrict__ meta,
+                                                   const uint32_t *__restrict__ bmesh, BuildState *gstate) {
 	extern __shared__ unsigned long long s_acc[];
 	uint32_t *s_acc32 = reinterpret_cast<uint32_t *>(s_acc);
-	__shared__ uint32_t s_lo, s_hi, s_over, s_leaves;
-	if (state->status & kStatusCapacity) return;
-	const uint64_t leaf_end = (uint64_t)state->lv[level].begin + state->lv[level].num;
-	if (leaf_end > capacity || leaf_end > SVO_MAX_POOL_WORDS) { // leaf blocks of dense parents: checked here
-		if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&state->status, kStatusCapacity);
-		return;
-	}
-	const bool items = level == 1 || level - 1 <= dv.D;
-	const uint32_t leaf_begin = state->lv[level].begin;
-	LeafParent lp;
-	lp.bits = nullptr, lp.prefix = nullptr;
-	lp.pool = pool;
-	lp.cache = cache;
-	lp.leaf_begin = leaf_begin;
-	const uint32_t nbuckets = state->buckets;
-	if (threadIdx.x == 0) s_leaves = 0;
+	__shared__ uint32_t s_lo, s_hi, s_over, s_leaves, s_skip;
+	const uint32_t nbuckets = gstate->buckets;
 	uint4 next = blockIdx.x < nbuckets ? meta[blockIdx.x] : make_uint4(0, 0, 0, 0);
 	for (uint32_t t = blockIdx.x; t < nbuckets; t += gridDim.x) {
 		const uint4 m = next;
 		if (t + gridDim.x < nbuckets) next = meta[t + gridDim.x];
+		const BuildMesh md = mesh_at<B>(bb, B ? bmesh[t] : 0u);
+		const uint32_t level = md.level;
+		const uint32_t leaf_begin = md.state->lv[level].begin;
+		if (threadIdx.x == 0) {
+			const uint64_t leaf_end = (uint64_t)leaf_begin + md.state->lv[level].num;
+			uint32_t skip = (md.state->status & kStatusCapacity) | (gstate->status & kStatusAbort);
+			if (!skip && (leaf_end > md.capacity || leaf_end > SVO_MAX_POOL_WORDS)) { // leaf blocks of dense parents
+				atomicOr(&md.state->status, kStatusCapacity);
+				skip = 1;
+			}
+			s_skip = skip;
+			s_leaves = 0;
+		}
+		__syncthreads();
+		if (s_skip) { // block-uniform
+			__syncthreads();
+			continue;
+		}
+		const bool items = level == 1 || level - 1 <= md.dv.D;
+		const uint32_t *pool_c = md.pool;
 		const uint32_t f0 = m.x, f1 = m.y;
 		uint32_t span_lo = m.z & ~7u, span_hi = (m.w | 7u) + 1u;
 		if (m.z > m.w) { // span reduced over the bucket's fragments
@@ -617,7 +724,7 @@ __global__ void __launch_bounds__(kTPB) build_leaf(const uint64_t *__restrict__ 
 #pragma unroll
 				for (int k = 0; k < 4; ++k)
 					if (fb + k * kTPB < f1) {
-						const uint32_t sl = leaf_slot(fr[k], fb + k * kTPB, lp);
+						const uint32_t sl = leaf_slot(fr[k], fb + k * kTPB, pool_c, cache, leaf_begin);
 						lo = min(lo, sl), hi = max(hi, sl);
 					}
 			}
@@ -625,6 +732,10 @@ __global__ void __launch_bounds__(kTPB) build_leaf(const uint64_t *__restrict__ 
 			if (lane_id() == 0) atomicMin(&s_lo, lo), atomicMax(&s_hi, hi);
 			__syncthreads();
 			span_lo = s_lo & ~7u, span_hi = (s_hi | 7u) + 1u;
+		}
+		if (span_hi > md.state->lv[level].num) { // only after a reported scan failure: never leave the leaf range
+			SVO_CHECK(false, 7u, gstate);
+			span_hi = span_lo;
 		}
 		for (uint32_t w0 = span_lo; w0 < span_hi; w0 += kLeafSlots) {
 			const uint32_t wn = min(kLeafSlots, span_hi - w0);
@@ -640,7 +751,8 @@ __global__ void __launch_bounds__(kTPB) build_leaf(const uint64_t *__restrict__ 
 #pragma unroll
 				for (int k = 0; k < 4; ++k) {
 					const bool in = fb + k * kTPB < f1;
-					sl[k] = !in ? 0xffffffffu : (items ? (uint32_t)(fr[k] >> 32) : leaf_slot(fr[k], fb + k * kTPB, lp)) - w0;
+					sl[k] = !in ? 0xffffffffu
+					            : (items ? (uint32_t)(fr[k] >> 32) : leaf_slot(fr[k], fb + k * kTPB, pool_c, cache, leaf_begin)) - w0;
 					rgb[k] = items ? (uint32_t)fr[k] : (uint32_t)(fr[k] >> 32);
 				}
 #pragma unroll
@@ -653,6 +765,7 @@ __global__ void __launch_bounds__(kTPB) build_leaf(const uint64_t *__restrict__ 
 			if (__any_sync(kFullMask, over) && lane_id() == 0) s_over = 1;
 			__syncthreads();
 			uint32_t leaves = 0;
+			uint32_t *dst = md.pool + leaf_begin + w0;
 			if (!s_over) {
 				for (uint32_t i = 4 * threadIdx.x; i < wn; i += 4 * kTPB) {
 					const uint4 a = *reinterpret_cast<const uint4 *>(s_acc32 + 2 * i);
@@ -665,7 +778,7 @@ __global__ void __launch_bounds__(kTPB) build_leaf(const uint64_t *__restrict__ 
 						word[j] = n ? leaf_word(n, rg[j] & 0xffffu, rg[j] >> 16, bn[j] & 0xffffu) : 0u;
 						leaves += word[j] != 0u;
 					}
-					*reinterpret_cast<uint4 *>(pool + leaf_begin + w0 + i) = make_uint4(word[0], word[1], word[2], word[3]);
+					*reinterpret_cast<uint4 *>(dst + i) = make_uint4(word[0], word[1], word[2], word[3]);
 				}
 			} else {
 				// exact sums for this window, kWideSlots slots at a time
@@ -677,7 +790,8 @@ __global__ void __launch_bounds__(kTPB) build_leaf(const uint64_t *__restrict__ 
 					__syncthreads();
 					for (uint32_t f = f0 + threadIdx.x; f < f1; f += kTPB) {
 						const uint64_t item = sorted[f];
-						const uint32_t sl = (items ? (uint32_t)(item >> 32) : leaf_slot(item, f, lp)) - w0 - v0;
+						const uint32_t sl =
+						    (items ? (uint32_t)(item >> 32) : leaf_slot(item, f, pool_c, cache, leaf_begin)) - w0 - v0;
 						const uint32_t c = items ? (uint32_t)item : (uint32_t)(item >> 32);
 						if (sl < vn) {
 							atomicAdd(acc4 + 4 * sl, (unsigned long long)(c & 0xffu));
@@ -691,7 +805,7 @@ __global__ void __launch_bounds__(kTPB) build_leaf(const uint64_t *__restrict__ 
 						const unsigned long long n = acc4[4 * i + 3];
 						// n < 2^32 (fragment counts are 32-bit)
 						const uint32_t word = n ? leaf_word_wide((uint32_t)n, acc4[4 * i], acc4[4 * i + 1], acc4[4 * i + 2]) : 0u;
-						pool[leaf_begin + w0 + v0 + i] = word;
+						dst[v0 + i] = word;
 						leaves += word != 0u;
 					}
 				}
@@ -700,25 +814,31 @@ __global__ void __launch_bounds__(kTPB) build_leaf(const uint64_t *__restrict__ 
 			if (lane_id() == 0 && leaves) atomicAdd(&s_leaves, leaves);
 			__syncthreads();
 		}
-	}
-	__syncthreads();
-	if (threadIdx.x == 0) {
-		if (s_leaves) atomicAdd(&state->leaves, s_leaves);
-		if (blockIdx.x == 0) state->range_words = leaf_end;
+		if (threadIdx.x == 0 && s_leaves) atomicAdd(&md.state->leaves, s_leaves);
+		__syncthreads();
 	}
 }
 
-// Writes svo_build_info followed by the status word to `out` (device) from the build state.
-__global__ void build_export(const BuildState *state, uint32_t level, uint32_t count, uint32_t *out) {
-	if (threadIdx.x != 0) return;
-	svo_build_info *info = reinterpret_cast<svo_build_info *>(out);
-	info->level = level;
-	info->fragments = count;
-	info->range_words = state->range_words;
-	info->leaves = state->leaves;
-	for (uint32_t d = 1; d <= SVO_LEVEL_MAX; ++d)
-		info->level_nodes[d - 1] = d < level ? state->lv[d].nodes : (d == level ? state->leaves : 0u);
-	out[sizeof(svo_build_info) / 4] = state->status;
+// Writes svo_build_info followed by the status word of every mesh to `out` (device), one record of
+// sizeof(svo_build_info) + 4 bytes per mesh.
+template <bool B> __global__ void build_export(BuildBatch bb, const BuildState *gstate, uint32_t *out) {
+	constexpr uint32_t kRec = sizeof(svo_build_info) / 4 + 1;
+	for (uint32_t mi = blockIdx.x * blockDim.x + threadIdx.x; mi < batch_size<B>(bb); mi += gridDim.x * blockDim.x) {
+		const BuildMesh md = mesh_at<B>(bb, mi);
+		const BuildState *state = md.state;
+		svo_build_info *info = reinterpret_cast<svo_build_info *>(out + kRec * mi);
+		info->level = md.level;
+		info->fragments = md.count;
+		info->range_words = state->range_words;
+		info->leaves = state->leaves;
+		for (uint32_t d = 1; d <= SVO_LEVEL_MAX; ++d)
+			info->level_nodes[d - 1] = d < md.level ? state->lv[d].nodes : (d == md.level ? state->leaves : 0u);
+#ifdef SVO_CHECKED
+		out[kRec * mi + kRec - 1] = state->status | gstate->status | (gstate->pad << 16);
+#else
+		out[kRec * mi + kRec - 1] = state->status | gstate->status;
+#endif
+	}
 }
 
 // ------------------------------------------------------------------------------------------ host side
@@ -733,13 +853,37 @@ uint64_t build_pool_bound(uint32_t count, uint32_t level) {
 
 uint32_t dense_depth(uint32_t level) { return level - 1 < kDenseMaxDepth ? level - 1 : kDenseMaxDepth; }
 
-static uint32_t dense_words_of(uint32_t d) { return d <= 1 ? 1u : (1u << (3 * d)) / 32u; }
+uint32_t dense_words_of(uint32_t d) { return d <= 1 ? 1u : (1u << (3 * d)) / 32u; }
 
-// Largest word range of one sparse depth: 8 * min(8^(i-1), count) over depths D+2..level-1.
-static uint64_t max_sparse_level_words(uint32_t count, uint32_t level, uint32_t D) {
+uint32_t dense_layout(uint32_t level, uint32_t off[kDenseMaxDepth + 2]) {
+	const uint32_t D = dense_depth(level);
+	uint32_t o = 0;
+	off[0] = 0;
+	for (uint32_t d = 1; d <= kDenseMaxDepth + 1; ++d) {
+		off[d] = o;
+		if (d <= D) o += (dense_words_of(d) + 7u) & ~7u; // 32-byte aligned levels (16-byte vector loads)
+	}
+	return o;
+}
+
+uint32_t dense_items(uint32_t level, const uint32_t off[kDenseMaxDepth + 2]) {
+	const uint32_t D = dense_depth(level);
+	if (D == 0) return 0;
+	const uint32_t last_parent_depth = D + 1 == level ? D - 1 : D;
+	return off[last_parent_depth + 1] + 1; // parent words of depths 1..last, and the root
+}
+
+// Words of a mesh's dense scan region: its bitmap words and the total entry, padded to whole tiles.
+static uint32_t dense_region(uint32_t level, uint32_t words) {
+	return dense_depth(level) ? (words + 1 + kBuildScanTile - 1) / kBuildScanTile * kBuildScanTile : 0u;
+}
+
+// Largest word range of one sparse depth: depth i spans 8 words per occupied cell of depth i-1, at most
+// 8 * min(8^(i-1), count), over the sparse depths D+1..level-1.
+uint64_t max_sparse_level_words(uint32_t count, uint32_t level, uint32_t D) {
 	uint64_t best = 8, per = 1;
 	for (uint32_t i = 1; i < level; ++i) {
-		if (i >= D + 2) {
+		if (i >= D + 1) {
 			const uint64_t w = 8 * (per < count ? per : (uint64_t)count);
 			best = w > best ? w : best;
 		}
@@ -762,22 +906,17 @@ void build_workspace_layout(void *ws, uint32_t count, uint32_t level, uint64_t c
 	};
 	const uint32_t D = dense_depth(level);
 	w.dv.D = D;
-	uint32_t o = 0;
-	w.dv.off[0] = 0;
-	for (uint32_t d = 1; d <= kDenseMaxDepth + 1; ++d) {
-		w.dv.off[d] = o;
-		if (d <= D) o += (dense_words_of(d) + 7u) & ~7u; // 32-byte aligned levels (16-byte vector loads)
-	}
-	w.dense_words = o;
+	const uint32_t o = dense_layout(level, w.dv.off);
+	w.dense_words = dense_region(level, o);
 	w.state = (BuildState *)take(sizeof(BuildState));
 	uint64_t sparse_words = max_sparse_level_words(count, level, D);
 	if (sparse_words > capacity) sparse_words = capacity;
-	const uint64_t scan_items = std::max<uint64_t>(o, sparse_words);
+	const uint64_t scan_items = std::max<uint64_t>(w.dense_words, sparse_words);
 	w.desc_count = (size_t)((scan_items + kScanTile - 1) / kScanTile + 2);
 	w.descs = (unsigned long long *)take(w.desc_count * sizeof(unsigned long long));
-	w.dv.bits = (uint32_t *)take((size_t)o * 4 + 32);
-	w.dv.prefix = (uint32_t *)take(((size_t)o + 1) * 4);
-	w.bshift = std::min<uint32_t>(level, kBucketVoxelBits);
+	w.dv.bits = (uint32_t *)take((size_t)w.dense_words * 4 + 32);
+	w.dv.prefix = (uint32_t *)take((size_t)w.dense_words * 4 + 32);
+	w.bshift = bucket_shift(level);
 	w.nb = 1u << (3 * (level - w.bshift));
 	w.bcount = (uint32_t *)take((size_t)w.nb * 4);
 	w.bfill = (uint32_t *)take((size_t)w.nb * 4);
@@ -796,6 +935,99 @@ static uint32_t grid_for(uint64_t items, uint32_t per_block, uint32_t cap) {
 	return (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(b, cap));
 }
 
+static BuildBatch single_batch(const BuildWorkspace &w, uint32_t count, uint32_t level, uint32_t *pool,
+                               uint64_t capacity) {
+	BuildBatch bb;
+	memset(&bb, 0, sizeof(bb));
+	bb.M = 1;
+	bb.dense_bits = w.dv.bits;
+	bb.dense_prefix = w.dv.prefix;
+	bb.gstate = w.state;
+	bb.sorted_total = count;
+	bb.dense_total = w.dense_words;
+	bb.nb_total = w.nb;
+	BuildMesh &m = bb.one;
+	m.pool = pool;
+	m.capacity = capacity;
+	m.state = w.state;
+	m.dv = w.dv;
+	m.frag_base = 0;
+	m.count = count;
+	m.level = level;
+	m.bshift = w.bshift;
+	m.nb = w.nb;
+	m.bucket_base = 0;
+	m.dense_base = 0;
+	m.item_base = 0;
+	m.sorted_pad = 0;
+	m.mark_word = w.dv.off[w.dv.D];
+	m.parent_off = level > 1 ? w.dv.off[std::min(level - 1, kDenseMaxDepth + 1)] : 0u;
+	return bb;
+}
+
+// The stages shared by a single build and a batch.  `maxD` = deepest dense depth of any mesh.
+template <bool B>
+static void launch_dense_and_scatter(const uint64_t *frags, uint64_t n, const BuildBatch &bb, uint32_t M, uint32_t maxD,
+                                     uint32_t dense_words, uint32_t items_total, uint32_t nb_total, BuildState *gstate,
+                                     unsigned long long *descs, uint32_t *bcount, uint32_t *boff, uint32_t *bfill,
+                                     uint32_t *blist, unsigned long long *bdescs, uint64_t *sorted,
+                                     cudaStream_t stream) {
+	const int sms = device_sm_count();
+	SVO_LAUNCH("build_init", stream, build_init<B><<<M, 256, 0, stream>>>(bb, gstate););
+	SVO_LAUNCH("dense_mark", stream,
+	           dense_mark<B><<<grid_for(n, kTPB, (uint32_t)sms * 16), kTPB, 0, stream>>>(frags, n, bb, bcount););
+	SVO_LAUNCH("bucket_scan", stream,
+	           bucket_scan<<<(nb_total + kScanTile - 1) / kScanTile, kTPB, 0, stream>>>(bcount, nb_total, boff, blist,
+	                                                                                   gstate, bdescs););
+	if (maxD >= 1) {
+		for (uint32_t d = maxD - 1; d >= 1; --d) {
+			const dim3 grid(grid_for(dense_words_of(d), kTPB, (uint32_t)sms * 8), M);
+			SVO_LAUNCH("dense_reduce", stream, dense_reduce<B><<<grid, kTPB, 0, stream>>>(bb, d););
+		}
+		SVO_LAUNCH("dense_scan", stream,
+		           dense_scan<B><<<grid_for(dense_words, kDenseTile, (uint32_t)sms * 4), kTPB, 0, stream>>>(
+		               bb, dense_words, gstate, descs););
+		SVO_LAUNCH("dense_finish", stream, dense_finish<B><<<(M + 127) / 128, 128, 0, stream>>>(bb););
+		SVO_LAUNCH("dense_write", stream,
+		           dense_write<B><<<grid_for(items_total, kTPB, (uint32_t)sms * 16), kTPB, 0, stream>>>(bb, items_total););
+	}
+	// the bucketed copy: leaf items when the leaf parents are dense (their bitmap is final now), fragments
+	// for the sparse levels otherwise
+	SVO_LAUNCH("bucket_scatter", stream,
+	           bucket_scatter<B><<<grid_for(n, kTPB, (uint32_t)sms * 16), kTPB, 0, stream>>>(frags, n, bb, boff, bfill,
+	                                                                                      sorted););
+}
+
+static void launch_sparse(const uint64_t *sorted, uint32_t count, uint32_t level, const DenseView &dv, uint32_t *pool,
+                          uint64_t capacity, uint32_t *cache, BuildState *state, unsigned long long *descs,
+                          const BuildState *gstate, cudaStream_t stream) {
+	const int sms = device_sm_count();
+	const uint32_t tag_blocks = grid_for(((uint64_t)count + 3) / 4, kTPB, (uint32_t)sms * 16);
+	for (uint32_t depth = dv.D + 1; depth < level; ++depth) {
+		SVO_LAUNCH("build_tag", stream,
+		           build_tag<<<tag_blocks, kTPB, 0, stream>>>(sorted, count, level, depth, pool, cache, dv, state,
+		                                                      gstate););
+		SVO_LAUNCH("build_alloc", stream,
+		           build_alloc<<<(uint32_t)sms * 4, kTPB, 0, stream>>>(pool, capacity, depth, level, state, descs,
+		                                                                     gstate););
+	}
+}
+
+template <bool B>
+static void launch_leaf_stage(const BuildBatch &bb, uint32_t M, uint32_t nb_total, const uint32_t *boff,
+                              const uint32_t *blist, const BuildState *gstate, uint4 *bmeta, uint32_t *bmesh,
+                              const uint64_t *sorted, const uint32_t *cache, cudaStream_t stream) {
+	const int sms = device_sm_count();
+	const size_t smem = kLeafSlots * sizeof(unsigned long long); // 32 KB: below the default dynamic limit
+	const uint32_t meta_items = std::max<uint32_t>(nb_total, M);
+	SVO_LAUNCH("bucket_meta", stream,
+	           bucket_meta<B><<<grid_for(meta_items, kTPB, (uint32_t)sms * 4), kTPB, 0, stream>>>(bb, boff, blist, gstate,
+	                                                                                         bmeta, bmesh););
+	SVO_LAUNCH("build_leaf", stream,
+	           build_leaf<B><<<(uint32_t)sms * 6, kTPB, smem, stream>>>(sorted, bb, cache, bmeta, bmesh,
+	                                                                     const_cast<BuildState *>(gstate)););
+}
+
 cudaError_t build_launch_interior(const uint64_t *frags, uint32_t count, uint32_t level, uint32_t *pool,
                                   uint64_t capacity, const BuildWorkspace &w, cudaStream_t stream) {
 	cudaError_t e = cudaMemsetAsync(w.descs, 0, w.desc_count * sizeof(unsigned long long), stream);
@@ -804,67 +1036,54 @@ cudaError_t build_launch_interior(const uint64_t *frags, uint32_t count, uint32_
 	if (e == cudaSuccess) e = cudaMemsetAsync(w.bcount, 0, (char *)w.boff - (char *)w.bcount, stream);
 	if (e == cudaSuccess) e = cudaMemsetAsync(w.bdescs, 0, w.bdesc_count * sizeof(unsigned long long), stream);
 	if (e != cudaSuccess) return e;
-	const int sms = device_sm_count();
-	const uint32_t D = w.dv.D;
-	SVO_LAUNCH("build_init", stream, build_init<<<1, 256, 0, stream>>>(w.state););
-	if (D >= 1) {
-		SVO_LAUNCH("dense_mark", stream,
-		           dense_mark<<<grid_for(count, kTPB, (uint32_t)sms * 16), kTPB, 0, stream>>>(frags, count, level, w.dv,
-		                                                                                      w.bshift, w.bcount););
-	} else {
-		SVO_LAUNCH("bucket_hist", stream,
-		           bucket_hist<<<grid_for(count, kTPB, (uint32_t)sms * 16), kTPB, 0, stream>>>(frags, count, w.bshift,
-		                                                                                       w.bcount););
-	}
-	SVO_LAUNCH("bucket_scan", stream,
-	           bucket_scan<<<(w.nb + kScanTile - 1) / kScanTile, kTPB, 0, stream>>>(w.bcount, w.nb, w.boff, w.blist,
-	                                                                               w.state, w.bdescs););
-	if (D >= 1) {
-		for (uint32_t d = D - 1; d >= 1; --d)
-			SVO_LAUNCH("dense_reduce", stream,
-			           dense_reduce<<<grid_for(dense_words_of(d), kTPB, (uint32_t)sms * 8), kTPB, 0, stream>>>(w.dv, d););
-		SVO_LAUNCH("dense_scan", stream,
-		           dense_scan<<<grid_for(w.dense_words, kScanTile, (uint32_t)sms * 4), kTPB, 0, stream>>>(
-		               w.dv, w.dense_words, w.state, w.descs););
-		SVO_LAUNCH("dense_finish", stream, dense_finish<<<1, 32, 0, stream>>>(w.dv, w.state););
-		SVO_LAUNCH("dense_write", stream,
-		           dense_write<<<grid_for((uint64_t)w.dense_words + 1, kTPB, (uint32_t)sms * 16), kTPB, 0, stream>>>(
-		               pool, capacity, w.dv, level, w.state););
-	}
-	// the bucketed copy: leaf items when the leaf parents are dense (their bitmap is final now), fragments
-	// for the sparse levels otherwise
-	const bool items = level == 1 || level - 1 <= D;
-	SVO_LAUNCH("bucket_scatter", stream,
-	           bucket_scatter<<<grid_for(count, kTPB, (uint32_t)sms * 16), kTPB, 0, stream>>>(
-	               frags, count, w.bshift, w.boff, w.bfill, w.sorted, items, w.dv, level, w.state););
-	const uint32_t tag_blocks = grid_for(((uint64_t)count + 3) / 4, kTPB, (uint32_t)sms * 16);
-	for (uint32_t depth = D + 1; depth < level; ++depth) {
-		SVO_LAUNCH("build_tag", stream,
-		           build_tag<<<tag_blocks, kTPB, 0, stream>>>(w.sorted, count, level, depth, pool, w.cache, w.dv,
-		                                                      w.state););
-		SVO_LAUNCH("build_alloc", stream,
-		           build_alloc<<<(uint32_t)sms * 4, kTPB, 0, stream>>>(pool, capacity, depth, level, w.state, w.descs););
-	}
+	const BuildBatch bb = single_batch(w, count, level, pool, capacity);
+	const uint32_t items = dense_items(level, w.dv.off);
+	launch_dense_and_scatter<false>(frags, count, bb, 1, w.dv.D, w.dense_words, items, w.nb, w.state, w.descs, w.bcount,
+	                                w.boff, w.bfill, w.blist, w.bdescs, w.sorted, stream);
+	if (level > w.dv.D + 1)
+		launch_sparse(w.sorted, count, level, w.dv, pool, capacity, w.cache, w.state, w.descs, w.state, stream);
 	return cudaGetLastError();
 }
 
 cudaError_t build_launch_leaf(uint32_t count, uint32_t level, uint32_t *pool, uint64_t capacity,
                               const BuildWorkspace &w, cudaStream_t stream) {
-	(void)count;
-	const int sms = device_sm_count();
-	const size_t smem = kLeafSlots * sizeof(unsigned long long); // 32 KB: below the default dynamic limit
-	SVO_LAUNCH("bucket_meta", stream,
-	           bucket_meta<<<grid_for(w.nb, kTPB, (uint32_t)sms * 4), kTPB, 0, stream>>>(w.boff, w.blist, w.nb, w.dv, level,
-	                                                                                w.state, w.bmeta););
-	SVO_LAUNCH("build_leaf", stream,
-	           build_leaf<<<(uint32_t)sms * 6, kTPB, smem, stream>>>(w.sorted, level, pool, capacity, w.cache, w.dv,
-	                                                                  w.bmeta, w.state););
+	const BuildBatch bb = single_batch(w, count, level, pool, capacity);
+	launch_leaf_stage<false>(bb, 1, w.nb, w.boff, w.blist, w.state, w.bmeta, nullptr, w.sorted, w.cache, stream);
 	return cudaGetLastError();
 }
 
 cudaError_t build_launch_export(const BuildWorkspace &w, uint32_t level, uint32_t count, void *out,
                                 cudaStream_t stream) {
-	SVO_LAUNCH("build_export", stream, build_export<<<1, 32, 0, stream>>>(w.state, level, count, (uint32_t *)out););
+	const BuildBatch bb = single_batch(w, count, level, nullptr, 0);
+	SVO_LAUNCH("build_export", stream, build_export<false><<<1, 32, 0, stream>>>(bb, w.state, (uint32_t *)out););
+	return cudaGetLastError();
+}
+
+// The whole build of a batch: clears, dense and bucket stages over all meshes, the sparse depths of the
+// meshes that have them (one mesh at a time), the leaf stage over all buckets, and one export record per
+// mesh to result_dev.
+cudaError_t build_launch_batch(const uint64_t *frags, const BuildBatchPlan &p, void *result_dev, cudaStream_t stream) {
+	cudaError_t e = cudaMemsetAsync(p.descs, 0, p.desc_count * sizeof(unsigned long long), stream);
+	if (e == cudaSuccess && p.dense_total)
+		e = cudaMemsetAsync(p.bb.dense_bits, 0, (size_t)p.dense_total * 4, stream);
+	if (e == cudaSuccess) e = cudaMemsetAsync(p.bcount, 0, (size_t)p.nb_total * 4, stream);
+	if (e == cudaSuccess) e = cudaMemsetAsync(p.bfill, 0, (size_t)p.nb_total * 4, stream);
+	if (e == cudaSuccess) e = cudaMemsetAsync(p.bdescs, 0, p.bdesc_count * sizeof(unsigned long long), stream);
+	if (e != cudaSuccess) return e;
+	launch_dense_and_scatter<true>(frags, p.frags_total, p.bb, p.M, p.max_D, p.dense_total, p.items_total, p.nb_total,
+	                               p.gstate, p.descs, p.bcount, p.boff, p.bfill, p.blist, p.bdescs, p.sorted, stream);
+	for (uint32_t m = 0; m < p.M; ++m) {
+		const BuildMesh &md = p.meshes[m];
+		if (md.level <= md.dv.D + 1) continue; // no sparse depths (an empty mesh still sets its leaf range)
+		e = cudaMemsetAsync(p.descs, 0, p.desc_count * sizeof(unsigned long long), stream);
+		if (e != cudaSuccess) return e;
+		const uint64_t sb = md.frag_base + md.sorted_pad;
+		launch_sparse(p.sorted + sb, md.count, md.level, md.dv, md.pool, md.capacity, p.cache + sb, md.state, p.descs,
+		              p.gstate, stream);
+	}
+	launch_leaf_stage<true>(p.bb, p.M, p.nb_total, p.boff, p.blist, p.gstate, p.bmeta, p.bmesh, p.sorted, p.cache, stream);
+	SVO_LAUNCH("build_export", stream,
+	           build_export<true><<<(p.M + 127) / 128, 128, 0, stream>>>(p.bb, p.gstate, (uint32_t *)result_dev););
 	return cudaGetLastError();
 }
 

@@ -76,12 +76,14 @@ SVO_DEV unsigned long long desc_load(const unsigned long long *d) {
 // Decoupled look-back for tile `t` once its aggregate is known, called by all 32 lanes of one warp:
 // each step inspects the 32 nearest unexamined predecessors at once and sums their aggregates up to
 // the nearest inclusive prefix.  Returns the tile's exclusive prefix on every lane.  Waits are bounded
-// (kSpinLimit); on timeout the status word gets kStatusTimeout.
+// (kSpinLimit); on timeout the status word gets kStatusTimeout.  A tile with seg_start set begins a
+// new segment (a segmented scan): its prefix is 0, and the look-back of later tiles stops there.
 SVO_DEV unsigned long long tile_lookback_warp(unsigned long long *descs, uint32_t t, uint32_t epoch,
-                                              unsigned long long aggregate, uint32_t *status) {
+                                              unsigned long long aggregate, uint32_t *status,
+                                              bool seg_start = false) {
 	const uint32_t lane = lane_id();
-	if (t == 0) {
-		if (lane == 0) desc_publish(&descs[0], epoch, 2, aggregate);
+	if (t == 0 || seg_start) {
+		if (lane == 0) desc_publish(&descs[t], epoch, 2, aggregate);
 		return 0;
 	}
 	if (lane == 0) desc_publish(&descs[t], epoch, 1, aggregate);

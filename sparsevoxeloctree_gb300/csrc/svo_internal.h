@@ -5,6 +5,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <cuda_runtime.h>
+#include <vector>
 
 #include "../../include/svo.h"
 
@@ -16,7 +17,9 @@ inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 enum : uint32_t {
 	kStatusTimeout = 1u,  // a bounded look-back wait gave up
 	kStatusCapacity = 2u, // an output buffer or the 30-bit pointer range would overflow
-	kStatusMalformed = 4u  // a march met a pointer outside the pool or a tree deeper than its level
+	kStatusMalformed = 4u, // a march met a pointer outside the pool or a tree deeper than its level
+	kStatusBadFragment = 16u, // a build met a fragment whose coordinates lie outside its octree level
+	kStatusCheck = 32u     // an internal bounds check failed (builds compiled with SVO_CHECKED; id in bits 16+)
 };
 
 void note_launch();      // counts kernel launches (svo_kernel_launches)
@@ -53,6 +56,24 @@ struct VoxWorkspace {
 	uint32_t *counters;            // tile tickets, status
 	unsigned long long *totals;    // [0] fragments, [1] units, [2] status (written by vox_launch_totals)
 };
+
+// One mesh of a voxelize batch.  The batch's triangles are indexed flat: mesh m owns flat triangles
+// [tri_base[m], tri_base[m+1]), read from its own buffer.
+struct VoxMesh {
+	const svo_triangle *tris; // (device)
+	uint32_t level;
+	uint32_t pad;
+};
+
+struct VoxBatch {
+	const VoxMesh *table;         // [M] (device; unused for a single mesh)
+	const uint32_t *tri_base;     // [M+1] (device)
+	unsigned long long *shifts;   // [2M] output shift of small / large fragments (vox_launch_batch_totals)
+	unsigned long long *mesh_out; // [4M] per mesh: fragments, first fragment, units, 0 (for the host)
+	uint32_t M;
+	VoxMesh one;                  // the mesh of a single voxelization
+};
+
 uint64_t vox_default_unit_cap(uint32_t n);
 size_t vox_workspace_bytes(uint32_t n, uint64_t unit_cap);
 size_t vox_workspace_layout(void *ws, uint32_t n, uint64_t unit_cap, VoxWorkspace &w);
@@ -61,6 +82,13 @@ cudaError_t vox_launch_count(const svo_triangle *tris, uint32_t n, uint32_t leve
 cudaError_t vox_launch_totals(const VoxWorkspace &w, cudaStream_t stream);
 cudaError_t vox_launch_emit(const svo_triangle *tris, uint32_t n, uint32_t level, const VoxWorkspace &w,
                             uint64_t *frags, uint64_t capacity, cudaStream_t stream);
+// Batched forms: n = flat triangles of all meshes.  The batch totals write per-mesh counts and the
+// output shifts that make every mesh's fragments contiguous (mesh order; inside a mesh the order of a
+// single voxelization of that mesh).
+cudaError_t vox_launch_count_batch(const VoxBatch &vb, uint32_t n, const VoxWorkspace &w, cudaStream_t stream);
+cudaError_t vox_launch_batch_totals(const VoxBatch &vb, uint32_t n, const VoxWorkspace &w, cudaStream_t stream);
+cudaError_t vox_launch_emit_batch(const VoxBatch &vb, uint32_t n, const VoxWorkspace &w, uint64_t *frags,
+                                  uint64_t capacity, cudaStream_t stream);
 
 // ---------------------------------------------------------------- build
 struct LevelInfo {
@@ -82,6 +110,7 @@ struct BuildState {
 };
 
 constexpr uint32_t kDenseMaxDepth = 9; // deepest depth held as a dense occupancy bitmap (8^9 bits)
+constexpr uint32_t kBuildScanTile = 8192; // words per tile of the dense scan (a mesh's dense region is a multiple)
 
 // Dense occupancy bitmaps of depths 1..D, concatenated (level d at word off[d]), and the exclusive
 // prefix of their popcounts over the concatenation (prefix[off[D+1]] = occupied cells of depths 1..D).
@@ -92,12 +121,50 @@ struct DenseView {
 	uint32_t D;
 };
 
+// One mesh of a build batch.  Fragments of mesh m are [frag_base, frag_base + count) of the batch's
+// fragment list; its bucketed copy starts at frag_base + sorted_pad (16-byte aligned); its buckets,
+// dense region and dense_write items are slices of the batch's concatenated arrays.
+struct BuildMesh {
+	uint32_t *pool;         // (device) the mesh's node pool
+	uint64_t capacity;      // words
+	BuildState *state;      // (device) the mesh's level table, counters and status
+	DenseView dv;           // the mesh's dense region (prefix values count from the mesh's first word)
+	uint64_t frag_base;
+	uint32_t count;
+	uint32_t level;
+	uint32_t bshift, nb;    // bucket key shift, buckets of the mesh
+	uint32_t bucket_base;   // first bucket in the concatenated bucket arrays
+	uint32_t dense_base;    // first word of the dense region in the concatenated bitmaps
+	uint32_t item_base;     // first dense_write item
+	uint32_t sorted_pad;    // padding of the mesh's bucketed copy before it (fragments)
+	// scalar copies of dv.off entries the per-fragment sweeps need (no runtime-indexed array in a loop)
+	uint32_t mark_word;     // dense_base + dv.off[D]: first word of the depth-D bitmap in the concatenation
+	uint32_t parent_off;    // dv.off[level-1]: depth level-1 bitmap (leaf parents) inside the mesh region
+};
+
+// Kernel view of a build: one mesh by value, or a table of M meshes in device memory with the flat
+// offsets the kernels search (each [M+1], non-decreasing).
+struct BuildBatch {
+	const BuildMesh *table;
+	const unsigned long long *frag_base;
+	const uint32_t *bucket_base;
+	const uint32_t *item_base;
+	const uint32_t *dense_base;
+	uint32_t *dense_bits;   // base of the concatenated bitmaps
+	uint32_t *dense_prefix; // base of the concatenated prefixes
+	BuildState *gstate;     // batch-wide tickets and status (the mesh's own state for a single build)
+	unsigned long long sorted_total; // entries of the bucketed copy (bounds checks)
+	uint32_t dense_total, nb_total;  // dense words and buckets of all meshes (bounds checks)
+	uint32_t M;
+	BuildMesh one;
+};
+
 struct BuildWorkspace {
 	BuildState *state;
 	unsigned long long *descs;
 	size_t desc_count;
 	DenseView dv;
-	uint32_t dense_words;
+	uint32_t dense_words;           // words of the dense scan (the region, padded to whole tiles)
 	uint32_t bshift;                // bucket key = Morton code of the voxel >> bshift bits per axis
 	uint32_t nb;                    // buckets (8^(level - bshift))
 	uint32_t *bcount;               // [nb] fragments per bucket
@@ -113,6 +180,13 @@ struct BuildWorkspace {
 };
 uint64_t build_pool_bound(uint32_t count, uint32_t level);
 uint32_t dense_depth(uint32_t level);
+uint32_t bucket_shift(uint32_t level); // bucket edge of the build's fragment buckets: 2^shift voxels
+uint32_t dense_words_of(uint32_t d);
+// Words of the dense bitmaps of depths 1..dense_depth(level) (32-byte aligned levels) and their offsets.
+uint32_t dense_layout(uint32_t level, uint32_t off[kDenseMaxDepth + 2]);
+// dense_write items of a mesh (parent words of the depths whose child blocks it writes, plus the root).
+uint32_t dense_items(uint32_t level, const uint32_t off[kDenseMaxDepth + 2]);
+uint64_t max_sparse_level_words(uint32_t count, uint32_t level, uint32_t D);
 void build_workspace_layout(void *ws, uint32_t count, uint32_t level, uint64_t capacity, BuildWorkspace &w);
 // Interior levels (dense bitmaps, then sparse tag/alloc); the leaf range ends up in state->lv[level].
 cudaError_t build_launch_interior(const uint64_t *frags, uint32_t count, uint32_t level, uint32_t *pool,
@@ -123,6 +197,31 @@ cudaError_t build_launch_leaf(uint32_t count, uint32_t level, uint32_t *pool, ui
 // svo_build_info followed by the uint32 status word, written to device memory `out`.
 cudaError_t build_launch_export(const BuildWorkspace &w, uint32_t level, uint32_t count, void *out,
                                 cudaStream_t stream);
+
+// A build batch: the host plan and the device views of its shared arrays.
+struct BuildBatchPlan {
+	BuildBatch bb;                  // device table view (bb.table etc. point into the plan buffer)
+	std::vector<BuildMesh> meshes;  // host copy of the table
+	uint32_t M;
+	uint64_t frags_total;           // fragments of all meshes
+	uint32_t nb_total;              // buckets of all meshes
+	uint32_t dense_total;           // dense words of all meshes (whole scan tiles per mesh)
+	uint32_t items_total;           // dense_write items of all meshes
+	uint32_t max_level, max_D;
+	uint64_t sorted_total;          // fragments of the bucketed copy, with per-mesh padding
+	BuildState *gstate;             // batch-wide tickets, bucket total and scan status
+	unsigned long long *descs;      // dense-scan / sparse-alloc descriptors
+	size_t desc_count;
+	uint32_t *bcount, *bfill, *boff, *blist;
+	uint4 *bmeta;
+	uint32_t *bmesh;                // [nb_total] mesh of each listed bucket
+	unsigned long long *bdescs;
+	size_t bdesc_count;
+	uint32_t *dense_prefix;
+	uint64_t *sorted;
+	uint32_t *cache;                // only when a mesh has sparse levels (level > 10)
+};
+cudaError_t build_launch_batch(const uint64_t *frags, const BuildBatchPlan &p, void *result_dev, cudaStream_t stream);
 
 // ---------------------------------------------------------------- march
 struct MarchArgs {
@@ -140,5 +239,35 @@ struct MarchArgs {
 };
 cudaError_t march_launch(const MarchArgs &a, bool camera, cudaStream_t stream);
 cudaError_t bounce_launch(const svo_hit *hits, uint32_t n, uint64_t seed, svo_ray *rays, cudaStream_t stream);
+
+// One request's share of a shared march launch: its octree, its rays (a ray buffer, or camera rays for
+// the first n pixels, row-major, of a width x height image) and its hit buffer.  Work slots of the
+// launch are numbered job after job; slot_begin is the job's first.
+struct MarchJob {
+	const uint32_t *pool;
+	uint32_t range, level;
+	const svo_ray *rays;   // null: camera rays
+	svo_camera cam;
+	uint32_t width, height;
+	uint32_t n;
+	uint32_t pad;
+	svo_hit *hits;
+	unsigned long long slot_begin;
+};
+// Work slots of a job (camera jobs: 32 per 8x4 tile of the rows holding its n pixels).
+uint64_t march_job_slots(const MarchJob &j);
+// `jobs` (device) holds njobs jobs whose slot_begin are set; total = slots of all jobs.  ticket (device,
+// 8 B) is zeroed here; status (device) gets kStatusMalformed for a malformed pool.
+cudaError_t march_jobs_launch(const MarchJob *jobs, uint32_t njobs, uint64_t total, unsigned long long *ticket,
+                              uint32_t *status, cudaStream_t stream);
+
+// One request's bounce rays: n hits in, n rays out, seeded per request (ray index local to the job).
+struct BounceJob {
+	const svo_hit *hits;
+	svo_ray *rays;
+	unsigned long long seed;
+	unsigned long long begin; // first flat index of the job in the launch
+};
+cudaError_t bounce_jobs_launch(const BounceJob *jobs, uint32_t njobs, uint64_t total, cudaStream_t stream);
 
 } // namespace svo

@@ -23,6 +23,8 @@
 //   vox_emit           small triangles by lane, then units by lane, at their offsets.
 // Fragment order is deterministic: small triangles in input order, then large triangles in input order
 // (spans, then pixels, in increasing order inside each).
+#include <cstring>
+
 #include "common.cuh"
 #include "svo_internal.h"
 
@@ -244,6 +246,25 @@ SVO_DEV uint32_t upper_index_in(const uint32_t *__restrict__ a, uint32_t lo, uin
 	return lo;
 }
 
+// Triangle t of a batch's flat triangle index: its buffer, index in it, level and mesh.  A single
+// voxelization (B = false) takes its one mesh by value and searches nothing.
+template <bool B>
+SVO_DEV void tri_of(const VoxBatch &vb, uint32_t t, const svo_triangle *&tris, uint32_t &local, uint32_t &level,
+                    uint32_t &mi) {
+	if constexpr (B) {
+		mi = upper_index(vb.tri_base, vb.M, t);
+		const VoxMesh vm = vb.table[mi];
+		tris = vm.tris;
+		local = t - __ldg(vb.tri_base + mi);
+		level = vm.level;
+	} else {
+		mi = 0;
+		tris = vb.one.tris;
+		local = t;
+		level = vb.one.level;
+	}
+}
+
 // ---------------------------------------------------------------------------------------------------
 constexpr int kTPB = 256;
 constexpr int kIPT = 2;
@@ -252,8 +273,8 @@ constexpr int kTile = kTPB * kIPT;
 // Per triangle: small fragment count and large unit count, both exclusive-scanned.
 //   small_off[t] = fragments of small triangles before t; small_off[n] = small total
 //   unit_off[t]  = units of large triangles before t;    unit_off[n]  = unit total
-__global__ void __launch_bounds__(kTPB) vox_classify_scan(const svo_triangle *__restrict__ tris, uint32_t n,
-                                                          uint32_t level, VoxWorkspace w) {
+template <bool B>
+__global__ void __launch_bounds__(kTPB) vox_classify_scan(VoxBatch vb, uint32_t n, VoxWorkspace w) {
 	__shared__ uint32_t s_tile;
 	__shared__ uint32_t s_cnt[kTile];
 	__shared__ uint32_t s_units[kTile];
@@ -268,7 +289,12 @@ __global__ void __launch_bounds__(kTPB) vox_classify_scan(const svo_triangle *__
 		const uint64_t t = base + (uint64_t)k * kTPB + threadIdx.x;
 		TriSetup s;
 		s.valid = 0;
-		if (t < n) tri_setup(tris, (uint32_t)t, level, s);
+		if (t < n) {
+			const svo_triangle *tp;
+			uint32_t local, lvl, mi;
+			tri_of<B>(vb, (uint32_t)t, tp, local, lvl, mi);
+			tri_setup(tp, local, lvl, s);
+		}
 		const bool large = is_large(s);
 		s_cnt[k * kTPB + threadIdx.x] = (s.valid && !large) ? count_serial(s) : 0u;
 		s_units[k * kTPB + threadIdx.x] = large ? unit_count(s) : 0u;
@@ -310,8 +336,8 @@ __global__ void __launch_bounds__(kTPB) vox_classify_scan(const svo_triangle *__
 
 // Per unit of a large triangle: covered length, scanned into unit_frag[u] (offset inside the large
 // region); unit_frag[units] = large total.  Persistent grid: tiles claimed in order by ticket.
-__global__ void __launch_bounds__(kTPB) vox_unit_scan(const svo_triangle *__restrict__ tris, uint32_t n,
-                                                      uint32_t level, VoxWorkspace w) {
+template <bool B>
+__global__ void __launch_bounds__(kTPB) vox_unit_scan(VoxBatch vb, uint32_t n, VoxWorkspace w) {
 	__shared__ uint32_t s_tile;
 	__shared__ unsigned long long s_warp[kTPB / 32 + 1];
 	__shared__ unsigned long long s_prefix;
@@ -342,7 +368,10 @@ __global__ void __launch_bounds__(kTPB) vox_unit_scan(const svo_triangle *__rest
 				const uint32_t t = upper_index_in(w.unit_off, t_first, t_end, u);
 				w.unit_tri[u] = t;
 				TriSetup s;
-				tri_setup(tris, t, level, s);
+				const svo_triangle *tp;
+				uint32_t local, lvl, mi;
+				tri_of<B>(vb, t, tp, local, lvl, mi);
+				tri_setup(tp, local, lvl, s);
 				int32_t v, lo, hi;
 				unit_interval(s, u - w.unit_off[t], v, lo, hi);
 				len[k] = hi >= lo ? (uint32_t)(hi - lo + 1) : 0u;
@@ -370,13 +399,23 @@ __global__ void __launch_bounds__(kTPB) vox_unit_scan(const svo_triangle *__rest
 }
 
 // Emission of small triangles: one lane per triangle, its fragments in order at its offset.
-__global__ void __launch_bounds__(kTPB) vox_emit(const svo_triangle *__restrict__ tris, uint32_t n, uint32_t level,
-                                                 VoxWorkspace w, uint64_t *__restrict__ frags, uint64_t capacity) {
+// In a batch, mesh m's small fragments move up by its shift (the large fragments of earlier meshes).
+template <bool B>
+__global__ void __launch_bounds__(kTPB) vox_emit(VoxBatch vb, uint32_t n, VoxWorkspace w, uint64_t *__restrict__ frags,
+                                                 uint64_t capacity) {
 	for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-		const uint64_t off = w.small_off[i], end = w.small_off[i + 1];
-		if (end == off || end > capacity) continue;
+		uint64_t off = w.small_off[i], end = w.small_off[i + 1];
+		if (end == off) continue;
+		const svo_triangle *tp;
+		uint32_t local, lvl, mi;
+		tri_of<B>(vb, (uint32_t)i, tp, local, lvl, mi);
+		if (B) {
+			const uint64_t sh = vb.shifts[2 * mi];
+			off += sh, end += sh;
+		}
+		if (end > capacity) continue;
 		TriSetup s;
-		tri_setup(tris, (uint32_t)i, level, s);
+		tri_setup(tp, local, lvl, s);
 		if (s.valid && !is_large(s)) emit_serial(s, frags + off);
 	}
 }
@@ -400,7 +439,10 @@ struct UnitRec {
 	int32_t excl, z0, z1;
 	uint32_t fields; // u shift | z shift << 8 | (u is the split z field) << 16 | (z is) << 17
 	uint32_t base_lo, base_hi;
+	int32_t R;       // resolution of the unit's mesh
+	uint32_t pad;
 	int64_t num0, nu, d;
+	uint64_t shift;  // output position of the unit's mesh's large region
 };
 constexpr float kDepthEps = 1.0f / 1024.0f;
 
@@ -409,17 +451,17 @@ SVO_DEV uint32_t field_of(int axis, int which) { return (uint32_t)((axis + which
 // Emission of large-triangle units, 32 consecutive units per warp.  Their fragments are contiguous in
 // the output, so the warp writes them together: lane k takes fragments k, k+32, ... of the group (each
 // store instruction covers 256 contiguous bytes), finds the unit holding its fragment and evaluates it
-// from that unit's record.
-__global__ void __launch_bounds__(kTPB, 4) vox_emit_units(const svo_triangle *__restrict__ tris, uint32_t n,
-                                                       uint32_t level, VoxWorkspace w, uint64_t *__restrict__ frags,
-                                                       uint64_t capacity) {
+// from that unit's record.  In a batch, the units of one warp may belong to different meshes, each of
+// whose large fragments start at its own shift.
+template <bool B>
+__global__ void __launch_bounds__(kTPB, 4) vox_emit_units(VoxBatch vb, uint32_t n, VoxWorkspace w,
+                                                       uint64_t *__restrict__ frags, uint64_t capacity) {
 	__shared__ UnitRec s_rec[kTPB];
 	__shared__ uint32_t s_incl[kTPB];
 	const uint32_t units = w.unit_off[n];
 	if (units > w.unit_cap) return; // reported by the count; nothing sensible to emit
 	const uint64_t small_total = w.small_off[n];
 	const uint32_t lane = lane_id();
-	const int32_t R = 1 << level;
 	const UnitRec *warp_rec = s_rec + (threadIdx.x & ~31u);
 	const uint32_t *warp_incl = s_incl + (threadIdx.x & ~31u);
 	const uint64_t warps = (uint64_t)gridDim.x * blockDim.x / 32;
@@ -429,7 +471,11 @@ __global__ void __launch_bounds__(kTPB, 4) vox_emit_units(const svo_triangle *__
 		if (u < units) {
 			const uint32_t t = w.unit_tri[u];
 			TriSetup S;
-			tri_setup(tris, t, level, S);
+			const svo_triangle *tp;
+			uint32_t local, lvl, mi;
+			tri_of<B>(vb, t, tp, local, lvl, mi);
+			tri_setup(tp, local, lvl, S);
+			const int32_t R = 1 << lvl;
 			int32_t v, lo, hi;
 			unit_interval(S, (uint32_t)u - w.unit_off[t], v, lo, hi);
 			if (hi >= lo) {
@@ -446,6 +492,8 @@ __global__ void __launch_bounds__(kTPB, 4) vox_emit_units(const svo_triangle *__
 				rec.num0 = num0;
 				rec.nu = S.NU;
 				rec.d = S.D;
+				rec.R = R;
+				rec.shift = B ? vb.shifts[2 * mi + 1] : small_total;
 				// coordinate fields: i -> (axis+1)%3, j -> (axis+2)%3, depth -> axis (0 x, 1 y, 2 z)
 				const uint32_t fi = field_of(S.axis, 1), fj = field_of(S.axis, 2), fz = field_of(S.axis, 0);
 				const uint32_t fu = S.cols ? fj : fi, fv = S.cols ? fi : fj;
@@ -460,11 +508,10 @@ __global__ void __launch_bounds__(kTPB, 4) vox_emit_units(const svo_triangle *__
 		s_incl[threadIdx.x] = incl;
 		s_rec[threadIdx.x].excl = (int32_t)(incl - len);
 		__syncwarp();
-		const uint64_t first = small_total + (uint64_t)w.unit_frag[g * 32];
-		uint64_t *out = frags + first;
-		const uint64_t room = first < capacity ? capacity - first : 0;
+		const uint64_t first = (uint64_t)w.unit_frag[g * 32];
 		uint32_t j = 0, have = 32;
-		int32_t k = 0, q0 = 0, lo = 0, z0 = 0, z1 = 0;
+		uint64_t out0 = 0;
+		int32_t k = 0, q0 = 0, lo = 0, z0 = 0, z1 = 0, R = 0;
 		float kf = 0.0f, fr0 = 0.0f, fb = 0.0f;
 		uint32_t ush = 0, zsh = 0, usplit = 0, zsplit = 0, base_lo = 0, base_hi = 0;
 		for (uint32_t f = lane; f < total; f += 32) {
@@ -477,6 +524,8 @@ __global__ void __launch_bounds__(kTPB, 4) vox_emit_units(const svo_triangle *__
 				ush = rec.fields & 0xffu, zsh = (rec.fields >> 8) & 0xffu;
 				usplit = 0u - ((rec.fields >> 16) & 1u), zsplit = 0u - ((rec.fields >> 17) & 1u);
 				base_lo = rec.base_lo, base_hi = rec.base_hi;
+				R = rec.R;
+				out0 = rec.shift + first;
 				have = j;
 			} else {
 				k += 32;
@@ -495,7 +544,7 @@ __global__ void __launch_bounds__(kTPB, 4) vox_emit_units(const svo_triangle *__
 			const uint32_t zz = (uint32_t)(z < z0 ? z0 : (z > z1 ? z1 : z)), uu = (uint32_t)(lo + k);
 			const uint32_t flo = base_lo | (uu << ush) | (zz << zsh);
 			const uint32_t fhi = base_hi | (((uu >> 8) << 28) & usplit) | (((zz >> 8) << 28) & zsplit);
-			if (f < room) out[f] = (uint64_t)flo | ((uint64_t)fhi << 32);
+			if (out0 + f < capacity) frags[out0 + f] = (uint64_t)flo | ((uint64_t)fhi << 32);
 		}
 		__syncwarp();
 	}
@@ -540,8 +589,16 @@ size_t vox_workspace_layout(void *ws, uint32_t n, uint64_t unit_cap, VoxWorkspac
 	return off;
 }
 
-cudaError_t vox_launch_count(const svo_triangle *tris, uint32_t n, uint32_t level, const VoxWorkspace &w,
-                             cudaStream_t stream) {
+static VoxBatch single_vox(const svo_triangle *tris, uint32_t level) {
+	VoxBatch vb;
+	memset(&vb, 0, sizeof(vb));
+	vb.M = 1;
+	vb.one.tris = tris;
+	vb.one.level = level;
+	return vb;
+}
+
+static cudaError_t clear_count_state(uint32_t n, const VoxWorkspace &w, cudaStream_t stream) {
 	cudaError_t e = cudaMemsetAsync(w.descs, 0, w.desc_bytes, stream);
 	if (e != cudaSuccess) return e;
 	e = cudaMemsetAsync(w.counters, 0, kCtrCount * sizeof(uint32_t), stream);
@@ -550,21 +607,37 @@ cudaError_t vox_launch_count(const svo_triangle *tris, uint32_t n, uint32_t leve
 		e = cudaMemsetAsync(w.small_off, 0, sizeof(uint64_t), stream);
 		if (e == cudaSuccess) e = cudaMemsetAsync(w.unit_off, 0, sizeof(uint32_t), stream);
 		if (e == cudaSuccess) e = cudaMemsetAsync(w.unit_frag, 0, sizeof(unsigned long long), stream);
-		return e;
 	}
-	SVO_LAUNCH("vox_classify_scan", stream, vox_classify_scan<<<(n + kTile - 1) / kTile, kTPB, 0, stream>>>(tris, n, level, w););
+	return e;
+}
+
+template <bool B> static void launch_count(const VoxBatch &vb, uint32_t n, const VoxWorkspace &w, cudaStream_t stream) {
+	SVO_LAUNCH("vox_classify_scan", stream, vox_classify_scan<B><<<(n + kTile - 1) / kTile, kTPB, 0, stream>>>(vb, n, w););
 	const int sms = device_sm_count();
-	SVO_LAUNCH("vox_unit_scan", stream, vox_unit_scan<<<(uint32_t)sms * 4, kTPB, 0, stream>>>(tris, n, level, w););
+	SVO_LAUNCH("vox_unit_scan", stream, vox_unit_scan<B><<<(uint32_t)sms * 4, kTPB, 0, stream>>>(vb, n, w););
+}
+
+template <bool B>
+static void launch_emit(const VoxBatch &vb, uint32_t n, const VoxWorkspace &w, uint64_t *frags, uint64_t capacity,
+                        cudaStream_t stream) {
+	const int sms = device_sm_count();
+	SVO_LAUNCH("vox_emit", stream, vox_emit<B><<<(uint32_t)sms * 16, kTPB, 0, stream>>>(vb, n, w, frags, capacity););
+	SVO_LAUNCH("vox_emit_units", stream,
+	           vox_emit_units<B><<<(uint32_t)sms * 8, kTPB, 0, stream>>>(vb, n, w, frags, capacity););
+}
+
+cudaError_t vox_launch_count(const svo_triangle *tris, uint32_t n, uint32_t level, const VoxWorkspace &w,
+                             cudaStream_t stream) {
+	cudaError_t e = clear_count_state(n, w, stream);
+	if (e != cudaSuccess || n == 0) return e;
+	launch_count<false>(single_vox(tris, level), n, w, stream);
 	return cudaGetLastError();
 }
 
 cudaError_t vox_launch_emit(const svo_triangle *tris, uint32_t n, uint32_t level, const VoxWorkspace &w,
                             uint64_t *frags, uint64_t capacity, cudaStream_t stream) {
 	if (n == 0) return cudaSuccess;
-	const int sms = device_sm_count();
-	SVO_LAUNCH("vox_emit", stream, vox_emit<<<(uint32_t)sms * 16, kTPB, 0, stream>>>(tris, n, level, w, frags, capacity););
-	SVO_LAUNCH("vox_emit_units", stream,
-	           vox_emit_units<<<(uint32_t)sms * 8, kTPB, 0, stream>>>(tris, n, level, w, frags, capacity););
+	launch_emit<false>(single_vox(tris, level), n, w, frags, capacity, stream);
 	return cudaGetLastError();
 }
 
@@ -578,6 +651,53 @@ __global__ void vox_totals(VoxWorkspace w) {
 
 cudaError_t vox_launch_totals(const VoxWorkspace &w, cudaStream_t stream) {
 	SVO_LAUNCH("vox_totals", stream, vox_totals<<<1, 1, 0, stream>>>(w););
+	return cudaGetLastError();
+}
+
+cudaError_t vox_launch_count_batch(const VoxBatch &vb, uint32_t n, const VoxWorkspace &w, cudaStream_t stream) {
+	cudaError_t e = clear_count_state(n, w, stream);
+	if (e != cudaSuccess || n == 0) return e;
+	launch_count<true>(vb, n, w, stream);
+	return cudaGetLastError();
+}
+
+cudaError_t vox_launch_emit_batch(const VoxBatch &vb, uint32_t n, const VoxWorkspace &w, uint64_t *frags,
+                                  uint64_t capacity, cudaStream_t stream) {
+	if (n == 0) return cudaSuccess;
+	launch_emit<true>(vb, n, w, frags, capacity, stream);
+	return cudaGetLastError();
+}
+
+// Per mesh m (triangles [T0, T1), units [U0, U1)): fragments = small + large, first fragment =
+// small_off[T0] + unit_frag[U0] (everything of earlier meshes), small shift = unit_frag[U0] (large
+// fragments of earlier meshes sit before its small ones), large shift = small_off[T1] (every small
+// fragment up to the end of the mesh sits before its large ones).  Thread 0 also writes the totals.
+__global__ void vox_batch_totals(VoxBatch vb, VoxWorkspace w) {
+	const uint32_t status = w.counters[kCtrStatus];
+	const bool units_ok = !(status & kStatusUnits);
+	for (uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < vb.M; m += gridDim.x * blockDim.x) {
+		const uint32_t t0 = vb.tri_base[m], t1 = vb.tri_base[m + 1];
+		const uint32_t u0 = w.unit_off[t0], u1 = w.unit_off[t1];
+		const unsigned long long s0 = w.small_off[t0], s1 = w.small_off[t1];
+		const unsigned long long f0 = units_ok ? w.unit_frag[u0] : 0ull, f1 = units_ok ? w.unit_frag[u1] : 0ull;
+		vb.shifts[2 * m] = f0;
+		vb.shifts[2 * m + 1] = s1;
+		vb.mesh_out[4 * m] = (s1 - s0) + (f1 - f0);
+		vb.mesh_out[4 * m + 1] = s0 + f0;
+		vb.mesh_out[4 * m + 2] = u1 - u0;
+		vb.mesh_out[4 * m + 3] = 0;
+	}
+	if (blockIdx.x == 0 && threadIdx.x == 0) {
+		const uint32_t units = w.unit_off[w.n];
+		w.totals[0] = w.small_off[w.n] + (units_ok ? w.unit_frag[units] : 0ull);
+		w.totals[1] = units;
+		w.totals[2] = status;
+	}
+}
+
+cudaError_t vox_launch_batch_totals(const VoxBatch &vb, uint32_t n, const VoxWorkspace &w, cudaStream_t stream) {
+	(void)n;
+	SVO_LAUNCH("vox_totals", stream, vox_batch_totals<<<(vb.M + 127) / 128, 128, 0, stream>>>(vb, w););
 	return cudaGetLastError();
 }
 

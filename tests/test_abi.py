@@ -65,3 +65,28 @@ def test_camera_from_angles_matches_python(lib):
     ref = scenes.camera_from_angles((1.5, 1.4, 1.3), 0.3, -0.2, np.pi / 3, 1.5)
     for k in ("pos", "look", "side", "up"):
         assert np.allclose(np.array(getattr(cam, k)[:3]), ref[k][:3], atol=1e-6)
+
+
+def test_batcher_rejects_bad_batches_before_any_launch(lib):
+    before = lib.svo_kernel_launches()
+    h = ctypes.c_void_p()
+    assert lib.svo_batcher_create(ctypes.byref(h)) == _lib.SVO_OK
+    try:
+        assert lib.svo_batcher_build(h, None, 0, None) == _lib.SVO_ERR_INVALID  # empty batch
+        arr = (_lib.BatchMesh * 2)()
+        arr[0].tris, arr[0].n_tris, arr[0].level = 256, 1, 8
+        arr[1].tris, arr[1].n_tris, arr[1].level = 256, 1, 13  # level out of range
+        assert lib.svo_batcher_build(h, arr, 2, None) == _lib.SVO_ERR_INVALID
+        assert b"mesh 1" in lib.svo_last_error()
+        arr[1].level, arr[1].tris = 8, 8  # misaligned triangles
+        assert lib.svo_batcher_build(h, arr, 2, None) == _lib.SVO_ERR_INVALID
+        arr[1].tris = None  # null buffer with triangles
+        assert lib.svo_batcher_build(h, arr, 2, None) == _lib.SVO_ERR_INVALID
+        assert lib.svo_batcher_meshes(h) == 0
+        assert lib.svo_batcher_result(h, 0, None, None, None) == _lib.SVO_ERR_INVALID
+        c, r = _lib.u64(), _lib.u64()
+        lib.svo_batcher_stats(h, ctypes.byref(c), ctypes.byref(r))
+        assert c.value == 0 and r.value == 0
+    finally:
+        lib.svo_batcher_destroy(h)
+    assert lib.svo_kernel_launches() == before
