@@ -397,6 +397,176 @@ def batch_leg(args, device) -> dict:
             "reps": reps, "kernel_launches_recorded": int(lib.svo_kernel_launches() - launches0)}
 
 
+# ------------------------------------------------------------------------------------------ serving
+def serve_leg(args, device, rates=(100, 500, 1000, 2000, 5000), seconds=1.0) -> dict:
+    """The serving workload: 16 resident octrees (levels 9..11, sphere + boxes + clutter meshes of 50k..2M
+    triangles), trace requests with a uniform scene and a log-uniform ray count of 1k..2M (half primary
+    camera rays, half diffuse-bounce rays), 2% rebuilds, admission under a 40 GB HBM budget.  Poisson
+    arrivals at each rate for `seconds`; latency = server submit -> completion (p50/p99); throughput =
+    rays / (last completion - first submission).  Saturation: every request of a set submitted at once.
+    One at a time: the same set through the plain C ABI calls (svo_raycast_camera, svo_bounce_rays,
+    svo_raycast, hit download, synchronize) one request after another, and through the server with one
+    lane and one request per batch."""
+    import math
+    import threading
+
+    import numpy as np
+    import torch
+
+    from sparsevoxeloctree_gb300 import _lib, api, scenes
+    from sparsevoxeloctree_gb300.formats import HIT_DTYPE
+
+    lib = _lib.load()
+    meshes = scenes.serving_scenes()
+    server = api.Server(hbm_budget_bytes=40 << 30, lanes=3)
+    tris_dev = [api.to_device(t) for t, _ in meshes]
+    octs = []
+    for t, (_, level) in zip(tris_dev, meshes):
+        octs.append(server.BuildScene(t, level))
+    torch.cuda.synchronize()
+    g = scenes.rng(55, 0)
+
+    def make_request(k):
+        n_rays = int(round(math.exp(g.uniform(math.log(1e3), math.log(2e6)))))
+        n = max(1, n_rays // 2)
+        w = min(n, 2048)
+        h = (n + w - 1) // w
+        pos = (float(g.uniform(0.2, 0.8)), float(g.uniform(0.2, 0.8)), float(g.uniform(0.2, 0.8)))
+        cam = scenes.camera_from_angles(tuple(p + 1.0 for p in pos), float(g.uniform(0, 2 * math.pi)),
+                                        float(g.uniform(-0.3, 0.3)), aspect=w / h)
+        return {"scene": int(g.integers(0, len(octs))), "cam": cam, "w": w, "h": h, "n": n,
+                "seed": int(g.integers(0, 2**62)), "rebuild": bool(g.uniform() < 0.02)}
+
+    # pinned hit buffers the client reuses: 20 for up to 2M hits, 64 for up to 64k hits
+    slot_bytes = 2 * (1 << 20) * HIT_DTYPE.itemsize
+    small_bytes = (1 << 16) * HIT_DTYPE.itemsize
+    bufs = [torch.empty(slot_bytes, dtype=torch.uint8).pin_memory() for _ in range(20)]
+    bufs += [torch.empty(small_bytes, dtype=torch.uint8).pin_memory() for _ in range(64)]
+    big_ids, small_ids = list(range(20)), list(range(20, 84))
+
+    def run(reqs, arrivals):
+        """Submit reqs at the given arrival offsets (seconds; None = all at once); returns per-request results."""
+        free = {True: list(big_ids), False: list(small_ids)}
+        cv = threading.Condition()
+        out = [None] * len(reqs)
+        tickets = []
+        done_flag = {"n": 0}
+
+        def collector():
+            for i, (t, slot, rb) in enumerate(iter(tickets_q.get, None)):
+                res = server.Wait(t)
+                out[t_index[t]] = res
+                with cv:
+                    if slot is not None:
+                        free[slot < 20].append(slot)
+                    done_flag["n"] += 1
+                    cv.notify_all()
+
+        import queue
+        tickets_q = queue.Queue()
+        t_index = {}
+        th = threading.Thread(target=collector, daemon=True)
+        th.start()
+        t0 = time.perf_counter()
+        for i, r in enumerate(reqs):
+            if arrivals is not None:
+                delay = t0 + arrivals[i] - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+            if r["rebuild"]:
+                sc = r["scene"]
+                t = server.SubmitRebuild(octs[sc], tris_dev[sc], meshes[sc][1])
+                t_index[t] = i
+                tickets_q.put((t, None, True))
+                continue
+            big = 2 * r["n"] * HIT_DTYPE.itemsize > small_bytes
+            with cv:
+                while not free[big]:
+                    cv.wait()
+                slot = free[big].pop()
+            t = server.SubmitCamera(octs[r["scene"]], r["cam"], r["w"], r["h"], r["n"], r["seed"], bufs[slot])
+            t_index[t] = i
+            tickets_q.put((t, slot, False))
+        tickets_q.put(None)
+        th.join()
+        return out
+
+    def summarize(reqs, res):
+        lat = [x["done_us"] - x["submit_us"] for x, r in zip(res, reqs) if not r["rebuild"]]
+        rays = sum(2 * r["n"] for r in reqs if not r["rebuild"])
+        span = (max(x["done_us"] for x in res) - min(x["submit_us"] for x in res)) * 1e-6
+        bs = [x["batch_requests"] for x, r in zip(res, reqs) if not r["rebuild"]]
+        return {"requests": len(reqs), "rebuilds": sum(r["rebuild"] for r in reqs), "rays": rays,
+                "p50_ms": float(np.percentile(lat, 50)) / 1e3, "p99_ms": float(np.percentile(lat, 99)) / 1e3,
+                "grays_per_s": rays / span / 1e9, "mean_batch_requests": float(np.mean(bs))}
+
+    # warm-up: one request per scene
+    run([dict(make_request(0), scene=i, rebuild=False) for i in range(len(octs))], None)
+    sweep = {}
+    for lam in rates:
+        n_req = max(20, int(lam * seconds))
+        reqs = [make_request(k) for k in range(n_req)]
+        arrivals = np.cumsum(g.exponential(1.0 / lam, size=n_req))
+        sweep[str(lam)] = summarize(reqs, run(reqs, arrivals))
+    sat_reqs = [dict(make_request(k), rebuild=False) for k in range(400)]
+    saturated = summarize(sat_reqs, run(sat_reqs, None))
+
+    # one request at a time, plain C ABI.  The sweep's rebuilds replaced scenes' octrees (and freed the old
+    # ones once their batches retired): take fresh views of the current octrees.
+    views = [server.Scene(i) for i in octs]
+    one_reqs = sat_reqs[:150]
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    hits_dev = torch.empty(slot_bytes, dtype=torch.uint8, device=device)
+    full_dev = torch.empty(2048 * 1024 * HIT_DTYPE.itemsize, dtype=torch.uint8, device=device)
+    rays_dev = torch.empty((1 << 20) * 24, dtype=torch.uint8, device=device)
+
+    def plain_one(r):
+        oc = views[r["scene"]].c_struct()
+        cam = api.camera_struct(r["cam"])
+        n = r["n"]
+        _lib.check(lib.svo_raycast_camera(ctypes.byref(oc), ctypes.byref(cam), r["w"], r["h"],
+                                          ctypes.c_void_p(full_dev.data_ptr()), None, s))
+        _lib.check(lib.svo_bounce_rays(ctypes.c_void_p(full_dev.data_ptr()), n, r["seed"],
+                                       ctypes.c_void_p(rays_dev.data_ptr()), s))
+        _lib.check(lib.svo_raycast(ctypes.byref(oc), ctypes.c_void_p(rays_dev.data_ptr()), n,
+                                   ctypes.c_void_p(hits_dev.data_ptr() + n * 32), None, s))
+        _lib.check(lib.svo_download(ctypes.c_void_p(bufs[0].data_ptr()), ctypes.c_void_p(full_dev.data_ptr()),
+                                    n * 32, 0, s))
+        _lib.check(lib.svo_download(ctypes.c_void_p(bufs[0].data_ptr() + n * 32),
+                                    ctypes.c_void_p(hits_dev.data_ptr() + n * 32), n * 32, 1, s))
+
+    for r in one_reqs[:5]:
+        plain_one(r)
+    t0 = time.perf_counter()
+    for r in one_reqs:
+        plain_one(r)
+    plain_s = time.perf_counter() - t0
+    one_rays = sum(2 * r["n"] for r in one_reqs)
+    one_server = api.Server(hbm_budget_bytes=40 << 30, lanes=1, max_batch_requests=1)
+    server_main = server
+    for v in views:
+        one_server.AddOctree(v)
+    server = one_server
+    one_res = summarize(one_reqs, run(one_reqs, None))
+    server = server_main
+    one_server.close()
+    served_sat = summarize(one_reqs, run(one_reqs, None))
+    st = server.stats()
+    server.close()
+    return {"workload": "serving: 16 resident octrees (levels 9..11, 50k..2M triangles, seeded), requests of "
+                        "1k..2M rays (log-uniform; half primary, half diffuse bounce), 2% rebuilds, 40 GB budget",
+            "resident_bytes": st["resident_bytes"], "scenes_triangles": int(sum(len(t) for t, _ in meshes)),
+            "poisson": sweep, "saturated_400": saturated,
+            "same_150_requests": {"served_grays_per_s": served_sat["grays_per_s"],
+                                  "one_at_a_time_plain_abi_grays_per_s": one_rays / plain_s / 1e9,
+                                  "one_at_a_time_server_grays_per_s": one_res["grays_per_s"],
+                                  "speedup_vs_plain_abi": served_sat["grays_per_s"] / (one_rays / plain_s / 1e9),
+                                  "speedup_vs_unbatched_server": served_sat["grays_per_s"] / one_res["grays_per_s"],
+                                  "served_p50_ms": served_sat["p50_ms"], "served_p99_ms": served_sat["p99_ms"]},
+            "server_stats": st, "lanes": 3,
+            "latency": "server clock, submission to completion of the request's hits in host memory"}
+
+
 # ------------------------------------------------------------------------------------------ CPU arms
 def cpu_baseline(scene, per_step: bool) -> dict:
     """The oracle (CPU restatement of the reference's path) on the host cores, full workload."""
@@ -444,6 +614,7 @@ def main() -> int:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-build leg")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -480,13 +651,16 @@ def main() -> int:
     res = engine_arm(args, rank, world, device)
     if not args.no_batch and rank == 0:
         res["batched"] = batch_leg(args, device)
+    if not args.no_serve and rank == 0:
+        res["served"] = serve_leg(args, device)
     config.update(res["config_extra"])
     line.update({"value": res["value"], "ms_per_step": res["ms_per_step"], "config": config,
                  "stages": res["stages"], "roofline": res["roofline"], "cpu_baseline": res["cpu_baseline"],
                  "e2e": res["e2e"], "clocks": res["clocks"], "gpu_launches": res["gpu_launches"],
                  "step_ms": res["step_ms_all"]})
-    if "batched" in res:
-        line["batched"] = res["batched"]
+    for key in ("batched", "served"):
+        if key in res:
+            line[key] = res[key]
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -302,6 +302,81 @@ int svo_raycast_camera(const svo_octree *o, const svo_camera *cam, uint32_t widt
  * without touching the octree. */
 int svo_bounce_rays(const svo_hit *hits, uint32_t n, uint64_t seed, svo_ray *rays, void *stream);
 
+/* ------------------------------------------------------------------ serving */
+
+/* A server keeps many octrees resident and traces requests from many callers in shared launches
+ * (continuous batching).  The reference renders one octree per frame (Application::draw_frame,
+ * src/Application.cpp:130-159; PathTracer::CmdRender, src/PathTracer.cpp:192-215) and rebuilds on its
+ * loader thread (src/LoaderThread.cpp:43-116); this is the multi-request form of that path.  A scheduler
+ * thread takes pending requests in arrival order into a batch while the batch's rays, request count and
+ * the device bytes in flight stay within the limits below, and issues it on a free lane (stream): one
+ * march launch for all primary rays, one bounce launch, one march launch for all bounce rays, one copy
+ * of each request's hits.  Up to `lanes` batches run at once; requests that arrive meanwhile are admitted
+ * as lanes and memory free up.  A request's hits are those of svo_raycast_camera / svo_bounce_rays /
+ * svo_raycast run for it alone. */
+typedef struct svo_server svo_server;
+
+typedef struct svo_server_config {
+	uint64_t hbm_budget_bytes;   /* resident octrees + buffers of requests in flight (0: 40 GiB) */
+	uint32_t lanes;              /* batches in flight at once (0: 3) */
+	uint32_t max_batch_rays;     /* hits per batch (0: 8 Mi); a larger request runs alone */
+	uint32_t max_batch_requests; /* requests per batch (0: 256) */
+	uint32_t reserved;
+} svo_server_config;
+
+#define SVO_REQUEST_CAMERA 0u /* primary camera rays, then one diffuse bounce ray per primary ray */
+#define SVO_REQUEST_RAYS 1u   /* caller-given rays */
+
+typedef struct svo_trace_request {
+	uint32_t scene;
+	uint32_t mode;          /* SVO_REQUEST_CAMERA or SVO_REQUEST_RAYS */
+	svo_camera camera;      /* camera mode: Camera_GenRay of the first n_primary pixels (row-major) of a */
+	uint32_t width, height; /*   width x height image, as svo_raycast_camera traces them */
+	uint32_t n_primary;
+	uint32_t n_rays;        /* rays mode */
+	const svo_ray *rays;    /* rays mode: host memory, read while the request runs */
+	svo_hit *hits;          /* host memory (page-locked for full overlap): camera mode 2 * n_primary hits,
+	                           primary then bounce (bounce i from primary hit i, svo_bounce_rays with `seed`);
+	                           rays mode n_rays hits.  Written when the request completes. */
+	uint64_t seed;
+} svo_trace_request;
+
+typedef struct svo_request_result {
+	int status;              /* svo_status of the request */
+	uint32_t batch_requests; /* requests in the batch it ran in */
+	double submit_us, launch_us, done_us; /* server clock: microseconds since svo_server_create */
+} svo_request_result;
+
+typedef struct svo_server_stats {
+	uint64_t submitted, completed, failed;
+	uint64_t batches, batched_requests; /* shared launches issued and the requests they carried */
+	uint64_t rays;                      /* hits produced */
+	uint64_t rebuilds;
+	uint64_t resident_bytes, inflight_bytes, pending;
+} svo_server_stats;
+
+int svo_server_create(const svo_server_config *cfg, svo_server **out);
+/* Finishes every submitted request, then releases the server's streams, buffers and owned octrees. */
+void svo_server_destroy(svo_server *s);
+/* Makes a caller-owned octree resident as a new scene (kept valid by the caller while the server uses it). */
+int svo_server_add_octree(svo_server *s, const svo_octree *o, uint32_t *scene);
+/* Voxelizes and builds `tris` (device) into a server-owned scene, pool shrunk to its range (blocking). */
+int svo_server_build_scene(svo_server *s, const svo_triangle *tris, uint32_t n_tris, uint32_t level, uint32_t *scene);
+/* View of a scene's current octree.  The view stays valid until the scene is rebuilt: a rebuild frees the
+ * server-owned octree it replaces once the batches that use it have completed. */
+int svo_server_scene(svo_server *s, uint32_t scene, svo_octree *view);
+/* Queues a trace request (thread-safe, does not block on the GPU); the request traces the scene's
+ * octree current at submission. */
+int svo_server_submit_trace(svo_server *s, const svo_trace_request *r, uint64_t *ticket);
+/* Queues a rebuild of `scene` from `tris` (device, valid until the request completes) on the server's
+ * rebuild thread and stream; the new octree replaces the scene's when done. */
+int svo_server_submit_rebuild(svo_server *s, uint32_t scene, const svo_triangle *tris, uint32_t n_tris, uint32_t level,
+                              uint64_t *ticket);
+/* Blocks until the request completes (timeout_ms < 0: no limit; otherwise SVO_ERR_TIMEOUT after it),
+ * fills `res` (may be NULL), releases the ticket and returns the request's status. */
+int svo_server_wait(svo_server *s, uint64_t ticket, int timeout_ms, svo_request_result *res);
+void svo_server_get_stats(svo_server *s, svo_server_stats *out);
+
 /* Host helper: Camera::fetch_uniform_data (src/Camera.cpp:77-95) for a position, yaw, pitch, fov and
  * aspect ratio (radians; the reference's default fov is pi/3, src/Camera.hpp:17). */
 void svo_camera_from_angles(const float pos[3], float yaw, float pitch, float fov, float aspect, svo_camera *cam);

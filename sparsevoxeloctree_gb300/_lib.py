@@ -50,6 +50,28 @@ class BatchMesh(ctypes.Structure):
     _fields_ = [("tris", P), ("n_tris", u32), ("level", u32)]
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", u64), ("lanes", u32), ("max_batch_rays", u32), ("max_batch_requests", u32),
+                ("reserved", u32)]
+
+
+class TraceRequest(ctypes.Structure):
+    _fields_ = [("scene", u32), ("mode", u32), ("camera", CameraC), ("width", u32), ("height", u32),
+                ("n_primary", u32), ("n_rays", u32), ("rays", P), ("hits", P), ("seed", u64)]
+
+
+class RequestResult(ctypes.Structure):
+    _fields_ = [("status", i32), ("batch_requests", u32), ("submit_us", ctypes.c_double),
+                ("launch_us", ctypes.c_double), ("done_us", ctypes.c_double)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(n, u64) for n in ("submitted", "completed", "failed", "batches", "batched_requests", "rays",
+                                   "rebuilds", "resident_bytes", "inflight_bytes", "pending")]
+
+
+SVO_REQUEST_CAMERA, SVO_REQUEST_RAYS = 0, 1
+
 ALLOC_FN = ctypes.CFUNCTYPE(P, P, sz)
 RELEASE_FN = ctypes.CFUNCTYPE(None, P, P)
 
@@ -94,6 +116,15 @@ _SIGNATURES = {
     "svo_batcher_result": ([P, u32, ctypes.POINTER(Fraglist), ctypes.POINTER(OctreeC), ctypes.POINTER(BuildInfo)], i32),
     "svo_batcher_set_graph": ([P, i32], i32),
     "svo_batcher_stats": ([P, ctypes.POINTER(u64), ctypes.POINTER(u64)], None),
+    "svo_server_create": ([ctypes.POINTER(ServerConfig), ctypes.POINTER(P)], i32),
+    "svo_server_destroy": ([P], None),
+    "svo_server_add_octree": ([P, ctypes.POINTER(OctreeC), ctypes.POINTER(u32)], i32),
+    "svo_server_build_scene": ([P, P, u32, u32, ctypes.POINTER(u32)], i32),
+    "svo_server_scene": ([P, u32, ctypes.POINTER(OctreeC)], i32),
+    "svo_server_submit_trace": ([P, ctypes.POINTER(TraceRequest), ctypes.POINTER(u64)], i32),
+    "svo_server_submit_rebuild": ([P, u32, P, u32, u32, ctypes.POINTER(u64)], i32),
+    "svo_server_wait": ([P, u64, i32, ctypes.POINTER(RequestResult)], i32),
+    "svo_server_get_stats": ([P, ctypes.POINTER(ServerStats)], None),
     "svo_camera_from_angles": ([ctypes.POINTER(f32), f32, f32, f32, f32, ctypes.POINTER(CameraC)], None),
 }
 

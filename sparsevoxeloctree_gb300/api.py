@@ -264,7 +264,13 @@ class Octree:
         return o
 
     def Empty(self) -> bool:
-        return self.m_buffer is None
+        return self.m_buffer is None and getattr(self, "_view", None) is None
+
+    @property
+    def device(self) -> torch.device:
+        if self.m_buffer is not None:
+            return self.m_buffer.device
+        return torch.device("cuda", torch.cuda.current_device())
 
     def GetBuffer(self) -> torch.Tensor:
         return self.m_buffer
@@ -321,14 +327,14 @@ class OctreeTracer:
         if not count_fetches:
             return ctypes.c_void_p(0)
         if self.fetches is None:
-            self.fetches = torch.zeros(1, dtype=torch.int64, device=self.m_octree.m_buffer.device)
+            self.fetches = torch.zeros(1, dtype=torch.int64, device=self.m_octree.device)
         return _ptr(self.fetches)
 
     def CmdDrawPipeline(self, hits: torch.Tensor | None = None, stream=None, count_fetches: bool = False) -> torch.Tensor:
         """One primary ray per pixel (shader/octree_tracer.frag:23-37); returns the hit buffer."""
         n = self.m_width * self.m_height
         if hits is None:
-            hits = torch.empty(n * HIT_DTYPE.itemsize, dtype=torch.uint8, device=self.m_octree.m_buffer.device)
+            hits = torch.empty(n * HIT_DTYPE.itemsize, dtype=torch.uint8, device=self.m_octree.device)
         cam = camera_struct(self.m_camera)
         oc = self.m_octree.c_struct()
         _lib.check(_lib.load().svo_raycast_camera(ctypes.byref(oc), ctypes.byref(cam), self.m_width, self.m_height,
@@ -425,6 +431,97 @@ class BatchBuilder:
         c, r = _lib.u64(), _lib.u64()
         _lib.load().svo_batcher_stats(self.handle, ctypes.byref(c), ctypes.byref(r))
         return {"graph_captures": int(c.value), "graph_replays": int(r.value)}
+
+
+# ------------------------------------------------------------------------------------------- serving
+class Server:
+    """Resident octrees and continuous batching of trace and rebuild requests (svo_server).  Requests are
+    submitted from any thread and complete asynchronously; Wait() returns their timings."""
+
+    def __init__(self, hbm_budget_bytes: int = 0, lanes: int = 0, max_batch_rays: int = 0,
+                 max_batch_requests: int = 0):
+        lib = _lib.load()
+        cfg = _lib.ServerConfig(hbm_budget_bytes, lanes, max_batch_rays, max_batch_requests, 0)
+        h = ctypes.c_void_p()
+        _lib.check(lib.svo_server_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self.handle = h
+        self._keep: dict[int, object] = {}  # host/device buffers a request reads or writes until it completes
+
+    def close(self) -> None:
+        h = getattr(self, "handle", None)
+        if h is not None and h.value and _lib._lib is not None:
+            _lib._lib.svo_server_destroy(h)
+        self.handle = None
+        self._keep.clear()
+
+    def __del__(self):
+        self.close()
+
+    def BuildScene(self, triangles, level: int) -> int:
+        t = to_device(np.asarray(triangles, TRIANGLE_DTYPE)) if isinstance(triangles, np.ndarray) else triangles
+        sid = _lib.u32()
+        _lib.check(_lib.load().svo_server_build_scene(self.handle, _ptr(t), t.numel() // TRIANGLE_DTYPE.itemsize,
+                                                      int(level), ctypes.byref(sid)))
+        return int(sid.value)
+
+    def AddOctree(self, octree: Octree) -> int:
+        oc = octree.c_struct()
+        sid = _lib.u32()
+        _lib.check(_lib.load().svo_server_add_octree(self.handle, ctypes.byref(oc), ctypes.byref(sid)))
+        self._keep[-1 - int(sid.value)] = octree
+        return int(sid.value)
+
+    def Scene(self, scene: int) -> Octree:
+        o = _lib.OctreeC()
+        _lib.check(_lib.load().svo_server_scene(self.handle, scene, ctypes.byref(o)))
+        return Octree.FromView(o, owner=self)
+
+    def SubmitCamera(self, scene: int, camera, width: int, height: int, n_primary: int, seed: int,
+                     hits_host: torch.Tensor) -> int:
+        """Camera request: hits_host (pinned uint8 tensor) receives 2 * n_primary hits."""
+        r = _lib.TraceRequest()
+        r.scene, r.mode = scene, _lib.SVO_REQUEST_CAMERA
+        r.camera = camera_struct(camera)
+        r.width, r.height, r.n_primary = width, height, n_primary
+        r.hits = hits_host.data_ptr()
+        r.seed = seed & 0xFFFFFFFFFFFFFFFF
+        t = _lib.u64()
+        _lib.check(_lib.load().svo_server_submit_trace(self.handle, ctypes.byref(r), ctypes.byref(t)))
+        self._keep[int(t.value)] = hits_host
+        return int(t.value)
+
+    def SubmitRays(self, scene: int, rays_host: torch.Tensor, hits_host: torch.Tensor) -> int:
+        r = _lib.TraceRequest()
+        r.scene, r.mode = scene, _lib.SVO_REQUEST_RAYS
+        r.n_rays = rays_host.numel() // RAY_DTYPE.itemsize
+        r.rays, r.hits = rays_host.data_ptr(), hits_host.data_ptr()
+        t = _lib.u64()
+        _lib.check(_lib.load().svo_server_submit_trace(self.handle, ctypes.byref(r), ctypes.byref(t)))
+        self._keep[int(t.value)] = (rays_host, hits_host)
+        return int(t.value)
+
+    def SubmitRebuild(self, scene: int, triangles: torch.Tensor, level: int) -> int:
+        t = _lib.u64()
+        _lib.check(_lib.load().svo_server_submit_rebuild(self.handle, scene, _ptr(triangles),
+                                                         triangles.numel() // TRIANGLE_DTYPE.itemsize, int(level),
+                                                         ctypes.byref(t)))
+        self._keep[int(t.value)] = triangles
+        return int(t.value)
+
+    def Wait(self, ticket: int, timeout_ms: int = -1) -> dict:
+        res = _lib.RequestResult()
+        code = _lib.load().svo_server_wait(self.handle, ticket, timeout_ms, ctypes.byref(res))
+        if code == _lib.SVO_ERR_TIMEOUT:  # still running: keep its buffers
+            _lib.check(code)
+        self._keep.pop(ticket, None)
+        _lib.check(code)
+        return {"status": int(res.status), "batch_requests": int(res.batch_requests), "submit_us": res.submit_us,
+                "launch_us": res.launch_us, "done_us": res.done_us}
+
+    def stats(self) -> dict:
+        st = _lib.ServerStats()
+        _lib.load().svo_server_get_stats(self.handle, ctypes.byref(st))
+        return {name: int(getattr(st, name)) for name, _ in _lib.ServerStats._fields_}
 
 
 # ------------------------------------------------------------------------------------------- functional

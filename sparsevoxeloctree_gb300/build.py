@@ -28,6 +28,7 @@ UNITS = {
     "march.cu": ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"],
     "noalloc.cu": [],
     "batch.cu": [],
+    "serve.cu": [],
 }
 HEADERS = ["common.cuh", "svo_internal.h"]
 

@@ -304,41 +304,116 @@ SVO_DEV void sincos_2pi(float u, float &s_out, float &c_out) {
 }
 
 // o = hit pos, d = Diffuse_Sample about the hit normal (shader/diffuse.glsl:7-14 with AlignDirection,
-// shader/util.glsl:5-9); misses give d = 0.
+// shader/util.glsl:5-9); misses give d = 0.  (u1, u2) come from a counter hash of (seed, i).
+SVO_DEV svo_ray bounce_one(const svo_hit &h, uint64_t i, uint64_t seed) {
+	float d[3] = {0.0f, 0.0f, 0.0f};
+	if (h.flags & SVO_HIT_FLAG_HIT) {
+		const uint64_t z = mix64(seed + 0x9E3779B97F4A7C15ull * (i + 1));
+		const float u1 = (float)(uint32_t)(z >> 40) * (1.0f / 16777216.0f);
+		const float u2 = (float)(uint32_t)((z >> 16) & 0xffffffu) * (1.0f / 16777216.0f);
+		const float rr = sqrtf(u1);
+		float sn, cs;
+		sincos_2pi(u2, sn, cs);
+		const float dl[3] = {rr * cs, rr * sn, sqrtf(1.0f - u1)};
+		const uint32_t ax = SVO_HIT_NORMAL_AXIS(h.flags);
+		float nrm[3] = {0.0f, 0.0f, 0.0f};
+		nrm[ax] = (h.flags & SVO_HIT_NORMAL_NEG) ? -1.0f : 1.0f;
+		float ref[3] = {0.0f, 0.0f, 0.0f};
+		if (fabsf(nrm[0]) > 0.01f)
+			ref[1] = 1.0f;
+		else
+			ref[0] = 1.0f;
+		float u[3] = {ref[1] * nrm[2] - ref[2] * nrm[1], ref[2] * nrm[0] - ref[0] * nrm[2],
+		              ref[0] * nrm[1] - ref[1] * nrm[0]};
+		const float ul = sqrtf((u[0] * u[0] + u[1] * u[1]) + u[2] * u[2]);
+#pragma unroll
+		for (int k = 0; k < 3; ++k) u[k] = u[k] / ul;
+		const float v[3] = {nrm[1] * u[2] - nrm[2] * u[1], nrm[2] * u[0] - nrm[0] * u[2],
+		                    nrm[0] * u[1] - nrm[1] * u[0]};
+#pragma unroll
+		for (int k = 0; k < 3; ++k) d[k] = (dl[0] * u[k] + dl[1] * v[k]) + dl[2] * nrm[k];
+	}
+	svo_ray r;
+	r.o[0] = h.pos[0], r.o[1] = h.pos[1], r.o[2] = h.pos[2];
+	r.d[0] = d[0], r.d[1] = d[1], r.d[2] = d[2];
+	return r;
+}
+
 __global__ void bounce_kernel(const svo_hit *__restrict__ hits, uint32_t n, uint64_t seed, svo_ray *__restrict__ rays) {
-	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-		const svo_hit h = hits[i];
-		float d[3] = {0.0f, 0.0f, 0.0f};
-		if (h.flags & SVO_HIT_FLAG_HIT) {
-			const uint64_t z = mix64(seed + 0x9E3779B97F4A7C15ull * ((uint64_t)i + 1));
-			const float u1 = (float)(uint32_t)(z >> 40) * (1.0f / 16777216.0f);
-			const float u2 = (float)(uint32_t)((z >> 16) & 0xffffffu) * (1.0f / 16777216.0f);
-			const float rr = sqrtf(u1);
-			float sn, cs;
-			sincos_2pi(u2, sn, cs);
-			const float dl[3] = {rr * cs, rr * sn, sqrtf(1.0f - u1)};
-			const uint32_t ax = SVO_HIT_NORMAL_AXIS(h.flags);
-			float nrm[3] = {0.0f, 0.0f, 0.0f};
-			nrm[ax] = (h.flags & SVO_HIT_NORMAL_NEG) ? -1.0f : 1.0f;
-			float ref[3] = {0.0f, 0.0f, 0.0f};
-			if (fabsf(nrm[0]) > 0.01f)
-				ref[1] = 1.0f;
-			else
-				ref[0] = 1.0f;
-			float u[3] = {ref[1] * nrm[2] - ref[2] * nrm[1], ref[2] * nrm[0] - ref[0] * nrm[2],
-			              ref[0] * nrm[1] - ref[1] * nrm[0]};
-			const float ul = sqrtf((u[0] * u[0] + u[1] * u[1]) + u[2] * u[2]);
-#pragma unroll
-			for (int k = 0; k < 3; ++k) u[k] = u[k] / ul;
-			const float v[3] = {nrm[1] * u[2] - nrm[2] * u[1], nrm[2] * u[0] - nrm[0] * u[2],
-			                    nrm[0] * u[1] - nrm[1] * u[0]};
-#pragma unroll
-			for (int k = 0; k < 3; ++k) d[k] = (dl[0] * u[k] + dl[1] * v[k]) + dl[2] * nrm[k];
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+		rays[i] = bounce_one(hits[i], i, seed);
+}
+
+// ------------------------------------------------------------------------------------ shared launches
+// Many requests in one launch (the serving loop): work slots are numbered job after job, every job's
+// slot count a multiple of 32, so the 32 slots of a warp ticket belong to one job.  Per ray the work is
+// exactly the single-request kernel's, so a request's hits do not depend on what it shares a launch with.
+SVO_DEV uint32_t job_of(const MarchJob *__restrict__ jobs, uint32_t njobs, uint64_t slot) {
+	uint32_t lo = 0, hi = njobs; // jobs[lo].slot_begin <= slot < jobs[hi].slot_begin
+	while (hi - lo > 1) {
+		const uint32_t mid = (lo + hi) >> 1;
+		if (jobs[mid].slot_begin <= slot)
+			lo = mid;
+		else
+			hi = mid;
+	}
+	return lo;
+}
+
+__global__ void __launch_bounds__(kMarchTPB) march_jobs_kernel(const MarchJob *__restrict__ jobs, uint32_t njobs,
+                                                                uint64_t total, unsigned long long *ticket,
+                                                                uint32_t *status) {
+	__shared__ uint32_t s_stack[SVO_LEVEL_MAX * kMarchTPB];
+	uint32_t *stack = s_stack + threadIdx.x;
+	const uint32_t lane = lane_id();
+	for (;;) {
+		unsigned long long base = 0;
+		if (lane == 0) base = atomicAdd(ticket, 32ull);
+		base = __shfl_sync(kFullMask, base, 0);
+		if (base >= total) break;
+		const MarchJob &J = jobs[job_of(jobs, njobs, base)]; // warp-uniform (jobs are whole tickets)
+		const uint64_t local = base + lane - J.slot_begin;
+		float o[3], d[3];
+		uint32_t r = 0;
+		bool live;
+		if (J.rays == nullptr) {
+			const uint32_t tiles_x = (J.width + 7u) / 8u;
+			const uint32_t tile = (uint32_t)(local >> 5), in = (uint32_t)(local & 31u);
+			const uint32_t x = (tile % tiles_x) * 8u + (in & 7u), y = (tile / tiles_x) * 4u + (in >> 3);
+			r = y * J.width + x;
+			live = x < J.width && r < J.n;
+			if (live) camera_ray(J.cam, J.width, J.height, r, o, d);
+		} else {
+			r = (uint32_t)local;
+			live = local < J.n;
+			if (live) {
+				const float2 *src = reinterpret_cast<const float2 *>(J.rays + r);
+				const float2 p0 = src[0], p1 = src[1], p2 = src[2];
+				o[0] = p0.x, o[1] = p0.y, o[2] = p1.x, d[0] = p1.y, d[1] = p2.x, d[2] = p2.y;
+			}
 		}
-		svo_ray r;
-		r.o[0] = h.pos[0], r.o[1] = h.pos[1], r.o[2] = h.pos[2];
-		r.d[0] = d[0], r.d[1] = d[1], r.d[2] = d[2];
-		rays[i] = r;
+		if (live) {
+			MarchOut m;
+			uint32_t nf;
+			march_ray(J.pool, J.range, J.level, o, d, stack, m, nf, status);
+			store_hit(J.hits, r, m);
+		}
+	}
+}
+
+__global__ void bounce_jobs_kernel(const BounceJob *__restrict__ jobs, uint32_t njobs, uint64_t total) {
+	for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
+		uint32_t lo = 0, hi = njobs;
+		while (hi - lo > 1) {
+			const uint32_t mid = (lo + hi) >> 1;
+			if (jobs[mid].begin <= i)
+				lo = mid;
+			else
+				hi = mid;
+		}
+		const BounceJob &J = jobs[lo];
+		const uint64_t local = i - J.begin;
+		J.rays[local] = bounce_one(J.hits[local], local, J.seed);
 	}
 }
 
@@ -362,6 +437,36 @@ cudaError_t bounce_launch(const svo_hit *hits, uint32_t n, uint64_t seed, svo_ra
 	const int sms = device_sm_count();
 	const uint32_t blocks = (uint32_t)std::min<uint64_t>(((uint64_t)n + 255) / 256, (uint64_t)sms * 8);
 	SVO_LAUNCH("bounce_kernel", stream, bounce_kernel<<<blocks, 256, 0, stream>>>(hits, n, seed, rays););
+	return cudaGetLastError();
+}
+
+} // namespace svo
+
+namespace svo {
+
+uint64_t march_job_slots(const MarchJob &j) {
+	if (j.n == 0) return 0;
+	if (j.rays) return (j.n + 31ull) / 32ull * 32ull;
+	const uint64_t rows = (j.n + (uint64_t)j.width - 1) / j.width; // rows holding the first n pixels
+	return (uint64_t)((j.width + 7u) / 8u) * ((rows + 3) / 4) * 32ull;
+}
+
+cudaError_t march_jobs_launch(const MarchJob *jobs, uint32_t njobs, uint64_t total, unsigned long long *ticket,
+                              uint32_t *status, cudaStream_t stream) {
+	cudaError_t e = cudaMemsetAsync(ticket, 0, sizeof(unsigned long long), stream);
+	if (e != cudaSuccess || total == 0 || njobs == 0) return e;
+	const int sms = device_sm_count();
+	const uint64_t blocks_needed = (total / 32 + kMarchTPB / 32 - 1) / (kMarchTPB / 32);
+	const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(blocks_needed, (uint64_t)sms * 16));
+	SVO_LAUNCH("march_jobs", stream, march_jobs_kernel<<<blocks, kMarchTPB, 0, stream>>>(jobs, njobs, total, ticket, status););
+	return cudaGetLastError();
+}
+
+cudaError_t bounce_jobs_launch(const BounceJob *jobs, uint32_t njobs, uint64_t total, cudaStream_t stream) {
+	if (total == 0 || njobs == 0) return cudaSuccess;
+	const int sms = device_sm_count();
+	const uint32_t blocks = (uint32_t)std::min<uint64_t>((total + 255) / 256, (uint64_t)sms * 8);
+	SVO_LAUNCH("bounce_jobs", stream, bounce_jobs_kernel<<<blocks, 256, 0, stream>>>(jobs, njobs, total););
 	return cudaGetLastError();
 }
 
