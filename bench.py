@@ -180,6 +180,16 @@ def engine_arm(args, rank: int, world: int, device) -> dict:
         builder.CmdBuild()
         tracer.CmdDrawPipeline(hits)
 
+    tuning = None
+    if not args.no_autotune:  # launch parameters measured on this workload before timing
+        from sparsevoxeloctree_gb300 import autotune
+        t_tune = time.perf_counter()
+        tuning = {"emit": autotune.tune_voxelize(vox), "build": autotune.tune_build(builder),
+                  "march": autotune.tune_march(tracer, hits)}
+        tuning = {k: {"best": v["best"], "best_ms": v["best_ms"], "level": v["level"], "size_class": v["size_class"],
+                      "candidates": len(v["trials"])} for k, v in tuning.items()}
+        tuning["seconds"] = time.perf_counter() - t_tune
+
     flush_buf = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=device)
     for _ in range(args.warmup):
         flush_buf.zero_()
@@ -256,6 +266,7 @@ def engine_arm(args, rank: int, world: int, device) -> dict:
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(scene, per_step=False)
     return {"value": ms, "ms_per_step": ms, "step_ms_all": step_ms, "stages": stages, "roofline": roofline,
+            "tuning": tuning,
             "clocks": clocks, "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": int(launches),
             "config_extra": {"level": scene.level, "triangles": T, "fragments": F, "rays": n_rays}}
 
@@ -354,6 +365,14 @@ def batch_leg(args, device) -> dict:
             out.append((time.perf_counter() - t0) * 1e3)
         return out
 
+    batched()  # first build: records the graphs
+    tuning = None
+    if not args.no_autotune:
+        from sparsevoxeloctree_gb300 import autotune
+        F0 = sum(bb.GetInfo(i)["fragments"] for i in range(len(meshes)))
+        tr = autotune.tune_batch(bb, batch, F0, sum(len(t) for t, _ in meshes))
+        tuning = {k: {"best": v["best"], "best_ms": v["best_ms"], "level": v["level"], "size_class": v["size_class"]}
+                  for k, v in tr.items()}
     reps = max(3, min(args.steps, 10))
     launches0 = lib.svo_kernel_launches()
     b_ms = timed(batched, reps)
@@ -393,7 +412,7 @@ def batch_leg(args, device) -> dict:
                          "achieved_gbs": alg / (bm * 1e-3) / 1e9, "peak": peaks["hbm_gbs"],
                          "frac": alg / (bm * 1e-3) / 1e9 / peaks["hbm_gbs"]},
             "graph": bb.stats(), "timing": "host wall clock per batch (median), blocking readbacks included",
-            "kernels_one_batch": kernels,
+            "kernels_one_batch": kernels, "autotuned": tuning,
             "reps": reps, "kernel_launches_recorded": int(lib.svo_kernel_launches() - launches0)}
 
 
@@ -615,6 +634,7 @@ def main() -> int:
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-build leg")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
+    ap.add_argument("--no-autotune", action="store_true", help="default launch parameters")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -657,7 +677,7 @@ def main() -> int:
     line.update({"value": res["value"], "ms_per_step": res["ms_per_step"], "config": config,
                  "stages": res["stages"], "roofline": res["roofline"], "cpu_baseline": res["cpu_baseline"],
                  "e2e": res["e2e"], "clocks": res["clocks"], "gpu_launches": res["gpu_launches"],
-                 "step_ms": res["step_ms_all"]})
+                 "step_ms": res["step_ms_all"], "autotuned": res["tuning"]})
     for key in ("batched", "served"):
         if key in res:
             line[key] = res[key]

@@ -164,6 +164,24 @@ int svo_stream_synchronize(void *stream);
 void svo_profile_enable(int on);
 size_t svo_profile_summary(char *buf, size_t cap);
 
+/* Launch parameters (an autotuner's table: sparsevoxeloctree_gb300/autotune.py measures the candidates and
+ * sets the best).  A value is kept per (parameter, octree level, size class), the size class of a launch
+ * being that of its work items (fragments, triangles or rays): class 0 below 65,536, then one class per
+ * factor 4, class 7 from 2^30.  Results do not depend on these values, only the speed does. */
+#define SVO_TUNE_MARCH_BLOCK 0u         /* threads per march block: 64, 128 (default), 256 */
+#define SVO_TUNE_MARCH_RAYS_PER_LANE 1u /* rays a lane takes per ticket: 1 (default), 2 */
+#define SVO_TUNE_MARCH_STACK_SHARED 2u  /* traversal stack in shared memory (1, default) or local memory (0) */
+#define SVO_TUNE_SWEEP_BLOCKS 3u        /* blocks per SM of the build's fragment sweeps (default 16) */
+#define SVO_TUNE_LEAF_BLOCKS 4u         /* blocks per SM of the build's leaf stage (default 6) */
+#define SVO_TUNE_EMIT_BLOCKS 5u         /* blocks per SM of the voxelizer's emission (default 16) */
+#define SVO_TUNE_PARAMS 6u
+/* level 0: every level; size_class -1: every class.  Rejects values a parameter does not allow. */
+int svo_tune_set(uint32_t param, uint32_t level, int32_t size_class, int32_t value);
+/* The value a launch of `items` work items at `level` uses. */
+int svo_tune_get(uint32_t param, uint32_t level, uint64_t items);
+uint32_t svo_tune_size_class(uint64_t items);
+void svo_tune_reset(void);
+
 /* ------------------------------------------------------------------ voxelize (Voxelizer) */
 
 /* Voxelizer::Create + CmdVoxelize (src/Voxelizer.cpp:5-26, 134-179): count pass, exact allocation,

@@ -108,6 +108,43 @@ int device_sm_count() {
 	return g_sm_count[dev];
 }
 
+// ---------------------------------------------------------------- launch-parameter table
+// Entry [param][level][size class]; level 0 is unused (a set with level 0 writes every level).
+constexpr uint32_t kTuneClasses = 8;
+static const int kTuneDefault[kTuneParams] = {128, 1, 1, 16, 6, 16};
+static std::atomic<int> g_tune[kTuneParams][SVO_LEVEL_MAX + 1][kTuneClasses];
+static std::once_flag g_tune_once;
+
+static void tune_init() {
+	std::call_once(g_tune_once, [] {
+		for (uint32_t p = 0; p < kTuneParams; ++p)
+			for (uint32_t l = 0; l <= SVO_LEVEL_MAX; ++l)
+				for (uint32_t c = 0; c < kTuneClasses; ++c) g_tune[p][l][c].store(kTuneDefault[p]);
+	});
+}
+
+static bool tune_valid(uint32_t param, int v) {
+	switch (param) {
+	case kTuneMarchBlock: return v == 64 || v == 128 || v == 256;
+	case kTuneMarchRays: return v == 1 || v == 2;
+	case kTuneMarchShared: return v == 0 || v == 1;
+	default: return v >= 1 && v <= 64;
+	}
+}
+
+static uint32_t size_class_of(uint64_t items) {
+	uint32_t c = 0; // < 64k items: class 0; then one class per factor 4, up to class 7 (>= 1G)
+	for (uint64_t lim = 1ull << 16; items >= lim && c + 1 < kTuneClasses; lim <<= 2) ++c;
+	return c;
+}
+
+int tune_value(uint32_t param, uint32_t level, uint64_t items) {
+	tune_init();
+	if (param >= kTuneParams) return 0;
+	if (level > SVO_LEVEL_MAX) level = SVO_LEVEL_MAX;
+	return g_tune[param][level][size_class_of(items)].load(std::memory_order_relaxed);
+}
+
 // Stream-ordered allocations come from the device's default memory pool; keeping freed memory in the
 // pool (release threshold = max) makes repeated builds allocation-free after the first one.
 static void prepare_pool() {
@@ -245,6 +282,30 @@ size_t svo_profile_summary(char *buf, size_t cap) {
 	return out.size();
 }
 const char *svo_version(void) { return "svo-gb300 0.1 (sm_103a)"; }
+
+uint32_t svo_tune_size_class(uint64_t items) { return size_class_of(items); }
+
+int svo_tune_set(uint32_t param, uint32_t level, int32_t size_class, int32_t value) {
+	tune_init();
+	if (param >= kTuneParams) return fail(SVO_ERR_INVALID, "unknown launch parameter %u", param);
+	if (level > SVO_LEVEL_MAX) return fail(SVO_ERR_INVALID, "level %u outside [0, %u]", level, SVO_LEVEL_MAX);
+	if (size_class >= (int32_t)kTuneClasses || size_class < -1)
+		return fail(SVO_ERR_INVALID, "size class %d outside [-1, %u]", size_class, kTuneClasses - 1);
+	if (!tune_valid(param, value)) return fail(SVO_ERR_INVALID, "value %d not allowed for parameter %u", value, param);
+	for (uint32_t l = level ? level : 1; l <= (level ? level : SVO_LEVEL_MAX); ++l)
+		for (uint32_t c = size_class < 0 ? 0 : (uint32_t)size_class; c <= (size_class < 0 ? kTuneClasses - 1 : (uint32_t)size_class); ++c)
+			g_tune[param][l][c].store(value);
+	return SVO_OK;
+}
+
+int svo_tune_get(uint32_t param, uint32_t level, uint64_t items) { return tune_value(param, level ? level : 1, items); }
+
+void svo_tune_reset(void) {
+	tune_init();
+	for (uint32_t p = 0; p < kTuneParams; ++p)
+		for (uint32_t l = 0; l <= SVO_LEVEL_MAX; ++l)
+			for (uint32_t c = 0; c < kTuneClasses; ++c) g_tune[p][l][c].store(kTuneDefault[p]);
+}
 uint64_t svo_kernel_launches(void) { return g_launches.load(); }
 
 // ------------------------------------------------------------------------------------------ voxelize

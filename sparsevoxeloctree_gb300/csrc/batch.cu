@@ -228,6 +228,8 @@ static int batch_build(Batcher &b, const svo_batch_mesh *meshes, uint32_t M, cud
 	vb.shifts = (unsigned long long *)(ds + pl.shifts);
 	vb.mesh_out = (unsigned long long *)(ds + pl.mesh_out);
 	vb.M = M;
+	vb.max_level = 1;
+	for (uint32_t m = 0; m < M; ++m) vb.max_level = std::max(vb.max_level, meshes[m].level);
 	const uint32_t n = (uint32_t)N;
 	uint64_t unit_cap = std::max<uint64_t>(vox_default_unit_cap(n), b.unit_hint);
 	VoxWorkspace vw;

@@ -967,15 +967,17 @@ static BuildBatch single_batch(const BuildWorkspace &w, uint32_t count, uint32_t
 
 // The stages shared by a single build and a batch.  `maxD` = deepest dense depth of any mesh.
 template <bool B>
-static void launch_dense_and_scatter(const uint64_t *frags, uint64_t n, const BuildBatch &bb, uint32_t M, uint32_t maxD,
+static void launch_dense_and_scatter(const uint64_t *frags, uint64_t n, uint32_t tune_level, const BuildBatch &bb,
+                                     uint32_t M, uint32_t maxD,
                                      uint32_t dense_words, uint32_t items_total, uint32_t nb_total, BuildState *gstate,
                                      unsigned long long *descs, uint32_t *bcount, uint32_t *boff, uint32_t *bfill,
                                      uint32_t *blist, unsigned long long *bdescs, uint64_t *sorted,
                                      cudaStream_t stream) {
 	const int sms = device_sm_count();
+	const uint32_t sweep = (uint32_t)sms * (uint32_t)tune_value(kTuneSweepBlocks, tune_level, n);
 	SVO_LAUNCH("build_init", stream, build_init<B><<<M, 256, 0, stream>>>(bb, gstate););
 	SVO_LAUNCH("dense_mark", stream,
-	           dense_mark<B><<<grid_for(n, kTPB, (uint32_t)sms * 16), kTPB, 0, stream>>>(frags, n, bb, bcount););
+	           dense_mark<B><<<grid_for(n, kTPB, sweep), kTPB, 0, stream>>>(frags, n, bb, bcount););
 	SVO_LAUNCH("bucket_scan", stream,
 	           bucket_scan<<<(nb_total + kScanTile - 1) / kScanTile, kTPB, 0, stream>>>(bcount, nb_total, boff, blist,
 	                                                                                   gstate, bdescs););
@@ -994,7 +996,7 @@ static void launch_dense_and_scatter(const uint64_t *frags, uint64_t n, const Bu
 	// the bucketed copy: leaf items when the leaf parents are dense (their bitmap is final now), fragments
 	// for the sparse levels otherwise
 	SVO_LAUNCH("bucket_scatter", stream,
-	           bucket_scatter<B><<<grid_for(n, kTPB, (uint32_t)sms * 16), kTPB, 0, stream>>>(frags, n, bb, boff, bfill,
+	           bucket_scatter<B><<<grid_for(n, kTPB, sweep), kTPB, 0, stream>>>(frags, n, bb, boff, bfill,
 	                                                                                      sorted););
 }
 
@@ -1002,7 +1004,8 @@ static void launch_sparse(const uint64_t *sorted, uint32_t count, uint32_t level
                           uint64_t capacity, uint32_t *cache, BuildState *state, unsigned long long *descs,
                           const BuildState *gstate, cudaStream_t stream) {
 	const int sms = device_sm_count();
-	const uint32_t tag_blocks = grid_for(((uint64_t)count + 3) / 4, kTPB, (uint32_t)sms * 16);
+	const uint32_t tag_blocks =
+	    grid_for(((uint64_t)count + 3) / 4, kTPB, (uint32_t)sms * (uint32_t)tune_value(kTuneSweepBlocks, level, count));
 	for (uint32_t depth = dv.D + 1; depth < level; ++depth) {
 		SVO_LAUNCH("build_tag", stream,
 		           build_tag<<<tag_blocks, kTPB, 0, stream>>>(sorted, count, level, depth, pool, cache, dv, state,
@@ -1014,7 +1017,8 @@ static void launch_sparse(const uint64_t *sorted, uint32_t count, uint32_t level
 }
 
 template <bool B>
-static void launch_leaf_stage(const BuildBatch &bb, uint32_t M, uint32_t nb_total, const uint32_t *boff,
+static void launch_leaf_stage(const BuildBatch &bb, uint32_t M, uint32_t tune_level, uint64_t n, uint32_t nb_total,
+                              const uint32_t *boff,
                               const uint32_t *blist, const BuildState *gstate, uint4 *bmeta, uint32_t *bmesh,
                               const uint64_t *sorted, const uint32_t *cache, cudaStream_t stream) {
 	const int sms = device_sm_count();
@@ -1024,7 +1028,8 @@ static void launch_leaf_stage(const BuildBatch &bb, uint32_t M, uint32_t nb_tota
 	           bucket_meta<B><<<grid_for(meta_items, kTPB, (uint32_t)sms * 4), kTPB, 0, stream>>>(bb, boff, blist, gstate,
 	                                                                                         bmeta, bmesh););
 	SVO_LAUNCH("build_leaf", stream,
-	           build_leaf<B><<<(uint32_t)sms * 6, kTPB, smem, stream>>>(sorted, bb, cache, bmeta, bmesh,
+	           build_leaf<B><<<(uint32_t)sms * (uint32_t)tune_value(kTuneLeafBlocks, tune_level, n), kTPB, smem, stream>>>(
+	               sorted, bb, cache, bmeta, bmesh,
 	                                                                     const_cast<BuildState *>(gstate)););
 }
 
@@ -1038,7 +1043,7 @@ cudaError_t build_launch_interior(const uint64_t *frags, uint32_t count, uint32_
 	if (e != cudaSuccess) return e;
 	const BuildBatch bb = single_batch(w, count, level, pool, capacity);
 	const uint32_t items = dense_items(level, w.dv.off);
-	launch_dense_and_scatter<false>(frags, count, bb, 1, w.dv.D, w.dense_words, items, w.nb, w.state, w.descs, w.bcount,
+	launch_dense_and_scatter<false>(frags, count, level, bb, 1, w.dv.D, w.dense_words, items, w.nb, w.state, w.descs, w.bcount,
 	                                w.boff, w.bfill, w.blist, w.bdescs, w.sorted, stream);
 	if (level > w.dv.D + 1)
 		launch_sparse(w.sorted, count, level, w.dv, pool, capacity, w.cache, w.state, w.descs, w.state, stream);
@@ -1048,7 +1053,8 @@ cudaError_t build_launch_interior(const uint64_t *frags, uint32_t count, uint32_
 cudaError_t build_launch_leaf(uint32_t count, uint32_t level, uint32_t *pool, uint64_t capacity,
                               const BuildWorkspace &w, cudaStream_t stream) {
 	const BuildBatch bb = single_batch(w, count, level, pool, capacity);
-	launch_leaf_stage<false>(bb, 1, w.nb, w.boff, w.blist, w.state, w.bmeta, nullptr, w.sorted, w.cache, stream);
+	launch_leaf_stage<false>(bb, 1, level, count, w.nb, w.boff, w.blist, w.state, w.bmeta, nullptr, w.sorted, w.cache,
+	                         stream);
 	return cudaGetLastError();
 }
 
@@ -1070,7 +1076,8 @@ cudaError_t build_launch_batch(const uint64_t *frags, const BuildBatchPlan &p, v
 	if (e == cudaSuccess) e = cudaMemsetAsync(p.bfill, 0, (size_t)p.nb_total * 4, stream);
 	if (e == cudaSuccess) e = cudaMemsetAsync(p.bdescs, 0, p.bdesc_count * sizeof(unsigned long long), stream);
 	if (e != cudaSuccess) return e;
-	launch_dense_and_scatter<true>(frags, p.frags_total, p.bb, p.M, p.max_D, p.dense_total, p.items_total, p.nb_total,
+	launch_dense_and_scatter<true>(frags, p.frags_total, p.max_level, p.bb, p.M, p.max_D, p.dense_total, p.items_total,
+	                               p.nb_total,
 	                               p.gstate, p.descs, p.bcount, p.boff, p.bfill, p.blist, p.bdescs, p.sorted, stream);
 	for (uint32_t m = 0; m < p.M; ++m) {
 		const BuildMesh &md = p.meshes[m];
@@ -1081,7 +1088,8 @@ cudaError_t build_launch_batch(const uint64_t *frags, const BuildBatchPlan &p, v
 		launch_sparse(p.sorted + sb, md.count, md.level, md.dv, md.pool, md.capacity, p.cache + sb, md.state, p.descs,
 		              p.gstate, stream);
 	}
-	launch_leaf_stage<true>(p.bb, p.M, p.nb_total, p.boff, p.blist, p.gstate, p.bmeta, p.bmesh, p.sorted, p.cache, stream);
+	launch_leaf_stage<true>(p.bb, p.M, p.max_level, p.frags_total, p.nb_total, p.boff, p.blist, p.gstate, p.bmeta,
+	                        p.bmesh, p.sorted, p.cache, stream);
 	SVO_LAUNCH("build_export", stream,
 	           build_export<true><<<(p.M + 127) / 128, 128, 0, stream>>>(p.bb, p.gstate, (uint32_t *)result_dev););
 	return cudaGetLastError();

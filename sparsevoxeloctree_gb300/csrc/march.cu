@@ -22,7 +22,6 @@
 namespace svo {
 
 constexpr int kMarchTPB = 128;
-constexpr uint32_t kRaysPerLane = 1; // rays a lane takes per ticket
 constexpr float kEps = 3.552713678800501e-15f; // EPS of shader/octree.glsl:44 (2^-48)
 
 SVO_DEV float max_glsl(float x, float y) { return x < y ? y : x; }
@@ -36,7 +35,9 @@ struct MarchOut {
 	uint32_t voxel_lo, voxel_hi; // packed uint16 voxel[3] and flags, as in svo_hit
 };
 
-// One ray; `stack` points at this thread's column of the shared stack (stride kMarchTPB).
+// One ray; `stack` points at this thread's stack: a column of a shared [level][thread] array (STRIDE =
+// threads per block) or a private array in local memory (STRIDE = 1).
+template <int STRIDE>
 SVO_DEV void march_ray(const uint32_t *__restrict__ pool, uint32_t range, uint32_t level, const float o[3],
                        const float dir[3], uint32_t *stack, MarchOut &out, uint32_t &nfetch, uint32_t *status) {
 	nfetch = 0;
@@ -48,7 +49,7 @@ SVO_DEV void march_ray(const uint32_t *__restrict__ pool, uint32_t range, uint32
 		out.voxel_hi = 0x0000ffffu;
 		return;
 	}
-	for (uint32_t k = 0; k < level; ++k) stack[k * kMarchTPB] = 0u;
+	for (uint32_t k = 0; k < level; ++k) stack[k * STRIDE] = 0u;
 	float d[3] = {eps_clamp(dir[0]), eps_clamp(dir[1]), eps_clamp(dir[2])};
 	float coef[3], bias[3];
 #pragma unroll
@@ -115,7 +116,7 @@ SVO_DEV void march_ray(const uint32_t *__restrict__ pool, uint32_t range, uint32
 				scale = 0xffffffffu;
 				break;
 			}
-			if (tc_max < h) stack[(SVO_STACK_SIZE - 1 - scale) * kMarchTPB] = parent; // push
+			if (tc_max < h) stack[(SVO_STACK_SIZE - 1 - scale) * STRIDE] = parent; // push
 			h = tc_max;
 			parent = cur & 0x3fffffffu;
 			idx = 0;
@@ -148,7 +149,7 @@ SVO_DEV void march_ray(const uint32_t *__restrict__ pool, uint32_t range, uint32
 			scale = diff ? 31u - (uint32_t)__clz(diff) : 0xffffffffu; // findMSB
 			if (scale >= SVO_STACK_SIZE) break;
 			scale_exp2 = __uint_as_float((scale - SVO_STACK_SIZE + 127u) << 23u);
-			parent = stack[(SVO_STACK_SIZE - 1 - scale) * kMarchTPB];
+			parent = stack[(SVO_STACK_SIZE - 1 - scale) * STRIDE];
 			uint32_t sh[3];
 #pragma unroll
 			for (int k = 0; k < 3; ++k) {
@@ -220,10 +221,15 @@ SVO_DEV void camera_ray(const svo_camera &cam, uint32_t width, uint32_t height, 
 	}
 }
 
-template <bool CAMERA>
-__global__ void __launch_bounds__(kMarchTPB) march_kernel(MarchArgs a) {
-	__shared__ uint32_t s_stack[SVO_LEVEL_MAX * kMarchTPB];
-	uint32_t *stack = s_stack + threadIdx.x;
+// Variants (chosen per launch from the launch-parameter table): TPB threads per block, RPL rays per lane
+// per ticket, SHARED: stack in shared memory ([level][thread], 32 distinct banks per warp) or in a
+// private local-memory array.
+template <bool CAMERA, int TPB, int RPL, bool SHARED>
+__global__ void __launch_bounds__(TPB) march_kernel(MarchArgs a) {
+	constexpr int kStride = SHARED ? TPB : 1;
+	__shared__ uint32_t s_stack[SHARED ? SVO_LEVEL_MAX * TPB : 1];
+	uint32_t l_stack[SHARED ? 1 : SVO_LEVEL_MAX];
+	uint32_t *stack = SHARED ? s_stack + threadIdx.x : l_stack;
 	const uint32_t lane = lane_id();
 	// work slots: ray indices, or for camera rays 32 slots per 8x4 tile of the (padded) image
 	const uint32_t tiles_x = CAMERA ? (a.width + 7u) / 8u : 0u;
@@ -231,11 +237,11 @@ __global__ void __launch_bounds__(kMarchTPB) march_kernel(MarchArgs a) {
 	unsigned long long fetched = 0;
 	for (;;) {
 		unsigned long long base = 0;
-		if (lane == 0) base = atomicAdd(a.ticket, (unsigned long long)(32u * kRaysPerLane));
+		if (lane == 0) base = atomicAdd(a.ticket, (unsigned long long)(32u * RPL));
 		base = __shfl_sync(kFullMask, base, 0);
 		if (base >= slots) break;
 #pragma unroll 1
-		for (uint32_t k = 0; k < kRaysPerLane; ++k) {
+		for (uint32_t k = 0; k < (uint32_t)RPL; ++k) {
 			const uint64_t slot = base + k * 32u + lane;
 			if (slot >= slots) break;
 			float o[3], d[3];
@@ -254,7 +260,7 @@ __global__ void __launch_bounds__(kMarchTPB) march_kernel(MarchArgs a) {
 			}
 			MarchOut m;
 			uint32_t nf;
-			march_ray(a.pool, a.range, a.level, o, d, stack, m, nf, a.status);
+			march_ray<kStride>(a.pool, a.range, a.level, o, d, stack, m, nf, a.status);
 			store_hit(a.hits, r, m);
 			fetched += nf;
 		}
@@ -395,7 +401,7 @@ __global__ void __launch_bounds__(kMarchTPB) march_jobs_kernel(const MarchJob *_
 		if (live) {
 			MarchOut m;
 			uint32_t nf;
-			march_ray(J.pool, J.range, J.level, o, d, stack, m, nf, status);
+			march_ray<kMarchTPB>(J.pool, J.range, J.level, o, d, stack, m, nf, status);
 			store_hit(J.hits, r, m);
 		}
 	}
@@ -418,17 +424,44 @@ __global__ void bounce_jobs_kernel(const BounceJob *__restrict__ jobs, uint32_t 
 }
 
 // ---------------------------------------------------------------------------------------------------
+template <bool CAMERA, int TPB, int RPL, bool SHARED>
+static void launch_variant(const MarchArgs &a, cudaStream_t stream) {
+	const int sms = device_sm_count();
+	const uint64_t warps_needed = ((uint64_t)a.n + 32 * RPL - 1) / (32 * RPL);
+	const uint64_t blocks_needed = (warps_needed + TPB / 32 - 1) / (TPB / 32);
+	const uint64_t cap = (uint64_t)sms * (2048 / TPB); // persistent: a full SM's worth of threads
+	const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(blocks_needed, cap));
+	SVO_LAUNCH(CAMERA ? "march_camera" : "march_rays", stream,
+	           march_kernel<CAMERA, TPB, RPL, SHARED><<<blocks, TPB, 0, stream>>>(a););
+}
+
+template <bool CAMERA, int TPB>
+static void launch_rpl(const MarchArgs &a, int rpl, bool shared, cudaStream_t stream) {
+	if (rpl == 2) {
+		if (shared) launch_variant<CAMERA, TPB, 2, true>(a, stream);
+		else launch_variant<CAMERA, TPB, 2, false>(a, stream);
+	} else {
+		if (shared) launch_variant<CAMERA, TPB, 1, true>(a, stream);
+		else launch_variant<CAMERA, TPB, 1, false>(a, stream);
+	}
+}
+
+template <bool CAMERA> static void launch_tuned(const MarchArgs &a, cudaStream_t stream) {
+	const int tpb = tune_value(kTuneMarchBlock, a.level, a.n);
+	const int rpl = tune_value(kTuneMarchRays, a.level, a.n);
+	const bool shared = tune_value(kTuneMarchShared, a.level, a.n) != 0;
+	if (tpb == 64) launch_rpl<CAMERA, 64>(a, rpl, shared, stream);
+	else if (tpb == 256) launch_rpl<CAMERA, 256>(a, rpl, shared, stream);
+	else launch_rpl<CAMERA, 128>(a, rpl, shared, stream);
+}
+
 cudaError_t march_launch(const MarchArgs &a, bool camera, cudaStream_t stream) {
 	cudaError_t e = cudaMemsetAsync(a.ticket, 0, sizeof(unsigned long long), stream);
 	if (e != cudaSuccess || a.n == 0) return e;
-	const int sms = device_sm_count();
-	const uint64_t warps_needed = ((uint64_t)a.n + 32 * kRaysPerLane - 1) / (32 * kRaysPerLane);
-	const uint64_t blocks_needed = (warps_needed + kMarchTPB / 32 - 1) / (kMarchTPB / 32);
-	const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(blocks_needed, (uint64_t)sms * 16));
 	if (camera)
-		SVO_LAUNCH("march_camera", stream, march_kernel<true><<<blocks, kMarchTPB, 0, stream>>>(a););
+		launch_tuned<true>(a, stream);
 	else
-		SVO_LAUNCH("march_rays", stream, march_kernel<false><<<blocks, kMarchTPB, 0, stream>>>(a););
+		launch_tuned<false>(a, stream);
 	return cudaGetLastError();
 }
 

@@ -40,6 +40,18 @@ struct ProfScope {
 	} while (0)
 int device_sm_count();   // SMs of the current device (cached per device)
 
+// Launch parameters set by the autotuner (svo_tune_set), per (level, size class of the launch's work).
+enum : uint32_t {
+	kTuneMarchBlock = 0,   // threads per march block: 64, 128, 256
+	kTuneMarchRays = 1,    // rays a lane takes per ticket: 1, 2
+	kTuneMarchShared = 2,  // traversal stack in shared (1) or local (0) memory
+	kTuneSweepBlocks = 3,  // blocks per SM of the fragment sweeps
+	kTuneLeafBlocks = 4,   // blocks per SM of the leaf stage
+	kTuneEmitBlocks = 5,   // blocks per SM of the voxelizer's emission
+	kTuneParams = 6
+};
+int tune_value(uint32_t param, uint32_t level, uint64_t items);
+
 // ---------------------------------------------------------------- voxelize
 enum : uint32_t { kCtrTicketA = 0, kCtrTicketB = 1, kCtrStatus = 2, kCtrCount = 8 };
 enum : uint32_t { kStatusUnits = 8u }; // the unit arrays of the workspace are too small (caller retries)
@@ -71,6 +83,7 @@ struct VoxBatch {
 	unsigned long long *shifts;   // [2M] output shift of small / large fragments (vox_launch_batch_totals)
 	unsigned long long *mesh_out; // [4M] per mesh: fragments, first fragment, units, 0 (for the host)
 	uint32_t M;
+	uint32_t max_level;           // deepest level of the batch (selects its launch parameters)
 	VoxMesh one;                  // the mesh of a single voxelization
 };
 

@@ -618,12 +618,13 @@ template <bool B> static void launch_count(const VoxBatch &vb, uint32_t n, const
 }
 
 template <bool B>
-static void launch_emit(const VoxBatch &vb, uint32_t n, const VoxWorkspace &w, uint64_t *frags, uint64_t capacity,
-                        cudaStream_t stream) {
+static void launch_emit(const VoxBatch &vb, uint32_t n, uint32_t tune_level, const VoxWorkspace &w, uint64_t *frags,
+                        uint64_t capacity, cudaStream_t stream) {
 	const int sms = device_sm_count();
-	SVO_LAUNCH("vox_emit", stream, vox_emit<B><<<(uint32_t)sms * 16, kTPB, 0, stream>>>(vb, n, w, frags, capacity););
+	const uint32_t per_sm = (uint32_t)tune_value(kTuneEmitBlocks, tune_level, n);
+	SVO_LAUNCH("vox_emit", stream, vox_emit<B><<<(uint32_t)sms * per_sm, kTPB, 0, stream>>>(vb, n, w, frags, capacity););
 	SVO_LAUNCH("vox_emit_units", stream,
-	           vox_emit_units<B><<<(uint32_t)sms * 8, kTPB, 0, stream>>>(vb, n, w, frags, capacity););
+	           vox_emit_units<B><<<(uint32_t)sms * std::max(1u, per_sm / 2), kTPB, 0, stream>>>(vb, n, w, frags, capacity););
 }
 
 cudaError_t vox_launch_count(const svo_triangle *tris, uint32_t n, uint32_t level, const VoxWorkspace &w,
@@ -637,7 +638,7 @@ cudaError_t vox_launch_count(const svo_triangle *tris, uint32_t n, uint32_t leve
 cudaError_t vox_launch_emit(const svo_triangle *tris, uint32_t n, uint32_t level, const VoxWorkspace &w,
                             uint64_t *frags, uint64_t capacity, cudaStream_t stream) {
 	if (n == 0) return cudaSuccess;
-	launch_emit<false>(single_vox(tris, level), n, w, frags, capacity, stream);
+	launch_emit<false>(single_vox(tris, level), n, level, w, frags, capacity, stream);
 	return cudaGetLastError();
 }
 
@@ -664,7 +665,7 @@ cudaError_t vox_launch_count_batch(const VoxBatch &vb, uint32_t n, const VoxWork
 cudaError_t vox_launch_emit_batch(const VoxBatch &vb, uint32_t n, const VoxWorkspace &w, uint64_t *frags,
                                   uint64_t capacity, cudaStream_t stream) {
 	if (n == 0) return cudaSuccess;
-	launch_emit<true>(vb, n, w, frags, capacity, stream);
+	launch_emit<true>(vb, n, vb.max_level, w, frags, capacity, stream);
 	return cudaGetLastError();
 }
 

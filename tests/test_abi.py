@@ -90,3 +90,27 @@ def test_batcher_rejects_bad_batches_before_any_launch(lib):
     finally:
         lib.svo_batcher_destroy(h)
     assert lib.svo_kernel_launches() == before
+
+
+def test_launch_parameter_table(lib):
+    from sparsevoxeloctree_gb300 import autotune
+    lib.svo_tune_reset()
+    try:
+        assert autotune.size_class(1000) == 0 and autotune.size_class(1 << 16) == 1
+        assert autotune.size_class(38_000_000) == 5 and autotune.size_class(1 << 40) == 7
+        assert autotune.get("march_block", 10, 2_000_000) == 128
+        autotune.set_value("march_block", 10, autotune.size_class(2_000_000), 256)
+        assert autotune.get("march_block", 10, 2_000_000) == 256
+        assert autotune.get("march_block", 9, 2_000_000) == 128      # other level untouched
+        assert autotune.get("march_block", 10, 20_000_000) == 128     # other size class untouched
+        autotune.set_value("leaf_blocks", 0, -1, 8)                    # every level and class
+        assert all(autotune.get("leaf_blocks", lv, 10 ** k) == 8 for lv in (1, 7, 12) for k in (3, 6, 9))
+        for bad in ((0, 10, 3, 100), (1, 10, 3, 3), (2, 10, 3, 2), (3, 10, 3, 0), (3, 13, 3, 8), (3, 10, 8, 8),
+                    (9, 10, 3, 8)):
+            assert lib.svo_tune_set(*bad) == _lib.SVO_ERR_INVALID
+        t = autotune.table()
+        assert t["march_block"]["default"] == 128 and t["march_block"]["10:3"] == 256
+        assert t["leaf_blocks"]["default"] == 8
+    finally:
+        lib.svo_tune_reset()
+    assert autotune.get("leaf_blocks", 10, 1000) == 6
