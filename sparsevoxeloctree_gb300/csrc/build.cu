@@ -120,8 +120,10 @@ SVO_DEV bool check_ok(bool ok, uint32_t id, BuildState *g) {
 	return ok;
 }
 #define SVO_CHECK(cond, id, g) check_ok((cond), (id), (g))
+#define SVO_CHECK_FAIL(id, g) (void)check_ok(false, (id), (g))
 #else
 #define SVO_CHECK(cond, id, g) true
+#define SVO_CHECK_FAIL(id, g) ((void)0)
 #endif
 
 // A fragment of a level-L octree has every coordinate below 2^L; the build skips any other (a caller's
@@ -487,9 +489,17 @@ __global__ void __launch_bounds__(kTPB) build_alloc(uint32_t *__restrict__ pool,
 // in the pool (breadth-first order is Morton order within a depth), so that block writes them whole.
 // In a batch the buckets of all meshes are concatenated in mesh order, so one scan over all of them
 // places every mesh's bucketed copy after the previous mesh's.
-// Bucket edge: 32 voxels (16^3 leaf parents).  Smaller buckets bound the leaf stage's span per bucket
-// but multiply its per-bucket cost (measured on the 2^10 room scene: 16-voxel buckets took 2.5x longer).
-uint32_t bucket_shift(uint32_t level) { return std::min<uint32_t>(level, 5u); }
+// Bucket edge: 16 voxels while the leaf parents are dense (level <= 10): a bucket then spans at most one
+// leaf window's worth of leaf words (8^3 parents x 8), which the windowed leaf stage relies on; 32 voxels
+// for deeper octrees, where 16-voxel buckets would need 8^8 bucket counters at level 12.
+uint32_t bucket_shift(uint32_t level) { return std::min<uint32_t>(level, level <= kDenseMaxDepth + 1 ? 4u : 5u); }
+
+// Leaf windows a dense-parent mesh can need: its leaf range is at most 8 words per possible parent.
+uint64_t leaf_window_bound(uint32_t count, uint32_t level) {
+	if (level > kDenseMaxDepth + 1) return 0;
+	const uint64_t parents = level == 1 ? 1ull : std::min<uint64_t>(1ull << (3 * (level - 1)), std::max<uint32_t>(count, 1u));
+	return (8ull * parents + 4095) / 4096;
+}
 
 SVO_DEV uint32_t bucket_of(uint32_t x, uint32_t y, uint32_t z, uint32_t bshift) { return morton(x, y, z, bshift); }
 
@@ -596,7 +606,7 @@ __global__ void __launch_bounds__(kTPB) bucket_scatter(const uint64_t *__restric
 			if (at < send) // always true after a complete bucket scan (a timed-out scan is reported)
 				sorted[at] = out;
 			else
-				SVO_CHECK(false, 4u, bb.gstate);
+				SVO_CHECK_FAIL(4u, bb.gstate);
 		}
 	}
 }
@@ -631,42 +641,222 @@ SVO_DEV uint32_t leaf_slot(uint64_t frag, uint64_t f, const uint32_t *__restrict
 constexpr uint32_t kLeafSlots = 4096;         // packed accumulators in shared memory (8 B each)
 constexpr uint32_t kWideSlots = kLeafSlots / 4; // exact accumulators (4 x 8 B each) of the overflow path
 
-// Extent of every non-empty bucket, in list order: first and last item, first and last leaf slot
-// (lo = 0xffffffff, hi = 0 when the leaf stage reduces the span over the bucket's fragments), and for
-// a batch the bucket's mesh.
-//   one bucket (level <= 5): the whole leaf range;
-//   dense parents: bucket b is 8^(bshift-1) parent cells (128 words of the depth level-1 bitmap), and the
-//     prefix entries at its first word and at the next bucket's give its first and last leaf block.
-// Also writes every mesh's range (its leaf range is final once the interior levels are built).
+// Leaf windows.  A mesh whose leaf parents are dense (level <= 10) has its leaf stage cut into windows of
+// kLeafSlots words of its leaf range; window k is built by one block from the buckets whose leaf spans
+// meet it.  Consecutive non-empty buckets of a mesh have adjacent spans (breadth-first order is Morton
+// order), so those buckets are one run of the bucket list and their items one range of the bucketed
+// copy; a 16^3-voxel bucket spans at most 512 parents = kLeafSlots words, so it meets at most two
+// windows and every item is read at most twice.
+constexpr uint32_t kWinBits = 12;
+static_assert((1u << kWinBits) == kLeafSlots, "a leaf window is one shared-memory accumulator window");
+
+SVO_DEV bool dense_parents(const BuildMesh &md) { return md.level == 1 || md.level - 1 <= md.dv.D; }
+
+// Leaf words [first, last] of local bucket bl of a dense-parent mesh: the prefix entries at its first
+// parent-bitmap word and at the next bucket's give its first and last leaf block.
+SVO_DEV uint2 bucket_span(const BuildMesh &md, uint32_t bl, uint32_t leaf_begin, uint32_t leaf_num) {
+	if (md.nb == 1) return make_uint2(0u, leaf_num - 1u);
+	const uint32_t *pprefix = md.dv.prefix + md.parent_off;
+	const uint32_t before = leaf_begin / 8u - 1u;              // occupied cells of depths below the parents
+	const uint32_t wpb = (1u << (3 * (md.bshift - 1))) >> 5;  // parent-bitmap words per bucket
+	return make_uint2(8u * (__ldg(pprefix + wpb * bl) - before), 8u * (__ldg(pprefix + wpb * (bl + 1)) - before) - 1u);
+}
+
+// Exclusive prefix of the meshes' window counts (one block); win_base[M] = windows of the batch.
+template <bool B> __global__ void __launch_bounds__(kTPB) leaf_window_scan(BuildBatch bb, uint32_t *__restrict__ win_base) {
+	__shared__ uint32_t s_warp[kTPB / 32 + 1];
+	uint32_t carry = 0;
+	const uint32_t M = batch_size<B>(bb);
+	for (uint32_t base = 0; base < M; base += kTPB) {
+		const uint32_t mi = base + threadIdx.x;
+		uint32_t c = 0;
+		if (mi < M) {
+			const BuildMesh md = mesh_at<B>(bb, mi);
+			if (dense_parents(md)) c = (md.state->lv[md.level].num + kLeafSlots - 1) >> kWinBits;
+		}
+		uint32_t total;
+		const uint32_t excl = block_exclusive_sum<uint32_t, kTPB>(c, s_warp, total);
+		if (mi < M) win_base[mi] = carry + excl;
+		carry += total;
+	}
+	if (threadIdx.x == 0) win_base[M] = carry;
+}
+
+// Extent of every non-empty bucket, in list order: first and last item, first and last leaf word
+// (lo = 0xffffffff, hi = 0 for meshes with sparse leaf parents, whose leaf stage reduces the span over
+// the bucket's fragments), and for a batch the bucket's mesh.  For dense-parent meshes, the first and
+// last bucket of every leaf window.  Also writes every mesh's range (final once the interior levels
+// are built).
 template <bool B>
 __global__ void bucket_meta(BuildBatch bb, const uint32_t *__restrict__ boff, const uint32_t *__restrict__ blist,
-                            const BuildState *gstate, uint4 *__restrict__ meta, uint32_t *__restrict__ bmesh) {
+                            const BuildState *gstate, uint4 *__restrict__ meta, uint32_t *__restrict__ bmesh,
+                            const uint32_t *__restrict__ win_base, uint32_t *__restrict__ wfirst,
+                            uint32_t *__restrict__ wlast) {
 	const uint32_t nbuckets = gstate->buckets;
 	for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nbuckets; t += gridDim.x * blockDim.x) {
 		const uint32_t b = blist[t];
 		const uint32_t mi = B ? mesh_search(bb.bucket_base, bb.M, b) : 0u;
 		const BuildMesh md = mesh_at<B>(bb, mi);
 		const uint32_t level = md.level, bl = b - md.bucket_base;
-		const bool items = level == 1 || level - 1 <= md.dv.D;
 		const uint32_t leaf_begin = md.state->lv[level].begin, leaf_num = md.state->lv[level].num;
 		uint4 m = make_uint4(boff[b] + md.sorted_pad, boff[b + 1] + md.sorted_pad, 0xffffffffu, 0u);
-		if (md.nb == 1) {
-			m.z = 0, m.w = leaf_num - 1;
-		} else if (items && level > 1) {
-			const uint32_t *pprefix = md.dv.prefix + md.dv.off[level - 1];
-			const uint32_t before = leaf_begin / 8u - 1u; // occupied cells of depths below the parents
-			const uint32_t wpb = (1u << (3 * (md.bshift - 1))) >> 5; // parent-bitmap words per bucket
-			m.z = 8u * (pprefix[wpb * bl] - before);
-			m.w = 8u * (pprefix[wpb * (bl + 1)] - before) - 1u;
+		if (dense_parents(md)) {
+			const uint2 sp = bucket_span(md, bl, leaf_begin, leaf_num);
+			m.z = sp.x, m.w = sp.y;
+			if (SVO_CHECK(sp.y < leaf_num && sp.x <= sp.y, 6u, bb.gstate)) {
+				// first / last bucket of each window this bucket meets (at most two)
+				const bool prev_in = t > 0 && blist[t - 1] >= md.bucket_base;
+				const bool next_in = t + 1 < nbuckets && blist[t + 1] < md.bucket_base + md.nb;
+				const uint32_t prev_end = prev_in ? bucket_span(md, blist[t - 1] - md.bucket_base, leaf_begin, leaf_num).y : 0u;
+				const uint32_t next_start =
+				    next_in ? bucket_span(md, blist[t + 1] - md.bucket_base, leaf_begin, leaf_num).x : 0u;
+				const uint32_t wb = win_base[mi];
+				for (uint32_t k = sp.x >> kWinBits; k <= (sp.y >> kWinBits); ++k) {
+					if (!prev_in || (prev_end >> kWinBits) < k) wfirst[wb + k] = t;
+					if (!next_in || (next_start >> kWinBits) > k) wlast[wb + k] = t;
+				}
+			} else {
+				m.y = m.x;
+			}
 		}
 		if (!SVO_CHECK(m.y <= bb.sorted_total && m.x <= m.y, 5u, bb.gstate)) m.y = m.x;
-		if (m.z <= m.w && !SVO_CHECK(m.w < leaf_num, 6u, bb.gstate)) m.y = m.x;
 		meta[t] = m;
 		if (B) bmesh[t] = mi;
 	}
 	for (uint32_t mi = blockIdx.x * blockDim.x + threadIdx.x; mi < batch_size<B>(bb); mi += gridDim.x * blockDim.x) {
 		const BuildMesh md = mesh_at<B>(bb, mi);
 		md.state->range_words = md.state->lv[md.level].begin + md.state->lv[md.level].num;
+	}
+}
+
+// Packed-accumulator window of the leaf stage, shared by both leaf kernels: adds items f0..f1 of the
+// bucketed copy whose slot (relative to the window start w0) is below wn, then writes the window's wn
+// leaf words to dst (empty slots as 0) and returns the block's count of non-empty words.  An
+// accumulator is two 32-bit words, (r | g << 16) and (b | n << 16): a field can carry only when a voxel
+// has more than 257 fragments (257 x 255 = 65535), so an add that sees a count of 257 or more marks the
+// window, which is then redone exactly with 64-bit r, g, b and n sums, kWideSlots slots at a time.
+// SLOT(item, f) gives an item's slot relative to the leaf range and RGB(item) its colour.
+template <typename SlotFn, typename RgbFn>
+SVO_DEV uint32_t leaf_window(const uint64_t *__restrict__ sorted, uint32_t f0, uint32_t f1, uint32_t w0, uint32_t wn,
+                             uint32_t *dst, unsigned long long *s_acc, uint32_t *s_over, SlotFn SLOT, RgbFn RGB) {
+	uint32_t *s_acc32 = reinterpret_cast<uint32_t *>(s_acc);
+	for (uint32_t i = threadIdx.x; i < wn; i += kTPB) s_acc[i] = 0ull;
+	if (threadIdx.x == 0) *s_over = 0;
+	__syncthreads();
+	bool over = false;
+	for (uint32_t fb = f0 + threadIdx.x; fb < f1; fb += 4 * kTPB) {
+		uint64_t fr[4];
+		uint32_t sl[4], rgb[4];
+#pragma unroll
+		for (int k = 0; k < 4; ++k) fr[k] = fb + k * kTPB < f1 ? __ldcs(sorted + fb + k * kTPB) : 0ull;
+#pragma unroll
+		for (int k = 0; k < 4; ++k) {
+			sl[k] = fb + k * kTPB < f1 ? SLOT(fr[k], fb + k * kTPB) - w0 : 0xffffffffu;
+			rgb[k] = RGB(fr[k]);
+		}
+#pragma unroll
+		for (int k = 0; k < 4; ++k)
+			if (sl[k] < wn) {
+				atomicAdd(s_acc32 + 2 * sl[k], (rgb[k] & 0xffu) | (((rgb[k] >> 8) & 0xffu) << 16));
+				over |= (atomicAdd(s_acc32 + 2 * sl[k] + 1, ((rgb[k] >> 16) & 0xffu) | (1u << 16)) >> 16) >= 257u;
+			}
+	}
+	if (__any_sync(kFullMask, over) && lane_id() == 0) *s_over = 1;
+	__syncthreads();
+	uint32_t leaves = 0;
+	if (!*s_over) {
+		for (uint32_t i = 4 * threadIdx.x; i < wn; i += 4 * kTPB) {
+			const uint4 a = *reinterpret_cast<const uint4 *>(s_acc32 + 2 * i);
+			const uint4 c = *reinterpret_cast<const uint4 *>(s_acc32 + 2 * i + 4);
+			const uint32_t rg[4] = {a.x, a.z, c.x, c.z}, bn[4] = {a.y, a.w, c.y, c.w};
+			uint32_t word[4];
+#pragma unroll
+			for (int j = 0; j < 4; ++j) {
+				const uint32_t n = bn[j] >> 16;
+				word[j] = n ? leaf_word(n, rg[j] & 0xffffu, rg[j] >> 16, bn[j] & 0xffffu) : 0u;
+				leaves += word[j] != 0u;
+			}
+			*reinterpret_cast<uint4 *>(dst + i) = make_uint4(word[0], word[1], word[2], word[3]);
+		}
+	} else {
+		unsigned long long *acc4 = s_acc;
+		for (uint32_t v0 = 0; v0 < wn; v0 += kWideSlots) {
+			const uint32_t vn = min(kWideSlots, wn - v0);
+			__syncthreads();
+			for (uint32_t i = threadIdx.x; i < 4 * vn; i += kTPB) acc4[i] = 0ull;
+			__syncthreads();
+			for (uint32_t f = f0 + threadIdx.x; f < f1; f += kTPB) {
+				const uint64_t item = sorted[f];
+				const uint32_t sl = SLOT(item, f) - w0 - v0;
+				const uint32_t c = RGB(item);
+				if (sl < vn) {
+					atomicAdd(acc4 + 4 * sl, (unsigned long long)(c & 0xffu));
+					atomicAdd(acc4 + 4 * sl + 1, (unsigned long long)((c >> 8) & 0xffu));
+					atomicAdd(acc4 + 4 * sl + 2, (unsigned long long)((c >> 16) & 0xffu));
+					atomicAdd(acc4 + 4 * sl + 3, 1ull);
+				}
+			}
+			__syncthreads();
+			for (uint32_t i = threadIdx.x; i < vn; i += kTPB) {
+				const unsigned long long n = acc4[4 * i + 3]; // < 2^32 (fragment counts are 32-bit)
+				const uint32_t word = n ? leaf_word_wide((uint32_t)n, acc4[4 * i], acc4[4 * i + 1], acc4[4 * i + 2]) : 0u;
+				dst[v0 + i] = word;
+				leaves += word != 0u;
+			}
+		}
+	}
+	__syncthreads(); // the accumulators are reused by the next window
+	return leaves;
+}
+
+// Leaf stage of dense-parent meshes: one leaf window per block at a time, windows of all meshes taken
+// grid-stride.  The bucketed copy holds (slot << 32 | rgb) items.
+template <bool B>
+__global__ void __launch_bounds__(kTPB) build_leaf_windows(const uint64_t *__restrict__ sorted, BuildBatch bb,
+                                                           const uint4 *__restrict__ meta,
+                                                           const uint32_t *__restrict__ win_base,
+                                                           const uint32_t *__restrict__ wfirst,
+                                                           const uint32_t *__restrict__ wlast, BuildState *gstate) {
+	extern __shared__ unsigned long long s_acc[];
+	__shared__ uint32_t s_over, s_leaves, s_skip;
+	const uint32_t M = batch_size<B>(bb);
+	const uint32_t total = win_base[M], nbuckets = gstate->buckets;
+	for (uint32_t gw = blockIdx.x; gw < total; gw += gridDim.x) {
+		const uint32_t mi = B ? mesh_search(win_base, M, gw) : 0u;
+		const BuildMesh md = mesh_at<B>(bb, mi);
+		const uint32_t level = md.level;
+		const uint32_t leaf_begin = md.state->lv[level].begin, leaf_num = md.state->lv[level].num;
+		const uint32_t w0 = (gw - win_base[mi]) << kWinBits;
+		const uint32_t t0 = wfirst[gw], t1 = wlast[gw];
+		if (threadIdx.x == 0) {
+			const uint64_t leaf_end = (uint64_t)leaf_begin + leaf_num;
+			uint32_t skip = (md.state->status & kStatusCapacity) | (gstate->status & kStatusAbort);
+			if (!skip && (leaf_end > md.capacity || leaf_end > SVO_MAX_POOL_WORDS)) { // leaf blocks: checked here
+				atomicOr(&md.state->status, kStatusCapacity);
+				skip = 1;
+			}
+			if (!skip && !(t0 <= t1 && t1 < nbuckets)) { // only after a reported scan failure
+				SVO_CHECK_FAIL(8u, gstate);
+				skip = 1;
+			}
+			s_skip = skip;
+			s_leaves = 0;
+		}
+		__syncthreads();
+		if (s_skip) {
+			__syncthreads();
+			continue;
+		}
+		const uint32_t f0 = meta[t0].x, f1 = meta[t1].y;
+		const uint32_t wn = min(kLeafSlots, leaf_num - w0);
+		const uint32_t leaves = leaf_window(
+		    sorted, f0, f1, w0, wn, md.pool + leaf_begin + w0, s_acc, &s_over,
+		    [](uint64_t item, uint32_t) { return (uint32_t)(item >> 32); }, [](uint64_t item) { return (uint32_t)item; });
+		const uint32_t wl = warp_sum(leaves);
+		if (lane_id() == 0 && wl) atomicAdd(&s_leaves, wl);
+		__syncthreads();
+		if (threadIdx.x == 0 && s_leaves) atomicAdd(&md.state->leaves, s_leaves);
+		__syncthreads();
 	}
 }
 
@@ -684,7 +874,6 @@ __global__ void __launch_bounds__(kTPB) build_leaf(const uint64_t *__restrict__ 
                                                    const uint32_t *__restrict__ cache, const uint4 *__restrict__ meta,
                                                    const uint32_t *__restrict__ bmesh, BuildState *gstate) {
 	extern __shared__ unsigned long long s_acc[];
-	uint32_t *s_acc32 = reinterpret_cast<uint32_t *>(s_acc);
 	__shared__ uint32_t s_lo, s_hi, s_over, s_leaves, s_skip;
 	const uint32_t nbuckets = gstate->buckets;
 	uint4 next = blockIdx.x < nbuckets ? meta[blockIdx.x] : make_uint4(0, 0, 0, 0);
@@ -692,6 +881,7 @@ __global__ void __launch_bounds__(kTPB) build_leaf(const uint64_t *__restrict__ 
 		const uint4 m = next;
 		if (t + gridDim.x < nbuckets) next = meta[t + gridDim.x];
 		const BuildMesh md = mesh_at<B>(bb, B ? bmesh[t] : 0u);
+		if (dense_parents(md)) continue; // block-uniform: built by build_leaf_windows
 		const uint32_t level = md.level;
 		const uint32_t leaf_begin = md.state->lv[level].begin;
 		if (threadIdx.x == 0) {
@@ -709,7 +899,6 @@ __global__ void __launch_bounds__(kTPB) build_leaf(const uint64_t *__restrict__ 
 			__syncthreads();
 			continue;
 		}
-		const bool items = level == 1 || level - 1 <= md.dv.D;
 		const uint32_t *pool_c = md.pool;
 		const uint32_t f0 = m.x, f1 = m.y;
 		uint32_t span_lo = m.z & ~7u, span_hi = (m.w | 7u) + 1u;
@@ -734,84 +923,17 @@ __global__ void __launch_bounds__(kTPB) build_leaf(const uint64_t *__restrict__ 
 			span_lo = s_lo & ~7u, span_hi = (s_hi | 7u) + 1u;
 		}
 		if (span_hi > md.state->lv[level].num) { // only after a reported scan failure: never leave the leaf range
-			SVO_CHECK(false, 7u, gstate);
+			SVO_CHECK_FAIL(7u, gstate);
 			span_hi = span_lo;
 		}
 		for (uint32_t w0 = span_lo; w0 < span_hi; w0 += kLeafSlots) {
 			const uint32_t wn = min(kLeafSlots, span_hi - w0);
-			for (uint32_t i = threadIdx.x; i < wn; i += kTPB) s_acc[i] = 0ull;
-			if (threadIdx.x == 0) s_over = 0;
-			__syncthreads();
-			bool over = false;
-			for (uint32_t fb = f0 + threadIdx.x; fb < f1; fb += 4 * kTPB) {
-				uint64_t fr[4];
-				uint32_t sl[4], rgb[4];
-#pragma unroll
-				for (int k = 0; k < 4; ++k) fr[k] = fb + k * kTPB < f1 ? sorted[fb + k * kTPB] : 0ull;
-#pragma unroll
-				for (int k = 0; k < 4; ++k) {
-					const bool in = fb + k * kTPB < f1;
-					sl[k] = !in ? 0xffffffffu
-					            : (items ? (uint32_t)(fr[k] >> 32) : leaf_slot(fr[k], fb + k * kTPB, pool_c, cache, leaf_begin)) - w0;
-					rgb[k] = items ? (uint32_t)fr[k] : (uint32_t)(fr[k] >> 32);
-				}
-#pragma unroll
-				for (int k = 0; k < 4; ++k)
-					if (sl[k] < wn) {
-						atomicAdd(s_acc32 + 2 * sl[k], (rgb[k] & 0xffu) | (((rgb[k] >> 8) & 0xffu) << 16));
-						over |= (atomicAdd(s_acc32 + 2 * sl[k] + 1, ((rgb[k] >> 16) & 0xffu) | (1u << 16)) >> 16) >= 257u;
-					}
-			}
-			if (__any_sync(kFullMask, over) && lane_id() == 0) s_over = 1;
-			__syncthreads();
-			uint32_t leaves = 0;
-			uint32_t *dst = md.pool + leaf_begin + w0;
-			if (!s_over) {
-				for (uint32_t i = 4 * threadIdx.x; i < wn; i += 4 * kTPB) {
-					const uint4 a = *reinterpret_cast<const uint4 *>(s_acc32 + 2 * i);
-					const uint4 c = *reinterpret_cast<const uint4 *>(s_acc32 + 2 * i + 4);
-					const uint32_t rg[4] = {a.x, a.z, c.x, c.z}, bn[4] = {a.y, a.w, c.y, c.w};
-					uint32_t word[4];
-#pragma unroll
-					for (int j = 0; j < 4; ++j) {
-						const uint32_t n = bn[j] >> 16;
-						word[j] = n ? leaf_word(n, rg[j] & 0xffffu, rg[j] >> 16, bn[j] & 0xffffu) : 0u;
-						leaves += word[j] != 0u;
-					}
-					*reinterpret_cast<uint4 *>(dst + i) = make_uint4(word[0], word[1], word[2], word[3]);
-				}
-			} else {
-				// exact sums for this window, kWideSlots slots at a time
-				unsigned long long *acc4 = s_acc;
-				for (uint32_t v0 = 0; v0 < wn; v0 += kWideSlots) {
-					const uint32_t vn = min(kWideSlots, wn - v0);
-					__syncthreads();
-					for (uint32_t i = threadIdx.x; i < 4 * vn; i += kTPB) acc4[i] = 0ull;
-					__syncthreads();
-					for (uint32_t f = f0 + threadIdx.x; f < f1; f += kTPB) {
-						const uint64_t item = sorted[f];
-						const uint32_t sl =
-						    (items ? (uint32_t)(item >> 32) : leaf_slot(item, f, pool_c, cache, leaf_begin)) - w0 - v0;
-						const uint32_t c = items ? (uint32_t)item : (uint32_t)(item >> 32);
-						if (sl < vn) {
-							atomicAdd(acc4 + 4 * sl, (unsigned long long)(c & 0xffu));
-							atomicAdd(acc4 + 4 * sl + 1, (unsigned long long)((c >> 8) & 0xffu));
-							atomicAdd(acc4 + 4 * sl + 2, (unsigned long long)((c >> 16) & 0xffu));
-							atomicAdd(acc4 + 4 * sl + 3, 1ull);
-						}
-					}
-					__syncthreads();
-					for (uint32_t i = threadIdx.x; i < vn; i += kTPB) {
-						const unsigned long long n = acc4[4 * i + 3];
-						// n < 2^32 (fragment counts are 32-bit)
-						const uint32_t word = n ? leaf_word_wide((uint32_t)n, acc4[4 * i], acc4[4 * i + 1], acc4[4 * i + 2]) : 0u;
-						dst[v0 + i] = word;
-						leaves += word != 0u;
-					}
-				}
-			}
-			leaves = warp_sum(leaves);
-			if (lane_id() == 0 && leaves) atomicAdd(&s_leaves, leaves);
+			const uint32_t leaves = leaf_window(
+			    sorted, f0, f1, w0, wn, md.pool + leaf_begin + w0, s_acc, &s_over,
+			    [&](uint64_t item, uint32_t f) { return leaf_slot(item, f, pool_c, cache, leaf_begin); },
+			    [](uint64_t item) { return (uint32_t)(item >> 32); });
+			const uint32_t wl = warp_sum(leaves);
+			if (lane_id() == 0 && wl) atomicAdd(&s_leaves, wl);
 			__syncthreads();
 		}
 		if (threadIdx.x == 0 && s_leaves) atomicAdd(&md.state->leaves, s_leaves);
@@ -925,6 +1047,10 @@ void build_workspace_layout(void *ws, uint32_t count, uint32_t level, uint64_t c
 	w.bmeta = (uint4 *)take((size_t)w.nb * 16);
 	w.bdesc_count = 2 * ((size_t)(w.nb + kScanTile - 1) / kScanTile + 1);
 	w.bdescs = (unsigned long long *)take(w.bdesc_count * sizeof(unsigned long long));
+	w.win_base = (uint32_t *)take(2 * 4);
+	const uint64_t wins = leaf_window_bound(count, level);
+	w.wfirst = (uint32_t *)take(wins * 4 + 4);
+	w.wlast = (uint32_t *)take(wins * 4 + 4);
 	w.sorted = (uint64_t *)take((size_t)count * 8 + 32);
 	w.cache = (uint32_t *)take(level > D + 1 ? (size_t)count * 4 + 16 : 16);
 	w.total_bytes = off;
@@ -1018,19 +1144,25 @@ static void launch_sparse(const uint64_t *sorted, uint32_t count, uint32_t level
 
 template <bool B>
 static void launch_leaf_stage(const BuildBatch &bb, uint32_t M, uint32_t tune_level, uint64_t n, uint32_t nb_total,
-                              const uint32_t *boff,
-                              const uint32_t *blist, const BuildState *gstate, uint4 *bmeta, uint32_t *bmesh,
-                              const uint64_t *sorted, const uint32_t *cache, cudaStream_t stream) {
+                              const uint32_t *boff, const uint32_t *blist, const BuildState *gstate, uint4 *bmeta,
+                              uint32_t *bmesh, uint32_t *win_base, uint32_t *wfirst, uint32_t *wlast, bool any_dense,
+                              bool any_sparse, const uint64_t *sorted, const uint32_t *cache, cudaStream_t stream) {
 	const int sms = device_sm_count();
 	const size_t smem = kLeafSlots * sizeof(unsigned long long); // 32 KB: below the default dynamic limit
 	const uint32_t meta_items = std::max<uint32_t>(nb_total, M);
+	const uint32_t blocks = (uint32_t)sms * (uint32_t)tune_value(kTuneLeafBlocks, tune_level, n);
+	SVO_LAUNCH("leaf_window_scan", stream, leaf_window_scan<B><<<1, kTPB, 0, stream>>>(bb, win_base););
 	SVO_LAUNCH("bucket_meta", stream,
-	           bucket_meta<B><<<grid_for(meta_items, kTPB, (uint32_t)sms * 4), kTPB, 0, stream>>>(bb, boff, blist, gstate,
-	                                                                                         bmeta, bmesh););
-	SVO_LAUNCH("build_leaf", stream,
-	           build_leaf<B><<<(uint32_t)sms * (uint32_t)tune_value(kTuneLeafBlocks, tune_level, n), kTPB, smem, stream>>>(
-	               sorted, bb, cache, bmeta, bmesh,
-	                                                                     const_cast<BuildState *>(gstate)););
+	           bucket_meta<B><<<grid_for(meta_items, kTPB, (uint32_t)sms * 4), kTPB, 0, stream>>>(
+	               bb, boff, blist, gstate, bmeta, bmesh, win_base, wfirst, wlast););
+	if (any_dense)
+		SVO_LAUNCH("build_leaf_windows", stream,
+		           build_leaf_windows<B><<<blocks, kTPB, smem, stream>>>(sorted, bb, bmeta, win_base, wfirst, wlast,
+		                                                                 const_cast<BuildState *>(gstate)););
+	if (any_sparse)
+		SVO_LAUNCH("build_leaf", stream,
+		           build_leaf<B><<<blocks, kTPB, smem, stream>>>(sorted, bb, cache, bmeta, bmesh,
+		                                                          const_cast<BuildState *>(gstate)););
 }
 
 cudaError_t build_launch_interior(const uint64_t *frags, uint32_t count, uint32_t level, uint32_t *pool,
@@ -1053,8 +1185,9 @@ cudaError_t build_launch_interior(const uint64_t *frags, uint32_t count, uint32_
 cudaError_t build_launch_leaf(uint32_t count, uint32_t level, uint32_t *pool, uint64_t capacity,
                               const BuildWorkspace &w, cudaStream_t stream) {
 	const BuildBatch bb = single_batch(w, count, level, pool, capacity);
-	launch_leaf_stage<false>(bb, 1, level, count, w.nb, w.boff, w.blist, w.state, w.bmeta, nullptr, w.sorted, w.cache,
-	                         stream);
+	const bool dense = level <= w.dv.D + 1;
+	launch_leaf_stage<false>(bb, 1, level, count, w.nb, w.boff, w.blist, w.state, w.bmeta, nullptr, w.win_base, w.wfirst,
+	                         w.wlast, dense, !dense, w.sorted, w.cache, stream);
 	return cudaGetLastError();
 }
 
@@ -1089,7 +1222,7 @@ cudaError_t build_launch_batch(const uint64_t *frags, const BuildBatchPlan &p, v
 		              p.gstate, stream);
 	}
 	launch_leaf_stage<true>(p.bb, p.M, p.max_level, p.frags_total, p.nb_total, p.boff, p.blist, p.gstate, p.bmeta,
-	                        p.bmesh, p.sorted, p.cache, stream);
+	                        p.bmesh, p.win_base, p.wfirst, p.wlast, p.any_dense, p.any_sparse, p.sorted, p.cache, stream);
 	SVO_LAUNCH("build_export", stream,
 	           build_export<true><<<(p.M + 127) / 128, 128, 0, stream>>>(p.bb, p.gstate, (uint32_t *)result_dev););
 	return cudaGetLastError();

@@ -187,6 +187,8 @@ struct BuildWorkspace {
 	uint4 *bmeta;                   // [nb] per listed bucket: first/last item, first/last leaf slot
 	unsigned long long *bdescs;     // look-back descriptors of the bucket scan (2 scans)
 	size_t bdesc_count;
+	uint32_t *win_base;             // [2] leaf windows before / after the mesh (leaf_window_scan)
+	uint32_t *wfirst, *wlast;       // [leaf_window_bound] first and last listed bucket of each leaf window
 	uint64_t *sorted;               // [count] the fragments, bucketed
 	uint32_t *cache;                // [count] node index of the previous sparse depth, per sorted fragment
 	size_t total_bytes;
@@ -194,6 +196,7 @@ struct BuildWorkspace {
 uint64_t build_pool_bound(uint32_t count, uint32_t level);
 uint32_t dense_depth(uint32_t level);
 uint32_t bucket_shift(uint32_t level); // bucket edge of the build's fragment buckets: 2^shift voxels
+uint64_t leaf_window_bound(uint32_t count, uint32_t level); // leaf windows a dense-parent mesh can need
 uint32_t dense_words_of(uint32_t d);
 // Words of the dense bitmaps of depths 1..dense_depth(level) (32-byte aligned levels) and their offsets.
 uint32_t dense_layout(uint32_t level, uint32_t off[kDenseMaxDepth + 2]);
@@ -233,6 +236,9 @@ struct BuildBatchPlan {
 	uint32_t *dense_prefix;
 	uint64_t *sorted;
 	uint32_t *cache;                // only when a mesh has sparse levels (level > 10)
+	uint32_t *win_base;             // [M+1] leaf windows before each mesh (leaf_window_scan)
+	uint32_t *wfirst, *wlast;       // [sum of leaf_window_bound] first and last listed bucket per window
+	bool any_dense, any_sparse;     // meshes whose leaf parents are dense / sparse
 };
 cudaError_t build_launch_batch(const uint64_t *frags, const BuildBatchPlan &p, void *result_dev, cudaStream_t stream);
 
