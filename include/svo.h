@@ -314,6 +314,27 @@ int svo_raycast(const svo_octree *o, const svo_ray *rays, uint32_t n, svo_hit *h
 int svo_raycast_camera(const svo_octree *o, const svo_camera *cam, uint32_t width, uint32_t height, svo_hit *hits,
                        uint64_t *fetches_dev, void *stream);
 
+/* Beam optimisation of the tracer (OctreeTracer::CmdBeamRenderPass, src/OctreeTracer.cpp:183-211, with
+ * shader/octree_tracer_beam.frag and Octree_RayMarchCoarse, shader/octree.glsl:47-177): one start distance
+ * per corner of each SVO_BEAM_SIZE x SVO_BEAM_SIZE pixel tile, written to `beam` (device floats,
+ * svo_beam_texels(width, height) of them, row-major with (width + 7) / 8 + 1 per row); 1e10 where the
+ * tile's cone misses the octree. */
+#define SVO_BEAM_SIZE 8u /* kBeamSize (src/Config.hpp:22) */
+uint64_t svo_beam_texels(uint32_t width, uint32_t height);
+int svo_beam_prepass(const svo_octree *o, const svo_camera *cam, uint32_t width, uint32_t height, float *beam,
+                     void *stream);
+
+/* svo_raycast_camera with the beam enabled (shader/octree_tracer.frag:27-33): each primary ray starts at
+ * o + d * (the least of the 4 beam texels at the corners of its tile), then Octree_RayMarchLeaf.  `beam`
+ * (device) from svo_beam_prepass for the same octree, camera and size, or NULL to run the pre-pass here
+ * (on stream-ordered scratch).  hit.t counts from the advanced origin. */
+int svo_raycast_camera_beam(const svo_octree *o, const svo_camera *cam, uint32_t width, uint32_t height,
+                            const float *beam, svo_hit *hits, uint64_t *fetches_dev, void *stream);
+
+/* Octree_RayMarchOcclude (shader/octree.glsl:504-629), the shadow-ray march of the path tracer:
+ * occluded[i] (device uint32) = 1 when ray i hits a leaf, else 0.  A ray with d = 0 is not occluded. */
+int svo_occlude(const svo_octree *o, const svo_ray *rays, uint32_t n, uint32_t *occluded, void *stream);
+
 /* Secondary rays for hits: o = hit pos, d = cosine-weighted direction about the hit normal
  * (shader/diffuse.glsl:7-14, shader/util.glsl:5-9, shader/path_tracer.comp:44-47) with (u1,u2) from a
  * counter hash of (seed, ray index).  Misses produce a ray with d = 0 that svo_raycast reports as a miss

@@ -60,6 +60,9 @@ def lib():
         L.oracle_canonicalize.restype = i32
         L.oracle_raycast.argtypes = [P, u64, u32, P, u64, P, P]
         L.oracle_camera_rays.argtypes = [P, u32, u32, P]
+        L.oracle_occlude.argtypes = [P, u64, u32, P, u64, P]
+        L.oracle_beam.argtypes = [P, u64, u32, P, u32, u32, u32, P]
+        L.oracle_camera_rays_beam.argtypes = [P, u32, u32, P, u32, P]
         L.oracle_bounce_rays.argtypes = [P, u64, u64, P]
         L.oracle_diffuse_sample.argtypes = [P, ctypes.c_float, ctypes.c_float, P]
         _lib = L
@@ -148,6 +151,37 @@ def camera_rays(cam: np.ndarray, width: int, height: int) -> np.ndarray:
     cam = np.ascontiguousarray(np.asarray(cam, CAMERA_DTYPE).reshape(1))
     rays = np.zeros(width * height, RAY_DTYPE)
     lib().oracle_camera_rays(_ptr(cam), width, height, _ptr(rays))
+    return rays
+
+
+def occlude(pool: np.ndarray, level: int, rays: np.ndarray) -> np.ndarray:
+    """Octree_RayMarchOcclude per ray (1 = the ray hits a leaf)."""
+    pool = np.ascontiguousarray(pool, np.uint32)
+    rays = np.ascontiguousarray(rays, RAY_DTYPE)
+    out = np.zeros(len(rays), np.uint32)
+    lib().oracle_occlude(_ptr(pool), len(pool), level, _ptr(rays), len(rays), _ptr(out))
+    return out
+
+
+BEAM_SIZE = 8  # kBeamSize: pixels per beam tile edge
+
+
+def beam(pool: np.ndarray, level: int, cam: np.ndarray, width: int, height: int, beam_size: int = BEAM_SIZE):
+    """Beam pre-pass: start distance per tile corner, shape ((H+bs-1)//bs+1, (W+bs-1)//bs+1)."""
+    pool = np.ascontiguousarray(pool, np.uint32)
+    cam = np.ascontiguousarray(np.asarray(cam, CAMERA_DTYPE).reshape(1))
+    bw, bh = (width + beam_size - 1) // beam_size + 1, (height + beam_size - 1) // beam_size + 1
+    out = np.zeros((bh, bw), np.float32)
+    lib().oracle_beam(_ptr(pool), len(pool), level, _ptr(cam), width, height, beam_size, _ptr(out))
+    return out
+
+
+def camera_rays_beam(cam: np.ndarray, width: int, height: int, beam_img: np.ndarray, beam_size: int = BEAM_SIZE):
+    """Primary rays advanced by the beam image (o += d * min of the 4 texels around the pixel's tile)."""
+    cam = np.ascontiguousarray(np.asarray(cam, CAMERA_DTYPE).reshape(1))
+    rays = np.zeros(width * height, RAY_DTYPE)
+    lib().oracle_camera_rays_beam(_ptr(cam), width, height, _ptr(np.ascontiguousarray(beam_img, np.float32)),
+                                  beam_size, _ptr(rays))
     return rays
 
 

@@ -737,6 +737,227 @@ void oracle_camera_rays(const svo_camera *cam, uint32_t width, uint32_t height, 
 		}
 }
 
+/* ====================================================================== occlusion and beam */
+
+/* The traversal of Octree_RayMarchOcclude (shader/octree.glsl:504-629; coarse = 0) and of
+ * Octree_RayMarchCoarse (shader/octree.glsl:47-177; coarse = 1).  They differ from the leaf march only in
+ * the direction clamp (occlude keeps |d| >= EPS, coarse keeps |d| > EPS, :505-507 and :48-50) and, for
+ * coarse, a stop at the first non-empty node at least as large as the cone footprint
+ * orig_sz + t * dir_sz (:96-97).  Returns 1 on a hit with *t_out = t_min and *size_out = the node size.
+ * The engine's guards end a ray on a malformed pool as a miss. */
+static int march_traverse(const uint32_t *pool, uint64_t range, uint32_t level, const float *o, const float *din,
+                          int coarse, float orig_sz, float dir_sz, float *t_out, float *size_out) {
+	float d[3];
+	for (int k = 0; k < 3; ++k)
+		d[k] = (coarse ? fabsf(din[k]) > MARCH_EPS : fabsf(din[k]) >= MARCH_EPS) ? din[k]
+		                                                                     : (din[k] >= 0.0f ? MARCH_EPS : -MARCH_EPS);
+	uint32_t stack[SVO_STACK_SIZE] = {0};
+	float coef[3], bias[3];
+	for (int k = 0; k < 3; ++k) {
+		coef[k] = 1.0f / -fabsf(d[k]);
+		bias[k] = coef[k] * o[k];
+	}
+	uint32_t oct_mask = 0;
+	for (int k = 0; k < 3; ++k)
+		if (d[k] > 0.0f) {
+			oct_mask ^= 1u << k;
+			bias[k] = 3.0f * coef[k] - bias[k];
+		}
+	float t_min = fmax_glsl(fmax_glsl(2.0f * coef[0] - bias[0], 2.0f * coef[1] - bias[1]), 2.0f * coef[2] - bias[2]);
+	float t_max = fmin_glsl(fmin_glsl(coef[0] - bias[0], coef[1] - bias[1]), coef[2] - bias[2]);
+	t_min = fmax_glsl(t_min, 0.0f);
+	float h = t_max;
+	uint32_t parent = 0, cur = 0, idx = 0;
+	float pos[3] = {1.0f, 1.0f, 1.0f};
+	for (int k = 0; k < 3; ++k)
+		if (1.5f * coef[k] - bias[k] > t_min) {
+			idx ^= 1u << k;
+			pos[k] = 1.5f;
+		}
+	uint32_t scale = SVO_STACK_SIZE - 1, iter = 0;
+	float scale_exp2 = 0.5f;
+	int aborted = 0;
+	const uint32_t min_scale = SVO_STACK_SIZE - level;
+	while (scale < SVO_STACK_SIZE) {
+		if (++iter > SVO_MARCH_MAX_ITER) {
+			aborted = 1;
+			break;
+		}
+		if (cur == 0u) {
+			uint64_t w = (uint64_t)parent + (idx ^ oct_mask);
+			if (w >= range) {
+				aborted = 1;
+				break;
+			}
+			cur = pool[w];
+		}
+		float tc[3];
+		for (int k = 0; k < 3; ++k)
+			tc[k] = pos[k] * coef[k] - bias[k];
+		float tc_max = fmin_glsl(fmin_glsl(tc[0], tc[1]), tc[2]);
+		if ((cur & 0x80000000u) != 0 && t_min <= t_max) {
+			if (coarse && orig_sz + tc_max * dir_sz >= scale_exp2)
+				break;
+			float half = scale_exp2 * 0.5f;
+			float t_center[3];
+			for (int k = 0; k < 3; ++k)
+				t_center[k] = half * coef[k] + tc[k];
+			if ((cur & 0x40000000u) != 0)
+				break;
+			if (scale <= min_scale) {
+				aborted = 1;
+				break;
+			}
+			if (tc_max < h)
+				stack[scale] = parent;
+			h = tc_max;
+			parent = cur & 0x3fffffffu;
+			idx = 0;
+			--scale;
+			scale_exp2 = half;
+			for (int k = 0; k < 3; ++k)
+				if (t_center[k] > t_min) {
+					idx ^= 1u << k;
+					pos[k] += scale_exp2;
+				}
+			cur = 0;
+			continue;
+		}
+		uint32_t step_mask = 0;
+		for (int k = 0; k < 3; ++k)
+			if (tc[k] <= tc_max) {
+				step_mask ^= 1u << k;
+				pos[k] -= scale_exp2;
+			}
+		t_min = tc_max;
+		idx ^= step_mask;
+		if ((idx & step_mask) != 0) {
+			uint32_t diff = 0;
+			for (int k = 0; k < 3; ++k)
+				if (step_mask & (1u << k))
+					diff |= f2u(pos[k]) ^ f2u(pos[k] + scale_exp2);
+			scale = diff ? 31u - (uint32_t)__builtin_clz(diff) : 0xffffffffu;
+			if (scale >= SVO_STACK_SIZE)
+				break;
+			scale_exp2 = u2f((scale - SVO_STACK_SIZE + 127u) << 23u);
+			parent = stack[scale];
+			uint32_t sh[3];
+			for (int k = 0; k < 3; ++k) {
+				sh[k] = f2u(pos[k]) >> scale;
+				pos[k] = u2f(sh[k] << scale);
+			}
+			idx = (sh[0] & 1u) | ((sh[1] & 1u) << 1) | ((sh[2] & 1u) << 2);
+			h = 0.0f;
+			cur = 0;
+		}
+	}
+	*t_out = t_min;
+	*size_out = scale_exp2;
+	return !aborted && scale < SVO_STACK_SIZE && t_min <= t_max;
+}
+
+typedef struct {
+	const uint32_t *pool;
+	uint64_t range;
+	uint32_t level;
+	const svo_ray *rays;
+	uint32_t *out;
+} occlude_ctx;
+
+static void occlude_range(void *p, uint64_t b, uint64_t e) {
+	occlude_ctx *c = (occlude_ctx *)p;
+	for (uint64_t r = b; r < e; ++r) {
+		const svo_ray *ray = &c->rays[r];
+		float t, sz;
+		const int none = ray->d[0] == 0.0f && ray->d[1] == 0.0f && ray->d[2] == 0.0f; /* ABI: no ray */
+		c->out[r] =
+		    none ? 0u : (uint32_t)march_traverse(c->pool, c->range, c->level, ray->o, ray->d, 0, 0.0f, 0.0f, &t, &sz);
+	}
+}
+
+void oracle_occlude(const uint32_t *pool, uint64_t range, uint32_t level, const svo_ray *rays, uint64_t n,
+                    uint32_t *occluded) {
+	occlude_ctx c = {pool, range, level, rays, occluded};
+	parallel_for(n, 256, occlude_range, &c);
+}
+
+/* Camera_GenRay of a normalised image coordinate (shader/camera.glsl:11-14). */
+static void gen_ray(const svo_camera *cam, float cx, float cy, float d[3]) {
+	cx = cx * 2.0f - 1.0f;
+	cy = cy * 2.0f - 1.0f;
+	float v[3];
+	for (int k = 0; k < 3; ++k)
+		v[k] = (cam->look[k] - cam->side[k] * cx) - cam->up[k] * cy;
+	float len = sqrtf((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]);
+	for (int k = 0; k < 3; ++k)
+		d[k] = v[k] / len;
+}
+
+/* RayTangent of shader/octree_tracer_beam.frag:17-20: tan of the angle between two unit vectors. */
+static float ray_tangent(const float x[3], const float y[3]) {
+	float c = (x[0] * y[0] + x[1] * y[1]) + x[2] * y[2];
+	return sqrtf(1.0f - c * c) / fabsf(c);
+}
+
+typedef struct {
+	const uint32_t *pool;
+	uint64_t range;
+	uint32_t level;
+	const svo_camera *cam;
+	uint32_t width, height, beam_size, bw;
+	float *beam;
+} beam_ctx;
+
+static void beam_range(void *p, uint64_t b, uint64_t e) {
+	beam_ctx *c = (beam_ctx *)p;
+	const float W = (float)c->width, H = (float)c->height, bs = (float)c->beam_size;
+	const float orig_sz = ldexpf(1.0f, 1 - (int)c->level); /* exp2f(1 - level), src/OctreeTracer.cpp:205 */
+	static const float bias[4][2] = {{0.5f, 0.5f}, {-0.5f, 0.5f}, {0.5f, -0.5f}, {-0.5f, -0.5f}};
+	for (uint64_t i = b; i < e; ++i) {
+		const uint32_t bx = (uint32_t)(i % c->bw), by = (uint32_t)(i / c->bw);
+		float d[3], tg[4];
+		gen_ray(c->cam, (float)bx / W * bs, (float)by / H * bs, d);
+		for (int k = 0; k < 4; ++k) {
+			float dk[3];
+			gen_ray(c->cam, ((float)bx + bias[k][0]) / W * bs, ((float)by + bias[k][1]) / H * bs, dk);
+			tg[k] = ray_tangent(d, dk);
+		}
+		const float dir_sz = 2.0f * fmax_glsl(fmax_glsl(tg[0], tg[1]), fmax_glsl(tg[2], tg[3]));
+		float t, sz;
+		const float o[3] = {c->cam->pos[0], c->cam->pos[1], c->cam->pos[2]};
+		c->beam[i] = march_traverse(c->pool, c->range, c->level, o, d, 1, orig_sz, dir_sz, &t, &sz)
+		                 ? fmax_glsl(0.0f, t - sz)
+		                 : 1e10f;
+	}
+}
+
+/* The beam pre-pass (shader/octree_tracer_beam.frag:22-30, src/OctreeTracer.cpp:183-211): one start
+ * distance per corner of each beam_size x beam_size pixel tile, (W + bs - 1)/bs + 1 by (H + bs - 1)/bs + 1
+ * texels (src/OctreeTracer.cpp:6), row-major. */
+void oracle_beam(const uint32_t *pool, uint64_t range, uint32_t level, const svo_camera *cam, uint32_t width,
+                 uint32_t height, uint32_t beam_size, float *beam) {
+	const uint32_t bw = (width + beam_size - 1) / beam_size + 1, bh = (height + beam_size - 1) / beam_size + 1;
+	beam_ctx c = {pool, range, level, cam, width, height, beam_size, bw, beam};
+	parallel_for((uint64_t)bw * bh, 64, beam_range, &c);
+}
+
+/* Primary rays advanced by the beam (shader/octree_tracer.frag:27-33): o += d * min of the 4 texels
+ * around the pixel's tile. */
+void oracle_camera_rays_beam(const svo_camera *cam, uint32_t width, uint32_t height, const float *beam,
+                             uint32_t beam_size, svo_ray *rays) {
+	const uint32_t bw = (width + beam_size - 1) / beam_size + 1;
+	oracle_camera_rays(cam, width, height, rays);
+	for (uint32_t y = 0; y < height; ++y)
+		for (uint32_t x = 0; x < width; ++x) {
+			const uint32_t bx = x / beam_size, by = y / beam_size;
+			const float *t0 = beam + (uint64_t)by * bw + bx, *t1 = t0 + bw;
+			const float m = fmin_glsl(fmin_glsl(t0[0], t0[1]), fmin_glsl(t1[0], t1[1]));
+			svo_ray *r = &rays[(uint64_t)y * width + x];
+			for (int k = 0; k < 3; ++k)
+				r->o[k] = r->o[k] + r->d[k] * m;
+		}
+}
+
 /* Counter hash for the bounce sample: splitmix64 finaliser of seed + golden * (index + 1). */
 static uint64_t mix64(uint64_t z) {
 	z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;

@@ -61,6 +61,14 @@ void oracle_raycast(const uint32_t *pool, uint64_t range, uint32_t level, const 
                     svo_hit *hits, uint32_t *fetches);
 /* Camera_GenRay (shader/camera.glsl:11-14) at ivec2(pixel)/size (shader/octree_tracer.frag:24). */
 void oracle_camera_rays(const svo_camera *cam, uint32_t width, uint32_t height, svo_ray *rays);
+/* Octree_RayMarchOcclude per ray: 1 when the ray hits a leaf. */
+void oracle_occlude(const uint32_t *pool, uint64_t range, uint32_t level, const svo_ray *rays, uint64_t n,
+                    uint32_t *occluded);
+/* Beam pre-pass texels and the primary rays it advances. */
+void oracle_beam(const uint32_t *pool, uint64_t range, uint32_t level, const svo_camera *cam, uint32_t width,
+                 uint32_t height, uint32_t beam_size, float *beam);
+void oracle_camera_rays_beam(const svo_camera *cam, uint32_t width, uint32_t height, const float *beam,
+                             uint32_t beam_size, svo_ray *rays);
 /* Diffuse_Sample for one normal and sample pair (shader/diffuse.glsl:7-14, shader/util.glsl:5-9). */
 void oracle_diffuse_sample(const float nrm[3], float u1, float u2, float out[3]);
 /* Cosine bounce rays for hits (shader/diffuse.glsl:7-14 + shader/util.glsl:5-9). */

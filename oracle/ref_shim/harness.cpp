@@ -113,6 +113,46 @@ void ref_occlude(const uint32_t *pool, uint32_t n, const float *o, const float *
 		                                            vec3(d[3 * r], d[3 * r + 1], d[3 * r + 2]));
 }
 
+// The beam pre-pass of shader/octree_tracer_beam.frag:12-30 as OctreeTracer::CmdBeamRenderPass runs it
+// (src/OctreeTracer.cpp:183-211): one texel per (beam_size x beam_size) pixel tile corner, width / height
+// texels (x + beam_size - 1) / beam_size + 1 (src/OctreeTracer.cpp:6), Octree_RayMarchCoarse from the
+// shader source; the texel arithmetic of the fragment shader's main() is restated here line for line.
+static float ray_tangent(vec3 x, vec3 y) {
+	float c = dot(x, y);
+	return sqrt(1.0f - c * c) / abs(c);
+}
+
+void ref_beam(const uint32_t *pool, const float *cam16, uint32_t width, uint32_t height, uint32_t beam_size,
+              float origin_size, float *beam) {
+	uOctree = (uint *)pool;
+	uPosition = vec4(cam16[0], cam16[1], cam16[2], cam16[3]);
+	uLook = vec4(cam16[4], cam16[5], cam16[6], cam16[7]);
+	uSide = vec4(cam16[8], cam16[9], cam16[10], cam16[11]);
+	uUp = vec4(cam16[12], cam16[13], cam16[14], cam16[15]);
+	const uint32_t bw = (width + beam_size - 1) / beam_size + 1, bh = (height + beam_size - 1) / beam_size + 1;
+	const vec2 size((float)width, (float)height);
+	const float bs = (float)beam_size;
+	for (uint32_t by = 0; by < bh; ++by)
+		for (uint32_t bx = 0; bx < bw; ++bx) {
+			const vec2 fc((float)(int)bx, (float)(int)by);
+			auto gen = [&](float ox, float oy) {
+				vec2 c = (fc + vec2(ox, oy)) / size;
+				c = c * bs;
+				return ref_camera::Camera_GenRay(c);
+			};
+			vec2 c0 = fc / size;
+			c0 = c0 * bs;
+			vec3 o = vec3(uPosition.x, uPosition.y, uPosition.z), d = ref_camera::Camera_GenRay(c0);
+			float t0 = ray_tangent(d, gen(0.5f, 0.5f));
+			float t1 = ray_tangent(d, gen(-0.5f, 0.5f));
+			float t2 = ray_tangent(d, gen(0.5f, -0.5f));
+			float t3 = ray_tangent(d, gen(-0.5f, -0.5f));
+			float dir_sz = 2.0f * max(max(t0, t1), max(t2, t3)), t, sz;
+			beam[(uint64_t)by * bw + bx] =
+			    ref_octree::Octree_RayMarchCoarse(o, d, origin_size, dir_sz, t, sz) ? max(0.0f, t - sz) : 1e10f;
+		}
+}
+
 // shader/octree_tracer.frag:24: d = Camera_GenRay(ivec2(gl_FragCoord.xy) / vec2(uWidth, uHeight)).
 void ref_camera_rays(const float *cam16, uint32_t width, uint32_t height, float *dirs) {
 	uPosition = vec4(cam16[0], cam16[1], cam16[2], cam16[3]);

@@ -48,6 +48,7 @@ def lib():
         L.ref_raycast.argtypes = [P, u32, P, P, i32, P, P, P, P, P]
         L.ref_occlude.argtypes = [P, u32, P, P, P]
         L.ref_camera_rays.argtypes = [P, u32, u32, P]
+        L.ref_beam.argtypes = [P, P, u32, u32, u32, f32, P]
         L.ref_diffuse_sample.argtypes = [P, f32, f32, P]
         L.ref_voxelize_triangle.argtypes = [P, u32, u32, i32, P, u64]
         L.ref_voxelize_triangle.restype = u64
@@ -87,6 +88,16 @@ def occlude(pool: np.ndarray, o: np.ndarray, d: np.ndarray) -> np.ndarray:
     hit = np.zeros(len(o), np.uint32)
     lib().ref_occlude(_p(pool), len(o), _p(o), _p(d), _p(hit))
     return hit
+
+
+def beam(pool: np.ndarray, cam, width: int, height: int, level: int, beam_size: int = 8) -> np.ndarray:
+    """Beam image (start distance per tile corner) of the reference's beam pre-pass."""
+    c = np.ascontiguousarray(np.frombuffer(np.asarray(cam).tobytes(), np.float32))
+    bw, bh = (width + beam_size - 1) // beam_size + 1, (height + beam_size - 1) // beam_size + 1
+    out = np.zeros((bh, bw), np.float32)
+    lib().ref_beam(_p(np.ascontiguousarray(pool)), _p(c), width, height, beam_size,
+                   float(np.ldexp(np.float32(1.0), 1 - level)), _p(out))
+    return out
 
 
 def camera_dirs(cam, width: int, height: int) -> np.ndarray:

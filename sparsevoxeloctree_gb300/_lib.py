@@ -125,6 +125,10 @@ _SIGNATURES = {
     "svo_server_submit_rebuild": ([P, u32, P, u32, u32, ctypes.POINTER(u64)], i32),
     "svo_server_wait": ([P, u64, i32, ctypes.POINTER(RequestResult)], i32),
     "svo_server_get_stats": ([P, ctypes.POINTER(ServerStats)], None),
+    "svo_beam_texels": ([u32, u32], u64),
+    "svo_beam_prepass": ([ctypes.POINTER(OctreeC), ctypes.POINTER(CameraC), u32, u32, P, P], i32),
+    "svo_raycast_camera_beam": ([ctypes.POINTER(OctreeC), ctypes.POINTER(CameraC), u32, u32, P, P, P, P], i32),
+    "svo_occlude": ([ctypes.POINTER(OctreeC), P, u32, P, P], i32),
     "svo_tune_set": ([u32, u32, ctypes.c_int32, ctypes.c_int32], i32),
     "svo_tune_get": ([u32, u32, u64], i32),
     "svo_tune_size_class": ([u64], u32),

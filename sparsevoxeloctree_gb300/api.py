@@ -341,6 +341,41 @@ class OctreeTracer:
                                                   _ptr(hits), self._fetch_ptr(count_fetches), _stream(stream)))
         return hits
 
+    def CmdBeamRenderPass(self, beam: torch.Tensor | None = None, stream=None) -> torch.Tensor:
+        """OctreeTracer::CmdBeamRenderPass (src/OctreeTracer.cpp:183-211): the beam image, one start distance
+        per corner of each 8x8 pixel tile (float32, ((H+7)//8+1) x ((W+7)//8+1))."""
+        lib = _lib.load()
+        bw, bh = (self.m_width + 7) // 8 + 1, (self.m_height + 7) // 8 + 1
+        if beam is None:
+            beam = torch.empty((bh, bw), dtype=torch.float32, device=self.m_octree.device)
+        cam = camera_struct(self.m_camera)
+        oc = self.m_octree.c_struct()
+        _lib.check(lib.svo_beam_prepass(ctypes.byref(oc), ctypes.byref(cam), self.m_width, self.m_height, _ptr(beam),
+                                        _stream(stream)))
+        return beam
+
+    def CmdDrawPipelineBeam(self, beam: torch.Tensor | None = None, hits: torch.Tensor | None = None, stream=None,
+                            count_fetches: bool = False) -> torch.Tensor:
+        """CmdDrawPipeline with the beam enabled (shader/octree_tracer.frag:27-33); beam None: computed here."""
+        n = self.m_width * self.m_height
+        if hits is None:
+            hits = torch.empty(n * HIT_DTYPE.itemsize, dtype=torch.uint8, device=self.m_octree.device)
+        cam = camera_struct(self.m_camera)
+        oc = self.m_octree.c_struct()
+        _lib.check(_lib.load().svo_raycast_camera_beam(ctypes.byref(oc), ctypes.byref(cam), self.m_width,
+                                                       self.m_height, _ptr(beam), _ptr(hits),
+                                                       self._fetch_ptr(count_fetches), _stream(stream)))
+        return hits
+
+    def Occlude(self, rays: torch.Tensor, out: torch.Tensor | None = None, stream=None) -> torch.Tensor:
+        """Octree_RayMarchOcclude per ray (shader/octree.glsl:504-629): int32 tensor, 1 = occluded."""
+        n = rays.numel() // RAY_DTYPE.itemsize
+        if out is None:
+            out = torch.empty(max(n, 1), dtype=torch.int32, device=rays.device)
+        oc = self.m_octree.c_struct()
+        _lib.check(_lib.load().svo_occlude(ctypes.byref(oc), _ptr(rays), n, _ptr(out), _stream(stream)))
+        return out[:n]
+
     def Trace(self, rays: torch.Tensor, hits: torch.Tensor | None = None, stream=None,
               count_fetches: bool = False) -> torch.Tensor:
         """Octree_RayMarchLeaf for an explicit ray buffer (RAY_DTYPE bytes on the device)."""

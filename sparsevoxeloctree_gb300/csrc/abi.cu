@@ -568,7 +568,8 @@ static int check_octree(const svo_octree *o) {
 }
 
 static int raycast_common(const svo_octree *o, const svo_ray *rays, const svo_camera *cam, uint32_t width,
-                          uint32_t height, uint32_t n, svo_hit *hits, uint64_t *fetches_dev, void *stream) {
+                          uint32_t height, uint32_t n, svo_hit *hits, uint64_t *fetches_dev, void *stream,
+                          const float *beam = nullptr) {
 	int rc;
 	if ((rc = check_octree(o))) return rc;
 	if (n && !hits) return fail(SVO_ERR_INVALID, "null hit buffer");
@@ -591,6 +592,7 @@ static int raycast_common(const svo_octree *o, const svo_ray *rays, const svo_ca
 	a.ticket = scratch;
 	a.status = reinterpret_cast<uint32_t *>(scratch + 1);
 	a.fetches = (unsigned long long *)fetches_dev;
+	a.beam = beam;
 	cudaError_t e = march_launch(a, cam != nullptr, s);
 	cudaFreeAsync(scratch, s);
 	if (e != cudaSuccess) return cuda_fail(e, "raycast");
@@ -608,6 +610,82 @@ int svo_raycast_camera(const svo_octree *o, const svo_camera *cam, uint32_t widt
 	const uint64_t n = (uint64_t)width * height;
 	if (n > 0xffffffffull) return fail(SVO_ERR_INVALID, "image too large");
 	return raycast_common(o, nullptr, cam, width, height, (uint32_t)n, hits, fetches_dev, stream);
+}
+
+uint64_t svo_beam_texels(uint32_t width, uint32_t height) {
+	return (uint64_t)((width + SVO_BEAM_SIZE - 1) / SVO_BEAM_SIZE + 1) * ((height + SVO_BEAM_SIZE - 1) / SVO_BEAM_SIZE + 1);
+}
+
+// MarchArgs with a 16-byte scratch (ticket + status) from the stream-ordered pool.
+static int march_args(const svo_octree *o, cudaStream_t s, MarchArgs &a, unsigned long long **scratch) {
+	int rc;
+	if ((rc = check_octree(o))) return rc;
+	SVO_CK(alloc_async(scratch, 2 * sizeof(unsigned long long), s), "march scratch allocation");
+	SVO_CK(cudaMemsetAsync(*scratch, 0, 2 * sizeof(unsigned long long), s), "march scratch");
+	memset(&a, 0, sizeof(a));
+	a.pool = o->words;
+	a.range = o->range_words;
+	a.level = o->level;
+	a.ticket = *scratch;
+	a.status = reinterpret_cast<uint32_t *>(*scratch + 1);
+	return SVO_OK;
+}
+
+int svo_beam_prepass(const svo_octree *o, const svo_camera *cam, uint32_t width, uint32_t height, float *beam,
+                     void *stream) {
+	if (!cam || !beam) return fail(SVO_ERR_INVALID, "null argument");
+	if (!width || !height) return fail(SVO_ERR_INVALID, "empty image");
+	if (!aligned(beam, 4)) return fail(SVO_ERR_INVALID, "beam buffer must be 4-byte aligned");
+	cudaStream_t s = (cudaStream_t)stream;
+	MarchArgs a;
+	unsigned long long *scratch = nullptr;
+	int rc = march_args(o, s, a, &scratch);
+	if (rc) return rc;
+	a.cam = *cam;
+	a.width = width;
+	a.height = height;
+	cudaError_t e = beam_launch(a, beam, s);
+	cudaFreeAsync(scratch, s);
+	if (e != cudaSuccess) return cuda_fail(e, "beam pre-pass");
+	return SVO_OK;
+}
+
+int svo_raycast_camera_beam(const svo_octree *o, const svo_camera *cam, uint32_t width, uint32_t height,
+                            const float *beam, svo_hit *hits, uint64_t *fetches_dev, void *stream) {
+	if (!cam) return fail(SVO_ERR_INVALID, "null camera");
+	const uint64_t n = (uint64_t)width * height;
+	if (n > 0xffffffffull) return fail(SVO_ERR_INVALID, "image too large");
+	if (n == 0) return raycast_common(o, nullptr, cam, width, height, 0, hits, fetches_dev, stream);
+	cudaStream_t s = (cudaStream_t)stream;
+	float *own = nullptr;
+	if (!beam) {
+		SVO_CK(alloc_async(&own, svo_beam_texels(width, height) * sizeof(float), s), "beam allocation");
+		const int rc = svo_beam_prepass(o, cam, width, height, own, stream);
+		if (rc) {
+			cudaFreeAsync(own, s);
+			return rc;
+		}
+		beam = own;
+	}
+	const int rc = raycast_common(o, nullptr, cam, width, height, (uint32_t)n, hits, fetches_dev, stream, beam);
+	if (own) cudaFreeAsync(own, s);
+	return rc;
+}
+
+int svo_occlude(const svo_octree *o, const svo_ray *rays, uint32_t n, uint32_t *occluded, void *stream) {
+	if (n && (!rays || !occluded)) return fail(SVO_ERR_INVALID, "null argument");
+	if (!aligned(rays, 8) || !aligned(occluded, 4)) return fail(SVO_ERR_INVALID, "misaligned buffer");
+	cudaStream_t s = (cudaStream_t)stream;
+	MarchArgs a;
+	unsigned long long *scratch = nullptr;
+	int rc = march_args(o, s, a, &scratch);
+	if (rc) return rc;
+	a.rays = rays;
+	a.n = n;
+	cudaError_t e = occlude_launch(a, occluded, s);
+	cudaFreeAsync(scratch, s);
+	if (e != cudaSuccess) return cuda_fail(e, "occlude");
+	return SVO_OK;
 }
 
 int svo_bounce_rays(const svo_hit *hits, uint32_t n, uint64_t seed, svo_ray *rays, void *stream) {

@@ -23,6 +23,7 @@ namespace svo {
 
 constexpr int kMarchTPB = 128;
 constexpr float kEps = 3.552713678800501e-15f; // EPS of shader/octree.glsl:44 (2^-48)
+constexpr uint32_t kBeamSize = SVO_BEAM_SIZE;   // pixels per beam tile edge (kBeamSize, src/Config.hpp:22)
 
 SVO_DEV float max_glsl(float x, float y) { return x < y ? y : x; }
 SVO_DEV float min_glsl(float x, float y) { return y < x ? y : x; }
@@ -205,9 +206,8 @@ SVO_DEV void store_hit(svo_hit *hits, uint32_t r, const MarchOut &m) {
 }
 
 // Camera_GenRay(ivec2(pixel) / size) (shader/camera.glsl:11-14, shader/octree_tracer.frag:24).
-SVO_DEV void camera_ray(const svo_camera &cam, uint32_t width, uint32_t height, uint32_t r, float o[3], float d[3]) {
-	const uint32_t y = r / width, x = r - y * width;
-	float cx = (float)x / (float)width, cy = (float)y / (float)height;
+// Camera_GenRay of a normalised image coordinate (shader/camera.glsl:11-14).
+SVO_DEV void gen_dir(const svo_camera &cam, float cx, float cy, float d[3]) {
 	cx = cx * 2.0f - 1.0f;
 	cy = cy * 2.0f - 1.0f;
 	float v[3];
@@ -215,10 +215,25 @@ SVO_DEV void camera_ray(const svo_camera &cam, uint32_t width, uint32_t height, 
 	for (int k = 0; k < 3; ++k) v[k] = (cam.look[k] - cam.side[k] * cx) - cam.up[k] * cy;
 	const float len = sqrtf((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]);
 #pragma unroll
-	for (int k = 0; k < 3; ++k) {
-		o[k] = cam.pos[k];
-		d[k] = v[k] / len;
-	}
+	for (int k = 0; k < 3; ++k) d[k] = v[k] / len;
+}
+
+SVO_DEV void camera_ray(const svo_camera &cam, uint32_t width, uint32_t height, uint32_t r, float o[3], float d[3]) {
+	const uint32_t y = r / width, x = r - y * width;
+	gen_dir(cam, (float)x / (float)width, (float)y / (float)height, d);
+#pragma unroll
+	for (int k = 0; k < 3; ++k) o[k] = cam.pos[k];
+}
+
+// shader/octree_tracer.frag:27-33: a primary ray starts at o + d * (the least of the 4 beam texels at
+// the corners of its pixel's tile).
+SVO_DEV void beam_advance(const float *__restrict__ beam, uint32_t width, uint32_t r, float o[3], const float d[3]) {
+	const uint32_t y = r / width, x = r - y * width;
+	const uint32_t bw = (width + kBeamSize - 1) / kBeamSize + 1;
+	const float *t0 = beam + (size_t)(y / kBeamSize) * bw + x / kBeamSize, *t1 = t0 + bw;
+	const float m = min_glsl(min_glsl(__ldg(t0), __ldg(t0 + 1)), min_glsl(__ldg(t1), __ldg(t1 + 1)));
+#pragma unroll
+	for (int k = 0; k < 3; ++k) o[k] = o[k] + d[k] * m;
 }
 
 // Variants (chosen per launch from the launch-parameter table): TPB threads per block, RPL rays per lane
@@ -252,6 +267,7 @@ __global__ void __launch_bounds__(TPB) march_kernel(MarchArgs a) {
 				if (x >= a.width || y >= a.height) continue; // padding slot of a partial edge tile
 				r = y * a.width + x;
 				camera_ray(a.cam, a.width, a.height, r, o, d);
+				if (a.beam) beam_advance(a.beam, a.width, r, o, d);
 			} else {
 				r = (uint32_t)slot;
 				const float2 *src = reinterpret_cast<const float2 *>(a.rays + r);
@@ -268,6 +284,191 @@ __global__ void __launch_bounds__(TPB) march_kernel(MarchArgs a) {
 	if (a.fetches) {
 		fetched = warp_sum(fetched);
 		if (lane == 0) atomicAdd(a.fetches, fetched);
+	}
+}
+
+// ------------------------------------------------------------------------------------ occlusion and beam
+// The traversal of Octree_RayMarchOcclude (shader/octree.glsl:504-629; COARSE = false) and of
+// Octree_RayMarchCoarse (shader/octree.glsl:47-177; COARSE = true): the leaf march without its outputs,
+// with the occlusion march's direction clamp (|d| >= EPS is kept) or, for the coarse march, the leaf
+// march's clamp and a stop at the first non-empty node at least as large as the cone footprint
+// orig_sz + t * dir_sz.  Returns true on a hit, with t = t_min and size = the node's size.  A malformed
+// pool ends the ray as a miss and sets kStatusMalformed.
+template <bool COARSE, int STRIDE>
+SVO_DEV bool march_traverse(const uint32_t *__restrict__ pool, uint32_t range, uint32_t level, const float o[3],
+                            const float dir[3], float orig_sz, float dir_sz, uint32_t *stack, float &t_out,
+                            float &size_out, uint32_t *status) {
+	float d[3];
+#pragma unroll
+	for (int k = 0; k < 3; ++k)
+		d[k] = (COARSE ? fabsf(dir[k]) > kEps : fabsf(dir[k]) >= kEps) ? dir[k] : (dir[k] >= 0.0f ? kEps : -kEps);
+	for (uint32_t k = 0; k < level; ++k) stack[k * STRIDE] = 0u;
+	float coef[3], bias[3];
+#pragma unroll
+	for (int k = 0; k < 3; ++k) {
+		coef[k] = 1.0f / -fabsf(d[k]);
+		bias[k] = coef[k] * o[k];
+	}
+	uint32_t oct_mask = 0;
+#pragma unroll
+	for (int k = 0; k < 3; ++k)
+		if (d[k] > 0.0f) {
+			oct_mask ^= 1u << k;
+			bias[k] = 3.0f * coef[k] - bias[k];
+		}
+	float t_min = max_glsl(max_glsl(2.0f * coef[0] - bias[0], 2.0f * coef[1] - bias[1]), 2.0f * coef[2] - bias[2]);
+	const float t_max = min_glsl(min_glsl(coef[0] - bias[0], coef[1] - bias[1]), coef[2] - bias[2]);
+	t_min = max_glsl(t_min, 0.0f);
+	float h = t_max;
+	uint32_t parent = 0, cur = 0, idx = 0;
+	float pos[3] = {1.0f, 1.0f, 1.0f};
+#pragma unroll
+	for (int k = 0; k < 3; ++k)
+		if (1.5f * coef[k] - bias[k] > t_min) {
+			idx ^= 1u << k;
+			pos[k] = 1.5f;
+		}
+	uint32_t scale = SVO_STACK_SIZE - 1, iter = 0;
+	float scale_exp2 = 0.5f;
+	bool aborted = false;
+	const uint32_t min_scale = SVO_STACK_SIZE - level;
+	while (scale < SVO_STACK_SIZE) {
+		if (++iter > SVO_MARCH_MAX_ITER) {
+			aborted = true;
+			break;
+		}
+		if (cur == 0u) {
+			const uint32_t w = parent + (idx ^ oct_mask);
+			if (w >= range) {
+				atomicOr(status, kStatusMalformed);
+				aborted = true;
+				break;
+			}
+			cur = __ldg(pool + w);
+		}
+		float tc[3];
+#pragma unroll
+		for (int k = 0; k < 3; ++k) tc[k] = pos[k] * coef[k] - bias[k];
+		const float tc_max = min_glsl(min_glsl(tc[0], tc[1]), tc[2]);
+		if ((cur & 0x80000000u) != 0u && t_min <= t_max) {
+			if (COARSE && orig_sz + tc_max * dir_sz >= scale_exp2) break;
+			const float half = scale_exp2 * 0.5f;
+			float t_center[3];
+#pragma unroll
+			for (int k = 0; k < 3; ++k) t_center[k] = half * coef[k] + tc[k];
+			if ((cur & 0x40000000u) != 0u) break; // leaf
+			if (scale <= min_scale) {
+				atomicOr(status, kStatusMalformed);
+				aborted = true;
+				break;
+			}
+			if (tc_max < h) stack[(SVO_STACK_SIZE - 1 - scale) * STRIDE] = parent;
+			h = tc_max;
+			parent = cur & 0x3fffffffu;
+			idx = 0;
+			--scale;
+			scale_exp2 = half;
+#pragma unroll
+			for (int k = 0; k < 3; ++k)
+				if (t_center[k] > t_min) {
+					idx ^= 1u << k;
+					pos[k] += scale_exp2;
+				}
+			cur = 0;
+			continue;
+		}
+		uint32_t step_mask = 0;
+#pragma unroll
+		for (int k = 0; k < 3; ++k)
+			if (tc[k] <= tc_max) {
+				step_mask ^= 1u << k;
+				pos[k] -= scale_exp2;
+			}
+		t_min = tc_max;
+		idx ^= step_mask;
+		if ((idx & step_mask) != 0u) {
+			uint32_t diff = 0;
+#pragma unroll
+			for (int k = 0; k < 3; ++k)
+				if (step_mask & (1u << k)) diff |= __float_as_uint(pos[k]) ^ __float_as_uint(pos[k] + scale_exp2);
+			scale = diff ? 31u - (uint32_t)__clz(diff) : 0xffffffffu;
+			if (scale >= SVO_STACK_SIZE) break;
+			scale_exp2 = __uint_as_float((scale - SVO_STACK_SIZE + 127u) << 23u);
+			parent = stack[(SVO_STACK_SIZE - 1 - scale) * STRIDE];
+			uint32_t sh[3];
+#pragma unroll
+			for (int k = 0; k < 3; ++k) {
+				sh[k] = __float_as_uint(pos[k]) >> scale;
+				pos[k] = __uint_as_float(sh[k] << scale);
+			}
+			idx = (sh[0] & 1u) | ((sh[1] & 1u) << 1) | ((sh[2] & 1u) << 2);
+			h = 0.0f;
+			cur = 0;
+		}
+	}
+	t_out = t_min;
+	size_out = scale_exp2;
+	return !aborted && scale < SVO_STACK_SIZE && t_min <= t_max;
+}
+
+// RayTangent of shader/octree_tracer_beam.frag:17-20.
+SVO_DEV float ray_tangent(const float x[3], const float y[3]) {
+	const float c = (x[0] * y[0] + x[1] * y[1]) + x[2] * y[2];
+	return sqrtf(1.0f - c * c) / fabsf(c);
+}
+
+// The beam pre-pass (shader/octree_tracer_beam.frag:22-30 as src/OctreeTracer.cpp:183-211 draws it): one
+// texel per corner of each kBeamSize x kBeamSize pixel tile.  The ray through the corner and the 4 rays
+// half a texel away give the cone's tangent; the coarse march stops at the first node the cone does
+// not resolve, and the texel is max(0, t - node size), or 1e10 when the cone misses.
+__global__ void __launch_bounds__(kMarchTPB) beam_kernel(MarchArgs a, float *__restrict__ beam, float orig_sz) {
+	__shared__ uint32_t s_stack[SVO_LEVEL_MAX * kMarchTPB];
+	uint32_t *stack = s_stack + threadIdx.x;
+	const uint32_t bw = (a.width + kBeamSize - 1) / kBeamSize + 1, bh = (a.height + kBeamSize - 1) / kBeamSize + 1;
+	const float W = (float)a.width, H = (float)a.height, bs = (float)kBeamSize;
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < bw * bh; i += gridDim.x * blockDim.x) {
+		const uint32_t by = i / bw, bx = i - by * bw;
+		const float fx = (float)bx, fy = (float)by;
+		float d[3], dk[3];
+		gen_dir(a.cam, fx / W * bs, fy / H * bs, d);
+		gen_dir(a.cam, (fx + 0.5f) / W * bs, (fy + 0.5f) / H * bs, dk);
+		const float t0 = ray_tangent(d, dk);
+		gen_dir(a.cam, (fx + -0.5f) / W * bs, (fy + 0.5f) / H * bs, dk);
+		const float t1 = ray_tangent(d, dk);
+		gen_dir(a.cam, (fx + 0.5f) / W * bs, (fy + -0.5f) / H * bs, dk);
+		const float t2 = ray_tangent(d, dk);
+		gen_dir(a.cam, (fx + -0.5f) / W * bs, (fy + -0.5f) / H * bs, dk);
+		const float t3 = ray_tangent(d, dk);
+		const float dir_sz = 2.0f * max_glsl(max_glsl(t0, t1), max_glsl(t2, t3));
+		const float o[3] = {a.cam.pos[0], a.cam.pos[1], a.cam.pos[2]};
+		float t, sz;
+		const bool hit = march_traverse<true, kMarchTPB>(a.pool, a.range, a.level, o, d, orig_sz, dir_sz, stack, t, sz,
+		                                                 a.status);
+		beam[i] = hit ? max_glsl(0.0f, t - sz) : 1e10f;
+	}
+}
+
+__global__ void __launch_bounds__(kMarchTPB) occlude_kernel(MarchArgs a, uint32_t *__restrict__ occluded) {
+	__shared__ uint32_t s_stack[SVO_LEVEL_MAX * kMarchTPB];
+	uint32_t *stack = s_stack + threadIdx.x;
+	const uint32_t lane = lane_id();
+	for (;;) {
+		unsigned long long base = 0;
+		if (lane == 0) base = atomicAdd(a.ticket, 32ull);
+		base = __shfl_sync(kFullMask, base, 0);
+		if (base >= a.n) break;
+		const uint64_t r = base + lane;
+		if (r < a.n) {
+			const float2 *src = reinterpret_cast<const float2 *>(a.rays + r);
+			const float2 p0 = src[0], p1 = src[1], p2 = src[2];
+			const float o[3] = {p0.x, p0.y, p1.x}, d[3] = {p1.y, p2.x, p2.y};
+			bool hit = false;
+			if (d[0] != 0.0f || d[1] != 0.0f || d[2] != 0.0f) { // a null ray (a missed bounce) hits nothing
+				float t, sz;
+				hit = march_traverse<false, kMarchTPB>(a.pool, a.range, a.level, o, d, 0.0f, 0.0f, stack, t, sz, a.status);
+			}
+			occluded[r] = hit ? 1u : 0u;
+		}
 	}
 }
 
@@ -500,6 +701,30 @@ cudaError_t bounce_jobs_launch(const BounceJob *jobs, uint32_t njobs, uint64_t t
 	const int sms = device_sm_count();
 	const uint32_t blocks = (uint32_t)std::min<uint64_t>((total + 255) / 256, (uint64_t)sms * 8);
 	SVO_LAUNCH("bounce_jobs", stream, bounce_jobs_kernel<<<blocks, 256, 0, stream>>>(jobs, njobs, total););
+	return cudaGetLastError();
+}
+
+} // namespace svo
+
+namespace svo {
+
+cudaError_t beam_launch(const MarchArgs &a, float *beam, cudaStream_t stream) {
+	const uint64_t texels = (uint64_t)((a.width + kBeamSize - 1) / kBeamSize + 1) * ((a.height + kBeamSize - 1) / kBeamSize + 1);
+	const int sms = device_sm_count();
+	const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((texels + kMarchTPB - 1) / kMarchTPB,
+	                                                                            (uint64_t)sms * 16));
+	const float orig_sz = ldexpf(1.0f, 1 - (int)a.level); // exp2f(1 - level), src/OctreeTracer.cpp:205
+	SVO_LAUNCH("beam_prepass", stream, beam_kernel<<<blocks, kMarchTPB, 0, stream>>>(a, beam, orig_sz););
+	return cudaGetLastError();
+}
+
+cudaError_t occlude_launch(const MarchArgs &a, uint32_t *occluded, cudaStream_t stream) {
+	cudaError_t e = cudaMemsetAsync(a.ticket, 0, sizeof(unsigned long long), stream);
+	if (e != cudaSuccess || a.n == 0) return e;
+	const int sms = device_sm_count();
+	const uint64_t blocks_needed = ((uint64_t)a.n / 32 + kMarchTPB / 32) / (kMarchTPB / 32);
+	const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(blocks_needed, (uint64_t)sms * 16));
+	SVO_LAUNCH("occlude", stream, occlude_kernel<<<blocks, kMarchTPB, 0, stream>>>(a, occluded););
 	return cudaGetLastError();
 }
 

@@ -255,8 +255,13 @@ struct MarchArgs {
 	unsigned long long *ticket;   // device work-slot ticket (zeroed by march_launch)
 	unsigned long long *fetches;  // optional node-load total
 	uint32_t *status;             // device status word
+	const float *beam;            // camera rays: beam texels to advance each ray by (null: none)
 };
 cudaError_t march_launch(const MarchArgs &a, bool camera, cudaStream_t stream);
+// Beam pre-pass texels ((width + 7) / 8 + 1) x ((height + 7) / 8 + 1) for camera `a.cam`.
+cudaError_t beam_launch(const MarchArgs &a, float *beam, cudaStream_t stream);
+// Octree_RayMarchOcclude for a.n rays: occluded[i] = 1 when ray i hits a leaf.
+cudaError_t occlude_launch(const MarchArgs &a, uint32_t *occluded, cudaStream_t stream);
 cudaError_t bounce_launch(const svo_hit *hits, uint32_t n, uint64_t seed, svo_ray *rays, cudaStream_t stream);
 
 // One request's share of a shared march launch: its octree, its rays (a ray buffer, or camera rays for

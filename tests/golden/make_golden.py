@@ -14,7 +14,11 @@ the reference checkout.
   golden_camera.npz  a camera and the directions Camera_GenRay produces for a 48x32 image;
   golden_vox.npz     grid-aligned triangles and the fragments the reference's conservative geometry
                      shader + fragment shader produce for them (pixel-centre raster in double);
-  golden_diffuse.npz normals, sample pairs and the reference's Diffuse_Sample directions.
+  golden_diffuse.npz normals, sample pairs and the reference's Diffuse_Sample directions;
+  golden_beam.npz    two cameras and the beam image of the reference's beam pre-pass (Octree_RayMarchCoarse
+                     from the shader source, texel arithmetic of shader/octree_tracer_beam.frag) on the
+                     golden_build pool;
+  golden_occlude.npz Octree_RayMarchOcclude of the golden_march rays on that pool.
 """
 from __future__ import annotations
 
@@ -93,6 +97,17 @@ def main() -> int:
         vcount.append(len(f))
     np.savez_compressed(os.path.join(OUT, "golden_vox.npz"), tris=np.concatenate(vtris).view(np.uint8), level=vl,
                         frags=np.concatenate(vfrag), counts=np.array(vcount, np.uint32))
+
+    # beam pre-pass (Octree_RayMarchCoarse + shader/octree_tracer_beam.frag) for an outside and an inside
+    # camera, and Octree_RayMarchOcclude for the march rays
+    beams = {}
+    for k, (pos, yaw, pitch, w, h) in enumerate([((1.5, 1.5, 0.5), 0.1, -0.05, 61, 45), ((1.45, 1.55, 1.3), 2.5, 0.2, 40, 33)]):
+        camk = scenes.camera_from_angles(pos, yaw, pitch, np.pi / 3, w / h)
+        beams[f"cam{k}"] = np.frombuffer(camk.tobytes(), np.float32)
+        beams[f"size{k}"] = np.array([w, h])
+        beams[f"beam{k}"] = ref.beam(pool, camk, w, h, level)
+    np.savez_compressed(os.path.join(OUT, "golden_beam.npz"), **beams)
+    np.savez_compressed(os.path.join(OUT, "golden_occlude.npz"), occluded=ref.occlude(pool, o, d).astype(np.uint32))
 
     g = scenes.rng(SEED, 4)
     normals = np.zeros((60, 3), np.float32)

@@ -410,3 +410,69 @@ def test_voxelizer_reemission_needs_exact_unit_scratch(cuda):
     v.CheckEmission()
     import torch
     assert torch.equal(v.GetVoxelFragmentList(), first)
+
+
+# ------------------------------------------------------------------------------------------- beam / occlusion
+def _golden_octree(golden_dir):
+    import torch
+    api = _api()
+    zb = np.load(f"{golden_dir}/golden_build.npz")
+    level, pool = int(zb["level"]), zb["pool"]
+    o = api.Octree()
+    o.m_buffer = torch.from_numpy(pool.view(np.int32)).cuda()
+    o.m_range, o.m_level = len(pool) * 4, level
+    return o, pool, level
+
+
+def test_beam_prepass_golden_and_oracle(cuda, golden_dir):
+    """The beam image bit for bit against the reference's beam pre-pass and the oracle; the beam march
+    (primary rays advanced by it) against the oracle's march of the advanced rays."""
+    from sparsevoxeloctree_gb300.formats import CAMERA_DTYPE
+    api = _api()
+    octree, pool, level = _golden_octree(golden_dir)
+    zbeam = np.load(f"{golden_dir}/golden_beam.npz")
+    for k in range(2):
+        cam = np.frombuffer(zbeam[f"cam{k}"].tobytes(), CAMERA_DTYPE)[0]
+        w, h = (int(x) for x in zbeam[f"size{k}"])
+        tr = api.OctreeTracer.Create(octree, cam, w, h)
+        beam = tr.CmdBeamRenderPass().cpu().numpy()
+        assert np.array_equal(beam, zbeam[f"beam{k}"])
+        hits = api.hits_numpy(tr.CmdDrawPipelineBeam())
+        ref = oracle.raycast(pool, level, oracle.camera_rays_beam(cam, w, h, zbeam[f"beam{k}"]))
+        assert_hits_equal(hits, ref)
+        again = api.hits_numpy(tr.CmdDrawPipelineBeam(beam=tr.CmdBeamRenderPass()))
+        assert np.array_equal(again, hits)
+
+
+def test_beam_on_built_scene_matches_oracle(cuda):
+    api = _api()
+    s = scenes.plain_256()
+    frags = oracle.voxelize(s.tris, s.level)
+    octree, pool = gpu_build(frags, s.level)
+    for pos, yaw, pitch, w, h in [((1.5, 1.5, 0.5), 0.0, 0.0, 64, 64), ((1.5, 1.45, 1.5), 0.7, -0.2, 97, 53)]:
+        cam = scenes.camera_from_angles(pos, yaw, pitch, aspect=w / h)
+        b_ref = oracle.beam(pool, s.level, cam, w, h)
+        tr = api.OctreeTracer.Create(octree, cam, w, h)
+        assert np.array_equal(tr.CmdBeamRenderPass().cpu().numpy(), b_ref)
+        assert_hits_equal(api.hits_numpy(tr.CmdDrawPipelineBeam()),
+                          oracle.raycast(pool, s.level, oracle.camera_rays_beam(cam, w, h, b_ref)))
+
+
+def test_occlusion_golden_and_oracle(cuda, golden_dir):
+    api = _api()
+    octree, pool, level = _golden_octree(golden_dir)
+    zm, zocc = np.load(f"{golden_dir}/golden_march.npz"), np.load(f"{golden_dir}/golden_occlude.npz")
+    rays = rays_from_arrays(zm["o"], zm["d"])
+    got = api.OctreeTracer.Create(octree).Occlude(api.to_device(rays)).cpu().numpy().view(np.uint32)
+    assert np.array_equal(got, zocc["occluded"])
+    # a built scene, random rays and null rays (missed bounces)
+    s = scenes.plain_256()
+    frags = oracle.voxelize(s.tris, s.level)
+    oc, pool2 = gpu_build(frags, s.level)
+    g = np.random.default_rng(12)
+    o, d = scenes.random_rays(g, 5000, inside=True)
+    r2 = rays_from_arrays(o, d)
+    r2["d"][:50] = 0
+    got2 = api.OctreeTracer.Create(oc).Occlude(api.to_device(r2)).cpu().numpy().view(np.uint32)
+    assert np.array_equal(got2, oracle.occlude(pool2, s.level, r2))
+    assert not got2[:50].any()

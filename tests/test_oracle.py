@@ -158,3 +158,15 @@ def test_capacity_error():
     frags = pack_fragments([1, 2, 3], [1, 2, 3], [1, 2, 3], [0, 0, 0])
     with pytest.raises(RuntimeError):
         oracle.build_octree(frags, 4, capacity=16)
+
+
+def test_golden_beam_and_occlusion(golden_dir):
+    zb, zm = np.load(f"{golden_dir}/golden_build.npz"), np.load(f"{golden_dir}/golden_march.npz")
+    zbeam, zocc = np.load(f"{golden_dir}/golden_beam.npz"), np.load(f"{golden_dir}/golden_occlude.npz")
+    level, pool = int(zb["level"]), zb["pool"]
+    for k in range(2):
+        cam = np.frombuffer(zbeam[f"cam{k}"].tobytes(), CAMERA_DTYPE)[0]
+        w, h = (int(x) for x in zbeam[f"size{k}"])
+        assert np.array_equal(oracle.beam(pool, level, cam, w, h), zbeam[f"beam{k}"])
+    rays = rays_from_arrays(zm["o"], zm["d"])
+    assert np.array_equal(oracle.occlude(pool, level, rays), zocc["occluded"])

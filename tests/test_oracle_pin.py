@@ -83,3 +83,22 @@ def test_voxelize_matches_reference_shaders():
             total += len(theirs)
             diff += len(mine ^ theirs)
     assert diff <= 0.002 * total
+
+
+@pytest.mark.parametrize("cam_args", [((1.5, 1.5, 0.5), 0.0, 0.0, 64, 48), ((1.5, 1.4, 1.45), 1.2, 0.3, 37, 29)])
+def test_beam_and_occlusion_match_reference_shaders(cam_args):
+    """Octree_RayMarchCoarse + the beam texel arithmetic, and Octree_RayMarchOcclude."""
+    s = scenes.plain_256()
+    frags = oracle.voxelize(s.tris, s.level)
+    pool = oracle.build_octree(frags, s.level)
+    pos, yaw, pitch, w, h = cam_args
+    cam = scenes.camera_from_angles(pos, yaw, pitch, aspect=w / h)
+    assert np.array_equal(oracle.beam(pool, s.level, cam, w, h), ref.beam(pool, cam, w, h, s.level))
+    rays = oracle.camera_rays(cam, w, h)
+    g = np.random.default_rng(4)
+    o, d = scenes.random_rays(g, 2000, inside=True)
+    rays = np.concatenate([rays, rays_from_arrays(o, d)])
+    rays["d"][:4] = np.float32([[1, 0, 0], [0, 1e-30, 1], [0, 0, -1], [-1, -3.552713678800501e-15, 0]])
+    got = oracle.occlude(pool, s.level, rays)
+    want = ref.occlude(pool, rays["o"].astype(np.float32), rays["d"].astype(np.float32)).astype(np.uint32)
+    assert np.array_equal(got, want)
