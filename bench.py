@@ -261,6 +261,28 @@ def engine_arm(args, rank: int, world: int, device) -> dict:
         "kernels": profile,
     }
 
+    # the tracer's beam optimisation on the same frame: pre-pass + advanced primary march
+    beam_img = tracer.CmdBeamRenderPass()
+    hits_beam = tracer.CmdDrawPipelineBeam(beam_img)
+    bev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+            torch.cuda.Event(enable_timing=True)) for _ in range(5)]
+    for e0, e1, e2 in bev:
+        flush_buf.zero_()
+        e0.record(stream)
+        tracer.CmdBeamRenderPass(beam_img)
+        e1.record(stream)
+        tracer.CmdDrawPipelineBeam(beam_img, hits_beam)
+        e2.record(stream)
+    torch.cuda.synchronize()
+    hb = api.hits_numpy(hits_beam)
+    beam = {"prepass_ms": float(np.median([a.elapsed_time(b) for a, b, _ in bev])),
+            "march_ms": float(np.median([b.elapsed_time(c) for _, b, c in bev])),
+            "mean_iterations": float(hb["iter"].mean()),
+            "voxel_agreement_with_plain_march": float((hb["voxel"] == hit_np["voxel"]).all(axis=1).mean()),
+            "texels": int(beam_img.numel())}
+    beam["grays_per_s"] = n_rays / ((beam["prepass_ms"] + beam["march_ms"]) * 1e-3) / 1e9
+    stages["beam"] = beam
+
     e2e = None if args.no_e2e else e2e_arm(args, scene, tris_host, device, world)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

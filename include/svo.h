@@ -416,6 +416,29 @@ int svo_server_submit_rebuild(svo_server *s, uint32_t scene, const svo_triangle 
 int svo_server_wait(svo_server *s, uint64_t ticket, int timeout_ms, svo_request_result *res);
 void svo_server_get_stats(svo_server *s, svo_server_stats *out);
 
+/* ------------------------------------------------------------------ files */
+
+/* Scene::Create's mesh loading (Scene::load_meshes, src/Scene.cpp:36-147) for the engine's triangle
+ * format: an OBJ file's faces (polygons as triangle fans; "v", "v/t", "v//n", "v/t/n" and negative
+ * indices), its materials' Kd from the mtllib beside it packed like packUnorm4x8 (src/Scene.cpp:164), the
+ * vertices the faces use normalised to [-1, 1] as the reference does ((p - centre) / (largest extent /
+ * 2), src/Scene.cpp:90-99) and mapped to [0, 1] by p = (p_ref + 1) / 2.  Like the reference, a file
+ * without materials is rejected; faces before the first usemtl, or naming an undefined material, take
+ * the library's first material.  Textures are not read.  *tris_host is allocated here: release it with svo_free_host. */
+int svo_load_obj(const char *path, svo_triangle **tris_host, uint32_t *n_tris);
+void svo_free_host(void *p);
+
+/* Octree files: a 32-byte header ("SVOOCT01", uint32 level, uint32 range_words, uint32 header size 32,
+ * 12 reserved bytes) followed by the range_words node words, little-endian.  Reading checks the header,
+ * the size and that every child pointer lies inside the range at a whole block. */
+int svo_octree_write_host(const uint32_t *words, uint32_t range_words, uint32_t level, const char *path);
+/* *words allocated here: release it with svo_free_host. */
+int svo_octree_read_host(const char *path, uint32_t **words, uint32_t *range_words, uint32_t *level);
+/* Device forms: save downloads the used range (blocking); load allocates an owned pool of exactly the
+ * range from the stream-ordered pool (free it with svo_octree_destroy). */
+int svo_octree_save(const svo_octree *o, const char *path, void *stream);
+int svo_octree_load(const char *path, svo_octree *out, void *stream);
+
 /* Host helper: Camera::fetch_uniform_data (src/Camera.cpp:77-95) for a position, yaw, pitch, fov and
  * aspect ratio (radians; the reference's default fov is pi/3, src/Camera.hpp:17). */
 void svo_camera_from_angles(const float pos[3], float yaw, float pitch, float fov, float aspect, svo_camera *cam);

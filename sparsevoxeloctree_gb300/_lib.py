@@ -129,6 +129,12 @@ _SIGNATURES = {
     "svo_beam_prepass": ([ctypes.POINTER(OctreeC), ctypes.POINTER(CameraC), u32, u32, P, P], i32),
     "svo_raycast_camera_beam": ([ctypes.POINTER(OctreeC), ctypes.POINTER(CameraC), u32, u32, P, P, P, P], i32),
     "svo_occlude": ([ctypes.POINTER(OctreeC), P, u32, P, P], i32),
+    "svo_load_obj": ([ctypes.c_char_p, ctypes.POINTER(P), ctypes.POINTER(u32)], i32),
+    "svo_free_host": ([P], None),
+    "svo_octree_write_host": ([P, u32, u32, ctypes.c_char_p], i32),
+    "svo_octree_read_host": ([ctypes.c_char_p, ctypes.POINTER(P), ctypes.POINTER(u32), ctypes.POINTER(u32)], i32),
+    "svo_octree_save": ([ctypes.POINTER(OctreeC), ctypes.c_char_p, P], i32),
+    "svo_octree_load": ([ctypes.c_char_p, ctypes.POINTER(OctreeC), P], i32),
     "svo_tune_set": ([u32, u32, ctypes.c_int32, ctypes.c_int32], i32),
     "svo_tune_get": ([u32, u32, u64], i32),
     "svo_tune_size_class": ([u64], u32),

@@ -559,6 +559,58 @@ class Server:
         return {name: int(getattr(st, name)) for name, _ in _lib.ServerStats._fields_}
 
 
+# ------------------------------------------------------------------------------------------- files
+def load_obj(path: str) -> np.ndarray:
+    """Scene::load_meshes for the engine (svo_load_obj): triangles (TRIANGLE_DTYPE) in [0,1]^3 with the
+    reference's normalisation and per-material albedo."""
+    lib = _lib.load()
+    ptr, n = ctypes.c_void_p(), _lib.u32()
+    _lib.check(lib.svo_load_obj(path.encode(), ctypes.byref(ptr), ctypes.byref(n)))
+    try:
+        raw = ctypes.string_at(ptr, n.value * TRIANGLE_DTYPE.itemsize)
+    finally:
+        lib.svo_free_host(ptr)
+    return np.frombuffer(raw, TRIANGLE_DTYPE).copy()
+
+
+def write_octree_file(words: np.ndarray, level: int, path: str) -> None:
+    w = np.ascontiguousarray(words, np.uint32)
+    _lib.check(_lib.load().svo_octree_write_host(w.ctypes.data_as(ctypes.c_void_p), len(w), int(level), path.encode()))
+
+
+def read_octree_file(path: str) -> tuple[np.ndarray, int]:
+    lib = _lib.load()
+    ptr, rng, lvl = ctypes.c_void_p(), _lib.u32(), _lib.u32()
+    _lib.check(lib.svo_octree_read_host(path.encode(), ctypes.byref(ptr), ctypes.byref(rng), ctypes.byref(lvl)))
+    try:
+        words = np.frombuffer(ctypes.string_at(ptr, rng.value * 4), np.uint32).copy()
+    finally:
+        lib.svo_free_host(ptr)
+    return words, int(lvl.value)
+
+
+class _OwnedPool:
+    """A library-owned device pool (svo_octree_load) released with svo_octree_destroy."""
+
+    def __init__(self, oc: _lib.OctreeC):
+        self.oc = oc
+
+    def __del__(self):
+        if _lib._lib is not None and self.oc.words:
+            _lib._lib.svo_octree_destroy(ctypes.byref(self.oc), None)
+
+
+def save_octree(octree: Octree, path: str, stream=None) -> None:
+    oc = octree.c_struct()
+    _lib.check(_lib.load().svo_octree_save(ctypes.byref(oc), path.encode(), _stream(stream)))
+
+
+def load_octree(path: str, stream=None) -> Octree:
+    oc = _lib.OctreeC()
+    _lib.check(_lib.load().svo_octree_load(path.encode(), ctypes.byref(oc), _stream(stream)))
+    return Octree.FromView(oc, owner=_OwnedPool(oc))
+
+
 # ------------------------------------------------------------------------------------------- functional
 def voxelize(triangles, level: int, stream=None) -> torch.Tensor:
     return Voxelizer.Create(triangles, level, stream).GetVoxelFragmentList()

@@ -29,6 +29,7 @@ UNITS = {
     "noalloc.cu": [],
     "batch.cu": [],
     "serve.cu": [],
+    "io.cu": [],
 }
 HEADERS = ["common.cuh", "svo_internal.h"]
 

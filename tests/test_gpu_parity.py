@@ -476,3 +476,32 @@ def test_occlusion_golden_and_oracle(cuda, golden_dir):
     got2 = api.OctreeTracer.Create(oc).Occlude(api.to_device(r2)).cpu().numpy().view(np.uint32)
     assert np.array_equal(got2, oracle.occlude(pool2, s.level, r2))
     assert not got2[:50].any()
+
+
+# ------------------------------------------------------------------------------------------- files
+def test_octree_save_load_and_obj_pipeline(cuda, tmp_path):
+    """An OBJ loaded with the reference's normalisation runs the whole path; the octree saved to a file
+    and loaded back traces identically."""
+    api = _api()
+    s = scenes.plain_256()
+    lines = ["mtllib m.mtl", "usemtl a"]
+    verts = s.tris["v"].reshape(-1, 3)[: 3 * 4000] * 7.0 - 2.0  # any frame: the loader normalises it
+    lines += [f"v {x:.7g} {y:.7g} {z:.7g}" for x, y, z in verts]
+    lines += [f"f {3 * i + 1} {3 * i + 2} {3 * i + 3}" for i in range(len(verts) // 3)]
+    (tmp_path / "m.obj").write_text("\n".join(lines) + "\n")
+    (tmp_path / "m.mtl").write_text("newmtl a\nKd 0.5 0.75 1.0\n")
+    tris = api.load_obj(str(tmp_path / "m.obj"))
+    level = 7
+    frags = gpu_voxelize(tris, level)
+    ref_frags = oracle.voxelize(tris, level)
+    assert_same_fragments(frags, ref_frags)
+    octree, words = gpu_build(frags, level)
+    assert np.array_equal(words, oracle.build_octree(ref_frags, level))
+    path = str(tmp_path / "m.svo")
+    api.save_octree(octree, path)
+    loaded = api.load_octree(path)
+    assert loaded.GetLevel() == level and np.array_equal(loaded.words().cpu().numpy().view(np.uint32), words)
+    g = np.random.default_rng(2)
+    o, d = scenes.random_rays(g, 3000)
+    rays = rays_from_arrays(o, d)
+    assert np.array_equal(gpu_trace(loaded, rays), gpu_trace(octree, rays))
