@@ -118,7 +118,9 @@ def algorithmic_bytes(kernel: str, w: dict) -> float | None:
         "vox_classify_scan": 48.0 * T + 12.0 * T,     # triangles in, offsets out
         "dense_mark": 8.0 * F,                        # the fragment list, read once
         "build_tag": 8.0 * F,                         # one sparse level: the fragment list
-        "build_leaf": 8.0 * F + 8.0 * F,              # fragments in, one 8 B accumulator update each
+        "build_leaf": 8.0 * F + 4.0 * leaf_words,     # items in, leaf words out (sparse-parent octrees)
+        "build_leaf_windows": 8.0 * F + 4.0 * leaf_words,  # items in, leaf words out
+        "bucket_scatter": 16.0 * F,                   # fragment in, bucketed item out
         "build_finalize": 12.0 * leaf_words,          # 8 B accumulator in, 4 B leaf word out
         "dense_write": 4.0 * (w["range_words"] - leaf_words),  # interior words out
         "march_camera": n * (32.0 + 4.0 * k),         # hit out + node words fetched (rays made in-kernel)
@@ -128,7 +130,8 @@ def algorithmic_bytes(kernel: str, w: dict) -> float | None:
 
 
 # ncu kernel names of the profile labels whose captures are committed under profiles/
-PROFILE_FILES = {"build_leaf": "build_leaf", "march_camera": "march_kernel", "vox_emit_units": "vox_emit_units"}
+PROFILE_FILES = {"build_leaf_windows": "build_leaf_windows", "bucket_scatter": "bucket_scatter",
+                 "march_camera": "march_kernel", "vox_emit_units": "vox_emit_units"}
 
 
 def profiled_traffic(label: str, workload: str) -> dict:
@@ -247,6 +250,9 @@ def engine_arm(args, rank: int, world: int, device) -> dict:
         ach = alg / (dom_launch_ms * 1e-3) / 1e9
         roofline.update({"achieved": ach, "frac": ach / peaks["hbm_gbs"], "algorithmic_bytes_per_launch": alg})
     roofline.update(profiled_traffic(dom_name, args.workload))
+    if dom_name.startswith("march"):
+        roofline["limiter"] = ("instruction issue: node words stay in L1/L2, DRAM idle (ncu, "
+                               "profiles/march_kernel_room_1024.md); the HBM fraction is low by construction")
 
     stages = {
         "voxelize_ms": vox_ms, "build_ms": build_ms, "march_ms": march_ms,
