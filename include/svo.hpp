@@ -11,6 +11,11 @@
 //   Octree::Update(pool, builder)   src/Octree.cpp:22-35 svo::Octree::Update(builder)
 //   OctreeTracer::CmdDrawPipeline(cb, frame) src/OctreeTracer.cpp:213-246
 //                                                        svo::OctreeTracer::CmdDrawPipeline(hits, stream)
+//   OctreeTracer::CmdBeamRenderPass(cb, frame) :183-211  svo::OctreeTracer::CmdBeamRenderPass(beam, stream)
+//                                                        (+ CmdDrawPipelineBeam, CmdOcclude)
+//   Scene::load_meshes(filename)   src/Scene.cpp:36-147  svo::LoadObj(path)
+//   (one mesh per loader run)  src/LoaderThread.cpp:43  svo::BatchBuilder (many meshes per launch)
+//   (one octree per frame)  src/Application.cpp:130-159 svo::Server (resident octrees, batched requests)
 //
 // Header-only; needs no CUDA headers.  Link against libsvo.so.  Errors throw svo::Error (the reference
 // logs and continues, e.g. src/Octree.cpp:30-33).  A `stream` is a cudaStream_t passed as void*.
@@ -183,8 +188,32 @@ private:
 
 class Octree {
 public:
+	Octree() = default;
+	Octree(const Octree &) = delete;
+	Octree &operator=(const Octree &) = delete;
+	~Octree() {
+		if (owned_) svo_octree_destroy(&octree_, nullptr);
+	}
 	static std::shared_ptr<Octree> Create() { return std::make_shared<Octree>(); }
+	// An octree file (svo_octree_load); the pool is owned and released with the object.
+	static std::shared_ptr<Octree> Load(const std::string &path, void *stream = nullptr) {
+		auto o = std::make_shared<Octree>();
+		Check(svo_octree_load(path.c_str(), &o->octree_, stream));
+		o->owned_ = true;
+		return o;
+	}
+	// A view of a pool owned elsewhere (a batcher's or a server's); `keep` keeps its owner alive.
+	static std::shared_ptr<Octree> FromView(const svo_octree &view, std::shared_ptr<void> keep = nullptr) {
+		auto o = std::make_shared<Octree>();
+		o->octree_ = view;
+		o->octree_.owned = 0;
+		o->keep_ = std::move(keep);
+		return o;
+	}
+	void Save(const std::string &path, void *stream = nullptr) const { Check(svo_octree_save(&octree_, path.c_str(), stream)); }
 	void Update(const std::shared_ptr<OctreeBuilder> &builder) {
+		if (owned_) svo_octree_destroy(&octree_, nullptr);
+		owned_ = false;
 		const uint64_t range = builder->GetOctreeRange();
 		builder_ = builder;
 		octree_.words = builder->GetOctree();
@@ -201,7 +230,9 @@ public:
 
 private:
 	std::shared_ptr<OctreeBuilder> builder_;
+	std::shared_ptr<void> keep_;
 	svo_octree octree_{};
+	bool owned_ = false;
 };
 
 // The tracer without a swapchain: one hit (svo_hit, 32 B) per pixel in a device buffer.
@@ -224,6 +255,19 @@ public:
 	void CmdTrace(const svo_ray *rays_device, uint32_t n, svo_hit *hits_device, void *stream = nullptr) const {
 		Check(svo_raycast(&octree_->Get(), rays_device, n, hits_device, nullptr, stream));
 	}
+	// OctreeTracer::CmdBeamRenderPass (src/OctreeTracer.cpp:183-211): svo_beam_texels(width, height) floats.
+	void CmdBeamRenderPass(float *beam_device, void *stream = nullptr) const {
+		Check(svo_beam_prepass(&octree_->Get(), &camera_, width_, height_, beam_device, stream));
+	}
+	// CmdDrawPipeline with the beam enabled (beam_device NULL: the pre-pass runs inside).
+	void CmdDrawPipelineBeam(const float *beam_device, svo_hit *hits_device, void *stream = nullptr) const {
+		Check(svo_raycast_camera_beam(&octree_->Get(), &camera_, width_, height_, beam_device, hits_device, nullptr,
+		                              stream));
+	}
+	// Octree_RayMarchOcclude per ray (shadow rays): occluded[i] = 1 when ray i hits a leaf.
+	void CmdOcclude(const svo_ray *rays_device, uint32_t n, uint32_t *occluded_device, void *stream = nullptr) const {
+		Check(svo_occlude(&octree_->Get(), rays_device, n, occluded_device, stream));
+	}
 	uint32_t GetWidth() const { return width_; }
 	uint32_t GetHeight() const { return height_; }
 
@@ -231,6 +275,108 @@ private:
 	std::shared_ptr<Octree> octree_;
 	svo_camera camera_{};
 	uint32_t width_ = 0, height_ = 0;
+};
+
+// Scene::load_meshes for the engine's triangle format (svo_load_obj).
+inline std::vector<svo_triangle> LoadObj(const std::string &path) {
+	svo_triangle *t = nullptr;
+	uint32_t n = 0;
+	Check(svo_load_obj(path.c_str(), &t, &n));
+	std::vector<svo_triangle> out(t, t + n);
+	svo_free_host(t);
+	return out;
+}
+
+// Many meshes voxelized and built together (svo_batcher); per mesh identical to Voxelizer + OctreeBuilder.
+class BatchBuilder {
+public:
+	static std::shared_ptr<BatchBuilder> Create() {
+		auto b = std::make_shared<BatchBuilder>();
+		Check(svo_batcher_create(&b->h_));
+		return b;
+	}
+	BatchBuilder() = default;
+	BatchBuilder(const BatchBuilder &) = delete;
+	BatchBuilder &operator=(const BatchBuilder &) = delete;
+	~BatchBuilder() { svo_batcher_destroy(h_); }
+	// meshes: device triangles and levels; blocks for the count and result readbacks.
+	void Build(const std::vector<svo_batch_mesh> &meshes, void *stream = nullptr) {
+		Check(svo_batcher_build(h_, meshes.data(), (uint32_t)meshes.size(), stream));
+	}
+	uint32_t GetMeshCount() const { return svo_batcher_meshes(h_); }
+	// View of mesh i's octree in the shared pool, valid until the next Build (holds the batcher alive).
+	static std::shared_ptr<Octree> GetOctree(const std::shared_ptr<BatchBuilder> &self, uint32_t i) {
+		svo_octree o;
+		Check(svo_batcher_result(self->h_, i, nullptr, &o, nullptr));
+		return Octree::FromView(o, self);
+	}
+	svo_build_info GetInfo(uint32_t i) const {
+		svo_build_info info;
+		Check(svo_batcher_result(h_, i, nullptr, nullptr, &info));
+		return info;
+	}
+
+private:
+	svo_batcher *h_ = nullptr;
+};
+
+// Resident octrees and continuous batching of trace / rebuild requests (svo_server).
+class Server {
+public:
+	static std::shared_ptr<Server> Create(const svo_server_config &cfg = svo_server_config{}) {
+		auto s = std::make_shared<Server>();
+		Check(svo_server_create(&cfg, &s->h_));
+		return s;
+	}
+	Server() = default;
+	Server(const Server &) = delete;
+	Server &operator=(const Server &) = delete;
+	~Server() { svo_server_destroy(h_); }
+	uint32_t BuildScene(const svo_triangle *tris_device, uint32_t n, uint32_t level) {
+		uint32_t id;
+		Check(svo_server_build_scene(h_, tris_device, n, level, &id));
+		return id;
+	}
+	uint32_t AddOctree(const std::shared_ptr<Octree> &octree) {
+		uint32_t id;
+		Check(svo_server_add_octree(h_, &octree->Get(), &id));
+		return id;
+	}
+	// Camera request: hits_host (page-locked for full overlap) receives 2 * n_primary hits.
+	uint64_t SubmitCamera(uint32_t scene, const svo_camera &cam, uint32_t width, uint32_t height, uint32_t n_primary,
+	                      uint64_t seed, svo_hit *hits_host) {
+		svo_trace_request r{};
+		r.scene = scene, r.mode = SVO_REQUEST_CAMERA, r.camera = cam;
+		r.width = width, r.height = height, r.n_primary = n_primary, r.hits = hits_host, r.seed = seed;
+		uint64_t t;
+		Check(svo_server_submit_trace(h_, &r, &t));
+		return t;
+	}
+	uint64_t SubmitRays(uint32_t scene, const svo_ray *rays_host, uint32_t n, svo_hit *hits_host) {
+		svo_trace_request r{};
+		r.scene = scene, r.mode = SVO_REQUEST_RAYS, r.rays = rays_host, r.n_rays = n, r.hits = hits_host;
+		uint64_t t;
+		Check(svo_server_submit_trace(h_, &r, &t));
+		return t;
+	}
+	uint64_t SubmitRebuild(uint32_t scene, const svo_triangle *tris_device, uint32_t n, uint32_t level) {
+		uint64_t t;
+		Check(svo_server_submit_rebuild(h_, scene, tris_device, n, level, &t));
+		return t;
+	}
+	svo_request_result Wait(uint64_t ticket, int timeout_ms = -1) {
+		svo_request_result r{};
+		Check(svo_server_wait(h_, ticket, timeout_ms, &r));
+		return r;
+	}
+	svo_server_stats Stats() const {
+		svo_server_stats st{};
+		svo_server_get_stats(h_, &st);
+		return st;
+	}
+
+private:
+	svo_server *h_ = nullptr;
 };
 
 } // namespace svo

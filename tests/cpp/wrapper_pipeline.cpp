@@ -2,7 +2,9 @@
 // thread and tracer do (src/LoaderThread.cpp:52-75, src/Application.cpp:144-152):
 //   Scene -> Voxelizer -> OctreeBuilder -> CmdBuild -> Octree::Update -> OctreeTracer::CmdDrawPipeline
 // Usage: wrapper_pipeline <triangles.bin> <level> <camera.bin (16 floats)> <width> <height> <out prefix>
-// Writes <out>.frags (uint64), <out>.pool (uint32, range words) and <out>.hits (svo_hit).
+// Writes <out>.frags (uint64), <out>.pool (uint32, range words), <out>.hits (svo_hit) and <out>.beam
+// (float beam image), and checks in-process that a two-mesh BatchBuilder, a Server camera request and an
+// octree file round trip agree with the single-mesh classes.
 #include <cstdio>
 #include <fstream>
 #include <iterator>
@@ -61,6 +63,55 @@ int main(int argc, char **argv) {
 		write_file(out + ".frags", frags);
 		write_file(out + ".pool", pool);
 		write_file(out + ".hits", h);
+
+		// beam pre-pass (the reference tracer's beam image)
+		svo::DeviceBuffer beam(sizeof(float) * svo_beam_texels(width, height), nullptr);
+		tracer->CmdBeamRenderPass((float *)beam.get());
+		std::vector<float> bimg(svo_beam_texels(width, height));
+		svo::Check(svo_download(bimg.data(), beam.get(), bimg.size() * 4, 1, nullptr));
+		write_file(out + ".beam", bimg);
+
+		// a two-mesh batch equals the single builds
+		auto batch = svo::BatchBuilder::Create();
+		batch->Build({{scene->GetTriangles(), scene->GetTriangleCount(), level},
+		              {scene->GetTriangles(), scene->GetTriangleCount(), level - 1}});
+		auto b0 = svo::BatchBuilder::GetOctree(batch, 0);
+		std::vector<uint32_t> bpool(b0->GetRange() / 4);
+		svo::Check(svo_download(bpool.data(), b0->GetBuffer(), b0->GetRange(), 1, nullptr));
+		if (bpool != pool) {
+			std::fprintf(stderr, "batch octree differs from the single build\n");
+			return 3;
+		}
+		auto v1 = svo::Voxelizer::Create(scene, level - 1);
+		auto ob1 = svo::OctreeBuilder::Create(v1);
+		ob1->CmdBuild();
+		if (ob1->GetOctreeRange() != svo::BatchBuilder::GetOctree(batch, 1)->GetRange()) {
+			std::fprintf(stderr, "batch range differs from the single build\n");
+			return 3;
+		}
+
+		// a served camera request equals the tracer's frame (primary hits)
+		{
+			auto server = svo::Server::Create();
+			const uint32_t sid = server->AddOctree(octree);
+			std::vector<svo_hit> sh(2 * (size_t)width * height);
+			const uint64_t t = server->SubmitCamera(sid, cam, width, height, width * height, 7, sh.data());
+			server->Wait(t);
+			if (std::memcmp(sh.data(), h.data(), h.size() * sizeof(svo_hit)) != 0) {
+				std::fprintf(stderr, "served hits differ from the tracer's\n");
+				return 4;
+			}
+		}
+
+		// octree file round trip
+		octree->Save(out + ".svo");
+		auto loaded = svo::Octree::Load(out + ".svo");
+		std::vector<uint32_t> lpool(loaded->GetRange() / 4);
+		svo::Check(svo_download(lpool.data(), loaded->GetBuffer(), loaded->GetRange(), 1, nullptr));
+		if (lpool != pool || loaded->GetLevel() != level) {
+			std::fprintf(stderr, "loaded octree differs\n");
+			return 5;
+		}
 		std::printf("fragments %u range %llu words levels", voxelizer->GetVoxelFragmentCount(),
 		            (unsigned long long)pool.size());
 		const svo_build_info &info = builder->GetInfo();

@@ -49,3 +49,5 @@ def test_cpp_wrapper_pipeline_matches_oracle(tmp_path, cuda):
     ref_pool = oracle.build_octree(ref_frags, s.level)
     assert np.array_equal(pool, ref_pool)
     assert np.array_equal(hits, oracle.raycast(ref_pool, s.level, oracle.camera_rays(s.camera, s.width, s.height)))
+    beam = np.fromfile(out + ".beam", np.float32)
+    assert np.array_equal(beam, oracle.beam(ref_pool, s.level, s.camera, s.width, s.height).reshape(-1))
