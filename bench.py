@@ -34,12 +34,18 @@ WORKLOADS = {
     "room_1024": "plain voxelize+build+march at 2^10: room shell, 200 cylinders, 210,932 clutter tris "
                  "(262,144 tris), 1920x1080 primary rays from a seeded interior camera",
     "plain_256": "plain voxelize+build+march at 2^8: icosphere (20,480 tris) + 64 boxes, 64x64 primary rays",
-    "clusters_4096": "plain voxelize+build+march at 2^12: ~10M tris in 4 clusters, 3840x2160 primary rays",
+    "clusters_4096": "plain voxelize+build+march at 2^12: ~10M tris in 4 clusters, 3840x2160 primary rays plus one "
+                     "diffuse bounce per hit (its octree needs 1.95G node words: beyond the 30-bit pointer format, "
+                     "reported as SVO_ERR_CAPACITY)",
+    "clusters_4096_4m": "plain voxelize+build+march at 2^12: the 4-cluster distribution with 4M tris (the largest "
+                        "that fits the 30-bit pointer format), 3840x2160 primary rays plus one diffuse bounce per hit",
 }
 
 
 def make_scene(name: str):
     from sparsevoxeloctree_gb300 import scenes
+    if name == "clusters_4096_4m":
+        return scenes.clusters_4096(n_tris=4_000_000)
     return {"room_1024": scenes.room_1024, "plain_256": scenes.plain_256, "clusters_4096": scenes.clusters_4096}[name]()
 
 
@@ -178,19 +184,33 @@ def engine_arm(args, rank: int, world: int, device) -> dict:
     info = builder.GetInfo()
     hit_np = api.hits_numpy(hits)
 
+    bounce_rays = bounce_hits = None
+    if scene.bounce:  # one cosine-weighted diffuse bounce per primary hit, traced in the same step
+        bounce_rays = api.OctreeTracer.Bounce(hits, scene.seed)
+        bounce_hits = tracer.Trace(bounce_rays)
+        torch.cuda.synchronize()
+
     def step():
         vox.CmdVoxelize()
         builder.CmdBuild()
         tracer.CmdDrawPipeline(hits)
+        if scene.bounce:
+            api.OctreeTracer.Bounce(hits, scene.seed, bounce_rays)
+            tracer.Trace(bounce_rays, bounce_hits)
 
     tuning = None
     if not args.no_autotune:  # launch parameters measured on this workload before timing
         from sparsevoxeloctree_gb300 import autotune
         t_tune = time.perf_counter()
-        tuning = {"emit": autotune.tune_voxelize(vox), "build": autotune.tune_build(builder),
-                  "march": autotune.tune_march(tracer, hits)}
+        tuning = {"emit": autotune.tune_voxelize(vox), "build": autotune.tune_build(builder)}
+        if scene.bounce:  # primary and bounce launches share a table entry (same level and ray count): tuned together
+            tuning["march"] = autotune._sweep(
+                ["march_block", "march_rays_per_lane", "march_stack_shared"], scene.level, n_rays,
+                lambda: (tracer.CmdDrawPipeline(hits), tracer.Trace(bounce_rays, bounce_hits)))
+        else:
+            tuning["march"] = autotune.tune_march(tracer, hits)
         tuning = {k: {"best": v["best"], "best_ms": v["best_ms"], "level": v["level"], "size_class": v["size_class"],
-                      "candidates": len(v["trials"])} for k, v in tuning.items()}
+                      "trials": [[t["params"], round(t["ms"], 4)] for t in v["trials"]]} for k, v in tuning.items()}
         tuning["seconds"] = time.perf_counter() - t_tune
 
     flush_buf = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=device)
@@ -234,7 +254,10 @@ def engine_arm(args, rank: int, world: int, device) -> dict:
     def stage_ms(prefixes):
         return sum(v["ms"] for k, v in profile.items() if k.startswith(prefixes)) / args.steps
 
-    vox_ms, build_ms, march_ms = stage_ms(("vox_",)), stage_ms(("build_", "dense_")), stage_ms(("march_",))
+    vox_ms = stage_ms(("vox_",))
+    build_ms = stage_ms(("build_", "dense_", "bucket_", "leaf_window"))
+    march_ms = stage_ms(("march_", "bounce_"))
+    n_traced = n_rays * (2 if scene.bounce else 1)
     leaf_words = 8 if scene.level == 1 else 8 * info["level_nodes"][scene.level - 2]
     wl = {"fragments": F, "triangles": T, "level": scene.level, "rays": n_rays, "fetches_per_ray": fetches / n_rays,
           "range_words": info["range_words"], "leaf_words": leaf_words}
@@ -258,7 +281,8 @@ def engine_arm(args, rank: int, world: int, device) -> dict:
         "voxelize_ms": vox_ms, "build_ms": build_ms, "march_ms": march_ms,
         "svo_build_ms": vox_ms + build_ms,
         "mfragments_per_s": F / (vox_ms * 1e-3) / 1e6 if vox_ms else None,
-        "grays_per_s": n_rays / (march_ms * 1e-3) / 1e9 if march_ms else None,
+        "grays_per_s": n_traced / (march_ms * 1e-3) / 1e9 if march_ms else None,
+        "rays_traced_per_step": n_traced,
         "voxelize_gbs": (48.0 * T + 8.0 * F) / (vox_ms * 1e-3) / 1e9 if vox_ms else None,
         "build_gbs": (8.0 * F * scene.level + 16.0 * info["range_words"]) / (build_ms * 1e-3) / 1e9 if build_ms else None,
         "march_gbs": n_rays * (24.0 + 32.0 + 4.0 * fetches / n_rays) / (march_ms * 1e-3) / 1e9 if march_ms else None,
@@ -310,9 +334,11 @@ def e2e_arm(args, scene, tris_host, device, world) -> dict:
 
     lib = _lib.load()
     n = scene.n_rays
-    hits_host = torch.empty(n * HIT_DTYPE.itemsize, dtype=torch.uint8).pin_memory()
+    n_out = n * (2 if scene.bounce else 1)  # primary hits, then bounce hits
+    hits_host = torch.empty(n_out * HIT_DTYPE.itemsize, dtype=torch.uint8).pin_memory()
     tris_dev = torch.empty_like(tris_host, device=device)
-    hits_dev = torch.empty(n * HIT_DTYPE.itemsize, dtype=torch.uint8, device=device)
+    hits_dev = torch.empty(n_out * HIT_DTYPE.itemsize, dtype=torch.uint8, device=device)
+    rays_dev = torch.empty(n * 24, dtype=torch.uint8, device=device) if scene.bounce else None
     cam = api.camera_struct(scene.camera)
     s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     T = len(scene.tris)
@@ -325,6 +351,11 @@ def e2e_arm(args, scene, tris_host, device, world) -> dict:
         _lib.check(lib.svo_build_fraglist(ctypes.byref(fl), ctypes.byref(oc), None, s))
         _lib.check(lib.svo_raycast_camera(ctypes.byref(oc), ctypes.byref(cam), scene.width, scene.height,
                                           ctypes.c_void_p(hits_dev.data_ptr()), None, s))
+        if scene.bounce:
+            _lib.check(lib.svo_bounce_rays(ctypes.c_void_p(hits_dev.data_ptr()), n, scene.seed,
+                                           ctypes.c_void_p(rays_dev.data_ptr()), s))
+            _lib.check(lib.svo_raycast(ctypes.byref(oc), ctypes.c_void_p(rays_dev.data_ptr()), n,
+                                       ctypes.c_void_p(hits_dev.data_ptr() + n * HIT_DTYPE.itemsize), None, s))
         hits_host.copy_(hits_dev, non_blocking=True)
         lib.svo_fraglist_destroy(ctypes.byref(fl), s)
         lib.svo_octree_destroy(ctypes.byref(oc), s)
@@ -624,7 +655,9 @@ def cpu_baseline(scene, per_step: bool) -> dict:
     pool = oracle.build_octree(frags, scene.level)
     t2 = time.perf_counter()
     rays = oracle.camera_rays(scene.camera, scene.width, scene.height)
-    oracle.raycast(pool, scene.level, rays)
+    hits = oracle.raycast(pool, scene.level, rays)
+    if scene.bounce:
+        oracle.raycast(pool, scene.level, oracle.bounce_rays(hits, scene.seed))
     t3 = time.perf_counter()
     ms = (t3 - t0) * 1e3
     return {"value": ms, "unit": "ms", "cores": oracle.threads(), "kind": "port",

@@ -169,7 +169,8 @@ size_t svo_profile_summary(char *buf, size_t cap);
  * being that of its work items (fragments, triangles or rays): class 0 below 65,536, then one class per
  * factor 4, class 7 from 2^30.  Results do not depend on these values, only the speed does. */
 #define SVO_TUNE_MARCH_BLOCK 0u         /* threads per march block: 64, 128 (default), 256 */
-#define SVO_TUNE_MARCH_RAYS_PER_LANE 1u /* rays a lane takes per ticket: 1 (default), 2 */
+#define SVO_TUNE_MARCH_RAYS_PER_LANE 1u /* rays a lane takes per warp ticket: 1 (default), 2; or 0: persistent
+                                           refill (each lane takes a new ray as soon as its ray ends) */
 #define SVO_TUNE_MARCH_STACK_SHARED 2u  /* traversal stack in shared memory (1, default) or local memory (0) */
 #define SVO_TUNE_SWEEP_BLOCKS 3u        /* blocks per SM of the build's fragment sweeps (default 16) */
 #define SVO_TUNE_LEAF_BLOCKS 4u         /* blocks per SM of the build's leaf stage (default 6) */

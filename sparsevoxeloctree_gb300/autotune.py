@@ -4,8 +4,8 @@ The library keeps one value per (parameter, octree level, size class of the laun
 every launch reads it (svo_tune_set / svo_tune_get, include/svo.h).  This module measures the candidate
 values on a real workload with CUDA events and sets the fastest:
 
-  march   threads per block (64 / 128 / 256) x rays per lane per ticket (1 / 2) x stack in shared or
-          local memory, exhaustively (12 variants), on the workload's ray launch;
+  march   threads per block (64 / 128 / 256) x rays per lane per ticket (1 / 2, or persistent refill) x
+          stack in shared or local memory, exhaustively (18 variants), on the workload's ray launch;
   build   blocks per SM of the fragment sweeps x blocks per SM of the leaf stage, on a build;
   emit    blocks per SM of the voxelizer's emission, on a voxelize pass.
 
@@ -25,7 +25,7 @@ from . import _lib
 
 PARAMS = {  # name -> (parameter id, candidate values)
     "march_block": (0, (64, 128, 256)),
-    "march_rays_per_lane": (1, (1, 2)),
+    "march_rays_per_lane": (1, (1, 2, 0)),  # 0: persistent refill
     "march_stack_shared": (2, (1, 0)),
     "sweep_blocks": (3, (8, 16, 32)),
     "leaf_blocks": (4, (4, 6, 8)),

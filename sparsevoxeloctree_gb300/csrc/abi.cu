@@ -126,7 +126,7 @@ static void tune_init() {
 static bool tune_valid(uint32_t param, int v) {
 	switch (param) {
 	case kTuneMarchBlock: return v == 64 || v == 128 || v == 256;
-	case kTuneMarchRays: return v == 1 || v == 2;
+	case kTuneMarchRays: return v == 0 || v == 1 || v == 2;
 	case kTuneMarchShared: return v == 0 || v == 1;
 	default: return v >= 1 && v <= 64;
 	}

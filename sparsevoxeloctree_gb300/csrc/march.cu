@@ -36,159 +36,185 @@ struct MarchOut {
 	uint32_t voxel_lo, voxel_hi; // packed uint16 voxel[3] and flags, as in svo_hit
 };
 
-// One ray; `stack` points at this thread's stack: a column of a shared [level][thread] array (STRIDE =
-// threads per block) or a private array in local memory (STRIDE = 1).
+// State of one ray's leaf march (Octree_RayMarchLeaf, shader/octree.glsl:179-340), so a lane can run a
+// ray as init + steps + finish and take a new ray as soon as its current one ends.  `stack` points at
+// the lane's stack: a column of a shared [level][thread] array (STRIDE = threads per block) or a private
+// array in local memory (STRIDE = 1).
+struct RayState {
+	float o[3], d[3], coef[3], bias[3], pos[3];
+	float t_min, t_max, h, scale_exp2;
+	uint32_t parent, cur, idx, scale, oct_mask, iter, nfetch, min_scale;
+	bool aborted, none;
+};
+
 template <int STRIDE>
-SVO_DEV void march_ray(const uint32_t *__restrict__ pool, uint32_t range, uint32_t level, const float o[3],
-                       const float dir[3], uint32_t *stack, MarchOut &out, uint32_t &nfetch, uint32_t *status) {
-	nfetch = 0;
-	if (dir[0] == 0.0f && dir[1] == 0.0f && dir[2] == 0.0f) { // no ray (miss of a previous bounce)
+SVO_DEV void ray_init(RayState &s, const float o[3], const float dir[3], uint32_t level, uint32_t *stack) {
+	s.nfetch = 0;
+	s.iter = 0;
+	s.aborted = false;
+	s.none = dir[0] == 0.0f && dir[1] == 0.0f && dir[2] == 0.0f; // no ray (miss of a previous bounce)
+#pragma unroll
+	for (int k = 0; k < 3; ++k) s.o[k] = o[k];
+	if (s.none) {
+		s.scale = 0xffffffffu; // ends at once
+		return;
+	}
+	for (uint32_t k = 0; k < level; ++k) stack[k * STRIDE] = 0u;
+#pragma unroll
+	for (int k = 0; k < 3; ++k) s.d[k] = eps_clamp(dir[k]);
+#pragma unroll
+	for (int k = 0; k < 3; ++k) {
+		s.coef[k] = 1.0f / -fabsf(s.d[k]);
+		s.bias[k] = s.coef[k] * o[k];
+	}
+	s.oct_mask = 0;
+#pragma unroll
+	for (int k = 0; k < 3; ++k)
+		if (s.d[k] > 0.0f) {
+			s.oct_mask ^= 1u << k;
+			s.bias[k] = 3.0f * s.coef[k] - s.bias[k];
+		}
+	s.t_min = max_glsl(max_glsl(2.0f * s.coef[0] - s.bias[0], 2.0f * s.coef[1] - s.bias[1]), 2.0f * s.coef[2] - s.bias[2]);
+	s.t_max = min_glsl(min_glsl(s.coef[0] - s.bias[0], s.coef[1] - s.bias[1]), s.coef[2] - s.bias[2]);
+	s.t_min = max_glsl(s.t_min, 0.0f);
+	s.h = s.t_max;
+	s.parent = 0, s.cur = 0, s.idx = 0;
+#pragma unroll
+	for (int k = 0; k < 3; ++k) {
+		s.pos[k] = 1.0f;
+		if (1.5f * s.coef[k] - s.bias[k] > s.t_min) {
+			s.idx ^= 1u << k;
+			s.pos[k] = 1.5f;
+		}
+	}
+	s.scale = SVO_STACK_SIZE - 1;
+	s.scale_exp2 = 0.5f;
+	s.min_scale = SVO_STACK_SIZE - level; // deepest scale a valid tree reaches
+}
+
+// One iteration of the march loop; returns true when the ray has ended (the loop of the shader breaks or
+// its condition fails).  A malformed pool (pointer outside the range, interior word below the octree
+// level, iteration bound) ends the ray as an aborted miss and sets kStatusMalformed.
+template <int STRIDE>
+SVO_DEV bool ray_step(RayState &s, const uint32_t *__restrict__ pool, uint32_t range, uint32_t *stack,
+                      uint32_t *status) {
+	if (s.scale >= SVO_STACK_SIZE) return true;
+	if (s.iter >= SVO_MARCH_MAX_ITER) {
+		s.aborted = true;
+		return true;
+	}
+	++s.iter;
+	if (s.cur == 0u) {
+		const uint32_t w = s.parent + (s.idx ^ s.oct_mask);
+		if (w >= range) {
+			atomicOr(status, kStatusMalformed);
+			s.aborted = true;
+			s.scale = 0xffffffffu;
+			return true;
+		}
+		s.cur = __ldg(pool + w);
+		++s.nfetch;
+	}
+	float tc[3];
+#pragma unroll
+	for (int k = 0; k < 3; ++k) tc[k] = s.pos[k] * s.coef[k] - s.bias[k];
+	const float tc_max = min_glsl(min_glsl(tc[0], tc[1]), tc[2]);
+
+	if ((s.cur & 0x80000000u) != 0u && s.t_min <= s.t_max) {
+		const float half = s.scale_exp2 * 0.5f;
+		float t_center[3];
+#pragma unroll
+		for (int k = 0; k < 3; ++k) t_center[k] = half * s.coef[k] + tc[k];
+		if ((s.cur & 0x40000000u) != 0u) return true; // leaf
+		if (s.scale <= s.min_scale) {                  // interior node below the leaf level: malformed pool
+			atomicOr(status, kStatusMalformed);
+			s.aborted = true;
+			s.scale = 0xffffffffu;
+			return true;
+		}
+		if (tc_max < s.h) stack[(SVO_STACK_SIZE - 1 - s.scale) * STRIDE] = s.parent; // push
+		s.h = tc_max;
+		s.parent = s.cur & 0x3fffffffu;
+		s.idx = 0;
+		--s.scale;
+		s.scale_exp2 = half;
+#pragma unroll
+		for (int k = 0; k < 3; ++k)
+			if (t_center[k] > s.t_min) {
+				s.idx ^= 1u << k;
+				s.pos[k] += s.scale_exp2;
+			}
+		s.cur = 0;
+		return false;
+	}
+	// advance
+	uint32_t step_mask = 0;
+#pragma unroll
+	for (int k = 0; k < 3; ++k)
+		if (tc[k] <= tc_max) {
+			step_mask ^= 1u << k;
+			s.pos[k] -= s.scale_exp2;
+		}
+	s.t_min = tc_max;
+	s.idx ^= step_mask;
+	if ((s.idx & step_mask) != 0u) { // pop
+		uint32_t diff = 0;
+#pragma unroll
+		for (int k = 0; k < 3; ++k)
+			if (step_mask & (1u << k)) diff |= __float_as_uint(s.pos[k]) ^ __float_as_uint(s.pos[k] + s.scale_exp2);
+		s.scale = diff ? 31u - (uint32_t)__clz(diff) : 0xffffffffu; // findMSB
+		if (s.scale >= SVO_STACK_SIZE) return true;
+		s.scale_exp2 = __uint_as_float((s.scale - SVO_STACK_SIZE + 127u) << 23u);
+		s.parent = stack[(SVO_STACK_SIZE - 1 - s.scale) * STRIDE];
+		uint32_t sh[3];
+#pragma unroll
+		for (int k = 0; k < 3; ++k) {
+			sh[k] = __float_as_uint(s.pos[k]) >> s.scale;
+			s.pos[k] = __uint_as_float(sh[k] << s.scale);
+		}
+		s.idx = (sh[0] & 1u) | ((sh[1] & 1u) << 1) | ((sh[2] & 1u) << 2);
+		s.h = 0.0f;
+		s.cur = 0;
+	}
+	return false;
+}
+
+// The outputs of an ended ray (shader/octree.glsl:307-340): normal from the exit corner, un-mirrored
+// cube position, o_pos clamped into the cube and nudged by EPS, hit flag.
+SVO_DEV void ray_finish(RayState &s, uint32_t level, MarchOut &out) {
+	if (s.none) {
 		out.t = 0.0f;
-		out.pos[0] = o[0], out.pos[1] = o[1], out.pos[2] = o[2];
+		out.pos[0] = s.o[0], out.pos[1] = s.o[1], out.pos[2] = s.o[2];
 		out.node = 0, out.iter = 0;
 		out.voxel_lo = 0xffffffffu;
 		out.voxel_hi = 0x0000ffffu;
 		return;
 	}
-	for (uint32_t k = 0; k < level; ++k) stack[k * STRIDE] = 0u;
-	float d[3] = {eps_clamp(dir[0]), eps_clamp(dir[1]), eps_clamp(dir[2])};
-	float coef[3], bias[3];
-#pragma unroll
-	for (int k = 0; k < 3; ++k) {
-		coef[k] = 1.0f / -fabsf(d[k]);
-		bias[k] = coef[k] * o[k];
-	}
-	uint32_t oct_mask = 0;
-#pragma unroll
-	for (int k = 0; k < 3; ++k)
-		if (d[k] > 0.0f) {
-			oct_mask ^= 1u << k;
-			bias[k] = 3.0f * coef[k] - bias[k];
-		}
-	float t_min = max_glsl(max_glsl(2.0f * coef[0] - bias[0], 2.0f * coef[1] - bias[1]), 2.0f * coef[2] - bias[2]);
-	const float t_max = min_glsl(min_glsl(coef[0] - bias[0], coef[1] - bias[1]), coef[2] - bias[2]);
-	t_min = max_glsl(t_min, 0.0f);
-	float h = t_max;
-	uint32_t parent = 0, cur = 0, idx = 0;
-	float pos[3] = {1.0f, 1.0f, 1.0f};
-#pragma unroll
-	for (int k = 0; k < 3; ++k)
-		if (1.5f * coef[k] - bias[k] > t_min) {
-			idx ^= 1u << k;
-			pos[k] = 1.5f;
-		}
-	uint32_t scale = SVO_STACK_SIZE - 1;
-	float scale_exp2 = 0.5f;
-	uint32_t iter = 0;
-	bool aborted = false; // pointer outside the pool, tree deeper than its level, or iteration bound
-	const uint32_t min_scale = SVO_STACK_SIZE - level; // deepest scale a valid tree reaches
-
-	while (scale < SVO_STACK_SIZE) {
-		if (iter >= SVO_MARCH_MAX_ITER) {
-			aborted = true;
-			break;
-		}
-		++iter;
-		if (cur == 0u) {
-			const uint32_t w = parent + (idx ^ oct_mask);
-			if (w >= range) {
-				atomicOr(status, kStatusMalformed);
-				aborted = true;
-				scale = 0xffffffffu;
-				break;
-			}
-			cur = __ldg(pool + w);
-			++nfetch;
-		}
-		float tc[3];
-#pragma unroll
-		for (int k = 0; k < 3; ++k) tc[k] = pos[k] * coef[k] - bias[k];
-		const float tc_max = min_glsl(min_glsl(tc[0], tc[1]), tc[2]);
-
-		if ((cur & 0x80000000u) != 0u && t_min <= t_max) {
-			const float half = scale_exp2 * 0.5f;
-			float t_center[3];
-#pragma unroll
-			for (int k = 0; k < 3; ++k) t_center[k] = half * coef[k] + tc[k];
-			if ((cur & 0x40000000u) != 0u) break; // leaf
-			if (scale <= min_scale) {              // interior node below the leaf level: malformed pool
-				atomicOr(status, kStatusMalformed);
-				aborted = true;
-				scale = 0xffffffffu;
-				break;
-			}
-			if (tc_max < h) stack[(SVO_STACK_SIZE - 1 - scale) * STRIDE] = parent; // push
-			h = tc_max;
-			parent = cur & 0x3fffffffu;
-			idx = 0;
-			--scale;
-			scale_exp2 = half;
-#pragma unroll
-			for (int k = 0; k < 3; ++k)
-				if (t_center[k] > t_min) {
-					idx ^= 1u << k;
-					pos[k] += scale_exp2;
-				}
-			cur = 0;
-			continue;
-		}
-		// advance
-		uint32_t step_mask = 0;
-#pragma unroll
-		for (int k = 0; k < 3; ++k)
-			if (tc[k] <= tc_max) {
-				step_mask ^= 1u << k;
-				pos[k] -= scale_exp2;
-			}
-		t_min = tc_max;
-		idx ^= step_mask;
-		if ((idx & step_mask) != 0u) { // pop
-			uint32_t diff = 0;
-#pragma unroll
-			for (int k = 0; k < 3; ++k)
-				if (step_mask & (1u << k)) diff |= __float_as_uint(pos[k]) ^ __float_as_uint(pos[k] + scale_exp2);
-			scale = diff ? 31u - (uint32_t)__clz(diff) : 0xffffffffu; // findMSB
-			if (scale >= SVO_STACK_SIZE) break;
-			scale_exp2 = __uint_as_float((scale - SVO_STACK_SIZE + 127u) << 23u);
-			parent = stack[(SVO_STACK_SIZE - 1 - scale) * STRIDE];
-			uint32_t sh[3];
-#pragma unroll
-			for (int k = 0; k < 3; ++k) {
-				sh[k] = __float_as_uint(pos[k]) >> scale;
-				pos[k] = __uint_as_float(sh[k] << scale);
-			}
-			idx = (sh[0] & 1u) | ((sh[1] & 1u) << 1) | ((sh[2] & 1u) << 2);
-			h = 0.0f;
-			cur = 0;
-		}
-	}
-
-	// normal from the exit corner, un-mirror, o_pos (shader/octree.glsl:307-334)
 	float tc[3];
 #pragma unroll
-	for (int k = 0; k < 3; ++k) tc[k] = coef[k] * (pos[k] + scale_exp2) - bias[k];
+	for (int k = 0; k < 3; ++k) tc[k] = s.coef[k] * (s.pos[k] + s.scale_exp2) - s.bias[k];
 	const uint32_t nax = (tc[0] > tc[1] && tc[0] > tc[2]) ? 0u : (tc[1] > tc[2] ? 1u : 2u);
-	const bool neg = (oct_mask >> nax) & 1u; // normal is -axis exactly when that axis was mirrored
+	const bool neg = (s.oct_mask >> nax) & 1u; // normal is -axis exactly when that axis was mirrored
 #pragma unroll
 	for (int k = 0; k < 3; ++k)
-		if (oct_mask & (1u << k)) pos[k] = 3.0f - scale_exp2 - pos[k];
+		if (s.oct_mask & (1u << k)) s.pos[k] = 3.0f - s.scale_exp2 - s.pos[k];
 #pragma unroll
 	for (int k = 0; k < 3; ++k) {
-		float v = o[k] + t_min * d[k];
-		v = min_glsl(max_glsl(v, pos[k]), pos[k] + scale_exp2);
-		if ((uint32_t)k == nax) v = neg ? pos[k] - kEps : pos[k] + scale_exp2 + kEps * 2.0f;
+		float v = s.o[k] + s.t_min * s.d[k];
+		v = min_glsl(max_glsl(v, s.pos[k]), s.pos[k] + s.scale_exp2);
+		if ((uint32_t)k == nax) v = neg ? s.pos[k] - kEps : s.pos[k] + s.scale_exp2 + kEps * 2.0f;
 		out.pos[k] = v;
 	}
-	const bool hit = !aborted && scale < SVO_STACK_SIZE && t_min <= t_max;
-	out.t = t_min;
-	out.iter = iter;
+	const bool hit = !s.aborted && s.scale < SVO_STACK_SIZE && s.t_min <= s.t_max;
+	out.t = s.t_min;
+	out.iter = s.iter;
 	const uint32_t flags = (hit ? SVO_HIT_FLAG_HIT : 0u) | (nax << 1) | (neg ? SVO_HIT_NORMAL_NEG : 0u) |
-	                       (aborted ? SVO_HIT_FLAG_ABORTED : 0u);
+	                       (s.aborted ? SVO_HIT_FLAG_ABORTED : 0u);
 	if (hit) {
 		const float res = (float)(1u << level);
-		const uint32_t vx = (uint32_t)((pos[0] - 1.0f) * res), vy = (uint32_t)((pos[1] - 1.0f) * res);
-		const uint32_t vz = (uint32_t)((pos[2] - 1.0f) * res);
-		out.node = cur;
+		const uint32_t vx = (uint32_t)((s.pos[0] - 1.0f) * res), vy = (uint32_t)((s.pos[1] - 1.0f) * res);
+		const uint32_t vz = (uint32_t)((s.pos[2] - 1.0f) * res);
+		out.node = s.cur;
 		out.voxel_lo = vx | (vy << 16);
 		out.voxel_hi = vz | (flags << 16);
 	} else {
@@ -196,6 +222,18 @@ SVO_DEV void march_ray(const uint32_t *__restrict__ pool, uint32_t range, uint32
 		out.voxel_lo = 0xffffffffu;
 		out.voxel_hi = 0xffffu | (flags << 16);
 	}
+}
+
+// One whole ray.
+template <int STRIDE>
+SVO_DEV void march_ray(const uint32_t *__restrict__ pool, uint32_t range, uint32_t level, const float o[3],
+                       const float dir[3], uint32_t *stack, MarchOut &out, uint32_t &nfetch, uint32_t *status) {
+	RayState s;
+	ray_init<STRIDE>(s, o, dir, level, stack);
+	while (!ray_step<STRIDE>(s, pool, range, stack, status)) {
+	}
+	ray_finish(s, level, out);
+	nfetch = s.nfetch;
 }
 
 SVO_DEV void store_hit(svo_hit *hits, uint32_t r, const MarchOut &m) {
@@ -279,6 +317,76 @@ __global__ void __launch_bounds__(TPB) march_kernel(MarchArgs a) {
 			march_ray<kStride>(a.pool, a.range, a.level, o, d, stack, m, nf, a.status);
 			store_hit(a.hits, r, m);
 			fetched += nf;
+		}
+	}
+	if (a.fetches) {
+		fetched = warp_sum(fetched);
+		if (lane == 0) atomicAdd(a.fetches, fetched);
+	}
+}
+
+// Persistent refill: a lane takes a new ray as soon as its ray ends, instead of the warp waiting for its
+// slowest ray.  Idle lanes claim consecutive work slots together (one atomic per claim) once at least
+// kRefillMin of them are idle, or all of them are.  Per ray the arithmetic is the single-ray march's.
+constexpr uint32_t kRefillMin = 8;
+
+template <bool CAMERA, int TPB, bool SHARED>
+__global__ void __launch_bounds__(TPB) march_refill_kernel(MarchArgs a) {
+	constexpr int kStride = SHARED ? TPB : 1;
+	__shared__ uint32_t s_stack[SHARED ? SVO_LEVEL_MAX * TPB : 1];
+	uint32_t l_stack[SHARED ? 1 : SVO_LEVEL_MAX];
+	uint32_t *stack = SHARED ? s_stack + threadIdx.x : l_stack;
+	const uint32_t lane = lane_id(), lt_mask = (1u << lane) - 1u;
+	const uint32_t tiles_x = CAMERA ? (a.width + 7u) / 8u : 0u;
+	const uint64_t slots = CAMERA ? (uint64_t)tiles_x * ((a.height + 3u) / 4u) * 32u : (uint64_t)a.n;
+	RayState s;
+	bool active = false, exhausted = false;
+	uint32_t r = 0;
+	unsigned long long fetched = 0;
+	for (;;) {
+		const uint32_t idle = __ballot_sync(kFullMask, !active);
+		const uint32_t nidle = __popc(idle);
+		if (!exhausted && (nidle >= kRefillMin || idle == kFullMask)) {
+			const uint32_t leader = __ffs(idle) - 1;
+			unsigned long long base = 0;
+			if (lane == leader) base = atomicAdd(a.ticket, (unsigned long long)nidle);
+			base = __shfl_sync(kFullMask, base, leader);
+			if (base + nidle >= slots) exhausted = true; // warp-uniform
+			const uint64_t slot = base + __popc(idle & lt_mask);
+			if (!active && slot < slots) {
+				float o[3], d[3];
+				bool live = true;
+				if constexpr (CAMERA) {
+					const uint32_t tile = (uint32_t)(slot >> 5), in = (uint32_t)(slot & 31u);
+					const uint32_t x = (tile % tiles_x) * 8u + (in & 7u), y = (tile / tiles_x) * 4u + (in >> 3);
+					live = x < a.width && y < a.height; // padding slots of partial edge tiles
+					if (live) {
+						r = y * a.width + x;
+						camera_ray(a.cam, a.width, a.height, r, o, d);
+						if (a.beam) beam_advance(a.beam, a.width, r, o, d);
+					}
+				} else {
+					r = (uint32_t)slot;
+					const float2 *src = reinterpret_cast<const float2 *>(a.rays + r);
+					const float2 p0 = src[0], p1 = src[1], p2 = src[2];
+					o[0] = p0.x, o[1] = p0.y, o[2] = p1.x, d[0] = p1.y, d[1] = p2.x, d[2] = p2.y;
+				}
+				if (live) {
+					ray_init<kStride>(s, o, d, a.level, stack);
+					active = true;
+				}
+			}
+		}
+		if (!__any_sync(kFullMask, active)) {
+			if (exhausted) break;
+			continue;
+		}
+		if (active && ray_step<kStride>(s, a.pool, a.range, stack, a.status)) {
+			MarchOut m;
+			ray_finish(s, a.level, m);
+			store_hit(a.hits, r, m);
+			fetched += s.nfetch;
+			active = false;
 		}
 	}
 	if (a.fetches) {
@@ -636,9 +744,21 @@ static void launch_variant(const MarchArgs &a, cudaStream_t stream) {
 	           march_kernel<CAMERA, TPB, RPL, SHARED><<<blocks, TPB, 0, stream>>>(a););
 }
 
+template <bool CAMERA, int TPB, bool SHARED> static void launch_refill(const MarchArgs &a, cudaStream_t stream) {
+	const int sms = device_sm_count();
+	const uint64_t blocks_needed = ((uint64_t)a.n + TPB - 1) / TPB;
+	const uint64_t cap = (uint64_t)sms * (2048 / TPB);
+	const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(blocks_needed, cap));
+	SVO_LAUNCH(CAMERA ? "march_camera" : "march_rays", stream,
+	           march_refill_kernel<CAMERA, TPB, SHARED><<<blocks, TPB, 0, stream>>>(a););
+}
+
 template <bool CAMERA, int TPB>
 static void launch_rpl(const MarchArgs &a, int rpl, bool shared, cudaStream_t stream) {
-	if (rpl == 2) {
+	if (rpl == 0) {
+		if (shared) launch_refill<CAMERA, TPB, true>(a, stream);
+		else launch_refill<CAMERA, TPB, false>(a, stream);
+	} else if (rpl == 2) {
 		if (shared) launch_variant<CAMERA, TPB, 2, true>(a, stream);
 		else launch_variant<CAMERA, TPB, 2, false>(a, stream);
 	} else {

@@ -43,7 +43,7 @@ int device_sm_count();   // SMs of the current device (cached per device)
 // Launch parameters set by the autotuner (svo_tune_set), per (level, size class of the launch's work).
 enum : uint32_t {
 	kTuneMarchBlock = 0,   // threads per march block: 64, 128, 256
-	kTuneMarchRays = 1,    // rays a lane takes per ticket: 1, 2
+	kTuneMarchRays = 1,    // rays a lane takes per ticket: 1, 2; 0 = persistent refill
 	kTuneMarchShared = 2,  // traversal stack in shared (1) or local (0) memory
 	kTuneSweepBlocks = 3,  // blocks per SM of the fragment sweeps
 	kTuneLeafBlocks = 4,   // blocks per SM of the leaf stage

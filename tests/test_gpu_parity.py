@@ -505,3 +505,33 @@ def test_octree_save_load_and_obj_pipeline(cuda, tmp_path):
     o, d = scenes.random_rays(g, 3000)
     rays = rays_from_arrays(o, d)
     assert np.array_equal(gpu_trace(loaded, rays), gpu_trace(octree, rays))
+
+
+# ------------------------------------------------------------------------------------------- launch variants
+def test_every_march_variant_matches_oracle(cuda):
+    """Every launch variant the autotuner can pick (block size, rays per lane or persistent refill, stack
+    in shared or local memory) gives the same hits, bit for bit."""
+    import itertools
+    from sparsevoxeloctree_gb300 import _lib, autotune
+    api = _api()
+    s = scenes.plain_256()
+    frags = oracle.voxelize(s.tris, s.level)
+    octree, pool = gpu_build(frags, s.level)
+    cam = scenes.camera_from_angles((1.5, 1.45, 1.4), 0.4, -0.1, aspect=1.3)
+    w, h = 83, 64
+    ref_cam = oracle.raycast(pool, s.level, oracle.camera_rays(cam, w, h))
+    g = np.random.default_rng(8)
+    o, d = scenes.random_rays(g, 7000, inside=True)
+    rays = rays_from_arrays(o, d)
+    rays["d"][:20] = 0  # null rays
+    ref_rays = oracle.raycast(pool, s.level, rays)
+    rays_dev = api.to_device(rays)
+    try:
+        for tpb, rpl, shared in itertools.product((64, 128, 256), (0, 1, 2), (0, 1)):
+            for name, v in (("march_block", tpb), ("march_rays_per_lane", rpl), ("march_stack_shared", shared)):
+                autotune.set_value(name, 0, -1, v)
+            tr = api.OctreeTracer.Create(octree, cam, w, h)
+            assert_hits_equal(api.hits_numpy(tr.CmdDrawPipeline()), ref_cam)
+            assert_hits_equal(api.hits_numpy(tr.Trace(rays_dev)), ref_rays)
+    finally:
+        _lib.load().svo_tune_reset()
