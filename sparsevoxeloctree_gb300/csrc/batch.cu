@@ -276,7 +276,7 @@ static int batch_build(Batcher &b, const svo_batch_mesh *meshes, uint32_t M, cud
 	p.max_level = 0, p.max_D = 0;
 	uint64_t pool_words = 0, sorted_total = 0, max_scan = 0;
 	uint32_t nb_total = 0, dense_total = 0, items_total = 0;
-	bool any_sparse = false, any_dense = false;
+	bool any_sparse = false;
 	uint64_t windows = 0;
 	hfb[0] = 0, hbb[0] = 0, hib[0] = 0, hdb[0] = 0;
 	for (uint32_t m = 0; m < M; ++m) {
@@ -316,7 +316,6 @@ static int batch_build(Batcher &b, const svo_batch_mesh *meshes, uint32_t M, cud
 		p.max_level = std::max(p.max_level, level);
 		p.max_D = std::max(p.max_D, bm.dv.D);
 		windows += leaf_window_bound(count, level);
-		if (level <= bm.dv.D + 1) any_dense = true;
 		if (level > bm.dv.D + 1) {
 			any_sparse = true;
 			max_scan = std::max<uint64_t>(max_scan, std::min<uint64_t>(max_sparse_level_words(count, level, bm.dv.D),
@@ -350,7 +349,6 @@ static int batch_build(Batcher &b, const svo_batch_mesh *meshes, uint32_t M, cud
 	const size_t o_boff = take(((size_t)nb_total + 1) * 4);
 	const size_t o_blist = take((size_t)nb_total * 4);
 	const size_t o_bmeta = take((size_t)nb_total * 16);
-	const size_t o_bmesh = take((size_t)nb_total * 4);
 	p.bdesc_count = 2 * ((size_t)(nb_total + 2047) / 2048 + 1);
 	const size_t o_bdescs = take(p.bdesc_count * 8);
 	const size_t o_win_base = take(4ull * (M + 1));
@@ -369,13 +367,11 @@ static int batch_build(Batcher &b, const svo_batch_mesh *meshes, uint32_t M, cud
 	p.boff = (uint32_t *)(ws + o_boff);
 	p.blist = (uint32_t *)(ws + o_blist);
 	p.bmeta = (uint4 *)(ws + o_bmeta);
-	p.bmesh = (uint32_t *)(ws + o_bmesh);
 	p.bdescs = (unsigned long long *)(ws + o_bdescs);
 	p.dense_prefix = prefix;
 	p.win_base = (uint32_t *)(ws + o_win_base);
 	p.wfirst = (uint32_t *)(ws + o_wfirst);
 	p.wlast = (uint32_t *)(ws + o_wlast);
-	p.any_dense = any_dense;
 	p.any_sparse = any_sparse;
 	p.sorted = (uint64_t *)(ws + o_sorted);
 	p.cache = (uint32_t *)(ws + o_cache);

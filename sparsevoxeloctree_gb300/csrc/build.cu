@@ -34,7 +34,7 @@
 namespace svo {
 
 constexpr int kTPB = 256;
-constexpr int kAllocIPT = 8;
+constexpr int kAllocIPT = 32; // words per thread of an alloc tile (large tiles: short look-back distances)
 constexpr int kAllocTile = kTPB * kAllocIPT;
 constexpr int kScanIPT = 8;
 constexpr int kScanTile = kTPB * kScanIPT;
@@ -429,8 +429,11 @@ __global__ void __launch_bounds__(kTPB) build_alloc(uint32_t *__restrict__ pool,
 		uint32_t w[kAllocIPT];
 		if (w0 + kAllocIPT <= li.num) {
 			const uint4 *src = reinterpret_cast<const uint4 *>(pool + li.begin + w0);
-			const uint4 x = src[0], y = src[1];
-			w[0] = x.x, w[1] = x.y, w[2] = x.z, w[3] = x.w, w[4] = y.x, w[5] = y.y, w[6] = y.z, w[7] = y.w;
+#pragma unroll
+			for (int k = 0; k < kAllocIPT / 4; ++k) {
+				const uint4 x = src[k];
+				w[4 * k] = x.x, w[4 * k + 1] = x.y, w[4 * k + 2] = x.z, w[4 * k + 3] = x.w;
+			}
 		} else {
 #pragma unroll
 			for (int k = 0; k < kAllocIPT; ++k) w[k] = w0 + k < li.num ? pool[li.begin + w0 + k] : 0u;
@@ -466,8 +469,8 @@ __global__ void __launch_bounds__(kTPB) build_alloc(uint32_t *__restrict__ pool,
 		}
 		if (w0 + kAllocIPT <= li.num) {
 			uint4 *dst = reinterpret_cast<uint4 *>(pool + li.begin + w0);
-			dst[0] = make_uint4(w[0], w[1], w[2], w[3]);
-			dst[1] = make_uint4(w[4], w[5], w[6], w[7]);
+#pragma unroll
+			for (int k = 0; k < kAllocIPT / 4; ++k) dst[k] = make_uint4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
 		} else {
 #pragma unroll
 			for (int k = 0; k < kAllocIPT; ++k)
@@ -496,7 +499,6 @@ uint32_t bucket_shift(uint32_t level) { return std::min<uint32_t>(level, level <
 
 // Leaf windows a dense-parent mesh can need: its leaf range is at most 8 words per possible parent.
 uint64_t leaf_window_bound(uint32_t count, uint32_t level) {
-	if (level > kDenseMaxDepth + 1) return 0;
 	const uint64_t parents = level == 1 ? 1ull : std::min<uint64_t>(1ull << (3 * (level - 1)), std::max<uint32_t>(count, 1u));
 	return (8ull * parents + 4095) / 4096;
 }
@@ -672,7 +674,7 @@ template <bool B> __global__ void __launch_bounds__(kTPB) leaf_window_scan(Build
 		uint32_t c = 0;
 		if (mi < M) {
 			const BuildMesh md = mesh_at<B>(bb, mi);
-			if (dense_parents(md)) c = (md.state->lv[md.level].num + kLeafSlots - 1) >> kWinBits;
+			c = (md.state->lv[md.level].num + kLeafSlots - 1) >> kWinBits;
 		}
 		uint32_t total;
 		const uint32_t excl = block_exclusive_sum<uint32_t, kTPB>(c, s_warp, total);
@@ -682,16 +684,13 @@ template <bool B> __global__ void __launch_bounds__(kTPB) leaf_window_scan(Build
 	if (threadIdx.x == 0) win_base[M] = carry;
 }
 
-// Extent of every non-empty bucket, in list order: first and last item, first and last leaf word
-// (lo = 0xffffffff, hi = 0 for meshes with sparse leaf parents, whose leaf stage reduces the span over
-// the bucket's fragments), and for a batch the bucket's mesh.  For dense-parent meshes, the first and
-// last bucket of every leaf window.  Also writes every mesh's range (final once the interior levels
-// are built).
+// Extent of every non-empty bucket, in list order: first and last item and first and last leaf word.
+// Dense-parent meshes: the span comes from the parent bitmap's prefix; sparse-parent meshes: it is
+// reduced over the bucket's fragments by bucket_span_sparse.  Also writes every mesh's range (final once
+// the interior levels are built).
 template <bool B>
 __global__ void bucket_meta(BuildBatch bb, const uint32_t *__restrict__ boff, const uint32_t *__restrict__ blist,
-                            const BuildState *gstate, uint4 *__restrict__ meta, uint32_t *__restrict__ bmesh,
-                            const uint32_t *__restrict__ win_base, uint32_t *__restrict__ wfirst,
-                            uint32_t *__restrict__ wlast) {
+                            const BuildState *gstate, uint4 *__restrict__ meta) {
 	const uint32_t nbuckets = gstate->buckets;
 	for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nbuckets; t += gridDim.x * blockDim.x) {
 		const uint32_t b = blist[t];
@@ -699,33 +698,79 @@ __global__ void bucket_meta(BuildBatch bb, const uint32_t *__restrict__ boff, co
 		const BuildMesh md = mesh_at<B>(bb, mi);
 		const uint32_t level = md.level, bl = b - md.bucket_base;
 		const uint32_t leaf_begin = md.state->lv[level].begin, leaf_num = md.state->lv[level].num;
-		uint4 m = make_uint4(boff[b] + md.sorted_pad, boff[b + 1] + md.sorted_pad, 0xffffffffu, 0u);
+		uint4 m = make_uint4(boff[b] + md.sorted_pad, boff[b + 1] + md.sorted_pad, 0u, 0u);
 		if (dense_parents(md)) {
 			const uint2 sp = bucket_span(md, bl, leaf_begin, leaf_num);
 			m.z = sp.x, m.w = sp.y;
-			if (SVO_CHECK(sp.y < leaf_num && sp.x <= sp.y, 6u, bb.gstate)) {
-				// first / last bucket of each window this bucket meets (at most two)
-				const bool prev_in = t > 0 && blist[t - 1] >= md.bucket_base;
-				const bool next_in = t + 1 < nbuckets && blist[t + 1] < md.bucket_base + md.nb;
-				const uint32_t prev_end = prev_in ? bucket_span(md, blist[t - 1] - md.bucket_base, leaf_begin, leaf_num).y : 0u;
-				const uint32_t next_start =
-				    next_in ? bucket_span(md, blist[t + 1] - md.bucket_base, leaf_begin, leaf_num).x : 0u;
-				const uint32_t wb = win_base[mi];
-				for (uint32_t k = sp.x >> kWinBits; k <= (sp.y >> kWinBits); ++k) {
-					if (!prev_in || (prev_end >> kWinBits) < k) wfirst[wb + k] = t;
-					if (!next_in || (next_start >> kWinBits) > k) wlast[wb + k] = t;
-				}
-			} else {
-				m.y = m.x;
-			}
+			if (!SVO_CHECK(sp.y < leaf_num && sp.x <= sp.y, 6u, bb.gstate)) m.y = m.x, m.z = 1, m.w = 0;
 		}
 		if (!SVO_CHECK(m.y <= bb.sorted_total && m.x <= m.y, 5u, bb.gstate)) m.y = m.x;
 		meta[t] = m;
-		if (B) bmesh[t] = mi;
 	}
 	for (uint32_t mi = blockIdx.x * blockDim.x + threadIdx.x; mi < batch_size<B>(bb); mi += gridDim.x * blockDim.x) {
 		const BuildMesh md = mesh_at<B>(bb, mi);
 		md.state->range_words = md.state->lv[md.level].begin + md.state->lv[md.level].num;
+	}
+}
+
+// Leaf span of each bucket of a sparse-parent mesh, one warp per bucket: the least and greatest leaf
+// slot of its fragments (through the node index the last sparse tag cached), widened to whole blocks.
+// A bucket holds all fragments of its parents, so its blocks are exactly those parents' blocks.
+template <bool B>
+__global__ void __launch_bounds__(kTPB) bucket_span_sparse(const uint64_t *__restrict__ sorted, BuildBatch bb,
+                                                           const uint32_t *__restrict__ blist,
+                                                           const uint32_t *__restrict__ cache,
+                                                           const BuildState *gstate, uint4 *__restrict__ meta) {
+	const uint32_t nbuckets = gstate->buckets, lane = lane_id();
+	const uint32_t warps = gridDim.x * (blockDim.x / 32);
+	for (uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) / 32; t < nbuckets; t += warps) {
+		const uint32_t mi = B ? mesh_search(bb.bucket_base, bb.M, blist[t]) : 0u;
+		const BuildMesh md = mesh_at<B>(bb, mi);
+		if (dense_parents(md)) continue; // warp-uniform
+		// the node cache is only complete when every sparse depth ran (no capacity, timeout or bad fragment)
+		if ((md.state->status & kStatusCapacity) || (gstate->status & kStatusAbort)) continue;
+		const uint4 m = meta[t];
+		const uint32_t leaf_begin = md.state->lv[md.level].begin, leaf_num = md.state->lv[md.level].num;
+		uint32_t lo = 0xffffffffu, hi = 0u;
+		for (uint32_t f = m.x + lane; f < m.y; f += 32) {
+			const uint32_t sl = leaf_slot(__ldcs(sorted + f), f, md.pool, cache, leaf_begin);
+			lo = min(lo, sl), hi = max(hi, sl);
+		}
+		lo = __reduce_min_sync(kFullMask, lo), hi = __reduce_max_sync(kFullMask, hi);
+		if (lane == 0) {
+			uint4 out = m;
+			if (lo <= hi && (hi | 7u) < leaf_num) { // always, after a complete tag (a failed one is reported)
+				out.z = lo & ~7u, out.w = hi | 7u;
+			} else {
+				SVO_CHECK_FAIL(9u, bb.gstate);
+				out.y = out.x, out.z = 1u, out.w = 0u;
+			}
+			meta[t] = out;
+		}
+	}
+}
+
+// First and last bucket of every leaf window from the buckets' spans: bucket t is a window's first when
+// the previous bucket of its mesh ends before the window, its last when the next one starts after it.
+// Consecutive buckets of a mesh have adjacent spans, so every window of the leaf range gets both.
+template <bool B>
+__global__ void bucket_windows(BuildBatch bb, const uint32_t *__restrict__ blist, const BuildState *gstate,
+                               const uint4 *__restrict__ meta, const uint32_t *__restrict__ win_base,
+                               uint32_t *__restrict__ wfirst, uint32_t *__restrict__ wlast) {
+	const uint32_t nbuckets = gstate->buckets;
+	for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nbuckets; t += gridDim.x * blockDim.x) {
+		const uint32_t mi = B ? mesh_search(bb.bucket_base, bb.M, blist[t]) : 0u;
+		const uint32_t b_lo = B ? __ldg(bb.bucket_base + mi) : 0u, b_hi = B ? __ldg(bb.bucket_base + mi + 1) : bb.one.nb;
+		const uint4 m = meta[t];
+		if (m.z > m.w) continue; // span rejected by a check
+		const bool prev_in = t > 0 && (!B || blist[t - 1] >= b_lo);
+		const bool next_in = t + 1 < nbuckets && blist[t + 1] < b_hi;
+		const uint32_t prev_end = prev_in ? meta[t - 1].w : 0u, next_start = next_in ? meta[t + 1].z : 0u;
+		const uint32_t wb = win_base[mi];
+		for (uint32_t k = m.z >> kWinBits; k <= (m.w >> kWinBits); ++k) {
+			if (!prev_in || (prev_end >> kWinBits) < k) wfirst[wb + k] = t;
+			if (!next_in || (next_start >> kWinBits) > k) wlast[wb + k] = t;
+		}
 	}
 }
 
@@ -809,14 +854,16 @@ SVO_DEV uint32_t leaf_window(const uint64_t *__restrict__ sorted, uint32_t f0, u
 	return leaves;
 }
 
-// Leaf stage of dense-parent meshes: one leaf window per block at a time, windows of all meshes taken
-// grid-stride.  The bucketed copy holds (slot << 32 | rgb) items.
+// Leaf stage: one leaf window per block at a time, windows of all meshes taken grid-stride.  For
+// dense-parent meshes the bucketed copy holds (slot << 32 | rgb) items; for sparse-parent meshes it holds
+// fragments, whose slot comes through the node index the last sparse tag cached.
 template <bool B>
 __global__ void __launch_bounds__(kTPB) build_leaf_windows(const uint64_t *__restrict__ sorted, BuildBatch bb,
                                                            const uint4 *__restrict__ meta,
                                                            const uint32_t *__restrict__ win_base,
                                                            const uint32_t *__restrict__ wfirst,
-                                                           const uint32_t *__restrict__ wlast, BuildState *gstate) {
+                                                           const uint32_t *__restrict__ wlast,
+                                                           const uint32_t *__restrict__ cache, BuildState *gstate) {
 	extern __shared__ unsigned long long s_acc[];
 	__shared__ uint32_t s_over, s_leaves, s_skip;
 	const uint32_t M = batch_size<B>(bb);
@@ -849,93 +896,21 @@ __global__ void __launch_bounds__(kTPB) build_leaf_windows(const uint64_t *__res
 		}
 		const uint32_t f0 = meta[t0].x, f1 = meta[t1].y;
 		const uint32_t wn = min(kLeafSlots, leaf_num - w0);
-		const uint32_t leaves = leaf_window(
-		    sorted, f0, f1, w0, wn, md.pool + leaf_begin + w0, s_acc, &s_over,
-		    [](uint64_t item, uint32_t) { return (uint32_t)(item >> 32); }, [](uint64_t item) { return (uint32_t)item; });
-		const uint32_t wl = warp_sum(leaves);
-		if (lane_id() == 0 && wl) atomicAdd(&s_leaves, wl);
-		__syncthreads();
-		if (threadIdx.x == 0 && s_leaves) atomicAdd(&md.state->leaves, s_leaves);
-		__syncthreads();
-	}
-}
-
-// One bucket per block at a time, buckets taken grid-stride from the list (the next bucket's extent is
-// loaded while the block works on the current one).  For each window of kLeafSlots slots of the
-// bucket's span: zero the shared accumulators, add every item of the window, and write the window's
-// leaf words (empty slots as 0).  An accumulator is two 32-bit words, (r | g << 16) and (b | n << 16):
-// a field can carry only when a voxel has more than 257 fragments (257 x 255 = 65535), so an add that
-// sees a count of 257 or more marks the window, which is then redone exactly with 64-bit r, g, b and n
-// sums, kWideSlots slots at a time.
-//   items (dense parents): the bucketed copy holds (slot << 32 | rgb);
-//   otherwise: fragments, slots through the cached parent index, span reduced over the bucket.
-template <bool B>
-__global__ void __launch_bounds__(kTPB) build_leaf(const uint64_t *__restrict__ sorted, BuildBatch bb,
-                                                   const uint32_t *__restrict__ cache, const uint4 *__restrict__ meta,
-                                                   const uint32_t *__restrict__ bmesh, BuildState *gstate) {
-	extern __shared__ unsigned long long s_acc[];
-	__shared__ uint32_t s_lo, s_hi, s_over, s_leaves, s_skip;
-	const uint32_t nbuckets = gstate->buckets;
-	uint4 next = blockIdx.x < nbuckets ? meta[blockIdx.x] : make_uint4(0, 0, 0, 0);
-	for (uint32_t t = blockIdx.x; t < nbuckets; t += gridDim.x) {
-		const uint4 m = next;
-		if (t + gridDim.x < nbuckets) next = meta[t + gridDim.x];
-		const BuildMesh md = mesh_at<B>(bb, B ? bmesh[t] : 0u);
-		if (dense_parents(md)) continue; // block-uniform: built by build_leaf_windows
-		const uint32_t level = md.level;
-		const uint32_t leaf_begin = md.state->lv[level].begin;
-		if (threadIdx.x == 0) {
-			const uint64_t leaf_end = (uint64_t)leaf_begin + md.state->lv[level].num;
-			uint32_t skip = (md.state->status & kStatusCapacity) | (gstate->status & kStatusAbort);
-			if (!skip && (leaf_end > md.capacity || leaf_end > SVO_MAX_POOL_WORDS)) { // leaf blocks of dense parents
-				atomicOr(&md.state->status, kStatusCapacity);
-				skip = 1;
-			}
-			s_skip = skip;
-			s_leaves = 0;
-		}
-		__syncthreads();
-		if (s_skip) { // block-uniform
-			__syncthreads();
-			continue;
-		}
-		const uint32_t *pool_c = md.pool;
-		const uint32_t f0 = m.x, f1 = m.y;
-		uint32_t span_lo = m.z & ~7u, span_hi = (m.w | 7u) + 1u;
-		if (m.z > m.w) { // span reduced over the bucket's fragments
-			if (threadIdx.x == 0) s_lo = 0xffffffffu, s_hi = 0u;
-			__syncthreads();
-			uint32_t lo = 0xffffffffu, hi = 0u;
-			for (uint32_t fb = f0 + threadIdx.x; fb < f1; fb += 4 * kTPB) {
-				uint64_t fr[4];
-#pragma unroll
-				for (int k = 0; k < 4; ++k) fr[k] = fb + k * kTPB < f1 ? sorted[fb + k * kTPB] : 0ull;
-#pragma unroll
-				for (int k = 0; k < 4; ++k)
-					if (fb + k * kTPB < f1) {
-						const uint32_t sl = leaf_slot(fr[k], fb + k * kTPB, pool_c, cache, leaf_begin);
-						lo = min(lo, sl), hi = max(hi, sl);
-					}
-			}
-			lo = __reduce_min_sync(kFullMask, lo), hi = __reduce_max_sync(kFullMask, hi);
-			if (lane_id() == 0) atomicMin(&s_lo, lo), atomicMax(&s_hi, hi);
-			__syncthreads();
-			span_lo = s_lo & ~7u, span_hi = (s_hi | 7u) + 1u;
-		}
-		if (span_hi > md.state->lv[level].num) { // only after a reported scan failure: never leave the leaf range
-			SVO_CHECK_FAIL(7u, gstate);
-			span_hi = span_lo;
-		}
-		for (uint32_t w0 = span_lo; w0 < span_hi; w0 += kLeafSlots) {
-			const uint32_t wn = min(kLeafSlots, span_hi - w0);
-			const uint32_t leaves = leaf_window(
+		uint32_t leaves;
+		if (dense_parents(md)) {
+			leaves = leaf_window(
+			    sorted, f0, f1, w0, wn, md.pool + leaf_begin + w0, s_acc, &s_over,
+			    [](uint64_t item, uint32_t) { return (uint32_t)(item >> 32); }, [](uint64_t item) { return (uint32_t)item; });
+		} else {
+			const uint32_t *pool_c = md.pool;
+			leaves = leaf_window(
 			    sorted, f0, f1, w0, wn, md.pool + leaf_begin + w0, s_acc, &s_over,
 			    [&](uint64_t item, uint32_t f) { return leaf_slot(item, f, pool_c, cache, leaf_begin); },
 			    [](uint64_t item) { return (uint32_t)(item >> 32); });
-			const uint32_t wl = warp_sum(leaves);
-			if (lane_id() == 0 && wl) atomicAdd(&s_leaves, wl);
-			__syncthreads();
 		}
+		const uint32_t wl = warp_sum(leaves);
+		if (lane_id() == 0 && wl) atomicAdd(&s_leaves, wl);
+		__syncthreads();
 		if (threadIdx.x == 0 && s_leaves) atomicAdd(&md.state->leaves, s_leaves);
 		__syncthreads();
 	}
@@ -1145,24 +1120,26 @@ static void launch_sparse(const uint64_t *sorted, uint32_t count, uint32_t level
 template <bool B>
 static void launch_leaf_stage(const BuildBatch &bb, uint32_t M, uint32_t tune_level, uint64_t n, uint32_t nb_total,
                               const uint32_t *boff, const uint32_t *blist, const BuildState *gstate, uint4 *bmeta,
-                              uint32_t *bmesh, uint32_t *win_base, uint32_t *wfirst, uint32_t *wlast, bool any_dense,
-                              bool any_sparse, const uint64_t *sorted, const uint32_t *cache, cudaStream_t stream) {
+                              uint32_t *win_base, uint32_t *wfirst, uint32_t *wlast, bool any_sparse,
+                              const uint64_t *sorted, const uint32_t *cache, cudaStream_t stream) {
 	const int sms = device_sm_count();
 	const size_t smem = kLeafSlots * sizeof(unsigned long long); // 32 KB: below the default dynamic limit
 	const uint32_t meta_items = std::max<uint32_t>(nb_total, M);
 	const uint32_t blocks = (uint32_t)sms * (uint32_t)tune_value(kTuneLeafBlocks, tune_level, n);
 	SVO_LAUNCH("leaf_window_scan", stream, leaf_window_scan<B><<<1, kTPB, 0, stream>>>(bb, win_base););
 	SVO_LAUNCH("bucket_meta", stream,
-	           bucket_meta<B><<<grid_for(meta_items, kTPB, (uint32_t)sms * 4), kTPB, 0, stream>>>(
-	               bb, boff, blist, gstate, bmeta, bmesh, win_base, wfirst, wlast););
-	if (any_dense)
-		SVO_LAUNCH("build_leaf_windows", stream,
-		           build_leaf_windows<B><<<blocks, kTPB, smem, stream>>>(sorted, bb, bmeta, win_base, wfirst, wlast,
-		                                                                 const_cast<BuildState *>(gstate)););
+	           bucket_meta<B><<<grid_for(meta_items, kTPB, (uint32_t)sms * 4), kTPB, 0, stream>>>(bb, boff, blist,
+	                                                                                          gstate, bmeta););
 	if (any_sparse)
-		SVO_LAUNCH("build_leaf", stream,
-		           build_leaf<B><<<blocks, kTPB, smem, stream>>>(sorted, bb, cache, bmeta, bmesh,
-		                                                          const_cast<BuildState *>(gstate)););
+		SVO_LAUNCH("bucket_span_sparse", stream,
+		           bucket_span_sparse<B><<<grid_for((uint64_t)nb_total * 32, kTPB, (uint32_t)sms * 8), kTPB, 0, stream>>>(
+		               sorted, bb, blist, cache, gstate, bmeta););
+	SVO_LAUNCH("bucket_windows", stream,
+	           bucket_windows<B><<<grid_for(nb_total, kTPB, (uint32_t)sms * 4), kTPB, 0, stream>>>(
+	               bb, blist, gstate, bmeta, win_base, wfirst, wlast););
+	SVO_LAUNCH("build_leaf_windows", stream,
+	           build_leaf_windows<B><<<blocks, kTPB, smem, stream>>>(sorted, bb, bmeta, win_base, wfirst, wlast, cache,
+	                                                                 const_cast<BuildState *>(gstate)););
 }
 
 cudaError_t build_launch_interior(const uint64_t *frags, uint32_t count, uint32_t level, uint32_t *pool,
@@ -1185,9 +1162,8 @@ cudaError_t build_launch_interior(const uint64_t *frags, uint32_t count, uint32_
 cudaError_t build_launch_leaf(uint32_t count, uint32_t level, uint32_t *pool, uint64_t capacity,
                               const BuildWorkspace &w, cudaStream_t stream) {
 	const BuildBatch bb = single_batch(w, count, level, pool, capacity);
-	const bool dense = level <= w.dv.D + 1;
-	launch_leaf_stage<false>(bb, 1, level, count, w.nb, w.boff, w.blist, w.state, w.bmeta, nullptr, w.win_base, w.wfirst,
-	                         w.wlast, dense, !dense, w.sorted, w.cache, stream);
+	launch_leaf_stage<false>(bb, 1, level, count, w.nb, w.boff, w.blist, w.state, w.bmeta, w.win_base, w.wfirst,
+	                         w.wlast, level > w.dv.D + 1, w.sorted, w.cache, stream);
 	return cudaGetLastError();
 }
 
@@ -1222,7 +1198,7 @@ cudaError_t build_launch_batch(const uint64_t *frags, const BuildBatchPlan &p, v
 		              p.gstate, stream);
 	}
 	launch_leaf_stage<true>(p.bb, p.M, p.max_level, p.frags_total, p.nb_total, p.boff, p.blist, p.gstate, p.bmeta,
-	                        p.bmesh, p.win_base, p.wfirst, p.wlast, p.any_dense, p.any_sparse, p.sorted, p.cache, stream);
+	                        p.win_base, p.wfirst, p.wlast, p.any_sparse, p.sorted, p.cache, stream);
 	SVO_LAUNCH("build_export", stream,
 	           build_export<true><<<(p.M + 127) / 128, 128, 0, stream>>>(p.bb, p.gstate, (uint32_t *)result_dev););
 	return cudaGetLastError();

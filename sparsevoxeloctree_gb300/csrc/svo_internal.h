@@ -230,7 +230,6 @@ struct BuildBatchPlan {
 	size_t desc_count;
 	uint32_t *bcount, *bfill, *boff, *blist;
 	uint4 *bmeta;
-	uint32_t *bmesh;                // [nb_total] mesh of each listed bucket
 	unsigned long long *bdescs;
 	size_t bdesc_count;
 	uint32_t *dense_prefix;
@@ -238,7 +237,7 @@ struct BuildBatchPlan {
 	uint32_t *cache;                // only when a mesh has sparse levels (level > 10)
 	uint32_t *win_base;             // [M+1] leaf windows before each mesh (leaf_window_scan)
 	uint32_t *wfirst, *wlast;       // [sum of leaf_window_bound] first and last listed bucket per window
-	bool any_dense, any_sparse;     // meshes whose leaf parents are dense / sparse
+	bool any_sparse;                // a mesh's leaf parents are sparse (level > 10)
 };
 cudaError_t build_launch_batch(const uint64_t *frags, const BuildBatchPlan &p, void *result_dev, cudaStream_t stream);
 
