@@ -444,6 +444,62 @@ int svo_octree_load(const char *path, svo_octree *out, void *stream);
  * aspect ratio (radians; the reference's default fov is pi/3, src/Camera.hpp:17). */
 void svo_camera_from_angles(const float pos[3], float yaw, float pitch, float fov, float aspect, svo_camera *cam);
 
+/* ------------------------------------------------------------------ path tracer
+ * PathTracer (src/PathTracer.hpp:15-75; shader/path_tracer.comp): per pixel and sample, the camera ray
+ * with a Sobol sub-pixel offset, up to `bounce` path vertices of leaf marches with cosine-weighted
+ * diffuse bounces, and the light: a constant colour, or an environment map sampled with multiple
+ * importance sampling (light sample with a shadow march + bsdf sample).  Radiance, first-hit albedo and
+ * normal accumulate as running means over samples in an rgba32f, an rgba8 unorm and an rgba8 snorm
+ * image.  The whole path runs in one kernel; the Sobol state advances on the device after each sample
+ * (Sobol::CmdNext).  Transcendentals are the engine's own float restatements (sin/cos, atan, acos),
+ * so results are bit-identical to the oracle's. */
+typedef struct svo_envmap svo_envmap;
+typedef struct svo_path_tracer svo_path_tracer;
+
+/* Lighting (src/Lighting.hpp:7-20) with EnvironmentMap::m_rotation / m_multiplier. */
+typedef struct svo_lighting {
+	uint32_t type;            /* 0 constant colour, 1 environment map (LightTypes) */
+	float sun_radiance[3];    /* m_sun_radiance; the reference's default is 5 (kDefaultConstantColor) */
+	float envmap_rotation;    /* radians, default 0 */
+	float envmap_multiplier;  /* default 1 */
+	const svo_envmap *envmap; /* type 1 with a null map renders with the constant colour (GetFinalLightType) */
+} svo_lighting;
+
+/* EnvironmentMap::Reset minus the file decoding (src/EnvironmentMap.cpp:44-52): rgba = width x height
+ * float texels (host, row-major; alpha ignored).  Builds the pdf weights (alpha channel) and the alias
+ * table on the host and uploads both.  SVO_ERR_INVALID for an image with no positive luminance. */
+int svo_envmap_create(const float *rgba, uint32_t width, uint32_t height, svo_envmap **out);
+/* Host copies of the tables: rgba (4 floats per texel, alpha = pdf weight), alias (prob, alias per
+ * texel).  Either may be null. */
+int svo_envmap_tables(const svo_envmap *e, float *rgba, uint32_t *alias);
+void svo_envmap_destroy(svo_envmap *e);
+
+/* The engine's default Sobol direction numbers: 64 dimensions x 32 (see svo_path_tracer_set_sobol_matrices). */
+int svo_sobol_default_matrices(uint32_t *out);
+
+/* PathTracer::Create + Reset: targets of width x height, `bounce` path vertices (1..31; the reference
+ * offers 2..16, default 4), default Sobol numbers and noise texture. */
+int svo_path_tracer_create(uint32_t width, uint32_t height, uint32_t bounce, svo_path_tracer **out);
+/* PathTracer::Reset: (re)sizes and clears the targets and the Sobol state. */
+int svo_path_tracer_reset(svo_path_tracer *pt, uint32_t width, uint32_t height, uint32_t bounce, void *stream);
+/* The 256 x 256 RG8 noise texture (uNoise, src/PathTracer.cpp set_noise_image); host or device memory. */
+int svo_path_tracer_set_noise(svo_path_tracer *pt, const uint8_t *rg, void *stream);
+/* Sobol direction numbers, 64 x 32 words (kMatrices of shader/sobol.comp); host or device memory. */
+int svo_path_tracer_set_sobol_matrices(svo_path_tracer *pt, const uint32_t *matrices, void *stream);
+/* PathTracer::CmdRender, `samples` times (stream-ordered, no host synchronisation). */
+int svo_path_tracer_render(svo_path_tracer *pt, const svo_octree *o, const svo_camera *cam, const svo_lighting *light,
+                           uint32_t samples, void *stream);
+/* Samples accumulated since the last reset; the device status word (blocking read; nonzero bits as in
+ * the march: a malformed pool). */
+int svo_path_tracer_info(const svo_path_tracer *pt, uint32_t *spp, uint32_t *status);
+/* Device pointers of the targets (float4 colour, uint32 rgba8 albedo and normal words) and of the Sobol
+ * state (65 words). */
+int svo_path_tracer_images(const svo_path_tracer *pt, void **color, void **albedo, void **normal, void **sobol);
+/* ExtractColorImage / ExtractAlbedoImage / ExtractNormalImage (src/PathTracer.cpp:229-298): image 0, 1
+ * or 2 as width x height x 3 floats on the host (blocking). */
+int svo_path_tracer_extract(const svo_path_tracer *pt, uint32_t image, float *rgb, void *stream);
+void svo_path_tracer_destroy(svo_path_tracer *pt);
+
 #ifdef __cplusplus
 }
 #endif

@@ -32,7 +32,7 @@ def build(force: bool = False) -> str:
 
 def _stale() -> bool:
     t = os.path.getmtime(LIB_PATH)
-    for f in ("oracle.c", "oracle.h", os.path.join("..", "include", "svo.h")):
+    for f in ("oracle.c", "oracle.h", "svo_trig.h", os.path.join("..", "include", "svo.h")):
         if os.path.getmtime(os.path.join(HERE, f)) > t:
             return True
     return False
@@ -65,6 +65,13 @@ def lib():
         L.oracle_camera_rays_beam.argtypes = [P, u32, u32, P, u32, P]
         L.oracle_bounce_rays.argtypes = [P, u64, u64, P]
         L.oracle_diffuse_sample.argtypes = [P, ctypes.c_float, ctypes.c_float, P]
+        f32 = ctypes.c_float
+        L.oracle_pt_render.argtypes = [P, u64, u32, P, u32, u32, u32, u32, P, f32, f32, P, P, u32, u32, P, P, P,
+                                       P, P]
+        L.oracle_sobol_next.argtypes = [P, P, u32]
+        L.oracle_envmap_build.argtypes = [P, u32, u32, P]
+        L.oracle_envmap_build.restype = i32
+        L.oracle_trig.argtypes = [f32, f32, P]
         _lib = L
     return _lib
 
@@ -196,4 +203,62 @@ def diffuse_sample(normal, u1: float, u2: float) -> np.ndarray:
     n = np.ascontiguousarray(normal, np.float32)
     out = np.zeros(3, np.float32)
     lib().oracle_diffuse_sample(_ptr(n), u1, u2, _ptr(out))
+    return out
+
+
+# ---------------------------------------------------------------------------------------------- path tracer
+class PathTraceState:
+    """Accumulation targets and Sobol state of one path-traced image, advanced by render()."""
+
+    def __init__(self, width: int, height: int, bounce: int, matrices: np.ndarray, noise: np.ndarray):
+        self.width, self.height, self.bounce = width, height, bounce
+        self.color = np.zeros((height, width, 4), np.float32)
+        self.albedo = np.zeros((height, width), np.uint32)
+        self.normal = np.zeros((height, width), np.uint32)
+        self.sobol = np.zeros(65, np.uint32)
+        self.matrices = np.ascontiguousarray(matrices, np.uint32).reshape(64 * 32)
+        self.noise = np.ascontiguousarray(noise, np.uint8).reshape(256 * 256 * 2)
+
+    def render(self, pool: np.ndarray, level: int, cam: np.ndarray, light_type: int = 0, const_color=(5.0, 5.0, 5.0),
+               rotation: float = 0.0, multiplier: float = 1.0, env=None, samples: int = 1) -> None:
+        """`samples` x (one sample per pixel, then the Sobol step).  env: (texels (h, w, 4) float32 with the
+        pdf weight in alpha, alias (h, w, 2) uint32) from envmap_build."""
+        pool = np.ascontiguousarray(pool, np.uint32)
+        cam = np.ascontiguousarray(np.asarray(cam, CAMERA_DTYPE).reshape(1))
+        cc = np.ascontiguousarray(const_color, np.float32)
+        if env is None:
+            tex, alias, ew, eh = np.zeros(4, np.float32), np.zeros(2, np.uint32), 0, 0
+        else:
+            tex, alias = np.ascontiguousarray(env[0], np.float32), np.ascontiguousarray(env[1], np.uint32)
+            eh, ew = tex.shape[0], tex.shape[1]
+        dim = 2 * (self.bounce + 1)
+        for _ in range(samples):
+            lib().oracle_pt_render(_ptr(pool), len(pool), level, _ptr(cam), self.width, self.height, self.bounce,
+                                   light_type, _ptr(cc), rotation, multiplier, _ptr(tex), _ptr(alias), ew, eh,
+                                   _ptr(self.sobol), _ptr(self.noise), _ptr(self.color), _ptr(self.albedo),
+                                   _ptr(self.normal))
+            lib().oracle_sobol_next(_ptr(self.sobol), _ptr(self.matrices), dim)
+
+
+def sobol_next(sobol: np.ndarray, matrices: np.ndarray, dim: int) -> None:
+    """Sobol::CmdNext in place on a uint32 state array."""
+    assert sobol.dtype == np.uint32 and sobol.flags.c_contiguous
+    lib().oracle_sobol_next(_ptr(sobol), _ptr(np.ascontiguousarray(matrices, np.uint32)), dim)
+
+
+def envmap_build(rgba: np.ndarray):
+    """(texels with the pdf weight in alpha, alias table (h, w, 2)) of an (h, w, 4) float32 image, or None
+    when the image has no positive luminance."""
+    tex = np.array(rgba, np.float32, copy=True, order="C")
+    h, w = tex.shape[:2]
+    alias = np.zeros((h, w, 2), np.uint32)
+    if not lib().oracle_envmap_build(_ptr(tex), w, h, _ptr(alias)):
+        return None
+    return tex, alias
+
+
+def trig(x: float, y: float) -> np.ndarray:
+    """(sin x, cos x, atan2(y, x), acos x) by the engine's float restatements."""
+    out = np.zeros(4, np.float32)
+    lib().oracle_trig(x, y, _ptr(out))
     return out

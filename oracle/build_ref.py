@@ -44,7 +44,45 @@ SHADERS = [
     ("voxelizer.geom", "ref_vgeom", "geom_main"),
     ("voxelizer_conservative.geom", "ref_vgeom_cons", "geom_main"),
     ("voxelizer.frag", "ref_vfrag", "frag_main"),
+    ("sobol.glsl", "ref_sobol", None),
+    ("sobol.comp", "ref_sobolc", "sobol_main"),
+    ("mis.glsl", "ref_mis", None),
+    ("environment_map.glsl", "ref_envmap", None),
+    ("path_tracer.comp", "ref_pt", "pt_main"),
 ]
+
+# Per-file rewrites on top of transform(): environment_map.glsl is compiled with its sampling half
+# enabled (path_tracer.comp defines ENVIRONMENT_MAP_ENABLE_SAMPLE before including it) and its
+# image-size global becomes an expression evaluated at use; sobol.comp's workgroup-shared variable
+# becomes a static and its direction-number table writable (a harness may run the shader with other
+# numbers); isnan maps to the shim's.
+FILE_FIXUPS = {
+    "environment_map.glsl": [(r"ivec2\s+env_map_dim\s*=[^;]*;", "#define env_map_dim textureSize(uEnvironmentMap, 0)"),
+                             (r"#ifndef ENVIRONMENT_MAP_ENABLE_SAMPLE", "#define ENVIRONMENT_MAP_ENABLE_SAMPLE 1\n#ifndef ENVIRONMENT_MAP_ENABLE_SAMPLE")],
+    "sobol.comp": [(r"^shared\s+", "static "), (r"^const\s+uint\s+kMatrices", "uint kMatrices")],
+    "path_tracer.comp": [(r"\bisnan\(", "glsl_isnan(")],
+}
+
+# EnvironmentMap::weigh_hdr_image and generate_alias_table (src/EnvironmentMap.cpp), compiled from their
+# place in the reference against stubs of the few library names they use.
+ENVMAP_PRELUDE = """// generated by oracle/build_ref.py from the reference's src/EnvironmentMap.cpp; do not commit
+#pragma once
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <vector>
+namespace spdlog { template <class... A> inline void info(A &&...) {} }
+namespace glm {
+using std::sin;
+template <class T> inline T clamp(T x, T lo, T hi) { return std::min(std::max(x, lo), hi); }
+}
+struct EnvironmentMap {
+	struct HdrImg { uint32_t m_width, m_height; float *m_data; };
+	struct AliasPair { uint32_t m_prob, m_alias; };
+	static std::vector<double> weigh_hdr_image(const HdrImg *img);
+	static void generate_alias_table(std::vector<double> *weights_ptr, AliasPair *alias_table);
+};
+"""
 
 FLOAT_LIT = re.compile(r"(?<![\w.])((?:\d+\.\d*|\.\d+)(?:[eE][+-]?\d+)?|\d+[eE][+-]?\d+)(?![\w.])")
 SWIZZLE = re.compile(r"\.(xyz|yzx|zxy|xy|zw)\b(?!\s*[-+*/]?=(?!=))")
@@ -92,13 +130,22 @@ def main() -> int:
         stem = fname.replace(".", "_")
         if fname.endswith(".glsl"):
             stem = fname[: -len(".glsl")]
+        for pat, rep in FILE_FIXUPS.get(fname, []):
+            src = re.sub(pat, rep, src, flags=re.M)
         with open(os.path.join(OUT, f"gen_{stem}.hpp"), "w") as f:
             f.write(transform(src, ns, main_name))
-    cmd = ["g++", "-std=c++20", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math", "-w",
-           "-I", OUT, "-o", os.path.join(OUT, "libsvo_ref.so"), os.path.join(HERE, "ref_shim", "harness.cpp"),
-           "-lpthread"]
-    subprocess.run(cmd, check=True)
-    print(os.path.join(OUT, "libsvo_ref.so"))
+    with open(os.path.join(args.reference, "src", "EnvironmentMap.cpp")) as f:
+        cpp = f.read()
+    begin, end = cpp.index("inline static float luminance"), cpp.index("void EnvironmentMap::create_images")
+    with open(os.path.join(OUT, "gen_envmap_cpp.hpp"), "w") as f:
+        f.write(ENVMAP_PRELUDE + cpp[begin:end])
+    # two builds: GLSL's sin / cos / atan / acos as libm, and as the engine's restatements
+    for lib_name, defs in (("libsvo_ref.so", []), ("libsvo_ref_etrig.so", ["-DSHIM_ENGINE_TRIG"])):
+        cmd = ["g++", "-std=c++20", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math", "-w", *defs,
+               "-I", OUT, "-o", os.path.join(OUT, lib_name), os.path.join(HERE, "ref_shim", "harness.cpp"),
+               "-lpthread"]
+        subprocess.run(cmd, check=True)
+        print(os.path.join(OUT, lib_name))
     return 0
 
 

@@ -7,6 +7,7 @@
  * Reference files cited below are paths inside AdamYuan/SparseVoxelOctree.
  */
 #include "oracle.h"
+#include "svo_trig.h"
 
 #include <math.h>
 #include <pthread.h>
@@ -965,36 +966,7 @@ static uint64_t mix64(uint64_t z) {
 	return z ^ (z >> 31);
 }
 
-/* sin and cos of 2*pi*u for u in [0,1): quadrant split, then Taylor polynomials of degree 13/12 on
- * [0, pi/2) in Horner form; every operation rounded separately so CPU and GPU agree bit for bit. */
-static void sincos_2pi(float u, float *s_out, float *c_out) {
-	float q4 = u * 4.0f;
-	int q = (int)q4;
-	float r = q4 - (float)q;
-	float a = r * 1.57079632679489662f;
-	float a2 = a * a;
-	float s = 1.0f / 6227020800.0f;
-	s = s * a2 + -1.0f / 39916800.0f;
-	s = s * a2 + 1.0f / 362880.0f;
-	s = s * a2 + -1.0f / 5040.0f;
-	s = s * a2 + 1.0f / 120.0f;
-	s = s * a2 + -1.0f / 6.0f;
-	s = s * a2 + 1.0f;
-	s = s * a;
-	float c = 1.0f / 479001600.0f;
-	c = c * a2 + -1.0f / 3628800.0f;
-	c = c * a2 + 1.0f / 40320.0f;
-	c = c * a2 + -1.0f / 720.0f;
-	c = c * a2 + 1.0f / 24.0f;
-	c = c * a2 + -0.5f;
-	c = c * a2 + 1.0f;
-	switch (q & 3) {
-	case 0: *s_out = s; *c_out = c; break;
-	case 1: *s_out = c; *c_out = -s; break;
-	case 2: *s_out = -s; *c_out = -c; break;
-	default: *s_out = -c; *c_out = s; break;
-	}
-}
+/* sin / cos / atan / acos: the engine's restatements (svo_trig.h). */
 
 /* Diffuse_Sample (shader/diffuse.glsl:7-14) with AlignDirection (shader/util.glsl:5-9) for an
  * axis-aligned normal; sin/cos from sincos_2pi. */
@@ -1036,4 +1008,312 @@ void oracle_bounce_rays(const svo_hit *hits, uint64_t n, uint64_t seed, svo_ray 
 		nrm[ax] = (h->flags & SVO_HIT_NORMAL_NEG) ? -1.0f : 1.0f;
 		oracle_diffuse_sample(nrm, u1, u2, r->d);
 	}
+}
+
+/* ====================================================================== path tracer */
+
+#define PT_PI 3.14159265358979323846f
+
+typedef struct pt_env {
+	const float *texels; /* 4 floats per texel: radiance rgb, pdf weight */
+	const uint32_t *alias;
+	uint32_t w, h;
+} pt_env;
+
+/* texture() with a linear filter and repeat addressing: the 4 texels around (u W - 1/2, v H - 1/2). */
+static void env_texture(const pt_env *e, float u, float v, float out[4]) {
+	float x = u * (float)e->w - 0.5f, y = v * (float)e->h - 0.5f;
+	float fx = floorf(x), fy = floorf(y);
+	float a = x - fx, b = y - fy;
+	int64_t W = e->w, H = e->h;
+	int64_t i0 = (((int64_t)fx % W) + W) % W, j0 = (((int64_t)fy % H) + H) % H;
+	int64_t i1 = i0 + 1 == W ? 0 : i0 + 1, j1 = j0 + 1 == H ? 0 : j0 + 1;
+	const float *t00 = e->texels + 4 * (j0 * W + i0), *t10 = e->texels + 4 * (j0 * W + i1);
+	const float *t01 = e->texels + 4 * (j1 * W + i0), *t11 = e->texels + 4 * (j1 * W + i1);
+	float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b), w01 = (1.0f - a) * b, w11 = a * b;
+	for (int k = 0; k < 4; ++k)
+		out[k] = ((w00 * t00[k] + w10 * t10[k]) + w01 * t01[k]) + w11 * t11[k];
+}
+
+static const float kTwoPiPi = 2.0f * PT_PI * PT_PI;
+
+/* EnvMap_Dir2Coord + texture (shader/environment_map.glsl:16-25). */
+static void env_lookup(const pt_env *e, const float d[3], float rot, float out[4]) {
+	float u = (svo_atan2(d[0], d[2]) + rot) / PT_PI * 0.5f;
+	float v = svo_acos(d[1]) / PT_PI;
+	env_texture(e, u, v, out);
+}
+
+/* EnvMap_Sample (shader/environment_map.glsl:31-48) with the engine's sin/cos rule. */
+static void env_sample(const pt_env *e, float s0, float s1, float rot, float d[3], float light[3], float *pdf) {
+	uint32_t sz = e->w * e->h;
+	uint32_t idx = (uint32_t)(s0 * (float)sz);
+	if (idx > sz - 1u)
+		idx = sz - 1u;
+	uint32_t prob = (uint32_t)(s1 * 4294967296.0f);
+	uint32_t pix = idx;
+	if (prob > e->alias[2 * idx])
+		pix = e->alias[2 * idx + 1];
+	uint32_t py = pix / e->w, px = pix - py * e->w;
+	float u = ((float)px + 0.5f) / (float)e->w, v = ((float)py + 0.5f) / (float)e->h;
+	float phi = 2.0f * PT_PI * u - rot, theta = PT_PI * v;
+	float st, ct, sp, cp;
+	svo_sincos(theta, &st, &ct);
+	svo_sincos(phi, &sp, &cp);
+	const float *tx = e->texels + 4 * (size_t)pix;
+	light[0] = tx[0], light[1] = tx[1], light[2] = tx[2];
+	*pdf = tx[3] / (kTwoPiPi * st);
+	d[0] = st * sp, d[1] = ct, d[2] = st * cp;
+}
+
+static float mis_power(float a, float b) {
+	float t = a * a;
+	return t / (b * b + t);
+}
+
+static float sobol_f(uint32_t v) { return (float)v * 2.3283064365386963e-10f; }
+
+static float unorm8_load(uint32_t w, int k) { return (float)((w >> (8 * k)) & 0xffu) / 255.0f; }
+static uint32_t unorm8_store(float v) { return (uint32_t)floorf(fminf(fmaxf(v, 0.0f), 1.0f) * 255.0f + 0.5f); }
+static float snorm8_load(uint32_t w, int k) { return fmaxf((float)(int32_t)(int8_t)((w >> (8 * k)) & 0xffu) / 127.0f, -1.0f); }
+static uint32_t snorm8_store(float v) {
+	return (uint32_t)(int32_t)floorf(fminf(fmaxf(v, -1.0f), 1.0f) * 127.0f + 0.5f) & 0xffu;
+}
+
+typedef struct pt_ctx {
+	const uint32_t *pool;
+	uint64_t range;
+	uint32_t level;
+	const svo_camera *cam;
+	uint32_t width, height, bounce, light_type;
+	const float *const_color;
+	float rot, mult;
+	pt_env env;
+	const uint32_t *sobol;
+	const uint8_t *noise;
+	float *color;
+	uint32_t *albedo, *normal;
+} pt_ctx;
+
+/* AlignDirection (shader/util.glsl:5-9). */
+static void align_direction(const float dl[3], const float nrm[3], float out[3]) {
+	float ref[3] = {0.0f, 0.0f, 0.0f};
+	if (fabsf(nrm[0]) > 0.01f)
+		ref[1] = 1.0f;
+	else
+		ref[0] = 1.0f;
+	float u[3] = {ref[1] * nrm[2] - ref[2] * nrm[1], ref[2] * nrm[0] - ref[0] * nrm[2],
+	              ref[0] * nrm[1] - ref[1] * nrm[0]};
+	float ul = sqrtf((u[0] * u[0] + u[1] * u[1]) + u[2] * u[2]);
+	for (int k = 0; k < 3; ++k)
+		u[k] = u[k] / ul;
+	float v[3] = {nrm[1] * u[2] - nrm[2] * u[1], nrm[2] * u[0] - nrm[0] * u[2], nrm[0] * u[1] - nrm[1] * u[0]};
+	for (int k = 0; k < 3; ++k)
+		out[k] = (dl[0] * u[k] + dl[1] * v[k]) + dl[2] * nrm[k];
+}
+
+/* Diffuse_Sample (shader/diffuse.glsl:7-14) as the path tracer calls it: phi = 2 * PI * samp.y, cos and
+ * sin of phi, pdf = d.z / PI. */
+static void pt_diffuse_sample(const float nrm[3], float s0, float s1, float out[3], float *pdf) {
+	float r = sqrtf(s0), phi = 2.0f * PT_PI * s1;
+	float sn, cs;
+	svo_sincos(phi, &sn, &cs);
+	float dl[3] = {r * cs, r * sn, sqrtf(1.0f - s0)};
+	*pdf = dl[2] / PT_PI;
+	align_direction(dl, nrm, out);
+}
+
+/* The 5-argument Octree_RayMarchLeaf (shader/octree.glsl:342-502) as the path tracer reads it: the
+ * |d| >= EPS clamp (applied first; the leaf march's > EPS clamp then keeps d), hit, o_pos,
+ * o_color = rgb * (1/255), o_normal. */
+static int pt_leaf(const pt_ctx *c, const float o[3], const float din[3], float pos[3], float alb[3], float nrm[3]) {
+	float d[3];
+	for (int k = 0; k < 3; ++k)
+		d[k] = fabsf(din[k]) >= MARCH_EPS ? din[k] : (din[k] >= 0.0f ? MARCH_EPS : -MARCH_EPS);
+	svo_ray r = {{o[0], o[1], o[2]}, {d[0], d[1], d[2]}};
+	svo_hit h;
+	march_one(c->pool, c->range, c->level, &r, &h, NULL);
+	for (int k = 0; k < 3; ++k) {
+		pos[k] = h.pos[k];
+		alb[k] = (float)((h.node >> (8 * k)) & 0xffu) * 0.00392156862745098f;
+		nrm[k] = 0.0f;
+	}
+	nrm[SVO_HIT_NORMAL_AXIS(h.flags)] = (h.flags & SVO_HIT_NORMAL_NEG) ? -1.0f : 1.0f;
+	return (h.flags & SVO_HIT_FLAG_HIT) != 0;
+}
+
+/* One sample of one pixel: ConstColorPathTrace / EnvMapPathTrace and main()
+ * (shader/path_tracer.comp:32-135). */
+static void pt_pixel(const pt_ctx *c, uint32_t x, uint32_t y) {
+	uint32_t spp = c->sobol[2 * (c->bounce + 1)];
+	uint32_t ni = (((y & 255u) << 8) | (x & 255u)) * 2u;
+	float nz[2] = {(float)c->noise[ni] / 255.0f, (float)c->noise[ni + 1] / 255.0f};
+	float o[3] = {c->cam->pos[0], c->cam->pos[1], c->cam->pos[2]}, d[3];
+	gen_ray(c->cam, ((float)x + sobol_f(c->sobol[0])) / (float)c->width,
+	        ((float)y + sobol_f(c->sobol[1])) / (float)c->height, d);
+	float acc[3] = {1.0f, 1.0f, 1.0f}, rad[3] = {0.0f, 0.0f, 0.0f};
+	float dalb[3] = {0.0f, 0.0f, 0.0f}, dnrm[3] = {0.0f, 0.0f, 0.0f};
+	float pos[3], alb[3], nrm[3];
+	if (pt_leaf(c, o, d, pos, alb, nrm)) {
+		for (int k = 0; k < 3; ++k) {
+			acc[k] *= alb[k];
+			dalb[k] = alb[k];
+			dnrm[k] = nrm[k];
+		}
+		for (uint32_t cur = 1; cur < c->bounce; ++cur) {
+			float samp[2] = {sobol_f(c->sobol[2 * cur]) + nz[0], sobol_f(c->sobol[2 * cur + 1]) + nz[1]};
+			samp[0] = samp[0] - floorf(samp[0]);
+			samp[1] = samp[1] - floorf(samp[1]);
+			for (int k = 0; k < 3; ++k)
+				o[k] = pos[k];
+			if (c->light_type == 1) {
+				float ld[3], light[3], light_pdf;
+				env_sample(&c->env, samp[0], samp[1], c->rot, ld, light, &light_pdf);
+				float ndd = (nrm[0] * ld[0] + nrm[1] * ld[1]) + nrm[2] * ld[2];
+				if (ndd > 0.0f && !isnan(light_pdf) && light_pdf > 0.0f) {
+					float t, sz;
+					if (!march_traverse(c->pool, c->range, c->level, o, ld, 0, 0.0f, 0.0f, &t, &sz)) {
+						float bsdf_pdf = ndd / PT_PI;
+						float w = mis_power(light_pdf, bsdf_pdf);
+						for (int k = 0; k < 3; ++k)
+							rad[k] += acc[k] * light[k] * c->mult * w * ndd * (1.0f / PT_PI) / light_pdf;
+					}
+				}
+			}
+			float bsdf_pdf;
+			pt_diffuse_sample(nrm, samp[0], samp[1], d, &bsdf_pdf);
+			if (pt_leaf(c, o, d, pos, alb, nrm)) {
+				for (int k = 0; k < 3; ++k)
+					acc[k] *= alb[k];
+			} else {
+				if (c->light_type == 1) {
+					float env[4];
+					env_lookup(&c->env, d, c->rot, env);
+					float light_pdf = env[3] / (kTwoPiPi * sqrtf(1.0f - d[1] * d[1]));
+					if (!isnan(light_pdf) && light_pdf > 0.0f) {
+						float w = mis_power(bsdf_pdf, light_pdf);
+						for (int k = 0; k < 3; ++k)
+							rad[k] += acc[k] * env[k] * c->mult * w;
+					}
+				} else {
+					for (int k = 0; k < 3; ++k)
+						rad[k] = acc[k] * c->const_color[k];
+				}
+				break;
+			}
+		}
+	} else if (c->light_type == 1) {
+		float env[4];
+		env_lookup(&c->env, d, c->rot, env);
+		rad[0] = env[0], rad[1] = env[1], rad[2] = env[2];
+	} else {
+		for (int k = 0; k < 3; ++k)
+			rad[k] = c->const_color[k];
+	}
+	size_t p = (size_t)y * c->width + x;
+	float fs = (float)spp, fn = (float)(spp + 1u);
+	float *col = c->color + 4 * p;
+	for (int k = 0; k < 3; ++k)
+		col[k] = (col[k] * fs + rad[k]) / fn;
+	col[3] = 1.0f;
+	uint32_t wa = c->albedo[p], wn = c->normal[p];
+	uint32_t oa = 255u << 24, on = 127u << 24;
+	for (int k = 0; k < 3; ++k) {
+		oa |= unorm8_store((unorm8_load(wa, k) * fs + dalb[k]) / fn) << (8 * k);
+		on |= snorm8_store((snorm8_load(wn, k) * fs + dnrm[k]) / fn) << (8 * k);
+	}
+	c->albedo[p] = oa;
+	c->normal[p] = on;
+}
+
+static void pt_range(void *p, uint64_t b, uint64_t e) {
+	const pt_ctx *c = (const pt_ctx *)p;
+	for (uint64_t i = b; i < e; ++i)
+		pt_pixel(c, (uint32_t)(i % c->width), (uint32_t)(i / c->width));
+}
+
+void oracle_pt_render(const uint32_t *pool, uint64_t range, uint32_t level, const svo_camera *cam, uint32_t width,
+                      uint32_t height, uint32_t bounce, uint32_t light_type, const float *const_color, float rot,
+                      float mult, const float *env_texels, const uint32_t *env_alias, uint32_t env_w, uint32_t env_h,
+                      const uint32_t *sobol, const uint8_t *noise, float *color, uint32_t *albedo, uint32_t *normal) {
+	pt_ctx c = {pool, range, level, cam, width, height, bounce, light_type, const_color, rot, mult,
+	            {env_texels, env_alias, env_w, env_h}, sobol, noise, color, albedo, normal};
+	parallel_for((uint64_t)width * height, 64, pt_range, &c);
+}
+
+/* Sobol::CmdNext (shader/sobol.comp:70-86). */
+void oracle_sobol_next(uint32_t *sobol, const uint32_t *matrices, uint32_t dim) {
+	uint32_t i = sobol[dim];
+	if (i == 0xffffffffu) {
+		sobol[dim] = 0;
+		return;
+	}
+	uint32_t c = (uint32_t)__builtin_ctz(~i);
+	sobol[dim] = i + 1u;
+	for (uint32_t j = 0; j < dim; ++j)
+		sobol[j] ^= matrices[j * 32 + c];
+}
+
+/* EnvironmentMap::weigh_hdr_image + generate_alias_table (src/EnvironmentMap.cpp:83-160) on a copy:
+ * rgba[4i+3] becomes the weight (float), alias gets (prob, alias) per texel.  Returns 0 when the image
+ * has no positive luminance. */
+int oracle_envmap_build(float *rgba, uint32_t w, uint32_t h, uint32_t *alias) {
+	size_t n = (size_t)w * h;
+	double *wt = (double *)malloc(n * sizeof(double));
+	uint32_t *sm = (uint32_t *)malloc(n * sizeof(uint32_t)), *lg = (uint32_t *)malloc(n * sizeof(uint32_t));
+	double sum = 0.0;
+	for (uint32_t j = 0; j < h; ++j) {
+		double st = sin(3.14159265358979323846 * ((double)j + 0.5) / (double)h);
+		for (uint32_t i = 0; i < w; ++i) {
+			const float *c = rgba + 4 * ((size_t)j * w + i);
+			float lum = 0.2126f * c[0] + 0.7152f * c[1] + 0.0722f * c[2];
+			wt[(size_t)j * w + i] = (double)lum * st;
+			sum += wt[(size_t)j * w + i];
+		}
+	}
+	int ok = sum > 0.0 && isfinite(sum);
+	if (ok) {
+		double mul = (double)n / sum;
+		for (size_t i = 0; i < n; ++i) {
+			wt[i] *= mul;
+			rgba[4 * i + 3] = (float)wt[i];
+		}
+		size_t ns = 0, nl = 0;
+		for (size_t i = 0; i < n; ++i) {
+			if (wt[i] < 1.0)
+				sm[ns++] = (uint32_t)i;
+			else
+				lg[nl++] = (uint32_t)i;
+		}
+		while (ns && nl) {
+			uint32_t s = sm[--ns], l = lg[nl - 1];
+			double p = wt[s] * 4294967296.0;
+			alias[2 * s] = (uint32_t)(p < 0.0 ? 0.0 : (p > 4294967295.0 ? 4294967295.0 : p));
+			alias[2 * s + 1] = l;
+			wt[l] -= 1.0 - wt[s];
+			if (wt[l] < 1.0) {
+				--nl;
+				sm[ns++] = l;
+			}
+		}
+		while (nl) {
+			uint32_t l = lg[--nl];
+			alias[2 * l] = alias[2 * l + 1] = 0xffffffffu;
+		}
+		while (ns) {
+			uint32_t s = sm[--ns];
+			alias[2 * s] = alias[2 * s + 1] = 0xffffffffu;
+		}
+	}
+	free(wt);
+	free(sm);
+	free(lg);
+	return ok;
+}
+
+/* The engine's transcendental restatements, for accuracy tests: sin x, cos x, atan2(y, x), acos x. */
+void oracle_trig(float x, float y, float *out) {
+	svo_sincos(x, &out[0], &out[1]);
+	out[2] = svo_atan2(y, x);
+	out[3] = svo_acos(x);
 }

@@ -74,6 +74,22 @@ void oracle_diffuse_sample(const float nrm[3], float u1, float u2, float out[3])
 /* Cosine bounce rays for hits (shader/diffuse.glsl:7-14 + shader/util.glsl:5-9). */
 void oracle_bounce_rays(const svo_hit *hits, uint64_t n, uint64_t seed, svo_ray *rays);
 
+/* ---- path tracer ---- */
+/* One sample per pixel of shader/path_tracer.comp (ConstColorPathTrace / EnvMapPathTrace and the running
+ * means of main()), updating color (4 floats per pixel), albedo and normal (rgba8 unorm / snorm words)
+ * in place.  sobol: the Sobol state (2 * (bounce + 1) values, then the sample index); noise: 256 x 256
+ * RG8; env_texels / env_alias: the environment map tables (light_type 1). */
+void oracle_pt_render(const uint32_t *pool, uint64_t range, uint32_t level, const svo_camera *cam, uint32_t width,
+                      uint32_t height, uint32_t bounce, uint32_t light_type, const float *const_color, float rot,
+                      float mult, const float *env_texels, const uint32_t *env_alias, uint32_t env_w, uint32_t env_h,
+                      const uint32_t *sobol, const uint8_t *noise, float *color, uint32_t *albedo, uint32_t *normal);
+/* Sobol::CmdNext (shader/sobol.comp:70-86) for `dim` dimensions of 32 direction numbers each. */
+void oracle_sobol_next(uint32_t *sobol, const uint32_t *matrices, uint32_t dim);
+/* EnvironmentMap::weigh_hdr_image + generate_alias_table (src/EnvironmentMap.cpp:83-160). */
+int oracle_envmap_build(float *rgba, uint32_t w, uint32_t h, uint32_t *alias);
+/* sin x, cos x, atan2(y, x), acos x by the engine's restatements (oracle/svo_trig.h). */
+void oracle_trig(float x, float y, float *out);
+
 #ifdef __cplusplus
 }
 #endif

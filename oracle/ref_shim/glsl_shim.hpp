@@ -171,6 +171,13 @@ SHIM_VEC_OPS(uvec2, uint, 2)
 SHIM_VEC_OPS(uvec3, uint, 3)
 SHIM_VEC_OPS(uvec4, uint, 4)
 
+SHIM_VEC_OPS(ivec2, int, 2)
+
+inline vec3 &operator*=(vec3 &a, const vec3 &b) {
+	for (int i = 0; i < 3; ++i) a[i] *= b[i];
+	return a;
+}
+inline ivec2 operator&(const ivec2 &a, int m) { return ivec2(a.x & m, a.y & m); }
 inline vec3 operator-(const vec3 &a) { return vec3(-a.x, -a.y, -a.z); }
 inline vec2 operator-(const vec2 &a) { return vec2(-a.x, -a.y); }
 inline uvec3 operator*(const uvec3 &a, const bvec3 &b) { return a * to_uvec3(b); }
@@ -193,12 +200,31 @@ inline vec3 cross(const vec3 &a, const vec3 &b) {
 inline float length(const vec3 &v) { return std::sqrt(dot(v, v)); }
 inline vec3 normalize(const vec3 &v) { return v / length(v); }
 inline float sqrt(float x) { return std::sqrt(x); }
+#ifdef SHIM_ENGINE_TRIG
+// GLSL leaves the precision of its transcendental built-ins to the implementation; this build evaluates
+// them with the engine's restatements (oracle/svo_trig.h) so a comparison isolates the shader logic.
+#include "../svo_trig.h"
+inline float cos(float x) { float s, c; svo_sincos(x, &s, &c); return c; }
+inline float sin(float x) { float s, c; svo_sincos(x, &s, &c); return s; }
+#else
 inline float cos(float x) { return std::cos(x); }
 inline float sin(float x) { return std::sin(x); }
+#endif
 inline bvec3 greaterThanEqual(const uvec3 &a, const uvec3 &b) { return bvec3(a.x >= b.x, a.y >= b.y, a.z >= b.z); }
 inline uint floatBitsToUint(float f) { uint u; std::memcpy(&u, &f, 4); return u; }
 inline float uintBitsToFloat(uint u) { float f; std::memcpy(&f, &u, 4); return f; }
 inline int findMSB(uint v) { return v ? 31 - __builtin_clz(v) : -1; }
+inline int findLSB(uint v) { return v ? __builtin_ctz(v) : -1; }
+inline vec2 fract(const vec2 &v) { return vec2(v.x - std::floor(v.x), v.y - std::floor(v.y)); }
+inline bool glsl_isnan(float x) { return std::isnan(x); }
+#ifdef SHIM_ENGINE_TRIG
+inline float atan(float y, float x) { return svo_atan2(y, x); }
+inline float acos(float x) { return svo_acos(x); }
+#else
+inline float atan(float y, float x) { return std::atan2(y, x); }
+inline float acos(float x) { return std::acos(x); }
+#endif
+inline void barrier() {}
 inline uint packUnorm4x8(const vec4 &v) {
 	uint r = 0;
 	for (int i = 0; i < 4; ++i) r |= (uint)std::lrint(clamp(v[i], 0.0f, 1.0f) * 255.0f) << (8 * i);
@@ -231,8 +257,79 @@ inline uint subgroupBallotExclusiveBitCount(const uvec4 &) { return 0u; }
 // ------------------------------------------------------------------------------------------ stages
 struct glsl_discard {};
 
-struct sampler2D {};
-inline vec4 texture(const sampler2D &, const vec2 &) { throw std::runtime_error("texture sampling is not shimmed"); }
+// Images and samplers as plain arrays.  The format conversions are the Vulkan rules as the engine
+// states them: unorm8 stores round(clamp(v, 0, 1) * 255) with ties up and loads c / 255; snorm8 stores
+// round(clamp(v, -1, 1) * 127) with ties up and loads max(c / 127, -1).
+struct image2D {
+	void *data = nullptr;
+	int w = 0, h = 0;
+	int format = 0; // 0 rgba32f, 1 rgba8 unorm, 2 rgba8 snorm
+};
+inline ivec2 imageSize(const image2D &im) { return ivec2(im.w, im.h); }
+inline vec4 imageLoad(const image2D &im, const ivec2 &p) {
+	const size_t i = (size_t)p.y * im.w + p.x;
+	if (im.format == 0) {
+		const float *f = (const float *)im.data + 4 * i;
+		return vec4(f[0], f[1], f[2], f[3]);
+	}
+	const uint w = ((const uint *)im.data)[i];
+	vec4 r;
+	for (int k = 0; k < 4; ++k) {
+		const uint b = (w >> (8 * k)) & 0xffu;
+		r[k] = im.format == 1 ? (float)b / 255.0f : std::fmax((float)(int8_t)b / 127.0f, -1.0f);
+	}
+	return r;
+}
+inline void imageStore(image2D &im, const ivec2 &p, const vec4 &v) {
+	const size_t i = (size_t)p.y * im.w + p.x;
+	if (im.format == 0) {
+		float *f = (float *)im.data + 4 * i;
+		for (int k = 0; k < 4; ++k) f[k] = v[k];
+		return;
+	}
+	uint w = 0;
+	for (int k = 0; k < 4; ++k) {
+		const uint b = im.format == 1 ? (uint)std::floor(clamp(v[k], 0.0f, 1.0f) * 255.0f + 0.5f)
+		                              : (uint)(int)std::floor(clamp(v[k], -1.0f, 1.0f) * 127.0f + 0.5f) & 0xffu;
+		w |= b << (8 * k);
+	}
+	((uint *)im.data)[i] = w;
+}
+
+// A float texture (4 channels per texel).  texture() is VK_FILTER_LINEAR with repeat addressing: the 4
+// texels around (u W - 1/2, v H - 1/2), integer coordinates wrapped.
+struct sampler2D {
+	const float *texels = nullptr;
+	int w = 0, h = 0;
+};
+struct usampler2D {
+	const uint *texels = nullptr; // 2 channels per texel
+	int w = 0, h = 0;
+};
+inline ivec2 textureSize(const sampler2D &s, int) { return ivec2(s.w, s.h); }
+inline vec4 texelFetch(const sampler2D &s, const ivec2 &p, int) {
+	const float *t = s.texels + 4 * ((size_t)p.y * s.w + p.x);
+	return vec4(t[0], t[1], t[2], t[3]);
+}
+inline uvec4 texelFetch(const usampler2D &s, const ivec2 &p, int) {
+	const uint *t = s.texels + 2 * ((size_t)p.y * s.w + p.x);
+	return uvec4(t[0], t[1], 0u, 1u);
+}
+inline vec4 texture(const sampler2D &s, const vec2 &uv) {
+	if (!s.texels) throw std::runtime_error("texture sampling of an unbound sampler");
+	const float x = uv.x * (float)s.w - 0.5f, y = uv.y * (float)s.h - 0.5f;
+	const float fx = std::floor(x), fy = std::floor(y);
+	const float a = x - fx, b = y - fy;
+	const int64_t W = s.w, H = s.h;
+	const int64_t i0 = (((int64_t)fx % W) + W) % W, j0 = (((int64_t)fy % H) + H) % H;
+	const int64_t i1 = i0 + 1 == W ? 0 : i0 + 1, j1 = j0 + 1 == H ? 0 : j0 + 1;
+	const float *t00 = s.texels + 4 * (j0 * W + i0), *t10 = s.texels + 4 * (j0 * W + i1);
+	const float *t01 = s.texels + 4 * (j1 * W + i0), *t11 = s.texels + 4 * (j1 * W + i1);
+	const float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b), w01 = (1.0f - a) * b, w11 = a * b;
+	vec4 r;
+	for (int k = 0; k < 4; ++k) r[k] = ((w00 * t00[k] + w10 * t10[k]) + w01 * t01[k]) + w11 * t11[k];
+	return r;
+}
 
 struct gl_PerVertex {
 	vec4 gl_Position;
@@ -248,6 +345,15 @@ extern uint kVoxelResolution, kFragmentCount, kTextureNum;
 extern uint uCountOnly, uTextureId, uAlbedo;
 extern vec4 uPosition, uLook, uSide, uUp;
 extern sampler2D uTextures[1];
+// path tracer (shader/path_tracer.comp, sobol.glsl / sobol.comp, environment_map.glsl); its uAlbedo image is
+// declared in the harness's ref_pt namespace (the voxelizer's uAlbedo is a push constant)
+extern uint *uSobol;
+extern uint uDimension;
+extern sampler2D uEnvironmentMap, uNoise;
+extern usampler2D uEnvMapAliasTable;
+extern image2D uColor, uNormal;
+extern uint uBounce, uLightType;
+extern float uConstColor[3], uEnvMapRotation, uEnvMapMultiplier;
 extern thread_local uvec3 gl_GlobalInvocationID;
 extern thread_local vec4 gl_FragCoord, gl_Position;
 extern thread_local gl_PerVertex gl_in[3];

@@ -25,6 +25,17 @@ thread_local uint gAxis;
 thread_local uvec4 gAABB;
 thread_local uvec2 gDepthRange;
 
+uint *uSobol;
+uint uDimension;
+sampler2D uEnvironmentMap, uNoise;
+usampler2D uEnvMapAliasTable;
+image2D uColor, uNormal;
+uint uBounce, uLightType;
+float uConstColor[3], uEnvMapRotation, uEnvMapMultiplier;
+namespace ref_pt {
+image2D uAlbedo; // path_tracer.comp's albedo target (the voxelizer's uAlbedo is its push constant)
+}
+
 static thread_local vec4 g_emitted[3];
 static thread_local int g_emit_count;
 void EmitVertex() {
@@ -47,6 +58,21 @@ using namespace ::ref_util;
 #include "gen_voxelizer_geom.hpp"
 #include "gen_voxelizer_conservative_geom.hpp"
 #include "gen_voxelizer_frag.hpp"
+#include "gen_sobol.hpp"
+#include "gen_mis.hpp"
+#include "gen_environment_map.hpp"
+#include "gen_sobol_comp.hpp"
+namespace ref_pt {
+using namespace ::ref_octree;
+using namespace ::ref_camera;
+using namespace ::ref_util;
+using namespace ::ref_diffuse;
+using namespace ::ref_mis;
+using namespace ::ref_envmap;
+using namespace ::ref_sobol;
+} // namespace ref_pt
+#include "gen_path_tracer_comp.hpp"
+#include "gen_envmap_cpp.hpp"
 
 static uint group_x_64(uint x) { return (x >> 6u) + ((x & 0x3fu) ? 1u : 0u); }
 
@@ -251,6 +277,97 @@ uint64_t ref_voxelize_triangle(const float *v9, uint32_t albedo, uint32_t level,
 			++n;
 		}
 	return n;
+}
+
+// ------------------------------------------------------------------------------------------ path tracer
+// The direction numbers of shader/sobol.comp (kMatrices, 64 x 32), as the shader source defines them.
+static uint g_ref_matrices[64][32];
+static bool g_ref_matrices_saved = false;
+static void save_ref_matrices() {
+	if (!g_ref_matrices_saved) std::memcpy(g_ref_matrices, ref_sobolc::kMatrices, sizeof(g_ref_matrices));
+	g_ref_matrices_saved = true;
+}
+void ref_sobol_matrices(uint32_t *out) {
+	save_ref_matrices();
+	std::memcpy(out, g_ref_matrices, sizeof(g_ref_matrices));
+}
+// Runs shader/sobol.comp with other direction numbers (null: the shader's own).
+static void use_matrices(const uint32_t *m) {
+	save_ref_matrices();
+	std::memcpy(ref_sobolc::kMatrices, m ? (const void *)m : (const void *)g_ref_matrices, sizeof(g_ref_matrices));
+}
+
+// Sobol::CmdNext (src/Sobol.cpp:46-52): one group of 64 invocations of shader/sobol.comp.
+void ref_sobol_next(uint32_t *sobol, uint32_t dim) {
+	use_matrices(nullptr);
+	uSobol = sobol;
+	uDimension = dim;
+	for (uint i = 0; i < 64u; ++i) {
+		gl_GlobalInvocationID = uvec3(i, 0u, 0u);
+		ref_sobolc::sobol_main();
+	}
+}
+
+// EnvironmentMap::weigh_hdr_image + generate_alias_table on an rgba float image (alpha overwritten with
+// the weights).  Returns 0 when the weight sum is not positive (the reference would divide by it).
+int ref_envmap_build(float *rgba, uint32_t w, uint32_t h, uint32_t *alias) {
+	EnvironmentMap::HdrImg img{w, h, rgba};
+	std::vector<double> weights = EnvironmentMap::weigh_hdr_image(&img);
+	double sum = 0.0;
+	for (double x : weights) sum += x;
+	if (!(sum > 0.0)) return 0;
+	EnvironmentMap::generate_alias_table(&weights, (EnvironmentMap::AliasPair *)alias);
+	return 1;
+}
+
+// PathTracer::CmdRender (src/PathTracer.cpp:205-227), `samples` times: shader/path_tracer.comp over
+// group_8(width) x group_8(height) groups of 8 x 8, then Sobol::CmdNext over (bounce + 1) * 2 dimensions
+// (PathTracer::Reset, src/PathTracer.cpp:201), with the shader's direction numbers or `matrices` (64 x 32)
+// when given.  noise: 256 x 256 RG8 as the R8G8_UNORM texture reads it.
+void ref_path_trace(const uint32_t *pool, const float *cam16, uint32_t width, uint32_t height, uint32_t bounce,
+                    uint32_t light_type, const float *const_color, float rot, float mult, const float *env_texels,
+                    const uint32_t *env_alias, uint32_t env_w, uint32_t env_h, uint32_t *sobol, const uint8_t *noise,
+                    float *color, uint32_t *albedo, uint32_t *normal, uint32_t samples, const uint32_t *matrices) {
+	uOctree = (uint *)pool;
+	uPosition = vec4(cam16[0], cam16[1], cam16[2], cam16[3]);
+	uLook = vec4(cam16[4], cam16[5], cam16[6], cam16[7]);
+	uSide = vec4(cam16[8], cam16[9], cam16[10], cam16[11]);
+	uUp = vec4(cam16[12], cam16[13], cam16[14], cam16[15]);
+	uBounce = bounce;
+	uLightType = light_type;
+	for (int k = 0; k < 3; ++k) uConstColor[k] = const_color[k];
+	uEnvMapRotation = rot;
+	uEnvMapMultiplier = mult;
+	uEnvironmentMap = sampler2D{env_texels, (int)env_w, (int)env_h};
+	uEnvMapAliasTable = usampler2D{env_alias, (int)env_w, (int)env_h};
+	std::vector<float> nz(256 * 256 * 4);
+	for (int i = 0; i < 256 * 256; ++i) {
+		nz[4 * i] = (float)noise[2 * i] / 255.0f;
+		nz[4 * i + 1] = (float)noise[2 * i + 1] / 255.0f;
+		nz[4 * i + 2] = 0.0f;
+		nz[4 * i + 3] = 1.0f;
+	}
+	uNoise = sampler2D{nz.data(), 256, 256};
+	uColor = image2D{color, (int)width, (int)height, 0};
+	ref_pt::uAlbedo = image2D{albedo, (int)width, (int)height, 1};
+	uNormal = image2D{normal, (int)width, (int)height, 2};
+	uSobol = sobol;
+	const uint gx = (width + 7u) / 8u * 8u, gy = (height + 7u) / 8u * 8u;
+	for (uint32_t s = 0; s < samples; ++s) {
+		uSobol = sobol;
+		for (uint y = 0; y < gy; ++y)
+			for (uint x = 0; x < gx; ++x) {
+				gl_GlobalInvocationID = uvec3(x, y, 0u);
+				ref_pt::pt_main();
+			}
+		use_matrices(matrices);
+		uDimension = (bounce + 1u) * 2u;
+		for (uint i = 0; i < 64u; ++i) {
+			gl_GlobalInvocationID = uvec3(i, 0u, 0u);
+			ref_sobolc::sobol_main();
+		}
+	}
+	use_matrices(nullptr);
 }
 
 } // extern "C"

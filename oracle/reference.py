@@ -18,6 +18,8 @@ LIB_PATH = os.path.join(HERE, "_ref", "libsvo_ref.so")
 REFERENCE_DIR = os.environ.get("SVO_REFERENCE", "/root/reference")
 
 _lib = None
+_lib_etrig = None
+LIB_ETRIG_PATH = os.path.join(HERE, "_ref", "libsvo_ref_etrig.so")
 
 
 def build() -> bool:
@@ -36,12 +38,16 @@ def available() -> bool:
         return False
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        if not os.path.exists(LIB_PATH):
+def lib(engine_trig: bool = False):
+    """The reference build; engine_trig selects the one whose GLSL sin / cos / atan / acos are the
+    engine's restatements instead of libm's."""
+    global _lib, _lib_etrig
+    cached = _lib_etrig if engine_trig else _lib
+    if cached is None:
+        path = LIB_ETRIG_PATH if engine_trig else LIB_PATH
+        if not os.path.exists(path):
             build()
-        L = ctypes.CDLL(LIB_PATH)
+        L = ctypes.CDLL(path)
         P, u32, u64, i32, f32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int, ctypes.c_float
         L.ref_build.argtypes = [P, u32, u32, P, u64]
         L.ref_build.restype = u64
@@ -52,8 +58,17 @@ def lib():
         L.ref_diffuse_sample.argtypes = [P, f32, f32, P]
         L.ref_voxelize_triangle.argtypes = [P, u32, u32, i32, P, u64]
         L.ref_voxelize_triangle.restype = u64
-        _lib = L
-    return _lib
+        L.ref_sobol_matrices.argtypes = [P]
+        L.ref_sobol_next.argtypes = [P, u32]
+        L.ref_envmap_build.argtypes = [P, u32, u32, P]
+        L.ref_envmap_build.restype = i32
+        L.ref_path_trace.argtypes = [P, P, u32, u32, u32, u32, P, f32, f32, P, P, u32, u32, P, P, P, P, P, u32, P]
+        if engine_trig:
+            _lib_etrig = L
+        else:
+            _lib = L
+        cached = L
+    return cached
 
 
 def _p(a):
@@ -124,3 +139,50 @@ def voxelize_triangle(v9_ref: np.ndarray, albedo: int, level: int, conservative_
         if n <= cap:
             return out[:n]
         cap = int(n)
+
+
+def sobol_matrices() -> np.ndarray:
+    """kMatrices of shader/sobol.comp, (64, 32) uint32."""
+    out = np.zeros((64, 32), np.uint32)
+    lib().ref_sobol_matrices(_p(out))
+    return out
+
+
+def sobol_next(sobol: np.ndarray, dim: int) -> None:
+    """shader/sobol.comp (one group of 64 invocations) on a uint32 state array, in place."""
+    assert sobol.dtype == np.uint32 and sobol.flags.c_contiguous
+    lib().ref_sobol_next(_p(sobol), dim)
+
+
+def envmap_build(rgba: np.ndarray):
+    """EnvironmentMap::weigh_hdr_image + generate_alias_table: (texels with the weight in alpha, alias
+    table (h, w, 2)), or None for an image of zero weight."""
+    tex = np.array(rgba, np.float32, copy=True, order="C")
+    h, w = tex.shape[:2]
+    alias = np.zeros((h, w, 2), np.uint32)
+    if not lib().ref_envmap_build(_p(tex), w, h, _p(alias)):
+        return None
+    return tex, alias
+
+
+def path_trace(pool: np.ndarray, cam, width: int, height: int, bounce: int, sobol: np.ndarray, noise: np.ndarray,
+               color: np.ndarray, albedo: np.ndarray, normal: np.ndarray, light_type: int = 0,
+               const_color=(5.0, 5.0, 5.0), rotation: float = 0.0, multiplier: float = 1.0, env=None,
+               samples: int = 1, engine_trig: bool = False, matrices: np.ndarray | None = None) -> None:
+    """shader/path_tracer.comp + shader/sobol.comp, `samples` times, updating the targets and the Sobol
+    state in place (color (h, w, 4) float32; albedo / normal (h, w) uint32 rgba8 words).  matrices: other
+    Sobol direction numbers (64 x 32) for sobol.comp to run with."""
+    cam16 = np.ascontiguousarray(np.frombuffer(np.asarray(cam).tobytes(), np.float32))
+    cc = np.ascontiguousarray(const_color, np.float32)
+    if env is None:
+        tex, alias, ew, eh = np.zeros(4, np.float32), np.zeros(2, np.uint32), 0, 0
+    else:
+        tex, alias = np.ascontiguousarray(env[0], np.float32), np.ascontiguousarray(env[1], np.uint32)
+        eh, ew = tex.shape[0], tex.shape[1]
+    for a in (sobol, color, albedo, normal):
+        assert a.flags.c_contiguous
+    lib(engine_trig).ref_path_trace(_p(np.ascontiguousarray(pool, np.uint32)), _p(cam16), width, height, bounce,
+                                    light_type,
+                         _p(cc), rotation, multiplier, _p(tex), _p(alias), ew, eh, _p(sobol),
+                         _p(np.ascontiguousarray(noise, np.uint8)), _p(color), _p(albedo), _p(normal), samples,
+                         None if matrices is None else _p(np.ascontiguousarray(matrices, np.uint32)))

@@ -1,14 +1,15 @@
 """GB300-native sparse-voxel-octree engine: voxelize -> build -> ray march, in hand-written sm_103a CUDA.
 
 The compute lives in libsvo.so (C ABI: include/svo.h).  This package holds its ctypes binding, the
-host-side mirror of the reference's Voxelizer / OctreeBuilder / Octree / OctreeTracer classes, the
+host-side mirror of the reference's Voxelizer / OctreeBuilder / Octree / OctreeTracer / PathTracer classes, the
 binary formats and the synthetic benchmark scenes.
 """
 import importlib
 
 from .formats import CAMERA_DTYPE, HIT_DTYPE, RAY_DTYPE, TRIANGLE_DTYPE  # noqa: F401
 
-_API_NAMES = ("Voxelizer", "OctreeBuilder", "Octree", "OctreeTracer", "voxelize", "raycast")
+_API_NAMES = ("Voxelizer", "OctreeBuilder", "Octree", "OctreeTracer", "PathTracer", "Lighting", "EnvironmentMap",
+              "BatchBuilder", "Server", "voxelize", "raycast")
 
 
 def __getattr__(name):

@@ -46,6 +46,12 @@ class CameraC(ctypes.Structure):
     _fields_ = [("pos", f32 * 4), ("look", f32 * 4), ("side", f32 * 4), ("up", f32 * 4)]
 
 
+class LightingC(ctypes.Structure):
+    """svo_lighting: light type, sun radiance, environment-map rotation / multiplier and handle."""
+    _fields_ = [("type", ctypes.c_uint32), ("sun_radiance", ctypes.c_float * 3), ("envmap_rotation", ctypes.c_float),
+                ("envmap_multiplier", ctypes.c_float), ("envmap", ctypes.c_void_p)]
+
+
 class BatchMesh(ctypes.Structure):
     _fields_ = [("tris", P), ("n_tris", u32), ("level", u32)]
 
@@ -140,6 +146,20 @@ _SIGNATURES = {
     "svo_tune_size_class": ([u64], u32),
     "svo_tune_reset": ([], None),
     "svo_camera_from_angles": ([ctypes.POINTER(f32), f32, f32, f32, f32, ctypes.POINTER(CameraC)], None),
+    "svo_sobol_default_matrices": ([P], i32),
+    "svo_envmap_create": ([P, u32, u32, ctypes.POINTER(P)], i32),
+    "svo_envmap_tables": ([P, P, P], i32),
+    "svo_envmap_destroy": ([P], None),
+    "svo_path_tracer_create": ([u32, u32, u32, ctypes.POINTER(P)], i32),
+    "svo_path_tracer_reset": ([P, u32, u32, u32, P], i32),
+    "svo_path_tracer_set_noise": ([P, P, P], i32),
+    "svo_path_tracer_set_sobol_matrices": ([P, P, P], i32),
+    "svo_path_tracer_render": ([P, ctypes.POINTER(OctreeC), ctypes.POINTER(CameraC), ctypes.POINTER(LightingC), u32, P],
+                               i32),
+    "svo_path_tracer_info": ([P, ctypes.POINTER(u32), ctypes.POINTER(u32)], i32),
+    "svo_path_tracer_images": ([P, ctypes.POINTER(P), ctypes.POINTER(P), ctypes.POINTER(P), ctypes.POINTER(P)], i32),
+    "svo_path_tracer_extract": ([P, u32, P, P], i32),
+    "svo_path_tracer_destroy": ([P], None),
 }
 
 _lib = None

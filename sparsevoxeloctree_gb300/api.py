@@ -397,6 +397,197 @@ class OctreeTracer:
         return rays
 
 
+# ------------------------------------------------------------------------------------------- path tracer
+class EnvironmentMap:
+    """EnvironmentMap (src/EnvironmentMap.hpp:10-54): an HDR image on the device with its pdf weights and
+    alias table.  Reset takes the decoded float image (the reference decodes .exr / .hdr files with
+    tinyexr / stb_image, which are not part of the engine)."""
+
+    def __init__(self):
+        self.m_rotation = 0.0
+        self.m_multiplier = 1.0
+        self._h = ctypes.c_void_p(0)
+        self.width = self.height = 0
+
+    @staticmethod
+    def Create() -> "EnvironmentMap":
+        return EnvironmentMap()
+
+    def Reset(self, rgba: np.ndarray | None = None) -> None:
+        """Reset() empties the map; Reset(image) loads an (h, w, 3|4) float image."""
+        lib = _lib.load()
+        if self._h:
+            lib.svo_envmap_destroy(self._h)
+            self._h = ctypes.c_void_p(0)
+            self.width = self.height = 0
+        if rgba is None:
+            return
+        img = np.asarray(rgba, np.float32)
+        if img.ndim != 3 or img.shape[2] not in (3, 4):
+            raise ValueError("environment map must be (h, w, 3) or (h, w, 4)")
+        if img.shape[2] == 3:
+            img = np.concatenate([img, np.ones(img.shape[:2] + (1,), np.float32)], axis=2)
+        img = np.ascontiguousarray(img)
+        h = ctypes.c_void_p(0)
+        _lib.check(lib.svo_envmap_create(img.ctypes.data_as(ctypes.c_void_p), img.shape[1], img.shape[0],
+                                         ctypes.byref(h)))
+        self._h, self.height, self.width = h, img.shape[0], img.shape[1]
+
+    def Empty(self) -> bool:
+        return not self._h
+
+    def GetTables(self) -> tuple[np.ndarray, np.ndarray]:
+        """(texels (h, w, 4) with the pdf weight in alpha, alias table (h, w, 2) uint32)."""
+        tex = np.zeros((self.height, self.width, 4), np.float32)
+        alias = np.zeros((self.height, self.width, 2), np.uint32)
+        _lib.check(_lib.load().svo_envmap_tables(self._h, tex.ctypes.data_as(ctypes.c_void_p),
+                                                 alias.ctypes.data_as(ctypes.c_void_p)))
+        return tex, alias
+
+    def __del__(self):
+        try:
+            if self._h:
+                _lib.load().svo_envmap_destroy(self._h)
+        except Exception:
+            pass
+
+
+class Lighting:
+    """Lighting (src/Lighting.hpp:7-20): a constant colour or the environment map."""
+
+    kConstantColor = 0
+    kEnvironmentMap = 1
+
+    def __init__(self, environment_map: EnvironmentMap | None = None):
+        self.m_light_type = Lighting.kConstantColor
+        self.m_sun_radiance = [5.0, 5.0, 5.0]  # kDefaultConstantColor
+        self.m_environment_map = environment_map if environment_map is not None else EnvironmentMap.Create()
+
+    @staticmethod
+    def Create(environment_map: EnvironmentMap | None = None) -> "Lighting":
+        return Lighting(environment_map)
+
+    def GetEnvironmentMapPtr(self) -> EnvironmentMap:
+        return self.m_environment_map
+
+    def GetFinalLightType(self) -> int:
+        if self.m_light_type == Lighting.kEnvironmentMap and self.m_environment_map.Empty():
+            return Lighting.kConstantColor
+        return self.m_light_type
+
+    def c_struct(self) -> _lib.LightingC:
+        e = self.m_environment_map
+        return _lib.LightingC(self.GetFinalLightType(), (ctypes.c_float * 3)(*self.m_sun_radiance),
+                              float(e.m_rotation), float(e.m_multiplier), e._h if not e.Empty() else None)
+
+
+class PathTracer:
+    """PathTracer (src/PathTracer.hpp:15-75): progressive path tracing of an octree, the whole path of a
+    pixel sample in one kernel (shader/path_tracer.comp), radiance / albedo / normal accumulated on the
+    device."""
+
+    kDefaultBounce = 4
+
+    def __init__(self):
+        self.m_octree: Octree | None = None
+        self.m_camera = None
+        self.m_lighting: Lighting | None = None
+        self.m_width, self.m_height = 1280, 720  # kDefaultWidth, kDefaultHeight
+        self.m_bounce = PathTracer.kDefaultBounce
+        self._h = ctypes.c_void_p(0)
+
+    @staticmethod
+    def Create(octree: Octree, camera, lighting: Lighting | None = None) -> "PathTracer":
+        pt = PathTracer()
+        pt.m_octree, pt.m_camera = octree, camera
+        pt.m_lighting = lighting if lighting is not None else Lighting.Create()
+        return pt
+
+    def Reset(self, stream=None) -> None:
+        """Targets of m_width x m_height cleared, Sobol state cleared (m_bounce path vertices)."""
+        lib = _lib.load()
+        if not self._h:
+            h = ctypes.c_void_p(0)
+            _lib.check(lib.svo_path_tracer_create(self.m_width, self.m_height, self.m_bounce, ctypes.byref(h)))
+            self._h = h
+        else:
+            _lib.check(lib.svo_path_tracer_reset(self._h, self.m_width, self.m_height, self.m_bounce,
+                                                 _stream(stream)))
+
+    def _handle(self):
+        if not self._h:
+            self.Reset()
+        return self._h
+
+    def SetNoise(self, rg: np.ndarray, stream=None) -> None:
+        """The 256 x 256 RG8 noise texture (e.g. a blue-noise table)."""
+        a = np.ascontiguousarray(rg, np.uint8).reshape(256 * 256 * 2)
+        _lib.check(_lib.load().svo_path_tracer_set_noise(self._handle(), a.ctypes.data_as(ctypes.c_void_p),
+                                                         _stream(stream)))
+        torch.cuda.synchronize()
+
+    def SetSobolMatrices(self, matrices: np.ndarray, stream=None) -> None:
+        """Sobol direction numbers, 64 x 32 uint32."""
+        a = np.ascontiguousarray(matrices, np.uint32).reshape(64 * 32)
+        _lib.check(_lib.load().svo_path_tracer_set_sobol_matrices(self._handle(), a.ctypes.data_as(ctypes.c_void_p),
+                                                                  _stream(stream)))
+        torch.cuda.synchronize()
+
+    def CmdRender(self, stream=None, samples: int = 1) -> None:
+        """PathTracer::CmdRender `samples` times (stream-ordered)."""
+        cam = camera_struct(self.m_camera)
+        oc = self.m_octree.c_struct()
+        light = self.m_lighting.c_struct()
+        _lib.check(_lib.load().svo_path_tracer_render(self._handle(), ctypes.byref(oc), ctypes.byref(cam),
+                                                      ctypes.byref(light), int(samples), _stream(stream)))
+
+    def GetSPP(self) -> int:
+        spp = ctypes.c_uint32(0)
+        _lib.check(_lib.load().svo_path_tracer_info(self._handle(), ctypes.byref(spp), None))
+        return int(spp.value)
+
+    def GetStatus(self) -> int:
+        st = ctypes.c_uint32(0)
+        _lib.check(_lib.load().svo_path_tracer_info(self._handle(), None, ctypes.byref(st)))
+        return int(st.value)
+
+    def _extract(self, image: int) -> np.ndarray:
+        out = np.zeros((self.m_height, self.m_width, 3), np.float32)
+        _lib.check(_lib.load().svo_path_tracer_extract(self._handle(), image, out.ctypes.data_as(ctypes.c_void_p),
+                                                       _stream()))
+        return out
+
+    def ExtractColorImage(self) -> np.ndarray:
+        return self._extract(0)
+
+    def ExtractAlbedoImage(self) -> np.ndarray:
+        return self._extract(1)
+
+    def ExtractNormalImage(self) -> np.ndarray:
+        return self._extract(2)
+
+    def GetImages(self) -> dict:
+        """Device copies of the raw targets: color (h, w, 4) float32, albedo / normal (h, w) int32 words,
+        sobol (65,) int32."""
+        c, a, n, s = (ctypes.c_void_p(0) for _ in range(4))
+        _lib.check(_lib.load().svo_path_tracer_images(self._handle(), ctypes.byref(c), ctypes.byref(a),
+                                                      ctypes.byref(n), ctypes.byref(s)))
+        npx = self.m_width * self.m_height
+        dev = self.m_octree.device if self.m_octree is not None else "cuda"
+        torch.cuda.synchronize()
+        return {"color": _copy_from(c.value, 4 * npx, torch.float32, dev).view(self.m_height, self.m_width, 4),
+                "albedo": _copy_from(a.value, npx, torch.int32, dev).view(self.m_height, self.m_width),
+                "normal": _copy_from(n.value, npx, torch.int32, dev).view(self.m_height, self.m_width),
+                "sobol": _copy_from(s.value, 65, torch.int32, dev)}
+
+    def __del__(self):
+        try:
+            if self._h:
+                _lib.load().svo_path_tracer_destroy(self._h)
+        except Exception:
+            pass
+
+
 # ------------------------------------------------------------------------------------------- batches
 def _copy_from(ptr: int, count: int, dtype: torch.dtype, device="cuda") -> torch.Tensor:
     """Device copy of `count` elements at an engine-owned device address."""

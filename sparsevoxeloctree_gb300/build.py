@@ -30,6 +30,7 @@ UNITS = {
     "batch.cu": [],
     "serve.cu": [],
     "io.cu": [],
+    "pt.cu": ["-Xcompiler", "-ffp-contract=off"],
 }
 HEADERS = ["common.cuh", "svo_internal.h"]
 

@@ -153,41 +153,65 @@ template <bool B> __global__ void build_init(BuildBatch bb, BuildState *gstate) 
 }
 
 // ------------------------------------------------------------------------------------------ dense stage
+// The fragment sweeps (dense_mark, bucket_scatter) take kSweepRuns warp-sized runs of fragments per warp
+// and pass, loading all of them before any is processed: each fragment's work is a short dependent chain
+// (load, bitmap lookups, one atomic per group of a warp), so independent loads in flight set the rate.
+constexpr uint32_t kSweepRuns = 4;
+
+// First run of warp w's pass and the run stride of the sweep.
+SVO_DEV uint64_t sweep_first_run() {
+	return ((uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * kSweepRuns;
+}
+SVO_DEV uint64_t sweep_run_stride() { return (uint64_t)gridDim.x * (blockDim.x >> 5) * kSweepRuns; }
+
 // Sets the depth-D occupancy bit of every fragment and counts the fragments of every bucket.  Per warp,
-// fragments that fall in the same bitmap word (or bucket) are merged first, so one atomic covers them.
-// Bitmap words and buckets are numbered over the whole batch, so merging never mixes meshes.
+// consecutive fragments that fall in the same bitmap word (or bucket) are merged first, so one atomic
+// covers them (a triangle's fragments are consecutive in the list).  Bitmap words and buckets are
+// numbered over the whole batch, so merging never mixes meshes.
 template <bool B>
 __global__ void __launch_bounds__(kTPB) dense_mark(const uint64_t *__restrict__ frags, uint64_t n, BuildBatch bb,
                                                    uint32_t *__restrict__ bcount) {
-	const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-	for (uint64_t f = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; f < ((n + 31ull) & ~31ull); f += stride) {
-		uint32_t word = 0xffffffffu, bit = 0, key = 0xffffffffu;
-		if (f < n) {
-			const uint32_t mi = B ? mesh_search(bb.frag_base, bb.M, (unsigned long long)f) : 0u;
-			const BuildMesh md = mesh_at<B>(bb, mi);
-			uint32_t x, y, z;
-			frag_xyz(__ldcs(frags + f), x, y, z);
-			const uint32_t D = md.dv.D;
-			if (!frag_in_level(x, y, z, md.level)) {
-				flag_bad_fragment(md.state, bb.gstate);
-			} else if (D >= 1) {
-				const uint32_t shift = md.level - D;
-				const uint32_t m = morton(x, y, z, shift);
-				word = md.mark_word + (m >> 5);
-				bit = 1u << (m & 31);
-				key = md.bucket_base + (m >> (3 * (md.bshift - shift))); // a prefix of the depth-D code
-			} else {
-				key = md.bucket_base + morton(x, y, z, md.bshift);
-			}
-			if (word != 0xffffffffu && !SVO_CHECK(word < bb.dense_total, 1u, bb.gstate)) word = 0xffffffffu, bit = 0;
-			if (key != 0xffffffffu && !SVO_CHECK(key < bb.nb_total, 2u, bb.gstate)) key = 0xffffffffu;
+	const uint64_t runs = (n + 31ull) >> 5;
+	const uint32_t lane = lane_id();
+	for (uint64_t r = sweep_first_run(); r < runs; r += sweep_run_stride()) {
+		uint64_t fr[kSweepRuns];
+#pragma unroll
+		for (uint32_t k = 0; k < kSweepRuns; ++k) {
+			const uint64_t f = ((r + k) << 5) + lane;
+			fr[k] = f < n ? __ldcs(frags + f) : 0ull;
 		}
-		const uint32_t peers = __match_any_sync(kFullMask, word);
-		const uint32_t merged = __reduce_or_sync(peers, bit);
-		if (word != 0xffffffffu && lane_id() == (uint32_t)(__ffs(peers) - 1)) atomicOr(bb.dense_bits + word, merged);
-		// fragments per bucket, for the bucketed copy
-		const uint32_t kpeers = __match_any_sync(kFullMask, key);
-		if (key != 0xffffffffu && lane_id() == (uint32_t)(__ffs(kpeers) - 1)) atomicAdd(bcount + key, __popc(kpeers));
+#pragma unroll
+		for (uint32_t k = 0; k < kSweepRuns; ++k) {
+			const uint64_t f = ((r + k) << 5) + lane;
+			uint32_t word = 0xffffffffu, bit = 0, key = 0xffffffffu;
+			if (f < n) {
+				const uint32_t mi = B ? mesh_search(bb.frag_base, bb.M, (unsigned long long)f) : 0u;
+				const BuildMesh md = mesh_at<B>(bb, mi);
+				uint32_t x, y, z;
+				frag_xyz(fr[k], x, y, z);
+				const uint32_t D = md.dv.D;
+				if (!frag_in_level(x, y, z, md.level)) {
+					flag_bad_fragment(md.state, bb.gstate);
+				} else if (D >= 1) {
+					const uint32_t shift = md.level - D;
+					const uint32_t m = morton(x, y, z, shift);
+					word = md.mark_word + (m >> 5);
+					bit = 1u << (m & 31);
+					key = md.bucket_base + (m >> (3 * (md.bshift - shift))); // a prefix of the depth-D code
+				} else {
+					key = md.bucket_base + morton(x, y, z, md.bshift);
+				}
+				if (word != 0xffffffffu && !SVO_CHECK(word < bb.dense_total, 1u, bb.gstate)) word = 0xffffffffu, bit = 0;
+				if (key != 0xffffffffu && !SVO_CHECK(key < bb.nb_total, 2u, bb.gstate)) key = 0xffffffffu;
+			}
+			uint32_t first, last;
+			lane_run(word, lane, first, last);
+			const uint32_t merged = run_or(bit, lane, last);
+			if (word != 0xffffffffu && lane == first) atomicOr(bb.dense_bits + word, merged);
+			// fragments per bucket, for the bucketed copy
+			lane_run(key, lane, first, last);
+			if (key != 0xffffffffu && lane == first) atomicAdd(bcount + key, last - first + 1u);
+		}
 	}
 }
 
@@ -559,56 +583,74 @@ template <bool B>
 __global__ void __launch_bounds__(kTPB) bucket_scatter(const uint64_t *__restrict__ frags, uint64_t n, BuildBatch bb,
                                                        const uint32_t *__restrict__ boff, uint32_t *__restrict__ bfill,
                                                        uint64_t *__restrict__ sorted) {
-	const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+	const uint64_t runs = (n + 31ull) >> 5;
 	const uint32_t lane = lane_id();
-	for (uint64_t f = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; f < ((n + 31ull) & ~31ull); f += stride) {
-		uint32_t key = 0xffffffffu, pad = 0;
-		uint64_t out = 0, send = 0;
-		if (f < n) {
-			const uint32_t mi = B ? mesh_search(bb.frag_base, bb.M, (unsigned long long)f) : 0u;
-			const BuildMesh md = mesh_at<B>(bb, mi);
-			const uint32_t level = md.level;
-			const bool items = level == 1 || level - 1 <= md.dv.D;
-			const uint64_t frag = __ldcs(frags + f);
-			uint32_t x, y, z;
-			frag_xyz(frag, x, y, z);
-			out = frag;
-			if (!frag_in_level(x, y, z, level)) {
-				// skipped (dense_mark reported it)
-			} else if (items && level > 1) { // parent cell m (depth level-1); the bucket key is its prefix
-				const uint32_t *pbits = md.dv.bits + md.parent_off;
-				const uint32_t *pprefix = md.dv.prefix + md.parent_off;
-				const uint32_t leaf_begin = md.state->lv[level].begin;
-				const uint32_t m = morton(x, y, z, 1), w = m >> 5;
-				key = m >> (3 * (md.bshift - 1));
-				out = ((uint64_t)(octant_at(x, y, z, 0) + 8u * (1u + __ldg(pprefix + w) +
-				                                                 __popc(__ldg(pbits + w) & ((1u << (m & 31)) - 1u))) -
-				                  leaf_begin)
-				       << 32) |
-				      ((frag >> 32) & 0xffffffu);
-			} else {
-				key = bucket_of(x, y, z, md.bshift);
-				if (items) // level 1: the leaf words are the root block
-					out = ((uint64_t)octant_at(x, y, z, 0) << 32) | ((frag >> 32) & 0xffffffu);
-			}
-			if (key != 0xffffffffu) {
-				key += md.bucket_base;
-				if (!SVO_CHECK(key < bb.nb_total, 3u, bb.gstate)) key = 0xffffffffu;
-			}
-			pad = md.sorted_pad;
-			send = md.frag_base + md.sorted_pad + md.count;
+	for (uint64_t r = sweep_first_run(); r < runs; r += sweep_run_stride()) {
+		uint64_t out[kSweepRuns], send[kSweepRuns];
+		uint32_t key[kSweepRuns], pad[kSweepRuns], first[kSweepRuns], base[kSweepRuns];
+#pragma unroll
+		for (uint32_t k = 0; k < kSweepRuns; ++k) {
+			const uint64_t f = ((r + k) << 5) + lane;
+			out[k] = f < n ? __ldcs(frags + f) : 0ull;
 		}
-		const uint32_t peers = __match_any_sync(kFullMask, key);
-		const uint32_t leader = __ffs(peers) - 1;
-		uint32_t base = 0;
-		if (key != 0xffffffffu && lane == leader) base = atomicAdd(bfill + key, __popc(peers));
-		base = __shfl_sync(kFullMask, base, leader);
-		if (key != 0xffffffffu) {
-			const uint64_t at = (uint64_t)boff[key] + pad + base + __popc(peers & ((1u << lane) - 1u));
-			if (at < send) // always true after a complete bucket scan (a timed-out scan is reported)
-				sorted[at] = out;
-			else
-				SVO_CHECK_FAIL(4u, bb.gstate);
+#pragma unroll
+		for (uint32_t k = 0; k < kSweepRuns; ++k) {
+			const uint64_t f = ((r + k) << 5) + lane;
+			key[k] = 0xffffffffu, pad[k] = 0, send[k] = 0;
+			if (f < n) {
+				const uint32_t mi = B ? mesh_search(bb.frag_base, bb.M, (unsigned long long)f) : 0u;
+				const BuildMesh md = mesh_at<B>(bb, mi);
+				const uint32_t level = md.level;
+				const bool items = level == 1 || level - 1 <= md.dv.D;
+				const uint64_t frag = out[k];
+				uint32_t x, y, z;
+				frag_xyz(frag, x, y, z);
+				if (!frag_in_level(x, y, z, level)) {
+					// skipped (dense_mark reported it)
+				} else if (items && level > 1) { // parent cell m (depth level-1); the bucket key is its prefix
+					const uint32_t *pbits = md.dv.bits + md.parent_off;
+					const uint32_t *pprefix = md.dv.prefix + md.parent_off;
+					const uint32_t leaf_begin = md.state->lv[level].begin;
+					const uint32_t m = morton(x, y, z, 1), w = m >> 5;
+					key[k] = m >> (3 * (md.bshift - 1));
+					out[k] = ((uint64_t)(octant_at(x, y, z, 0) +
+					                     8u * (1u + __ldg(pprefix + w) +
+					                           __popc(__ldg(pbits + w) & ((1u << (m & 31)) - 1u))) -
+					                     leaf_begin)
+					          << 32) |
+					         ((frag >> 32) & 0xffffffu);
+				} else {
+					key[k] = bucket_of(x, y, z, md.bshift);
+					if (items) // level 1: the leaf words are the root block
+						out[k] = ((uint64_t)octant_at(x, y, z, 0) << 32) | ((frag >> 32) & 0xffffffu);
+				}
+				if (key[k] != 0xffffffffu) {
+					key[k] += md.bucket_base;
+					if (!SVO_CHECK(key[k] < bb.nb_total, 3u, bb.gstate)) key[k] = 0xffffffffu;
+				}
+				pad[k] = md.sorted_pad;
+				send[k] = md.frag_base + md.sorted_pad + md.count;
+			}
+		}
+		// one cursor atomic per run of equal keys in consecutive lanes; the atomics of all runs of
+		// fragments are in flight together
+#pragma unroll
+		for (uint32_t k = 0; k < kSweepRuns; ++k) {
+			uint32_t last;
+			lane_run(key[k], lane, first[k], last);
+			base[k] = 0;
+			if (key[k] != 0xffffffffu && lane == first[k]) base[k] = atomicAdd(bfill + key[k], last - first[k] + 1u);
+		}
+#pragma unroll
+		for (uint32_t k = 0; k < kSweepRuns; ++k) {
+			const uint32_t b = __shfl_sync(kFullMask, base[k], first[k]);
+			if (key[k] != 0xffffffffu) {
+				const uint64_t at = (uint64_t)__ldg(boff + key[k]) + pad[k] + b + (lane - first[k]);
+				if (at < send[k]) // always true after a complete bucket scan (a timed-out scan is reported)
+					sorted[at] = out[k];
+				else
+					SVO_CHECK_FAIL(4u, bb.gstate);
+			}
 		}
 	}
 }
@@ -1078,7 +1120,7 @@ static void launch_dense_and_scatter(const uint64_t *frags, uint64_t n, uint32_t
 	const uint32_t sweep = (uint32_t)sms * (uint32_t)tune_value(kTuneSweepBlocks, tune_level, n);
 	SVO_LAUNCH("build_init", stream, build_init<B><<<M, 256, 0, stream>>>(bb, gstate););
 	SVO_LAUNCH("dense_mark", stream,
-	           dense_mark<B><<<grid_for(n, kTPB, sweep), kTPB, 0, stream>>>(frags, n, bb, bcount););
+	           dense_mark<B><<<grid_for(n, kTPB * kSweepRuns, sweep), kTPB, 0, stream>>>(frags, n, bb, bcount););
 	SVO_LAUNCH("bucket_scan", stream,
 	           bucket_scan<<<(nb_total + kScanTile - 1) / kScanTile, kTPB, 0, stream>>>(bcount, nb_total, boff, blist,
 	                                                                                   gstate, bdescs););
@@ -1097,7 +1139,7 @@ static void launch_dense_and_scatter(const uint64_t *frags, uint64_t n, uint32_t
 	// the bucketed copy: leaf items when the leaf parents are dense (their bitmap is final now), fragments
 	// for the sparse levels otherwise
 	SVO_LAUNCH("bucket_scatter", stream,
-	           bucket_scatter<B><<<grid_for(n, kTPB, sweep), kTPB, 0, stream>>>(frags, n, bb, boff, bfill,
+	           bucket_scatter<B><<<grid_for(n, kTPB * kSweepRuns, sweep), kTPB, 0, stream>>>(frags, n, bb, boff, bfill,
 	                                                                                      sorted););
 }
 

@@ -36,6 +36,28 @@ template <typename T> SVO_DEV T warp_sum(T v) {
 	return v;
 }
 
+// Runs of equal keys in consecutive lanes (called by the full warp): the first and last lane of this
+// lane's run.  Equal keys in separate runs form separate runs.  A shuffle and a ballot instead of
+// __match_any_sync, whose throughput limits warp-merging sweeps.
+SVO_DEV void lane_run(uint32_t key, uint32_t lane, uint32_t &first, uint32_t &last) {
+	const uint32_t prev = __shfl_up_sync(kFullMask, key, 1);
+	const uint32_t heads = __ballot_sync(kFullMask, lane == 0u || key != prev);
+	const uint32_t upto = lane == 31u ? kFullMask : ((2u << lane) - 1u); // lanes 0..lane
+	first = 31u - (uint32_t)__clz(heads & upto);
+	const uint32_t after = heads & ~upto;
+	last = after ? (uint32_t)__ffs(after) - 2u : 31u;
+}
+
+// OR of v over lanes lane..last (called by the full warp); at a run's first lane, the OR of its run.
+SVO_DEV uint32_t run_or(uint32_t v, uint32_t lane, uint32_t last) {
+#pragma unroll
+	for (uint32_t d = 1; d < 32; d <<= 1) {
+		const uint32_t o = __shfl_down_sync(kFullMask, v, d);
+		if (lane + d <= last) v |= o;
+	}
+	return v;
+}
+
 // Exclusive block scan of one value per thread; returns the exclusive prefix and the block total.
 // `warp_tmp` must hold blockDim.x / 32 + 1 elements.
 template <typename T, int TPB> SVO_DEV T block_exclusive_sum(T v, T *warp_tmp, T &total) {

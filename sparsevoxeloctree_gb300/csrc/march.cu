@@ -618,35 +618,47 @@ SVO_DEV void sincos_2pi(float u, float &s_out, float &c_out) {
 	}
 }
 
-// o = hit pos, d = Diffuse_Sample about the hit normal (shader/diffuse.glsl:7-14 with AlignDirection,
-// shader/util.glsl:5-9); misses give d = 0.  (u1, u2) come from a counter hash of (seed, i).
+constexpr float kPi = 3.14159265358979323846f; // PI of shader/util.glsl:4 as a float
+
+// AlignDirection (shader/util.glsl:5-9): dl expressed in the frame (u, v, n) about the unit normal n.
+SVO_DEV void align_direction(const float dl[3], const float nrm[3], float d[3]) {
+	float ref[3] = {0.0f, 0.0f, 0.0f};
+	if (fabsf(nrm[0]) > 0.01f)
+		ref[1] = 1.0f;
+	else
+		ref[0] = 1.0f;
+	float u[3] = {ref[1] * nrm[2] - ref[2] * nrm[1], ref[2] * nrm[0] - ref[0] * nrm[2], ref[0] * nrm[1] - ref[1] * nrm[0]};
+	const float ul = sqrtf((u[0] * u[0] + u[1] * u[1]) + u[2] * u[2]);
+#pragma unroll
+	for (int k = 0; k < 3; ++k) u[k] = u[k] / ul;
+	const float v[3] = {nrm[1] * u[2] - nrm[2] * u[1], nrm[2] * u[0] - nrm[0] * u[2], nrm[0] * u[1] - nrm[1] * u[0]};
+#pragma unroll
+	for (int k = 0; k < 3; ++k) d[k] = (dl[0] * u[k] + dl[1] * v[k]) + dl[2] * nrm[k];
+}
+
+// Diffuse_Sample (shader/diffuse.glsl:7-14): cosine-weighted direction about the unit normal and its pdf.
+SVO_DEV void diffuse_sample(const float nrm[3], float u1, float u2, float d[3], float &pdf) {
+	const float rr = sqrtf(u1);
+	float sn, cs;
+	sincos_2pi(u2, sn, cs);
+	const float dl[3] = {rr * cs, rr * sn, sqrtf(1.0f - u1)};
+	pdf = dl[2] / kPi;
+	align_direction(dl, nrm, d);
+}
+
+// o = hit pos, d = Diffuse_Sample about the hit normal; misses give d = 0.  (u1, u2) come from a
+// counter hash of (seed, i).
 SVO_DEV svo_ray bounce_one(const svo_hit &h, uint64_t i, uint64_t seed) {
 	float d[3] = {0.0f, 0.0f, 0.0f};
 	if (h.flags & SVO_HIT_FLAG_HIT) {
 		const uint64_t z = mix64(seed + 0x9E3779B97F4A7C15ull * (i + 1));
 		const float u1 = (float)(uint32_t)(z >> 40) * (1.0f / 16777216.0f);
 		const float u2 = (float)(uint32_t)((z >> 16) & 0xffffffu) * (1.0f / 16777216.0f);
-		const float rr = sqrtf(u1);
-		float sn, cs;
-		sincos_2pi(u2, sn, cs);
-		const float dl[3] = {rr * cs, rr * sn, sqrtf(1.0f - u1)};
 		const uint32_t ax = SVO_HIT_NORMAL_AXIS(h.flags);
 		float nrm[3] = {0.0f, 0.0f, 0.0f};
 		nrm[ax] = (h.flags & SVO_HIT_NORMAL_NEG) ? -1.0f : 1.0f;
-		float ref[3] = {0.0f, 0.0f, 0.0f};
-		if (fabsf(nrm[0]) > 0.01f)
-			ref[1] = 1.0f;
-		else
-			ref[0] = 1.0f;
-		float u[3] = {ref[1] * nrm[2] - ref[2] * nrm[1], ref[2] * nrm[0] - ref[0] * nrm[2],
-		              ref[0] * nrm[1] - ref[1] * nrm[0]};
-		const float ul = sqrtf((u[0] * u[0] + u[1] * u[1]) + u[2] * u[2]);
-#pragma unroll
-		for (int k = 0; k < 3; ++k) u[k] = u[k] / ul;
-		const float v[3] = {nrm[1] * u[2] - nrm[2] * u[1], nrm[2] * u[0] - nrm[0] * u[2],
-		                    nrm[0] * u[1] - nrm[1] * u[0]};
-#pragma unroll
-		for (int k = 0; k < 3; ++k) d[k] = (dl[0] * u[k] + dl[1] * v[k]) + dl[2] * nrm[k];
+		float pdf;
+		diffuse_sample(nrm, u1, u2, d, pdf);
 	}
 	svo_ray r;
 	r.o[0] = h.pos[0], r.o[1] = h.pos[1], r.o[2] = h.pos[2];
@@ -657,6 +669,273 @@ SVO_DEV svo_ray bounce_one(const svo_hit &h, uint64_t i, uint64_t seed) {
 __global__ void bounce_kernel(const svo_hit *__restrict__ hits, uint32_t n, uint64_t seed, svo_ray *__restrict__ rays) {
 	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
 		rays[i] = bounce_one(hits[i], i, seed);
+}
+
+// ------------------------------------------------------------------------------------ path tracer
+// shader/path_tracer.comp:32-135 per pixel, fused on the device: the camera ray, every bounce's leaf
+// march, the environment light's shadow march, MIS weights and the accumulation into the target images,
+// one lane per pixel for the whole path.  Transcendentals are this file's own restatements (rounded
+// operation by operation like the march), so the oracle reproduces every value bit for bit; the
+// reference's GPU evaluates sin/cos/atan/acos with its own approximations.
+
+// atan(z) for 0 <= z <= 1: two half-angle reductions z' = z / (1 + sqrt(1 + z^2)) (atan z = 2 atan z'),
+// which leave |z''| <= tan(pi/16), then the Taylor series of atan to the z^15 term.
+SVO_DEV float atan_unit(float z) {
+	z = z / (1.0f + sqrtf(1.0f + z * z));
+	z = z / (1.0f + sqrtf(1.0f + z * z));
+	const float z2 = z * z;
+	float p = -1.0f / 15.0f;
+	p = p * z2 + 1.0f / 13.0f;
+	p = p * z2 + -1.0f / 11.0f;
+	p = p * z2 + 1.0f / 9.0f;
+	p = p * z2 + -1.0f / 7.0f;
+	p = p * z2 + 1.0f / 5.0f;
+	p = p * z2 + -1.0f / 3.0f;
+	p = p * z2 + 1.0f;
+	return 4.0f * (z * p);
+}
+
+// sin and cos of x radians: sincos_2pi of frac(x / (2 pi)).
+SVO_DEV void sincos_rad(float x, float &s, float &c) {
+	float u = x * 0.159154943091895336f;
+	u = u - floorf(u);
+	sincos_2pi(u, s, c);
+}
+
+// GLSL atan(y, x) in [-pi, pi] (0 for x = y = 0, which GLSL leaves undefined).
+SVO_DEV float atan2_svo(float y, float x) {
+	const float ax = fabsf(x), ay = fabsf(y);
+	if (ax == 0.0f && ay == 0.0f) return 0.0f;
+	float a = ay <= ax ? atan_unit(ay / ax) : 1.57079632679489662f - atan_unit(ax / ay);
+	if (x < 0.0f) a = kPi - a;
+	return y < 0.0f ? -a : a;
+}
+
+// GLSL acos(x) in [0, pi] as atan(sqrt((1 - x)(1 + x)), x); x is clamped to [-1, 1].
+SVO_DEV float acos_svo(float x) {
+	x = fminf(fmaxf(x, -1.0f), 1.0f);
+	return atan2_svo(sqrtf((1.0f - x) * (1.0f + x)), x);
+}
+
+// texture(uEnvironmentMap, uv) with VK_FILTER_LINEAR and VK_SAMPLER_ADDRESS_MODE_REPEAT
+// (src/EnvironmentMap.cpp:10): the 4 texels around (u W - 1/2, v H - 1/2), integer coordinates wrapped,
+// weights (1-a)(1-b), a(1-b), (1-a)b, ab summed in that order.
+SVO_DEV float4 env_texture(const EnvMapView &e, float u, float v) {
+	const float x = u * (float)e.width - 0.5f, y = v * (float)e.height - 0.5f;
+	const float fx = floorf(x), fy = floorf(y);
+	const float a = x - fx, b = y - fy;
+	const int64_t W = e.width, H = e.height;
+	const int64_t i0 = (((int64_t)fx % W) + W) % W, j0 = (((int64_t)fy % H) + H) % H;
+	const int64_t i1 = i0 + 1 == W ? 0 : i0 + 1, j1 = j0 + 1 == H ? 0 : j0 + 1;
+	const float4 t00 = __ldg(e.texels + j0 * W + i0), t10 = __ldg(e.texels + j0 * W + i1);
+	const float4 t01 = __ldg(e.texels + j1 * W + i0), t11 = __ldg(e.texels + j1 * W + i1);
+	const float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b), w01 = (1.0f - a) * b, w11 = a * b;
+	float4 r;
+	r.x = ((w00 * t00.x + w10 * t10.x) + w01 * t01.x) + w11 * t11.x;
+	r.y = ((w00 * t00.y + w10 * t10.y) + w01 * t01.y) + w11 * t11.y;
+	r.z = ((w00 * t00.z + w10 * t10.z) + w01 * t01.z) + w11 * t11.z;
+	r.w = ((w00 * t00.w + w10 * t10.w) + w01 * t01.w) + w11 * t11.w;
+	return r;
+}
+
+constexpr float kTwoPiPi = 2.0f * kPi * kPi; // 2 * PI * PI of shader/environment_map.glsl:24,45
+
+// EnvMap_Dir2Coord + texture (shader/environment_map.glsl:16-25): the filtered texel in direction d; its w
+// over 2 pi^2 sqrt(1 - d.y^2) is EnvMap_PDF.
+SVO_DEV float4 env_lookup(const EnvMapView &e, const float d[3], float rot) {
+	const float u = (atan2_svo(d[0], d[2]) + rot) / kPi * 0.5f;
+	const float v = acos_svo(d[1]) / kPi;
+	return env_texture(e, u, v);
+}
+
+// EnvMap_Sample (shader/environment_map.glsl:31-48): alias-table pick of a texel, its centre's direction
+// (phi = 2 PI u - rot, theta = PI v as the shader forms them), radiance and pdf.
+SVO_DEV void env_sample(const EnvMapView &e, float s0, float s1, float rot, float d[3], float light[3], float &pdf) {
+	const uint32_t sz = e.width * e.height;
+	const uint32_t idx = min((uint32_t)(s0 * (float)sz), sz - 1u);
+	const uint32_t prob = (uint32_t)(s1 * 4294967296.0f);
+	uint32_t pix = idx;
+	const uint2 al = __ldg(e.alias + idx);
+	if (prob > al.x) pix = al.y;
+	const uint32_t py = pix / e.width, px = pix - py * e.width;
+	const float u = ((float)px + 0.5f) / (float)e.width, v = ((float)py + 0.5f) / (float)e.height;
+	const float phi = 2.0f * kPi * u - rot, theta = kPi * v;
+	float st, ct, sp, cp;
+	sincos_rad(theta, st, ct);
+	sincos_rad(phi, sp, cp);
+	const float4 tx = __ldg(e.texels + pix);
+	light[0] = tx.x, light[1] = tx.y, light[2] = tx.z;
+	pdf = tx.w / (kTwoPiPi * st);
+	d[0] = st * sp, d[1] = ct, d[2] = st * cp;
+}
+
+// MIS_PowerHeuristic (shader/mis.glsl:4-7).
+SVO_DEV float mis_power(float a, float b) {
+	const float t = a * a;
+	return t / (b * b + t);
+}
+
+// Sobol_GetVec2 component (shader/sobol.glsl:10): the 32-bit value over 2^32.
+SVO_DEV float sobol_f(uint32_t v) { return (float)v * 2.3283064365386963e-10f; }
+
+// The 5-argument Octree_RayMarchLeaf the path tracer calls (shader/octree.glsl:342-502): its direction
+// clamp keeps |d| >= EPS (applied here; the march's own > EPS clamp then leaves d unchanged) and its
+// outputs are hit, o_pos, o_color = rgb * (1/255) (:499) and o_normal.
+template <int STRIDE>
+SVO_DEV bool pt_leaf(const PtArgs &a, const float o[3], const float dir[3], uint32_t *stack, float pos[3],
+                     float albedo[3], float nrm[3]) {
+	float d[3];
+#pragma unroll
+	for (int k = 0; k < 3; ++k) d[k] = fabsf(dir[k]) >= kEps ? dir[k] : (dir[k] >= 0.0f ? kEps : -kEps);
+	MarchOut m;
+	uint32_t nf;
+	march_ray<STRIDE>(a.pool, a.range, a.level, o, d, stack, m, nf, a.status);
+	const uint32_t flags = m.voxel_hi >> 16;
+#pragma unroll
+	for (int k = 0; k < 3; ++k) {
+		pos[k] = m.pos[k];
+		albedo[k] = (float)((m.node >> (8 * k)) & 0xffu) * 0.00392156862745098f;
+		nrm[k] = 0.0f;
+	}
+	nrm[(flags >> 1) & 3u] = (flags & SVO_HIT_NORMAL_NEG) ? -1.0f : 1.0f;
+	return (flags & SVO_HIT_FLAG_HIT) != 0u;
+}
+
+// Accumulation targets: rgba8 unorm / snorm words as imageStore writes them (round to nearest, ties
+// up, after clamping) and imageLoad reads them back.
+SVO_DEV float unorm8_load(uint32_t w, int k) { return (float)((w >> (8 * k)) & 0xffu) / 255.0f; }
+SVO_DEV uint32_t unorm8_store(float v) { return (uint32_t)floorf(fminf(fmaxf(v, 0.0f), 1.0f) * 255.0f + 0.5f); }
+SVO_DEV float snorm8_load(uint32_t w, int k) {
+	return fmaxf((float)(int32_t)(int8_t)((w >> (8 * k)) & 0xffu) / 127.0f, -1.0f);
+}
+SVO_DEV uint32_t snorm8_store(float v) {
+	return (uint32_t)(int32_t)floorf(fminf(fmaxf(v, -1.0f), 1.0f) * 127.0f + 0.5f) & 0xffu;
+}
+
+// One sample of pixel (x, y): ConstColorPathTrace / EnvMapPathTrace (shader/path_tracer.comp:32-109) and
+// the running means of main() (shader/path_tracer.comp:111-135).
+template <uint32_t LIGHT, int STRIDE>
+SVO_DEV void pt_pixel(const PtArgs &a, uint32_t x, uint32_t y, uint32_t spp, float s0x, float s0y, uint32_t *stack) {
+	const uint32_t ni = (((y & 255u) << 8) | (x & 255u)) * 2u;
+	const float nz[2] = {(float)__ldg(a.noise + ni) / 255.0f, (float)__ldg(a.noise + ni + 1) / 255.0f};
+	float o[3] = {a.cam.pos[0], a.cam.pos[1], a.cam.pos[2]}, d[3];
+	gen_dir(a.cam, ((float)x + s0x) / (float)a.width, ((float)y + s0y) / (float)a.height, d);
+
+	float acc[3] = {1.0f, 1.0f, 1.0f}, rad[3] = {0.0f, 0.0f, 0.0f};
+	float dalb[3] = {0.0f, 0.0f, 0.0f}, dnrm[3] = {0.0f, 0.0f, 0.0f};
+	float pos[3], alb[3], nrm[3];
+	if (pt_leaf<STRIDE>(a, o, d, stack, pos, alb, nrm)) {
+#pragma unroll
+		for (int k = 0; k < 3; ++k) acc[k] *= alb[k], dalb[k] = alb[k], dnrm[k] = nrm[k];
+		for (uint32_t cur = 1; cur < a.bounce; ++cur) {
+			float samp[2] = {sobol_f(__ldg(a.sobol + 2 * cur)) + nz[0], sobol_f(__ldg(a.sobol + 2 * cur + 1)) + nz[1]};
+			samp[0] = samp[0] - floorf(samp[0]);
+			samp[1] = samp[1] - floorf(samp[1]);
+#pragma unroll
+			for (int k = 0; k < 3; ++k) o[k] = pos[k];
+			if (LIGHT == 1) { // multiple importance sampling, light sample
+				float ld[3], light[3], light_pdf;
+				env_sample(a.env, samp[0], samp[1], a.env_rotation, ld, light, light_pdf);
+				const float ndd = (nrm[0] * ld[0] + nrm[1] * ld[1]) + nrm[2] * ld[2];
+				if (ndd > 0.0f && !isnan(light_pdf) && light_pdf > 0.0f) {
+					float t, sz;
+					if (!march_traverse<false, STRIDE>(a.pool, a.range, a.level, o, ld, 0.0f, 0.0f, stack, t, sz,
+					                                   a.status)) {
+						const float bsdf_pdf = ndd / kPi;
+						const float w = mis_power(light_pdf, bsdf_pdf);
+#pragma unroll
+						for (int k = 0; k < 3; ++k)
+							rad[k] += acc[k] * light[k] * a.env_multiplier * w * ndd * (1.0f / kPi) / light_pdf;
+					}
+				}
+			}
+			// Diffuse_Sample (shader/diffuse.glsl:7-14) with phi = 2 * PI * samp.y as the shader forms it
+			float bsdf_pdf;
+			{
+				const float r = sqrtf(samp[0]), phi = 2.0f * kPi * samp[1];
+				float sn, cs;
+				sincos_rad(phi, sn, cs);
+				const float dl[3] = {r * cs, r * sn, sqrtf(1.0f - samp[0])};
+				bsdf_pdf = dl[2] / kPi;
+				align_direction(dl, nrm, d);
+			}
+			if (pt_leaf<STRIDE>(a, o, d, stack, pos, alb, nrm)) {
+#pragma unroll
+				for (int k = 0; k < 3; ++k) acc[k] *= alb[k];
+			} else {
+				if (LIGHT == 1) { // multiple importance sampling, bsdf sample
+					// EnvMap_PDF and EnvMap_Radiance read the same filtered texel
+					const float4 env = env_lookup(a.env, d, a.env_rotation);
+					const float light_pdf = env.w / (kTwoPiPi * sqrtf(1.0f - d[1] * d[1]));
+					if (!isnan(light_pdf) && light_pdf > 0.0f) {
+						const float w = mis_power(bsdf_pdf, light_pdf);
+						const float e3[3] = {env.x, env.y, env.z};
+#pragma unroll
+						for (int k = 0; k < 3; ++k) rad[k] += acc[k] * e3[k] * a.env_multiplier * w;
+					}
+				} else {
+#pragma unroll
+					for (int k = 0; k < 3; ++k) rad[k] = acc[k] * a.const_color[k];
+				}
+				break;
+			}
+		}
+	} else if (LIGHT == 1) {
+		const float4 env = env_lookup(a.env, d, a.env_rotation);
+		rad[0] = env.x, rad[1] = env.y, rad[2] = env.z;
+	} else {
+#pragma unroll
+		for (int k = 0; k < 3; ++k) rad[k] = a.const_color[k];
+	}
+
+	const size_t p = (size_t)y * a.width + x;
+	const float fs = (float)spp, fn = (float)(spp + 1u);
+	const float4 c = a.color[p];
+	a.color[p] = make_float4((c.x * fs + rad[0]) / fn, (c.y * fs + rad[1]) / fn, (c.z * fs + rad[2]) / fn, 1.0f);
+	const uint32_t wa = a.albedo[p], wn = a.normal[p];
+	uint32_t oa = 255u << 24, on = 127u << 24;
+#pragma unroll
+	for (int k = 0; k < 3; ++k) {
+		oa |= unorm8_store((unorm8_load(wa, k) * fs + dalb[k]) / fn) << (8 * k);
+		on |= snorm8_store((snorm8_load(wn, k) * fs + dnrm[k]) / fn) << (8 * k);
+	}
+	a.albedo[p] = oa;
+	a.normal[p] = on;
+}
+
+// One sample per pixel; warps claim 8x4-pixel tiles from a ticket like the camera march.
+template <uint32_t LIGHT>
+__global__ void __launch_bounds__(kMarchTPB) pt_kernel(PtArgs a) {
+	__shared__ uint32_t s_stack[SVO_LEVEL_MAX * kMarchTPB];
+	uint32_t *stack = s_stack + threadIdx.x;
+	const uint32_t lane = lane_id();
+	const uint32_t tiles_x = (a.width + 7u) / 8u;
+	const uint64_t slots = (uint64_t)tiles_x * ((a.height + 3u) / 4u) * 32u;
+	const uint32_t spp = __ldg(a.sobol + 2u * (a.bounce + 1u)); // Sobol_Current((uBounce + 1) << 1)
+	const float s0x = sobol_f(__ldg(a.sobol)), s0y = sobol_f(__ldg(a.sobol + 1));
+	for (;;) {
+		unsigned long long base = 0;
+		if (lane == 0) base = atomicAdd(a.ticket, 32ull);
+		base = __shfl_sync(kFullMask, base, 0);
+		if (base >= slots) break;
+		const uint64_t slot = base + lane;
+		const uint32_t tile = (uint32_t)(slot >> 5), in = (uint32_t)(slot & 31u);
+		const uint32_t x = (tile % tiles_x) * 8u + (in & 7u), y = (tile / tiles_x) * 4u + (in >> 3);
+		if (x < a.width && y < a.height) pt_pixel<LIGHT, kMarchTPB>(a, x, y, spp, s0x, s0y, stack);
+	}
+}
+
+// Sobol::CmdNext (shader/sobol.comp:70-86): c = index of the lowest zero bit of the sample index, which
+// then increments; every dimension's value takes the XOR of its direction number c.
+__global__ void sobol_next_kernel(uint32_t *sobol, const uint32_t *__restrict__ matrices, uint32_t dim) {
+	__shared__ uint32_t c;
+	if (threadIdx.x == 0) {
+		const uint32_t i = sobol[dim];
+		c = (uint32_t)__ffs(~i) - 1u; // 0xffffffff when every bit is set: no step
+		sobol[dim] = i + 1u;
+	}
+	__syncthreads();
+	if (threadIdx.x < dim && c < 32u) sobol[threadIdx.x] ^= matrices[threadIdx.x * 32u + c];
 }
 
 // ------------------------------------------------------------------------------------ shared launches
@@ -845,6 +1124,25 @@ cudaError_t occlude_launch(const MarchArgs &a, uint32_t *occluded, cudaStream_t 
 	const uint64_t blocks_needed = ((uint64_t)a.n / 32 + kMarchTPB / 32) / (kMarchTPB / 32);
 	const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(blocks_needed, (uint64_t)sms * 16));
 	SVO_LAUNCH("occlude", stream, occlude_kernel<<<blocks, kMarchTPB, 0, stream>>>(a, occluded););
+	return cudaGetLastError();
+}
+
+cudaError_t pt_render_launch(const PtArgs &a, cudaStream_t stream) {
+	cudaError_t e = cudaMemsetAsync(a.ticket, 0, sizeof(unsigned long long), stream);
+	if (e != cudaSuccess || a.width == 0 || a.height == 0) return e;
+	const int sms = device_sm_count();
+	const uint64_t slots = (uint64_t)((a.width + 7u) / 8u) * ((a.height + 3u) / 4u) * 32u;
+	const uint64_t blocks_needed = (slots / 32 + kMarchTPB / 32 - 1) / (kMarchTPB / 32);
+	const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(blocks_needed, (uint64_t)sms * 16));
+	if (a.light_type == 1)
+		SVO_LAUNCH("pt_envmap", stream, pt_kernel<1><<<blocks, kMarchTPB, 0, stream>>>(a););
+	else
+		SVO_LAUNCH("pt_const", stream, pt_kernel<0><<<blocks, kMarchTPB, 0, stream>>>(a););
+	return cudaGetLastError();
+}
+
+cudaError_t sobol_next_launch(uint32_t *sobol, const uint32_t *matrices, uint32_t dim, cudaStream_t stream) {
+	SVO_LAUNCH("sobol_next", stream, sobol_next_kernel<<<1, 64, 0, stream>>>(sobol, matrices, dim););
 	return cudaGetLastError();
 }
 

@@ -263,6 +263,36 @@ cudaError_t beam_launch(const MarchArgs &a, float *beam, cudaStream_t stream);
 cudaError_t occlude_launch(const MarchArgs &a, uint32_t *occluded, cudaStream_t stream);
 cudaError_t bounce_launch(const svo_hit *hits, uint32_t n, uint64_t seed, svo_ray *rays, cudaStream_t stream);
 
+// Path tracer (shader/path_tracer.comp as PathTracer::CmdRender dispatches it, src/PathTracer.cpp:205-227).
+// The environment map as shader/environment_map.glsl samples it: texels = (radiance rgb, pdf weight) and
+// the alias table (prob, alias) per texel, both row-major width x height.
+struct EnvMapView {
+	const float4 *texels;
+	const uint2 *alias;
+	uint32_t width, height;
+};
+struct PtArgs {
+	const uint32_t *pool;
+	uint32_t range, level;
+	svo_camera cam;
+	uint32_t width, height;
+	uint32_t bounce;     // uBounce: path vertices per sample
+	uint32_t light_type; // uLightType: 0 constant colour, 1 environment map
+	float const_color[3];
+	float env_rotation, env_multiplier;
+	EnvMapView env;
+	const uint32_t *sobol; // Sobol state: 2 * (bounce + 1) dimensions, then the sample index
+	const uint8_t *noise;  // 256 x 256 RG8 noise texture
+	float4 *color;         // accumulated radiance (rgba32f)
+	uint32_t *albedo;      // accumulated first-hit albedo (rgba8 unorm)
+	uint32_t *normal;      // accumulated first-hit normal (rgba8 snorm)
+	unsigned long long *ticket;
+	uint32_t *status;
+};
+cudaError_t pt_render_launch(const PtArgs &a, cudaStream_t stream);
+// Sobol::CmdNext (sobol.comp): advances the first `dim` dimensions by the Gray-code step.
+cudaError_t sobol_next_launch(uint32_t *sobol, const uint32_t *matrices, uint32_t dim, cudaStream_t stream);
+
 // One request's share of a shared march launch: its octree, its rays (a ray buffer, or camera rays for
 // the first n pixels, row-major, of a width x height image) and its hit buffer.  Work slots of the
 // launch are numbered job after job; slot_begin is the job's first.

@@ -18,7 +18,12 @@ the reference checkout.
   golden_beam.npz    two cameras and the beam image of the reference's beam pre-pass (Octree_RayMarchCoarse
                      from the shader source, texel arithmetic of shader/octree_tracer_beam.frag) on the
                      golden_build pool;
-  golden_occlude.npz Octree_RayMarchOcclude of the golden_march rays on that pool.
+  golden_occlude.npz Octree_RayMarchOcclude of the golden_march rays on that pool;
+  golden_pathtrace.npz the reference's path tracer (shader/path_tracer.comp + shader/sobol.comp, built with
+                     GLSL's sin / cos / atan / acos evaluated by the engine's restatements) on the
+                     golden_build pool: constant-colour and environment-map light, 4 path vertices,
+                     3 samples of a 40x30 image, with the engine's default Sobol numbers, a seeded noise
+                     texture and a small environment map.
 """
 from __future__ import annotations
 
@@ -48,6 +53,38 @@ def small_scene(level: int = 6):
     tris["v"] = verts.astype(np.float32).reshape(-1, 9)
     tris["rgb"] = scenes.random_colors(g, len(verts))
     return tris, level
+
+
+def pathtrace_inputs():
+    """Seeded inputs of golden_pathtrace (rebuilt the same way by the tests): camera, noise, env image."""
+    g = scenes.rng(SEED, 5)
+    noise = g.integers(0, 256, size=256 * 256 * 2, dtype=np.uint8)
+    env = np.zeros((16, 32, 4), np.float32)
+    env[..., :3] = g.random((16, 32, 3), dtype=np.float32)
+    env[3, 7, :3] = 40.0
+    cam = scenes.camera_from_angles((1.5, 1.45, 1.05), 0.35, -0.2, np.pi / 3, 40 / 30)
+    return cam, noise, env
+
+
+def pathtrace_golden(pool, level):
+    import ctypes
+
+    from sparsevoxeloctree_gb300 import _lib
+    matrices = np.zeros(64 * 32, np.uint32)
+    _lib.check(_lib.load().svo_sobol_default_matrices(matrices.ctypes.data_as(ctypes.c_void_p)))
+    cam, noise, env = pathtrace_inputs()
+    out = {"matrices": matrices, "env": env, "cam": np.frombuffer(cam.tobytes(), np.float32)}
+    env_r = ref.envmap_build(env)
+    for lt in (0, 1):
+        sob = np.zeros(65, np.uint32)
+        col = np.zeros((30, 40, 4), np.float32)
+        alb = np.zeros((30, 40), np.uint32)
+        nrm = np.zeros((30, 40), np.uint32)
+        # the engine's default direction numbers replace the reference's kMatrices for this fixture
+        ref.path_trace(pool, cam, 40, 30, 4, sob, noise, col, alb, nrm, light_type=lt, env=env_r if lt else None,
+                       rotation=0.7, multiplier=1.3, samples=3, engine_trig=True, matrices=matrices)
+        out[f"color{lt}"], out[f"albedo{lt}"], out[f"normal{lt}"], out[f"sobol{lt}"] = col, alb, nrm, sob
+    np.savez_compressed(os.path.join(OUT, "golden_pathtrace.npz"), **out)
 
 
 def main() -> int:
@@ -108,6 +145,8 @@ def main() -> int:
         beams[f"beam{k}"] = ref.beam(pool, camk, w, h, level)
     np.savez_compressed(os.path.join(OUT, "golden_beam.npz"), **beams)
     np.savez_compressed(os.path.join(OUT, "golden_occlude.npz"), occluded=ref.occlude(pool, o, d).astype(np.uint32))
+
+    pathtrace_golden(pool, level)
 
     g = scenes.rng(SEED, 4)
     normals = np.zeros((60, 3), np.float32)
