@@ -312,6 +312,7 @@ def engine_arm(args, rank: int, world: int, device) -> dict:
             "texels": int(beam_img.numel())}
     beam["grays_per_s"] = n_rays / ((beam["prepass_ms"] + beam["march_ms"]) * 1e-3) / 1e9
     stages["beam"] = beam
+    stages["path_trace"] = path_trace_stats(api, octree, scene, stream)
 
     e2e = None if args.no_e2e else e2e_arm(args, scene, tris_host, device, world)
     cpu = None
@@ -381,6 +382,41 @@ def e2e_arm(args, scene, tris_host, device, world) -> dict:
 
 
 # ------------------------------------------------------------------------------------------ batched build
+def path_trace_stats(api, octree, scene, stream, samples: int = 8) -> dict:
+    """PathTracer::CmdRender on the step's octree and camera at the step's image size: device ms per sample
+    (one sample per pixel, kDefaultBounce = 4 path vertices: the primary march, up to 3 diffuse bounces
+    and, with the environment map, a shadow march per bounce), for the constant light and a seeded
+    512x256 environment map with a sun."""
+    import torch
+    g = np.random.default_rng(11)
+    env = np.zeros((256, 512, 4), np.float32)
+    env[..., :3] = g.random((256, 512, 3), dtype=np.float32)
+    env[60:64, 100:104, :3] = 200.0
+    out = {"width": scene.width, "height": scene.height, "bounce": api.PathTracer.kDefaultBounce,
+           "samples_timed": samples}
+    for name, light_type in (("constant", 0), ("envmap", 1)):
+        em = api.EnvironmentMap.Create()
+        if light_type:
+            em.Reset(env)
+        light = api.Lighting.Create(em)
+        light.m_light_type = light_type
+        pt = api.PathTracer.Create(octree, scene.camera, light)
+        pt.m_width, pt.m_height = scene.width, scene.height
+        pt.Reset()
+        pt.CmdRender(stream, samples=2)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        pt.CmdRender(stream, samples=samples)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / samples
+        col = pt.ExtractColorImage()
+        out[name] = {"ms_per_sample": ms, "msamples_per_s": scene.width * scene.height / (ms * 1e-3) / 1e6,
+                     "mean_radiance": float(col.mean()), "status": pt.GetStatus()}
+    return out
+
+
 def batch_leg(args, device) -> dict:
     """The batched-build workload: 64 clutter meshes (triangles log-uniform in [1e3, 5e5], levels 7..10)
     voxelized and built (a) in one svo_batcher batch (one count pass, one readback of the counts, one

@@ -444,6 +444,37 @@ int svo_octree_load(const char *path, svo_octree *out, void *stream);
  * aspect ratio (radians; the reference's default fov is pi/3, src/Camera.hpp:17). */
 void svo_camera_from_angles(const float pos[3], float yaw, float pitch, float fov, float aspect, svo_camera *cam);
 
+/* ------------------------------------------------------------------ textured voxelization
+ * shader/voxelizer.frag:27-36: a textured triangle's fragment takes its texture's colour at the pixel
+ * centre (packUnorm4x8 of the sRGB-decoded, trilinearly filtered sample) and is discarded where the
+ * sampled alpha is below 0.5.  Textures are RGBA8 with sRGB colour and linear alpha
+ * (VK_FORMAT_R8G8B8A8_SRGB, src/Scene.cpp:262), repeat addressing, linear filtering between and
+ * within mip levels (src/Scene.cpp:409-411); the mip chain is built on the host.  The level of detail
+ * comes from the exact screen-space derivatives of the triangle's affine texture mapping. */
+typedef struct svo_texture_set svo_texture_set;
+
+/* Texture coordinates of one triangle's vertices and its texture (an index into the set; 0xffffffff or
+ * an index beyond the set: the triangle's own colour, as for a draw without a texture). */
+typedef struct svo_triangle_uv {
+	float uv[6];
+	uint32_t texture;
+	uint32_t reserved;
+} svo_triangle_uv;
+
+/* Scene::load_textures minus the file decoding: `count` RGBA8 images (host, row-major, as stb_image loads
+ * them with 4 channels), each up to 32768 x 32768. */
+int svo_texture_set_create(const uint8_t *const *rgba, const uint32_t *width, const uint32_t *height, uint32_t count,
+                           svo_texture_set **out);
+/* One mip level's RGBA8 bytes (host copy; rgba may be null to query the size). */
+int svo_texture_set_level(const svo_texture_set *s, uint32_t texture, uint32_t level, uint8_t *rgba, uint32_t *width,
+                          uint32_t *height);
+void svo_texture_set_destroy(svo_texture_set *s);
+/* svo_voxelize with texture-sampled colour and the alpha discard: uvs[i] belongs to tris[i] (device,
+ * 8-byte aligned).  The list's capacity is the untextured fragment count; count = the survivors, in the
+ * order svo_voxelize emits them. */
+int svo_voxelize_textured(const svo_triangle *tris, const svo_triangle_uv *uvs, uint32_t n_tris, uint32_t level,
+                          const svo_texture_set *textures, svo_fraglist *out, void *stream);
+
 /* ------------------------------------------------------------------ path tracer
  * PathTracer (src/PathTracer.hpp:15-75; shader/path_tracer.comp): per pixel and sample, the camera ray
  * with a Sobol sub-pixel offset, up to `bounce` path vertices of leaf marches with cosine-weighted

@@ -16,6 +16,11 @@
 //   Scene::load_meshes(filename)   src/Scene.cpp:36-147  svo::LoadObj(path)
 //   (one mesh per loader run)  src/LoaderThread.cpp:43  svo::BatchBuilder (many meshes per launch)
 //   (one octree per frame)  src/Application.cpp:130-159 svo::Server (resident octrees, batched requests)
+//   EnvironmentMap::Reset(pool, filename) src/EnvironmentMap.cpp:44-52
+//                                                        svo::EnvironmentMap::Reset(rgba, width, height)
+//   Lighting (src/Lighting.hpp)                          svo::Lighting
+//   PathTracer::Create / Reset / CmdRender / Extract*Image src/PathTracer.cpp:168-298
+//                                                        svo::PathTracer (same names, stream-ordered)
 //
 // Header-only; needs no CUDA headers.  Link against libsvo.so.  Errors throw svo::Error (the reference
 // logs and continues, e.g. src/Octree.cpp:30-33).  A `stream` is a cudaStream_t passed as void*.
@@ -275,6 +280,108 @@ private:
 	std::shared_ptr<Octree> octree_;
 	svo_camera camera_{};
 	uint32_t width_ = 0, height_ = 0;
+};
+
+// EnvironmentMap (src/EnvironmentMap.hpp): decoded float rgba image -> device texels + alias table.
+class EnvironmentMap {
+public:
+	float m_rotation = 0.0f, m_multiplier = 1.0f;
+	static std::shared_ptr<EnvironmentMap> Create() { return std::make_shared<EnvironmentMap>(); }
+	~EnvironmentMap() { Reset(); }
+	void Reset() {
+		if (map_) svo_envmap_destroy(map_);
+		map_ = nullptr;
+	}
+	void Reset(const float *rgba_host, uint32_t width, uint32_t height) {
+		Reset();
+		Check(svo_envmap_create(rgba_host, width, height, &map_));
+	}
+	bool Empty() const { return map_ == nullptr; }
+	const svo_envmap *Get() const { return map_; }
+
+private:
+	svo_envmap *map_ = nullptr;
+};
+
+// Lighting (src/Lighting.hpp:7-20).
+class Lighting {
+public:
+	enum class LightTypes : uint32_t { kConstantColor = 0, kEnvironmentMap = 1 };
+	LightTypes m_light_type = LightTypes::kConstantColor;
+	float m_sun_radiance[3] = {5.0f, 5.0f, 5.0f}; // kDefaultConstantColor
+	static std::shared_ptr<Lighting> Create(const std::shared_ptr<EnvironmentMap> &environment_map) {
+		auto l = std::make_shared<Lighting>();
+		l->env_ = environment_map;
+		return l;
+	}
+	const std::shared_ptr<EnvironmentMap> &GetEnvironmentMapPtr() const { return env_; }
+	LightTypes GetFinalLightType() const {
+		return (m_light_type == LightTypes::kEnvironmentMap && (!env_ || env_->Empty())) ? LightTypes::kConstantColor
+		                                                                               : m_light_type;
+	}
+	svo_lighting Get() const {
+		svo_lighting l{};
+		l.type = (uint32_t)GetFinalLightType();
+		for (int k = 0; k < 3; ++k) l.sun_radiance[k] = m_sun_radiance[k];
+		l.envmap_rotation = env_ ? env_->m_rotation : 0.0f;
+		l.envmap_multiplier = env_ ? env_->m_multiplier : 1.0f;
+		l.envmap = env_ ? env_->Get() : nullptr;
+		return l;
+	}
+
+private:
+	std::shared_ptr<EnvironmentMap> env_;
+};
+
+// PathTracer (src/PathTracer.hpp:15-75): progressive path tracing, one fused kernel per sample.
+class PathTracer {
+public:
+	uint32_t m_width = 1280, m_height = 720; // kDefaultWidth, kDefaultHeight
+	uint32_t m_bounce = 4;                   // kDefaultBounce
+	static std::shared_ptr<PathTracer> Create(const std::shared_ptr<Octree> &octree, const svo_camera &camera,
+	                                          const std::shared_ptr<Lighting> &lighting) {
+		auto p = std::make_shared<PathTracer>();
+		p->octree_ = octree;
+		p->camera_ = camera;
+		p->lighting_ = lighting;
+		return p;
+	}
+	~PathTracer() {
+		if (pt_) svo_path_tracer_destroy(pt_);
+	}
+	void SetCamera(const svo_camera &camera) { camera_ = camera; }
+	// PathTracer::Reset: targets of m_width x m_height cleared, Sobol state cleared.
+	void Reset(void *stream = nullptr) {
+		if (!pt_)
+			Check(svo_path_tracer_create(m_width, m_height, m_bounce, &pt_));
+		else
+			Check(svo_path_tracer_reset(pt_, m_width, m_height, m_bounce, stream));
+	}
+	void CmdRender(void *stream = nullptr, uint32_t samples = 1) {
+		if (!pt_) Reset(stream);
+		const svo_lighting l = lighting_->Get();
+		Check(svo_path_tracer_render(pt_, &octree_->Get(), &camera_, &l, samples, stream));
+	}
+	uint32_t GetSPP() const {
+		uint32_t spp = 0;
+		if (pt_) Check(svo_path_tracer_info(pt_, &spp, nullptr));
+		return spp;
+	}
+	std::vector<float> ExtractColorImage() const { return extract(0); }
+	std::vector<float> ExtractAlbedoImage() const { return extract(1); }
+	std::vector<float> ExtractNormalImage() const { return extract(2); }
+	svo_path_tracer *Get() const { return pt_; }
+
+private:
+	std::vector<float> extract(uint32_t image) const {
+		std::vector<float> out((size_t)m_width * m_height * 3);
+		if (pt_) Check(svo_path_tracer_extract(pt_, image, out.data(), nullptr));
+		return out;
+	}
+	std::shared_ptr<Octree> octree_;
+	std::shared_ptr<Lighting> lighting_;
+	svo_camera camera_{};
+	svo_path_tracer *pt_ = nullptr;
 };
 
 // Scene::load_meshes for the engine's triangle format (svo_load_obj).

@@ -72,6 +72,10 @@ def lib():
         L.oracle_envmap_build.argtypes = [P, u32, u32, P]
         L.oracle_envmap_build.restype = i32
         L.oracle_trig.argtypes = [f32, f32, P]
+        L.oracle_texture_mips.argtypes = [P, u32, u32, P]
+        L.oracle_texture_mips.restype = u32
+        L.oracle_voxelize_textured.argtypes = [P, P, u32, u32, P, P, P, u32, P]
+        L.oracle_voxelize_textured.restype = u64
         _lib = L
     return _lib
 
@@ -262,3 +266,35 @@ def trig(x: float, y: float) -> np.ndarray:
     out = np.zeros(4, np.float32)
     lib().oracle_trig(x, y, _ptr(out))
     return out
+
+
+UV_DTYPE = np.dtype([("uv", "<f4", (6,)), ("texture", "<u4"), ("reserved", "<u4")])
+
+
+def texture_mips(rgba: np.ndarray) -> list:
+    """Mip chain of an (h, w, 4) uint8 texture: a list of (h_l, w_l, 4) uint8 levels."""
+    img = np.ascontiguousarray(rgba, np.uint8)
+    h, w = img.shape[:2]
+    out = np.zeros(w * h * 4 * 2 + 256, np.uint8)
+    levels = lib().oracle_texture_mips(_ptr(img), w, h, _ptr(out))
+    res, off = [], 0
+    for lv in range(levels):
+        wl, hl = max(1, w >> lv), max(1, h >> lv)
+        res.append(out[off: off + wl * hl * 4].reshape(hl, wl, 4).copy())
+        off += wl * hl * 4
+    return res
+
+
+def voxelize_textured(tris: np.ndarray, uvs: np.ndarray, level: int, textures: list) -> np.ndarray:
+    """Fragments with texture-sampled colour (textures: (h, w, 4) uint8 images)."""
+    tris = np.ascontiguousarray(tris, TRIANGLE_DTYPE)
+    uvs = np.ascontiguousarray(uvs, UV_DTYPE)
+    imgs = [np.ascontiguousarray(t, np.uint8) for t in textures]
+    ptrs = (ctypes.c_void_p * max(1, len(imgs)))(*[i.ctypes.data for i in imgs])
+    ws = np.array([i.shape[1] for i in imgs] + [0], np.uint32)
+    hs = np.array([i.shape[0] for i in imgs] + [0], np.uint32)
+    total = lib().oracle_voxelize_count(_ptr(tris), len(tris), level, None)
+    out = np.zeros(max(int(total), 1), np.uint64)
+    n = lib().oracle_voxelize_textured(_ptr(tris), _ptr(uvs), len(tris), level, ptrs, _ptr(ws), _ptr(hs), len(imgs),
+                                       _ptr(out))
+    return out[: int(n)]

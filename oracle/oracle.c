@@ -1317,3 +1317,227 @@ void oracle_trig(float x, float y, float *out) {
 	out[2] = svo_atan2(y, x);
 	out[3] = svo_acos(x);
 }
+
+/* ====================================================================== textured voxelization */
+
+static double srgb_decode_d(double c) { return c <= 0.04045 ? c / 12.92 : pow((c + 0.055) / 1.055, 2.4); }
+static double srgb_encode_d(double x) { return x <= 0.0031308 ? 12.92 * x : 1.055 * pow(x, 1.0 / 2.4) - 0.055; }
+static uint8_t to_byte_d(double x) { return (uint8_t)floor(fmin(fmax(x, 0.0), 1.0) * 255.0 + 0.5); }
+
+/* The texture's mip chain (CmdGenerateMipmap2D as the engine states it): level l+1 texel (i, j) is the
+ * bilinear, clamp-to-edge, linear-space sample of level l at ((i + 1/2) w / w' - 1/2, (j + 1/2) h / h' - 1/2),
+ * re-encoded to sRGB bytes (alpha linear), rounding to nearest.  out: every level's RGBA8 bytes, level
+ * 0 first; returns the number of levels.  out must hold the chain (< 4/3 w h 4 + 4 * levels bytes). */
+uint32_t oracle_texture_mips(const uint8_t *rgba, uint32_t w, uint32_t h, uint8_t *out) {
+	double lin[256];
+	for (int c = 0; c < 256; ++c)
+		lin[c] = srgb_decode_d(c / 255.0);
+	memcpy(out, rgba, (size_t)w * h * 4);
+	uint8_t *src = out;
+	uint32_t levels = 1;
+	while (w > 1 || h > 1) {
+		uint32_t w2 = w > 1 ? w / 2 : 1, h2 = h > 1 ? h / 2 : 1;
+		uint8_t *dst = src + (size_t)w * h * 4;
+		for (uint32_t j = 0; j < h2; ++j)
+			for (uint32_t i = 0; i < w2; ++i) {
+				double x = ((double)i + 0.5) * (double)w / (double)w2 - 0.5;
+				double y = ((double)j + 0.5) * (double)h / (double)h2 - 0.5;
+				double fx = floor(x), fy = floor(y), a = x - fx, b = y - fy;
+				int64_t i0 = (int64_t)fx, j0 = (int64_t)fy;
+				size_t xs[2], ys[2];
+				for (int q = 0; q < 2; ++q) {
+					int64_t xi = i0 + q, yj = j0 + q;
+					xs[q] = (size_t)(xi < 0 ? 0 : (xi >= (int64_t)w ? w - 1 : xi));
+					ys[q] = (size_t)(yj < 0 ? 0 : (yj >= (int64_t)h ? h - 1 : yj));
+				}
+				double wt[4] = {(1 - a) * (1 - b), a * (1 - b), (1 - a) * b, a * b};
+				for (int ch = 0; ch < 4; ++ch) {
+					double acc = 0.0;
+					for (int q = 0; q < 4; ++q) {
+						uint8_t v = src[(ys[q >> 1] * w + xs[q & 1]) * 4 + ch];
+						acc += wt[q] * (ch < 3 ? lin[v] : v / 255.0);
+					}
+					dst[((size_t)j * w2 + i) * 4 + ch] = to_byte_d(ch < 3 ? srgb_encode_d(acc) : acc);
+				}
+			}
+		src = dst;
+		w = w2;
+		h = h2;
+		++levels;
+	}
+	return levels;
+}
+
+typedef struct tex_view {
+	const float *texels; /* linear rgba floats of every level of every texture */
+	const uint64_t *level_off; /* [texture * 16 + level]: first texel of the level */
+	const uint32_t *dims;      /* [texture * 3]: width, height, levels */
+	uint32_t count;
+} tex_view;
+
+static float log2_svo(float x) {
+	if (!(x > 0.0f))
+		return -1e30f;
+	uint32_t bits = f2u(x);
+	int e = (int)((bits >> 23) & 255u) - 127;
+	float m = u2f((bits & 0x7fffffu) | 0x3f800000u);
+	if (m > 1.41421356237309505f) {
+		m = m * 0.5f;
+		e += 1;
+	}
+	float s = (m - 1.0f) / (m + 1.0f), s2 = s * s;
+	float p = 1.0f / 11.0f;
+	p = p * s2 + 1.0f / 9.0f;
+	p = p * s2 + 1.0f / 7.0f;
+	p = p * s2 + 1.0f / 5.0f;
+	p = p * s2 + 1.0f / 3.0f;
+	p = p * s2 + 1.0f;
+	return (float)e + (2.0f * (s * p)) * 1.44269504088896341f;
+}
+
+static void tex_bilinear(const tex_view *tv, uint32_t t, uint32_t l, float u, float v, float out[4]) {
+	int64_t W = tv->dims[3 * t] >> l, H = tv->dims[3 * t + 1] >> l;
+	if (W < 1) W = 1;
+	if (H < 1) H = 1;
+	float x = u * (float)W - 0.5f, y = v * (float)H - 0.5f;
+	float fx = floorf(x), fy = floorf(y);
+	float a = x - fx, b = y - fy;
+	int64_t ix = (int64_t)fminf(fmaxf(fx, -4e18f), 4e18f), jy = (int64_t)fminf(fmaxf(fy, -4e18f), 4e18f);
+	int64_t i0 = ((ix % W) + W) % W, j0 = ((jy % H) + H) % H;
+	int64_t i1 = i0 + 1 == W ? 0 : i0 + 1, j1 = j0 + 1 == H ? 0 : j0 + 1;
+	const float *L = tv->texels + 4 * tv->level_off[16 * t + l];
+	const float *t00 = L + 4 * (j0 * W + i0), *t10 = L + 4 * (j0 * W + i1);
+	const float *t01 = L + 4 * (j1 * W + i0), *t11 = L + 4 * (j1 * W + i1);
+	float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b), w01 = (1.0f - a) * b, w11 = a * b;
+	for (int k = 0; k < 4; ++k)
+		out[k] = ((w00 * t00[k] + w10 * t10[k]) + w01 * t01[k]) + w11 * t11[k];
+}
+
+static uint32_t unorm8_tex(float v) { return (uint32_t)floorf(fminf(fmaxf(v, 0.0f), 1.0f) * 255.0f + 0.5f); }
+
+/* shader/voxelizer.frag:27-36 for one candidate fragment of triangle tri: returns 0 when discarded. */
+static int tex_fragment(uint64_t *frag, const svo_triangle *tri, const svo_triangle_uv *uv, uint32_t level,
+                        const tex_view *tv) {
+	if (uv->texture == 0xffffffffu || uv->texture >= tv->count)
+		return 1;
+	float scale = (float)(256 << level);
+	int64_t X[3], Y[3], Z[3];
+	for (int k = 0; k < 3; ++k) {
+		X[k] = snap(tri->v[3 * k], scale);
+		Y[k] = snap(tri->v[3 * k + 1], scale);
+		Z[k] = snap(tri->v[3 * k + 2], scale);
+	}
+	int64_t e1x = X[1] - X[0], e1y = Y[1] - Y[0], e1z = Z[1] - Z[0];
+	int64_t e2x = X[2] - X[0], e2y = Y[2] - Y[0], e2z = Z[2] - Z[0];
+	int64_t nx = e1y * e2z - e1z * e2y, ny = e1z * e2x - e1x * e2z, nz = e1x * e2y - e1y * e2x;
+	int64_t ax = nx < 0 ? -nx : nx, ay = ny < 0 ? -ny : ny, az = nz < 0 ? -nz : nz;
+	int axis = (ax > ay && ax > az) ? 0 : (ay > az ? 1 : 2);
+	int64_t A[3], B[3];
+	for (int k = 0; k < 3; ++k) {
+		A[k] = axis == 0 ? Y[k] : (axis == 1 ? Z[k] : X[k]);
+		B[k] = axis == 0 ? Z[k] : (axis == 1 ? X[k] : Y[k]);
+	}
+	uint32_t fx = (uint32_t)*frag, fy = (uint32_t)(*frag >> 32);
+	int64_t vx = fx & 0xfffu, vy = (fx >> 12) & 0xfffu, vz = (fx >> 24) | ((fy >> 28) << 8);
+	int64_t pi = axis == 0 ? vy : (axis == 1 ? vz : vx), pj = axis == 0 ? vz : (axis == 1 ? vx : vy);
+	int64_t px = 256 * pi + 128, py = 256 * pj + 128;
+	int64_t a0 = A[1] - A[0], a1 = B[1] - B[0], b0 = A[2] - A[0], b1 = B[2] - B[0];
+	int64_t area = a0 * b1 - a1 * b0;
+	if (area == 0)
+		return 1;
+	int64_t q0 = px - A[0], q1 = py - B[0];
+	float fa = (float)area;
+	float l1 = (float)(q0 * b1 - q1 * b0) / fa, l2 = (float)(a0 * q1 - a1 * q0) / fa;
+	float du1 = uv->uv[2] - uv->uv[0], dv1 = uv->uv[3] - uv->uv[1];
+	float du2 = uv->uv[4] - uv->uv[0], dv2 = uv->uv[5] - uv->uv[1];
+	float u = (uv->uv[0] + l1 * du1) + l2 * du2, v = (uv->uv[1] + l1 * dv1) + l2 * dv2;
+	float g1i = (float)(256 * b1) / fa, g1j = (float)(-256 * b0) / fa;
+	float g2i = (float)(-256 * a1) / fa, g2j = (float)(256 * a0) / fa;
+	uint32_t t = uv->texture, levels = tv->dims[3 * t + 2];
+	float W = (float)tv->dims[3 * t], H = (float)tv->dims[3 * t + 1];
+	float dux = (g1i * du1 + g2i * du2) * W, dvx = (g1i * dv1 + g2i * dv2) * H;
+	float duy = (g1j * du1 + g2j * du2) * W, dvy = (g1j * dv1 + g2j * dv2) * H;
+	float rho = fmaxf(sqrtf(dux * dux + dvx * dvx), sqrtf(duy * duy + dvy * dvy));
+	float lod = log2_svo(rho), c[4];
+	if (!(lod > 0.0f)) {
+		tex_bilinear(tv, t, 0, u, v, c);
+	} else {
+		float d = fminf(lod, (float)(levels - 1));
+		uint32_t lo = (uint32_t)floorf(d), hi = lo + 1 < levels ? lo + 1 : levels - 1;
+		float f = d - (float)lo, c0[4], c1[4];
+		tex_bilinear(tv, t, lo, u, v, c0);
+		tex_bilinear(tv, t, hi, u, v, c1);
+		for (int k = 0; k < 4; ++k)
+			c[k] = (1.0f - f) * c0[k] + f * c1[k];
+	}
+	if (c[3] < 0.5f)
+		return 0;
+	uint32_t rgb = unorm8_tex(c[0]) | (unorm8_tex(c[1]) << 8) | (unorm8_tex(c[2]) << 16);
+	*frag = (*frag & 0xF0000000FFFFFFFFull) | ((uint64_t)rgb << 32);
+	return 1;
+}
+
+/* Voxelization with texture-sampled colour: the canonical fragments of every triangle, each textured
+ * one's coloured or dropped.  textures: `count` RGBA8 images (sizes in widths / heights).  Returns the
+ * fragment count written to out (out holds at least oracle_voxelize_count's total). */
+uint64_t oracle_voxelize_textured(const svo_triangle *tris, const svo_triangle_uv *uvs, uint32_t n, uint32_t level,
+                                  const uint8_t *const *textures, const uint32_t *widths, const uint32_t *heights,
+                                  uint32_t count, uint64_t *out) {
+	/* linear texels of every level */
+	uint64_t total_texels = 0;
+	uint64_t *level_off = (uint64_t *)calloc((size_t)count * 16 + 1, sizeof(uint64_t));
+	uint32_t *dims = (uint32_t *)calloc((size_t)count * 3 + 1, sizeof(uint32_t));
+	uint8_t **chains = (uint8_t **)calloc((size_t)count + 1, sizeof(uint8_t *));
+	for (uint32_t t = 0; t < count; ++t) {
+		size_t bytes = (size_t)widths[t] * heights[t] * 4 * 2 + 64 * 4;
+		chains[t] = (uint8_t *)malloc(bytes);
+		uint32_t levels = oracle_texture_mips(textures[t], widths[t], heights[t], chains[t]);
+		dims[3 * t] = widths[t], dims[3 * t + 1] = heights[t], dims[3 * t + 2] = levels;
+		for (uint32_t l = 0; l < levels; ++l) {
+			uint64_t w = widths[t] >> l, h = heights[t] >> l;
+			level_off[16 * t + l] = total_texels;
+			total_texels += (w ? w : 1) * (h ? h : 1);
+		}
+	}
+	float lin[256];
+	for (int c = 0; c < 256; ++c)
+		lin[c] = (float)srgb_decode_d(c / 255.0);
+	float *texels = (float *)malloc((size_t)(total_texels + 1) * 16);
+	for (uint32_t t = 0; t < count; ++t) {
+		const uint8_t *p = chains[t];
+		for (uint32_t l = 0; l < dims[3 * t + 2]; ++l) {
+			uint64_t w = widths[t] >> l, h = heights[t] >> l, m = (w ? w : 1) * (h ? h : 1);
+			float *dst = texels + 4 * level_off[16 * t + l];
+			for (uint64_t i = 0; i < m; ++i, p += 4) {
+				dst[4 * i] = lin[p[0]], dst[4 * i + 1] = lin[p[1]], dst[4 * i + 2] = lin[p[2]];
+				dst[4 * i + 3] = (float)(p[3] / 255.0);
+			}
+		}
+	}
+	tex_view tv = {texels, level_off, dims, count};
+	uint32_t *counts = (uint32_t *)malloc(((size_t)n + 1) * sizeof(uint32_t));
+	uint64_t total = oracle_voxelize_count(tris, n, level, counts);
+	uint64_t *offsets = (uint64_t *)malloc(((size_t)n + 1) * sizeof(uint64_t));
+	offsets[0] = 0;
+	for (uint32_t t = 0; t < n; ++t)
+		offsets[t + 1] = offsets[t] + counts[t];
+	uint64_t *cand = (uint64_t *)malloc((size_t)(total + 1) * sizeof(uint64_t));
+	oracle_voxelize_emit(tris, n, level, offsets, cand);
+	uint64_t kept = 0;
+	for (uint32_t t = 0; t < n; ++t)
+		for (uint64_t f = offsets[t]; f < offsets[t + 1]; ++f) {
+			uint64_t fr = cand[f];
+			if (tex_fragment(&fr, &tris[t], &uvs[t], level, &tv))
+				out[kept++] = fr;
+		}
+	for (uint32_t t = 0; t < count; ++t)
+		free(chains[t]);
+	free(chains);
+	free(level_off);
+	free(dims);
+	free(texels);
+	free(counts);
+	free(offsets);
+	free(cand);
+	return kept;
+}

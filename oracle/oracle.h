@@ -87,6 +87,14 @@ void oracle_pt_render(const uint32_t *pool, uint64_t range, uint32_t level, cons
 void oracle_sobol_next(uint32_t *sobol, const uint32_t *matrices, uint32_t dim);
 /* EnvironmentMap::weigh_hdr_image + generate_alias_table (src/EnvironmentMap.cpp:83-160). */
 int oracle_envmap_build(float *rgba, uint32_t w, uint32_t h, uint32_t *alias);
+/* ---- textured voxelization ---- */
+/* The mip chain of an RGBA8 texture (every level's bytes, level 0 first); returns the level count. */
+uint32_t oracle_texture_mips(const uint8_t *rgba, uint32_t w, uint32_t h, uint8_t *out);
+/* shader/voxelizer.frag:27-36 over the canonical fragments: textured triangles' fragments coloured by
+ * their texture or dropped (alpha < 0.5).  Returns the count written to out. */
+uint64_t oracle_voxelize_textured(const svo_triangle *tris, const svo_triangle_uv *uvs, uint32_t n, uint32_t level,
+                                  const uint8_t *const *textures, const uint32_t *widths, const uint32_t *heights,
+                                  uint32_t count, uint64_t *out);
 /* sin x, cos x, atan2(y, x), acos x by the engine's restatements (oracle/svo_trig.h). */
 void oracle_trig(float x, float y, float *out);
 

@@ -210,6 +210,8 @@ void ref_diffuse_sample(const float *normal, float u1, float u2, float *dir) {
 //                        centre lies in the emitted triangle (closed test, double).
 // Depth at the pixel centre is interpolated from the emitted vertices in double and rounded to float.
 // Fragments are appended to out (uint64: x | y << 32).  Returns the number written.
+static const float *g_texel = nullptr; // a 1x1 texture for the textured form (null: untextured)
+
 uint64_t ref_voxelize_triangle(const float *v9, uint32_t albedo, uint32_t level, int conservative_sw, uint64_t *out,
                                uint64_t cap) {
 	const uint32_t R = 1u << level;
@@ -235,7 +237,8 @@ uint64_t ref_voxelize_triangle(const float *v9, uint32_t albedo, uint32_t level,
 	x0 = std::max(x0, 0), y0 = std::max(y0, 0), x1 = std::min(x1, (int)R - 1), y1 = std::min(y1, (int)R - 1);
 	uFragmentList = nullptr;
 	uCountOnly = 1;
-	uTextureId = 0xffffffffu;
+	uTextureId = g_texel ? 0u : 0xffffffffu;
+	uTextures[0] = sampler2D{g_texel, 1, 1};
 	uAlbedo = albedo;
 	uint64_t n = 0;
 	for (int py = y0; py <= y1; ++py)
@@ -276,6 +279,23 @@ uint64_t ref_voxelize_triangle(const float *v9, uint32_t albedo, uint32_t level,
 			if (n < cap) out[n] = (uint64_t)frag.x | ((uint64_t)frag.y << 32);
 			++n;
 		}
+	return n;
+}
+
+// voxelizer.frag with uTextureId = 0 bound to a 1x1 texture of linear rgba `texel` (the value every
+// filtered sample of it has, whatever the coordinate and level of detail): Sample()'s alpha discard and
+// packUnorm4x8 colour, on the same raster as ref_voxelize_triangle.
+uint64_t ref_voxelize_triangle_texel(const float *v9, const float *texel, uint32_t level, int conservative_sw,
+                                     uint64_t *out, uint64_t cap) {
+	g_texel = texel;
+	uint64_t n = 0;
+	try {
+		n = ref_voxelize_triangle(v9, 0u, level, conservative_sw, out, cap);
+	} catch (...) {
+		g_texel = nullptr;
+		throw;
+	}
+	g_texel = nullptr;
 	return n;
 }
 

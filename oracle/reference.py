@@ -58,6 +58,8 @@ def lib(engine_trig: bool = False):
         L.ref_diffuse_sample.argtypes = [P, f32, f32, P]
         L.ref_voxelize_triangle.argtypes = [P, u32, u32, i32, P, u64]
         L.ref_voxelize_triangle.restype = u64
+        L.ref_voxelize_triangle_texel.argtypes = [P, P, u32, i32, P, u64]
+        L.ref_voxelize_triangle_texel.restype = u64
         L.ref_sobol_matrices.argtypes = [P]
         L.ref_sobol_next.argtypes = [P, u32]
         L.ref_envmap_build.argtypes = [P, u32, u32, P]
@@ -186,3 +188,13 @@ def path_trace(pool: np.ndarray, cam, width: int, height: int, bounce: int, sobo
                          _p(cc), rotation, multiplier, _p(tex), _p(alias), ew, eh, _p(sobol),
                          _p(np.ascontiguousarray(noise, np.uint8)), _p(color), _p(albedo), _p(normal), samples,
                          None if matrices is None else _p(np.ascontiguousarray(matrices, np.uint32)))
+
+
+def voxelize_triangle_texel(v9_ref: np.ndarray, texel_linear, level: int, conservative_sw: bool) -> np.ndarray:
+    """voxelizer.frag with a 1x1 texture of linear rgba `texel_linear` bound (alpha discard, packUnorm4x8)."""
+    v = np.ascontiguousarray(v9_ref, np.float32)
+    t = np.ascontiguousarray(texel_linear, np.float32)
+    cap = 1 << 16
+    out = np.zeros(cap, np.uint64)
+    n = lib().ref_voxelize_triangle_texel(_p(v), _p(t), level, int(conservative_sw), _p(out), cap)
+    return out[: min(int(n), cap)]

@@ -146,6 +146,10 @@ _SIGNATURES = {
     "svo_tune_size_class": ([u64], u32),
     "svo_tune_reset": ([], None),
     "svo_camera_from_angles": ([ctypes.POINTER(f32), f32, f32, f32, f32, ctypes.POINTER(CameraC)], None),
+    "svo_texture_set_create": ([P, P, P, u32, ctypes.POINTER(P)], i32),
+    "svo_texture_set_level": ([P, u32, u32, P, ctypes.POINTER(u32), ctypes.POINTER(u32)], i32),
+    "svo_texture_set_destroy": ([P], None),
+    "svo_voxelize_textured": ([P, P, u32, u32, P, ctypes.POINTER(Fraglist), P], i32),
     "svo_sobol_default_matrices": ([P], i32),
     "svo_envmap_create": ([P, u32, u32, ctypes.POINTER(P)], i32),
     "svo_envmap_tables": ([P, P, P], i32),

@@ -802,6 +802,58 @@ def load_octree(path: str, stream=None) -> Octree:
     return Octree.FromView(oc, owner=_OwnedPool(oc))
 
 
+# ------------------------------------------------------------------------------------------- textures
+UV_DTYPE = np.dtype([("uv", "<f4", (6,)), ("texture", "<u4"), ("reserved", "<u4")])
+
+
+class TextureSet:
+    """The scene's textures (Scene::load_textures, src/Scene.cpp:225-309, minus the file decoding): RGBA8
+    images with sRGB colour and linear alpha; mip chains built on the host, texels on the device."""
+
+    def __init__(self, images):
+        imgs = [np.ascontiguousarray(i, np.uint8) for i in images]
+        for i in imgs:
+            if i.ndim != 3 or i.shape[2] != 4:
+                raise ValueError("textures must be (h, w, 4) uint8")
+        ptrs = (ctypes.c_void_p * max(1, len(imgs)))(*[i.ctypes.data for i in imgs])
+        ws = np.array([i.shape[1] for i in imgs] + [0], np.uint32)
+        hs = np.array([i.shape[0] for i in imgs] + [0], np.uint32)
+        h = ctypes.c_void_p(0)
+        _lib.check(_lib.load().svo_texture_set_create(ptrs, ws.ctypes.data_as(ctypes.c_void_p),
+                                                      hs.ctypes.data_as(ctypes.c_void_p), len(imgs), ctypes.byref(h)))
+        self._h, self.count = h, len(imgs)
+
+    def GetLevel(self, texture: int, level: int) -> np.ndarray:
+        w, h = ctypes.c_uint32(0), ctypes.c_uint32(0)
+        lib = _lib.load()
+        _lib.check(lib.svo_texture_set_level(self._h, texture, level, None, ctypes.byref(w), ctypes.byref(h)))
+        out = np.zeros((h.value, w.value, 4), np.uint8)
+        _lib.check(lib.svo_texture_set_level(self._h, texture, level, out.ctypes.data_as(ctypes.c_void_p), None, None))
+        return out
+
+    def __del__(self):
+        try:
+            if self._h:
+                _lib.load().svo_texture_set_destroy(self._h)
+        except Exception:
+            pass
+
+
+def voxelize_textured(triangles, uvs, level: int, textures: TextureSet | None, stream=None) -> torch.Tensor:
+    """Voxelizer with texture-sampled fragment colour and the alpha discard (shader/voxelizer.frag:27-36):
+    uvs[i] (UV_DTYPE) belongs to triangles[i]; returns the surviving fragments (int64 tensor)."""
+    tris = triangles if isinstance(triangles, torch.Tensor) else to_device(np.asarray(triangles, TRIANGLE_DTYPE))
+    uv = uvs if isinstance(uvs, torch.Tensor) else to_device(np.asarray(uvs, UV_DTYPE))
+    n = tris.numel() // TRIANGLE_DTYPE.itemsize
+    fl = _lib.Fraglist()
+    _lib.check(_lib.load().svo_voxelize_textured(_ptr(tris), _ptr(uv), n, level,
+                                                 textures._h if textures is not None else None, ctypes.byref(fl),
+                                                 _stream(stream)))
+    out = _copy_from(fl.data, fl.count, torch.int64, tris.device)
+    _lib.load().svo_fraglist_destroy(ctypes.byref(fl), _stream(stream))
+    return out
+
+
 # ------------------------------------------------------------------------------------------- functional
 def voxelize(triangles, level: int, stream=None) -> torch.Tensor:
     return Voxelizer.Create(triangles, level, stream).GetVoxelFragmentList()

@@ -31,6 +31,7 @@ UNITS = {
     "serve.cu": [],
     "io.cu": [],
     "pt.cu": ["-Xcompiler", "-ffp-contract=off"],
+    "texture.cu": ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-Xcompiler", "-ffp-contract=off"],
 }
 HEADERS = ["common.cuh", "svo_internal.h"]
 

@@ -412,6 +412,53 @@ int svo_voxelize(const svo_triangle *tris, uint32_t n_tris, uint32_t level, svo_
 	return svo_voxelize_ex(tris, n_tris, level, nullptr, out, stream);
 }
 
+int svo_voxelize_textured(const svo_triangle *tris, const svo_triangle_uv *uvs, uint32_t n_tris, uint32_t level,
+                          const svo_texture_set *textures, svo_fraglist *out, void *stream) {
+	int rc;
+	if ((rc = check_level(level)) || (rc = check_tris(tris, n_tris))) return rc;
+	if (!out || (n_tris && !uvs)) return fail(SVO_ERR_INVALID, "null argument");
+	if (!aligned(uvs, 8)) return fail(SVO_ERR_INVALID, "texture coordinates must be 8-byte aligned");
+	cudaStream_t s = (cudaStream_t)stream;
+	Mem mem{nullptr, s};
+	void *ws = nullptr;
+	VoxWorkspace w;
+	uint64_t total = 0, units = 0;
+	if ((rc = voxelize_count_pass(tris, n_tris, level, mem, &ws, w, total, units))) return rc;
+	if (total > 0xffffffffull) {
+		mem.put(ws);
+		return fail(SVO_ERR_CAPACITY, "%llu fragments exceed the 32-bit fragment count", (unsigned long long)total);
+	}
+	void *cand = nullptr, *frags = nullptr, *scratch = nullptr;
+	cudaError_t e = mem.get(&cand, total * sizeof(uint64_t));
+	if (e == cudaSuccess) e = mem.get(&frags, total * sizeof(uint64_t));
+	if (e == cudaSuccess) e = mem.get(&scratch, vox_texture_scratch_bytes(total));
+	if (e == cudaSuccess) e = vox_launch_emit(tris, n_tris, level, w, (uint64_t *)cand, total, s);
+	if (e == cudaSuccess)
+		e = vox_texture_launch((const uint64_t *)cand, total, tris, uvs, n_tris, level, w, textures, (uint64_t *)frags,
+		                       (unsigned long long *)scratch, s);
+	unsigned long long res[2] = {0, 0};
+	if (e == cudaSuccess && total) e = cudaMemcpyAsync(res, scratch, sizeof(res), cudaMemcpyDeviceToHost, s);
+	if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+	mem.put(ws);
+	mem.put(cand);
+	mem.put(scratch);
+	if (e != cudaSuccess) {
+		mem.put(frags);
+		return cuda_fail(e, "textured voxelize");
+	}
+	if ((rc = status_to_error((uint32_t)(res[1] >> 32), "textured voxelize"))) {
+		mem.put(frags);
+		return rc;
+	}
+	out->data = (uint64_t *)frags;
+	out->count = (uint32_t)res[0];
+	out->level = level;
+	out->capacity = total;
+	out->owned = mem.owned();
+	out->units = (uint32_t)units;
+	return SVO_OK;
+}
+
 int svo_voxelize_into(const svo_triangle *tris, uint32_t n_tris, uint32_t level, uint64_t *frags, uint64_t capacity,
                       uint64_t *count_dev, void *workspace, size_t workspace_bytes, void *stream) {
 	int rc;

@@ -103,6 +103,20 @@ cudaError_t vox_launch_batch_totals(const VoxBatch &vb, uint32_t n, const VoxWor
 cudaError_t vox_launch_emit_batch(const VoxBatch &vb, uint32_t n, const VoxWorkspace &w, uint64_t *frags,
                                   uint64_t capacity, cudaStream_t stream);
 
+// Texture-sampled fragment colour (texture.cu).  One texture of a set: its size, mip levels and the
+// first texel of every level in the set's linear float texel array.
+struct TexDesc {
+	uint64_t level_off[16];
+	uint32_t width, height, levels, pad;
+};
+// Samples the textured candidates (colour, alpha test) and compacts the survivors in order into `out`;
+// scratch (vox_texture_scratch_bytes, device) returns the survivor count in its first word.
+cudaError_t vox_texture_launch(const uint64_t *cand, uint64_t n_cand, const svo_triangle *tris,
+                               const svo_triangle_uv *uvs, uint32_t n_tris, uint32_t level, const VoxWorkspace &w,
+                               const svo_texture_set *set, uint64_t *out, unsigned long long *scratch,
+                               cudaStream_t stream);
+size_t vox_texture_scratch_bytes(uint64_t n_cand);
+
 // ---------------------------------------------------------------- build
 struct LevelInfo {
 	uint32_t begin;         // first word of this depth's node range

@@ -3,8 +3,9 @@
 //   Scene -> Voxelizer -> OctreeBuilder -> CmdBuild -> Octree::Update -> OctreeTracer::CmdDrawPipeline
 // Usage: wrapper_pipeline <triangles.bin> <level> <camera.bin (16 floats)> <width> <height> <out prefix>
 // Writes <out>.frags (uint64), <out>.pool (uint32, range words), <out>.hits (svo_hit) and <out>.beam
-// (float beam image), and checks in-process that a two-mesh BatchBuilder, a Server camera request and an
-// octree file round trip agree with the single-mesh classes.
+// (float beam image) and <out>.pt (2 path-traced samples, rgb floats), and checks in-process that a
+// two-mesh BatchBuilder, a Server camera request and an octree file round trip agree with the
+// single-mesh classes.
 #include <cstdio>
 #include <fstream>
 #include <iterator>
@@ -101,6 +102,25 @@ int main(int argc, char **argv) {
 				std::fprintf(stderr, "served hits differ from the tracer's\n");
 				return 4;
 			}
+		}
+
+		// path tracer (PathTracer::Reset + CmdRender x2, constant light, 3 path vertices), noise byte i = 37 i
+		{
+			auto env = svo::EnvironmentMap::Create();
+			auto lighting = svo::Lighting::Create(env);
+			lighting->m_sun_radiance[0] = 1.0f, lighting->m_sun_radiance[1] = 2.0f, lighting->m_sun_radiance[2] = 3.0f;
+			auto pt = svo::PathTracer::Create(octree, cam, lighting);
+			pt->m_width = width, pt->m_height = height, pt->m_bounce = 3;
+			pt->Reset();
+			std::vector<uint8_t> noise(256 * 256 * 2);
+			for (size_t i = 0; i < noise.size(); ++i) noise[i] = (uint8_t)(i * 37u);
+			svo::Check(svo_path_tracer_set_noise(pt->Get(), noise.data(), nullptr));
+			pt->CmdRender(nullptr, 2);
+			if (pt->GetSPP() != 2) {
+				std::fprintf(stderr, "path tracer sample count\n");
+				return 6;
+			}
+			write_file(out + ".pt", pt->ExtractColorImage());
 		}
 
 		// octree file round trip

@@ -51,3 +51,14 @@ def test_cpp_wrapper_pipeline_matches_oracle(tmp_path, cuda):
     assert np.array_equal(hits, oracle.raycast(ref_pool, s.level, oracle.camera_rays(s.camera, s.width, s.height)))
     beam = np.fromfile(out + ".beam", np.float32)
     assert np.array_equal(beam, oracle.beam(ref_pool, s.level, s.camera, s.width, s.height).reshape(-1))
+    # PathTracer: 2 samples, constant light (1, 2, 3), 3 path vertices, noise byte i = 37 i
+    import ctypes
+
+    from sparsevoxeloctree_gb300 import _lib
+    m = np.zeros(64 * 32, np.uint32)
+    _lib.check(_lib.load().svo_sobol_default_matrices(m.ctypes.data_as(ctypes.c_void_p)))
+    noise = (np.arange(256 * 256 * 2, dtype=np.uint64) * 37 % 256).astype(np.uint8)
+    st = oracle.PathTraceState(s.width, s.height, 3, m, noise)
+    st.render(ref_pool, s.level, s.camera, const_color=(1.0, 2.0, 3.0), samples=2)
+    pt = np.fromfile(out + ".pt", np.float32).reshape(s.height, s.width, 3)
+    assert np.array_equal(pt, st.color[..., :3])

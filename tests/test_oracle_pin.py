@@ -186,3 +186,38 @@ def test_path_trace_with_libm_trig_matches_in_distribution(light_type):
     assert np.array_equal(alb, st.albedo) and np.array_equal(nrm, st.normal)
     assert (col == st.color).all(axis=2).mean() >= (0.8 if light_type == 0 else 0.1)
     assert abs(col[..., :3].mean() - st.color[..., :3].mean()) <= 0.02 * col[..., :3].mean()
+
+
+# ---------------------------------------------------------------------------------------------- textures
+def test_textured_fragment_shader_logic_matches_reference():
+    """voxelizer.frag's textured branch (Sample(): alpha < 0.5 discards; packUnorm4x8 colour) with a 1x1
+    texture, whose every filtered sample is its one texel: the oracle keeps or drops each triangle's
+    fragments as the reference shader does and gives them the same colour word."""
+    g = np.random.default_rng(12)
+    L = 5
+    S = (1 << L) * 256
+    lin = [((c / 255.0) / 12.92 if c / 255.0 <= 0.04045 else ((c / 255.0 + 0.055) / 1.055) ** 2.4) for c in range(256)]
+    total = diff = 0
+    for it in range(120):
+        c = g.integers(0, S, size=3)
+        sz = int(g.choice([40, 300, 2000]))
+        V = np.clip(c[None, :] + g.integers(-sz, sz + 1, size=(3, 3)), 0, S - 1)
+        p = (V / S).astype(np.float32)
+        t = np.zeros(1, TRIANGLE_DTYPE)
+        t["v"] = p.reshape(1, 9)
+        img = g.integers(0, 256, size=(1, 1, 4), dtype=np.uint8)
+        img[0, 0, 3] = [0, 100, 127, 128, 200, 255][it % 6]
+        uv = np.zeros(1, oracle.UV_DTYPE)
+        uv["uv"] = g.uniform(-2, 3, size=(1, 6)).astype(np.float32)
+        uv["texture"] = 0
+        mine = oracle.voxelize_textured(t, uv, L, [img])
+        texel = np.array([lin[img[0, 0, 0]], lin[img[0, 0, 1]], lin[img[0, 0, 2]], img[0, 0, 3] / 255.0], np.float32)
+        theirs = ref.voxelize_triangle_texel((2 * p - 1).reshape(9), texel, L, True)
+        if img[0, 0, 3] < 128:
+            assert len(mine) == 0 and len(theirs) == 0
+            continue
+        assert len(set((mine >> 32).tolist())) <= 1 and set((mine >> 32).tolist()) == set((theirs >> 32).tolist())
+        a, b = set(mine.tolist()), set(theirs.tolist())
+        total += len(b)
+        diff += len(a ^ b)
+    assert total > 0 and diff <= 0.002 * total
