@@ -387,6 +387,7 @@ def path_trace_stats(api, octree, scene, stream, samples: int = 8) -> dict:
     (one sample per pixel, kDefaultBounce = 4 path vertices: the primary march, up to 3 diffuse bounces
     and, with the environment map, a shadow march per bounce), for the constant light and a seeded
     512x256 environment map with a sun."""
+    import numpy as np
     import torch
     g = np.random.default_rng(11)
     env = np.zeros((256, 512, 4), np.float32)
