@@ -4,8 +4,9 @@
 One step = one pass of the whole path over the 2^10 room workload (262,144 triangles, 1920x1080 primary
 rays; a seeded synthetic scene standing in for the reference's OBJ scenes): count + emit the fragment
 list, build the octree level by level, march every pixel's primary ray.  `value` is the device time of a
-step with inputs already in HBM (lower is better); `e2e` is the same step through the C ABI with host
-buffers (triangle upload, the ABI's own count/range readbacks, hit download).
+step with inputs already in HBM (lower is better), the step's launches recorded once as a CUDA graph and
+replayed; `e2e` is the same step through the C ABI with host buffers (triangle upload, the ABI's own
+count/range readbacks, hit download), launched call by call.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference] [--workload NAME]
 
@@ -227,10 +228,45 @@ def engine_arm(args, rank: int, world: int, device) -> dict:
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
+    # the step recorded once as a CUDA graph and replayed: the same kernels on the same buffers, without
+    # the host launch gaps between the step's ~26 launches (stream capture; the library's per-launch
+    # events are off while capturing)
+    graph, graph_note = None, None
+    try:
+        side = torch.cuda.Stream()
+        side.wait_stream(stream)
+        with torch.cuda.stream(side):
+            step()
+        stream.wait_stream(side)
+        torch.cuda.synchronize()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            step()
+        torch.cuda.synchronize()
+        for _ in range(args.warmup):
+            flush_buf.zero_()
+            graph.replay()
+        torch.cuda.synchronize()
+        vox.CheckEmission()
+    except Exception as e:  # capture not possible: the eager step is the measurement
+        graph, graph_note = None, f"graph capture failed ({type(e).__name__}: {e}); eager step timed"
+        torch.cuda.synchronize()
+
     sampler = ClockSampler(device.index if device.index is not None else 0)
-    events = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     barrier()
     sampler.start()
+    graph_ms = None
+    if graph is not None:
+        gev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        for a, b in gev:
+            flush_buf.zero_()
+            a.record(stream)
+            graph.replay()
+            b.record(stream)
+        barrier()
+        graph_ms = [a.elapsed_time(b) for a, b in gev]
+    # eager steps with the library's per-kernel events: the stage and kernel breakdown
+    events = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     launches0 = lib.svo_kernel_launches()
     lib.svo_profile_enable(1)
     for a, b in events:
@@ -243,7 +279,8 @@ def engine_arm(args, rank: int, world: int, device) -> dict:
     profile = _lib.profile_summary()
     lib.svo_profile_enable(0)
     clocks = sampler.stop()
-    step_ms = [a.elapsed_time(b) for a, b in events]
+    eager_ms = [a.elapsed_time(b) for a, b in events]
+    step_ms = graph_ms if graph_ms is not None else eager_ms
     ms = float(np.mean(step_ms))
     if world > 1:
         t = torch.tensor([ms], device=device)
@@ -289,6 +326,10 @@ def engine_arm(args, rank: int, world: int, device) -> dict:
         "hit_fraction": float((hit_np["flags"] & 1).mean()), "mean_iterations": float(hit_np["iter"].mean()),
         "node_fetches_per_ray": fetches / n_rays, "octree_words": info["range_words"], "leaves": info["leaves"],
         "kernels": profile,
+        "step_timing": "CUDA graph replay of the step" if graph_ms is not None else "eager launches",
+        "eager_step_ms": float(np.mean(eager_ms)),
+        "graph_step_ms": float(np.mean(graph_ms)) if graph_ms is not None else None,
+        "graph_note": graph_note,
     }
 
     # the tracer's beam optimisation on the same frame: pre-pass + advanced primary march
@@ -311,6 +352,17 @@ def engine_arm(args, rank: int, world: int, device) -> dict:
             "voxel_agreement_with_plain_march": float((hb["voxel"] == hit_np["voxel"]).all(axis=1).mean()),
             "texels": int(beam_img.numel())}
     beam["grays_per_s"] = n_rays / ((beam["prepass_ms"] + beam["march_ms"]) * 1e-3) / 1e9
+    # the pre-pass and the march in one launch (the tracer's beam path when no beam image is given)
+    hits_fused = tracer.CmdDrawPipelineBeam(None)
+    fev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(5)]
+    for e0, e1 in fev:
+        flush_buf.zero_()
+        e0.record(stream)
+        tracer.CmdDrawPipelineBeam(None, hits_fused)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    beam["fused_ms"] = float(np.median([a.elapsed_time(b) for a, b in fev]))
+    beam["fused_hits_equal_two_launch"] = bool(np.array_equal(api.hits_numpy(hits_fused), hb))
     stages["beam"] = beam
     stages["path_trace"] = path_trace_stats(api, octree, scene, stream)
 
@@ -745,7 +797,8 @@ def main() -> int:
             "data": "synthetic (seeded scene with the benchmark configuration's shapes; the reference's OBJ "
                     "scenes are not available)"}
     config = {"workload": f"{args.workload}: {WORKLOADS[args.workload]}",
-              "step": "voxelize (count+emit) + octree build + primary-ray march",
+              "step": "voxelize (count+emit) + octree build + primary-ray march, recorded once as a CUDA graph "
+                      "and replayed (stages: eager steps with per-kernel events)",
               "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MiB write); fragment list and node "
                     "pool exceed L2", "parallelism": f"replicas x{world}" if world > 1 else "single GPU"}
 

@@ -703,20 +703,29 @@ int svo_raycast_camera_beam(const svo_octree *o, const svo_camera *cam, uint32_t
 	const uint64_t n = (uint64_t)width * height;
 	if (n > 0xffffffffull) return fail(SVO_ERR_INVALID, "image too large");
 	if (n == 0) return raycast_common(o, nullptr, cam, width, height, 0, hits, fetches_dev, stream);
+	if (beam) return raycast_common(o, nullptr, cam, width, height, (uint32_t)n, hits, fetches_dev, stream, beam);
+	// no beam image given: pre-pass and march in one launch (the same texels and hits)
+	if (!hits || !aligned(hits, 16)) return fail(SVO_ERR_INVALID, "hit buffer must be 16-byte aligned");
 	cudaStream_t s = (cudaStream_t)stream;
+	MarchArgs a;
+	unsigned long long *scratch = nullptr;
+	int rc = march_args(o, s, a, &scratch);
+	if (rc) return rc;
 	float *own = nullptr;
-	if (!beam) {
-		SVO_CK(alloc_async(&own, svo_beam_texels(width, height) * sizeof(float), s), "beam allocation");
-		const int rc = svo_beam_prepass(o, cam, width, height, own, stream);
-		if (rc) {
-			cudaFreeAsync(own, s);
-			return rc;
-		}
-		beam = own;
+	cudaError_t e = alloc_async(&own, svo_beam_texels(width, height) * sizeof(float), s);
+	if (e == cudaSuccess) {
+		a.cam = *cam;
+		a.width = width;
+		a.height = height;
+		a.n = (uint32_t)n;
+		a.hits = hits;
+		a.fetches = (unsigned long long *)fetches_dev;
+		e = march_beam_fused_launch(a, own, s);
+		cudaFreeAsync(own, s);
 	}
-	const int rc = raycast_common(o, nullptr, cam, width, height, (uint32_t)n, hits, fetches_dev, stream, beam);
-	if (own) cudaFreeAsync(own, s);
-	return rc;
+	cudaFreeAsync(scratch, s);
+	if (e != cudaSuccess) return cuda_fail(e, "beam march");
+	return SVO_OK;
 }
 
 int svo_occlude(const svo_octree *o, const svo_ray *rays, uint32_t n, uint32_t *occluded, void *stream) {

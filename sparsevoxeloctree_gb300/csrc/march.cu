@@ -529,30 +529,109 @@ SVO_DEV float ray_tangent(const float x[3], const float y[3]) {
 // texel per corner of each kBeamSize x kBeamSize pixel tile.  The ray through the corner and the 4 rays
 // half a texel away give the cone's tangent; the coarse march stops at the first node the cone does
 // not resolve, and the texel is max(0, t - node size), or 1e10 when the cone misses.
+SVO_DEV float beam_texel(const MarchArgs &a, uint32_t i, uint32_t bw, float orig_sz, uint32_t *stack) {
+	const float W = (float)a.width, H = (float)a.height, bs = (float)kBeamSize;
+	const uint32_t by = i / bw, bx = i - by * bw;
+	const float fx = (float)bx, fy = (float)by;
+	float d[3], dk[3];
+	gen_dir(a.cam, fx / W * bs, fy / H * bs, d);
+	gen_dir(a.cam, (fx + 0.5f) / W * bs, (fy + 0.5f) / H * bs, dk);
+	const float t0 = ray_tangent(d, dk);
+	gen_dir(a.cam, (fx + -0.5f) / W * bs, (fy + 0.5f) / H * bs, dk);
+	const float t1 = ray_tangent(d, dk);
+	gen_dir(a.cam, (fx + 0.5f) / W * bs, (fy + -0.5f) / H * bs, dk);
+	const float t2 = ray_tangent(d, dk);
+	gen_dir(a.cam, (fx + -0.5f) / W * bs, (fy + -0.5f) / H * bs, dk);
+	const float t3 = ray_tangent(d, dk);
+	const float dir_sz = 2.0f * max_glsl(max_glsl(t0, t1), max_glsl(t2, t3));
+	const float o[3] = {a.cam.pos[0], a.cam.pos[1], a.cam.pos[2]};
+	float t, sz;
+	const bool hit = march_traverse<true, kMarchTPB>(a.pool, a.range, a.level, o, d, orig_sz, dir_sz, stack, t, sz,
+	                                                 a.status);
+	return hit ? max_glsl(0.0f, t - sz) : 1e10f;
+}
+
 __global__ void __launch_bounds__(kMarchTPB) beam_kernel(MarchArgs a, float *__restrict__ beam, float orig_sz) {
 	__shared__ uint32_t s_stack[SVO_LEVEL_MAX * kMarchTPB];
 	uint32_t *stack = s_stack + threadIdx.x;
 	const uint32_t bw = (a.width + kBeamSize - 1) / kBeamSize + 1, bh = (a.height + kBeamSize - 1) / kBeamSize + 1;
-	const float W = (float)a.width, H = (float)a.height, bs = (float)kBeamSize;
-	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < bw * bh; i += gridDim.x * blockDim.x) {
-		const uint32_t by = i / bw, bx = i - by * bw;
-		const float fx = (float)bx, fy = (float)by;
-		float d[3], dk[3];
-		gen_dir(a.cam, fx / W * bs, fy / H * bs, d);
-		gen_dir(a.cam, (fx + 0.5f) / W * bs, (fy + 0.5f) / H * bs, dk);
-		const float t0 = ray_tangent(d, dk);
-		gen_dir(a.cam, (fx + -0.5f) / W * bs, (fy + 0.5f) / H * bs, dk);
-		const float t1 = ray_tangent(d, dk);
-		gen_dir(a.cam, (fx + 0.5f) / W * bs, (fy + -0.5f) / H * bs, dk);
-		const float t2 = ray_tangent(d, dk);
-		gen_dir(a.cam, (fx + -0.5f) / W * bs, (fy + -0.5f) / H * bs, dk);
-		const float t3 = ray_tangent(d, dk);
-		const float dir_sz = 2.0f * max_glsl(max_glsl(t0, t1), max_glsl(t2, t3));
-		const float o[3] = {a.cam.pos[0], a.cam.pos[1], a.cam.pos[2]};
-		float t, sz;
-		const bool hit = march_traverse<true, kMarchTPB>(a.pool, a.range, a.level, o, d, orig_sz, dir_sz, stack, t, sz,
-		                                                 a.status);
-		beam[i] = hit ? max_glsl(0.0f, t - sz) : 1e10f;
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < bw * bh; i += gridDim.x * blockDim.x)
+		beam[i] = beam_texel(a, i, bw, orig_sz, stack);
+}
+
+// Beam pre-pass and beam-advanced primary march in one persistent launch.  Work slots come from one
+// ticket: first the texels (32 per claim), then the 8x4-pixel tiles of the image (32 rays per claim).
+// A tile's 4 beam texels (an 8x4 tile lies inside one 8x8 beam tile) were all claimed before the
+// tile, by warps that are running and wait on nothing, so the tile's warp polls them (acquire loads,
+// bounded) and marches as soon as they are published; the slow coarse marches of a few texels overlap
+// the other tiles' marches instead of ending a separate launch.  Texels start as the all-ones pattern,
+// which no texel value has.  Every value is the separate kernels' value bit for bit.
+constexpr uint32_t kBeamUnset = 0xffffffffu;
+
+__global__ void __launch_bounds__(kMarchTPB) march_beam_fused_kernel(MarchArgs a, float *__restrict__ beam,
+                                                                     float orig_sz) {
+	__shared__ uint32_t s_stack[SVO_LEVEL_MAX * kMarchTPB];
+	uint32_t *stack = s_stack + threadIdx.x;
+	const uint32_t lane = lane_id();
+	const uint32_t bw = (a.width + kBeamSize - 1) / kBeamSize + 1, bh = (a.height + kBeamSize - 1) / kBeamSize + 1;
+	const uint64_t texels = (uint64_t)bw * bh, texel_slots = (texels + 31u) / 32u * 32u;
+	const uint32_t tiles_x = (a.width + 7u) / 8u;
+	const uint64_t slots = texel_slots + (uint64_t)tiles_x * ((a.height + 3u) / 4u) * 32u;
+	unsigned long long fetched = 0;
+	for (;;) {
+		unsigned long long base = 0;
+		if (lane == 0) base = atomicAdd(a.ticket, 32ull);
+		base = __shfl_sync(kFullMask, base, 0);
+		if (base >= slots) break;
+		if (base < texel_slots) {
+			const uint64_t i = base + lane;
+			if (i < texels) {
+				const float v = beam_texel(a, (uint32_t)i, bw, orig_sz, stack);
+				asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(beam + i), "r"(__float_as_uint(v)) : "memory");
+			}
+			continue;
+		}
+		const uint64_t slot = base - texel_slots + lane;
+		const uint32_t tile = (uint32_t)(slot >> 5), in = (uint32_t)(slot & 31u);
+		const uint32_t tx = tile % tiles_x, ty = tile / tiles_x;
+		const uint32_t x = tx * 8u + (in & 7u), y = ty * 4u + (in >> 3);
+		// lanes 0..3 fetch texels (bx, by), (bx + 1, by), (bx, by + 1), (bx + 1, by + 1) of the beam tile
+		float tv = 0.0f;
+		if (lane < 4) {
+			const uint32_t bx = tx * 8u / kBeamSize, by = ty * 4u / kBeamSize;
+			const float *p = beam + (size_t)(by + (lane >> 1)) * bw + bx + (lane & 1u);
+			uint32_t w, spins = 0;
+			for (;;) {
+				asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(w) : "l"(p) : "memory");
+				if (w != kBeamUnset) break;
+				if (++spins > kSpinLimit) { // a texel that never came: report, march from the camera
+					atomicOr(a.status, kStatusTimeout);
+					w = 0u;
+					break;
+				}
+				__nanosleep(64);
+			}
+			tv = __uint_as_float(w);
+		}
+		const float t00 = __shfl_sync(kFullMask, tv, 0), t01 = __shfl_sync(kFullMask, tv, 1);
+		const float t10 = __shfl_sync(kFullMask, tv, 2), t11 = __shfl_sync(kFullMask, tv, 3);
+		const float m = min_glsl(min_glsl(t00, t01), min_glsl(t10, t11));
+		if (x < a.width && y < a.height) {
+			const uint32_t r = y * a.width + x;
+			float o[3], d[3];
+			camera_ray(a.cam, a.width, a.height, r, o, d);
+#pragma unroll
+			for (int k = 0; k < 3; ++k) o[k] = o[k] + d[k] * m;
+			MarchOut mo;
+			uint32_t nf;
+			march_ray<kMarchTPB>(a.pool, a.range, a.level, o, d, stack, mo, nf, a.status);
+			store_hit(a.hits, r, mo);
+			fetched += nf;
+		}
+	}
+	if (a.fetches) {
+		fetched = warp_sum(fetched);
+		if (lane == 0) atomicAdd(a.fetches, fetched);
 	}
 }
 
@@ -1114,6 +1193,20 @@ cudaError_t beam_launch(const MarchArgs &a, float *beam, cudaStream_t stream) {
 	                                                                            (uint64_t)sms * 16));
 	const float orig_sz = ldexpf(1.0f, 1 - (int)a.level); // exp2f(1 - level), src/OctreeTracer.cpp:205
 	SVO_LAUNCH("beam_prepass", stream, beam_kernel<<<blocks, kMarchTPB, 0, stream>>>(a, beam, orig_sz););
+	return cudaGetLastError();
+}
+
+cudaError_t march_beam_fused_launch(const MarchArgs &a, float *beam, cudaStream_t stream) {
+	const uint64_t texels = (uint64_t)((a.width + kBeamSize - 1) / kBeamSize + 1) * ((a.height + kBeamSize - 1) / kBeamSize + 1);
+	cudaError_t e = cudaMemsetAsync(a.ticket, 0, sizeof(unsigned long long), stream);
+	if (e == cudaSuccess) e = cudaMemsetAsync(beam, 0xff, texels * sizeof(float), stream); // kBeamUnset
+	if (e != cudaSuccess || a.width == 0 || a.height == 0) return e;
+	const int sms = device_sm_count();
+	const uint64_t slots = (texels + 31) / 32 * 32 + (uint64_t)((a.width + 7u) / 8u) * ((a.height + 3u) / 4u) * 32u;
+	const uint64_t blocks_needed = (slots / 32 + kMarchTPB / 32 - 1) / (kMarchTPB / 32);
+	const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(blocks_needed, (uint64_t)sms * 16));
+	const float orig_sz = ldexpf(1.0f, 1 - (int)a.level);
+	SVO_LAUNCH("march_beam", stream, march_beam_fused_kernel<<<blocks, kMarchTPB, 0, stream>>>(a, beam, orig_sz););
 	return cudaGetLastError();
 }
 

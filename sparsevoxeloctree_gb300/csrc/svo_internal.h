@@ -273,6 +273,9 @@ struct MarchArgs {
 cudaError_t march_launch(const MarchArgs &a, bool camera, cudaStream_t stream);
 // Beam pre-pass texels ((width + 7) / 8 + 1) x ((height + 7) / 8 + 1) for camera `a.cam`.
 cudaError_t beam_launch(const MarchArgs &a, float *beam, cudaStream_t stream);
+// Beam pre-pass + beam-advanced camera march in one launch (hits as march_launch with a.beam, and the
+// beam image written to `beam`).
+cudaError_t march_beam_fused_launch(const MarchArgs &a, float *beam, cudaStream_t stream);
 // Octree_RayMarchOcclude for a.n rays: occluded[i] = 1 when ray i hits a leaf.
 cudaError_t occlude_launch(const MarchArgs &a, uint32_t *occluded, cudaStream_t stream);
 cudaError_t bounce_launch(const svo_hit *hits, uint32_t n, uint64_t seed, svo_ray *rays, cudaStream_t stream);
