@@ -62,6 +62,17 @@ SVO_DEV uint32_t morton(uint32_t x, uint32_t y, uint32_t z, uint32_t shift) {
 	return spread3(x >> shift) | (spread3(y >> shift) << 1) | (spread3(z >> shift) << 2);
 }
 
+// The fragment sweeps spread coordinates through a 1024-entry table in shared memory (three loads
+// instead of three 4-step bit spreads); the table holds spread3(i) for every 10-bit i.
+constexpr uint32_t kSpreadEntries = 1024;
+SVO_DEV void spread_table_init(uint32_t *tab) {
+	for (uint32_t i = threadIdx.x; i < kSpreadEntries; i += blockDim.x) tab[i] = spread3(i);
+	__syncthreads();
+}
+SVO_DEV uint32_t morton_tab(const uint32_t *tab, uint32_t x, uint32_t y, uint32_t z, uint32_t shift) {
+	return tab[(x >> shift) & 0x3ffu] | (tab[(y >> shift) & 0x3ffu] << 1) | (tab[(z >> shift) & 0x3ffu] << 2);
+}
+
 SVO_DEV uint32_t octant_at(uint32_t x, uint32_t y, uint32_t z, uint32_t shift) {
 	return ((x >> shift) & 1u) | (((y >> shift) & 1u) << 1) | (((z >> shift) & 1u) << 2);
 }
@@ -171,6 +182,8 @@ SVO_DEV uint64_t sweep_run_stride() { return (uint64_t)gridDim.x * (blockDim.x >
 template <bool B>
 __global__ void __launch_bounds__(kTPB) dense_mark(const uint64_t *__restrict__ frags, uint64_t n, BuildBatch bb,
                                                    uint32_t *__restrict__ bcount) {
+	__shared__ uint32_t s_spread[kSpreadEntries];
+	spread_table_init(s_spread);
 	const uint64_t runs = (n + 31ull) >> 5;
 	const uint32_t lane = lane_id();
 	for (uint64_t r = sweep_first_run(); r < runs; r += sweep_run_stride()) {
@@ -194,12 +207,12 @@ __global__ void __launch_bounds__(kTPB) dense_mark(const uint64_t *__restrict__ 
 					flag_bad_fragment(md.state, bb.gstate);
 				} else if (D >= 1) {
 					const uint32_t shift = md.level - D;
-					const uint32_t m = morton(x, y, z, shift);
+					const uint32_t m = morton_tab(s_spread, x, y, z, shift);
 					word = md.mark_word + (m >> 5);
 					bit = 1u << (m & 31);
 					key = md.bucket_base + (m >> (3 * (md.bshift - shift))); // a prefix of the depth-D code
 				} else {
-					key = md.bucket_base + morton(x, y, z, md.bshift);
+					key = md.bucket_base + morton_tab(s_spread, x, y, z, md.bshift);
 				}
 				if (word != 0xffffffffu && !SVO_CHECK(word < bb.dense_total, 1u, bb.gstate)) word = 0xffffffffu, bit = 0;
 				if (key != 0xffffffffu && !SVO_CHECK(key < bb.nb_total, 2u, bb.gstate)) key = 0xffffffffu;
@@ -527,7 +540,6 @@ uint64_t leaf_window_bound(uint32_t count, uint32_t level) {
 	return (8ull * parents + 4095) / 4096;
 }
 
-SVO_DEV uint32_t bucket_of(uint32_t x, uint32_t y, uint32_t z, uint32_t bshift) { return morton(x, y, z, bshift); }
 
 // Exclusive prefix of the bucket counts (boff[nb] = total) and the list of non-empty buckets in order;
 // two single-pass look-back scans, tiles claimed in order by ticket.
@@ -583,6 +595,8 @@ template <bool B>
 __global__ void __launch_bounds__(kTPB) bucket_scatter(const uint64_t *__restrict__ frags, uint64_t n, BuildBatch bb,
                                                        const uint32_t *__restrict__ boff, uint32_t *__restrict__ bfill,
                                                        uint64_t *__restrict__ sorted) {
+	__shared__ uint32_t s_spread[kSpreadEntries];
+	spread_table_init(s_spread);
 	const uint64_t runs = (n + 31ull) >> 5;
 	const uint32_t lane = lane_id();
 	for (uint64_t r = sweep_first_run(); r < runs; r += sweep_run_stride()) {
@@ -611,7 +625,7 @@ __global__ void __launch_bounds__(kTPB) bucket_scatter(const uint64_t *__restric
 					const uint32_t *pbits = md.dv.bits + md.parent_off;
 					const uint32_t *pprefix = md.dv.prefix + md.parent_off;
 					const uint32_t leaf_begin = md.state->lv[level].begin;
-					const uint32_t m = morton(x, y, z, 1), w = m >> 5;
+					const uint32_t m = morton_tab(s_spread, x, y, z, 1), w = m >> 5;
 					key[k] = m >> (3 * (md.bshift - 1));
 					out[k] = ((uint64_t)(octant_at(x, y, z, 0) +
 					                     8u * (1u + __ldg(pprefix + w) +
@@ -620,7 +634,7 @@ __global__ void __launch_bounds__(kTPB) bucket_scatter(const uint64_t *__restric
 					          << 32) |
 					         ((frag >> 32) & 0xffffffu);
 				} else {
-					key[k] = bucket_of(x, y, z, md.bshift);
+					key[k] = morton_tab(s_spread, x, y, z, md.bshift);
 					if (items) // level 1: the leaf words are the root block
 						out[k] = ((uint64_t)octant_at(x, y, z, 0) << 32) | ((frag >> 32) & 0xffffffu);
 				}
