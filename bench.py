@@ -364,7 +364,8 @@ def engine_arm(args, rank: int, world: int, device) -> dict:
     beam["fused_ms"] = float(np.median([a.elapsed_time(b) for a, b in fev]))
     beam["fused_hits_equal_two_launch"] = bool(np.array_equal(api.hits_numpy(hits_fused), hb))
     stages["beam"] = beam
-    stages["path_trace"] = path_trace_stats(api, octree, scene, stream)
+    if not args.no_path_trace:
+        stages["path_trace"] = path_trace_stats(api, octree, scene, stream)
 
     e2e = None if args.no_e2e else e2e_arm(args, scene, tris_host, device, world)
     cpu = None
@@ -785,6 +786,7 @@ def main() -> int:
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-build leg")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
     ap.add_argument("--no-autotune", action="store_true", help="default launch parameters")
+    ap.add_argument("--no-path-trace", action="store_true", help="skip the path-tracer statistics")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 

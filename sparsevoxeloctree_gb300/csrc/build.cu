@@ -167,13 +167,14 @@ template <bool B> __global__ void build_init(BuildBatch bb, BuildState *gstate) 
 // The fragment sweeps (dense_mark, bucket_scatter) take kSweepRuns warp-sized runs of fragments per warp
 // and pass, loading all of them before any is processed: each fragment's work is a short dependent chain
 // (load, bitmap lookups, one atomic per group of a warp), so independent loads in flight set the rate.
-constexpr uint32_t kSweepRuns = 4;
+constexpr uint32_t kSweepRuns = 4;   // dense_mark
+constexpr uint32_t kScatterRuns = 2; // bucket_scatter (more state per fragment: fewer runs, more warps)
 
-// First run of warp w's pass and the run stride of the sweep.
-SVO_DEV uint64_t sweep_first_run() {
-	return ((uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * kSweepRuns;
+// First run of warp w's pass and the run stride of a sweep taking R runs per warp and pass.
+template <uint32_t R> SVO_DEV uint64_t sweep_first_run() {
+	return ((uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * R;
 }
-SVO_DEV uint64_t sweep_run_stride() { return (uint64_t)gridDim.x * (blockDim.x >> 5) * kSweepRuns; }
+template <uint32_t R> SVO_DEV uint64_t sweep_run_stride() { return (uint64_t)gridDim.x * (blockDim.x >> 5) * R; }
 
 // Sets the depth-D occupancy bit of every fragment and counts the fragments of every bucket.  Per warp,
 // consecutive fragments that fall in the same bitmap word (or bucket) are merged first, so one atomic
@@ -186,7 +187,7 @@ __global__ void __launch_bounds__(kTPB) dense_mark(const uint64_t *__restrict__ 
 	spread_table_init(s_spread);
 	const uint64_t runs = (n + 31ull) >> 5;
 	const uint32_t lane = lane_id();
-	for (uint64_t r = sweep_first_run(); r < runs; r += sweep_run_stride()) {
+	for (uint64_t r = sweep_first_run<kSweepRuns>(); r < runs; r += sweep_run_stride<kSweepRuns>()) {
 		uint64_t fr[kSweepRuns];
 #pragma unroll
 		for (uint32_t k = 0; k < kSweepRuns; ++k) {
@@ -599,16 +600,16 @@ __global__ void __launch_bounds__(kTPB) bucket_scatter(const uint64_t *__restric
 	spread_table_init(s_spread);
 	const uint64_t runs = (n + 31ull) >> 5;
 	const uint32_t lane = lane_id();
-	for (uint64_t r = sweep_first_run(); r < runs; r += sweep_run_stride()) {
-		uint64_t out[kSweepRuns], send[kSweepRuns];
-		uint32_t key[kSweepRuns], pad[kSweepRuns], first[kSweepRuns], base[kSweepRuns];
+	for (uint64_t r = sweep_first_run<kScatterRuns>(); r < runs; r += sweep_run_stride<kScatterRuns>()) {
+		uint64_t out[kScatterRuns], send[kScatterRuns];
+		uint32_t key[kScatterRuns], pad[kScatterRuns], first[kScatterRuns], base[kScatterRuns];
 #pragma unroll
-		for (uint32_t k = 0; k < kSweepRuns; ++k) {
+		for (uint32_t k = 0; k < kScatterRuns; ++k) {
 			const uint64_t f = ((r + k) << 5) + lane;
 			out[k] = f < n ? __ldcs(frags + f) : 0ull;
 		}
 #pragma unroll
-		for (uint32_t k = 0; k < kSweepRuns; ++k) {
+		for (uint32_t k = 0; k < kScatterRuns; ++k) {
 			const uint64_t f = ((r + k) << 5) + lane;
 			key[k] = 0xffffffffu, pad[k] = 0, send[k] = 0;
 			if (f < n) {
@@ -649,14 +650,14 @@ __global__ void __launch_bounds__(kTPB) bucket_scatter(const uint64_t *__restric
 		// one cursor atomic per run of equal keys in consecutive lanes; the atomics of all runs of
 		// fragments are in flight together
 #pragma unroll
-		for (uint32_t k = 0; k < kSweepRuns; ++k) {
+		for (uint32_t k = 0; k < kScatterRuns; ++k) {
 			uint32_t last;
 			lane_run(key[k], lane, first[k], last);
 			base[k] = 0;
 			if (key[k] != 0xffffffffu && lane == first[k]) base[k] = atomicAdd(bfill + key[k], last - first[k] + 1u);
 		}
 #pragma unroll
-		for (uint32_t k = 0; k < kSweepRuns; ++k) {
+		for (uint32_t k = 0; k < kScatterRuns; ++k) {
 			const uint32_t b = __shfl_sync(kFullMask, base[k], first[k]);
 			if (key[k] != 0xffffffffu) {
 				const uint64_t at = (uint64_t)__ldg(boff + key[k]) + pad[k] + b + (lane - first[k]);
@@ -1153,7 +1154,7 @@ static void launch_dense_and_scatter(const uint64_t *frags, uint64_t n, uint32_t
 	// the bucketed copy: leaf items when the leaf parents are dense (their bitmap is final now), fragments
 	// for the sparse levels otherwise
 	SVO_LAUNCH("bucket_scatter", stream,
-	           bucket_scatter<B><<<grid_for(n, kTPB * kSweepRuns, sweep), kTPB, 0, stream>>>(frags, n, bb, boff, bfill,
+	           bucket_scatter<B><<<grid_for(n, kTPB * kScatterRuns, sweep), kTPB, 0, stream>>>(frags, n, bb, boff, bfill,
 	                                                                                      sorted););
 }
 
