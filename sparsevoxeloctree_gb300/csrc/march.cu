@@ -891,35 +891,117 @@ SVO_DEV uint32_t snorm8_store(float v) {
 	return (uint32_t)(int32_t)floorf(fminf(fmaxf(v, -1.0f), 1.0f) * 127.0f + 0.5f) & 0xffu;
 }
 
-// One sample of pixel (x, y): ConstColorPathTrace / EnvMapPathTrace (shader/path_tracer.comp:32-109) and
-// the running means of main() (shader/path_tracer.comp:111-135).
-template <uint32_t LIGHT, int STRIDE>
-SVO_DEV void pt_pixel(const PtArgs &a, uint32_t x, uint32_t y, uint32_t spp, float s0x, float s0y, uint32_t *stack) {
-	const uint32_t ni = (((y & 255u) << 8) | (x & 255u)) * 2u;
-	const float nz[2] = {(float)__ldg(a.noise + ni) / 255.0f, (float)__ldg(a.noise + ni + 1) / 255.0f};
-	float o[3] = {a.cam.pos[0], a.cam.pos[1], a.cam.pos[2]}, d[3];
-	gen_dir(a.cam, ((float)x + s0x) / (float)a.width, ((float)y + s0y) / (float)a.height, d);
+// Wavefront form of ConstColorPathTrace / EnvMapPathTrace (shader/path_tracer.comp:32-109): one launch
+// per path vertex over the paths still alive, so a warp's lanes all march one ray (and, with the
+// environment light, one shadow ray) instead of waiting for the warp's longest path.  Each path's
+// arithmetic is the shader's loop body in its order, so the images are those of the per-pixel loop.
+// Path state lives in HBM between launches; the surviving paths of a vertex are appended to a queue
+// (warp-aggregated cursor), counts and tickets are device words, so a sample needs no host round trip.
+SVO_DEV uint32_t nrm_code(const float n[3]) {
+	const uint32_t ax = n[0] != 0.0f ? 0u : (n[1] != 0.0f ? 1u : 2u);
+	return ax | ((n[ax] < 0.0f ? 1u : 0u) << 2);
+}
+SVO_DEV void nrm_decode(uint32_t c, float n[3]) {
+	n[0] = n[1] = n[2] = 0.0f;
+	if (c != kPathNoNormal) n[c & 3u] = (c & 4u) ? -1.0f : 1.0f;
+}
 
-	float acc[3] = {1.0f, 1.0f, 1.0f}, rad[3] = {0.0f, 0.0f, 0.0f};
-	float dalb[3] = {0.0f, 0.0f, 0.0f}, dnrm[3] = {0.0f, 0.0f, 0.0f};
-	float pos[3], alb[3], nrm[3];
-	if (pt_leaf<STRIDE>(a, o, d, stack, pos, alb, nrm)) {
+// Appends the lanes with `alive` set to queue `q` (count `*cnt`), in lane order within the warp.
+SVO_DEV void queue_append(bool alive, uint32_t p, uint32_t *q, uint32_t *cnt) {
+	const uint32_t lane = lane_id(), m = __ballot_sync(kFullMask, alive);
+	if (!m) return;
+	uint32_t base = 0;
+	if (lane == (uint32_t)(__ffs(m) - 1)) base = atomicAdd(cnt, (uint32_t)__popc(m));
+	base = __shfl_sync(kFullMask, base, __ffs(m) - 1);
+	if (alive) q[base + __popc(m & ((1u << lane) - 1u))] = p;
+}
+
+// Vertex 0: the camera ray of every pixel (main(), shader/path_tracer.comp:115-119) and its first hit.
+template <uint32_t LIGHT>
+__global__ void __launch_bounds__(kMarchTPB) pt_primary_kernel(PtArgs a) {
+	__shared__ uint32_t s_stack[SVO_LEVEL_MAX * kMarchTPB];
+	uint32_t *stack = s_stack + threadIdx.x;
+	const uint32_t lane = lane_id();
+	const uint32_t tiles_x = (a.width + 7u) / 8u;
+	const uint64_t slots = (uint64_t)tiles_x * ((a.height + 3u) / 4u) * 32u;
+	const float s0x = sobol_f(__ldg(a.sobol)), s0y = sobol_f(__ldg(a.sobol + 1));
+	for (;;) {
+		unsigned long long base = 0;
+		if (lane == 0) base = atomicAdd(a.tickets, 32ull);
+		base = __shfl_sync(kFullMask, base, 0);
+		if (base >= slots) break;
+		const uint64_t slot = base + lane;
+		const uint32_t tile = (uint32_t)(slot >> 5), in = (uint32_t)(slot & 31u);
+		const uint32_t x = (tile % tiles_x) * 8u + (in & 7u), y = (tile / tiles_x) * 4u + (in >> 3);
+		const bool live = x < a.width && y < a.height;
+		bool alive = false;
+		const uint32_t p = y * a.width + x;
+		if (live) {
+			float o[3] = {a.cam.pos[0], a.cam.pos[1], a.cam.pos[2]}, d[3];
+			gen_dir(a.cam, ((float)x + s0x) / (float)a.width, ((float)y + s0y) / (float)a.height, d);
+			float pos[3], alb[3], nrm[3];
+			PathState &S = a.paths[p];
+			if (pt_leaf<kMarchTPB>(a, o, d, stack, pos, alb, nrm)) {
 #pragma unroll
-		for (int k = 0; k < 3; ++k) acc[k] *= alb[k], dalb[k] = alb[k], dnrm[k] = nrm[k];
-		for (uint32_t cur = 1; cur < a.bounce; ++cur) {
-			float samp[2] = {sobol_f(__ldg(a.sobol + 2 * cur)) + nz[0], sobol_f(__ldg(a.sobol + 2 * cur + 1)) + nz[1]};
+				for (int k = 0; k < 3; ++k) S.acc[k] = 1.0f * alb[k], S.rad[k] = 0.0f, S.pos[k] = pos[k], S.dalb[k] = alb[k];
+				S.nrm = S.first_nrm = nrm_code(nrm);
+				alive = a.bounce > 1;
+			} else {
+				float rad[3];
+				if (LIGHT == 1) {
+					const float4 env = env_lookup(a.env, d, a.env_rotation);
+					rad[0] = env.x, rad[1] = env.y, rad[2] = env.z;
+				} else {
+					rad[0] = a.const_color[0], rad[1] = a.const_color[1], rad[2] = a.const_color[2];
+				}
+#pragma unroll
+				for (int k = 0; k < 3; ++k) S.rad[k] = rad[k], S.dalb[k] = 0.0f;
+				S.first_nrm = kPathNoNormal;
+			}
+		}
+		queue_append(alive, p, a.queue[1], a.counts + 1);
+	}
+}
+
+// Path vertex `cur` (1 <= cur < bounce) of every path alive at it: the loop body of
+// ConstColorPathTrace / EnvMapPathTrace (light sample with its shadow march, diffuse bounce, leaf march).
+template <uint32_t LIGHT>
+__global__ void __launch_bounds__(kMarchTPB) pt_bounce_kernel(PtArgs a, uint32_t cur) {
+	__shared__ uint32_t s_stack[SVO_LEVEL_MAX * kMarchTPB];
+	uint32_t *stack = s_stack + threadIdx.x;
+	const uint32_t lane = lane_id();
+	const uint32_t n = a.counts[cur];
+	const uint32_t *qin = a.queue[cur & 1u];
+	uint32_t *qout = a.queue[(cur + 1u) & 1u];
+	const float sx = sobol_f(__ldg(a.sobol + 2 * cur)), sy = sobol_f(__ldg(a.sobol + 2 * cur + 1));
+	for (;;) {
+		unsigned long long base = 0;
+		if (lane == 0) base = atomicAdd(a.tickets + cur, 32ull);
+		base = __shfl_sync(kFullMask, base, 0);
+		if (base >= n) break;
+		const uint64_t i = base + lane;
+		bool alive = false;
+		uint32_t p = 0;
+		if (i < n) {
+			p = qin[i];
+			const uint32_t y = p / a.width, x = p - y * a.width;
+			PathState &S = a.paths[p];
+			const uint32_t ni = (((y & 255u) << 8) | (x & 255u)) * 2u;
+			float samp[2] = {sx + (float)__ldg(a.noise + ni) / 255.0f, sy + (float)__ldg(a.noise + ni + 1) / 255.0f};
 			samp[0] = samp[0] - floorf(samp[0]);
 			samp[1] = samp[1] - floorf(samp[1]);
+			float o[3], acc[3], rad[3], nrm[3], d[3];
 #pragma unroll
-			for (int k = 0; k < 3; ++k) o[k] = pos[k];
+			for (int k = 0; k < 3; ++k) o[k] = S.pos[k], acc[k] = S.acc[k], rad[k] = S.rad[k];
+			nrm_decode(S.nrm, nrm);
 			if (LIGHT == 1) { // multiple importance sampling, light sample
 				float ld[3], light[3], light_pdf;
 				env_sample(a.env, samp[0], samp[1], a.env_rotation, ld, light, light_pdf);
 				const float ndd = (nrm[0] * ld[0] + nrm[1] * ld[1]) + nrm[2] * ld[2];
 				if (ndd > 0.0f && !isnan(light_pdf) && light_pdf > 0.0f) {
 					float t, sz;
-					if (!march_traverse<false, STRIDE>(a.pool, a.range, a.level, o, ld, 0.0f, 0.0f, stack, t, sz,
-					                                   a.status)) {
+					if (!march_traverse<false, kMarchTPB>(a.pool, a.range, a.level, o, ld, 0.0f, 0.0f, stack, t, sz,
+					                                      a.status)) {
 						const float bsdf_pdf = ndd / kPi;
 						const float w = mis_power(light_pdf, bsdf_pdf);
 #pragma unroll
@@ -938,69 +1020,53 @@ SVO_DEV void pt_pixel(const PtArgs &a, uint32_t x, uint32_t y, uint32_t spp, flo
 				bsdf_pdf = dl[2] / kPi;
 				align_direction(dl, nrm, d);
 			}
-			if (pt_leaf<STRIDE>(a, o, d, stack, pos, alb, nrm)) {
+			float pos[3], alb[3];
+			if (pt_leaf<kMarchTPB>(a, o, d, stack, pos, alb, nrm)) {
 #pragma unroll
-				for (int k = 0; k < 3; ++k) acc[k] *= alb[k];
-			} else {
-				if (LIGHT == 1) { // multiple importance sampling, bsdf sample
-					// EnvMap_PDF and EnvMap_Radiance read the same filtered texel
-					const float4 env = env_lookup(a.env, d, a.env_rotation);
-					const float light_pdf = env.w / (kTwoPiPi * sqrtf(1.0f - d[1] * d[1]));
-					if (!isnan(light_pdf) && light_pdf > 0.0f) {
-						const float w = mis_power(bsdf_pdf, light_pdf);
-						const float e3[3] = {env.x, env.y, env.z};
+				for (int k = 0; k < 3; ++k) S.acc[k] = acc[k] * alb[k], S.pos[k] = pos[k];
+				S.nrm = nrm_code(nrm);
+				alive = cur + 1u < a.bounce;
+			} else if (LIGHT == 1) { // multiple importance sampling, bsdf sample
+				// EnvMap_PDF and EnvMap_Radiance read the same filtered texel
+				const float4 env = env_lookup(a.env, d, a.env_rotation);
+				const float light_pdf = env.w / (kTwoPiPi * sqrtf(1.0f - d[1] * d[1]));
+				if (!isnan(light_pdf) && light_pdf > 0.0f) {
+					const float w = mis_power(bsdf_pdf, light_pdf);
+					const float e3[3] = {env.x, env.y, env.z};
 #pragma unroll
-						for (int k = 0; k < 3; ++k) rad[k] += acc[k] * e3[k] * a.env_multiplier * w;
-					}
-				} else {
-#pragma unroll
-					for (int k = 0; k < 3; ++k) rad[k] = acc[k] * a.const_color[k];
+					for (int k = 0; k < 3; ++k) rad[k] += acc[k] * e3[k] * a.env_multiplier * w;
 				}
-				break;
+			} else {
+#pragma unroll
+				for (int k = 0; k < 3; ++k) rad[k] = acc[k] * a.const_color[k];
 			}
+#pragma unroll
+			for (int k = 0; k < 3; ++k) S.rad[k] = rad[k];
 		}
-	} else if (LIGHT == 1) {
-		const float4 env = env_lookup(a.env, d, a.env_rotation);
-		rad[0] = env.x, rad[1] = env.y, rad[2] = env.z;
-	} else {
-#pragma unroll
-		for (int k = 0; k < 3; ++k) rad[k] = a.const_color[k];
+		queue_append(alive, p, qout, a.counts + cur + 1);
 	}
-
-	const size_t p = (size_t)y * a.width + x;
-	const float fs = (float)spp, fn = (float)(spp + 1u);
-	const float4 c = a.color[p];
-	a.color[p] = make_float4((c.x * fs + rad[0]) / fn, (c.y * fs + rad[1]) / fn, (c.z * fs + rad[2]) / fn, 1.0f);
-	const uint32_t wa = a.albedo[p], wn = a.normal[p];
-	uint32_t oa = 255u << 24, on = 127u << 24;
-#pragma unroll
-	for (int k = 0; k < 3; ++k) {
-		oa |= unorm8_store((unorm8_load(wa, k) * fs + dalb[k]) / fn) << (8 * k);
-		on |= snorm8_store((snorm8_load(wn, k) * fs + dnrm[k]) / fn) << (8 * k);
-	}
-	a.albedo[p] = oa;
-	a.normal[p] = on;
 }
 
-// One sample per pixel; warps claim 8x4-pixel tiles from a ticket like the camera march.
-template <uint32_t LIGHT>
-__global__ void __launch_bounds__(kMarchTPB) pt_kernel(PtArgs a) {
-	__shared__ uint32_t s_stack[SVO_LEVEL_MAX * kMarchTPB];
-	uint32_t *stack = s_stack + threadIdx.x;
-	const uint32_t lane = lane_id();
-	const uint32_t tiles_x = (a.width + 7u) / 8u;
-	const uint64_t slots = (uint64_t)tiles_x * ((a.height + 3u) / 4u) * 32u;
+// main()'s running means (shader/path_tracer.comp:121-134) of every pixel's sample.
+__global__ void pt_accumulate_kernel(PtArgs a) {
 	const uint32_t spp = __ldg(a.sobol + 2u * (a.bounce + 1u)); // Sobol_Current((uBounce + 1) << 1)
-	const float s0x = sobol_f(__ldg(a.sobol)), s0y = sobol_f(__ldg(a.sobol + 1));
-	for (;;) {
-		unsigned long long base = 0;
-		if (lane == 0) base = atomicAdd(a.ticket, 32ull);
-		base = __shfl_sync(kFullMask, base, 0);
-		if (base >= slots) break;
-		const uint64_t slot = base + lane;
-		const uint32_t tile = (uint32_t)(slot >> 5), in = (uint32_t)(slot & 31u);
-		const uint32_t x = (tile % tiles_x) * 8u + (in & 7u), y = (tile / tiles_x) * 4u + (in >> 3);
-		if (x < a.width && y < a.height) pt_pixel<LIGHT, kMarchTPB>(a, x, y, spp, s0x, s0y, stack);
+	const float fs = (float)spp, fn = (float)(spp + 1u);
+	const size_t npx = (size_t)a.width * a.height;
+	for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < npx; p += (size_t)gridDim.x * blockDim.x) {
+		const PathState &S = a.paths[p];
+		float dnrm[3];
+		nrm_decode(S.first_nrm, dnrm);
+		const float4 c = a.color[p];
+		a.color[p] = make_float4((c.x * fs + S.rad[0]) / fn, (c.y * fs + S.rad[1]) / fn, (c.z * fs + S.rad[2]) / fn, 1.0f);
+		const uint32_t wa = a.albedo[p], wn = a.normal[p];
+		uint32_t oa = 255u << 24, on = 127u << 24;
+#pragma unroll
+		for (int k = 0; k < 3; ++k) {
+			oa |= unorm8_store((unorm8_load(wa, k) * fs + S.dalb[k]) / fn) << (8 * k);
+			on |= snorm8_store((snorm8_load(wn, k) * fs + dnrm[k]) / fn) << (8 * k);
+		}
+		a.albedo[p] = oa;
+		a.normal[p] = on;
 	}
 }
 
@@ -1221,16 +1287,25 @@ cudaError_t occlude_launch(const MarchArgs &a, uint32_t *occluded, cudaStream_t 
 }
 
 cudaError_t pt_render_launch(const PtArgs &a, cudaStream_t stream) {
-	cudaError_t e = cudaMemsetAsync(a.ticket, 0, sizeof(unsigned long long), stream);
+	// tickets and queue counts of every vertex start at zero
+	cudaError_t e = cudaMemsetAsync(a.tickets, 0, kPtScratchBytes, stream);
 	if (e != cudaSuccess || a.width == 0 || a.height == 0) return e;
 	const int sms = device_sm_count();
 	const uint64_t slots = (uint64_t)((a.width + 7u) / 8u) * ((a.height + 3u) / 4u) * 32u;
 	const uint64_t blocks_needed = (slots / 32 + kMarchTPB / 32 - 1) / (kMarchTPB / 32);
 	const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(blocks_needed, (uint64_t)sms * 16));
-	if (a.light_type == 1)
-		SVO_LAUNCH("pt_envmap", stream, pt_kernel<1><<<blocks, kMarchTPB, 0, stream>>>(a););
-	else
-		SVO_LAUNCH("pt_const", stream, pt_kernel<0><<<blocks, kMarchTPB, 0, stream>>>(a););
+	if (a.light_type == 1) {
+		SVO_LAUNCH("pt_primary", stream, pt_primary_kernel<1><<<blocks, kMarchTPB, 0, stream>>>(a););
+		for (uint32_t cur = 1; cur < a.bounce; ++cur)
+			SVO_LAUNCH("pt_bounce", stream, pt_bounce_kernel<1><<<blocks, kMarchTPB, 0, stream>>>(a, cur););
+	} else {
+		SVO_LAUNCH("pt_primary", stream, pt_primary_kernel<0><<<blocks, kMarchTPB, 0, stream>>>(a););
+		for (uint32_t cur = 1; cur < a.bounce; ++cur)
+			SVO_LAUNCH("pt_bounce", stream, pt_bounce_kernel<0><<<blocks, kMarchTPB, 0, stream>>>(a, cur););
+	}
+	const uint64_t npx = (uint64_t)a.width * a.height;
+	const uint32_t ablocks = (uint32_t)std::min<uint64_t>((npx + 255) / 256, (uint64_t)sms * 8);
+	SVO_LAUNCH("pt_accumulate", stream, pt_accumulate_kernel<<<ablocks, 256, 0, stream>>>(a););
 	return cudaGetLastError();
 }
 

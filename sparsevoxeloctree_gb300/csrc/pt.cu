@@ -24,7 +24,10 @@ struct svo_path_tracer {
 	uint32_t *sobol = nullptr;    // kSobolWords: dimension values, then the sample index
 	uint32_t *matrices = nullptr; // kSobolDims x 32 direction numbers
 	uint8_t *noise = nullptr;     // 256 x 256 x 2
-	unsigned long long *scratch = nullptr; // ticket, status
+	unsigned long long *scratch = nullptr; // [1]: status word
+	svo::PathState *paths = nullptr;       // one per pixel
+	uint32_t *queue = nullptr;             // two queues of width x height path indices
+	unsigned long long *wave = nullptr;    // per-sample tickets and counts (kPtScratchBytes)
 };
 
 namespace svo {
@@ -218,6 +221,9 @@ void svo_path_tracer_destroy(svo_path_tracer *pt) {
 	cudaFree(pt->matrices);
 	cudaFree(pt->noise);
 	cudaFree(pt->scratch);
+	cudaFree(pt->paths);
+	cudaFree(pt->queue);
+	cudaFree(pt->wave);
 	delete pt;
 }
 
@@ -235,10 +241,14 @@ int svo_path_tracer_reset(svo_path_tracer *pt, uint32_t width, uint32_t height, 
 		cudaFree(pt->color);
 		cudaFree(pt->albedo);
 		cudaFree(pt->normal);
-		pt->color = nullptr, pt->albedo = pt->normal = nullptr;
+		cudaFree(pt->paths);
+		cudaFree(pt->queue);
+		pt->color = nullptr, pt->albedo = pt->normal = nullptr, pt->paths = nullptr, pt->queue = nullptr;
 		PT_CK(cudaMalloc(&pt->color, n * sizeof(float4)), "path tracer targets");
 		PT_CK(cudaMalloc(&pt->albedo, n * sizeof(uint32_t)), "path tracer targets");
 		PT_CK(cudaMalloc(&pt->normal, n * sizeof(uint32_t)), "path tracer targets");
+		PT_CK(cudaMalloc(&pt->paths, n * sizeof(PathState)), "path state");
+		PT_CK(cudaMalloc(&pt->queue, 2 * n * sizeof(uint32_t)), "path queues");
 	}
 	pt->width = width, pt->height = height, pt->bounce = bounce, pt->spp = 0;
 	PT_CK(cudaMemsetAsync(pt->color, 0, n * sizeof(float4), s), "path tracer clear");
@@ -270,6 +280,7 @@ int svo_path_tracer_create(uint32_t width, uint32_t height, uint32_t bounce, svo
 	if (e == cudaSuccess) e = cudaMalloc(&pt->matrices, m.size() * sizeof(uint32_t));
 	if (e == cudaSuccess) e = cudaMalloc(&pt->noise, noise.size());
 	if (e == cudaSuccess) e = cudaMalloc(&pt->scratch, 2 * sizeof(unsigned long long));
+	if (e == cudaSuccess) e = cudaMalloc(&pt->wave, kPtScratchBytes);
 	if (e == cudaSuccess) e = cudaMemcpy(pt->matrices, m.data(), m.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
 	if (e == cudaSuccess) e = cudaMemcpy(pt->noise, noise.data(), noise.size(), cudaMemcpyHostToDevice);
 	if (e != cudaSuccess) {
@@ -330,7 +341,11 @@ int svo_path_tracer_render(svo_path_tracer *pt, const svo_octree *o, const svo_c
 	a.sobol = pt->sobol;
 	a.noise = pt->noise;
 	a.color = pt->color, a.albedo = pt->albedo, a.normal = pt->normal;
-	a.ticket = pt->scratch;
+	a.paths = pt->paths;
+	a.queue[0] = pt->queue;
+	a.queue[1] = pt->queue + (size_t)pt->width * pt->height;
+	a.tickets = pt->wave;
+	a.counts = reinterpret_cast<uint32_t *>(pt->wave + kPtMaxVertices);
 	a.status = reinterpret_cast<uint32_t *>(pt->scratch + 1);
 	for (uint32_t i = 0; i < samples; ++i) {
 		PT_CK(pt_render_launch(a, s), "path tracer render");

@@ -288,6 +288,16 @@ struct EnvMapView {
 	const uint2 *alias;
 	uint32_t width, height;
 };
+// A path between the wavefront launches of one sample: throughput, radiance, current vertex (position,
+// normal code: axis | negative << 2), and the first hit's albedo and normal code (kPathNoNormal: none).
+constexpr uint32_t kPathNoNormal = 0xffu;
+struct PathState {
+	float acc[3], rad[3], pos[3], dalb[3];
+	uint32_t nrm, first_nrm;
+};
+// Tickets (one per launch of a sample) and surviving-path counts (one per vertex), zeroed per sample.
+constexpr uint32_t kPtMaxVertices = 32;
+constexpr size_t kPtScratchBytes = kPtMaxVertices * sizeof(unsigned long long) + (kPtMaxVertices + 1) * sizeof(uint32_t);
 struct PtArgs {
 	const uint32_t *pool;
 	uint32_t range, level;
@@ -303,7 +313,10 @@ struct PtArgs {
 	float4 *color;         // accumulated radiance (rgba32f)
 	uint32_t *albedo;      // accumulated first-hit albedo (rgba8 unorm)
 	uint32_t *normal;      // accumulated first-hit normal (rgba8 snorm)
-	unsigned long long *ticket;
+	PathState *paths;      // one per pixel
+	uint32_t *queue[2];    // surviving paths of the current / next vertex
+	unsigned long long *tickets; // kPtScratchBytes: tickets[kPtMaxVertices], then counts[kPtMaxVertices + 1]
+	uint32_t *counts;
 	uint32_t *status;
 };
 cudaError_t pt_render_launch(const PtArgs &a, cudaStream_t stream);
