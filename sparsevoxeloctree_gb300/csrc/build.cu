@@ -1088,6 +1088,48 @@ void build_workspace_layout(void *ws, uint32_t count, uint32_t level, uint64_t c
 	w.total_bytes = off;
 }
 
+// A fork of the caller's stream onto a second stream of the calling thread (one per thread and device,
+// so concurrent callers and stream captures never share it) and back, with events made per call.  When
+// a stream or event cannot be had, every "side" launch runs on the caller's stream instead.
+class SideFork {
+public:
+	explicit SideFork(cudaStream_t main) : main_(main) {
+		thread_local cudaStream_t side = nullptr;
+		thread_local int side_dev = -1;
+		int dev = 0;
+		if (cudaGetDevice(&dev) != cudaSuccess) return;
+		if (!side || side_dev != dev) {
+			if (cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking) != cudaSuccess) {
+				side = nullptr;
+				return;
+			}
+			side_dev = dev;
+		}
+		for (cudaEvent_t &e : ev_)
+			if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return;
+		if (cudaEventRecord(ev_[2], main_) != cudaSuccess || cudaStreamWaitEvent(side, ev_[2], 0) != cudaSuccess) return;
+		side_ = side;
+	}
+	~SideFork() {
+		for (cudaEvent_t e : ev_)
+			if (e) cudaEventDestroy(e);
+	}
+	cudaStream_t side() const { return side_ ? side_ : main_; }
+	void mark_side(int k) {
+		if (side_) cudaEventRecord(ev_[k], side_);
+	}
+	void main_waits(int k) {
+		if (side_) cudaStreamWaitEvent(main_, ev_[k], 0);
+	}
+	void side_waits_main() {
+		if (side_ && cudaEventRecord(ev_[3], main_) == cudaSuccess) cudaStreamWaitEvent(side_, ev_[3], 0);
+	}
+
+private:
+	cudaStream_t main_, side_ = nullptr;
+	cudaEvent_t ev_[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+
 static uint32_t grid_for(uint64_t items, uint32_t per_block, uint32_t cap) {
 	const uint64_t b = (items + per_block - 1) / per_block;
 	return (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(b, cap));
@@ -1136,9 +1178,15 @@ static void launch_dense_and_scatter(const uint64_t *frags, uint64_t n, uint32_t
 	SVO_LAUNCH("build_init", stream, build_init<B><<<M, 256, 0, stream>>>(bb, gstate););
 	SVO_LAUNCH("dense_mark", stream,
 	           dense_mark<B><<<grid_for(n, kTPB * kSweepRuns, sweep), kTPB, 0, stream>>>(frags, n, bb, bcount););
-	SVO_LAUNCH("bucket_scan", stream,
-	           bucket_scan<<<(nb_total + kScanTile - 1) / kScanTile, kTPB, 0, stream>>>(bcount, nb_total, boff, blist,
-	                                                                                   gstate, bdescs););
+	// Two independent chains after the sweep: the bucket scan (then, once the dense prefix is final, the
+	// interior words) on a second stream, the dense reduce / scan on the caller's stream; the bucketed
+	// copy needs the bucket offsets and the dense prefix, and the caller's later work waits for both.
+	SideFork fork(stream);
+	cudaStream_t aux = fork.side();
+	SVO_LAUNCH("bucket_scan", aux,
+	           bucket_scan<<<(nb_total + kScanTile - 1) / kScanTile, kTPB, 0, aux>>>(bcount, nb_total, boff, blist,
+	                                                                                gstate, bdescs););
+	fork.mark_side(0);
 	if (maxD >= 1) {
 		for (uint32_t d = maxD - 1; d >= 1; --d) {
 			const dim3 grid(grid_for(dense_words_of(d), kTPB, (uint32_t)sms * 8), M);
@@ -1148,14 +1196,18 @@ static void launch_dense_and_scatter(const uint64_t *frags, uint64_t n, uint32_t
 		           dense_scan<B><<<grid_for(dense_words, kDenseTile, (uint32_t)sms * 4), kTPB, 0, stream>>>(
 		               bb, dense_words, gstate, descs););
 		SVO_LAUNCH("dense_finish", stream, dense_finish<B><<<(M + 127) / 128, 128, 0, stream>>>(bb););
-		SVO_LAUNCH("dense_write", stream,
-		           dense_write<B><<<grid_for(items_total, kTPB, (uint32_t)sms * 16), kTPB, 0, stream>>>(bb, items_total););
+		fork.side_waits_main();
+		SVO_LAUNCH("dense_write", aux,
+		           dense_write<B><<<grid_for(items_total, kTPB, (uint32_t)sms * 16), kTPB, 0, aux>>>(bb, items_total););
 	}
+	fork.mark_side(1);
+	fork.main_waits(0); // bucket offsets
 	// the bucketed copy: leaf items when the leaf parents are dense (their bitmap is final now), fragments
 	// for the sparse levels otherwise
 	SVO_LAUNCH("bucket_scatter", stream,
 	           bucket_scatter<B><<<grid_for(n, kTPB * kScatterRuns, sweep), kTPB, 0, stream>>>(frags, n, bb, boff, bfill,
 	                                                                                      sorted););
+	fork.main_waits(1); // interior words
 }
 
 static void launch_sparse(const uint64_t *sorted, uint32_t count, uint32_t level, const DenseView &dv, uint32_t *pool,
