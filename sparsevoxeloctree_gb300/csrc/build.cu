@@ -229,28 +229,73 @@ __global__ void __launch_bounds__(kTPB) dense_mark(const uint64_t *__restrict__ 
 	}
 }
 
-// bitmap of depth d from depth d+1: bit p = (byte p of the child bitmap != 0).  blockIdx.y = mesh.
-template <bool B> __global__ void dense_reduce(BuildBatch bb, uint32_t d) {
+// Bitmaps of depths D-1 .. 1 from depth D in one launch (bit p of depth d = byte p of depth d+1 is
+// nonzero).  Block b reduces chunk b (kReduceChunk words) of depth D level by level in shared memory:
+// the words of a level that the chunk covers whole are written directly, and once the chunk's image is
+// smaller than a word its bits are ORed into place (atomicOr), so higher levels collect every chunk's
+// contribution.  The bitmaps were zeroed before the build.  blockIdx.y = mesh.
+constexpr uint32_t kReduceChunk = 2048;
+
+SVO_DEV uint32_t byte_bits(uint32_t v) { // bit j = byte j of v is nonzero
+	return (uint32_t)((v & 0xffu) != 0u) | ((uint32_t)((v & 0xff00u) != 0u) << 1) |
+	       ((uint32_t)((v & 0xff0000u) != 0u) << 2) | ((uint32_t)((v & 0xff000000u) != 0u) << 3);
+}
+
+template <bool B> __global__ void __launch_bounds__(256) dense_reduce(BuildBatch bb) {
+	__shared__ uint32_t s_buf[2][kReduceChunk / 8];
 	const DenseView dv = mesh_at<B>(bb, blockIdx.y).dv;
-	if (dv.D < d + 1) return;
-	const uint32_t nbits = 1u << (3 * d);
-	const uint32_t nwords = (nbits + 31) / 32;
-	const uint8_t *child = reinterpret_cast<const uint8_t *>(dv.bits + dv.off[d + 1]);
-	uint32_t *parent = dv.bits + dv.off[d];
-	for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < nwords; w += gridDim.x * blockDim.x) {
-		uint32_t out = 0;
-		if (nbits >= 32) {
-			const uint4 *c = reinterpret_cast<const uint4 *>(child + 32 * (size_t)w);
-			const uint4 a = c[0], b = c[1];
-			const uint32_t v[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+	const uint32_t D = dv.D;
+	if (D < 2) return;
+	const uint32_t words_D = (1u << (3 * D)) / 32u; // D >= 2: at least 2 words
+	const uint32_t chunk = min(words_D, kReduceChunk);
+	const uint32_t first = blockIdx.x * chunk;
+	if (first >= words_D) return;
+	uint32_t nbits = chunk * 32u, bit0 = first * 32u; // the chunk's image at the current level
+	const uint32_t *src = dv.bits + dv.off[D] + first;
+	bool src_shared = false;
+	int cur = 0;
+	for (uint32_t c = D; c >= 2; --c) {
+		uint32_t *parent = dv.bits + dv.off[c - 1];
+		const uint32_t nb_out = nbits / 8u, out0 = bit0 / 8u;
+		if (nb_out >= 32u) { // whole words, owned by this block
+			const uint32_t nw = nb_out / 32u;
+			for (uint32_t w = threadIdx.x; w < nw; w += blockDim.x) {
+				uint32_t out = 0;
+				if (src_shared) {
 #pragma unroll
-			for (int i = 0; i < 8; ++i)
+					for (int i = 0; i < 8; ++i) out |= byte_bits(src[8 * w + i]) << (4 * i);
+				} else {
+					const uint4 *c4 = reinterpret_cast<const uint4 *>(src + 8 * w);
+					const uint4 p = c4[0], q = c4[1];
+					const uint32_t v[8] = {p.x, p.y, p.z, p.w, q.x, q.y, q.z, q.w};
 #pragma unroll
-				for (int j = 0; j < 4; ++j) out |= (uint32_t)(((v[i] >> (8 * j)) & 0xffu) != 0u) << (4 * i + j);
-		} else {
-			for (uint32_t p = 0; p < nbits; ++p) out |= (uint32_t)(child[p] != 0) << p;
+					for (int i = 0; i < 8; ++i) out |= byte_bits(v[i]) << (4 * i);
+				}
+				parent[out0 / 32u + w] = out;
+				s_buf[cur][w] = out;
+			}
+		} else { // fewer than 32 bits: OR them into the parent word
+			if (threadIdx.x == 0) {
+				uint32_t out = 0;
+				for (uint32_t p = 0; p < nb_out; ++p) out |= (uint32_t)(((src[p >> 2] >> (8 * (p & 3u))) & 0xffu) != 0u) << p;
+				if (out) atomicOr(parent + out0 / 32u, out << (out0 % 32u));
+				s_buf[cur][0] = out;
+			}
 		}
-		parent[w] = out;
+		__syncthreads();
+		src = s_buf[cur];
+		src_shared = true;
+		cur ^= 1;
+		nbits = nb_out, bit0 = out0;
+		if (nbits < 8u) { // the chunk's image is one bit or less: it ORs one bit into each level above
+			const bool any = s_buf[cur ^ 1][0] != 0u;
+			if (threadIdx.x == 0 && any)
+				for (uint32_t d = c - 2; d >= 1; --d) {
+					bit0 /= 8u;
+					atomicOr(dv.bits + dv.off[d] + bit0 / 32u, 1u << (bit0 % 32u));
+				}
+			return;
+		}
 	}
 }
 
@@ -1188,9 +1233,10 @@ static void launch_dense_and_scatter(const uint64_t *frags, uint64_t n, uint32_t
 	                                                                                gstate, bdescs););
 	fork.mark_side(0);
 	if (maxD >= 1) {
-		for (uint32_t d = maxD - 1; d >= 1; --d) {
-			const dim3 grid(grid_for(dense_words_of(d), kTPB, (uint32_t)sms * 8), M);
-			SVO_LAUNCH("dense_reduce", stream, dense_reduce<B><<<grid, kTPB, 0, stream>>>(bb, d););
+		if (maxD >= 2) {
+			const uint32_t words_D = (1u << (3 * maxD)) / 32u;
+			const dim3 grid((words_D + kReduceChunk - 1) / kReduceChunk, M);
+			SVO_LAUNCH("dense_reduce", stream, dense_reduce<B><<<grid, 256, 0, stream>>>(bb););
 		}
 		SVO_LAUNCH("dense_scan", stream,
 		           dense_scan<B><<<grid_for(dense_words, kDenseTile, (uint32_t)sms * 4), kTPB, 0, stream>>>(
