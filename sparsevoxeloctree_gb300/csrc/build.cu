@@ -1133,48 +1133,6 @@ void build_workspace_layout(void *ws, uint32_t count, uint32_t level, uint64_t c
 	w.total_bytes = off;
 }
 
-// A fork of the caller's stream onto a second stream of the calling thread (one per thread and device,
-// so concurrent callers and stream captures never share it) and back, with events made per call.  When
-// a stream or event cannot be had, every "side" launch runs on the caller's stream instead.
-class SideFork {
-public:
-	explicit SideFork(cudaStream_t main) : main_(main) {
-		thread_local cudaStream_t side = nullptr;
-		thread_local int side_dev = -1;
-		int dev = 0;
-		if (cudaGetDevice(&dev) != cudaSuccess) return;
-		if (!side || side_dev != dev) {
-			if (cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking) != cudaSuccess) {
-				side = nullptr;
-				return;
-			}
-			side_dev = dev;
-		}
-		for (cudaEvent_t &e : ev_)
-			if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return;
-		if (cudaEventRecord(ev_[2], main_) != cudaSuccess || cudaStreamWaitEvent(side, ev_[2], 0) != cudaSuccess) return;
-		side_ = side;
-	}
-	~SideFork() {
-		for (cudaEvent_t e : ev_)
-			if (e) cudaEventDestroy(e);
-	}
-	cudaStream_t side() const { return side_ ? side_ : main_; }
-	void mark_side(int k) {
-		if (side_) cudaEventRecord(ev_[k], side_);
-	}
-	void main_waits(int k) {
-		if (side_) cudaStreamWaitEvent(main_, ev_[k], 0);
-	}
-	void side_waits_main() {
-		if (side_ && cudaEventRecord(ev_[3], main_) == cudaSuccess) cudaStreamWaitEvent(side_, ev_[3], 0);
-	}
-
-private:
-	cudaStream_t main_, side_ = nullptr;
-	cudaEvent_t ev_[4] = {nullptr, nullptr, nullptr, nullptr};
-};
-
 static uint32_t grid_for(uint64_t items, uint32_t per_block, uint32_t cap) {
 	const uint64_t b = (items + per_block - 1) / per_block;
 	return (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(b, cap));

@@ -40,6 +40,50 @@ struct ProfScope {
 	} while (0)
 int device_sm_count();   // SMs of the current device (cached per device)
 
+// A fork of the caller's stream onto a second stream of the calling thread (one per thread and device,
+// so concurrent callers and stream captures never share it) and back, with events made per call.  When
+// a stream or event cannot be had, every "side" launch runs on the caller's stream instead.
+class SideFork {
+public:
+	explicit SideFork(cudaStream_t main, bool enabled = true) : main_(main) {
+		if (!enabled) return;
+		thread_local cudaStream_t side = nullptr;
+		thread_local int side_dev = -1;
+		int dev = 0;
+		if (cudaGetDevice(&dev) != cudaSuccess) return;
+		if (!side || side_dev != dev) {
+			if (cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking) != cudaSuccess) {
+				side = nullptr;
+				return;
+			}
+			side_dev = dev;
+		}
+		for (cudaEvent_t &e : ev_)
+			if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return;
+		if (cudaEventRecord(ev_[2], main_) != cudaSuccess || cudaStreamWaitEvent(side, ev_[2], 0) != cudaSuccess) return;
+		side_ = side;
+	}
+	~SideFork() {
+		for (cudaEvent_t e : ev_)
+			if (e) cudaEventDestroy(e);
+	}
+	cudaStream_t side() const { return side_ ? side_ : main_; }
+	void mark_side(int k) {
+		if (side_) cudaEventRecord(ev_[k], side_);
+	}
+	void main_waits(int k) {
+		if (side_) cudaStreamWaitEvent(main_, ev_[k], 0);
+	}
+	void side_waits_main() {
+		if (side_ && cudaEventRecord(ev_[3], main_) == cudaSuccess) cudaStreamWaitEvent(side_, ev_[3], 0);
+	}
+
+private:
+	cudaStream_t main_, side_ = nullptr;
+	cudaEvent_t ev_[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+
+
 // Launch parameters set by the autotuner (svo_tune_set), per (level, size class of the launch's work).
 enum : uint32_t {
 	kTuneMarchBlock = 0,   // threads per march block: 64, 128, 256
