@@ -1,7 +1,8 @@
 // pt.cu — host side of the path tracer (PathTracer, src/PathTracer.{hpp,cpp}): the environment-map
 // tables (EnvironmentMap::weigh_hdr_image / generate_alias_table, src/EnvironmentMap.cpp:81-160), the
 // Sobol state and direction numbers (Sobol, src/Sobol.cpp; shader/sobol.comp), the accumulation targets
-// and the C ABI.  The per-pixel path is march.cu's pt_kernel.
+// and the C ABI.  The per-pixel paths are march.cu's wavefront kernels (pt_primary_kernel,
+// pt_bounce_kernel, pt_accumulate_kernel).
 #include <cmath>
 #include <cstdio>
 #include <cstring>
