@@ -398,25 +398,87 @@ __global__ void __launch_bounds__(kTPB) vox_unit_scan(VoxBatch vb, uint32_t n, V
 	if (ntiles == 0 && blockIdx.x == 0 && threadIdx.x == 0) w.unit_frag[0] = 0;
 }
 
-// Emission of small triangles: one lane per triangle, its fragments in order at its offset.
+// Emission of small triangles, 32 consecutive triangles per warp.  Each lane sets up its triangle
+// and records, in shared memory, the packing record and the start and covered length of each of its
+// spans (a small triangle has at most kSmallArea spans and fragments); then the warp writes the group's
+// fragments together: lane k takes fragments k, k+32, ... of the group (contiguous in the list: the
+// small fragments are in triangle order), finds its triangle and span and packs the fragment.  A lane
+// never waits for a large triangle's fragments, and every store instruction covers 256 contiguous bytes.
 // In a batch, mesh m's small fragments move up by its shift (the large fragments of earlier meshes).
+constexpr int kEmitTPB = 128;
+
+struct SmallRec {
+	int64_t K, NU, NV, D; // plane depth numerator / denominator (make_fragment)
+	uint64_t off;         // output position of the triangle's first fragment
+	int32_t z0, z1, v0, level;
+	uint32_t axis, cols, rgb, cnt;
+};
+
 template <bool B>
-__global__ void __launch_bounds__(kTPB) vox_emit(VoxBatch vb, uint32_t n, VoxWorkspace w, uint64_t *__restrict__ frags,
-                                                 uint64_t capacity) {
-	for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-		uint64_t off = w.small_off[i], end = w.small_off[i + 1];
-		if (end == off) continue;
-		const svo_triangle *tp;
-		uint32_t local, lvl, mi;
-		tri_of<B>(vb, (uint32_t)i, tp, local, lvl, mi);
-		if (B) {
-			const uint64_t sh = vb.shifts[2 * mi];
-			off += sh, end += sh;
+__global__ void __launch_bounds__(kEmitTPB) vox_emit(VoxBatch vb, uint32_t n, VoxWorkspace w, uint64_t *__restrict__ frags,
+                                                     uint64_t capacity) {
+	__shared__ SmallRec s_rec[kEmitTPB];
+	__shared__ uint8_t s_cum[kEmitTPB][kSmallArea + 1];
+	__shared__ int16_t s_lo[kEmitTPB][kSmallArea];
+	__shared__ uint32_t s_incl[kEmitTPB];
+	const uint32_t lane = lane_id(), wb = threadIdx.x & ~31u;
+	const uint64_t warps = (uint64_t)gridDim.x * blockDim.x / 32;
+	for (uint64_t g = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32; g * 32 < n; g += warps) {
+		const uint64_t t = g * 32 + lane;
+		uint32_t cnt = 0;
+		if (t < n) {
+			uint64_t off = w.small_off[t];
+			cnt = (uint32_t)(w.small_off[t + 1] - off);
+			if (cnt) {
+				const svo_triangle *tp;
+				uint32_t local, lvl, mi;
+				tri_of<B>(vb, (uint32_t)t, tp, local, lvl, mi);
+				if (B) off += vb.shifts[2 * mi];
+				TriSetup S;
+				tri_setup(tp, local, lvl, S);
+				if (!S.valid || is_large(S) || off + cnt > capacity) {
+					cnt = 0;
+				} else {
+					SmallRec &r = s_rec[threadIdx.x];
+					r.K = S.K, r.NU = S.NU, r.NV = S.NV, r.D = S.D, r.off = off;
+					r.z0 = S.z0, r.z1 = S.z1, r.v0 = S.v0, r.level = S.level;
+					r.axis = (uint32_t)S.axis, r.cols = (uint32_t)S.cols, r.rgb = S.rgb, r.cnt = cnt;
+					uint32_t acc = 0;
+					const int32_t nspans = S.v1 - S.v0 + 1;
+					for (int32_t k = 0; k < nspans; ++k) {
+						int32_t lo, hi;
+						span_interval(S, S.v0 + k, lo, hi);
+						s_cum[threadIdx.x][k] = (uint8_t)acc;
+						s_lo[threadIdx.x][k] = (int16_t)lo;
+						acc += hi >= lo ? (uint32_t)(hi - lo + 1) : 0u;
+					}
+					s_cum[threadIdx.x][nspans] = (uint8_t)acc;
+					if (acc != cnt) cnt = 0; // cannot happen: the count pass walked the same spans
+					r.cnt = cnt;
+					// spans past the last one read as "no more fragments"
+					for (int32_t k = nspans + 1; k <= kSmallArea; ++k) s_cum[threadIdx.x][k] = 0xffu;
+				}
+			}
 		}
-		if (end > capacity) continue;
-		TriSetup s;
-		tri_setup(tp, local, lvl, s);
-		if (s.valid && !is_large(s)) emit_serial(s, frags + off);
+		const uint32_t incl = warp_inclusive_sum(cnt);
+		const uint32_t total = __shfl_sync(kFullMask, incl, 31);
+		s_incl[threadIdx.x] = incl;
+		__syncwarp();
+		uint32_t j = 0;
+		for (uint32_t f = lane; f < total; f += 32) {
+			while (s_incl[wb + j] <= f) ++j;
+			const uint32_t tj = wb + j;
+			const SmallRec &r = s_rec[tj];
+			const uint32_t q = f - (s_incl[tj] - r.cnt);
+			uint32_t k = 0;
+			while (s_cum[tj][k + 1] <= q) ++k; // the span holding fragment q (empty spans are skipped)
+			TriSetup S;
+			S.K = r.K, S.NU = r.NU, S.NV = r.NV, S.D = r.D;
+			S.z0 = r.z0, S.z1 = r.z1, S.level = r.level, S.axis = (int32_t)r.axis, S.cols = (int32_t)r.cols, S.rgb = r.rgb;
+			const int32_t u = (int32_t)s_lo[tj][k] + (int32_t)(q - s_cum[tj][k]), v = r.v0 + (int32_t)k;
+			frags[r.off + q] = make_fragment(S, u, v);
+		}
+		__syncwarp();
 	}
 }
 
@@ -622,7 +684,8 @@ static void launch_emit(const VoxBatch &vb, uint32_t n, uint32_t tune_level, con
                         uint64_t capacity, cudaStream_t stream) {
 	const int sms = device_sm_count();
 	const uint32_t per_sm = (uint32_t)tune_value(kTuneEmitBlocks, tune_level, n);
-	SVO_LAUNCH("vox_emit", stream, vox_emit<B><<<(uint32_t)sms * per_sm, kTPB, 0, stream>>>(vb, n, w, frags, capacity););
+	SVO_LAUNCH("vox_emit", stream,
+	           vox_emit<B><<<(uint32_t)sms * per_sm * (kTPB / kEmitTPB), kEmitTPB, 0, stream>>>(vb, n, w, frags, capacity););
 	SVO_LAUNCH("vox_emit_units", stream,
 	           vox_emit_units<B><<<(uint32_t)sms * std::max(1u, per_sm / 2), kTPB, 0, stream>>>(vb, n, w, frags, capacity););
 }
