@@ -6,7 +6,8 @@ values on a real workload with CUDA events and sets the fastest:
 
   march   threads per block (64 / 128 / 256) x rays per lane per ticket (1 / 2, or persistent refill) x
           stack in shared or local memory, exhaustively (18 variants), on the workload's ray launch;
-  build   blocks per SM of the fragment sweeps x blocks per SM of the leaf stage, on a build;
+  build   blocks per SM of the fragment sweeps x blocks per SM of the leaf stage x one or two streams
+          for the bucket / dense stages, on a build;
   emit    blocks per SM of the voxelizer's emission, on a voxelize pass.
 
 The resulting table (parameter -> {"level:size_class": value}) is what `save` writes and `load` applies,
@@ -30,6 +31,7 @@ PARAMS = {  # name -> (parameter id, candidate values)
     "sweep_blocks": (3, (8, 16, 32)),
     "leaf_blocks": (4, (4, 6, 8)),
     "emit_blocks": (5, (8, 16, 32)),
+    "build_streams": (6, (2, 1)),
 }
 
 
@@ -88,7 +90,8 @@ def tune_march(tracer, hits=None, reps: int = 3) -> dict:
 
 def tune_build(builder, reps: int = 3) -> dict:
     """builder: api.OctreeBuilder; tunes the fragment sweeps and the leaf stage of its build."""
-    return _sweep(["sweep_blocks", "leaf_blocks"], builder.GetLevel(), builder.m_count, builder.CmdBuild, reps)
+    return _sweep(["sweep_blocks", "leaf_blocks", "build_streams"], builder.GetLevel(), builder.m_count,
+                  builder.CmdBuild, reps)
 
 
 def tune_voxelize(voxelizer, reps: int = 3) -> dict:
@@ -100,7 +103,8 @@ def tune_batch(batcher, meshes, fragments: int, triangles: int, reps: int = 2) -
     """batcher: api.BatchBuilder with `meshes` built once; tunes sweeps, leaf stage and emission at the
     batch's deepest level (the level its launches select their parameters by)."""
     level = max(lv for _, lv in meshes)
-    out = {"build": _sweep(["sweep_blocks", "leaf_blocks"], level, fragments, lambda: batcher.Build(meshes), reps)}
+    out = {"build": _sweep(["sweep_blocks", "leaf_blocks", "build_streams"], level, fragments,
+                           lambda: batcher.Build(meshes), reps)}
     out["emit"] = _sweep(["emit_blocks"], level, triangles, lambda: batcher.Build(meshes), reps)
     return out
 

@@ -1184,7 +1184,7 @@ static void launch_dense_and_scatter(const uint64_t *frags, uint64_t n, uint32_t
 	// Two independent chains after the sweep: the bucket scan (then, once the dense prefix is final, the
 	// interior words) on a second stream, the dense reduce / scan on the caller's stream; the bucketed
 	// copy needs the bucket offsets and the dense prefix, and the caller's later work waits for both.
-	SideFork fork(stream);
+	SideFork fork(stream, tune_value(kTuneBuildStreams, tune_level, n) == 2);
 	cudaStream_t aux = fork.side();
 	SVO_LAUNCH("bucket_scan", aux,
 	           bucket_scan<<<(nb_total + kScanTile - 1) / kScanTile, kTPB, 0, aux>>>(bcount, nb_total, boff, blist,

@@ -92,7 +92,8 @@ enum : uint32_t {
 	kTuneSweepBlocks = 3,  // blocks per SM of the fragment sweeps
 	kTuneLeafBlocks = 4,   // blocks per SM of the leaf stage
 	kTuneEmitBlocks = 5,   // blocks per SM of the voxelizer's emission
-	kTuneParams = 6
+	kTuneBuildStreams = 6, // streams of the build's bucket / dense stages: 1, or 2 (a second stream overlaps them)
+	kTuneParams = 7
 };
 int tune_value(uint32_t param, uint32_t level, uint64_t items);
 
