@@ -963,85 +963,123 @@ __global__ void __launch_bounds__(kMarchTPB) pt_primary_kernel(PtArgs a) {
 	}
 }
 
-// Path vertex `cur` (1 <= cur < bounce) of every path alive at it: the loop body of
-// ConstColorPathTrace / EnvMapPathTrace (light sample with its shadow march, diffuse bounce, leaf march).
+// Path vertex `cur` with lanes refilled: a lane takes the next queued path as soon as its work on the
+// current one ends (idle lanes claim together once kRefillMin of them are idle, or all are), so a warp
+// does not wait for its longest incoherent ray.  A lane's path vertex is up to two marches: the shadow
+// ray of the environment light's sample (Octree_RayMarchOcclude is the 5-argument leaf march without
+// its outputs, shader/octree.glsl:504-629, so the same stepper serves it), then the bounce ray.  Per
+// path the arithmetic is the loop body of ConstColorPathTrace / EnvMapPathTrace
+// (shader/path_tracer.comp:41-58, 70-105): light sample with its shadow march, diffuse bounce, leaf march.
 template <uint32_t LIGHT>
-__global__ void __launch_bounds__(kMarchTPB) pt_bounce_kernel(PtArgs a, uint32_t cur) {
+__global__ void __launch_bounds__(kMarchTPB) pt_bounce_refill_kernel(PtArgs a, uint32_t cur) {
 	__shared__ uint32_t s_stack[SVO_LEVEL_MAX * kMarchTPB];
 	uint32_t *stack = s_stack + threadIdx.x;
-	const uint32_t lane = lane_id();
+	const uint32_t lane = lane_id(), lt_mask = (1u << lane) - 1u;
 	const uint32_t n = a.counts[cur];
 	const uint32_t *qin = a.queue[cur & 1u];
 	uint32_t *qout = a.queue[(cur + 1u) & 1u];
 	const float sx = sobol_f(__ldg(a.sobol + 2 * cur)), sy = sobol_f(__ldg(a.sobol + 2 * cur + 1));
+	RayState s;
+	bool active = false, exhausted = false, shadow = false;
+	uint32_t p = 0;
+	float acc[3] = {0.0f, 0.0f, 0.0f}, rad[3] = {0.0f, 0.0f, 0.0f}, o[3] = {0.0f, 0.0f, 0.0f}, db[3] = {0.0f, 0.0f, 0.0f};
+	float light[3] = {0.0f, 0.0f, 0.0f}, light_pdf = 0.0f, ndd = 0.0f, bsdf_pdf = 0.0f;
 	for (;;) {
-		unsigned long long base = 0;
-		if (lane == 0) base = atomicAdd(a.tickets + cur, 32ull);
-		base = __shfl_sync(kFullMask, base, 0);
-		if (base >= n) break;
-		const uint64_t i = base + lane;
+		const uint32_t idle = __ballot_sync(kFullMask, !active);
+		const uint32_t nidle = __popc(idle);
+		if (!exhausted && (nidle >= kRefillMin || idle == kFullMask)) {
+			const uint32_t leader = __ffs(idle) - 1;
+			unsigned long long base = 0;
+			if (lane == leader) base = atomicAdd(a.tickets + cur, (unsigned long long)nidle);
+			base = __shfl_sync(kFullMask, base, leader);
+			if (base + nidle >= n) exhausted = true; // warp-uniform
+			const uint64_t slot = base + __popc(idle & lt_mask);
+			if (!active && slot < n) {
+				p = qin[slot];
+				const uint32_t y = p / a.width, x = p - y * a.width;
+				const PathState &S = a.paths[p];
+				const uint32_t ni = (((y & 255u) << 8) | (x & 255u)) * 2u;
+				float samp[2] = {sx + (float)__ldg(a.noise + ni) / 255.0f, sy + (float)__ldg(a.noise + ni + 1) / 255.0f};
+				samp[0] = samp[0] - floorf(samp[0]);
+				samp[1] = samp[1] - floorf(samp[1]);
+				float nrm[3];
+#pragma unroll
+				for (int k = 0; k < 3; ++k) o[k] = S.pos[k], acc[k] = S.acc[k], rad[k] = S.rad[k];
+				nrm_decode(S.nrm, nrm);
+				shadow = false;
+				float sd[3];
+				if (LIGHT == 1) { // multiple importance sampling, light sample
+					env_sample(a.env, samp[0], samp[1], a.env_rotation, sd, light, light_pdf);
+					ndd = (nrm[0] * sd[0] + nrm[1] * sd[1]) + nrm[2] * sd[2];
+					shadow = ndd > 0.0f && !isnan(light_pdf) && light_pdf > 0.0f;
+				}
+				{ // Diffuse_Sample (shader/diffuse.glsl:7-14) with phi = 2 * PI * samp.y
+					const float r = sqrtf(samp[0]), phi = 2.0f * kPi * samp[1];
+					float sn, cs;
+					sincos_rad(phi, sn, cs);
+					const float dl[3] = {r * cs, r * sn, sqrtf(1.0f - samp[0])};
+					bsdf_pdf = dl[2] / kPi;
+					align_direction(dl, nrm, db);
+				}
+				const float *d = shadow ? sd : db;
+				float dc[3];
+#pragma unroll
+				for (int k = 0; k < 3; ++k) dc[k] = fabsf(d[k]) >= kEps ? d[k] : (d[k] >= 0.0f ? kEps : -kEps);
+				ray_init<kMarchTPB>(s, o, dc, a.level, stack);
+				active = true;
+			}
+		}
+		if (!__any_sync(kFullMask, active)) {
+			if (exhausted) break;
+			continue;
+		}
 		bool alive = false;
-		uint32_t p = 0;
-		if (i < n) {
-			p = qin[i];
-			const uint32_t y = p / a.width, x = p - y * a.width;
-			PathState &S = a.paths[p];
-			const uint32_t ni = (((y & 255u) << 8) | (x & 255u)) * 2u;
-			float samp[2] = {sx + (float)__ldg(a.noise + ni) / 255.0f, sy + (float)__ldg(a.noise + ni + 1) / 255.0f};
-			samp[0] = samp[0] - floorf(samp[0]);
-			samp[1] = samp[1] - floorf(samp[1]);
-			float o[3], acc[3], rad[3], nrm[3], d[3];
+		if (active && ray_step<kMarchTPB>(s, a.pool, a.range, stack, a.status)) {
+			MarchOut m;
+			ray_finish(s, a.level, m);
+			const uint32_t flags = m.voxel_hi >> 16;
+			if (shadow) { // the light sample's contribution unless occluded, then the bounce ray
+				if (!(flags & SVO_HIT_FLAG_HIT)) {
+					const float bp = ndd / kPi;
+					const float w = mis_power(light_pdf, bp);
 #pragma unroll
-			for (int k = 0; k < 3; ++k) o[k] = S.pos[k], acc[k] = S.acc[k], rad[k] = S.rad[k];
-			nrm_decode(S.nrm, nrm);
-			if (LIGHT == 1) { // multiple importance sampling, light sample
-				float ld[3], light[3], light_pdf;
-				env_sample(a.env, samp[0], samp[1], a.env_rotation, ld, light, light_pdf);
-				const float ndd = (nrm[0] * ld[0] + nrm[1] * ld[1]) + nrm[2] * ld[2];
-				if (ndd > 0.0f && !isnan(light_pdf) && light_pdf > 0.0f) {
-					float t, sz;
-					if (!march_traverse<false, kMarchTPB>(a.pool, a.range, a.level, o, ld, 0.0f, 0.0f, stack, t, sz,
-					                                      a.status)) {
-						const float bsdf_pdf = ndd / kPi;
-						const float w = mis_power(light_pdf, bsdf_pdf);
-#pragma unroll
-						for (int k = 0; k < 3; ++k)
-							rad[k] += acc[k] * light[k] * a.env_multiplier * w * ndd * (1.0f / kPi) / light_pdf;
-					}
+					for (int k = 0; k < 3; ++k)
+						rad[k] += acc[k] * light[k] * a.env_multiplier * w * ndd * (1.0f / kPi) / light_pdf;
 				}
-			}
-			// Diffuse_Sample (shader/diffuse.glsl:7-14) with phi = 2 * PI * samp.y as the shader forms it
-			float bsdf_pdf;
-			{
-				const float r = sqrtf(samp[0]), phi = 2.0f * kPi * samp[1];
-				float sn, cs;
-				sincos_rad(phi, sn, cs);
-				const float dl[3] = {r * cs, r * sn, sqrtf(1.0f - samp[0])};
-				bsdf_pdf = dl[2] / kPi;
-				align_direction(dl, nrm, d);
-			}
-			float pos[3], alb[3];
-			if (pt_leaf<kMarchTPB>(a, o, d, stack, pos, alb, nrm)) {
+				shadow = false;
+				float dc[3];
 #pragma unroll
-				for (int k = 0; k < 3; ++k) S.acc[k] = acc[k] * alb[k], S.pos[k] = pos[k];
-				S.nrm = nrm_code(nrm);
-				alive = cur + 1u < a.bounce;
-			} else if (LIGHT == 1) { // multiple importance sampling, bsdf sample
-				// EnvMap_PDF and EnvMap_Radiance read the same filtered texel
-				const float4 env = env_lookup(a.env, d, a.env_rotation);
-				const float light_pdf = env.w / (kTwoPiPi * sqrtf(1.0f - d[1] * d[1]));
-				if (!isnan(light_pdf) && light_pdf > 0.0f) {
-					const float w = mis_power(bsdf_pdf, light_pdf);
-					const float e3[3] = {env.x, env.y, env.z};
-#pragma unroll
-					for (int k = 0; k < 3; ++k) rad[k] += acc[k] * e3[k] * a.env_multiplier * w;
-				}
+				for (int k = 0; k < 3; ++k) dc[k] = fabsf(db[k]) >= kEps ? db[k] : (db[k] >= 0.0f ? kEps : -kEps);
+				ray_init<kMarchTPB>(s, o, dc, a.level, stack);
 			} else {
+				PathState &S = a.paths[p];
+				if (flags & SVO_HIT_FLAG_HIT) {
+					float nrm[3] = {0.0f, 0.0f, 0.0f};
+					nrm[(flags >> 1) & 3u] = (flags & SVO_HIT_NORMAL_NEG) ? -1.0f : 1.0f;
 #pragma unroll
-				for (int k = 0; k < 3; ++k) rad[k] = acc[k] * a.const_color[k];
+					for (int k = 0; k < 3; ++k) {
+						S.acc[k] = acc[k] * ((float)((m.node >> (8 * k)) & 0xffu) * 0.00392156862745098f);
+						S.pos[k] = m.pos[k];
+					}
+					S.nrm = nrm_code(nrm);
+					alive = cur + 1u < a.bounce;
+				} else if (LIGHT == 1) { // multiple importance sampling, bsdf sample
+					const float4 env = env_lookup(a.env, db, a.env_rotation);
+					const float lp = env.w / (kTwoPiPi * sqrtf(1.0f - db[1] * db[1]));
+					if (!isnan(lp) && lp > 0.0f) {
+						const float w = mis_power(bsdf_pdf, lp);
+						const float e3[3] = {env.x, env.y, env.z};
+#pragma unroll
+						for (int k = 0; k < 3; ++k) rad[k] += acc[k] * e3[k] * a.env_multiplier * w;
+					}
+				} else {
+#pragma unroll
+					for (int k = 0; k < 3; ++k) rad[k] = acc[k] * a.const_color[k];
+				}
+#pragma unroll
+				for (int k = 0; k < 3; ++k) S.rad[k] = rad[k];
+				active = false;
 			}
-#pragma unroll
-			for (int k = 0; k < 3; ++k) S.rad[k] = rad[k];
 		}
 		queue_append(alive, p, qout, a.counts + cur + 1);
 	}
@@ -1297,11 +1335,11 @@ cudaError_t pt_render_launch(const PtArgs &a, cudaStream_t stream) {
 	if (a.light_type == 1) {
 		SVO_LAUNCH("pt_primary", stream, pt_primary_kernel<1><<<blocks, kMarchTPB, 0, stream>>>(a););
 		for (uint32_t cur = 1; cur < a.bounce; ++cur)
-			SVO_LAUNCH("pt_bounce", stream, pt_bounce_kernel<1><<<blocks, kMarchTPB, 0, stream>>>(a, cur););
+			SVO_LAUNCH("pt_bounce", stream, pt_bounce_refill_kernel<1><<<blocks, kMarchTPB, 0, stream>>>(a, cur););
 	} else {
 		SVO_LAUNCH("pt_primary", stream, pt_primary_kernel<0><<<blocks, kMarchTPB, 0, stream>>>(a););
 		for (uint32_t cur = 1; cur < a.bounce; ++cur)
-			SVO_LAUNCH("pt_bounce", stream, pt_bounce_kernel<0><<<blocks, kMarchTPB, 0, stream>>>(a, cur););
+			SVO_LAUNCH("pt_bounce", stream, pt_bounce_refill_kernel<0><<<blocks, kMarchTPB, 0, stream>>>(a, cur););
 	}
 	const uint64_t npx = (uint64_t)a.width * a.height;
 	const uint32_t ablocks = (uint32_t)std::min<uint64_t>((npx + 255) / 256, (uint64_t)sms * 8);

@@ -2,7 +2,7 @@
 // tables (EnvironmentMap::weigh_hdr_image / generate_alias_table, src/EnvironmentMap.cpp:81-160), the
 // Sobol state and direction numbers (Sobol, src/Sobol.cpp; shader/sobol.comp), the accumulation targets
 // and the C ABI.  The per-pixel paths are march.cu's wavefront kernels (pt_primary_kernel,
-// pt_bounce_kernel, pt_accumulate_kernel).
+// pt_bounce_refill_kernel, pt_accumulate_kernel).
 #include <cmath>
 #include <cstdio>
 #include <cstring>
