@@ -206,8 +206,8 @@ def engine_arm(args, rank: int, world: int, device) -> dict:
         tuning = {"emit": autotune.tune_voxelize(vox), "build": autotune.tune_build(builder)}
         if scene.bounce:  # primary and bounce launches share a table entry (same level and ray count): tuned together
             tuning["march"] = autotune._sweep(
-                ["march_block", "march_rays_per_lane", "march_stack_shared"], scene.level, n_rays,
-                lambda: (tracer.CmdDrawPipeline(hits), tracer.Trace(bounce_rays, bounce_hits)))
+                ["march_block", "march_rays_per_lane", "march_stack_shared", "march_buffer_rays"], scene.level,
+                n_rays, lambda: (tracer.CmdDrawPipeline(hits), tracer.Trace(bounce_rays, bounce_hits)))
         else:
             tuning["march"] = autotune.tune_march(tracer, hits)
         tuning = {k: {"best": v["best"], "best_ms": v["best_ms"], "level": v["level"], "size_class": v["size_class"],

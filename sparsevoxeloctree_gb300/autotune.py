@@ -5,7 +5,8 @@ every launch reads it (svo_tune_set / svo_tune_get, include/svo.h).  This module
 values on a real workload with CUDA events and sets the fastest:
 
   march   threads per block (64 / 128 / 256) x rays per lane per ticket (1 / 2, or persistent refill) x
-          stack in shared or local memory, exhaustively (18 variants), on the workload's ray launch;
+          stack in shared or local memory, exhaustively (18 variants), on the workload's camera launch
+          (and the rays-per-lane choice of ray-buffer launches when the workload traces bounce rays);
   build   blocks per SM of the fragment sweeps x blocks per SM of the leaf stage x one or two streams
           for the bucket / dense stages, on a build;
   emit    blocks per SM of the voxelizer's emission, on a voxelize pass.
@@ -32,6 +33,7 @@ PARAMS = {  # name -> (parameter id, candidate values)
     "leaf_blocks": (4, (4, 6, 8)),
     "emit_blocks": (5, (8, 16, 32)),
     "build_streams": (6, (2, 1)),
+    "march_buffer_rays": (7, (0, 1, 2)),  # rays per lane for ray-buffer marches (0: persistent refill)
 }
 
 

@@ -111,7 +111,7 @@ int device_sm_count() {
 // ---------------------------------------------------------------- launch-parameter table
 // Entry [param][level][size class]; level 0 is unused (a set with level 0 writes every level).
 constexpr uint32_t kTuneClasses = 8;
-static const int kTuneDefault[kTuneParams] = {128, 1, 1, 16, 6, 16, 2};
+static const int kTuneDefault[kTuneParams] = {128, 1, 1, 16, 6, 16, 2, 0};
 static std::atomic<int> g_tune[kTuneParams][SVO_LEVEL_MAX + 1][kTuneClasses];
 static std::once_flag g_tune_once;
 
@@ -126,7 +126,8 @@ static void tune_init() {
 static bool tune_valid(uint32_t param, int v) {
 	switch (param) {
 	case kTuneMarchBlock: return v == 64 || v == 128 || v == 256;
-	case kTuneMarchRays: return v == 0 || v == 1 || v == 2;
+	case kTuneMarchRays:
+	case kTuneMarchBufferRays: return v == 0 || v == 1 || v == 2;
 	case kTuneMarchShared: return v == 0 || v == 1;
 	case kTuneBuildStreams: return v == 1 || v == 2;
 	default: return v >= 1 && v <= 64;

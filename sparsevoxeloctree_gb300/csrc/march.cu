@@ -1231,7 +1231,8 @@ static void launch_rpl(const MarchArgs &a, int rpl, bool shared, cudaStream_t st
 
 template <bool CAMERA> static void launch_tuned(const MarchArgs &a, cudaStream_t stream) {
 	const int tpb = tune_value(kTuneMarchBlock, a.level, a.n);
-	const int rpl = tune_value(kTuneMarchRays, a.level, a.n);
+	// camera rays and ray buffers (bounce rays, usually incoherent) have their own rays-per-lane choice
+	const int rpl = tune_value(CAMERA ? kTuneMarchRays : kTuneMarchBufferRays, a.level, a.n);
 	const bool shared = tune_value(kTuneMarchShared, a.level, a.n) != 0;
 	if (tpb == 64) launch_rpl<CAMERA, 64>(a, rpl, shared, stream);
 	else if (tpb == 256) launch_rpl<CAMERA, 256>(a, rpl, shared, stream);

@@ -528,7 +528,8 @@ def test_every_march_variant_matches_oracle(cuda):
     rays_dev = api.to_device(rays)
     try:
         for tpb, rpl, shared in itertools.product((64, 128, 256), (0, 1, 2), (0, 1)):
-            for name, v in (("march_block", tpb), ("march_rays_per_lane", rpl), ("march_stack_shared", shared)):
+            for name, v in (("march_block", tpb), ("march_rays_per_lane", rpl), ("march_stack_shared", shared),
+                            ("march_buffer_rays", rpl)):
                 autotune.set_value(name, 0, -1, v)
             tr = api.OctreeTracer.Create(octree, cam, w, h)
             assert_hits_equal(api.hits_numpy(tr.CmdDrawPipeline()), ref_cam)
