@@ -177,8 +177,7 @@ size_t svo_profile_summary(char *buf, size_t cap);
 #define SVO_TUNE_EMIT_BLOCKS 5u         /* blocks per SM of the voxelizer's emission (default 16) */
 #define SVO_TUNE_BUILD_STREAMS 6u       /* streams of the build's bucket and dense stages: 1, or 2 (default: a second
                                            stream of the calling thread overlaps them) */
-#define SVO_TUNE_MARCH_BUFFER_RAYS 7u   /* as SVO_TUNE_MARCH_RAYS_PER_LANE for svo_raycast's ray buffers (default 0:
-                                           persistent refill, which suits incoherent bounce rays) */
+#define SVO_TUNE_MARCH_BUFFER_RAYS 7u   /* as SVO_TUNE_MARCH_RAYS_PER_LANE for svo_raycast's ray buffers (default 1) */
 #define SVO_TUNE_PARAMS 8u
 /* level 0: every level; size_class -1: every class.  Rejects values a parameter does not allow. */
 int svo_tune_set(uint32_t param, uint32_t level, int32_t size_class, int32_t value);

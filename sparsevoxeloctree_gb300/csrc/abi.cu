@@ -111,7 +111,7 @@ int device_sm_count() {
 // ---------------------------------------------------------------- launch-parameter table
 // Entry [param][level][size class]; level 0 is unused (a set with level 0 writes every level).
 constexpr uint32_t kTuneClasses = 8;
-static const int kTuneDefault[kTuneParams] = {128, 1, 1, 16, 6, 16, 2, 0};
+static const int kTuneDefault[kTuneParams] = {128, 1, 1, 16, 6, 16, 2, 1};
 static std::atomic<int> g_tune[kTuneParams][SVO_LEVEL_MAX + 1][kTuneClasses];
 static std::once_flag g_tune_once;
 

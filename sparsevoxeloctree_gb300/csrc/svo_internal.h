@@ -93,7 +93,7 @@ enum : uint32_t {
 	kTuneLeafBlocks = 4,   // blocks per SM of the leaf stage
 	kTuneEmitBlocks = 5,   // blocks per SM of the voxelizer's emission
 	kTuneBuildStreams = 6, // streams of the build's bucket / dense stages: 1, or 2 (a second stream overlaps them)
-	kTuneMarchBufferRays = 7, // as kTuneMarchRays, for marches of a ray buffer (svo_raycast)
+	kTuneMarchBufferRays = 7, // as kTuneMarchRays, for marches of a ray buffer (svo_raycast); tuned separately
 	kTuneParams = 8
 };
 int tune_value(uint32_t param, uint32_t level, uint64_t items);
