@@ -28,6 +28,8 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+from sparsevoxeloctree_gb300 import replicas  # noqa: E402
+
 METRIC = "SVO build ms & Grays/s ray march; batched/served vs plain; served p50/p99 ms"
 L2_FLUSH_BYTES = 512 << 20
 
@@ -155,7 +157,7 @@ def profiled_traffic(label: str, workload: str) -> dict:
     return {"traffic": None}
 
 
-def engine_arm(args, rank: int, world: int, device) -> dict:
+def engine_arm(args, env, device) -> dict:
     import numpy as np
     import torch
 
@@ -224,9 +226,8 @@ def engine_arm(args, rank: int, world: int, device) -> dict:
         raise RuntimeError("re-recorded build differs from the first build")
 
     def barrier():
-        if world > 1:
-            torch.distributed.barrier()
         torch.cuda.synchronize()
+        replicas.barrier(env)
 
     # the step recorded once as a CUDA graph and replayed: the same kernels on the same buffers, without
     # the host launch gaps between the step's ~26 launches (stream capture; the library's per-launch
@@ -281,11 +282,7 @@ def engine_arm(args, rank: int, world: int, device) -> dict:
     clocks = sampler.stop()
     eager_ms = [a.elapsed_time(b) for a, b in events]
     step_ms = graph_ms if graph_ms is not None else eager_ms
-    ms = float(np.mean(step_ms))
-    if world > 1:
-        t = torch.tensor([ms], device=device)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = replicas.max_over_ranks(env, float(np.mean(step_ms)), device)
 
     # per-stage device time from the per-kernel events
     def stage_ms(prefixes):
@@ -367,9 +364,9 @@ def engine_arm(args, rank: int, world: int, device) -> dict:
     if not args.no_path_trace:
         stages["path_trace"] = path_trace_stats(api, octree, scene, stream)
 
-    e2e = None if args.no_e2e else e2e_arm(args, scene, tris_host, device, world)
+    e2e = None if args.no_e2e else e2e_arm(args, scene, tris_host, device, env)
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if env.leader and env.world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(scene, per_step=False)
     return {"value": ms, "ms_per_step": ms, "step_ms_all": step_ms, "stages": stages, "roofline": roofline,
             "tuning": tuning,
@@ -377,7 +374,7 @@ def engine_arm(args, rank: int, world: int, device) -> dict:
             "config_extra": {"level": scene.level, "triangles": T, "fragments": F, "rays": n_rays}}
 
 
-def e2e_arm(args, scene, tris_host, device, world) -> dict:
+def e2e_arm(args, scene, tris_host, device, env) -> dict:
     """The same step through the C ABI with host buffers: upload triangles from pinned memory, svo_voxelize
     (count pass, its blocking count readback, exact allocation, emit), svo_build (its blocking range
     readback), svo_raycast_camera, download the hits to pinned memory."""
@@ -418,16 +415,14 @@ def e2e_arm(args, scene, tris_host, device, world) -> dict:
     for _ in range(args.warmup):
         one()
     torch.cuda.synchronize()
+    replicas.barrier(env)
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
         one()
         times.append((time.perf_counter() - t0) * 1e3)
-    ms = float(statistics.mean(times))
-    if world > 1:
-        t = torch.tensor([ms], device=device)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    replicas.barrier(env)
+    ms = replicas.max_over_ranks(env, float(statistics.mean(times)), device)
     return {"value": ms, "unit": "ms", "h2d_bytes_per_step": int(tris_host.numel()),
             "d2h_bytes_per_step": int(hits_host.numel()) + 8 * 3 + 256,
             "path": "svo_voxelize -> svo_build_fraglist -> svo_raycast_camera with pinned host buffers",
@@ -790,9 +785,7 @@ def main() -> int:
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    env = replicas.replica_env()
 
     line = {"metric": METRIC, "unit": "ms", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "fp32+u32",
@@ -802,10 +795,10 @@ def main() -> int:
               "step": "voxelize (count+emit) + octree build + primary-ray march, recorded once as a CUDA graph "
                       "and replayed (stages: eager steps with per-kernel events)",
               "l2": f"flushed between timed steps ({L2_FLUSH_BYTES >> 20} MiB write); fragment list and node "
-                    "pool exceed L2", "parallelism": f"replicas x{world}" if world > 1 else "single GPU"}
+                    "pool exceed L2", "parallelism": env.parallelism}
 
     if args.impl == "reference":
-        res = reference_arm(args, rank)
+        res = reference_arm(args, env.rank)
         if res is None:
             return 0
         line.update({"impl": "reference", "value": res["value"], "ms_per_step": res["ms_per_step"],
@@ -816,15 +809,13 @@ def main() -> int:
         return 0
 
     import torch
-    if world > 1:
-        torch.cuda.set_device(local_rank)
-        torch.distributed.init_process_group("nccl")
-    device = torch.device("cuda", local_rank)
+    device = torch.device("cuda", env.local_rank)
     torch.cuda.set_device(device)
-    res = engine_arm(args, rank, world, device)
-    if not args.no_batch and rank == 0:
+    replicas.init(env, "nccl")
+    res = engine_arm(args, env, device)
+    if not args.no_batch and env.leader:
         res["batched"] = batch_leg(args, device)
-    if not args.no_serve and rank == 0:
+    if not args.no_serve and env.leader:
         res["served"] = serve_leg(args, device)
     config.update(res["config_extra"])
     line.update({"value": res["value"], "ms_per_step": res["ms_per_step"], "config": config,
@@ -834,10 +825,9 @@ def main() -> int:
     for key in ("batched", "served"):
         if key in res:
             line[key] = res[key]
-    if rank == 0:
+    if env.leader:
         print(json.dumps(line), flush=True)
-    if world > 1:
-        torch.distributed.destroy_process_group()
+    replicas.finish(env)
     return 0
 
 
