@@ -377,7 +377,8 @@ def engine_arm(args, env, device) -> dict:
 def e2e_arm(args, scene, tris_host, device, env) -> dict:
     """The same step through the C ABI with host buffers: upload triangles from pinned memory, svo_voxelize
     (count pass, its blocking count readback, exact allocation, emit), svo_build (its blocking range
-    readback), svo_raycast_camera, download the hits to pinned memory."""
+    readback), svo_raycast_camera_download (the march stores the hits straight into the pinned, mapped host
+    buffer).  Scenes with a bounce: svo_raycast_camera + svo_bounce_rays + svo_raycast, one download."""
     import torch
 
     from sparsevoxeloctree_gb300 import _lib, api
@@ -400,14 +401,18 @@ def e2e_arm(args, scene, tris_host, device, env) -> dict:
         _lib.check(lib.svo_voxelize(ctypes.c_void_p(tris_dev.data_ptr()), T, scene.level, ctypes.byref(fl), s))
         oc = _lib.OctreeC()
         _lib.check(lib.svo_build_fraglist(ctypes.byref(fl), ctypes.byref(oc), None, s))
-        _lib.check(lib.svo_raycast_camera(ctypes.byref(oc), ctypes.byref(cam), scene.width, scene.height,
-                                          ctypes.c_void_p(hits_dev.data_ptr()), None, s))
-        if scene.bounce:
+        if scene.bounce:  # the bounce rays start from the primary hits on the device
+            _lib.check(lib.svo_raycast_camera(ctypes.byref(oc), ctypes.byref(cam), scene.width, scene.height,
+                                              ctypes.c_void_p(hits_dev.data_ptr()), None, s))
             _lib.check(lib.svo_bounce_rays(ctypes.c_void_p(hits_dev.data_ptr()), n, scene.seed,
                                            ctypes.c_void_p(rays_dev.data_ptr()), s))
             _lib.check(lib.svo_raycast(ctypes.byref(oc), ctypes.c_void_p(rays_dev.data_ptr()), n,
                                        ctypes.c_void_p(hits_dev.data_ptr() + n * HIT_DTYPE.itemsize), None, s))
-        hits_host.copy_(hits_dev, non_blocking=True)
+            hits_host.copy_(hits_dev, non_blocking=True)
+        else:  # the hits stored into the pinned host buffer by the march itself (or copied in row bands)
+            _lib.check(lib.svo_raycast_camera_download(ctypes.byref(oc), ctypes.byref(cam), scene.width,
+                                                       scene.height, ctypes.c_void_p(hits_dev.data_ptr()),
+                                                       ctypes.c_void_p(hits_host.data_ptr()), None, s))
         lib.svo_fraglist_destroy(ctypes.byref(fl), s)
         lib.svo_octree_destroy(ctypes.byref(oc), s)
         torch.cuda.current_stream().synchronize()
@@ -425,7 +430,7 @@ def e2e_arm(args, scene, tris_host, device, env) -> dict:
     ms = replicas.max_over_ranks(env, float(statistics.mean(times)), device)
     return {"value": ms, "unit": "ms", "h2d_bytes_per_step": int(tris_host.numel()),
             "d2h_bytes_per_step": int(hits_host.numel()) + 8 * 3 + 256,
-            "path": "svo_voxelize -> svo_build_fraglist -> svo_raycast_camera with pinned host buffers",
+            "path": "svo_voxelize -> svo_build_fraglist -> svo_raycast_camera_download with pinned host buffers",
             "timing": "host wall clock per step (includes the ABI's blocking readbacks)"}
 
 

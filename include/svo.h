@@ -178,7 +178,9 @@ size_t svo_profile_summary(char *buf, size_t cap);
 #define SVO_TUNE_BUILD_STREAMS 6u       /* streams of the build's bucket and dense stages: 1, or 2 (default: a second
                                            stream of the calling thread overlaps them) */
 #define SVO_TUNE_MARCH_BUFFER_RAYS 7u   /* as SVO_TUNE_MARCH_RAYS_PER_LANE for svo_raycast's ray buffers (default 1) */
-#define SVO_TUNE_PARAMS 8u
+#define SVO_TUNE_DOWNLOAD_BANDS 8u      /* svo_raycast_camera_download: 0 (default): the march writes into a mapped
+                                         * host buffer; 1, 2, 4, 8, 16: row bands traced and copied in turn */
+#define SVO_TUNE_PARAMS 9u
 /* level 0: every level; size_class -1: every class.  Rejects values a parameter does not allow. */
 int svo_tune_set(uint32_t param, uint32_t level, int32_t size_class, int32_t value);
 /* The value a launch of `items` work items at `level` uses. */
@@ -317,6 +319,17 @@ int svo_raycast(const svo_octree *o, const svo_ray *rays, uint32_t n, svo_hit *h
  * (shader/camera.glsl:11-14), origin = cam->pos.  Hit of pixel (x, y) goes to hits[y * width + x]. */
 int svo_raycast_camera(const svo_octree *o, const svo_camera *cam, uint32_t width, uint32_t height, svo_hit *hits,
                        uint64_t *fetches_dev, void *stream);
+
+/* svo_raycast_camera with the hits delivered into host memory (`hits_host`, width * height hits, 16-byte
+ * aligned) as they are produced.  When `hits_host` is page-locked and mapped into the device's address space
+ * (cudaHostAlloc; cudaHostRegister with cudaHostRegisterMapped) the march stores the hits straight into it
+ * and `hits` may be NULL.  Otherwise (or with SVO_TUNE_DOWNLOAD_BANDS set to a band count) the image is
+ * traced in bands of rows into `hits` (device, the whole image) and each band is copied to `hits_host` on a
+ * second stream while the next band is traced.  Either way the hits are in host memory once `stream`
+ * reaches this point, and they are those of svo_raycast_camera (OctreeTracer::CmdDrawPipeline + reading
+ * the image back). */
+int svo_raycast_camera_download(const svo_octree *o, const svo_camera *cam, uint32_t width, uint32_t height,
+                                svo_hit *hits, svo_hit *hits_host, uint64_t *fetches_dev, void *stream);
 
 /* Beam optimisation of the tracer (OctreeTracer::CmdBeamRenderPass, src/OctreeTracer.cpp:183-211, with
  * shader/octree_tracer_beam.frag and Octree_RayMarchCoarse, shader/octree.glsl:47-177): one start distance

@@ -257,6 +257,11 @@ public:
 	void CmdDrawPipeline(svo_hit *hits_device, void *stream = nullptr) const {
 		Check(svo_raycast_camera(&octree_->Get(), &camera_, width_, height_, hits_device, nullptr, stream));
 	}
+	// CmdDrawPipeline and the read-back of the image, overlapped: hits_host (page-locked) receives the hits.
+	void CmdDrawPipelineToHost(svo_hit *hits_device, svo_hit *hits_host, void *stream = nullptr) const {
+		Check(svo_raycast_camera_download(&octree_->Get(), &camera_, width_, height_, hits_device, hits_host, nullptr,
+		                                  stream));
+	}
 	void CmdTrace(const svo_ray *rays_device, uint32_t n, svo_hit *hits_device, void *stream = nullptr) const {
 		Check(svo_raycast(&octree_->Get(), rays_device, n, hits_device, nullptr, stream));
 	}

@@ -114,6 +114,7 @@ _SIGNATURES = {
     "svo_octree_destroy": ([ctypes.POINTER(OctreeC), P], None),
     "svo_raycast": ([ctypes.POINTER(OctreeC), P, u32, P, P, P], i32),
     "svo_raycast_camera": ([ctypes.POINTER(OctreeC), ctypes.POINTER(CameraC), u32, u32, P, P, P], i32),
+    "svo_raycast_camera_download": ([ctypes.POINTER(OctreeC), ctypes.POINTER(CameraC), u32, u32, P, P, P, P], i32),
     "svo_bounce_rays": ([P, u32, u64, P, P], i32),
     "svo_batcher_create": ([ctypes.POINTER(P)], i32),
     "svo_batcher_destroy": ([P], None),

@@ -341,6 +341,26 @@ class OctreeTracer:
                                                   _ptr(hits), self._fetch_ptr(count_fetches), _stream(stream)))
         return hits
 
+    def CmdDrawPipelineToHost(self, hits_host: torch.Tensor | None = None, hits: torch.Tensor | None = None,
+                              stream=None) -> torch.Tensor:
+        """CmdDrawPipeline with the image read back to host memory while it is traced (svo_raycast_camera_download:
+        the image in row bands, each copied on a second stream as the next is traced).  hits_host: a page-locked
+        uint8 tensor of W*H*32 bytes (allocated pinned when None); hits: the device staging buffer.  Returns
+        hits_host; its contents are valid once `stream` has reached this point."""
+        n = self.m_width * self.m_height
+        if hits is None:
+            hits = torch.empty(n * HIT_DTYPE.itemsize, dtype=torch.uint8, device=self.m_octree.device)
+        if hits_host is None:
+            hits_host = torch.empty(n * HIT_DTYPE.itemsize, dtype=torch.uint8).pin_memory()
+        if hits_host.device.type != "cpu" or hits_host.numel() * hits_host.element_size() < n * HIT_DTYPE.itemsize:
+            raise ValueError("hits_host must be a host tensor of width * height * 32 bytes")
+        cam = camera_struct(self.m_camera)
+        oc = self.m_octree.c_struct()
+        _lib.check(_lib.load().svo_raycast_camera_download(ctypes.byref(oc), ctypes.byref(cam), self.m_width,
+                                                           self.m_height, _ptr(hits), _ptr(hits_host),
+                                                           ctypes.c_void_p(0), _stream(stream)))
+        return hits_host
+
     def CmdBeamRenderPass(self, beam: torch.Tensor | None = None, stream=None) -> torch.Tensor:
         """OctreeTracer::CmdBeamRenderPass (src/OctreeTracer.cpp:183-211): the beam image, one start distance
         per corner of each 8x8 pixel tile (float32, ((H+7)//8+1) x ((W+7)//8+1))."""

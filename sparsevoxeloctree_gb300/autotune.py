@@ -34,6 +34,7 @@ PARAMS = {  # name -> (parameter id, candidate values)
     "emit_blocks": (5, (8, 16, 32)),
     "build_streams": (6, (2, 1)),
     "march_buffer_rays": (7, (0, 1, 2)),  # rays per lane for ray-buffer marches (0: persistent refill)
+    "download_bands": (8, (0, 1, 2, 4)),  # camera-to-host: 0 = store into mapped host memory, else row bands
 }
 
 

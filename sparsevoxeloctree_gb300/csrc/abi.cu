@@ -111,7 +111,7 @@ int device_sm_count() {
 // ---------------------------------------------------------------- launch-parameter table
 // Entry [param][level][size class]; level 0 is unused (a set with level 0 writes every level).
 constexpr uint32_t kTuneClasses = 8;
-static const int kTuneDefault[kTuneParams] = {128, 1, 1, 16, 6, 16, 2, 1};
+static const int kTuneDefault[kTuneParams] = {128, 1, 1, 16, 6, 16, 2, 1, 0};
 static std::atomic<int> g_tune[kTuneParams][SVO_LEVEL_MAX + 1][kTuneClasses];
 static std::once_flag g_tune_once;
 
@@ -130,6 +130,7 @@ static bool tune_valid(uint32_t param, int v) {
 	case kTuneMarchBufferRays: return v == 0 || v == 1 || v == 2;
 	case kTuneMarchShared: return v == 0 || v == 1;
 	case kTuneBuildStreams: return v == 1 || v == 2;
+	case kTuneDownloadBands: return v == 0 || v == 1 || v == 2 || v == 4 || v == 8 || v == 16;
 	default: return v >= 1 && v <= 64;
 	}
 }
@@ -659,6 +660,78 @@ int svo_raycast_camera(const svo_octree *o, const svo_camera *cam, uint32_t widt
 	const uint64_t n = (uint64_t)width * height;
 	if (n > 0xffffffffull) return fail(SVO_ERR_INVALID, "image too large");
 	return raycast_common(o, nullptr, cam, width, height, (uint32_t)n, hits, fetches_dev, stream);
+}
+
+// Page-locked host memory the device can address (cudaHostAlloc, or cudaHostRegister with the mapped
+// flag): its device-side address, else null.
+static svo_hit *mapped_host(svo_hit *p) {
+	cudaPointerAttributes attr;
+	if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+		cudaGetLastError(); // not a CUDA-known pointer: clear the error
+		return nullptr;
+	}
+	return attr.type == cudaMemoryTypeHost && attr.devicePointer ? static_cast<svo_hit *>(attr.devicePointer) : nullptr;
+}
+
+// Mode 0 (mapped host buffer): the march stores each hit straight into host memory over the GPU-CPU link,
+// so the download runs inside the march.  Otherwise the image in row bands (multiples of 4 rows, the
+// camera launch's tile height): each band is traced on `stream`, then copied to the host on a second
+// stream while the next band is traced; `stream` waits for the copies at the end.  Per pixel the march is
+// svo_raycast_camera's, so the hits are identical either way.
+int svo_raycast_camera_download(const svo_octree *o, const svo_camera *cam, uint32_t width, uint32_t height,
+                                svo_hit *hits, svo_hit *hits_host, uint64_t *fetches_dev, void *stream) {
+	if (!cam) return fail(SVO_ERR_INVALID, "null camera");
+	const uint64_t n = (uint64_t)width * height;
+	if (n > 0xffffffffull) return fail(SVO_ERR_INVALID, "image too large");
+	int rc;
+	if ((rc = check_octree(o))) return rc;
+	if (n == 0) return SVO_OK;
+	if (!hits_host) return fail(SVO_ERR_INVALID, "null host hit buffer");
+	if (!aligned(hits_host, 16)) return fail(SVO_ERR_INVALID, "host hit buffer must be 16-byte aligned");
+	uint32_t bands = (uint32_t)tune_value(kTuneDownloadBands, o->level, n);
+	if (bands == 0) {
+		if (svo_hit *direct = mapped_host(hits_host))
+			return raycast_common(o, nullptr, cam, width, height, (uint32_t)n, direct, fetches_dev, stream);
+		bands = 2; // not mapped: copies
+	}
+	if (!hits) return fail(SVO_ERR_INVALID, "null hit buffer (the host buffer is not mapped)");
+	if (!aligned(hits, 16)) return fail(SVO_ERR_INVALID, "hit buffer must be 16-byte aligned");
+	cudaStream_t s = (cudaStream_t)stream;
+	const uint32_t band_rows = std::max<uint32_t>(4u, (height + bands - 1) / bands + 3u) / 4u * 4u;
+	unsigned long long *scratch = nullptr;
+	SVO_CK(alloc_async(&scratch, 2 * sizeof(unsigned long long), s), "ray ticket allocation");
+	SVO_CK(cudaMemsetAsync(scratch + 1, 0, sizeof(unsigned long long), s), "ray status");
+	MarchArgs a;
+	memset(&a, 0, sizeof(a));
+	a.pool = o->words;
+	a.range = o->range_words;
+	a.level = o->level;
+	a.cam = *cam;
+	a.width = width;
+	a.height = height;
+	a.n = (uint32_t)n; // launch shape and launch parameters of the whole image
+	a.hits = hits;
+	a.ticket = scratch;
+	a.status = reinterpret_cast<uint32_t *>(scratch + 1);
+	a.fetches = (unsigned long long *)fetches_dev;
+	cudaError_t e = cudaSuccess;
+	{
+		SideFork fork(s, bands > 1);
+		for (uint32_t row0 = 0; row0 < height && e == cudaSuccess; row0 += band_rows) {
+			a.row0 = row0;
+			a.rows = std::min(band_rows, height - row0);
+			e = march_launch(a, true, s);
+			if (e != cudaSuccess) break;
+			fork.side_waits_main();
+			const size_t off = (size_t)row0 * width, bytes = (size_t)a.rows * width * sizeof(svo_hit);
+			e = cudaMemcpyAsync(hits_host + off, hits + off, bytes, cudaMemcpyDeviceToHost, fork.side());
+		}
+		fork.mark_side(0);
+		fork.main_waits(0);
+	}
+	cudaFreeAsync(scratch, s);
+	if (e != cudaSuccess) return cuda_fail(e, "raycast download");
+	return SVO_OK;
 }
 
 uint64_t svo_beam_texels(uint32_t width, uint32_t height) {

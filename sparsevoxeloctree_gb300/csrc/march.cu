@@ -274,6 +274,11 @@ SVO_DEV void beam_advance(const float *__restrict__ beam, uint32_t width, uint32
 	for (int k = 0; k < 3; ++k) o[k] = o[k] + d[k] * m;
 }
 
+// One past the last image row a camera launch traces (the launch covers rows [row0, that)).
+SVO_DEV uint32_t camera_row_end(const MarchArgs &a) {
+	return a.rows ? min(a.height, a.row0 + a.rows) : a.height;
+}
+
 // Variants (chosen per launch from the launch-parameter table): TPB threads per block, RPL rays per lane
 // per ticket, SHARED: stack in shared memory ([level][thread], 32 distinct banks per warp) or in a
 // private local-memory array.
@@ -286,7 +291,8 @@ __global__ void __launch_bounds__(TPB) march_kernel(MarchArgs a) {
 	const uint32_t lane = lane_id();
 	// work slots: ray indices, or for camera rays 32 slots per 8x4 tile of the (padded) image
 	const uint32_t tiles_x = CAMERA ? (a.width + 7u) / 8u : 0u;
-	const uint64_t slots = CAMERA ? (uint64_t)tiles_x * ((a.height + 3u) / 4u) * 32u : (uint64_t)a.n;
+	const uint32_t y_end = camera_row_end(a);
+	const uint64_t slots = CAMERA ? (uint64_t)tiles_x * ((y_end - a.row0 + 3u) / 4u) * 32u : (uint64_t)a.n;
 	unsigned long long fetched = 0;
 	for (;;) {
 		unsigned long long base = 0;
@@ -301,8 +307,8 @@ __global__ void __launch_bounds__(TPB) march_kernel(MarchArgs a) {
 			uint32_t r;
 			if constexpr (CAMERA) {
 				const uint32_t tile = (uint32_t)(slot >> 5), in = (uint32_t)(slot & 31u);
-				const uint32_t x = (tile % tiles_x) * 8u + (in & 7u), y = (tile / tiles_x) * 4u + (in >> 3);
-				if (x >= a.width || y >= a.height) continue; // padding slot of a partial edge tile
+				const uint32_t x = (tile % tiles_x) * 8u + (in & 7u), y = a.row0 + (tile / tiles_x) * 4u + (in >> 3);
+				if (x >= a.width || y >= y_end) continue; // padding slot of a partial edge tile
 				r = y * a.width + x;
 				camera_ray(a.cam, a.width, a.height, r, o, d);
 				if (a.beam) beam_advance(a.beam, a.width, r, o, d);
@@ -338,7 +344,8 @@ __global__ void __launch_bounds__(TPB) march_refill_kernel(MarchArgs a) {
 	uint32_t *stack = SHARED ? s_stack + threadIdx.x : l_stack;
 	const uint32_t lane = lane_id(), lt_mask = (1u << lane) - 1u;
 	const uint32_t tiles_x = CAMERA ? (a.width + 7u) / 8u : 0u;
-	const uint64_t slots = CAMERA ? (uint64_t)tiles_x * ((a.height + 3u) / 4u) * 32u : (uint64_t)a.n;
+	const uint32_t y_end = camera_row_end(a);
+	const uint64_t slots = CAMERA ? (uint64_t)tiles_x * ((y_end - a.row0 + 3u) / 4u) * 32u : (uint64_t)a.n;
 	RayState s;
 	bool active = false, exhausted = false;
 	uint32_t r = 0;
@@ -358,8 +365,8 @@ __global__ void __launch_bounds__(TPB) march_refill_kernel(MarchArgs a) {
 				bool live = true;
 				if constexpr (CAMERA) {
 					const uint32_t tile = (uint32_t)(slot >> 5), in = (uint32_t)(slot & 31u);
-					const uint32_t x = (tile % tiles_x) * 8u + (in & 7u), y = (tile / tiles_x) * 4u + (in >> 3);
-					live = x < a.width && y < a.height; // padding slots of partial edge tiles
+					const uint32_t x = (tile % tiles_x) * 8u + (in & 7u), y = a.row0 + (tile / tiles_x) * 4u + (in >> 3);
+					live = x < a.width && y < y_end; // padding slots of partial edge tiles
 					if (live) {
 						r = y * a.width + x;
 						camera_ray(a.cam, a.width, a.height, r, o, d);

@@ -94,7 +94,8 @@ enum : uint32_t {
 	kTuneEmitBlocks = 5,   // blocks per SM of the voxelizer's emission
 	kTuneBuildStreams = 6, // streams of the build's bucket / dense stages: 1, or 2 (a second stream overlaps them)
 	kTuneMarchBufferRays = 7, // as kTuneMarchRays, for marches of a ray buffer (svo_raycast); tuned separately
-	kTuneParams = 8
+	kTuneDownloadBands = 8,   // row bands of svo_raycast_camera_download (traced and copied to the host in turn)
+	kTuneParams = 9
 };
 int tune_value(uint32_t param, uint32_t level, uint64_t items);
 
@@ -315,6 +316,7 @@ struct MarchArgs {
 	unsigned long long *fetches;  // optional node-load total
 	uint32_t *status;             // device status word
 	const float *beam;            // camera rays: beam texels to advance each ray by (null: none)
+	uint32_t row0, rows;          // camera rays: trace image rows [row0, row0 + rows) only (rows = 0: to the end)
 };
 cudaError_t march_launch(const MarchArgs &a, bool camera, cudaStream_t stream);
 // Beam pre-pass texels ((width + 7) / 8 + 1) x ((height + 7) / 8 + 1) for camera `a.cam`.

@@ -107,10 +107,11 @@ def test_launch_parameter_table(lib):
         assert all(autotune.get("leaf_blocks", lv, 10 ** k) == 8 for lv in (1, 7, 12) for k in (3, 6, 9))
         assert autotune.get("build_streams", 10, 1000) == 2
         assert autotune.get("march_buffer_rays", 10, 1000) == 1
+        assert autotune.get("download_bands", 10, 1000) == 0
         autotune.set_value("build_streams", 10, 0, 1)
         assert autotune.get("build_streams", 10, 1000) == 1
         for bad in ((0, 10, 3, 100), (1, 10, 3, 3), (2, 10, 3, 2), (3, 10, 3, 0), (3, 13, 3, 8), (3, 10, 8, 8),
-                    (6, 10, 3, 3), (9, 10, 3, 8)):
+                    (6, 10, 3, 3), (8, 10, 3, 3), (9, 10, 3, 8)):
             assert lib.svo_tune_set(*bad) == _lib.SVO_ERR_INVALID
         t = autotune.table()
         assert t["march_block"]["default"] == 128 and t["march_block"]["10:3"] == 256

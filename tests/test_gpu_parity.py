@@ -397,6 +397,49 @@ def test_camera_image_sizes_not_multiple_of_the_tile(cuda, size):
     assert_hits_equal(got, oracle.raycast(pool, s.level, oracle.camera_rays(cam, w, h)))
 
 
+@pytest.mark.parametrize("bands", [0, 1, 2, 4, 8, 16])
+@pytest.mark.parametrize("size", [(37, 23), (1, 1), (64, 3), (300, 97)])
+@pytest.mark.parametrize("pinned", [True, False])
+def test_camera_download_to_host(cuda, size, bands, pinned):
+    """svo_raycast_camera_download: mode 0 stores the hits straight into a mapped (pinned) host buffer;
+    band counts trace the image in row bands and copy each band while the next is traced (a pageable host
+    buffer always takes the copies).  The host image equals the oracle's and nothing is written past it."""
+    import torch
+
+    from sparsevoxeloctree_gb300 import autotune
+    if bands not in (0, 2) and not pinned:
+        pytest.skip("pageable buffers: one copy mode is enough")
+    api = _api()
+    s = scenes.plain_256()
+    frags = oracle.voxelize(s.tris, s.level)
+    o, pool = gpu_build(frags, s.level)
+    w, h = size
+    n = w * h
+    cam = scenes.camera_from_angles((1.5, 1.5, 0.5), 0.05, 0.02, np.pi / 3, w / h)
+    autotune.set_value("download_bands", 0, -1, bands)
+    try:
+        dev = torch.full((n * 32 + 64,), 0xAB, dtype=torch.uint8, device="cuda")
+        host = torch.full((n * 32 + 64,), 0xCD, dtype=torch.uint8)
+        if pinned:
+            host = host.pin_memory()
+        api.OctreeTracer.Create(o, cam, w, h).CmdDrawPipelineToHost(host, dev[: n * 32])
+        torch.cuda.synchronize()
+    finally:
+        _lib_reset_tune()
+    raw = host.numpy()
+    assert (raw[n * 32:] == 0xCD).all() and (dev[n * 32:].cpu().numpy() == 0xAB).all()
+    if bands == 0 and pinned:
+        assert (dev.cpu().numpy() == 0xAB).all()  # written straight to the host: the staging buffer is untouched
+    else:
+        assert np.array_equal(raw[: n * 32], dev[: n * 32].cpu().numpy())
+    assert_hits_equal(raw[: n * 32].view(HIT_DTYPE), oracle.raycast(pool, s.level, oracle.camera_rays(cam, w, h)))
+
+
+def _lib_reset_tune():
+    from sparsevoxeloctree_gb300 import _lib
+    _lib.load().svo_tune_reset()
+
+
 def test_voxelizer_reemission_needs_exact_unit_scratch(cuda):
     """The room scene's walls and cylinders need more raster units than the default guess: re-emission
     (CmdVoxelize) must use the unit count from the first pass and reproduce every fragment."""
