@@ -94,11 +94,13 @@ SVO_DEV void ray_init(RayState &s, const float o[3], const float dir[3], uint32_
 
 // One iteration of the march loop; returns true when the ray has ended (the loop of the shader breaks or
 // its condition fails).  A malformed pool (pointer outside the range, interior word below the octree
-// level, iteration bound) ends the ray as an aborted miss and sets kStatusMalformed.
-template <int STRIDE>
+// level, iteration bound) ends the ray as an aborted miss and sets kStatusMalformed.  CHECK_END = false
+// skips the loop condition for callers that never step an ended ray (every path that ends the ray
+// returns true at once, so only a ray without direction enters the loop ended).
+template <int STRIDE, bool CHECK_END = true>
 SVO_DEV bool ray_step(RayState &s, const uint32_t *__restrict__ pool, uint32_t range, uint32_t *stack,
                       uint32_t *status) {
-	if (s.scale >= SVO_STACK_SIZE) return true;
+	if (CHECK_END && s.scale >= SVO_STACK_SIZE) return true;
 	if (s.iter >= SVO_MARCH_MAX_ITER) {
 		s.aborted = true;
 		return true;
@@ -118,7 +120,11 @@ SVO_DEV bool ray_step(RayState &s, const uint32_t *__restrict__ pool, uint32_t r
 	float tc[3];
 #pragma unroll
 	for (int k = 0; k < 3; ++k) tc[k] = s.pos[k] * s.coef[k] - s.bias[k];
-	const float tc_max = min_glsl(min_glsl(tc[0], tc[1]), tc[2]);
+	// GLSL min (y < x ? y : x) as one min instruction.  For a finite origin and direction, pos * coef is
+	// finite and nonzero (pos in [1, 2], coef = -1 / max(|d|, EPS)), so tc = pos * coef - bias is never
+	// NaN (bias may overflow to an infinity, never both terms) and never -0 (a - b gives -0 only for
+	// a = -0); fminf then returns the same value as the GLSL form.
+	const float tc_max = fminf(fminf(tc[0], tc[1]), tc[2]);
 
 	if ((s.cur & 0x80000000u) != 0u && s.t_min <= s.t_max) {
 		const float half = s.scale_exp2 * 0.5f;
@@ -230,8 +236,9 @@ SVO_DEV void march_ray(const uint32_t *__restrict__ pool, uint32_t range, uint32
                        const float dir[3], uint32_t *stack, MarchOut &out, uint32_t &nfetch, uint32_t *status) {
 	RayState s;
 	ray_init<STRIDE>(s, o, dir, level, stack);
-	while (!ray_step<STRIDE>(s, pool, range, stack, status)) {
-	}
+	if (!s.none)
+		while (!ray_step<STRIDE, false>(s, pool, range, stack, status)) {
+		}
 	ray_finish(s, level, out);
 	nfetch = s.nfetch;
 }
