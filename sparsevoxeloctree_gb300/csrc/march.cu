@@ -471,7 +471,7 @@ SVO_DEV bool march_traverse(const uint32_t *__restrict__ pool, uint32_t range, u
 		float tc[3];
 #pragma unroll
 		for (int k = 0; k < 3; ++k) tc[k] = pos[k] * coef[k] - bias[k];
-		const float tc_max = min_glsl(min_glsl(tc[0], tc[1]), tc[2]);
+		const float tc_max = fminf(fminf(tc[0], tc[1]), tc[2]); // the GLSL min for finite rays (ray_step)
 		if ((cur & 0x80000000u) != 0u && t_min <= t_max) {
 			if (COARSE && orig_sz + tc_max * dir_sz >= scale_exp2) break;
 			const float half = scale_exp2 * 0.5f;
