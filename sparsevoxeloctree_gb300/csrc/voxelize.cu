@@ -576,6 +576,7 @@ __global__ void __launch_bounds__(kTPB, 4) vox_emit_units(VoxBatch vb, uint32_t 
 		int32_t k = 0, q0 = 0, lo = 0, z0 = 0, z1 = 0, R = 0;
 		float kf = 0.0f, fr0 = 0.0f, fb = 0.0f;
 		uint32_t ush = 0, zsh = 0, usplit = 0, zsplit = 0, base_lo = 0, base_hi = 0;
+#pragma unroll 2
 		for (uint32_t f = lane; f < total; f += 32) {
 			while (warp_incl[j] <= f) ++j;
 			if (j != have) {
