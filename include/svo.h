@@ -391,7 +391,8 @@ typedef struct svo_trace_request {
 	uint32_t n_primary;
 	uint32_t n_rays;        /* rays mode */
 	const svo_ray *rays;    /* rays mode: host memory, read while the request runs */
-	svo_hit *hits;          /* host memory (page-locked for full overlap): camera mode 2 * n_primary hits,
+	svo_hit *hits;          /* host memory (page-locked and mapped, as cudaHostAlloc gives it: the march stores
+	                           the final hits there directly; otherwise copied): camera mode 2 * n_primary hits,
 	                           primary then bounce (bounce i from primary hit i, svo_bounce_rays with `seed`);
 	                           rays mode n_rays hits.  Written when the request completes. */
 	uint64_t seed;

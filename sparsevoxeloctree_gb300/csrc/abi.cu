@@ -662,16 +662,7 @@ int svo_raycast_camera(const svo_octree *o, const svo_camera *cam, uint32_t widt
 	return raycast_common(o, nullptr, cam, width, height, (uint32_t)n, hits, fetches_dev, stream);
 }
 
-// Page-locked host memory the device can address (cudaHostAlloc, or cudaHostRegister with the mapped
-// flag): its device-side address, else null.
-static svo_hit *mapped_host(svo_hit *p) {
-	cudaPointerAttributes attr;
-	if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
-		cudaGetLastError(); // not a CUDA-known pointer: clear the error
-		return nullptr;
-	}
-	return attr.type == cudaMemoryTypeHost && attr.devicePointer ? static_cast<svo_hit *>(attr.devicePointer) : nullptr;
-}
+static svo_hit *mapped_host(svo_hit *p) { return static_cast<svo_hit *>(svo::mapped_host_ptr(p, 16)); }
 
 // Mode 0 (mapped host buffer): the march stores each hit straight into host memory over the GPU-CPU link,
 // so the download runs inside the march.  Otherwise the image in row bands (multiples of 4 rows, the

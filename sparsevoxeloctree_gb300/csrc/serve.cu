@@ -8,7 +8,8 @@
 //     rays, request count and the device bytes in flight stay within the configured limits, and issues
 //     the batch on a free lane (a stream): one march launch for every request's primary rays, one bounce
 //     launch, one march launch for the bounce rays, and one copy of each request's hits to its host
-//     buffer;
+//     buffer (when that buffer is page-locked and mapped, the march stores the final hits there directly
+//     and only a camera request's primary hits are copied);
 //   * up to `lanes` batches are in flight at once, so requests that arrive while others run are admitted
 //     as soon as a lane and memory free up, and their work overlaps on the device;
 //   * a waiter thread per lane blocks on the lane's completion event and retires its requests (their
@@ -195,6 +196,12 @@ static cudaError_t issue(Server *S, Lane &L) {
 	BounceJob *bj = (BounceJob *)(host + o_bjobs);
 	uint64_t slots1 = 0, slots2 = 0, nbounce = 0;
 	uint32_t k2 = 0;
+	// A request whose hit buffer is page-locked and mapped gets its final hits stored in place by the march
+	// over the GPU-CPU link (rays requests: all of them; camera requests: the bounce hits, while the primary
+	// hits stay in the arena for the bounce launch to read and are copied).  Everything the kernels read
+	// stays in device memory: reads over the link would stall the shared launches.
+	std::vector<svo_hit *> hits_mapped(nb);
+	for (size_t i = 0; i < nb; ++i) hits_mapped[i] = static_cast<svo_hit *>(mapped_host_ptr(batch[i]->tr.hits, 16));
 	for (size_t i = 0; i < nb; ++i) {
 		Req *r = batch[i];
 		const svo_trace_request &t = r->tr;
@@ -204,7 +211,7 @@ static cudaError_t issue(Server *S, Lane &L) {
 		j.pool = o.words;
 		j.range = o.range_words;
 		j.level = o.level;
-		j.hits = (svo_hit *)(dev + o_hits[i]);
+		j.hits = hits_mapped[i] && t.mode == SVO_REQUEST_RAYS ? hits_mapped[i] : (svo_hit *)(dev + o_hits[i]);
 		if (t.mode == SVO_REQUEST_CAMERA) {
 			j.rays = nullptr;
 			j.cam = t.camera;
@@ -223,7 +230,7 @@ static cudaError_t issue(Server *S, Lane &L) {
 			bj[k2] = b;
 			MarchJob m2 = j;
 			m2.rays = b.rays;
-			m2.hits = j.hits + t.n_primary;
+			m2.hits = (hits_mapped[i] ? hits_mapped[i] : j.hits) + t.n_primary;
 			m2.slot_begin = slots2;
 			slots2 += march_job_slots(m2);
 			j2[k2++] = m2;
@@ -247,9 +254,12 @@ static cudaError_t issue(Server *S, Lane &L) {
 	if (e == cudaSuccess && ncam) e = bounce_jobs_launch((const BounceJob *)(dev + o_bjobs), ncam, nbounce, L.s);
 	if (e == cudaSuccess && ncam)
 		e = march_jobs_launch((const MarchJob *)(dev + o_jobs2), ncam, slots2, ticket, status, L.s);
-	for (size_t i = 0; i < nb && e == cudaSuccess; ++i)
-		e = cudaMemcpyAsync(batch[i]->tr.hits, dev + o_hits[i], sizeof(svo_hit) * batch[i]->hits, cudaMemcpyDeviceToHost,
-		                    L.s);
+	for (size_t i = 0; i < nb && e == cudaSuccess; ++i) {
+		const svo_trace_request &t = batch[i]->tr;
+		// mapped: nothing for rays requests, the primary half for camera requests
+		const uint64_t n = !hits_mapped[i] ? batch[i]->hits : (t.mode == SVO_REQUEST_CAMERA ? t.n_primary : 0);
+		if (n) e = cudaMemcpyAsync(t.hits, dev + o_hits[i], sizeof(svo_hit) * n, cudaMemcpyDeviceToHost, L.s);
+	}
 	if (e == cudaSuccess) e = cudaMemcpyAsync(L.staging, status, 4, cudaMemcpyDeviceToHost, L.s);
 	if (e == cudaSuccess) e = cudaEventRecord(L.done, L.s);
 	return e;

@@ -387,6 +387,18 @@ struct MarchJob {
 };
 // Work slots of a job (camera jobs: 32 per 8x4 tile of the rows holding its n pixels).
 uint64_t march_job_slots(const MarchJob &j);
+// Device-side address of page-locked host memory mapped into the device's address space (cudaHostAlloc;
+// cudaHostRegister with the mapped flag), when it is aligned to `align` bytes; null otherwise.
+inline void *mapped_host_ptr(const void *p, size_t align) {
+	if (!p) return nullptr;
+	cudaPointerAttributes attr;
+	if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+		cudaGetLastError(); // not a CUDA-known pointer: clear the error
+		return nullptr;
+	}
+	if (attr.type != cudaMemoryTypeHost || !attr.devicePointer) return nullptr;
+	return ((uintptr_t)attr.devicePointer % align) == 0 ? attr.devicePointer : nullptr;
+}
 // `jobs` (device) holds njobs jobs whose slot_begin are set; total = slots of all jobs.  ticket (device,
 // 8 B) is zeroed here; status (device) gets kStatusMalformed for a malformed pool.
 cudaError_t march_jobs_launch(const MarchJob *jobs, uint32_t njobs, uint64_t total, unsigned long long *ticket,

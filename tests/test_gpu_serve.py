@@ -106,7 +106,31 @@ def test_alone_equals_mix_equals_direct(built):
         assert np.array_equal(alone[i], ref), f"request {i}: differs from the single-request path"
 
 
-def test_ray_requests_match_svo_raycast(built):
+def pageable(nbytes):
+    import torch
+    return torch.empty(max(nbytes, 1), dtype=torch.uint8)
+
+
+def test_pageable_and_mapped_buffers_agree(built):
+    """Pinned (mapped) host buffers receive the bounce hits from the march in place; pageable ones get
+    every hit through the lane's arena and copies.  A mix of both, in shared launches, gives the
+    single-request hits."""
+    server, ids, octrees = built
+    reqs = requests(len(ids), 12, seed=11)
+    sub = []
+    for k, r in enumerate(reqs):
+        buf = (pinned if k % 2 else pageable)(2 * r["n"] * HIT_DTYPE.itemsize)
+        sub.append((server.SubmitCamera(r["scene"], r["cam"], r["w"], r["h"], r["n"], r["seed"], buf), buf))
+    for (t, buf), r in zip(sub, reqs):
+        assert server.Wait(t)["status"] == 0
+        ref = direct_camera(octrees[r["scene"]], r["cam"], r["w"], r["h"], r["n"], r["seed"])
+        assert np.array_equal(hits_of(buf, 2 * r["n"]), ref)
+
+
+@pytest.mark.parametrize("alloc", ["pinned", "pageable", "pinned_offset"])
+def test_ray_requests_match_svo_raycast(built, alloc):
+    """pinned_offset: mapped buffers whose rays start 8 bytes in and hits 16 bytes in (still aligned
+    for the march's stores) or 4 bytes in (unaligned: copied instead)."""
     import torch
     api = _api()
     server, ids, octrees = built
@@ -115,9 +139,15 @@ def test_ray_requests_match_svo_raycast(built):
     for k in range(6):
         o, d = scenes.random_rays(g, int(g.integers(1, 5000)), inside=bool(k % 2))
         rays = rays_from_arrays(o, d)
-        rh = pinned(rays.nbytes)
+        if alloc == "pageable":
+            rh, hh = pageable(rays.nbytes), pageable(len(rays) * HIT_DTYPE.itemsize)
+        elif alloc == "pinned":
+            rh, hh = pinned(rays.nbytes), pinned(len(rays) * HIT_DTYPE.itemsize)
+        else:
+            hit_off = 16 if k % 2 else 4
+            rh = pinned(rays.nbytes + 8)[8:]
+            hh = pinned(len(rays) * HIT_DTYPE.itemsize + hit_off)[hit_off:]
         rh.numpy()[:] = rays.view(np.uint8)
-        hh = pinned(len(rays) * HIT_DTYPE.itemsize)
         sc = k % len(ids)
         tickets.append((server.SubmitRays(sc, rh, hh), hh, rays, sc))
     for t, hh, rays, sc in tickets:
