@@ -39,6 +39,14 @@ def test_invalid_arguments_are_rejected_before_any_launch(lib):
     assert lib.svo_raycast(ctypes.byref(oc), None, 0, None, None, None) == _lib.SVO_ERR_INVALID  # null octree
     oc.words, oc.level, oc.range_words = 256, 5, 12  # range not a multiple of 8
     assert lib.svo_raycast(ctypes.byref(oc), None, 0, None, None, None) == _lib.SVO_ERR_INVALID
+    oc.range_words = 16
+    cam = _lib.CameraC()
+    dl = lib.svo_raycast_camera_download
+    assert dl(ctypes.byref(oc), None, 4, 4, None, None, None, None) == _lib.SVO_ERR_INVALID  # null camera
+    assert dl(ctypes.byref(oc), ctypes.byref(cam), 4, 4, None, None, None, None) == _lib.SVO_ERR_INVALID  # no host buffer
+    assert dl(ctypes.byref(oc), ctypes.byref(cam), 4, 4, None, ctypes.c_void_p(8), None, None) == _lib.SVO_ERR_INVALID
+    assert b"aligned" in lib.svo_last_error()
+    assert dl(ctypes.byref(oc), ctypes.byref(cam), 0, 4, None, None, None, None) == _lib.SVO_OK  # empty image
     assert lib.svo_build_into(ctypes.c_void_p(256), 1, 3, ctypes.c_void_p(256), 4, ctypes.c_void_p(256), 1 << 20,
                               ctypes.c_void_p(256), None) == _lib.SVO_ERR_CAPACITY
     assert lib.svo_build_into(ctypes.c_void_p(256), 1, 3, ctypes.c_void_p(256), 64, ctypes.c_void_p(256), 64,
