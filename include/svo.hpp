@@ -11,6 +11,7 @@
 //   Octree::Update(pool, builder)   src/Octree.cpp:22-35 svo::Octree::Update(builder)
 //   OctreeTracer::CmdDrawPipeline(cb, frame) src/OctreeTracer.cpp:213-246
 //                                                        svo::OctreeTracer::CmdDrawPipeline(hits, stream)
+//   (+ reading the frame back)                           svo::OctreeTracer::CmdDrawPipelineToHost(hits, host, stream)
 //   OctreeTracer::CmdBeamRenderPass(cb, frame) :183-211  svo::OctreeTracer::CmdBeamRenderPass(beam, stream)
 //                                                        (+ CmdDrawPipelineBeam, CmdOcclude)
 //   Scene::load_meshes(filename)   src/Scene.cpp:36-147  svo::LoadObj(path)

@@ -54,6 +54,10 @@ int main(int argc, char **argv) {
 		auto tracer = svo::OctreeTracer::Create(octree, cam, width, height);
 		svo::DeviceBuffer hits(sizeof(svo_hit) * width * height, nullptr);
 		tracer->CmdDrawPipeline((svo_hit *)hits.get());
+		// the same frame read back into (pageable) host memory while it is traced
+		svo::DeviceBuffer hits2(sizeof(svo_hit) * width * height, nullptr);
+		std::vector<svo_hit> to_host(width * height);
+		tracer->CmdDrawPipelineToHost((svo_hit *)hits2.get(), to_host.data());
 
 		std::vector<uint64_t> frags(voxelizer->GetVoxelFragmentCount());
 		svo::Check(svo_download(frags.data(), voxelizer->GetVoxelFragmentList(), frags.size() * 8, 0, nullptr));
@@ -61,6 +65,10 @@ int main(int argc, char **argv) {
 		svo::Check(svo_download(pool.data(), octree->GetBuffer(), octree->GetRange(), 0, nullptr));
 		std::vector<svo_hit> h(width * height);
 		svo::Check(svo_download(h.data(), hits.get(), h.size() * sizeof(svo_hit), 1, nullptr));
+		if (std::memcmp(h.data(), to_host.data(), h.size() * sizeof(svo_hit)) != 0) {
+			std::fprintf(stderr, "CmdDrawPipelineToHost differs from CmdDrawPipeline + download\n");
+			return 4;
+		}
 		write_file(out + ".frags", frags);
 		write_file(out + ".pool", pool);
 		write_file(out + ".hits", h);
