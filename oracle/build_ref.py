@@ -115,9 +115,14 @@ def transform(src: str, namespace: str, main_name: str | None) -> str:
            f"{s}\n}} // namespace {namespace}\n"
 
 
+# Where the reference checkout is read from: $SVO_REFERENCE, else the checkout's location in the build
+# container (this recipe is the one file that names it; the GPU machine has no checkout and builds nothing here).
+DEFAULT_REFERENCE = os.environ.get("SVO_REFERENCE") or "/root/reference"
+
+
 def main() -> int:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default=os.environ.get("SVO_REFERENCE", "/root/reference"))
+    ap.add_argument("--reference", default=DEFAULT_REFERENCE)
     args = ap.parse_args()
     shader_dir = os.path.join(args.reference, "shader")
     if not os.path.isdir(shader_dir):

@@ -15,7 +15,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_ref", "libsvo_ref.so")
-REFERENCE_DIR = os.environ.get("SVO_REFERENCE", "/root/reference")
+from .build_ref import DEFAULT_REFERENCE as REFERENCE_DIR  # noqa: E402  (the recipe owns the location)
 
 _lib = None
 _lib_etrig = None

@@ -1,8 +1,9 @@
 """Build libsvo.so (the engine's CUDA kernels + C ABI) in-tree for sm_103a with nvcc.
 
-Four translation units compile in parallel (seconds each) and link into
-sparsevoxeloctree_gb300/libsvo.so; objects go to sparsevoxeloctree_gb300/_build/.  The march unit is
-compiled with -fmad=false so its float arithmetic is rounded exactly like the reference's scalar code.
+The translation units listed in UNITS compile in parallel (seconds each) and link into
+sparsevoxeloctree_gb300/libsvo.so; objects go to sparsevoxeloctree_gb300/_build/.  The march and texture
+units are compiled with -fmad=false so their float arithmetic is rounded exactly like the reference's
+scalar code.
 """
 from __future__ import annotations
 

@@ -12,19 +12,22 @@
 //   * that word sits at 8 * (1 + grank(d-1, m >> 3)) + (m & 7), i.e. in its parent's child block.
 // GB300 design, in four stages:
 //   dense   depths 1..D (D = min(L-1, 9); 8^9 bits = 16 MB stays in L2): one sweep over the fragments sets
-//           the occupancy bits of depth D (warp-deduplicated atomicOr), coarser depths are OR-reductions of
+//           the occupancy bits of depth D (run-merged atomicOr), coarser depths are OR-reductions of
 //           8-bit groups, one single-pass look-back scan of popcounts over all depths gives every grank,
 //           and one pass writes all interior words of depths 1..D;
-//   buckets the same sweep counts fragments per bucket of 32^3 voxels; a look-back scan and one scatter
-//           copy the fragments into bucket order (8 B per fragment), which every later sweep reads;
+//   buckets the same sweep counts fragments per bucket (16^3 voxels while the leaf parents are dense,
+//           L <= 10; 32^3 voxels deeper); a look-back scan and one scatter copy the fragments into bucket
+//           order (8 B each: a leaf item, slot << 32 | rgb, when the leaf parents are dense, else the
+//           fragment), which every later sweep reads;
 //   sparse  depths D+1..L-1 (only when L > 10): the reference's tag / prefix-sum alloc per level with a
 //           per-fragment cached node index (4 B per fragment), so tag reads one parent word;
-//   leaf    one block per bucket: the bucket's leaf blocks are contiguous in the pool, so the block
-//           accumulates their colours in shared memory (r, g, b, n in 16-bit fields, one shared atomic
-//           per fragment) and writes every leaf word, 0xC0000000 | min(n,63)<<24 | floor(sum/n) (the
-//           channel-wise integer mean), with no accumulator array in device memory.  The packing is exact
-//           up to 257 fragments per voxel; a window where a voxel exceeds that is redone with exact
-//           64-bit sums in the same block.
+//   leaf    one block per leaf window (4096 consecutive words of the leaf range) at a time: the window's
+//           items come from the run of buckets whose leaf spans meet it (each item is read at most
+//           twice), the block accumulates their colours in shared memory (r, g, b, n in 16-bit fields,
+//           one shared atomic per item) and writes every leaf word of the window,
+//           0xC0000000 | min(n,63)<<24 | floor(sum/n) (the channel-wise integer mean), with no
+//           accumulator array in device memory.  The packing is exact up to 257 fragments per voxel; a
+//           window where a voxel exceeds that is redone with exact 64-bit sums in the same block.
 // Sizes stay on the device (BuildState): no host round trip inside a stage.
 #include <cstring>
 

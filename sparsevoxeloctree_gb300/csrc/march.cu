@@ -16,6 +16,36 @@
 //   * node words are read through the read-only path (ld.global.nc), so hot upper levels stay in L1/L2;
 //   * camera rays are generated in the kernel (no ray buffer), hits are written as two 16 B stores
 //     (row-major by pixel, whatever the claim order).
+//
+// The traversal (ray_init / ray_step / ray_finish below, and the occlusion, coarse and path-tracer
+// marches built on it) restates the sparse-voxel-octree ray cast of Laine and Karras, "Efficient Sparse
+// Voxel Octrees" (NVIDIA Research, 2010), as the reference carries it in shader/octree.glsl:15-42,
+// 179-629.  That code is distributed under the following notice, which applies to this restatement:
+//
+//   Copyright (c) 2009-2011, NVIDIA Corporation
+//   All rights reserved.
+//
+//   Redistribution and use in source and binary forms, with or without
+//   modification, are permitted provided that the following conditions are met:
+//       * Redistributions of source code must retain the above copyright
+//         notice, this list of conditions and the following disclaimer.
+//       * Redistributions in binary form must reproduce the above copyright
+//         notice, this list of conditions and the following disclaimer in the
+//         documentation and/or other materials provided with the distribution.
+//       * Neither the name of NVIDIA Corporation nor the
+//         names of its contributors may be used to endorse or promote products
+//         derived from this software without specific prior written permission.
+//
+//   THIS SOFTWARE IS PROVIDED BY THE COPYRIGHT HOLDERS AND CONTRIBUTORS "AS IS"
+//   AND ANY EXPRESS OR IMPLIED WARRANTIES, INCLUDING, BUT NOT LIMITED TO, THE
+//   IMPLIED WARRANTIES OF MERCHANTABILITY AND FITNESS FOR A PARTICULAR PURPOSE
+//   ARE DISCLAIMED. IN NO EVENT SHALL <COPYRIGHT HOLDER> BE LIABLE FOR ANY
+//   DIRECT, INDIRECT, INCIDENTAL, SPECIAL, EXEMPLARY, OR CONSEQUENTIAL DAMAGES
+//   (INCLUDING, BUT NOT LIMITED TO, PROCUREMENT OF SUBSTITUTE GOODS OR SERVICES;
+//   LOSS OF USE, DATA, OR PROFITS; OR BUSINESS INTERRUPTION) HOWEVER CAUSED AND
+//   ON ANY THEORY OF LIABILITY, WHETHER IN CONTRACT, STRICT LIABILITY, OR TORT
+//   (INCLUDING NEGLIGENCE OR OTHERWISE) ARISING IN ANY WAY OUT OF THE USE OF
+//   THIS SOFTWARE, EVEN IF ADVISED OF THE POSSIBILITY OF SUCH DAMAGE.
 #include "common.cuh"
 #include "svo_internal.h"
 
