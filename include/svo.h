@@ -84,7 +84,10 @@ typedef struct svo_camera {
  *   flags    bit0 hit; bits1-2 normal axis (0=x,1=y,2=z); bit3 normal points to -axis;
  *            bit4 the march was aborted (a child pointer outside the pool's range, an interior word
  *            below the octree level, or SVO_MARCH_MAX_ITER iterations): the pool is malformed and the
- *            ray counts as a miss.  A pool made by svo_build never sets it. */
+ *            ray counts as a miss.  A pool made by svo_build never sets it;
+ *            bit5 (beam march without a beam image only) the wait for one of the ray's tile's beam
+ *            texels gave up, so the ray was marched from the camera: apart from this bit its result is
+ *            svo_raycast_camera's.  A correct run never sets it. */
 typedef struct svo_hit {
 	float t;
 	float pos[3];
@@ -98,6 +101,7 @@ typedef struct svo_hit {
 #define SVO_HIT_NORMAL_AXIS(f) (((f) >> 1) & 3u)
 #define SVO_HIT_NORMAL_NEG 8u
 #define SVO_HIT_FLAG_ABORTED 16u
+#define SVO_HIT_FLAG_BEAM_WAIT 32u
 
 /* A voxel-fragment list (device memory). data holds `count` uint64 fragments: low word = fragment.x,
  * high word = fragment.y (the reference's uvec2 layout). */
@@ -145,6 +149,17 @@ const char *svo_last_error(void);
 const char *svo_version(void);
 /* Number of kernels this library launched since load (all devices); a cheap sanity counter for callers. */
 uint64_t svo_kernel_launches(void);
+/* Number of memory allocation calls (device, stream-ordered, pinned host, or through a caller's
+ * svo_allocator) this library made since load; lets a caller check that a path allocates nothing. */
+uint64_t svo_allocation_calls(void);
+/* Test hook for the failure path of the bounded device waits; no counterpart in the reference, whose
+ * shaders wait on nothing.  With spin_limit > 0 every wait of the single-pass scans (voxelize, build,
+ * textured compaction) and of the fused beam march gives up after spin_limit iterations, and the scan tile
+ * or beam texel numbered `withheld` never publishes its value, so the waits on it run out: scans then
+ * report SVO_ERR_TIMEOUT (no later stage writes through their offsets) and beam marches set
+ * SVO_HIT_FLAG_BEAM_WAIT on the rays concerned.  spin_limit = 0 restores the defaults.  It applies to the
+ * current device, process-wide, to calls launched after it returns; not for production use. */
+int svo_debug_wait_fault(uint32_t spin_limit, uint32_t withheld);
 
 /* Device memory and transfers for callers without the CUDA headers (C, C++, FFI bindings).  Allocation
  * is stream-ordered (freed memory stays pooled for reuse); copies are asynchronous on `stream` except
@@ -410,6 +425,7 @@ typedef struct svo_server_stats {
 	uint64_t rays;                      /* hits produced */
 	uint64_t rebuilds;
 	uint64_t resident_bytes, inflight_bytes, pending;
+	uint64_t node_fetches;              /* node words the served rays read (the march's memory traffic) */
 } svo_server_stats;
 
 int svo_server_create(const svo_server_config *cfg, svo_server **out);

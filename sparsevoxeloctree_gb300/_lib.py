@@ -73,7 +73,7 @@ class RequestResult(ctypes.Structure):
 
 class ServerStats(ctypes.Structure):
     _fields_ = [(n, u64) for n in ("submitted", "completed", "failed", "batches", "batched_requests", "rays",
-                                   "rebuilds", "resident_bytes", "inflight_bytes", "pending")]
+                                   "rebuilds", "resident_bytes", "inflight_bytes", "pending", "node_fetches")]
 
 
 SVO_REQUEST_CAMERA, SVO_REQUEST_RAYS = 0, 1
@@ -90,6 +90,8 @@ _SIGNATURES = {
     "svo_last_error": ([], ctypes.c_char_p),
     "svo_version": ([], ctypes.c_char_p),
     "svo_kernel_launches": ([], u64),
+    "svo_allocation_calls": ([], u64),
+    "svo_debug_wait_fault": ([u32, u32], i32),
     "svo_device_alloc": ([ctypes.POINTER(P), sz, P], i32),
     "svo_device_free": ([P, P], None),
     "svo_upload": ([P, P, sz, P], i32),

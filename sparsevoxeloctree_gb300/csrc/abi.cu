@@ -16,6 +16,8 @@ namespace svo {
 
 static std::atomic<uint64_t> g_launches{0};
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+static std::atomic<uint64_t> g_allocations{0};
+void note_allocation() { g_allocations.fetch_add(1, std::memory_order_relaxed); }
 
 static thread_local std::string g_error;
 
@@ -163,7 +165,7 @@ static void prepare_pool() {
 
 template <typename T> static cudaError_t alloc_async(T **p, size_t bytes, cudaStream_t s) {
 	prepare_pool();
-	return cudaMallocAsync((void **)p, bytes ? bytes : 16, s);
+	return counted_malloc_async(p, bytes ? bytes : 16, s);
 }
 
 static bool aligned(const void *p, size_t a) { return ((uintptr_t)p % a) == 0; }
@@ -174,6 +176,7 @@ struct Mem {
 	cudaStream_t s;
 	cudaError_t get(void **p, size_t bytes) {
 		if (a && a->alloc) {
+			note_allocation();
 			*p = a->alloc(a->user, bytes ? bytes : 16);
 			return *p ? cudaSuccess : cudaErrorMemoryAllocation;
 		}
@@ -310,6 +313,16 @@ void svo_tune_reset(void) {
 			for (uint32_t c = 0; c < kTuneClasses; ++c) g_tune[p][l][c].store(kTuneDefault[p]);
 }
 uint64_t svo_kernel_launches(void) { return g_launches.load(); }
+uint64_t svo_allocation_calls(void) { return g_allocations.load(); }
+
+int svo_debug_wait_fault(uint32_t spin_limit, uint32_t withheld) {
+	cudaError_t e = vox_set_wait_fault(spin_limit, withheld);
+	if (e == cudaSuccess) e = build_set_wait_fault(spin_limit, withheld);
+	if (e == cudaSuccess) e = march_set_wait_fault(spin_limit, withheld);
+	if (e == cudaSuccess) e = texture_set_wait_fault(spin_limit, withheld);
+	if (e != cudaSuccess) return cuda_fail(e, "wait-fault hook");
+	return SVO_OK;
+}
 
 // ------------------------------------------------------------------------------------------ voxelize
 static int check_tris(const svo_triangle *tris, uint32_t n) {

@@ -30,7 +30,7 @@ struct DevArena {
 		ptr = nullptr;
 		cap = 0;
 		const size_t want = bytes + bytes / 4 + 4096;
-		cudaError_t e = cudaMalloc(&ptr, want);
+		cudaError_t e = counted_malloc(&ptr, want);
 		if (e != cudaSuccess) {
 			ptr = nullptr;
 			return e;
@@ -54,7 +54,7 @@ struct HostArena {
 		ptr = nullptr;
 		cap = 0;
 		const size_t want = bytes + bytes / 4 + 4096;
-		cudaError_t e = cudaMallocHost(&ptr, want);
+		cudaError_t e = counted_malloc_host(&ptr, want);
 		if (e != cudaSuccess) {
 			ptr = nullptr;
 			return e;

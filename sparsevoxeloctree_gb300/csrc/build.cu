@@ -388,6 +388,7 @@ template <bool B> __global__ void dense_finish(BuildBatch bb) {
 // blocks whole.  One bitmap word and one prefix word of the child depth serve all 8 children.
 template <bool B>
 __global__ void __launch_bounds__(kTPB) dense_write(BuildBatch bb, uint32_t total_items) {
+	if (bb.gstate->status & kStatusAbort) return; // the prefix is not a complete scan: write nothing
 	for (uint32_t gitem = blockIdx.x * blockDim.x + threadIdx.x; gitem < total_items; gitem += gridDim.x * blockDim.x) {
 		const uint32_t mi = B ? mesh_search(bb.item_base, bb.M, gitem) : 0u;
 		const BuildMesh md = mesh_at<B>(bb, mi);
@@ -484,7 +485,7 @@ __global__ void __launch_bounds__(kTPB) build_tag(const uint64_t *__restrict__ f
 // of a node is zeroed (the next depth's init) unless the next depth is the leaf depth.
 __global__ void __launch_bounds__(kTPB) build_alloc(uint32_t *__restrict__ pool, uint64_t capacity, uint32_t depth,
                                                     uint32_t level, BuildState *state, unsigned long long *descs,
-                                                    const BuildState *gstate) {
+                                                    BuildState *gstate) {
 	__shared__ uint32_t s_tile;
 	__shared__ uint32_t s_warp[kTPB / 32 + 1];
 	__shared__ uint32_t s_prefix;
@@ -530,7 +531,8 @@ __global__ void __launch_bounds__(kTPB) build_alloc(uint32_t *__restrict__ pool,
 		uint32_t total;
 		const uint32_t rank0 = block_exclusive_sum<uint32_t, kTPB>(cnt, s_warp, total);
 		if (threadIdx.x < 32) {
-			const uint32_t p = (uint32_t)tile_lookback_warp(descs, tile, depth, total, &state->status);
+			// a timeout goes to the batch-wide status, which every later stage of every mesh checks
+			const uint32_t p = (uint32_t)tile_lookback_warp(descs, tile, depth, total, &gstate->status);
 			if (threadIdx.x == 0) s_prefix = p;
 		}
 		__syncthreads();
@@ -777,7 +779,7 @@ template <bool B> __global__ void __launch_bounds__(kTPB) leaf_window_scan(Build
 	for (uint32_t base = 0; base < M; base += kTPB) {
 		const uint32_t mi = base + threadIdx.x;
 		uint32_t c = 0;
-		if (mi < M) {
+		if (mi < M && !(bb.gstate->status & kStatusAbort)) { // no windows after an aborted scan
 			const BuildMesh md = mesh_at<B>(bb, mi);
 			c = (md.state->lv[md.level].num + kLeafSlots - 1) >> kWinBits;
 		}
@@ -796,7 +798,8 @@ template <bool B> __global__ void __launch_bounds__(kTPB) leaf_window_scan(Build
 template <bool B>
 __global__ void bucket_meta(BuildBatch bb, const uint32_t *__restrict__ boff, const uint32_t *__restrict__ blist,
                             const BuildState *gstate, uint4 *__restrict__ meta) {
-	const uint32_t nbuckets = gstate->buckets;
+	// after an aborted scan the bucket list may hold entries no tile wrote: nothing is read through it
+	const uint32_t nbuckets = (gstate->status & kStatusAbort) ? 0u : gstate->buckets;
 	for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nbuckets; t += gridDim.x * blockDim.x) {
 		const uint32_t b = blist[t];
 		const uint32_t mi = B ? mesh_search(bb.bucket_base, bb.M, b) : 0u;
@@ -826,7 +829,7 @@ __global__ void __launch_bounds__(kTPB) bucket_span_sparse(const uint64_t *__res
                                                            const uint32_t *__restrict__ blist,
                                                            const uint32_t *__restrict__ cache,
                                                            const BuildState *gstate, uint4 *__restrict__ meta) {
-	const uint32_t nbuckets = gstate->buckets, lane = lane_id();
+	const uint32_t nbuckets = (gstate->status & kStatusAbort) ? 0u : gstate->buckets, lane = lane_id();
 	const uint32_t warps = gridDim.x * (blockDim.x / 32);
 	for (uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) / 32; t < nbuckets; t += warps) {
 		const uint32_t mi = B ? mesh_search(bb.bucket_base, bb.M, blist[t]) : 0u;
@@ -862,7 +865,7 @@ template <bool B>
 __global__ void bucket_windows(BuildBatch bb, const uint32_t *__restrict__ blist, const BuildState *gstate,
                                const uint4 *__restrict__ meta, const uint32_t *__restrict__ win_base,
                                uint32_t *__restrict__ wfirst, uint32_t *__restrict__ wlast) {
-	const uint32_t nbuckets = gstate->buckets;
+	const uint32_t nbuckets = (gstate->status & kStatusAbort) ? 0u : gstate->buckets; // as in bucket_meta
 	for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nbuckets; t += gridDim.x * blockDim.x) {
 		const uint32_t mi = B ? mesh_search(bb.bucket_base, bb.M, blist[t]) : 0u;
 		const uint32_t b_lo = B ? __ldg(bb.bucket_base + mi) : 0u, b_hi = B ? __ldg(bb.bucket_base + mi + 1) : bb.one.nb;
@@ -972,6 +975,7 @@ __global__ void __launch_bounds__(kTPB) build_leaf_windows(const uint64_t *__res
 	extern __shared__ unsigned long long s_acc[];
 	__shared__ uint32_t s_over, s_leaves, s_skip;
 	const uint32_t M = batch_size<B>(bb);
+	if (gstate->status & kStatusAbort) return; // no window bookkeeping was made (leaf_window_scan)
 	const uint32_t total = win_base[M], nbuckets = gstate->buckets;
 	for (uint32_t gw = blockIdx.x; gw < total; gw += gridDim.x) {
 		const uint32_t mi = B ? mesh_search(win_base, M, gw) : 0u;
@@ -1044,6 +1048,8 @@ template <bool B> __global__ void build_export(BuildBatch bb, const BuildState *
 }
 
 // ------------------------------------------------------------------------------------------ host side
+cudaError_t build_set_wait_fault(uint32_t limit, uint32_t withheld) { return set_wait_fault_here(limit, withheld); }
+
 uint64_t build_pool_bound(uint32_t count, uint32_t level) {
 	uint64_t words = 8, per = 1;
 	for (uint32_t i = 1; i < level; ++i) {
@@ -1219,7 +1225,7 @@ static void launch_dense_and_scatter(const uint64_t *frags, uint64_t n, uint32_t
 
 static void launch_sparse(const uint64_t *sorted, uint32_t count, uint32_t level, const DenseView &dv, uint32_t *pool,
                           uint64_t capacity, uint32_t *cache, BuildState *state, unsigned long long *descs,
-                          const BuildState *gstate, cudaStream_t stream) {
+                          BuildState *gstate, cudaStream_t stream) {
 	const int sms = device_sm_count();
 	const uint32_t tag_blocks =
 	    grid_for(((uint64_t)count + 3) / 4, kTPB, (uint32_t)sms * (uint32_t)tune_value(kTuneSweepBlocks, level, count));

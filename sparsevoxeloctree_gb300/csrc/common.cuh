@@ -18,6 +18,20 @@ constexpr unsigned kFullMask = 0xffffffffu;
 // against a broken invariant and is never reached in a correct run.
 constexpr uint32_t kSpinLimit = 1u << 22;
 
+// Test hook of the bounded waits (svo_debug_wait_fault): `limit` bounds every wait's iterations, and the
+// look-back tile or beam texel numbered `withheld` never publishes, so the waits on it run out and take
+// their timeout path (a status bit, never a trap).  The defaults, kSpinLimit and no tile, leave the
+// kernels' behaviour unchanged.  Each translation unit holds its own copy, set by its own setter.
+struct WaitFault {
+	uint32_t limit;
+	uint32_t withheld;
+};
+static __constant__ WaitFault c_wait_fault = {kSpinLimit, 0xffffffffu};
+static inline cudaError_t set_wait_fault_here(uint32_t limit, uint32_t withheld) {
+	const WaitFault f = {limit ? limit : kSpinLimit, limit ? withheld : 0xffffffffu};
+	return cudaMemcpyToSymbol(c_wait_fault, &f, sizeof(f));
+}
+
 // ------------------------------------------------------------------------------- warp / block scans
 SVO_DEV uint32_t lane_id() { return threadIdx.x & 31u; }
 
@@ -98,17 +112,21 @@ SVO_DEV unsigned long long desc_load(const unsigned long long *d) {
 // Decoupled look-back for tile `t` once its aggregate is known, called by all 32 lanes of one warp:
 // each step inspects the 32 nearest unexamined predecessors at once and sums their aggregates up to
 // the nearest inclusive prefix.  Returns the tile's exclusive prefix on every lane.  Waits are bounded
-// (kSpinLimit); on timeout the status word gets kStatusTimeout.  A tile with seg_start set begins a
+// (c_wait_fault.limit, kSpinLimit unless a test lowers it); on timeout the status word gets kStatusTimeout
+// and the returned prefix is a partial sum of published aggregates, never above the true prefix, so
+// offsets derived from it stay inside the buffers their totals size.  A tile with seg_start set begins a
 // new segment (a segmented scan): its prefix is 0, and the look-back of later tiles stops there.
 SVO_DEV unsigned long long tile_lookback_warp(unsigned long long *descs, uint32_t t, uint32_t epoch,
                                               unsigned long long aggregate, uint32_t *status,
                                               bool seg_start = false) {
 	const uint32_t lane = lane_id();
+	const WaitFault wf = c_wait_fault;
+	const bool publish = t != wf.withheld;
 	if (t == 0 || seg_start) {
-		if (lane == 0) desc_publish(&descs[t], epoch, 2, aggregate);
+		if (lane == 0 && publish) desc_publish(&descs[t], epoch, 2, aggregate);
 		return 0;
 	}
-	if (lane == 0) desc_publish(&descs[t], epoch, 1, aggregate);
+	if (lane == 0 && publish) desc_publish(&descs[t], epoch, 1, aggregate);
 	unsigned long long prefix = 0;
 	int64_t end = (int64_t)t - 1; // window: descriptors end, end-1, ..., end-31 (lane k reads end-k)
 	uint32_t spins = 0;
@@ -124,7 +142,7 @@ SVO_DEV unsigned long long tile_lookback_warp(unsigned long long *descs, uint32_
 		const uint32_t first = incl ? (uint32_t)(__ffs(incl) - 1) : 31u;
 		const uint32_t need = first == 31u ? kFullMask : ((2u << first) - 1u);
 		if (__ballot_sync(kFullMask, flag == 0) & need) { // a needed predecessor has not published yet
-			if (++spins > kSpinLimit) {
+			if (++spins > wf.limit) { // prefix stays a partial sum of real aggregates: below the true one
 				if (lane == 0) atomicOr(status, kStatusTimeout);
 				break;
 			}
@@ -135,7 +153,7 @@ SVO_DEV unsigned long long tile_lookback_warp(unsigned long long *descs, uint32_
 		if (incl) break;
 		end -= 32;
 	}
-	if (lane == 0) desc_publish(&descs[t], epoch, 2, prefix + aggregate);
+	if (lane == 0 && publish) desc_publish(&descs[t], epoch, 2, prefix + aggregate);
 	return prefix;
 }
 

@@ -297,7 +297,7 @@ int svo_octree_load(const char *path, svo_octree *out, void *stream) {
 	int rc = svo_octree_read_host(path, &w, &range, &level);
 	if (rc) return rc;
 	void *dev = nullptr;
-	cudaError_t e = cudaMallocAsync(&dev, (size_t)range * 4, (cudaStream_t)stream);
+	cudaError_t e = counted_malloc_async(&dev, (size_t)range * 4, (cudaStream_t)stream);
 	if (e == cudaSuccess) e = cudaMemcpyAsync(dev, w, (size_t)range * 4, cudaMemcpyHostToDevice, (cudaStream_t)stream);
 	if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream); // the host copy is freed next
 	free(w);

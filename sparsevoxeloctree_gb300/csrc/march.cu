@@ -629,7 +629,7 @@ __global__ void __launch_bounds__(kMarchTPB) march_beam_fused_kernel(MarchArgs a
 		if (base >= slots) break;
 		if (base < texel_slots) {
 			const uint64_t i = base + lane;
-			if (i < texels) {
+			if (i < texels && i != c_wait_fault.withheld) { // (a test may withhold one texel)
 				const float v = beam_texel(a, (uint32_t)i, bw, orig_sz, stack);
 				asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(beam + i), "r"(__float_as_uint(v)) : "memory");
 			}
@@ -641,22 +641,27 @@ __global__ void __launch_bounds__(kMarchTPB) march_beam_fused_kernel(MarchArgs a
 		const uint32_t x = tx * 8u + (in & 7u), y = ty * 4u + (in >> 3);
 		// lanes 0..3 fetch texels (bx, by), (bx + 1, by), (bx, by + 1), (bx + 1, by + 1) of the beam tile
 		float tv = 0.0f;
+		bool gave_up = false;
 		if (lane < 4) {
 			const uint32_t bx = tx * 8u / kBeamSize, by = ty * 4u / kBeamSize;
 			const float *p = beam + (size_t)(by + (lane >> 1)) * bw + bx + (lane & 1u);
+			const uint32_t limit = c_wait_fault.limit;
 			uint32_t w, spins = 0;
 			for (;;) {
 				asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(w) : "l"(p) : "memory");
 				if (w != kBeamUnset) break;
-				if (++spins > kSpinLimit) { // a texel that never came: report, march from the camera
+				if (++spins > limit) { // a texel that never came: report, march from the camera
 					atomicOr(a.status, kStatusTimeout);
 					w = 0u;
+					gave_up = true;
 					break;
 				}
 				__nanosleep(64);
 			}
 			tv = __uint_as_float(w);
 		}
+		// a tile whose wait gave up marches from the camera (start distance 0) and flags its rays
+		const uint32_t waited_out = __any_sync(kFullMask, gave_up) ? (SVO_HIT_FLAG_BEAM_WAIT << 16) : 0u;
 		const float t00 = __shfl_sync(kFullMask, tv, 0), t01 = __shfl_sync(kFullMask, tv, 1);
 		const float t10 = __shfl_sync(kFullMask, tv, 2), t11 = __shfl_sync(kFullMask, tv, 3);
 		const float m = min_glsl(min_glsl(t00, t01), min_glsl(t10, t11));
@@ -669,6 +674,7 @@ __global__ void __launch_bounds__(kMarchTPB) march_beam_fused_kernel(MarchArgs a
 			MarchOut mo;
 			uint32_t nf;
 			march_ray<kMarchTPB>(a.pool, a.range, a.level, o, d, stack, mo, nf, a.status);
+			mo.voxel_hi |= waited_out;
 			store_hit(a.hits, r, mo);
 			fetched += nf;
 		}
@@ -1183,10 +1189,11 @@ SVO_DEV uint32_t job_of(const MarchJob *__restrict__ jobs, uint32_t njobs, uint6
 
 __global__ void __launch_bounds__(kMarchTPB) march_jobs_kernel(const MarchJob *__restrict__ jobs, uint32_t njobs,
                                                                 uint64_t total, unsigned long long *ticket,
-                                                                uint32_t *status) {
+                                                                uint32_t *status, unsigned long long *fetches) {
 	__shared__ uint32_t s_stack[SVO_LEVEL_MAX * kMarchTPB];
 	uint32_t *stack = s_stack + threadIdx.x;
 	const uint32_t lane = lane_id();
+	unsigned long long fetched = 0;
 	for (;;) {
 		unsigned long long base = 0;
 		if (lane == 0) base = atomicAdd(ticket, 32ull);
@@ -1216,9 +1223,14 @@ __global__ void __launch_bounds__(kMarchTPB) march_jobs_kernel(const MarchJob *_
 		if (live) {
 			MarchOut m;
 			uint32_t nf;
-			march_ray<kMarchTPB>(J.pool, J.range, J.level, o, d, stack, m, nf, status);
+			march_ray<kMarchTPB>(J.pool, J.range, J.level, o, d, stack, m, nf, status + J.req);
 			store_hit(J.hits, r, m);
+			fetched += nf;
 		}
+	}
+	if (fetches) {
+		fetched = warp_sum(fetched);
+		if (lane == 0 && fetched) atomicAdd(fetches, fetched);
 	}
 }
 
@@ -1313,13 +1325,13 @@ uint64_t march_job_slots(const MarchJob &j) {
 }
 
 cudaError_t march_jobs_launch(const MarchJob *jobs, uint32_t njobs, uint64_t total, unsigned long long *ticket,
-                              uint32_t *status, cudaStream_t stream) {
+                              uint32_t *status, unsigned long long *fetches, cudaStream_t stream) {
 	cudaError_t e = cudaMemsetAsync(ticket, 0, sizeof(unsigned long long), stream);
 	if (e != cudaSuccess || total == 0 || njobs == 0) return e;
 	const int sms = device_sm_count();
 	const uint64_t blocks_needed = (total / 32 + kMarchTPB / 32 - 1) / (kMarchTPB / 32);
 	const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(blocks_needed, (uint64_t)sms * 16));
-	SVO_LAUNCH("march_jobs", stream, march_jobs_kernel<<<blocks, kMarchTPB, 0, stream>>>(jobs, njobs, total, ticket, status););
+	SVO_LAUNCH("march_jobs", stream, march_jobs_kernel<<<blocks, kMarchTPB, 0, stream>>>(jobs, njobs, total, ticket, status, fetches););
 	return cudaGetLastError();
 }
 
@@ -1344,6 +1356,8 @@ cudaError_t beam_launch(const MarchArgs &a, float *beam, cudaStream_t stream) {
 	SVO_LAUNCH("beam_prepass", stream, beam_kernel<<<blocks, kMarchTPB, 0, stream>>>(a, beam, orig_sz););
 	return cudaGetLastError();
 }
+
+cudaError_t march_set_wait_fault(uint32_t limit, uint32_t withheld) { return set_wait_fault_here(limit, withheld); }
 
 cudaError_t march_beam_fused_launch(const MarchArgs &a, float *beam, cudaStream_t stream) {
 	const uint64_t texels = (uint64_t)((a.width + kBeamSize - 1) / kBeamSize + 1) * ((a.height + kBeamSize - 1) / kBeamSize + 1);

@@ -11,6 +11,8 @@
 #include <cstring>
 #include <mutex>
 
+#include <cuda.h>
+
 #include "svo_internal.h"
 
 namespace svo {
@@ -34,23 +36,60 @@ static uint64_t static_unit_cap(uint32_t n) {
 static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
 
 constexpr int kMaxDevices = 64;
-static void *g_scratch_addr[kMaxDevices];
+struct ScratchAddr {
+	unsigned long long ctx_id; // the driver's unique id of the context the address belongs to (0 = none)
+	void *ptr;
+};
+static ScratchAddr g_scratch_addr[kMaxDevices];
 static std::mutex g_scratch_mu;
 
-// Device address of g_static_scratch on the current device, looked up once per device.
+// Unique id of the calling thread's current context (never reused within a process, so a context
+// re-created after cudaDeviceReset gets a new one), through the driver entry points the runtime hands
+// out; 0 when there is no current context or the driver lacks the calls.
+static unsigned long long current_context_id() {
+	using GetCurrentFn = CUresult (*)(CUcontext *);
+	using GetIdFn = CUresult (*)(CUcontext, unsigned long long *);
+	static GetCurrentFn get_current = nullptr;
+	static GetIdFn get_id = nullptr;
+	static std::once_flag once;
+	std::call_once(once, [] {
+		cudaDriverEntryPointQueryResult q;
+		void *f = nullptr;
+		if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+		    q == cudaDriverEntryPointSuccess)
+			get_current = (GetCurrentFn)f;
+		f = nullptr;
+		if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+		    q == cudaDriverEntryPointSuccess)
+			get_id = (GetIdFn)f;
+	});
+	CUcontext ctx = nullptr;
+	unsigned long long id = 0;
+	if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS)
+		return 0;
+	return id;
+}
+
+// Device address of g_static_scratch in the current device's context, looked up with the device
+// current the first time a context uses it, and again whenever that context has been replaced (after a
+// cudaDeviceReset the module is loaded anew and the array may move).  In host code the array's name
+// only stands in for it; kernels must be given this address.
 static cudaError_t static_scratch(void **out) {
 	int dev = 0;
 	cudaError_t e = cudaGetDevice(&dev);
 	if (e != cudaSuccess) return e;
 	if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
 	std::lock_guard<std::mutex> lk(g_scratch_mu);
-	if (!g_scratch_addr[dev]) {
+	const unsigned long long id = current_context_id();
+	ScratchAddr &c = g_scratch_addr[dev];
+	if (!c.ptr || id == 0 || c.ctx_id != id) {
 		void *p = nullptr;
-		e = cudaGetSymbolAddress(&p, g_static_scratch);
+		e = cudaGetSymbolAddress(&p, g_static_scratch); // also brings up the device's context if needed
 		if (e != cudaSuccess) return e;
-		g_scratch_addr[dev] = p;
+		c.ptr = p;
+		c.ctx_id = id ? id : current_context_id();
 	}
-	*out = g_scratch_addr[dev];
+	*out = c.ptr;
 	return cudaSuccess;
 }
 

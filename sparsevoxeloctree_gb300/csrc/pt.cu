@@ -185,8 +185,8 @@ int svo_envmap_create(const float *rgba, uint32_t width, uint32_t height, svo_en
 	}
 	e->table.resize(2 * n);
 	envmap_alias(weights, e->table.data());
-	cudaError_t err = cudaMalloc(&e->texels, n * sizeof(float4));
-	if (err == cudaSuccess) err = cudaMalloc(&e->alias, n * sizeof(uint2));
+	cudaError_t err = counted_malloc(&e->texels, n * sizeof(float4));
+	if (err == cudaSuccess) err = counted_malloc(&e->alias, n * sizeof(uint2));
 	if (err == cudaSuccess) err = cudaMemcpy(e->texels, e->rgba.data(), n * sizeof(float4), cudaMemcpyHostToDevice);
 	if (err == cudaSuccess) err = cudaMemcpy(e->alias, e->table.data(), n * sizeof(uint2), cudaMemcpyHostToDevice);
 	if (err != cudaSuccess) {
@@ -245,11 +245,11 @@ int svo_path_tracer_reset(svo_path_tracer *pt, uint32_t width, uint32_t height, 
 		cudaFree(pt->paths);
 		cudaFree(pt->queue);
 		pt->color = nullptr, pt->albedo = pt->normal = nullptr, pt->paths = nullptr, pt->queue = nullptr;
-		PT_CK(cudaMalloc(&pt->color, n * sizeof(float4)), "path tracer targets");
-		PT_CK(cudaMalloc(&pt->albedo, n * sizeof(uint32_t)), "path tracer targets");
-		PT_CK(cudaMalloc(&pt->normal, n * sizeof(uint32_t)), "path tracer targets");
-		PT_CK(cudaMalloc(&pt->paths, n * sizeof(PathState)), "path state");
-		PT_CK(cudaMalloc(&pt->queue, 2 * n * sizeof(uint32_t)), "path queues");
+		PT_CK(counted_malloc(&pt->color, n * sizeof(float4)), "path tracer targets");
+		PT_CK(counted_malloc(&pt->albedo, n * sizeof(uint32_t)), "path tracer targets");
+		PT_CK(counted_malloc(&pt->normal, n * sizeof(uint32_t)), "path tracer targets");
+		PT_CK(counted_malloc(&pt->paths, n * sizeof(PathState)), "path state");
+		PT_CK(counted_malloc(&pt->queue, 2 * n * sizeof(uint32_t)), "path queues");
 	}
 	pt->width = width, pt->height = height, pt->bounce = bounce, pt->spp = 0;
 	PT_CK(cudaMemsetAsync(pt->color, 0, n * sizeof(float4), s), "path tracer clear");
@@ -277,11 +277,11 @@ int svo_path_tracer_create(uint32_t width, uint32_t height, uint32_t bounce, svo
 		const uint64_t z = splitmix64(rng);
 		for (size_t b = 0; b < 8; ++b) noise[i + b] = (uint8_t)(z >> (8 * b));
 	}
-	cudaError_t e = cudaMalloc(&pt->sobol, kSobolWords * sizeof(uint32_t));
-	if (e == cudaSuccess) e = cudaMalloc(&pt->matrices, m.size() * sizeof(uint32_t));
-	if (e == cudaSuccess) e = cudaMalloc(&pt->noise, noise.size());
-	if (e == cudaSuccess) e = cudaMalloc(&pt->scratch, 2 * sizeof(unsigned long long));
-	if (e == cudaSuccess) e = cudaMalloc(&pt->wave, kPtScratchBytes);
+	cudaError_t e = counted_malloc(&pt->sobol, kSobolWords * sizeof(uint32_t));
+	if (e == cudaSuccess) e = counted_malloc(&pt->matrices, m.size() * sizeof(uint32_t));
+	if (e == cudaSuccess) e = counted_malloc(&pt->noise, noise.size());
+	if (e == cudaSuccess) e = counted_malloc(&pt->scratch, 2 * sizeof(unsigned long long));
+	if (e == cudaSuccess) e = counted_malloc(&pt->wave, kPtScratchBytes);
 	if (e == cudaSuccess) e = cudaMemcpy(pt->matrices, m.data(), m.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
 	if (e == cudaSuccess) e = cudaMemcpy(pt->noise, noise.data(), noise.size(), cudaMemcpyHostToDevice);
 	if (e != cudaSuccess) {

@@ -73,7 +73,7 @@ struct Lane {
 	uint64_t bytes = 0;
 	void *arena = nullptr;
 	size_t arena_cap = 0;
-	char *staging = nullptr; // pinned: job tables and the status word
+	char *staging = nullptr; // pinned: the batch's node-fetch count and one status word per request, then the job tables
 	size_t staging_cap = 0;
 	std::condition_variable cv;
 	std::thread waiter;
@@ -105,12 +105,15 @@ struct Server {
 
 static uint64_t scene_bytes(const svo_octree &o) { return (uint64_t)o.capacity * 4; }
 
-// Retires a completed batch (lock held).
+// Retires a completed batch (lock held).  Each request has its own status word, so a malformed pool
+// (a scene added from a damaged file, say) fails only the requests that traced it.
 static void retire(Server *S, Lane &L, double t) {
-	const uint32_t status = *reinterpret_cast<const uint32_t *>(L.staging);
-	for (Req *r : L.reqs) {
+	S->st.node_fetches += *reinterpret_cast<const unsigned long long *>(L.staging);
+	const uint32_t *status = reinterpret_cast<const uint32_t *>(L.staging + 8);
+	for (size_t i = 0; i < L.reqs.size(); ++i) {
+		Req *r = L.reqs[i];
 		r->t_done = t;
-		if (status & kStatusMalformed) {
+		if (status[i] & kStatusMalformed) {
 			r->status = SVO_ERR_INVALID;
 			r->error = "malformed octree pool";
 			++S->st.failed;
@@ -151,7 +154,7 @@ static cudaError_t grow_device(void **p, size_t *cap, size_t need, cudaStream_t 
 	*p = nullptr;
 	*cap = 0;
 	const size_t want = need + need / 4 + 65536;
-	cudaError_t e = cudaMallocAsync(p, want, s);
+	cudaError_t e = counted_malloc_async(p, want, s);
 	if (e == cudaSuccess) *cap = want;
 	return e;
 }
@@ -170,8 +173,8 @@ static cudaError_t issue(Server *S, Lane &L) {
 	const size_t o_jobs2 = off;
 	off = align256(off + sizeof(MarchJob) * ncam);
 	const size_t table_bytes = off;
-	const size_t o_ticket = off;
-	off = align256(off + 16);
+	const size_t o_ticket = off; // the ticket (8 B), the node-fetch count (8 B), one status word per request
+	off = align256(off + 16 + 4 * nb);
 	std::vector<size_t> o_hits(nb), o_rays(nb);
 	for (size_t i = 0; i < nb; ++i) {
 		const svo_trace_request &t = batch[i]->tr;
@@ -183,15 +186,16 @@ static cudaError_t issue(Server *S, Lane &L) {
 	}
 	cudaError_t e = grow_device(&L.arena, &L.arena_cap, off, L.s);
 	if (e != cudaSuccess) return e;
-	if (table_bytes + 256 > L.staging_cap) {
+	const size_t status_bytes = align256(8 + 4 * nb); // the fetch count and the status words, read back
+	if (table_bytes + status_bytes > L.staging_cap) {
 		if (L.staging) cudaFreeHost(L.staging);
 		L.staging = nullptr;
 		L.staging_cap = 0;
-		e = cudaMallocHost((void **)&L.staging, table_bytes + 256 + 4096);
+		e = counted_malloc_host((void **)&L.staging, table_bytes + status_bytes + 4096);
 		if (e != cudaSuccess) return e;
-		L.staging_cap = table_bytes + 256 + 4096;
+		L.staging_cap = table_bytes + status_bytes + 4096;
 	}
-	char *dev = (char *)L.arena, *host = L.staging + 256; // staging[0..4) = the status word
+	char *dev = (char *)L.arena, *host = L.staging + status_bytes; // staging: fetch count, status words
 	MarchJob *j1 = (MarchJob *)(host + o_jobs1), *j2 = (MarchJob *)(host + o_jobs2);
 	BounceJob *bj = (BounceJob *)(host + o_bjobs);
 	uint64_t slots1 = 0, slots2 = 0, nbounce = 0;
@@ -212,6 +216,7 @@ static cudaError_t issue(Server *S, Lane &L) {
 		j.range = o.range_words;
 		j.level = o.level;
 		j.hits = hits_mapped[i] && t.mode == SVO_REQUEST_RAYS ? hits_mapped[i] : (svo_hit *)(dev + o_hits[i]);
+		j.req = (uint32_t)i;
 		if (t.mode == SVO_REQUEST_CAMERA) {
 			j.rays = nullptr;
 			j.cam = t.camera;
@@ -243,24 +248,26 @@ static cudaError_t issue(Server *S, Lane &L) {
 		}
 	}
 	unsigned long long *ticket = (unsigned long long *)(dev + o_ticket);
-	uint32_t *status = (uint32_t *)(ticket + 1);
+	unsigned long long *fetches = ticket + 1;
+	uint32_t *status = (uint32_t *)(ticket + 2);
 	e = cudaMemcpyAsync(dev, host, table_bytes, cudaMemcpyHostToDevice, L.s);
-	if (e == cudaSuccess) e = cudaMemsetAsync(status, 0, 4, L.s);
+	if (e == cudaSuccess) e = cudaMemsetAsync(fetches, 0, 8 + 4 * nb, L.s);
 	for (size_t i = 0; i < nb && e == cudaSuccess; ++i)
 		if (batch[i]->tr.mode == SVO_REQUEST_RAYS)
 			e = cudaMemcpyAsync(dev + o_rays[i], batch[i]->tr.rays, sizeof(svo_ray) * batch[i]->tr.n_rays,
 			                    cudaMemcpyHostToDevice, L.s);
-	if (e == cudaSuccess) e = march_jobs_launch((const MarchJob *)(dev + o_jobs1), (uint32_t)nb, slots1, ticket, status, L.s);
+	if (e == cudaSuccess)
+		e = march_jobs_launch((const MarchJob *)(dev + o_jobs1), (uint32_t)nb, slots1, ticket, status, fetches, L.s);
 	if (e == cudaSuccess && ncam) e = bounce_jobs_launch((const BounceJob *)(dev + o_bjobs), ncam, nbounce, L.s);
 	if (e == cudaSuccess && ncam)
-		e = march_jobs_launch((const MarchJob *)(dev + o_jobs2), ncam, slots2, ticket, status, L.s);
+		e = march_jobs_launch((const MarchJob *)(dev + o_jobs2), ncam, slots2, ticket, status, fetches, L.s);
 	for (size_t i = 0; i < nb && e == cudaSuccess; ++i) {
 		const svo_trace_request &t = batch[i]->tr;
 		// mapped: nothing for rays requests, the primary half for camera requests
 		const uint64_t n = !hits_mapped[i] ? batch[i]->hits : (t.mode == SVO_REQUEST_CAMERA ? t.n_primary : 0);
 		if (n) e = cudaMemcpyAsync(t.hits, dev + o_hits[i], sizeof(svo_hit) * n, cudaMemcpyDeviceToHost, L.s);
 	}
-	if (e == cudaSuccess) e = cudaMemcpyAsync(L.staging, status, 4, cudaMemcpyDeviceToHost, L.s);
+	if (e == cudaSuccess) e = cudaMemcpyAsync(L.staging, fetches, 8 + 4 * nb, cudaMemcpyDeviceToHost, L.s);
 	if (e == cudaSuccess) e = cudaEventRecord(L.done, L.s);
 	return e;
 }
@@ -361,7 +368,7 @@ static int build_scene(const svo_triangle *tris, uint32_t n, uint32_t level, cud
 	if (rc) return rc;
 	void *exact = nullptr;
 	const uint32_t range = o.range_words;
-	cudaError_t e = cudaMallocAsync(&exact, (size_t)range * 4, s);
+	cudaError_t e = counted_malloc_async(&exact, (size_t)range * 4, s);
 	if (e == cudaSuccess) e = cudaMemcpyAsync(exact, o.words, (size_t)range * 4, cudaMemcpyDeviceToDevice, s);
 	if (e == cudaSuccess) e = cudaStreamSynchronize(s);
 	svo_octree_destroy(&o, s); // (clears o)

@@ -23,7 +23,27 @@ enum : uint32_t {
 };
 
 void note_launch();      // counts kernel launches (svo_kernel_launches)
+void note_allocation();  // counts memory allocation calls the library makes (svo_allocation_calls)
+// The wait-fault test hook (svo_debug_wait_fault) of each translation unit with bounded device waits.
+cudaError_t vox_set_wait_fault(uint32_t limit, uint32_t withheld);
+cudaError_t build_set_wait_fault(uint32_t limit, uint32_t withheld);
+cudaError_t march_set_wait_fault(uint32_t limit, uint32_t withheld);
+cudaError_t texture_set_wait_fault(uint32_t limit, uint32_t withheld);
 int svo_fail(int code, const char *fmt, ...); // sets the calling thread's svo_last_error message
+
+// Every memory allocation the library makes goes through these (counted by svo_allocation_calls).
+template <typename T> cudaError_t counted_malloc(T **p, size_t bytes) {
+	note_allocation();
+	return cudaMalloc((void **)p, bytes);
+}
+template <typename T> cudaError_t counted_malloc_async(T **p, size_t bytes, cudaStream_t s) {
+	note_allocation();
+	return cudaMallocAsync((void **)p, bytes, s);
+}
+template <typename T> cudaError_t counted_malloc_host(T **p, size_t bytes) {
+	note_allocation();
+	return cudaMallocHost((void **)p, bytes);
+}
 
 // Brackets one kernel launch with CUDA events on its stream while profiling is enabled.
 struct ProfScope {
@@ -381,7 +401,7 @@ struct MarchJob {
 	svo_camera cam;
 	uint32_t width, height;
 	uint32_t n;
-	uint32_t pad;
+	uint32_t req; // the job's request in its batch: its rays report a malformed pool in status[req]
 	svo_hit *hits;
 	unsigned long long slot_begin;
 };
@@ -401,8 +421,9 @@ inline void *mapped_host_ptr(const void *p, size_t align) {
 }
 // `jobs` (device) holds njobs jobs whose slot_begin are set; total = slots of all jobs.  ticket (device,
 // 8 B) is zeroed here; status (device) gets kStatusMalformed for a malformed pool.
+// fetches (may be null) accumulates the node words the jobs' rays read.
 cudaError_t march_jobs_launch(const MarchJob *jobs, uint32_t njobs, uint64_t total, unsigned long long *ticket,
-                              uint32_t *status, cudaStream_t stream);
+                              uint32_t *status, unsigned long long *fetches, cudaStream_t stream);
 
 // One request's bounce rays: n hits in, n rays out, seeded per request (ray index local to the job).
 struct BounceJob {

@@ -302,6 +302,8 @@ cudaError_t vox_texture_launch(const uint64_t *cand, uint64_t n_cand, const svo_
 
 size_t vox_texture_scratch_bytes(uint64_t n_cand) { return (2 + (n_cand + kTexTile - 1) / kTexTile) * 8; }
 
+cudaError_t texture_set_wait_fault(uint32_t limit, uint32_t withheld) { return set_wait_fault_here(limit, withheld); }
+
 } // namespace svo
 
 using namespace svo;
@@ -342,8 +344,8 @@ int svo_texture_set_create(const uint8_t *const *rgba, const uint32_t *width, co
 			host[k++] = make_float4(lin[lv[i]], lin[lv[i + 1]], lin[lv[i + 2]], (float)(lv[i + 3] / 255.0));
 	cudaError_t e = cudaSuccess;
 	if (count) {
-		e = cudaMalloc(&s->desc_dev, count * sizeof(TexDesc));
-		if (e == cudaSuccess) e = cudaMalloc(&s->texels_dev, texels * sizeof(float4));
+		e = counted_malloc(&s->desc_dev, count * sizeof(TexDesc));
+		if (e == cudaSuccess) e = counted_malloc(&s->texels_dev, texels * sizeof(float4));
 		if (e == cudaSuccess) e = cudaMemcpy(s->desc_dev, s->desc.data(), count * sizeof(TexDesc), cudaMemcpyHostToDevice);
 		if (e == cudaSuccess) e = cudaMemcpy(s->texels_dev, host.data(), texels * sizeof(float4), cudaMemcpyHostToDevice);
 	}

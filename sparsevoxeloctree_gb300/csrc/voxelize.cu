@@ -691,6 +691,8 @@ static void launch_emit(const VoxBatch &vb, uint32_t n, uint32_t tune_level, con
 	           vox_emit_units<B><<<(uint32_t)sms * std::max(1u, per_sm / 2), kTPB, 0, stream>>>(vb, n, w, frags, capacity););
 }
 
+cudaError_t vox_set_wait_fault(uint32_t limit, uint32_t withheld) { return set_wait_fault_here(limit, withheld); }
+
 cudaError_t vox_launch_count(const svo_triangle *tris, uint32_t n, uint32_t level, const VoxWorkspace &w,
                              cudaStream_t stream) {
 	cudaError_t e = clear_count_state(n, w, stream);

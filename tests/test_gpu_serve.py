@@ -210,3 +210,43 @@ def test_budget_admission(cuda):
         assert st["failed"] == 1 and st["inflight_bytes"] == 0
     finally:
         server.close()
+
+
+def test_malformed_scene_fails_only_its_own_requests(cuda):
+    """A scene added from a damaged pool (pointers past its range) shares launches with a healthy one:
+    the requests that trace the damaged scene fail with SVO_ERR_INVALID, the co-batched requests on the
+    healthy scene complete with the single-request path's hits."""
+    import torch
+
+    from sparsevoxeloctree_gb300 import _lib
+    api = _api()
+    server = api.Server(lanes=1)
+    try:
+        tris, level = small_scene(6, 3000, 7)
+        good = server.BuildScene(tris, level)
+        good_oct = server.Scene(good)
+        bad_oct = api.Octree()
+        bad_oct.m_buffer = torch.from_numpy(np.array([0x80000000 | 0x0FFF0000] * 8, np.uint32).view(np.int32)).cuda()
+        bad_oct.m_range = 32
+        bad_oct.m_level = 3
+        bad = server.AddOctree(bad_oct)
+        reqs = requests(2, 16, seed=31)
+        for k, r in enumerate(reqs):
+            r["scene"] = bad if k % 4 == 1 else good
+        sub = [submit(server, r) for r in reqs]
+        shared = False
+        for (t, buf), r in zip(sub, reqs):
+            if r["scene"] == bad:
+                with pytest.raises(_lib.SvoError) as e:
+                    server.Wait(t)
+                assert e.value.code == _lib.SVO_ERR_INVALID
+            else:
+                res = server.Wait(t)
+                assert res["status"] == 0
+                shared |= res["batch_requests"] > 1
+                ref = direct_camera(good_oct, r["cam"], r["w"], r["h"], r["n"], r["seed"])
+                assert np.array_equal(hits_of(buf, 2 * r["n"]), ref)
+        assert shared, "no healthy request shared a launch"
+        assert server.stats()["failed"] == 4
+    finally:
+        server.close()
