@@ -157,7 +157,9 @@ def profiled_traffic(label: str, workload: str) -> dict:
     return {"traffic": None}
 
 
-def engine_arm(args, env, device) -> dict:
+def engine_arm(args, env, device, workload: str | None = None, light: bool = False) -> dict:
+    """The plain step on `workload` (default: the headline workload).  light: the step, its kernel
+    breakdown, roofline and oracle parity only (no beam, path-trace or end-to-end legs)."""
     import numpy as np
     import torch
 
@@ -165,7 +167,8 @@ def engine_arm(args, env, device) -> dict:
     from sparsevoxeloctree_gb300.formats import HIT_DTYPE
 
     lib = _lib.load()
-    scene = make_scene(args.workload)
+    workload = workload or args.workload
+    scene = make_scene(workload)
     T = len(scene.tris)
     n_rays = scene.n_rays
     tris_host = torch.from_numpy(np.ascontiguousarray(scene.tris).view(np.uint8).reshape(-1)).pin_memory()
@@ -306,7 +309,7 @@ def engine_arm(args, env, device) -> dict:
     if alg is not None:
         ach = alg / (dom_launch_ms * 1e-3) / 1e9
         roofline.update({"achieved": ach, "frac": ach / peaks["hbm_gbs"], "algorithmic_bytes_per_launch": alg})
-    roofline.update(profiled_traffic(dom_name, args.workload))
+    roofline.update(profiled_traffic(dom_name, workload))
     if dom_name.startswith("march"):
         roofline["limiter"] = ("instruction issue: node words stay in L1/L2, DRAM idle (ncu, "
                                "profiles/march_kernel_room_1024.md); the HBM fraction is low by construction")
@@ -318,7 +321,8 @@ def engine_arm(args, env, device) -> dict:
         "grays_per_s": n_traced / (march_ms * 1e-3) / 1e9 if march_ms else None,
         "rays_traced_per_step": n_traced,
         "voxelize_gbs": (48.0 * T + 8.0 * F) / (vox_ms * 1e-3) / 1e9 if vox_ms else None,
-        "build_gbs": (8.0 * F * scene.level + 16.0 * info["range_words"]) / (build_ms * 1e-3) / 1e9 if build_ms else None,
+        # the build's minimum traffic (each fragment read once, each node word written once) over its time
+        "build_min_bytes_gbs": (8.0 * F + 4.0 * info["range_words"]) / (build_ms * 1e-3) / 1e9 if build_ms else None,
         "march_gbs": n_rays * (24.0 + 32.0 + 4.0 * fetches / n_rays) / (march_ms * 1e-3) / 1e9 if march_ms else None,
         "hit_fraction": float((hit_np["flags"] & 1).mean()), "mean_iterations": float(hit_np["iter"].mean()),
         "node_fetches_per_ray": fetches / n_rays, "octree_words": info["range_words"], "leaves": info["leaves"],
@@ -328,6 +332,10 @@ def engine_arm(args, env, device) -> dict:
         "graph_step_ms": float(np.mean(graph_ms)) if graph_ms is not None else None,
         "graph_note": graph_note,
     }
+
+    if light:
+        return light_result(args, env, scene, F, T, n_rays, ms, stages, roofline, clocks, launches, vox, octree,
+                            hits, bounce_hits, device)
 
     # the tracer's beam optimisation on the same frame: pre-pass + advanced primary march
     beam_img = tracer.CmdBeamRenderPass()
@@ -365,13 +373,53 @@ def engine_arm(args, env, device) -> dict:
         stages["path_trace"] = path_trace_stats(api, octree, scene, stream)
 
     e2e = None if args.no_e2e else e2e_arm(args, scene, tris_host, device, env)
-    cpu = None
+    cpu = parity = None
     if env.leader and env.world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(scene, per_step=False)
+        # the timed steps' own outputs (the last step's fragment list, pool and hits), compared with the
+        # oracle pass the CPU baseline times on the same scene
+        ref = {}
+        cpu = cpu_baseline(scene, per_step=False, outputs=ref)
+        torch.cuda.synchronize()
+        parity = parity_vs_oracle(vox.GetVoxelFragmentList(), octree.words(), api.hits_numpy(hits),
+                                  api.hits_numpy(bounce_hits) if scene.bounce else None, ref, device)
+        del ref
     return {"value": ms, "ms_per_step": ms, "step_ms_all": step_ms, "stages": stages, "roofline": roofline,
             "tuning": tuning,
-            "clocks": clocks, "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": int(launches),
+            "clocks": clocks, "e2e": e2e, "cpu_baseline": cpu, "parity": parity, "gpu_launches": int(launches),
             "config_extra": {"level": scene.level, "triangles": T, "fragments": F, "rays": n_rays}}
+
+
+def light_result(args, env, scene, F, T, n_rays, ms, stages, roofline, clocks, launches, vox, octree, hits,
+                 bounce_hits, device) -> dict:
+    """Result of a light engine_arm run, with the oracle comparison of its outputs when the CPU baseline
+    leg runs (the oracle pass is timed as this workload's CPU baseline)."""
+    import torch
+
+    from sparsevoxeloctree_gb300 import api
+    cpu = parity = None
+    if env.leader and env.world == 1 and not args.no_cpu_baseline:
+        ref = {}
+        cpu = cpu_baseline(scene, per_step=False, outputs=ref)
+        torch.cuda.synchronize()
+        parity = parity_vs_oracle(vox.GetVoxelFragmentList(), octree.words(), api.hits_numpy(hits),
+                                  api.hits_numpy(bounce_hits) if scene.bounce else None, ref, device)
+        del ref
+    st = {k: stages[k] for k in ("voxelize_ms", "build_ms", "march_ms", "svo_build_ms", "mfragments_per_s",
+                                 "grays_per_s", "rays_traced_per_step", "node_fetches_per_ray", "octree_words",
+                                 "hit_fraction", "step_timing")}
+    st["kernels_ms_per_step"] = {k: round(v["ms"] / args.steps, 4) for k, v in stages["kernels"].items()}
+    summary = {"step_ms": round(ms, 3), "grays_per_s": round(stages["grays_per_s"], 3),
+               "svo_build_ms": round(stages["svo_build_ms"], 3), "march_frac": round(roofline.get("frac", 0.0), 4),
+               "rays": stages["rays_traced_per_step"]}
+    if parity:
+        summary["parity"] = {"fragments": parity["fragments"], "octree": parity["octree"],
+                             "hits_equal_frac": round(parity["hits_equal_frac"], 6),
+                             "bounce_hits_equal_frac": round(parity.get("bounce_hits_equal_frac", 1.0), 6)}
+    return {"workload": f"{scene.name}: {len(scene.tris)} triangles at level {scene.level}, "
+                        f"{scene.width}x{scene.height} primary rays" + (" plus one diffuse bounce per hit"
+                                                                        if scene.bounce else ""),
+            "value": ms, "fragments": F, "stages": st, "roofline": roofline, "clocks": clocks,
+            "gpu_launches": int(launches), "cpu_baseline": cpu, "parity": parity, "summary": summary}
 
 
 def e2e_arm(args, scene, tris_host, device, env) -> dict:
@@ -471,7 +519,7 @@ def path_trace_stats(api, octree, scene, stream, samples: int = 8) -> dict:
     return out
 
 
-def batch_leg(args, device) -> dict:
+def batch_leg(args, device, meshes=None, workload: str | None = None, check_identity: bool = False) -> dict:
     """The batched-build workload: 64 clutter meshes (triangles log-uniform in [1e3, 5e5], levels 7..10)
     voxelized and built (a) in one svo_batcher batch (one count pass, one readback of the counts, one
     recorded launch sequence for emit + every build level over all meshes, one readback of the results)
@@ -484,7 +532,9 @@ def batch_leg(args, device) -> dict:
     from sparsevoxeloctree_gb300 import _lib, api, scenes
 
     lib = _lib.load()
-    meshes = scenes.batch_64()
+    if meshes is None:
+        meshes = scenes.batch_64()
+        workload = "batch_64: 64 clutter meshes, triangles log-uniform in [1e3, 5e5] (seeded), levels 7..10"
     tris = [api.to_device(t) for t, _ in meshes]
     s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     bb = api.BatchBuilder(use_graph=True)
@@ -546,10 +596,28 @@ def batch_leg(args, device) -> dict:
     kernels = _lib.profile_summary()
     lib.svo_profile_enable(0)
     del prof_bb
+    identical = None
+    if check_identity:  # every mesh's octree from the batch equals its plain build's, word for word
+        identical = True
+        bb.Build(batch)
+        for i, (t, (_, level)) in enumerate(zip(tris, meshes)):
+            fl = _lib.Fraglist()
+            _lib.check(lib.svo_voxelize(ctypes.c_void_p(t.data_ptr()), t.numel() // 48, level, ctypes.byref(fl), s))
+            oc = _lib.OctreeC()
+            _lib.check(lib.svo_build_fraglist(ctypes.byref(fl), ctypes.byref(oc), None, s))
+            plain = api._copy_from(oc.words, oc.range_words, torch.int32)
+            identical &= bool(torch.equal(plain, bb.GetOctree(i).words()))
+            del plain
+            lib.svo_fraglist_destroy(ctypes.byref(fl), s)
+            lib.svo_octree_destroy(ctypes.byref(oc), s)
+        torch.cuda.synchronize()
     peaks = load_peaks()
     alg = 48.0 * T + 40.0 * F + 4.0 * W
     bm, sm = float(np.median(b_ms)), float(np.median(seq_ms))
-    return {"workload": "batch_64: 64 clutter meshes, triangles log-uniform in [1e3, 5e5] (seeded), levels 7..10",
+    frac = alg / (bm * 1e-3) / 1e9 / peaks["hbm_gbs"]
+    return {"workload": workload, "summary": {"batched_ms": round(bm, 3), "sequential_ms": round(sm, 3),
+                                              "speedup": round(sm / bm, 3), "frac": round(frac, 4),
+                                              "bit_identical_to_plain": identical},
             "meshes": len(meshes), "triangles": T, "fragments": F, "octree_words": W,
             "batched_ms": bm, "sequential_plain_ms": sm, "speedup_vs_sequential": sm / bm,
             "batched_mfragments_per_s": F / (bm * 1e-3) / 1e6,
@@ -679,6 +747,32 @@ def serve_leg(args, device, rates=(100, 500, 1000, 2000, 5000), seconds=1.0) -> 
     sat_reqs = [dict(make_request(k), rebuild=False) for k in range(400)]
     saturated = summarize(sat_reqs, run(sat_reqs, None))
 
+    # roofline of the served march: the same 400 requests again with the library's per-launch events on.
+    # Bytes per ray: 32 B hit out, 4 B per node word read (counted by the server's march), and 24 B ray in
+    # for the bounce half (camera rays are made in the kernel).
+    f0 = server.stats()["node_fetches"]
+    lib.svo_profile_enable(1)
+    prof_res = run(sat_reqs, None)
+    prof = _lib.profile_summary()
+    lib.svo_profile_enable(0)
+    fetches = server.stats()["node_fetches"] - f0
+    prof_sum = summarize(sat_reqs, prof_res)
+    rays = prof_sum["rays"]
+    served_bytes = 32.0 * rays + 4.0 * fetches + 24.0 * (rays / 2)
+    mj = prof.get("march_jobs", {"ms": 0.0, "launches": 0})
+    span_s = rays / (prof_sum["grays_per_s"] * 1e9)
+    peaks = load_peaks()
+    roof = {"bound": "hbm", "unit": "GB/s", "peak": peaks["hbm_gbs"], "peak_source": peaks["source"],
+            "rays": rays, "node_fetches_per_ray": fetches / rays, "bytes_per_ray": served_bytes / rays,
+            "march_launches": mj["launches"], "launch_ms": mj["ms"] / max(mj["launches"], 1),
+            "march_event_ms_summed_over_lanes": mj["ms"],
+            "achieved": served_bytes / span_s / 1e9,
+            "frac": served_bytes / span_s / 1e9 / peaks["hbm_gbs"],
+            "formula": "rays x (32 B hit + 24 B ray for the bounce half) + 4 B x node words read, over the wall "
+                       "span of the saturated run (delivered); the lanes' march launches overlap, so their "
+                       "summed event time is not a busy time",
+            "kernels": {k: {"ms": round(v["ms"], 3), "launches": v["launches"]} for k, v in prof.items()}}
+
     # one request at a time, plain C ABI.  The sweep's rebuilds replaced scenes' octrees (and freed the old
     # ones once their batches retired): take fresh views of the current octrees.
     views = [server.Scene(i) for i in octs]
@@ -724,7 +818,7 @@ def serve_leg(args, device, rates=(100, 500, 1000, 2000, 5000), seconds=1.0) -> 
     return {"workload": "serving: 16 resident octrees (levels 9..11, 50k..2M triangles, seeded), requests of "
                         "1k..2M rays (log-uniform; half primary, half diffuse bounce), 2% rebuilds, 40 GB budget",
             "resident_bytes": st["resident_bytes"], "scenes_triangles": int(sum(len(t) for t, _ in meshes)),
-            "poisson": sweep, "saturated_400": saturated,
+            "poisson": sweep, "saturated_400": saturated, "roofline": roof,
             "same_150_requests": {"served_grays_per_s": served_sat["grays_per_s"],
                                   "one_at_a_time_plain_abi_grays_per_s": one_rays / plain_s / 1e9,
                                   "one_at_a_time_server_grays_per_s": one_res["grays_per_s"],
@@ -736,8 +830,10 @@ def serve_leg(args, device, rates=(100, 500, 1000, 2000, 5000), seconds=1.0) -> 
 
 
 # ------------------------------------------------------------------------------------------ CPU arms
-def cpu_baseline(scene, per_step: bool) -> dict:
-    """The oracle (CPU restatement of the reference's path) on the host cores, full workload."""
+def cpu_baseline(scene, per_step: bool, outputs: dict | None = None) -> dict:
+    """The oracle (CPU restatement of the reference's path) on the host cores, full workload.  With
+    `outputs` (a dict), the pass's fragment list, node pool and hits are stored there for the parity
+    comparison with the engine's outputs of the same workload."""
     import oracle
     t0 = time.perf_counter()
     frags = oracle.voxelize(scene.tris, scene.level)
@@ -746,14 +842,53 @@ def cpu_baseline(scene, per_step: bool) -> dict:
     t2 = time.perf_counter()
     rays = oracle.camera_rays(scene.camera, scene.width, scene.height)
     hits = oracle.raycast(pool, scene.level, rays)
+    bounce_hits = None
     if scene.bounce:
-        oracle.raycast(pool, scene.level, oracle.bounce_rays(hits, scene.seed))
+        bounce_hits = oracle.raycast(pool, scene.level, oracle.bounce_rays(hits, scene.seed))
     t3 = time.perf_counter()
     ms = (t3 - t0) * 1e3
+    if outputs is not None:
+        outputs.update(frags=frags, pool=pool, hits=hits, bounce_hits=bounce_hits)
     return {"value": ms, "unit": "ms", "cores": oracle.threads(), "kind": "port",
             "sample": f"full {scene.name} workload, one pass ({len(scene.tris)} tris, {len(frags)} fragments, "
                       f"{scene.n_rays} rays)",
+            "fragments": int(len(frags)),
             "stages_ms": {"voxelize": (t1 - t0) * 1e3, "build": (t2 - t1) * 1e3, "march": (t3 - t2) * 1e3}}
+
+
+def parity_vs_oracle(frags_dev, pool_dev, hits_np, bounce_np, ref: dict, device) -> dict:
+    """The engine's outputs of the timed workload against the oracle's on the same scene: the fragment
+    multisets (both lists sorted on the device), the node pools word for word (canonical breadth-first
+    order on both sides), and every ray's hit field by field; plus the tolerance the engine promises
+    (voxel id on >= 99.99% of rays, |dt| <= 1e-5 of the extent)."""
+    import numpy as np
+    import torch
+    rf = torch.from_numpy(np.ascontiguousarray(ref["frags"]).view(np.int64)).to(device)
+    ef = frags_dev.view(torch.int64)
+    frags_ok = ef.numel() == rf.numel() and bool(torch.equal(torch.sort(ef)[0], torch.sort(rf)[0]))
+    rp = torch.from_numpy(np.ascontiguousarray(ref["pool"]).view(np.int32)).to(device)
+    ep = pool_dev.view(torch.int32)
+    pool_ok = ep.numel() == rp.numel() and bool(torch.equal(ep, rp))
+    del rf, rp
+
+    def hit_stats(got, want):
+        same = np.ones(len(want), bool)
+        for f in want.dtype.names:
+            same &= (got[f] == want[f]).reshape(len(want), -1).all(axis=1)
+        voxel = (got["voxel"] == want["voxel"]).all(axis=1) & ((got["flags"] & 1) == (want["flags"] & 1))
+        both = (got["flags"] & 1).astype(bool) & (want["flags"] & 1).astype(bool)
+        dt = float(np.abs(got["t"][both] - want["t"][both]).max()) if both.any() else 0.0
+        return float(same.mean()), float(voxel.mean()), dt
+
+    eq, vox, dt = hit_stats(hits_np, ref["hits"])
+    out = {"fragments": frags_ok, "fragment_count": int(ef.numel()), "octree": pool_ok, "octree_words": int(ep.numel()),
+           "hits_equal_frac": eq, "hits_voxel_frac": vox, "max_abs_dt": dt, "rays": int(len(hits_np))}
+    if bounce_np is not None and ref.get("bounce_hits") is not None:
+        beq, bvox, bdt = hit_stats(bounce_np, ref["bounce_hits"])
+        out.update({"bounce_hits_equal_frac": beq, "bounce_hits_voxel_frac": bvox, "bounce_max_abs_dt": bdt})
+    out["within_tolerance"] = bool(frags_ok and pool_ok and vox >= 0.9999 and dt <= 1e-5 and
+                                   out.get("bounce_hits_voxel_frac", 1.0) >= 0.9999)
+    return out
 
 
 def reference_arm(args, rank: int) -> dict | None:
@@ -769,11 +904,43 @@ def reference_arm(args, rank: int) -> dict | None:
     cpu["value"] = ms
     return {"value": ms, "ms_per_step": ms, "cpu_baseline": cpu,
             "e2e": {"value": ms, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "config_extra": {"level": scene.level, "triangles": len(scene.tris), "rays": scene.n_rays,
-                             "cores": oracle.threads()}}
+            "config_extra": {"level": scene.level, "triangles": len(scene.tris), "fragments": cpu["fragments"],
+                             "rays": scene.n_rays}}
 
 
 # ------------------------------------------------------------------------------------------ main
+def summary_block(line: dict) -> dict:
+    """Compact copy of the headline figures, printed as the line's last key so that a reader who keeps
+    only the end of the output still sees them: parity against the oracle, the batched and served
+    speed-ups with their roofline fractions, and served latency per arrival rate."""
+    def r(x, n=4):
+        return None if x is None else round(float(x), n)
+    out = {"step_ms": r(line.get("value")), "e2e_ms": r((line.get("e2e") or {}).get("value")),
+           "march_frac": r(line["roofline"].get("frac"))}
+    p = line.get("parity")
+    if p:
+        out["parity"] = {"fragments": p["fragments"], "octree": p["octree"], "hits_equal_frac": r(p["hits_equal_frac"], 6)}
+    b = line.get("batched")
+    if b:
+        out["batched_speedup"] = r(b["speedup_vs_sequential"], 3)
+        out["batched_frac"] = r(b["roofline"]["frac"])
+        out["batched_ms"] = r(b["batched_ms"], 3)
+    sv = line.get("served")
+    if sv:
+        same = sv["same_150_requests"]
+        out["served_speedup"] = r(same["speedup_vs_plain_abi"], 3)
+        out["served_speedup_vs_unbatched"] = r(same["speedup_vs_unbatched_server"], 3)
+        out["served_grays_per_s"] = r(sv["saturated_400"]["grays_per_s"], 3)
+        if sv.get("roofline"):
+            out["served_frac"] = r(sv["roofline"]["frac"])
+            out["served_march_launch_ms"] = r(sv["roofline"]["launch_ms"])
+        out["served_p50_p99_ms"] = {k: [r(v["p50_ms"], 3), r(v["p99_ms"], 3)] for k, v in sv["poisson"].items()}
+    for key in ("large", "large_batched"):
+        if line.get(key):
+            out[key] = line[key].get("summary")
+    return out
+
+
 def main() -> int:
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -787,6 +954,8 @@ def main() -> int:
     ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
     ap.add_argument("--no-autotune", action="store_true", help="default launch parameters")
     ap.add_argument("--no-path-trace", action="store_true", help="skip the path-tracer statistics")
+    ap.add_argument("--no-large", action="store_true",
+                    help="skip the 2^12 legs (plain 4M-triangle step; 10M triangles as 4 batched meshes)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -822,14 +991,30 @@ def main() -> int:
         res["batched"] = batch_leg(args, device)
     if not args.no_serve and env.leader:
         res["served"] = serve_leg(args, device)
+    if not args.no_large and env.leader:
+        # the 2^12 configuration: one 4M-triangle octree (the largest the 30-bit pointer format holds) with
+        # primary and bounce rays, and the full 10M triangles as its 4 clustered groups in one batch
+        torch.cuda.empty_cache()
+        res["large"] = engine_arm(args, env, device, workload="clusters_4096_4m", light=True)
+        torch.cuda.empty_cache()
+        from sparsevoxeloctree_gb300 import scenes
+        res["large_batched"] = batch_leg(
+            args, device, meshes=scenes.clusters_4096_groups(),
+            workload="clusters_4096_groups: the 10M-triangle 4-cluster scene as 4 meshes (one per group, "
+                     "~2.5M triangles each) at level 12, one batch vs 4 sequential plain builds",
+            check_identity=True)
     config.update(res["config_extra"])
     line.update({"value": res["value"], "ms_per_step": res["ms_per_step"], "config": config,
                  "stages": res["stages"], "roofline": res["roofline"], "cpu_baseline": res["cpu_baseline"],
                  "e2e": res["e2e"], "clocks": res["clocks"], "gpu_launches": res["gpu_launches"],
                  "step_ms": res["step_ms_all"], "autotuned": res["tuning"]})
-    for key in ("batched", "served"):
+    for key in ("batched", "served", "large", "large_batched"):
         if key in res:
             line[key] = res[key]
+    if res.get("parity") is not None:
+        line["parity"] = res["parity"]
+    # last: the figures a reader of the line's tail needs, compact
+    line["summary"] = summary_block(line)
     if env.leader:
         print(json.dumps(line), flush=True)
     replicas.finish(env)

@@ -10,6 +10,7 @@ Five workloads, with the shapes, sizes and value distributions of the engine's b
 * ``batch_64``    — 64 clutter meshes, T log-uniform in [1e3, 5e5], level in {7,8,9,10};
 * ``clusters_4096`` — level 12: ~10M tris in 4 Gaussian clusters (sigma 0.1, edge lognormal(ln 0.001, 0.8)),
                     3840x2160 primary rays plus one diffuse bounce per hit;
+* ``clusters_4096_groups`` — the clusters_4096 triangles as 4 meshes, one per group (batched build).
 * ``serving``     — 16 resident scenes (levels 9..11, sphere+boxes+clutter, T log-uniform [5e4, 2e6]).
 
 Meshes are triangle soups in the unit cube (TRIANGLE_DTYPE) with uniform random RGB8 per vertex.  Rays are
@@ -189,16 +190,29 @@ def room_1024(seed: int = 2, clutter_tris: int = 210_932, width: int = 1920, hei
     return Scene("room_1024", tris, level, cam, width, height, seed=seed)
 
 
-def clusters_4096(seed: int = 4, n_tris: int = 10_000_000, width: int = 3840, height: int = 2160,
-                  level: int = 12) -> Scene:
+def _clusters(seed: int, n_tris: int):
+    """Triangles of the 4-cluster distribution and each triangle's cluster."""
     g = rng(seed, 0)
     centres_c = g.uniform(0.25, 0.75, size=(4, 3))
     which = g.integers(0, 4, size=n_tris)
     centres = np.clip(centres_c[which] + g.normal(0.0, 0.1, size=(n_tris, 3)), 0.0, np.nextafter(1.0, 0.0))
     verts = clutter(rng(seed, 1), n_tris, math.log(0.001), 0.8, centres=centres)
-    tris = _soup(verts, random_colors(rng(seed, 2), n_tris))
+    return _soup(verts, random_colors(rng(seed, 2), n_tris)), which
+
+
+def clusters_4096(seed: int = 4, n_tris: int = 10_000_000, width: int = 3840, height: int = 2160,
+                  level: int = 12) -> Scene:
+    tris, _ = _clusters(seed, n_tris)
     cam = interior_camera(rng(seed, 3), width / height)
     return Scene("clusters_4096", tris, level, cam, width, height, bounce=True, seed=seed)
+
+
+def clusters_4096_groups(seed: int = 4, n_tris: int = 10_000_000, level: int = 12):
+    """The same triangles as clusters_4096 split into its 4 clustered groups: a list of 4 (tris, level)
+    meshes for the batched build.  Each group's octree (about a quarter of the whole scene's 1.95 G node
+    words at 10 M triangles) fits the 30-bit child-pointer format that the single octree exceeds."""
+    tris, which = _clusters(seed, n_tris)
+    return [(np.ascontiguousarray(tris[which == k]), level) for k in range(4)]
 
 
 def batch_64(seed: int = 3, n_meshes: int = 64, t_lo: float = 1e3, t_hi: float = 5e5):
