@@ -71,7 +71,8 @@ struct HostArena {
 
 // Offsets of the plan buffer (device) and of its pinned host mirror; every part 256-byte aligned.
 struct PlanLayout {
-	size_t vox_mesh, tri_base, shifts, mesh_out, build_mesh, frag_base, bucket_base, item_base, dense_base, results;
+	size_t vox_mesh, tri_base, shifts, mesh_out, build_mesh, frag_base, bucket_base, item_base, dense_base, reduce_base,
+	    results;
 	size_t total;
 	PlanLayout(uint32_t M) {
 		size_t off = 0;
@@ -89,6 +90,7 @@ struct PlanLayout {
 		bucket_base = take(4ull * (M + 1));
 		item_base = take(4ull * (M + 1));
 		dense_base = take(4ull * (M + 1));
+		reduce_base = take(4ull * (M + 1));
 		results = take(kResultRec * 4ull * M);
 		total = off;
 	}
@@ -269,7 +271,7 @@ static int batch_build(Batcher &b, const svo_batch_mesh *meshes, uint32_t M, cud
 	BuildMesh *hbm = (BuildMesh *)(hs + pl.build_mesh);
 	unsigned long long *hfb = (unsigned long long *)(hs + pl.frag_base);
 	uint32_t *hbb = (uint32_t *)(hs + pl.bucket_base), *hib = (uint32_t *)(hs + pl.item_base),
-	         *hdb = (uint32_t *)(hs + pl.dense_base);
+	         *hdb = (uint32_t *)(hs + pl.dense_base), *hrb = (uint32_t *)(hs + pl.reduce_base);
 	BuildBatchPlan p;
 	p.M = M;
 	p.frags_total = F;
@@ -278,7 +280,8 @@ static int batch_build(Batcher &b, const svo_batch_mesh *meshes, uint32_t M, cud
 	uint32_t nb_total = 0, dense_total = 0, items_total = 0;
 	bool any_sparse = false;
 	uint64_t windows = 0;
-	hfb[0] = 0, hbb[0] = 0, hib[0] = 0, hdb[0] = 0;
+	hfb[0] = 0, hbb[0] = 0, hib[0] = 0, hdb[0] = 0, hrb[0] = 0;
+	uint32_t reduce_total = 0;
 	for (uint32_t m = 0; m < M; ++m) {
 		MeshResult &r = b.results[m];
 		r.frag_count = hmo[4 * m];
@@ -313,6 +316,8 @@ static int batch_build(Batcher &b, const svo_batch_mesh *meshes, uint32_t M, cud
 		hbb[m + 1] = nb_total;
 		hib[m + 1] = items_total;
 		hdb[m + 1] = dense_total;
+		reduce_total += dense_reduce_chunks(level);
+		hrb[m + 1] = reduce_total;
 		p.max_level = std::max(p.max_level, level);
 		p.max_D = std::max(p.max_D, bm.dv.D);
 		windows += leaf_window_bound(count, level);
@@ -391,6 +396,8 @@ static int batch_build(Batcher &b, const svo_batch_mesh *meshes, uint32_t M, cud
 	p.bb.bucket_base = (const uint32_t *)(ds + pl.bucket_base);
 	p.bb.item_base = (const uint32_t *)(ds + pl.item_base);
 	p.bb.dense_base = (const uint32_t *)(ds + pl.dense_base);
+	p.bb.reduce_base = (const uint32_t *)(ds + pl.reduce_base);
+	p.bb.reduce_total = reduce_total;
 	p.bb.dense_bits = bits;
 	p.bb.dense_prefix = prefix;
 	p.bb.gstate = p.gstate;

@@ -233,26 +233,25 @@ __global__ void __launch_bounds__(kTPB) dense_mark(const uint64_t *__restrict__ 
 }
 
 // Bitmaps of depths D-1 .. 1 from depth D in one launch (bit p of depth d = byte p of depth d+1 is
-// nonzero).  Block b reduces chunk b (kReduceChunk words) of depth D level by level in shared memory:
-// the words of a level that the chunk covers whole are written directly, and once the chunk's image is
-// smaller than a word its bits are ORed into place (atomicOr), so higher levels collect every chunk's
-// contribution.  The bitmaps were zeroed before the build.  blockIdx.y = mesh.
-constexpr uint32_t kReduceChunk = 2048;
+// nonzero).  Work items are chunks of kReduceChunk words of a mesh's depth-D bitmap, listed over the batch
+// (reduce_base) and taken grid-stride, so no block is spent on a mesh without that chunk.  A block
+// reduces its chunk level by level in shared memory: the words of a level that the chunk covers whole are
+// written directly, and once the chunk's image is smaller than a word its bits are ORed into place
+// (atomicOr), so higher levels collect every chunk's contribution.  The bitmaps were zeroed before the
+// build.
+constexpr uint32_t kReduceChunk = 8192;
 
 SVO_DEV uint32_t byte_bits(uint32_t v) { // bit j = byte j of v is nonzero
 	return (uint32_t)((v & 0xffu) != 0u) | ((uint32_t)((v & 0xff00u) != 0u) << 1) |
 	       ((uint32_t)((v & 0xff0000u) != 0u) << 2) | ((uint32_t)((v & 0xff000000u) != 0u) << 3);
 }
 
-template <bool B> __global__ void __launch_bounds__(256) dense_reduce(BuildBatch bb) {
-	__shared__ uint32_t s_buf[2][kReduceChunk / 8];
-	const DenseView dv = mesh_at<B>(bb, blockIdx.y).dv;
+// One chunk (called by the whole block; D >= 2).
+SVO_DEV void reduce_chunk(const DenseView &dv, uint32_t chunk_idx, uint32_t (*s_buf)[kReduceChunk / 8]) {
 	const uint32_t D = dv.D;
-	if (D < 2) return;
 	const uint32_t words_D = (1u << (3 * D)) / 32u; // D >= 2: at least 2 words
 	const uint32_t chunk = min(words_D, kReduceChunk);
-	const uint32_t first = blockIdx.x * chunk;
-	if (first >= words_D) return;
+	const uint32_t first = chunk_idx * chunk;
 	uint32_t nbits = chunk * 32u, bit0 = first * 32u; // the chunk's image at the current level
 	const uint32_t *src = dv.bits + dv.off[D] + first;
 	bool src_shared = false;
@@ -269,7 +268,7 @@ template <bool B> __global__ void __launch_bounds__(256) dense_reduce(BuildBatch
 					for (int i = 0; i < 8; ++i) out |= byte_bits(src[8 * w + i]) << (4 * i);
 				} else {
 					const uint4 *c4 = reinterpret_cast<const uint4 *>(src + 8 * w);
-					const uint4 p = c4[0], q = c4[1];
+					const uint4 p = __ldcs(c4), q = __ldcs(c4 + 1);
 					const uint32_t v[8] = {p.x, p.y, p.z, p.w, q.x, q.y, q.z, q.w};
 #pragma unroll
 					for (int i = 0; i < 8; ++i) out |= byte_bits(v[i]) << (4 * i);
@@ -299,6 +298,25 @@ template <bool B> __global__ void __launch_bounds__(256) dense_reduce(BuildBatch
 				}
 			return;
 		}
+	}
+}
+
+uint32_t dense_reduce_chunks(uint32_t level) {
+	const uint32_t D = dense_depth(level);
+	if (D < 2) return 0;
+	const uint32_t words_D = (1u << (3 * D)) / 32u;
+	return (words_D + kReduceChunk - 1) / kReduceChunk;
+}
+
+template <bool B> __global__ void __launch_bounds__(256) dense_reduce(BuildBatch bb) {
+	__shared__ uint32_t s_buf[2][kReduceChunk / 8];
+	const uint32_t total = bb.reduce_total;
+	for (uint32_t item = blockIdx.x; item < total; item += gridDim.x) {
+		const uint32_t mi = B ? mesh_search(bb.reduce_base, bb.M, item) : 0u;
+		const uint32_t chunk_idx = item - (B ? __ldg(bb.reduce_base + mi) : 0u);
+		const DenseView dv = mesh_at<B>(bb, mi).dv;
+		reduce_chunk(dv, chunk_idx, s_buf);
+		__syncthreads(); // s_buf is reused by the next item
 	}
 }
 
@@ -1158,6 +1176,7 @@ static BuildBatch single_batch(const BuildWorkspace &w, uint32_t count, uint32_t
 	bb.sorted_total = count;
 	bb.dense_total = w.dense_words;
 	bb.nb_total = w.nb;
+	bb.reduce_total = dense_reduce_chunks(level);
 	BuildMesh &m = bb.one;
 	m.pool = pool;
 	m.capacity = capacity;
@@ -1200,11 +1219,9 @@ static void launch_dense_and_scatter(const uint64_t *frags, uint64_t n, uint32_t
 	                                                                                gstate, bdescs););
 	fork.mark_side(0);
 	if (maxD >= 1) {
-		if (maxD >= 2) {
-			const uint32_t words_D = (1u << (3 * maxD)) / 32u;
-			const dim3 grid((words_D + kReduceChunk - 1) / kReduceChunk, M);
-			SVO_LAUNCH("dense_reduce", stream, dense_reduce<B><<<grid, 256, 0, stream>>>(bb););
-		}
+		if (maxD >= 2 && bb.reduce_total)
+			SVO_LAUNCH("dense_reduce", stream,
+			           dense_reduce<B><<<std::min<uint32_t>(bb.reduce_total, (uint32_t)sms * 8), 256, 0, stream>>>(bb););
 		SVO_LAUNCH("dense_scan", stream,
 		           dense_scan<B><<<grid_for(dense_words, kDenseTile, (uint32_t)sms * 4), kTPB, 0, stream>>>(
 		               bb, dense_words, gstate, descs););

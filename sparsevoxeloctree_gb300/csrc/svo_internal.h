@@ -244,11 +244,13 @@ struct BuildBatch {
 	const uint32_t *bucket_base;
 	const uint32_t *item_base;
 	const uint32_t *dense_base;
+	const uint32_t *reduce_base; // [M+1] dense_reduce chunks before each mesh (chunks of meshes with D >= 2)
 	uint32_t *dense_bits;   // base of the concatenated bitmaps
 	uint32_t *dense_prefix; // base of the concatenated prefixes
 	BuildState *gstate;     // batch-wide tickets and status (the mesh's own state for a single build)
 	unsigned long long sorted_total; // entries of the bucketed copy (bounds checks)
 	uint32_t dense_total, nb_total;  // dense words and buckets of all meshes (bounds checks)
+	uint32_t reduce_total;           // dense_reduce chunks of all meshes
 	uint32_t M;
 	BuildMesh one;
 };
@@ -279,6 +281,7 @@ uint32_t dense_depth(uint32_t level);
 uint32_t bucket_shift(uint32_t level); // bucket edge of the build's fragment buckets: 2^shift voxels
 uint64_t leaf_window_bound(uint32_t count, uint32_t level); // leaf windows a dense-parent mesh can need
 uint32_t dense_words_of(uint32_t d);
+uint32_t dense_reduce_chunks(uint32_t level); // work items of dense_reduce for a mesh at `level`
 // Words of the dense bitmaps of depths 1..dense_depth(level) (32-byte aligned levels) and their offsets.
 uint32_t dense_layout(uint32_t level, uint32_t off[kDenseMaxDepth + 2]);
 // dense_write items of a mesh (parent words of the depths whose child blocks it writes, plus the root).
