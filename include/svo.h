@@ -392,8 +392,12 @@ typedef struct svo_server_config {
 	uint32_t lanes;              /* batches in flight at once (0: 3) */
 	uint32_t max_batch_rays;     /* hits per batch (0: 8 Mi); a larger request runs alone */
 	uint32_t max_batch_requests; /* requests per batch (0: 256) */
-	uint32_t reserved;
+	uint32_t flags;              /* SVO_SERVER_COUNT_FETCHES: count the node words the march reads */
 } svo_server_config;
+
+/* svo_server_config.flags: count node fetches into svo_server_stats.node_fetches (for a roofline;
+ * costs the served march about 7%). */
+#define SVO_SERVER_COUNT_FETCHES 1u
 
 #define SVO_REQUEST_CAMERA 0u /* primary camera rays, then one diffuse bounce ray per primary ray */
 #define SVO_REQUEST_RAYS 1u   /* caller-given rays */
@@ -425,7 +429,7 @@ typedef struct svo_server_stats {
 	uint64_t rays;                      /* hits produced */
 	uint64_t rebuilds;
 	uint64_t resident_bytes, inflight_bytes, pending;
-	uint64_t node_fetches;              /* node words the served rays read (the march's memory traffic) */
+	uint64_t node_fetches;              /* node words the served rays read (with SVO_SERVER_COUNT_FETCHES) */
 } svo_server_stats;
 
 int svo_server_create(const svo_server_config *cfg, svo_server **out);

@@ -608,10 +608,6 @@ static void march_one(const uint32_t *pool, uint64_t range, uint32_t level, cons
 	int aborted = 0;
 	const uint32_t min_scale = SVO_STACK_SIZE - level;
 	while (scale < SVO_STACK_SIZE) {
-		if (iter >= SVO_MARCH_MAX_ITER) { /* never reached on a valid octree */
-			aborted = 1;
-			break;
-		}
 		++iter;
 		if (cur == 0u) {
 			uint64_t w = (uint64_t)parent + (idx ^ oct_mask);
@@ -655,7 +651,13 @@ static void march_one(const uint32_t *pool, uint64_t range, uint32_t level, cons
 			cur = 0;
 			continue;
 		}
-		/* advance */
+		/* advance.  The iteration bound is tested here, not in every iteration: pushes in a row are
+		 * limited by the tree depth, so every endless sequence has advances (also with NaN arithmetic,
+		 * where nothing is fetched); never reached on a valid octree. */
+		if (iter >= SVO_MARCH_MAX_ITER) {
+			aborted = 1;
+			break;
+		}
 		uint32_t step_mask = 0;
 		for (int k = 0; k < 3; ++k)
 			if (tc[k] <= tc_max) {

@@ -58,7 +58,10 @@ class BatchMesh(ctypes.Structure):
 
 class ServerConfig(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", u64), ("lanes", u32), ("max_batch_rays", u32), ("max_batch_requests", u32),
-                ("reserved", u32)]
+                ("flags", u32)]
+
+
+SVO_SERVER_COUNT_FETCHES = 1
 
 
 class TraceRequest(ctypes.Structure):

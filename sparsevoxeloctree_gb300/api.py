@@ -685,9 +685,10 @@ class Server:
     submitted from any thread and complete asynchronously; Wait() returns their timings."""
 
     def __init__(self, hbm_budget_bytes: int = 0, lanes: int = 0, max_batch_rays: int = 0,
-                 max_batch_requests: int = 0):
+                 max_batch_requests: int = 0, count_fetches: bool = False):
         lib = _lib.load()
-        cfg = _lib.ServerConfig(hbm_budget_bytes, lanes, max_batch_rays, max_batch_requests, 0)
+        cfg = _lib.ServerConfig(hbm_budget_bytes, lanes, max_batch_rays, max_batch_requests,
+                                _lib.SVO_SERVER_COUNT_FETCHES if count_fetches else 0)
         h = ctypes.c_void_p()
         _lib.check(lib.svo_server_create(ctypes.byref(cfg), ctypes.byref(h)))
         self.handle = h

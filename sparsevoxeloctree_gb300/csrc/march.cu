@@ -126,15 +126,18 @@ SVO_DEV void ray_init(RayState &s, const float o[3], const float dir[3], uint32_
 // its condition fails).  A malformed pool (pointer outside the range, interior word below the octree
 // level, iteration bound) ends the ray as an aborted miss and sets kStatusMalformed.  CHECK_END = false
 // skips the loop condition for callers that never step an ended ray (every path that ends the ray
-// returns true at once, so only a ray without direction enters the loop ended).
-template <int STRIDE, bool CHECK_END = true>
+// returns true at once, so only a ray without direction enters the loop ended).  COUNT = false leaves
+// the node-fetch counter alone (callers that do not report it).
+//
+// The iteration bound is tested where an iteration advances, not in every iteration: consecutive pushes
+// are limited by the tree depth (a push below the octree level aborts), so every iteration sequence
+// that does not end contains advances, and a ray is stopped within SVO_STACK_SIZE iterations of the
+// bound, also when its arithmetic is NaN and nothing is fetched.  (Testing the bound in every iteration
+// cost 10% of the march on the room frame.)  The oracle tests it at the same place.
+template <int STRIDE, bool CHECK_END = true, bool COUNT = true>
 SVO_DEV bool ray_step(RayState &s, const uint32_t *__restrict__ pool, uint32_t range, uint32_t *stack,
                       uint32_t *status) {
 	if (CHECK_END && s.scale >= SVO_STACK_SIZE) return true;
-	if (s.iter >= SVO_MARCH_MAX_ITER) {
-		s.aborted = true;
-		return true;
-	}
 	++s.iter;
 	if (s.cur == 0u) {
 		const uint32_t w = s.parent + (s.idx ^ s.oct_mask);
@@ -145,7 +148,7 @@ SVO_DEV bool ray_step(RayState &s, const uint32_t *__restrict__ pool, uint32_t r
 			return true;
 		}
 		s.cur = __ldg(pool + w);
-		++s.nfetch;
+		if (COUNT) ++s.nfetch;
 	}
 	float tc[3];
 #pragma unroll
@@ -184,6 +187,10 @@ SVO_DEV bool ray_step(RayState &s, const uint32_t *__restrict__ pool, uint32_t r
 		return false;
 	}
 	// advance
+	if (s.iter >= SVO_MARCH_MAX_ITER) { // the iteration bound (see above); never reached on a valid octree
+		s.aborted = true;
+		return true;
+	}
 	uint32_t step_mask = 0;
 #pragma unroll
 	for (int k = 0; k < 3; ++k)
@@ -260,14 +267,14 @@ SVO_DEV void ray_finish(RayState &s, uint32_t level, MarchOut &out) {
 	}
 }
 
-// One whole ray.
-template <int STRIDE>
+// One whole ray (nfetch: node words read, when COUNT).
+template <int STRIDE, bool COUNT = true>
 SVO_DEV void march_ray(const uint32_t *__restrict__ pool, uint32_t range, uint32_t level, const float o[3],
                        const float dir[3], uint32_t *stack, MarchOut &out, uint32_t &nfetch, uint32_t *status) {
 	RayState s;
 	ray_init<STRIDE>(s, o, dir, level, stack);
 	if (!s.none)
-		while (!ray_step<STRIDE, false>(s, pool, range, stack, status)) {
+		while (!ray_step<STRIDE, false, COUNT>(s, pool, range, stack, status)) {
 		}
 	ray_finish(s, level, out);
 	nfetch = s.nfetch;
@@ -318,8 +325,9 @@ SVO_DEV uint32_t camera_row_end(const MarchArgs &a) {
 
 // Variants (chosen per launch from the launch-parameter table): TPB threads per block, RPL rays per lane
 // per ticket, SHARED: stack in shared memory ([level][thread], 32 distinct banks per warp) or in a
-// private local-memory array.
-template <bool CAMERA, int TPB, int RPL, bool SHARED>
+// private local-memory array.  COUNT: the launch reports node fetches (a.fetches); a separate
+// instantiation, so the usual launch carries no counter and no second copy of the loop.
+template <bool CAMERA, int TPB, int RPL, bool SHARED, bool COUNT>
 __global__ void __launch_bounds__(TPB) march_kernel(MarchArgs a) {
 	constexpr int kStride = SHARED ? TPB : 1;
 	__shared__ uint32_t s_stack[SHARED ? SVO_LEVEL_MAX * TPB : 1];
@@ -356,13 +364,13 @@ __global__ void __launch_bounds__(TPB) march_kernel(MarchArgs a) {
 				o[0] = p0.x, o[1] = p0.y, o[2] = p1.x, d[0] = p1.y, d[1] = p2.x, d[2] = p2.y;
 			}
 			MarchOut m;
-			uint32_t nf;
-			march_ray<kStride>(a.pool, a.range, a.level, o, d, stack, m, nf, a.status);
+			uint32_t nf = 0;
+			march_ray<kStride, COUNT>(a.pool, a.range, a.level, o, d, stack, m, nf, a.status);
 			store_hit(a.hits, r, m);
 			fetched += nf;
 		}
 	}
-	if (a.fetches) {
+	if (COUNT && a.fetches) {
 		fetched = warp_sum(fetched);
 		if (lane == 0) atomicAdd(a.fetches, fetched);
 	}
@@ -373,7 +381,7 @@ __global__ void __launch_bounds__(TPB) march_kernel(MarchArgs a) {
 // kRefillMin of them are idle, or all of them are.  Per ray the arithmetic is the single-ray march's.
 constexpr uint32_t kRefillMin = 8;
 
-template <bool CAMERA, int TPB, bool SHARED>
+template <bool CAMERA, int TPB, bool SHARED, bool COUNT>
 __global__ void __launch_bounds__(TPB) march_refill_kernel(MarchArgs a) {
 	constexpr int kStride = SHARED ? TPB : 1;
 	__shared__ uint32_t s_stack[SHARED ? SVO_LEVEL_MAX * TPB : 1];
@@ -425,7 +433,7 @@ __global__ void __launch_bounds__(TPB) march_refill_kernel(MarchArgs a) {
 			if (exhausted) break;
 			continue;
 		}
-		if (active && ray_step<kStride>(s, a.pool, a.range, stack, a.status)) {
+		if (active && ray_step<kStride, true, COUNT>(s, a.pool, a.range, stack, a.status)) {
 			MarchOut m;
 			ray_finish(s, a.level, m);
 			store_hit(a.hits, r, m);
@@ -612,6 +620,7 @@ __global__ void __launch_bounds__(kMarchTPB) beam_kernel(MarchArgs a, float *__r
 // which no texel value has.  Every value is the separate kernels' value bit for bit.
 constexpr uint32_t kBeamUnset = 0xffffffffu;
 
+template <bool COUNT>
 __global__ void __launch_bounds__(kMarchTPB) march_beam_fused_kernel(MarchArgs a, float *__restrict__ beam,
                                                                      float orig_sz) {
 	__shared__ uint32_t s_stack[SVO_LEVEL_MAX * kMarchTPB];
@@ -672,8 +681,8 @@ __global__ void __launch_bounds__(kMarchTPB) march_beam_fused_kernel(MarchArgs a
 #pragma unroll
 			for (int k = 0; k < 3; ++k) o[k] = o[k] + d[k] * m;
 			MarchOut mo;
-			uint32_t nf;
-			march_ray<kMarchTPB>(a.pool, a.range, a.level, o, d, stack, mo, nf, a.status);
+			uint32_t nf = 0;
+			march_ray<kMarchTPB, COUNT>(a.pool, a.range, a.level, o, d, stack, mo, nf, a.status);
 			mo.voxel_hi |= waited_out;
 			store_hit(a.hits, r, mo);
 			fetched += nf;
@@ -918,7 +927,7 @@ SVO_DEV bool pt_leaf(const PtArgs &a, const float o[3], const float dir[3], uint
 	for (int k = 0; k < 3; ++k) d[k] = fabsf(dir[k]) >= kEps ? dir[k] : (dir[k] >= 0.0f ? kEps : -kEps);
 	MarchOut m;
 	uint32_t nf;
-	march_ray<STRIDE>(a.pool, a.range, a.level, o, d, stack, m, nf, a.status);
+	march_ray<STRIDE, false>(a.pool, a.range, a.level, o, d, stack, m, nf, a.status);
 	const uint32_t flags = m.voxel_hi >> 16;
 #pragma unroll
 	for (int k = 0; k < 3; ++k) {
@@ -1084,7 +1093,7 @@ __global__ void __launch_bounds__(kMarchTPB) pt_bounce_refill_kernel(PtArgs a, u
 			continue;
 		}
 		bool alive = false;
-		if (active && ray_step<kMarchTPB>(s, a.pool, a.range, stack, a.status)) {
+		if (active && ray_step<kMarchTPB, true, false>(s, a.pool, a.range, stack, a.status)) {
 			MarchOut m;
 			ray_finish(s, a.level, m);
 			const uint32_t flags = m.voxel_hi >> 16;
@@ -1187,6 +1196,7 @@ SVO_DEV uint32_t job_of(const MarchJob *__restrict__ jobs, uint32_t njobs, uint6
 	return lo;
 }
 
+template <bool COUNT>
 __global__ void __launch_bounds__(kMarchTPB) march_jobs_kernel(const MarchJob *__restrict__ jobs, uint32_t njobs,
                                                                 uint64_t total, unsigned long long *ticket,
                                                                 uint32_t *status, unsigned long long *fetches) {
@@ -1222,13 +1232,13 @@ __global__ void __launch_bounds__(kMarchTPB) march_jobs_kernel(const MarchJob *_
 		}
 		if (live) {
 			MarchOut m;
-			uint32_t nf;
-			march_ray<kMarchTPB>(J.pool, J.range, J.level, o, d, stack, m, nf, status + J.req);
+			uint32_t nf = 0;
+			march_ray<kMarchTPB, COUNT>(J.pool, J.range, J.level, o, d, stack, m, nf, status + J.req);
 			store_hit(J.hits, r, m);
 			fetched += nf;
 		}
 	}
-	if (fetches) {
+	if (COUNT && fetches) {
 		fetched = warp_sum(fetched);
 		if (lane == 0 && fetched) atomicAdd(fetches, fetched);
 	}
@@ -1251,7 +1261,7 @@ __global__ void bounce_jobs_kernel(const BounceJob *__restrict__ jobs, uint32_t 
 }
 
 // ---------------------------------------------------------------------------------------------------
-template <bool CAMERA, int TPB, int RPL, bool SHARED>
+template <bool CAMERA, int TPB, int RPL, bool SHARED, bool COUNT = false>
 static void launch_variant(const MarchArgs &a, cudaStream_t stream) {
 	const int sms = device_sm_count();
 	const uint64_t warps_needed = ((uint64_t)a.n + 32 * RPL - 1) / (32 * RPL);
@@ -1259,7 +1269,7 @@ static void launch_variant(const MarchArgs &a, cudaStream_t stream) {
 	const uint64_t cap = (uint64_t)sms * (2048 / TPB); // persistent: a full SM's worth of threads
 	const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(blocks_needed, cap));
 	SVO_LAUNCH(CAMERA ? "march_camera" : "march_rays", stream,
-	           march_kernel<CAMERA, TPB, RPL, SHARED><<<blocks, TPB, 0, stream>>>(a););
+	           march_kernel<CAMERA, TPB, RPL, SHARED, COUNT><<<blocks, TPB, 0, stream>>>(a););
 }
 
 template <bool CAMERA, int TPB, bool SHARED> static void launch_refill(const MarchArgs &a, cudaStream_t stream) {
@@ -1268,7 +1278,7 @@ template <bool CAMERA, int TPB, bool SHARED> static void launch_refill(const Mar
 	const uint64_t cap = (uint64_t)sms * (2048 / TPB);
 	const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(blocks_needed, cap));
 	SVO_LAUNCH(CAMERA ? "march_camera" : "march_rays", stream,
-	           march_refill_kernel<CAMERA, TPB, SHARED><<<blocks, TPB, 0, stream>>>(a););
+	           march_refill_kernel<CAMERA, TPB, SHARED, false><<<blocks, TPB, 0, stream>>>(a););
 }
 
 template <bool CAMERA, int TPB>
@@ -1286,6 +1296,10 @@ static void launch_rpl(const MarchArgs &a, int rpl, bool shared, cudaStream_t st
 }
 
 template <bool CAMERA> static void launch_tuned(const MarchArgs &a, cudaStream_t stream) {
+	if (a.fetches) { // a launch that counts node fetches: the default variant with the counter
+		launch_variant<CAMERA, 128, 1, true, true>(a, stream);
+		return;
+	}
 	const int tpb = tune_value(kTuneMarchBlock, a.level, a.n);
 	// camera rays and ray buffers (bounce rays, usually incoherent) have their own rays-per-lane choice
 	const int rpl = tune_value(CAMERA ? kTuneMarchRays : kTuneMarchBufferRays, a.level, a.n);
@@ -1331,7 +1345,12 @@ cudaError_t march_jobs_launch(const MarchJob *jobs, uint32_t njobs, uint64_t tot
 	const int sms = device_sm_count();
 	const uint64_t blocks_needed = (total / 32 + kMarchTPB / 32 - 1) / (kMarchTPB / 32);
 	const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(blocks_needed, (uint64_t)sms * 16));
-	SVO_LAUNCH("march_jobs", stream, march_jobs_kernel<<<blocks, kMarchTPB, 0, stream>>>(jobs, njobs, total, ticket, status, fetches););
+	if (fetches)
+		SVO_LAUNCH("march_jobs", stream,
+		           march_jobs_kernel<true><<<blocks, kMarchTPB, 0, stream>>>(jobs, njobs, total, ticket, status, fetches););
+	else
+		SVO_LAUNCH("march_jobs", stream,
+		           march_jobs_kernel<false><<<blocks, kMarchTPB, 0, stream>>>(jobs, njobs, total, ticket, status, nullptr););
 	return cudaGetLastError();
 }
 
@@ -1369,7 +1388,10 @@ cudaError_t march_beam_fused_launch(const MarchArgs &a, float *beam, cudaStream_
 	const uint64_t blocks_needed = (slots / 32 + kMarchTPB / 32 - 1) / (kMarchTPB / 32);
 	const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(blocks_needed, (uint64_t)sms * 16));
 	const float orig_sz = ldexpf(1.0f, 1 - (int)a.level);
-	SVO_LAUNCH("march_beam", stream, march_beam_fused_kernel<<<blocks, kMarchTPB, 0, stream>>>(a, beam, orig_sz););
+	if (a.fetches)
+		SVO_LAUNCH("march_beam", stream, march_beam_fused_kernel<true><<<blocks, kMarchTPB, 0, stream>>>(a, beam, orig_sz););
+	else
+		SVO_LAUNCH("march_beam", stream, march_beam_fused_kernel<false><<<blocks, kMarchTPB, 0, stream>>>(a, beam, orig_sz););
 	return cudaGetLastError();
 }
 

@@ -248,10 +248,11 @@ static cudaError_t issue(Server *S, Lane &L) {
 		}
 	}
 	unsigned long long *ticket = (unsigned long long *)(dev + o_ticket);
-	unsigned long long *fetches = ticket + 1;
+	// the node-fetch count is kept only when the server was asked to (it costs the march ~7%)
+	unsigned long long *fetches = (S->cfg.flags & SVO_SERVER_COUNT_FETCHES) ? ticket + 1 : nullptr;
 	uint32_t *status = (uint32_t *)(ticket + 2);
 	e = cudaMemcpyAsync(dev, host, table_bytes, cudaMemcpyHostToDevice, L.s);
-	if (e == cudaSuccess) e = cudaMemsetAsync(fetches, 0, 8 + 4 * nb, L.s);
+	if (e == cudaSuccess) e = cudaMemsetAsync(ticket + 1, 0, 8 + 4 * nb, L.s);
 	for (size_t i = 0; i < nb && e == cudaSuccess; ++i)
 		if (batch[i]->tr.mode == SVO_REQUEST_RAYS)
 			e = cudaMemcpyAsync(dev + o_rays[i], batch[i]->tr.rays, sizeof(svo_ray) * batch[i]->tr.n_rays,
@@ -267,7 +268,7 @@ static cudaError_t issue(Server *S, Lane &L) {
 		const uint64_t n = !hits_mapped[i] ? batch[i]->hits : (t.mode == SVO_REQUEST_CAMERA ? t.n_primary : 0);
 		if (n) e = cudaMemcpyAsync(t.hits, dev + o_hits[i], sizeof(svo_hit) * n, cudaMemcpyDeviceToHost, L.s);
 	}
-	if (e == cudaSuccess) e = cudaMemcpyAsync(L.staging, fetches, 8 + 4 * nb, cudaMemcpyDeviceToHost, L.s);
+	if (e == cudaSuccess) e = cudaMemcpyAsync(L.staging, ticket + 1, 8 + 4 * nb, cudaMemcpyDeviceToHost, L.s);
 	if (e == cudaSuccess) e = cudaEventRecord(L.done, L.s);
 	return e;
 }
@@ -456,10 +457,14 @@ int svo_server_create(const svo_server_config *cfg, svo_server **out) {
 	memset(&S->st, 0, sizeof(S->st));
 	cudaGetDevice(&S->device);
 	S->t0 = Clock::now();
-	cudaError_t e = cudaStreamCreateWithFlags(&S->rb_stream, cudaStreamNonBlocking);
+	// trace lanes at the device's highest stream priority, rebuilds at its lowest: when both have blocks
+	// waiting for an SM, a trace batch's go first, so requests queued behind a rebuild wait less
+	int least = 0, greatest = 0;
+	cudaError_t e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+	if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&S->rb_stream, cudaStreamNonBlocking, least);
 	for (uint32_t i = 0; i < c.lanes && e == cudaSuccess; ++i) {
 		auto L = std::make_unique<Lane>();
-		e = cudaStreamCreateWithFlags(&L->s, cudaStreamNonBlocking);
+		e = cudaStreamCreateWithPriority(&L->s, cudaStreamNonBlocking, greatest);
 		if (e == cudaSuccess) e = cudaEventCreateWithFlags(&L->done, cudaEventDisableTiming);
 		S->lanes.push_back(std::move(L));
 	}

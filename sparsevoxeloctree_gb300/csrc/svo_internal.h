@@ -60,23 +60,30 @@ struct ProfScope {
 	} while (0)
 int device_sm_count();   // SMs of the current device (cached per device)
 
-// A fork of the caller's stream onto a second stream of the calling thread (one per thread and device,
-// so concurrent callers and stream captures never share it) and back, with events made per call.  When
-// a stream or event cannot be had, every "side" launch runs on the caller's stream instead.
+// A fork of the caller's stream onto a second stream of the calling thread (one per thread, device and
+// stream priority, so concurrent callers and stream captures never share it, and the side work keeps
+// the caller's priority) and back, with events made per call.  When a stream or event cannot be had,
+// every "side" launch runs on the caller's stream instead.
 class SideFork {
 public:
 	explicit SideFork(cudaStream_t main, bool enabled = true) : main_(main) {
 		if (!enabled) return;
-		thread_local cudaStream_t side = nullptr;
-		thread_local int side_dev = -1;
-		int dev = 0;
+		constexpr int kSlots = 8; // priority levels kept apart (the device's range is smaller)
+		thread_local cudaStream_t sides[kSlots] = {};
+		thread_local int side_dev[kSlots] = {-1, -1, -1, -1, -1, -1, -1, -1};
+		int dev = 0, prio = 0, least = 0, greatest = 0;
 		if (cudaGetDevice(&dev) != cudaSuccess) return;
-		if (!side || side_dev != dev) {
-			if (cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking) != cudaSuccess) {
+		if (cudaStreamGetPriority(main, &prio) != cudaSuccess ||
+		    cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess)
+			prio = least = greatest = 0;
+		const int slot = std::min(std::max(least - prio, 0), kSlots - 1);
+		cudaStream_t &side = sides[slot];
+		if (!side || side_dev[slot] != dev) {
+			if (cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, prio) != cudaSuccess) {
 				side = nullptr;
 				return;
 			}
-			side_dev = dev;
+			side_dev[slot] = dev;
 		}
 		for (cudaEvent_t &e : ev_)
 			if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return;

@@ -579,3 +579,43 @@ def test_every_march_variant_matches_oracle(cuda):
             assert_hits_equal(api.hits_numpy(tr.Trace(rays_dev)), ref_rays)
     finally:
         _lib.load().svo_tune_reset()
+
+
+def test_node_fetch_counts_match_oracle(cuda):
+    """Launches that report node fetches run their own kernel instantiation (the usual launch carries no
+    counter): the count equals the oracle's per-ray fetches summed, and the hits are the same as
+    without counting, for camera rays, a ray buffer and the counting server."""
+    import torch
+    api = _api()
+    s = scenes.plain_256()
+    frags = oracle.voxelize(s.tris, s.level)
+    pool = oracle.build_octree(frags, s.level)
+    octree, _ = gpu_build(frags, s.level)
+    tr = api.OctreeTracer.Create(octree, s.camera, s.width, s.height)
+    ref_hits, ref_f = oracle.raycast(pool, s.level, oracle.camera_rays(s.camera, s.width, s.height),
+                                     return_fetches=True)
+    plain = api.hits_numpy(tr.CmdDrawPipeline())
+    counted = api.hits_numpy(tr.CmdDrawPipeline(count_fetches=True))
+    torch.cuda.synchronize()
+    assert_hits_equal(plain, ref_hits)
+    assert_hits_equal(counted, ref_hits)
+    assert int(tr.fetches.item()) == int(ref_f.sum())
+    g = np.random.default_rng(23)
+    o, d = scenes.random_rays(g, 20000, inside=True)
+    rays = rays_from_arrays(o, d)
+    ref_hits, ref_f = oracle.raycast(pool, s.level, rays, return_fetches=True)
+    t2 = api.OctreeTracer.Create(octree)
+    got = api.hits_numpy(t2.Trace(api.to_device(rays), count_fetches=True))
+    torch.cuda.synchronize()
+    assert_hits_equal(got, ref_hits)
+    assert int(t2.fetches.item()) == int(ref_f.sum())
+    server = api.Server(lanes=1, count_fetches=True)
+    try:
+        sid = server.AddOctree(octree)
+        rh = torch.from_numpy(rays.view(np.uint8).copy()).pin_memory()
+        hh = torch.empty(len(rays) * HIT_DTYPE.itemsize, dtype=torch.uint8).pin_memory()
+        assert server.Wait(server.SubmitRays(sid, rh, hh))["status"] == 0
+        assert_hits_equal(hh.numpy().view(HIT_DTYPE), ref_hits)
+        assert server.stats()["node_fetches"] == int(ref_f.sum())
+    finally:
+        server.close()
