@@ -293,15 +293,15 @@ static int batch_build(Batcher &b, const svo_batch_mesh *meshes, uint32_t M, cud
 		bm.level = level;
 		bm.count = count;
 		bm.frag_base = r.frag_base;
-		bm.dv.D = dense_depth(level);
-		const uint32_t words = dense_layout(level, bm.dv.off);
+		bm.dv.D = dense_depth(level, count);
+		const uint32_t words = dense_layout(bm.dv.D, bm.dv.off);
 		const uint32_t region = bm.dv.D ? (words + 1 + kBuildScanTile - 1) / kBuildScanTile * kBuildScanTile : 0u;
 		bm.dense_base = dense_total;
 		bm.mark_word = dense_total + bm.dv.off[bm.dv.D];
 		bm.parent_off = level > 1 ? bm.dv.off[std::min(level - 1, kDenseMaxDepth + 1)] : 0u;
 		bm.item_base = items_total;
 		bm.bucket_base = nb_total;
-		bm.bshift = bucket_shift(level);
+		bm.bshift = bucket_shift(level, bm.dv.D);
 		bm.nb = 1u << (3 * (level - bm.bshift));
 		const uint64_t sorted_base = (sorted_total + 3) & ~3ull; // 32-byte aligned per mesh (vector loads)
 		bm.sorted_pad = (uint32_t)(sorted_base - r.frag_base);
@@ -310,13 +310,13 @@ static int batch_build(Batcher &b, const svo_batch_mesh *meshes, uint32_t M, cud
 		r.pool_base = pool_words;
 		pool_words += (r.capacity + 63) & ~63ull; // 256-byte aligned pools
 		dense_total += region;
-		items_total += dense_items(level, bm.dv.off);
+		items_total += dense_items(level, bm.dv.D, bm.dv.off);
 		nb_total += bm.nb;
 		hfb[m + 1] = r.frag_base + count;
 		hbb[m + 1] = nb_total;
 		hib[m + 1] = items_total;
 		hdb[m + 1] = dense_total;
-		reduce_total += dense_reduce_chunks(level);
+		reduce_total += dense_reduce_chunks(bm.dv.D);
 		hrb[m + 1] = reduce_total;
 		p.max_level = std::max(p.max_level, level);
 		p.max_D = std::max(p.max_D, bm.dv.D);

@@ -301,8 +301,7 @@ SVO_DEV void reduce_chunk(const DenseView &dv, uint32_t chunk_idx, uint32_t (*s_
 	}
 }
 
-uint32_t dense_reduce_chunks(uint32_t level) {
-	const uint32_t D = dense_depth(level);
+uint32_t dense_reduce_chunks(uint32_t D) {
 	if (D < 2) return 0;
 	const uint32_t words_D = (1u << (3 * D)) / 32u;
 	return (words_D + kReduceChunk - 1) / kReduceChunk;
@@ -400,10 +399,10 @@ template <bool B> __global__ void dense_finish(BuildBatch bb) {
 	}
 }
 
-// Writes the child blocks of every occupied cell of depths 0 (the root) .. D that has interior or
-// sparse children: interior words of depths 1..D, and zeroed words of depth D+1 when sparse levels
-// follow.  When depth D+1 is the leaf depth, depth-D cells are skipped: the leaf stage writes those
-// blocks whole.  One bitmap word and one prefix word of the child depth serve all 8 children.
+// Writes the child blocks of every occupied cell of depths 0 (the root) .. D-1: the interior words of
+// depths 1..D.  The blocks of depth-D cells are the leaf stage's when depth D+1 is the leaf depth, and
+// zero_level's when sparse depths follow.  One bitmap word and one prefix word of the child depth serve
+// all 8 children.
 template <bool B>
 __global__ void __launch_bounds__(kTPB) dense_write(BuildBatch bb, uint32_t total_items) {
 	if (bb.gstate->status & kStatusAbort) return; // the prefix is not a complete scan: write nothing
@@ -449,6 +448,24 @@ __global__ void __launch_bounds__(kTPB) dense_write(BuildBatch bb, uint32_t tota
 			dst[1] = make_uint4(w[4], w[5], w[6], w[7]);
 		}
 	}
+}
+
+// Zeroes the word range of `depth` (the first sparse depth: the init of shader/octree_init_node.comp:7-11
+// for the blocks of the depth-D cells) with 16-byte stores, grid-stride.  The range is 8-word aligned.
+// A range beyond the pool is reported as a capacity overflow and not written.
+__global__ void __launch_bounds__(kTPB) zero_level(uint32_t *__restrict__ pool, uint64_t capacity, BuildState *state,
+                                                   uint32_t depth, const BuildState *gstate) {
+	if (gstate->status & kStatusAbort) return; // the level range comes from an incomplete scan
+	const LevelInfo li = state->lv[depth];
+	const uint64_t begin = li.begin, end = begin + li.num;
+	if (end > capacity || end > SVO_MAX_POOL_WORDS) {
+		if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&state->status, kStatusCapacity);
+		return;
+	}
+	uint4 *dst = reinterpret_cast<uint4 *>(pool + begin);
+	const uint64_t n4 = (end - begin) / 4;
+	for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (uint64_t)gridDim.x * blockDim.x)
+		dst[i] = make_uint4(0u, 0u, 0u, 0u);
 }
 
 // ------------------------------------------------------------------------------------------ tag (sparse levels)
@@ -598,10 +615,10 @@ __global__ void __launch_bounds__(kTPB) build_alloc(uint32_t *__restrict__ pool,
 // in the pool (breadth-first order is Morton order within a depth), so that block writes them whole.
 // In a batch the buckets of all meshes are concatenated in mesh order, so one scan over all of them
 // places every mesh's bucketed copy after the previous mesh's.
-// Bucket edge: 16 voxels while the leaf parents are dense (level <= 10): a bucket then spans at most one
-// leaf window's worth of leaf words (8^3 parents x 8), which the windowed leaf stage relies on; 32 voxels
-// for deeper octrees, where 16-voxel buckets would need 8^8 bucket counters at level 12.
-uint32_t bucket_shift(uint32_t level) { return std::min<uint32_t>(level, level <= kDenseMaxDepth + 1 ? 4u : 5u); }
+// Bucket edge: 16 voxels while the leaf parents are dense (level <= D + 1): a bucket then spans at most
+// one leaf window's worth of leaf words (8^3 parents x 8), which the windowed leaf stage relies on; 32
+// voxels when they are sparse, where 16-voxel buckets would need 8^8 bucket counters at level 12.
+uint32_t bucket_shift(uint32_t level, uint32_t D) { return std::min<uint32_t>(level, level <= D + 1 ? 4u : 5u); }
 
 // Leaf windows a dense-parent mesh can need: its leaf range is at most 8 words per possible parent.
 uint64_t leaf_window_bound(uint32_t count, uint32_t level) {
@@ -1077,12 +1094,14 @@ uint64_t build_pool_bound(uint32_t count, uint32_t level) {
 	return words < SVO_MAX_POOL_WORDS ? words : SVO_MAX_POOL_WORDS;
 }
 
-uint32_t dense_depth(uint32_t level) { return level - 1 < kDenseMaxDepth ? level - 1 : kDenseMaxDepth; }
+uint32_t dense_depth(uint32_t level, uint32_t count) {
+	const uint32_t D = level - 1 < 9u ? level - 1 : 9u;
+	return level >= 11 && count >= kDeepDenseMinFragments ? 10u : D;
+}
 
 uint32_t dense_words_of(uint32_t d) { return d <= 1 ? 1u : (1u << (3 * d)) / 32u; }
 
-uint32_t dense_layout(uint32_t level, uint32_t off[kDenseMaxDepth + 2]) {
-	const uint32_t D = dense_depth(level);
+uint32_t dense_layout(uint32_t D, uint32_t off[kDenseMaxDepth + 2]) {
 	uint32_t o = 0;
 	off[0] = 0;
 	for (uint32_t d = 1; d <= kDenseMaxDepth + 1; ++d) {
@@ -1092,16 +1111,15 @@ uint32_t dense_layout(uint32_t level, uint32_t off[kDenseMaxDepth + 2]) {
 	return o;
 }
 
-uint32_t dense_items(uint32_t level, const uint32_t off[kDenseMaxDepth + 2]) {
-	const uint32_t D = dense_depth(level);
+uint32_t dense_items(uint32_t level, uint32_t D, const uint32_t off[kDenseMaxDepth + 2]) {
+	(void)level;
 	if (D == 0) return 0;
-	const uint32_t last_parent_depth = D + 1 == level ? D - 1 : D;
-	return off[last_parent_depth + 1] + 1; // parent words of depths 1..last, and the root
+	return off[D] + 1; // parent words of depths 1..D-1, and the root
 }
 
 // Words of a mesh's dense scan region: its bitmap words and the total entry, padded to whole tiles.
-static uint32_t dense_region(uint32_t level, uint32_t words) {
-	return dense_depth(level) ? (words + 1 + kBuildScanTile - 1) / kBuildScanTile * kBuildScanTile : 0u;
+static uint32_t dense_region(uint32_t D, uint32_t words) {
+	return D ? (words + 1 + kBuildScanTile - 1) / kBuildScanTile * kBuildScanTile : 0u;
 }
 
 // Largest word range of one sparse depth: depth i spans 8 words per occupied cell of depth i-1, at most
@@ -1130,10 +1148,10 @@ void build_workspace_layout(void *ws, uint32_t count, uint32_t level, uint64_t c
 		off += align_up(bytes, 256);
 		return q;
 	};
-	const uint32_t D = dense_depth(level);
+	const uint32_t D = dense_depth(level, count);
 	w.dv.D = D;
-	const uint32_t o = dense_layout(level, w.dv.off);
-	w.dense_words = dense_region(level, o);
+	const uint32_t o = dense_layout(D, w.dv.off);
+	w.dense_words = dense_region(D, o);
 	w.state = (BuildState *)take(sizeof(BuildState));
 	uint64_t sparse_words = max_sparse_level_words(count, level, D);
 	if (sparse_words > capacity) sparse_words = capacity;
@@ -1142,7 +1160,7 @@ void build_workspace_layout(void *ws, uint32_t count, uint32_t level, uint64_t c
 	w.descs = (unsigned long long *)take(w.desc_count * sizeof(unsigned long long));
 	w.dv.bits = (uint32_t *)take((size_t)w.dense_words * 4 + 32);
 	w.dv.prefix = (uint32_t *)take((size_t)w.dense_words * 4 + 32);
-	w.bshift = bucket_shift(level);
+	w.bshift = bucket_shift(level, D);
 	w.nb = 1u << (3 * (level - w.bshift));
 	w.bcount = (uint32_t *)take((size_t)w.nb * 4);
 	w.bfill = (uint32_t *)take((size_t)w.nb * 4);
@@ -1176,7 +1194,7 @@ static BuildBatch single_batch(const BuildWorkspace &w, uint32_t count, uint32_t
 	bb.sorted_total = count;
 	bb.dense_total = w.dense_words;
 	bb.nb_total = w.nb;
-	bb.reduce_total = dense_reduce_chunks(level);
+	bb.reduce_total = dense_reduce_chunks(w.dv.D);
 	BuildMesh &m = bb.one;
 	m.pool = pool;
 	m.capacity = capacity;
@@ -1246,6 +1264,9 @@ static void launch_sparse(const uint64_t *sorted, uint32_t count, uint32_t level
 	const int sms = device_sm_count();
 	const uint32_t tag_blocks =
 	    grid_for(((uint64_t)count + 3) / 4, kTPB, (uint32_t)sms * (uint32_t)tune_value(kTuneSweepBlocks, level, count));
+	// the first sparse depth's words start at zero (later depths' blocks are zeroed by the alloc before)
+	SVO_LAUNCH("zero_level", stream,
+	           zero_level<<<(uint32_t)sms * 8, kTPB, 0, stream>>>(pool, capacity, state, dv.D + 1, gstate););
 	for (uint32_t depth = dv.D + 1; depth < level; ++depth) {
 		SVO_LAUNCH("build_tag", stream,
 		           build_tag<<<tag_blocks, kTPB, 0, stream>>>(sorted, count, level, depth, pool, cache, dv, state,
@@ -1290,7 +1311,7 @@ cudaError_t build_launch_interior(const uint64_t *frags, uint32_t count, uint32_
 	if (e == cudaSuccess) e = cudaMemsetAsync(w.bdescs, 0, w.bdesc_count * sizeof(unsigned long long), stream);
 	if (e != cudaSuccess) return e;
 	const BuildBatch bb = single_batch(w, count, level, pool, capacity);
-	const uint32_t items = dense_items(level, w.dv.off);
+	const uint32_t items = dense_items(level, w.dv.D, w.dv.off);
 	launch_dense_and_scatter<false>(frags, count, level, bb, 1, w.dv.D, w.dense_words, items, w.nb, w.state, w.descs, w.bcount,
 	                                w.boff, w.bfill, w.blist, w.bdescs, w.sorted, stream);
 	if (level > w.dv.D + 1)

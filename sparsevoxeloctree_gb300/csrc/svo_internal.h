@@ -210,7 +210,10 @@ struct BuildState {
 	uint32_t leaf_ticket;               // buckets claimed by the leaf stage
 };
 
-constexpr uint32_t kDenseMaxDepth = 9; // deepest depth held as a dense occupancy bitmap (8^9 bits)
+constexpr uint32_t kDenseMaxDepth = 10; // deepest depth held as a dense occupancy bitmap (8^10 bits, 128 MiB)
+// Fragments from which an octree of level >= 11 keeps depth 10 dense too: its 8^10-bit bitmap and prefix
+// (256 MiB, scanned once) cost about what one sparse tag + alloc pass over that many fragments does.
+constexpr uint32_t kDeepDenseMinFragments = 1u << 24;
 constexpr uint32_t kBuildScanTile = 8192; // words per tile of the dense scan (a mesh's dense region is a multiple)
 
 // Dense occupancy bitmaps of depths 1..D, concatenated (level d at word off[d]), and the exclusive
@@ -284,15 +287,15 @@ struct BuildWorkspace {
 	size_t total_bytes;
 };
 uint64_t build_pool_bound(uint32_t count, uint32_t level);
-uint32_t dense_depth(uint32_t level);
-uint32_t bucket_shift(uint32_t level); // bucket edge of the build's fragment buckets: 2^shift voxels
+uint32_t dense_depth(uint32_t level, uint32_t count); // deepest dense depth D of a build of `count` fragments
+uint32_t bucket_shift(uint32_t level, uint32_t D);   // bucket edge of the build's fragment buckets: 2^shift voxels
 uint64_t leaf_window_bound(uint32_t count, uint32_t level); // leaf windows a dense-parent mesh can need
 uint32_t dense_words_of(uint32_t d);
-uint32_t dense_reduce_chunks(uint32_t level); // work items of dense_reduce for a mesh at `level`
-// Words of the dense bitmaps of depths 1..dense_depth(level) (32-byte aligned levels) and their offsets.
-uint32_t dense_layout(uint32_t level, uint32_t off[kDenseMaxDepth + 2]);
+uint32_t dense_reduce_chunks(uint32_t D); // work items of dense_reduce for a mesh whose dense depth is D
+// Words of the dense bitmaps of depths 1..D (32-byte aligned levels) and their offsets.
+uint32_t dense_layout(uint32_t D, uint32_t off[kDenseMaxDepth + 2]);
 // dense_write items of a mesh (parent words of the depths whose child blocks it writes, plus the root).
-uint32_t dense_items(uint32_t level, const uint32_t off[kDenseMaxDepth + 2]);
+uint32_t dense_items(uint32_t level, uint32_t D, const uint32_t off[kDenseMaxDepth + 2]);
 uint64_t max_sparse_level_words(uint32_t count, uint32_t level, uint32_t D);
 void build_workspace_layout(void *ws, uint32_t count, uint32_t level, uint64_t capacity, BuildWorkspace &w);
 // Interior levels (dense bitmaps, then sparse tag/alloc); the leaf range ends up in state->lv[level].

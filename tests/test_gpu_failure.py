@@ -94,17 +94,18 @@ def test_build_scan_timeout_writes_nothing_through_its_offsets(cuda, wait_fault)
 
 
 def test_sparse_alloc_timeout_through_allocating_entry_point(cuda, wait_fault):
-    """The room shell at level 11: depths 1..9 are dense (a 586-tile bitmap scan), the bucket scan has
-    128 tiles, and the sparse alloc of depth 10 has about 1,536 tiles of 8192 words (8 per occupied
-    depth-9 cell, ~1.57 million cells on the walls).  Tile 700 exists only in that alloc, so only its
-    look-back gives up.  svo_build returns SVO_ERR_TIMEOUT and hands out no octree; the same call with the
-    hook cleared gives the octree of a fault-free build, word for word."""
+    """Three walls of the room shell at level 11 (12.6 M fragments, below the 2^24 from which depth 10 is
+    kept dense): depths 1..9 are dense (a 586-tile bitmap scan), the bucket scan has 128 tiles, and the
+    sparse alloc of depth 10 has about 768 tiles of 8192 words (8 per occupied depth-9 cell, ~786 k cells
+    on the walls).  Tile 700 exists only in that alloc, so only its look-back gives up.  svo_build returns
+    SVO_ERR_TIMEOUT and hands out no octree; the same call with the hook cleared gives the octree of a
+    fault-free build, word for word."""
     import torch
 
     from sparsevoxeloctree_gb300 import _lib, api
     lib = _lib.load()
     level = 11
-    tris = scenes._soup(scenes.room_shell(level), scenes.random_colors(scenes.rng(9), 12))
+    tris = scenes._soup(scenes.room_shell(level)[:6], scenes.random_colors(scenes.rng(9), 6))
     ft = api.voxelize(api.to_device(tris), level)
     n = int(ft.numel())
 
@@ -122,6 +123,7 @@ def test_sparse_alloc_timeout_through_allocating_entry_point(cuda, wait_fault):
     rc, oc = build()
     assert rc == _lib.SVO_OK, lib.svo_last_error()
     want = words(oc)
+    assert n < (1 << 24)  # the depth-10 words are built by the sparse alloc
     assert len(want) > 8 * 700 * 8192 // 8  # the depth-10 range spans more than 700 alloc tiles
     wait_fault(700)
     rc, oc = build()

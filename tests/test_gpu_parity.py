@@ -619,3 +619,16 @@ def test_node_fetch_counts_match_oracle(cuda):
         assert server.stats()["node_fetches"] == int(ref_f.sum())
     finally:
         server.close()
+
+
+@pytest.mark.parametrize("level,walls", [(11, 6), (12, 2)])
+def test_build_with_depth_10_dense_matches_oracle(cuda, level, walls):
+    """From 2^24 fragments up, octrees of level >= 11 keep depth 10 as a dense bitmap too: at level 11
+    the leaf parents are then dense (windowed leaf stage, 16^3-voxel buckets), at level 12 depth 11 is
+    the one sparse depth.  Walls of the room shell give 25.2 M (level 11, six walls) and 33.5 M (level 12,
+    two walls) fragments; the octree must be the oracle's word for word."""
+    tris = scenes._soup(scenes.room_shell(level)[: 2 * walls], scenes.random_colors(scenes.rng(level), 2 * walls))
+    frags = oracle.voxelize(tris, level)
+    assert len(frags) >= 1 << 24
+    _, got = gpu_build(frags, level)
+    assert np.array_equal(got, oracle.build_octree(frags, level))
