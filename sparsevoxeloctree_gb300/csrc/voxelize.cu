@@ -128,8 +128,21 @@ SVO_DEV void tri_setup(const svo_triangle *__restrict__ tris, uint32_t t, uint32
 	s.D = 256 * nc;
 }
 
-// Covered interval [lo, hi] of span v (empty when lo > hi).
-SVO_DEV void span_interval(const TriSetup &s, int32_t v, int32_t &lo, int32_t &hi) {
+// The fields of a triangle's set-up that span_interval reads, kept in shared memory so that the lanes
+// of a warp can evaluate the spans of each other's triangles.
+struct SpanSetup {
+	int32_t u0, u1, v0, level;
+	int32_t gu[3], gv[3], pu[3], pv[3];
+};
+
+SVO_DEV void span_setup(const TriSetup &s, SpanSetup &o) {
+	o.u0 = s.u0, o.u1 = s.u1, o.v0 = s.v0, o.level = s.level;
+#pragma unroll
+	for (int k = 0; k < 3; ++k) o.gu[k] = s.gu[k], o.gv[k] = s.gv[k], o.pu[k] = s.pu[k], o.pv[k] = s.pv[k];
+}
+
+// Covered interval [lo, hi] of span v (empty when lo > hi); S is TriSetup or SpanSetup.
+template <typename S> SVO_DEV void span_interval(const S &s, int32_t v, int32_t &lo, int32_t &hi) {
 	const int32_t R = 1 << s.level;
 	lo = s.u0;
 	hi = s.u1;
@@ -177,22 +190,19 @@ SVO_DEV uint32_t pieces_per_span(const TriSetup &s) { return (uint32_t)((s.u1 - 
 
 SVO_DEV uint32_t unit_count(const TriSetup &s) { return (uint32_t)(s.v1 - s.v0 + 1) * pieces_per_span(s); }
 
-SVO_DEV uint32_t count_serial(const TriSetup &s) {
-	uint32_t n = 0;
-	for (int32_t v = s.v0; v <= s.v1; ++v) {
+// The spans of a warp's small triangles, evaluated by all 32 lanes together instead of by each
+// triangle's own lane (whose row counts differ, so most lanes would idle): lane j's triangle owns rows
+// [incl[j] - rows_j, incl[j]) of the warp's row list (incl: the inclusive prefix of the row counts, in
+// shared memory at `incl`, the setups at `sp`).  fn(j, row, lo, hi) is called once per row.
+template <typename Fn>
+SVO_DEV void warp_rows(const uint32_t *incl, const SpanSetup *sp, uint32_t total, Fn fn) {
+	uint32_t j = 0;
+	for (uint32_t r = lane_id(); r < total; r += 32) {
+		while (incl[j] <= r) ++j;
+		const uint32_t row = r - (j ? incl[j - 1] : 0u);
 		int32_t lo, hi;
-		span_interval(s, v, lo, hi);
-		n += hi >= lo ? (uint32_t)(hi - lo + 1) : 0u;
-	}
-	return n;
-}
-
-SVO_DEV void emit_serial(const TriSetup &s, uint64_t *__restrict__ out) {
-	uint32_t k = 0;
-	for (int32_t v = s.v0; v <= s.v1; ++v) {
-		int32_t lo, hi;
-		span_interval(s, v, lo, hi);
-		for (int32_t u = lo; u <= hi; ++u) out[k++] = make_fragment(s, u, v);
+		span_interval(sp[j], sp[j].v0 + (int32_t)row, lo, hi);
+		fn(j, row, lo, hi);
 	}
 }
 
@@ -280,6 +290,9 @@ __global__ void __launch_bounds__(kTPB) vox_classify_scan(VoxBatch vb, uint32_t 
 	__shared__ uint32_t s_units[kTile];
 	__shared__ unsigned long long s_warp[kTPB / 32 + 1];
 	__shared__ unsigned long long s_prefix[2];
+	__shared__ SpanSetup s_sp[kTPB];
+	__shared__ uint32_t s_rows[kTPB];
+	const uint32_t wb = threadIdx.x & ~31u;
 	if (threadIdx.x == 0) s_tile = atomicAdd(&w.counters[kCtrTicketA], 1u);
 	__syncthreads();
 	const uint32_t tile = s_tile;
@@ -296,8 +309,20 @@ __global__ void __launch_bounds__(kTPB) vox_classify_scan(VoxBatch vb, uint32_t 
 			tri_setup(tp, local, lvl, s);
 		}
 		const bool large = is_large(s);
-		s_cnt[k * kTPB + threadIdx.x] = (s.valid && !large) ? count_serial(s) : 0u;
+		// small triangles: fragments = the covered lengths of their spans, counted by the whole warp
+		const uint32_t rows = (s.valid && !large) ? (uint32_t)(s.v1 - s.v0 + 1) : 0u;
+		if (rows) span_setup(s, s_sp[threadIdx.x]);
+		const uint32_t rincl = warp_inclusive_sum(rows);
+		s_rows[threadIdx.x] = rincl;
+		s_cnt[k * kTPB + threadIdx.x] = 0u;
 		s_units[k * kTPB + threadIdx.x] = large ? unit_count(s) : 0u;
+		__syncwarp();
+		uint32_t *cnt = s_cnt + k * kTPB + wb;
+		warp_rows(s_rows + wb, s_sp + wb, __shfl_sync(kFullMask, rincl, 31),
+		          [&](uint32_t j, uint32_t, int32_t lo, int32_t hi) {
+			          if (hi >= lo) atomicAdd(cnt + j, (uint32_t)(hi - lo + 1));
+		          });
+		__syncwarp();
 	}
 	__syncthreads();
 	unsigned long long lc = 0, lu = 0;
@@ -421,11 +446,12 @@ __global__ void __launch_bounds__(kEmitTPB) vox_emit(VoxBatch vb, uint32_t n, Vo
 	__shared__ uint8_t s_cum[kEmitTPB][kSmallArea + 1];
 	__shared__ int16_t s_lo[kEmitTPB][kSmallArea];
 	__shared__ uint32_t s_incl[kEmitTPB];
+	__shared__ SpanSetup s_sp[kEmitTPB];
 	const uint32_t lane = lane_id(), wb = threadIdx.x & ~31u;
 	const uint64_t warps = (uint64_t)gridDim.x * blockDim.x / 32;
 	for (uint64_t g = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32; g * 32 < n; g += warps) {
 		const uint64_t t = g * 32 + lane;
-		uint32_t cnt = 0;
+		uint32_t cnt = 0, rows = 0;
 		if (t < n) {
 			uint64_t off = w.small_off[t];
 			cnt = (uint32_t)(w.small_off[t + 1] - off);
@@ -443,23 +469,36 @@ __global__ void __launch_bounds__(kEmitTPB) vox_emit(VoxBatch vb, uint32_t n, Vo
 					r.K = S.K, r.NU = S.NU, r.NV = S.NV, r.D = S.D, r.off = off;
 					r.z0 = S.z0, r.z1 = S.z1, r.v0 = S.v0, r.level = S.level;
 					r.axis = (uint32_t)S.axis, r.cols = (uint32_t)S.cols, r.rgb = S.rgb, r.cnt = cnt;
-					uint32_t acc = 0;
-					const int32_t nspans = S.v1 - S.v0 + 1;
-					for (int32_t k = 0; k < nspans; ++k) {
-						int32_t lo, hi;
-						span_interval(S, S.v0 + k, lo, hi);
-						s_cum[threadIdx.x][k] = (uint8_t)acc;
-						s_lo[threadIdx.x][k] = (int16_t)lo;
-						acc += hi >= lo ? (uint32_t)(hi - lo + 1) : 0u;
-					}
-					s_cum[threadIdx.x][nspans] = (uint8_t)acc;
-					if (acc != cnt) cnt = 0; // cannot happen: the count pass walked the same spans
-					r.cnt = cnt;
-					// spans past the last one read as "no more fragments"
-					for (int32_t k = nspans + 1; k <= kSmallArea; ++k) s_cum[threadIdx.x][k] = 0xffu;
+					rows = (uint32_t)(S.v1 - S.v0 + 1);
+					span_setup(S, s_sp[threadIdx.x]);
 				}
 			}
 		}
+		// the spans of the warp's triangles, evaluated by the whole warp: each row's first pixel and covered
+		// length (the length parked in s_cum), then each triangle's running sum over its rows
+		const uint32_t rincl = warp_inclusive_sum(rows);
+		s_incl[threadIdx.x] = rincl;
+		__syncwarp();
+		warp_rows(s_incl + wb, s_sp + wb, __shfl_sync(kFullMask, rincl, 31),
+		          [&](uint32_t j, uint32_t row, int32_t lo, int32_t hi) {
+			          s_lo[wb + j][row] = (int16_t)lo;
+			          s_cum[wb + j][row] = (uint8_t)(hi >= lo ? hi - lo + 1 : 0);
+		          });
+		__syncwarp();
+		if (rows) {
+			uint32_t acc = 0;
+			for (uint32_t k = 0; k < rows; ++k) {
+				const uint32_t len = s_cum[threadIdx.x][k];
+				s_cum[threadIdx.x][k] = (uint8_t)acc;
+				acc += len;
+			}
+			s_cum[threadIdx.x][rows] = (uint8_t)acc;
+			if (acc != cnt) cnt = 0; // cannot happen: the count pass walked the same spans
+			s_rec[threadIdx.x].cnt = cnt;
+			// spans past the last one read as "no more fragments"
+			for (uint32_t k = rows + 1; k <= (uint32_t)kSmallArea; ++k) s_cum[threadIdx.x][k] = 0xffu;
+		}
+		__syncwarp();
 		const uint32_t incl = warp_inclusive_sum(cnt);
 		const uint32_t total = __shfl_sync(kFullMask, incl, 31);
 		s_incl[threadIdx.x] = incl;
