@@ -277,17 +277,25 @@ SVO_DEV void tri_of(const VoxBatch &vb, uint32_t t, const svo_triangle *&tris, u
 
 // ---------------------------------------------------------------------------------------------------
 constexpr int kTPB = 256;
+// Items per thread of the scan tiles.  Larger tiles mean fewer look-backs (a tile waits for the prefix
+// of the tiles before it) but more work per block: measured on the room, cluster and batch workloads,
+// the count pass takes 2 triangles per thread below 2^20 triangles and 4 from there (kTile, the tile of
+// the smaller form, sizes its descriptors), the unit scan 4 units per thread.
 constexpr int kIPT = 2;
 constexpr int kTile = kTPB * kIPT;
+constexpr uint32_t kBigCountTris = 1u << 20;
+constexpr int kUnitIPT = 4;
+constexpr int kUnitTile = kTPB * kUnitIPT;
 
 // Per triangle: small fragment count and large unit count, both exclusive-scanned.
 //   small_off[t] = fragments of small triangles before t; small_off[n] = small total
 //   unit_off[t]  = units of large triangles before t;    unit_off[n]  = unit total
-template <bool B>
+template <bool B, int IPT>
 __global__ void __launch_bounds__(kTPB) vox_classify_scan(VoxBatch vb, uint32_t n, VoxWorkspace w) {
+	constexpr int TILE = kTPB * IPT;
 	__shared__ uint32_t s_tile;
-	__shared__ uint32_t s_cnt[kTile];
-	__shared__ uint32_t s_units[kTile];
+	__shared__ uint32_t s_cnt[TILE];
+	__shared__ uint32_t s_units[TILE];
 	__shared__ unsigned long long s_warp[kTPB / 32 + 1];
 	__shared__ unsigned long long s_prefix[2];
 	__shared__ SpanSetup s_sp[kTPB];
@@ -296,9 +304,9 @@ __global__ void __launch_bounds__(kTPB) vox_classify_scan(VoxBatch vb, uint32_t 
 	if (threadIdx.x == 0) s_tile = atomicAdd(&w.counters[kCtrTicketA], 1u);
 	__syncthreads();
 	const uint32_t tile = s_tile;
-	const uint64_t base = (uint64_t)tile * kTile;
+	const uint64_t base = (uint64_t)tile * TILE;
 #pragma unroll 1
-	for (int k = 0; k < kIPT; ++k) {
+	for (int k = 0; k < IPT; ++k) {
 		const uint64_t t = base + (uint64_t)k * kTPB + threadIdx.x;
 		TriSetup s;
 		s.valid = 0;
@@ -327,9 +335,9 @@ __global__ void __launch_bounds__(kTPB) vox_classify_scan(VoxBatch vb, uint32_t 
 	__syncthreads();
 	unsigned long long lc = 0, lu = 0;
 #pragma unroll
-	for (int k = 0; k < kIPT; ++k) {
-		lc += s_cnt[threadIdx.x * kIPT + k];
-		lu += s_units[threadIdx.x * kIPT + k];
+	for (int k = 0; k < IPT; ++k) {
+		lc += s_cnt[threadIdx.x * IPT + k];
+		lu += s_units[threadIdx.x * IPT + k];
 	}
 	unsigned long long tc, tu;
 	const unsigned long long ec = block_exclusive_sum<unsigned long long, kTPB>(lc, s_warp, tc);
@@ -342,16 +350,16 @@ __global__ void __launch_bounds__(kTPB) vox_classify_scan(VoxBatch vb, uint32_t 
 	__syncthreads();
 	unsigned long long rc = s_prefix[0] + ec, ru = s_prefix[1] + eu;
 #pragma unroll
-	for (int k = 0; k < kIPT; ++k) {
-		const uint64_t t = base + (uint64_t)threadIdx.x * kIPT + k;
+	for (int k = 0; k < IPT; ++k) {
+		const uint64_t t = base + (uint64_t)threadIdx.x * IPT + k;
 		if (t < n) {
 			w.small_off[t] = rc;
 			w.unit_off[t] = (uint32_t)ru;
 		}
-		rc += s_cnt[threadIdx.x * kIPT + k];
-		ru += s_units[threadIdx.x * kIPT + k];
+		rc += s_cnt[threadIdx.x * IPT + k];
+		ru += s_units[threadIdx.x * IPT + k];
 	}
-	if (base + kTile >= n && base <= n && threadIdx.x == 0) {
+	if (base + TILE >= n && base <= n && threadIdx.x == 0) {
 		w.small_off[n] = s_prefix[0] + tc;
 		const unsigned long long units = s_prefix[1] + tu;
 		w.unit_off[n] = units > 0xffffffffull ? 0xffffffffu : (uint32_t)units;
@@ -368,26 +376,26 @@ __global__ void __launch_bounds__(kTPB) vox_unit_scan(VoxBatch vb, uint32_t n, V
 	__shared__ unsigned long long s_prefix;
 	const uint32_t units = w.unit_off[n];
 	if (units > w.unit_cap) return; // the host re-runs with a workspace sized for `units`
-	const uint32_t ntiles = (units + kTile - 1) / kTile;
+	const uint32_t ntiles = (units + kUnitTile - 1) / kUnitTile;
 	for (;;) {
 		if (threadIdx.x == 0) s_tile = atomicAdd(&w.counters[kCtrTicketB], 1u);
 		__syncthreads();
 		const uint32_t tile = s_tile;
 		__syncthreads();
 		if (tile >= ntiles) break;
-		uint32_t len[kIPT];
+		uint32_t len[kUnitIPT];
 		unsigned long long local = 0;
-		// the warp's kIPT * 32 consecutive units lie in triangles [t_first, t_last]
-		const uint32_t u_first = tile * kTile + (threadIdx.x & ~31u) * kIPT;
+		// the warp's kUnitIPT * 32 consecutive units lie in triangles [t_first, t_last]
+		const uint32_t u_first = tile * kUnitTile + (threadIdx.x & ~31u) * kUnitIPT;
 		uint32_t t_first = 0, t_end = 0;
 		if (u_first < units) {
-			const uint32_t u_last = min(u_first + 32 * kIPT - 1, units - 1);
+			const uint32_t u_last = min(u_first + 32 * kUnitIPT - 1, units - 1);
 			t_first = warp_upper_index(w.unit_off, 0, n, u_first);
 			t_end = warp_upper_index(w.unit_off, t_first, n, u_last) + 1;
 		}
 #pragma unroll
-		for (int k = 0; k < kIPT; ++k) {
-			const uint32_t u = tile * kTile + threadIdx.x * kIPT + k;
+		for (int k = 0; k < kUnitIPT; ++k) {
+			const uint32_t u = tile * kUnitTile + threadIdx.x * kUnitIPT + k;
 			len[k] = 0;
 			if (u < units) {
 				const uint32_t t = upper_index_in(w.unit_off, t_first, t_end, u);
@@ -412,8 +420,8 @@ __global__ void __launch_bounds__(kTPB) vox_unit_scan(VoxBatch vb, uint32_t n, V
 		__syncthreads();
 		unsigned long long run = s_prefix + excl;
 #pragma unroll
-		for (int k = 0; k < kIPT; ++k) {
-			const uint32_t u = tile * kTile + threadIdx.x * kIPT + k;
+		for (int k = 0; k < kUnitIPT; ++k) {
+			const uint32_t u = tile * kUnitTile + threadIdx.x * kUnitIPT + k;
 			if (u < units) w.unit_frag[u] = run;
 			run += len[k];
 		}
@@ -659,7 +667,7 @@ __global__ void __launch_bounds__(kTPB, 4) vox_emit_units(VoxBatch vb, uint32_t 
 // retries with vox_workspace_bytes(n, units).
 uint64_t vox_default_unit_cap(uint32_t n) { return 2ull * n + 65536; }
 
-static size_t tiles_for(uint64_t items) { return (size_t)((items + kTile - 1) / kTile + 1); }
+static size_t tiles_for(uint64_t items, uint64_t tile = kTile) { return (size_t)((items + tile - 1) / tile + 1); }
 
 size_t vox_workspace_bytes(uint32_t n, uint64_t unit_cap) {
 	VoxWorkspace w;
@@ -680,7 +688,7 @@ size_t vox_workspace_layout(void *ws, uint32_t n, uint64_t unit_cap, VoxWorkspac
 	w.unit_off = (uint32_t *)take(sizeof(uint32_t) * ((size_t)n + 1));
 	w.unit_frag = (unsigned long long *)take(sizeof(unsigned long long) * (size_t)(unit_cap + 1));
 	w.unit_tri = (uint32_t *)take(sizeof(uint32_t) * (size_t)(unit_cap + 1));
-	const size_t t1 = tiles_for(n), t3 = tiles_for(unit_cap);
+	const size_t t1 = tiles_for(n), t3 = tiles_for(unit_cap, kUnitTile);
 	w.descs = (unsigned long long *)(p + off);
 	w.desc_bytes = align_up((2 * t1 + t3) * sizeof(unsigned long long), 256);
 	w.descs2 = w.descs + t1;
@@ -714,7 +722,11 @@ static cudaError_t clear_count_state(uint32_t n, const VoxWorkspace &w, cudaStre
 }
 
 template <bool B> static void launch_count(const VoxBatch &vb, uint32_t n, const VoxWorkspace &w, cudaStream_t stream) {
-	SVO_LAUNCH("vox_classify_scan", stream, vox_classify_scan<B><<<(n + kTile - 1) / kTile, kTPB, 0, stream>>>(vb, n, w););
+	if (n >= kBigCountTris)
+		SVO_LAUNCH("vox_classify_scan", stream,
+		           vox_classify_scan<B, 2 * kIPT><<<(n + 2 * kTile - 1) / (2 * kTile), kTPB, 0, stream>>>(vb, n, w););
+	else
+		SVO_LAUNCH("vox_classify_scan", stream, vox_classify_scan<B, kIPT><<<(n + kTile - 1) / kTile, kTPB, 0, stream>>>(vb, n, w););
 	const int sms = device_sm_count();
 	SVO_LAUNCH("vox_unit_scan", stream, vox_unit_scan<B><<<(uint32_t)sms * 4, kTPB, 0, stream>>>(vb, n, w););
 }
