@@ -155,6 +155,7 @@ SVO_DEV void flag_bad_fragment(BuildState *state, BuildState *g) {
 // ------------------------------------------------------------------------------------------ init
 // Block m clears mesh m's state (and block 0 the batch-wide state of a batch).
 template <bool B> __global__ void build_init(BuildBatch bb, BuildState *gstate) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	BuildState *state = mesh_at<B>(bb, blockIdx.x).state;
 	uint32_t *s = reinterpret_cast<uint32_t *>(state);
 	for (uint32_t k = threadIdx.x; k < sizeof(BuildState) / 4; k += blockDim.x) s[k] = 0u;
@@ -186,6 +187,7 @@ template <uint32_t R> SVO_DEV uint64_t sweep_run_stride() { return (uint64_t)gri
 template <bool B>
 __global__ void __launch_bounds__(kTPB) dense_mark(const uint64_t *__restrict__ frags, uint64_t n, BuildBatch bb,
                                                    uint32_t *__restrict__ bcount) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	__shared__ uint32_t s_spread[kSpreadEntries];
 	spread_table_init(s_spread);
 	const uint64_t runs = (n + 31ull) >> 5;
@@ -308,6 +310,7 @@ uint32_t dense_reduce_chunks(uint32_t D) {
 }
 
 template <bool B> __global__ void __launch_bounds__(256) dense_reduce(BuildBatch bb) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	__shared__ uint32_t s_buf[2][kReduceChunk / 8];
 	const uint32_t total = bb.reduce_total;
 	for (uint32_t item = blockIdx.x; item < total; item += gridDim.x) {
@@ -331,6 +334,7 @@ static_assert(kDenseTile == kBuildScanTile, "dense regions are padded to whole s
 template <bool B>
 __global__ void __launch_bounds__(kTPB) dense_scan(BuildBatch bb, uint32_t total_words, BuildState *gstate,
                                                    unsigned long long *descs) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	__shared__ uint32_t s_tile;
 	__shared__ uint32_t s_warp[kTPB / 32 + 1];
 	__shared__ uint32_t s_prefix;
@@ -381,6 +385,7 @@ __global__ void __launch_bounds__(kTPB) dense_scan(BuildBatch bb, uint32_t total
 // Level ranges of depths 1..D+1 from the scanned counts (BuildState.lv as the sparse stage keeps it);
 // one thread per mesh.
 template <bool B> __global__ void dense_finish(BuildBatch bb) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	for (uint32_t mi = blockIdx.x * blockDim.x + threadIdx.x; mi < batch_size<B>(bb); mi += gridDim.x * blockDim.x) {
 		const BuildMesh md = mesh_at<B>(bb, mi);
 		const DenseView &dv = md.dv;
@@ -405,6 +410,7 @@ template <bool B> __global__ void dense_finish(BuildBatch bb) {
 // all 8 children.
 template <bool B>
 __global__ void __launch_bounds__(kTPB) dense_write(BuildBatch bb, uint32_t total_items) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	if (bb.gstate->status & kStatusAbort) return; // the prefix is not a complete scan: write nothing
 	for (uint32_t gitem = blockIdx.x * blockDim.x + threadIdx.x; gitem < total_items; gitem += gridDim.x * blockDim.x) {
 		const uint32_t mi = B ? mesh_search(bb.item_base, bb.M, gitem) : 0u;
@@ -455,6 +461,7 @@ __global__ void __launch_bounds__(kTPB) dense_write(BuildBatch bb, uint32_t tota
 // A range beyond the pool is reported as a capacity overflow and not written.
 __global__ void __launch_bounds__(kTPB) zero_level(uint32_t *__restrict__ pool, uint64_t capacity, BuildState *state,
                                                    uint32_t depth, const BuildState *gstate) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	if (gstate->status & kStatusAbort) return; // the level range comes from an incomplete scan
 	const LevelInfo li = state->lv[depth];
 	const uint64_t begin = li.begin, end = begin + li.num;
@@ -489,6 +496,7 @@ __global__ void __launch_bounds__(kTPB) build_tag(const uint64_t *__restrict__ f
                                                   uint32_t depth, uint32_t *__restrict__ pool,
                                                   uint32_t *__restrict__ cache, DenseView dv, BuildState *state,
                                                   const BuildState *gstate) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	if ((state->status & kStatusCapacity) || (gstate->status & kStatusAbort)) return;
 	const bool parent_dense = depth == 1 || depth - 1 <= dv.D;
 	const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -521,6 +529,7 @@ __global__ void __launch_bounds__(kTPB) build_tag(const uint64_t *__restrict__ f
 __global__ void __launch_bounds__(kTPB) build_alloc(uint32_t *__restrict__ pool, uint64_t capacity, uint32_t depth,
                                                     uint32_t level, BuildState *state, unsigned long long *descs,
                                                     BuildState *gstate) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	__shared__ uint32_t s_tile;
 	__shared__ uint32_t s_warp[kTPB / 32 + 1];
 	__shared__ uint32_t s_prefix;
@@ -632,6 +641,7 @@ uint64_t leaf_window_bound(uint32_t count, uint32_t level) {
 __global__ void __launch_bounds__(kTPB) bucket_scan(const uint32_t *__restrict__ bcount, uint32_t nb,
                                                     uint32_t *__restrict__ boff, uint32_t *__restrict__ blist,
                                                     BuildState *state, unsigned long long *descs) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	__shared__ uint32_t s_tile;
 	__shared__ uint32_t s_warp[kTPB / 32 + 1];
 	__shared__ uint32_t s_prefix[2];
@@ -681,6 +691,7 @@ template <bool B>
 __global__ void __launch_bounds__(kTPB) bucket_scatter(const uint64_t *__restrict__ frags, uint64_t n, BuildBatch bb,
                                                        const uint32_t *__restrict__ boff, uint32_t *__restrict__ bfill,
                                                        uint64_t *__restrict__ sorted) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	__shared__ uint32_t s_spread[kSpreadEntries];
 	spread_table_init(s_spread);
 	const uint64_t runs = (n + 31ull) >> 5;
@@ -808,6 +819,7 @@ SVO_DEV uint2 bucket_span(const BuildMesh &md, uint32_t bl, uint32_t leaf_begin,
 
 // Exclusive prefix of the meshes' window counts (one block); win_base[M] = windows of the batch.
 template <bool B> __global__ void __launch_bounds__(kTPB) leaf_window_scan(BuildBatch bb, uint32_t *__restrict__ win_base) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	__shared__ uint32_t s_warp[kTPB / 32 + 1];
 	uint32_t carry = 0;
 	const uint32_t M = batch_size<B>(bb);
@@ -833,6 +845,7 @@ template <bool B> __global__ void __launch_bounds__(kTPB) leaf_window_scan(Build
 template <bool B>
 __global__ void bucket_meta(BuildBatch bb, const uint32_t *__restrict__ boff, const uint32_t *__restrict__ blist,
                             const BuildState *gstate, uint4 *__restrict__ meta) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	// after an aborted scan the bucket list may hold entries no tile wrote: nothing is read through it
 	const uint32_t nbuckets = (gstate->status & kStatusAbort) ? 0u : gstate->buckets;
 	for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nbuckets; t += gridDim.x * blockDim.x) {
@@ -864,6 +877,7 @@ __global__ void __launch_bounds__(kTPB) bucket_span_sparse(const uint64_t *__res
                                                            const uint32_t *__restrict__ blist,
                                                            const uint32_t *__restrict__ cache,
                                                            const BuildState *gstate, uint4 *__restrict__ meta) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	const uint32_t nbuckets = (gstate->status & kStatusAbort) ? 0u : gstate->buckets, lane = lane_id();
 	const uint32_t warps = gridDim.x * (blockDim.x / 32);
 	for (uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) / 32; t < nbuckets; t += warps) {
@@ -900,6 +914,7 @@ template <bool B>
 __global__ void bucket_windows(BuildBatch bb, const uint32_t *__restrict__ blist, const BuildState *gstate,
                                const uint4 *__restrict__ meta, const uint32_t *__restrict__ win_base,
                                uint32_t *__restrict__ wfirst, uint32_t *__restrict__ wlast) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	const uint32_t nbuckets = (gstate->status & kStatusAbort) ? 0u : gstate->buckets; // as in bucket_meta
 	for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nbuckets; t += gridDim.x * blockDim.x) {
 		const uint32_t mi = B ? mesh_search(bb.bucket_base, bb.M, blist[t]) : 0u;
@@ -1007,6 +1022,7 @@ __global__ void __launch_bounds__(kTPB) build_leaf_windows(const uint64_t *__res
                                                            const uint32_t *__restrict__ wfirst,
                                                            const uint32_t *__restrict__ wlast,
                                                            const uint32_t *__restrict__ cache, BuildState *gstate) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	extern __shared__ unsigned long long s_acc[];
 	__shared__ uint32_t s_over, s_leaves, s_skip;
 	const uint32_t M = batch_size<B>(bb);
@@ -1063,6 +1079,7 @@ __global__ void __launch_bounds__(kTPB) build_leaf_windows(const uint64_t *__res
 // Writes svo_build_info followed by the status word of every mesh to `out` (device), one record of
 // sizeof(svo_build_info) + 4 bytes per mesh.
 template <bool B> __global__ void build_export(BuildBatch bb, const BuildState *gstate, uint32_t *out) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	constexpr uint32_t kRec = sizeof(svo_build_info) / 4 + 1;
 	for (uint32_t mi = blockIdx.x * blockDim.x + threadIdx.x; mi < batch_size<B>(bb); mi += gridDim.x * blockDim.x) {
 		const BuildMesh md = mesh_at<B>(bb, mi);
@@ -1224,37 +1241,34 @@ static void launch_dense_and_scatter(const uint64_t *frags, uint64_t n, uint32_t
                                      cudaStream_t stream) {
 	const int sms = device_sm_count();
 	const uint32_t sweep = (uint32_t)sms * (uint32_t)tune_value(kTuneSweepBlocks, tune_level, n);
-	SVO_LAUNCH("build_init", stream, build_init<B><<<M, 256, 0, stream>>>(bb, gstate););
+	SVO_LAUNCH("build_init", stream, ::svo::launch_k(build_init<B>, M, 256, 0, stream, bb, gstate););
 	SVO_LAUNCH("dense_mark", stream,
-	           dense_mark<B><<<grid_for(n, kTPB * kSweepRuns, sweep), kTPB, 0, stream>>>(frags, n, bb, bcount););
+	           ::svo::launch_k(dense_mark<B>, grid_for(n, kTPB * kSweepRuns, sweep), kTPB, 0, stream, frags, n, bb, bcount););
 	// Two independent chains after the sweep: the bucket scan (then, once the dense prefix is final, the
 	// interior words) on a second stream, the dense reduce / scan on the caller's stream; the bucketed
 	// copy needs the bucket offsets and the dense prefix, and the caller's later work waits for both.
 	SideFork fork(stream, tune_value(kTuneBuildStreams, tune_level, n) == 2);
 	cudaStream_t aux = fork.side();
 	SVO_LAUNCH("bucket_scan", aux,
-	           bucket_scan<<<(nb_total + kScanTile - 1) / kScanTile, kTPB, 0, aux>>>(bcount, nb_total, boff, blist,
-	                                                                                gstate, bdescs););
+	           ::svo::launch_k(bucket_scan, (nb_total + kScanTile - 1) / kScanTile, kTPB, 0, aux, bcount, nb_total, boff, blist, gstate, bdescs););
 	fork.mark_side(0);
 	if (maxD >= 1) {
 		if (maxD >= 2 && bb.reduce_total)
 			SVO_LAUNCH("dense_reduce", stream,
-			           dense_reduce<B><<<std::min<uint32_t>(bb.reduce_total, (uint32_t)sms * 8), 256, 0, stream>>>(bb););
+			           ::svo::launch_k(dense_reduce<B>, std::min<uint32_t>(bb.reduce_total, (uint32_t)sms * 8), 256, 0, stream, bb););
 		SVO_LAUNCH("dense_scan", stream,
-		           dense_scan<B><<<grid_for(dense_words, kDenseTile, (uint32_t)sms * 4), kTPB, 0, stream>>>(
-		               bb, dense_words, gstate, descs););
-		SVO_LAUNCH("dense_finish", stream, dense_finish<B><<<(M + 127) / 128, 128, 0, stream>>>(bb););
+		           ::svo::launch_k(dense_scan<B>, grid_for(dense_words, kDenseTile, (uint32_t)sms * 4), kTPB, 0, stream, bb, dense_words, gstate, descs););
+		SVO_LAUNCH("dense_finish", stream, ::svo::launch_k(dense_finish<B>, (M + 127) / 128, 128, 0, stream, bb););
 		fork.side_waits_main();
 		SVO_LAUNCH("dense_write", aux,
-		           dense_write<B><<<grid_for(items_total, kTPB, (uint32_t)sms * 16), kTPB, 0, aux>>>(bb, items_total););
+		           ::svo::launch_k(dense_write<B>, grid_for(items_total, kTPB, (uint32_t)sms * 16), kTPB, 0, aux, bb, items_total););
 	}
 	fork.mark_side(1);
 	fork.main_waits(0); // bucket offsets
 	// the bucketed copy: leaf items when the leaf parents are dense (their bitmap is final now), fragments
 	// for the sparse levels otherwise
 	SVO_LAUNCH("bucket_scatter", stream,
-	           bucket_scatter<B><<<grid_for(n, kTPB * kScatterRuns, sweep), kTPB, 0, stream>>>(frags, n, bb, boff, bfill,
-	                                                                                      sorted););
+	           ::svo::launch_k(bucket_scatter<B>, grid_for(n, kTPB * kScatterRuns, sweep), kTPB, 0, stream, frags, n, bb, boff, bfill, sorted););
 	fork.main_waits(1); // interior words
 }
 
@@ -1266,14 +1280,12 @@ static void launch_sparse(const uint64_t *sorted, uint32_t count, uint32_t level
 	    grid_for(((uint64_t)count + 3) / 4, kTPB, (uint32_t)sms * (uint32_t)tune_value(kTuneSweepBlocks, level, count));
 	// the first sparse depth's words start at zero (later depths' blocks are zeroed by the alloc before)
 	SVO_LAUNCH("zero_level", stream,
-	           zero_level<<<(uint32_t)sms * 8, kTPB, 0, stream>>>(pool, capacity, state, dv.D + 1, gstate););
+	           ::svo::launch_k(zero_level, (uint32_t)sms * 8, kTPB, 0, stream, pool, capacity, state, dv.D + 1, gstate););
 	for (uint32_t depth = dv.D + 1; depth < level; ++depth) {
 		SVO_LAUNCH("build_tag", stream,
-		           build_tag<<<tag_blocks, kTPB, 0, stream>>>(sorted, count, level, depth, pool, cache, dv, state,
-		                                                      gstate););
+		           ::svo::launch_k(build_tag, tag_blocks, kTPB, 0, stream, sorted, count, level, depth, pool, cache, dv, state, gstate););
 		SVO_LAUNCH("build_alloc", stream,
-		           build_alloc<<<(uint32_t)sms * 4, kTPB, 0, stream>>>(pool, capacity, depth, level, state, descs,
-		                                                                     gstate););
+		           ::svo::launch_k(build_alloc, (uint32_t)sms * 4, kTPB, 0, stream, pool, capacity, depth, level, state, descs, gstate););
 	}
 }
 
@@ -1286,20 +1298,16 @@ static void launch_leaf_stage(const BuildBatch &bb, uint32_t M, uint32_t tune_le
 	const size_t smem = kLeafSlots * sizeof(unsigned long long); // 32 KB: below the default dynamic limit
 	const uint32_t meta_items = std::max<uint32_t>(nb_total, M);
 	const uint32_t blocks = (uint32_t)sms * (uint32_t)tune_value(kTuneLeafBlocks, tune_level, n);
-	SVO_LAUNCH("leaf_window_scan", stream, leaf_window_scan<B><<<1, kTPB, 0, stream>>>(bb, win_base););
+	SVO_LAUNCH("leaf_window_scan", stream, ::svo::launch_k(leaf_window_scan<B>, 1, kTPB, 0, stream, bb, win_base););
 	SVO_LAUNCH("bucket_meta", stream,
-	           bucket_meta<B><<<grid_for(meta_items, kTPB, (uint32_t)sms * 4), kTPB, 0, stream>>>(bb, boff, blist,
-	                                                                                          gstate, bmeta););
+	           ::svo::launch_k(bucket_meta<B>, grid_for(meta_items, kTPB, (uint32_t)sms * 4), kTPB, 0, stream, bb, boff, blist, gstate, bmeta););
 	if (any_sparse)
 		SVO_LAUNCH("bucket_span_sparse", stream,
-		           bucket_span_sparse<B><<<grid_for((uint64_t)nb_total * 32, kTPB, (uint32_t)sms * 8), kTPB, 0, stream>>>(
-		               sorted, bb, blist, cache, gstate, bmeta););
+		           ::svo::launch_k(bucket_span_sparse<B>, grid_for((uint64_t)nb_total * 32, kTPB, (uint32_t)sms * 8), kTPB, 0, stream, sorted, bb, blist, cache, gstate, bmeta););
 	SVO_LAUNCH("bucket_windows", stream,
-	           bucket_windows<B><<<grid_for(nb_total, kTPB, (uint32_t)sms * 4), kTPB, 0, stream>>>(
-	               bb, blist, gstate, bmeta, win_base, wfirst, wlast););
+	           ::svo::launch_k(bucket_windows<B>, grid_for(nb_total, kTPB, (uint32_t)sms * 4), kTPB, 0, stream, bb, blist, gstate, bmeta, win_base, wfirst, wlast););
 	SVO_LAUNCH("build_leaf_windows", stream,
-	           build_leaf_windows<B><<<blocks, kTPB, smem, stream>>>(sorted, bb, bmeta, win_base, wfirst, wlast, cache,
-	                                                                 const_cast<BuildState *>(gstate)););
+	           ::svo::launch_k(build_leaf_windows<B>, blocks, kTPB, smem, stream, sorted, bb, bmeta, win_base, wfirst, wlast, cache, const_cast<BuildState *>(gstate)););
 }
 
 cudaError_t build_launch_interior(const uint64_t *frags, uint32_t count, uint32_t level, uint32_t *pool,
@@ -1330,7 +1338,7 @@ cudaError_t build_launch_leaf(uint32_t count, uint32_t level, uint32_t *pool, ui
 cudaError_t build_launch_export(const BuildWorkspace &w, uint32_t level, uint32_t count, void *out,
                                 cudaStream_t stream) {
 	const BuildBatch bb = single_batch(w, count, level, nullptr, 0);
-	SVO_LAUNCH("build_export", stream, build_export<false><<<1, 32, 0, stream>>>(bb, w.state, (uint32_t *)out););
+	SVO_LAUNCH("build_export", stream, ::svo::launch_k(build_export<false>, 1, 32, 0, stream, bb, w.state, (uint32_t *)out););
 	return cudaGetLastError();
 }
 
@@ -1360,7 +1368,7 @@ cudaError_t build_launch_batch(const uint64_t *frags, const BuildBatchPlan &p, v
 	launch_leaf_stage<true>(p.bb, p.M, p.max_level, p.frags_total, p.nb_total, p.boff, p.blist, p.gstate, p.bmeta,
 	                        p.win_base, p.wfirst, p.wlast, p.any_sparse, p.sorted, p.cache, stream);
 	SVO_LAUNCH("build_export", stream,
-	           build_export<true><<<(p.M + 127) / 128, 128, 0, stream>>>(p.bb, p.gstate, (uint32_t *)result_dev););
+	           ::svo::launch_k(build_export<true>, (p.M + 127) / 128, 128, 0, stream, p.bb, p.gstate, (uint32_t *)result_dev););
 	return cudaGetLastError();
 }
 

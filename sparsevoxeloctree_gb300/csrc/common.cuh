@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <utility>
 #include <cuda_runtime.h>
 
 #include "../../include/svo.h"
@@ -17,6 +18,30 @@ constexpr unsigned kFullMask = 0xffffffffu;
 // order by an atomic ticket, so the predecessor is always running or done; the bound only guards
 // against a broken invariant and is never reached in a correct run.
 constexpr uint32_t kSpinLimit = 1u << 22;
+
+// Programmatic dependent launch.  Every engine kernel is launched with programmatic stream
+// serialization, so the launch and set-up of a kernel overlap the last blocks of the kernel before it
+// on the same stream; each kernel's first statement waits (`griddepcontrol.wait`) until that
+// predecessor has completed and its memory operations are visible, which keeps the ordering of a plain
+// stream launch.  No kernel triggers its dependents early, so a dependent's blocks take SM resources
+// only as the predecessor's blocks retire.  Without the launch attribute the wait is a no-op.
+SVO_DEV void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_k(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
+                            Args &&...args) {
+	cudaLaunchAttribute attr[1];
+	attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+	attr[0].val.programmaticStreamSerializationAllowed = 1;
+	cudaLaunchConfig_t cfg = {};
+	cfg.gridDim = grid;
+	cfg.blockDim = block;
+	cfg.dynamicSmemBytes = smem;
+	cfg.stream = stream;
+	cfg.attrs = attr;
+	cfg.numAttrs = 1;
+	return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 // Test hook of the bounded waits (svo_debug_wait_fault): `limit` bounds every wait's iterations, and the
 // look-back tile or beam texel numbered `withheld` never publishes, so the waits on it run out and take

@@ -329,6 +329,7 @@ SVO_DEV uint32_t camera_row_end(const MarchArgs &a) {
 // instantiation, so the usual launch carries no counter and no second copy of the loop.
 template <bool CAMERA, int TPB, int RPL, bool SHARED, bool COUNT>
 __global__ void __launch_bounds__(TPB) march_kernel(MarchArgs a) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	constexpr int kStride = SHARED ? TPB : 1;
 	__shared__ uint32_t s_stack[SHARED ? SVO_LEVEL_MAX * TPB : 1];
 	uint32_t l_stack[SHARED ? 1 : SVO_LEVEL_MAX];
@@ -383,6 +384,7 @@ constexpr uint32_t kRefillMin = 8;
 
 template <bool CAMERA, int TPB, bool SHARED, bool COUNT>
 __global__ void __launch_bounds__(TPB) march_refill_kernel(MarchArgs a) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	constexpr int kStride = SHARED ? TPB : 1;
 	__shared__ uint32_t s_stack[SHARED ? SVO_LEVEL_MAX * TPB : 1];
 	uint32_t l_stack[SHARED ? 1 : SVO_LEVEL_MAX];
@@ -604,6 +606,7 @@ SVO_DEV float beam_texel(const MarchArgs &a, uint32_t i, uint32_t bw, float orig
 }
 
 __global__ void __launch_bounds__(kMarchTPB) beam_kernel(MarchArgs a, float *__restrict__ beam, float orig_sz) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	__shared__ uint32_t s_stack[SVO_LEVEL_MAX * kMarchTPB];
 	uint32_t *stack = s_stack + threadIdx.x;
 	const uint32_t bw = (a.width + kBeamSize - 1) / kBeamSize + 1, bh = (a.height + kBeamSize - 1) / kBeamSize + 1;
@@ -623,6 +626,7 @@ constexpr uint32_t kBeamUnset = 0xffffffffu;
 template <bool COUNT>
 __global__ void __launch_bounds__(kMarchTPB) march_beam_fused_kernel(MarchArgs a, float *__restrict__ beam,
                                                                      float orig_sz) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	__shared__ uint32_t s_stack[SVO_LEVEL_MAX * kMarchTPB];
 	uint32_t *stack = s_stack + threadIdx.x;
 	const uint32_t lane = lane_id();
@@ -695,6 +699,7 @@ __global__ void __launch_bounds__(kMarchTPB) march_beam_fused_kernel(MarchArgs a
 }
 
 __global__ void __launch_bounds__(kMarchTPB) occlude_kernel(MarchArgs a, uint32_t *__restrict__ occluded) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	__shared__ uint32_t s_stack[SVO_LEVEL_MAX * kMarchTPB];
 	uint32_t *stack = s_stack + threadIdx.x;
 	const uint32_t lane = lane_id();
@@ -805,6 +810,7 @@ SVO_DEV svo_ray bounce_one(const svo_hit &h, uint64_t i, uint64_t seed) {
 }
 
 __global__ void bounce_kernel(const svo_hit *__restrict__ hits, uint32_t n, uint64_t seed, svo_ray *__restrict__ rays) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
 		rays[i] = bounce_one(hits[i], i, seed);
 }
@@ -978,6 +984,7 @@ SVO_DEV void queue_append(bool alive, uint32_t p, uint32_t *q, uint32_t *cnt) {
 // Vertex 0: the camera ray of every pixel (main(), shader/path_tracer.comp:115-119) and its first hit.
 template <uint32_t LIGHT>
 __global__ void __launch_bounds__(kMarchTPB) pt_primary_kernel(PtArgs a) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	__shared__ uint32_t s_stack[SVO_LEVEL_MAX * kMarchTPB];
 	uint32_t *stack = s_stack + threadIdx.x;
 	const uint32_t lane = lane_id();
@@ -1031,6 +1038,7 @@ __global__ void __launch_bounds__(kMarchTPB) pt_primary_kernel(PtArgs a) {
 // (shader/path_tracer.comp:41-58, 70-105): light sample with its shadow march, diffuse bounce, leaf march.
 template <uint32_t LIGHT>
 __global__ void __launch_bounds__(kMarchTPB) pt_bounce_refill_kernel(PtArgs a, uint32_t cur) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	__shared__ uint32_t s_stack[SVO_LEVEL_MAX * kMarchTPB];
 	uint32_t *stack = s_stack + threadIdx.x;
 	const uint32_t lane = lane_id(), lt_mask = (1u << lane) - 1u;
@@ -1146,6 +1154,7 @@ __global__ void __launch_bounds__(kMarchTPB) pt_bounce_refill_kernel(PtArgs a, u
 
 // main()'s running means (shader/path_tracer.comp:121-134) of every pixel's sample.
 __global__ void pt_accumulate_kernel(PtArgs a) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	const uint32_t spp = __ldg(a.sobol + 2u * (a.bounce + 1u)); // Sobol_Current((uBounce + 1) << 1)
 	const float fs = (float)spp, fn = (float)(spp + 1u);
 	const size_t npx = (size_t)a.width * a.height;
@@ -1170,6 +1179,7 @@ __global__ void pt_accumulate_kernel(PtArgs a) {
 // Sobol::CmdNext (shader/sobol.comp:70-86): c = index of the lowest zero bit of the sample index, which
 // then increments; every dimension's value takes the XOR of its direction number c.
 __global__ void sobol_next_kernel(uint32_t *sobol, const uint32_t *__restrict__ matrices, uint32_t dim) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	__shared__ uint32_t c;
 	if (threadIdx.x == 0) {
 		const uint32_t i = sobol[dim];
@@ -1200,6 +1210,7 @@ template <bool COUNT>
 __global__ void __launch_bounds__(kMarchTPB) march_jobs_kernel(const MarchJob *__restrict__ jobs, uint32_t njobs,
                                                                 uint64_t total, unsigned long long *ticket,
                                                                 uint32_t *status, unsigned long long *fetches) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	__shared__ uint32_t s_stack[SVO_LEVEL_MAX * kMarchTPB];
 	uint32_t *stack = s_stack + threadIdx.x;
 	const uint32_t lane = lane_id();
@@ -1245,6 +1256,7 @@ __global__ void __launch_bounds__(kMarchTPB) march_jobs_kernel(const MarchJob *_
 }
 
 __global__ void bounce_jobs_kernel(const BounceJob *__restrict__ jobs, uint32_t njobs, uint64_t total) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
 		uint32_t lo = 0, hi = njobs;
 		while (hi - lo > 1) {
@@ -1269,7 +1281,7 @@ static void launch_variant(const MarchArgs &a, cudaStream_t stream) {
 	const uint64_t cap = (uint64_t)sms * (2048 / TPB); // persistent: a full SM's worth of threads
 	const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(blocks_needed, cap));
 	SVO_LAUNCH(CAMERA ? "march_camera" : "march_rays", stream,
-	           march_kernel<CAMERA, TPB, RPL, SHARED, COUNT><<<blocks, TPB, 0, stream>>>(a););
+	           ::svo::launch_k(march_kernel<CAMERA, TPB, RPL, SHARED, COUNT>, blocks, TPB, 0, stream, a););
 }
 
 template <bool CAMERA, int TPB, bool SHARED> static void launch_refill(const MarchArgs &a, cudaStream_t stream) {
@@ -1278,7 +1290,7 @@ template <bool CAMERA, int TPB, bool SHARED> static void launch_refill(const Mar
 	const uint64_t cap = (uint64_t)sms * (2048 / TPB);
 	const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(blocks_needed, cap));
 	SVO_LAUNCH(CAMERA ? "march_camera" : "march_rays", stream,
-	           march_refill_kernel<CAMERA, TPB, SHARED, false><<<blocks, TPB, 0, stream>>>(a););
+	           ::svo::launch_k(march_refill_kernel<CAMERA, TPB, SHARED, false>, blocks, TPB, 0, stream, a););
 }
 
 template <bool CAMERA, int TPB>
@@ -1323,7 +1335,7 @@ cudaError_t bounce_launch(const svo_hit *hits, uint32_t n, uint64_t seed, svo_ra
 	if (n == 0) return cudaSuccess;
 	const int sms = device_sm_count();
 	const uint32_t blocks = (uint32_t)std::min<uint64_t>(((uint64_t)n + 255) / 256, (uint64_t)sms * 8);
-	SVO_LAUNCH("bounce_kernel", stream, bounce_kernel<<<blocks, 256, 0, stream>>>(hits, n, seed, rays););
+	SVO_LAUNCH("bounce_kernel", stream, ::svo::launch_k(bounce_kernel, blocks, 256, 0, stream, hits, n, seed, rays););
 	return cudaGetLastError();
 }
 
@@ -1347,10 +1359,10 @@ cudaError_t march_jobs_launch(const MarchJob *jobs, uint32_t njobs, uint64_t tot
 	const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(blocks_needed, (uint64_t)sms * 16));
 	if (fetches)
 		SVO_LAUNCH("march_jobs", stream,
-		           march_jobs_kernel<true><<<blocks, kMarchTPB, 0, stream>>>(jobs, njobs, total, ticket, status, fetches););
+		           ::svo::launch_k(march_jobs_kernel<true>, blocks, kMarchTPB, 0, stream, jobs, njobs, total, ticket, status, fetches););
 	else
 		SVO_LAUNCH("march_jobs", stream,
-		           march_jobs_kernel<false><<<blocks, kMarchTPB, 0, stream>>>(jobs, njobs, total, ticket, status, nullptr););
+		           ::svo::launch_k(march_jobs_kernel<false>, blocks, kMarchTPB, 0, stream, jobs, njobs, total, ticket, status, nullptr););
 	return cudaGetLastError();
 }
 
@@ -1358,7 +1370,7 @@ cudaError_t bounce_jobs_launch(const BounceJob *jobs, uint32_t njobs, uint64_t t
 	if (total == 0 || njobs == 0) return cudaSuccess;
 	const int sms = device_sm_count();
 	const uint32_t blocks = (uint32_t)std::min<uint64_t>((total + 255) / 256, (uint64_t)sms * 8);
-	SVO_LAUNCH("bounce_jobs", stream, bounce_jobs_kernel<<<blocks, 256, 0, stream>>>(jobs, njobs, total););
+	SVO_LAUNCH("bounce_jobs", stream, ::svo::launch_k(bounce_jobs_kernel, blocks, 256, 0, stream, jobs, njobs, total););
 	return cudaGetLastError();
 }
 
@@ -1372,7 +1384,7 @@ cudaError_t beam_launch(const MarchArgs &a, float *beam, cudaStream_t stream) {
 	const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((texels + kMarchTPB - 1) / kMarchTPB,
 	                                                                            (uint64_t)sms * 16));
 	const float orig_sz = ldexpf(1.0f, 1 - (int)a.level); // exp2f(1 - level), src/OctreeTracer.cpp:205
-	SVO_LAUNCH("beam_prepass", stream, beam_kernel<<<blocks, kMarchTPB, 0, stream>>>(a, beam, orig_sz););
+	SVO_LAUNCH("beam_prepass", stream, ::svo::launch_k(beam_kernel, blocks, kMarchTPB, 0, stream, a, beam, orig_sz););
 	return cudaGetLastError();
 }
 
@@ -1389,9 +1401,9 @@ cudaError_t march_beam_fused_launch(const MarchArgs &a, float *beam, cudaStream_
 	const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(blocks_needed, (uint64_t)sms * 16));
 	const float orig_sz = ldexpf(1.0f, 1 - (int)a.level);
 	if (a.fetches)
-		SVO_LAUNCH("march_beam", stream, march_beam_fused_kernel<true><<<blocks, kMarchTPB, 0, stream>>>(a, beam, orig_sz););
+		SVO_LAUNCH("march_beam", stream, ::svo::launch_k(march_beam_fused_kernel<true>, blocks, kMarchTPB, 0, stream, a, beam, orig_sz););
 	else
-		SVO_LAUNCH("march_beam", stream, march_beam_fused_kernel<false><<<blocks, kMarchTPB, 0, stream>>>(a, beam, orig_sz););
+		SVO_LAUNCH("march_beam", stream, ::svo::launch_k(march_beam_fused_kernel<false>, blocks, kMarchTPB, 0, stream, a, beam, orig_sz););
 	return cudaGetLastError();
 }
 
@@ -1401,7 +1413,7 @@ cudaError_t occlude_launch(const MarchArgs &a, uint32_t *occluded, cudaStream_t 
 	const int sms = device_sm_count();
 	const uint64_t blocks_needed = ((uint64_t)a.n / 32 + kMarchTPB / 32) / (kMarchTPB / 32);
 	const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(blocks_needed, (uint64_t)sms * 16));
-	SVO_LAUNCH("occlude", stream, occlude_kernel<<<blocks, kMarchTPB, 0, stream>>>(a, occluded););
+	SVO_LAUNCH("occlude", stream, ::svo::launch_k(occlude_kernel, blocks, kMarchTPB, 0, stream, a, occluded););
 	return cudaGetLastError();
 }
 
@@ -1414,22 +1426,22 @@ cudaError_t pt_render_launch(const PtArgs &a, cudaStream_t stream) {
 	const uint64_t blocks_needed = (slots / 32 + kMarchTPB / 32 - 1) / (kMarchTPB / 32);
 	const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(blocks_needed, (uint64_t)sms * 16));
 	if (a.light_type == 1) {
-		SVO_LAUNCH("pt_primary", stream, pt_primary_kernel<1><<<blocks, kMarchTPB, 0, stream>>>(a););
+		SVO_LAUNCH("pt_primary", stream, ::svo::launch_k(pt_primary_kernel<1>, blocks, kMarchTPB, 0, stream, a););
 		for (uint32_t cur = 1; cur < a.bounce; ++cur)
-			SVO_LAUNCH("pt_bounce", stream, pt_bounce_refill_kernel<1><<<blocks, kMarchTPB, 0, stream>>>(a, cur););
+			SVO_LAUNCH("pt_bounce", stream, ::svo::launch_k(pt_bounce_refill_kernel<1>, blocks, kMarchTPB, 0, stream, a, cur););
 	} else {
-		SVO_LAUNCH("pt_primary", stream, pt_primary_kernel<0><<<blocks, kMarchTPB, 0, stream>>>(a););
+		SVO_LAUNCH("pt_primary", stream, ::svo::launch_k(pt_primary_kernel<0>, blocks, kMarchTPB, 0, stream, a););
 		for (uint32_t cur = 1; cur < a.bounce; ++cur)
-			SVO_LAUNCH("pt_bounce", stream, pt_bounce_refill_kernel<0><<<blocks, kMarchTPB, 0, stream>>>(a, cur););
+			SVO_LAUNCH("pt_bounce", stream, ::svo::launch_k(pt_bounce_refill_kernel<0>, blocks, kMarchTPB, 0, stream, a, cur););
 	}
 	const uint64_t npx = (uint64_t)a.width * a.height;
 	const uint32_t ablocks = (uint32_t)std::min<uint64_t>((npx + 255) / 256, (uint64_t)sms * 8);
-	SVO_LAUNCH("pt_accumulate", stream, pt_accumulate_kernel<<<ablocks, 256, 0, stream>>>(a););
+	SVO_LAUNCH("pt_accumulate", stream, ::svo::launch_k(pt_accumulate_kernel, ablocks, 256, 0, stream, a););
 	return cudaGetLastError();
 }
 
 cudaError_t sobol_next_launch(uint32_t *sobol, const uint32_t *matrices, uint32_t dim, cudaStream_t stream) {
-	SVO_LAUNCH("sobol_next", stream, sobol_next_kernel<<<1, 64, 0, stream>>>(sobol, matrices, dim););
+	SVO_LAUNCH("sobol_next", stream, ::svo::launch_k(sobol_next_kernel, 1, 64, 0, stream, sobol, matrices, dim););
 	return cudaGetLastError();
 }
 

@@ -236,6 +236,7 @@ __global__ void __launch_bounds__(kTexTPB) vox_texture_compact(const uint64_t *_
                                                              const float4 *texels, uint32_t ntex, uint64_t *out,
                                                              unsigned long long *out_count, uint32_t *tile_ticket,
                                                              unsigned long long *descs, uint32_t *status) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	__shared__ uint32_t s_tile;
 	__shared__ uint32_t s_warp[kTexTPB / 32 + 1];
 	__shared__ unsigned long long s_prefix;
@@ -293,8 +294,7 @@ cudaError_t vox_texture_launch(const uint64_t *cand, uint64_t n_cand, const svo_
 	if (e != cudaSuccess || n_cand == 0) return e;
 	uint32_t *ticket = reinterpret_cast<uint32_t *>(scratch + 1);
 	SVO_LAUNCH("vox_texture", stream,
-	           vox_texture_compact<<<(uint32_t)ntiles, kTexTPB, 0, stream>>>(
-	               cand, n_cand, tris, uvs, n_tris, level, w, set ? set->desc_dev : nullptr,
+	           ::svo::launch_k(vox_texture_compact, (uint32_t)ntiles, kTexTPB, 0, stream, cand, n_cand, tris, uvs, n_tris, level, w, set ? set->desc_dev : nullptr,
 	               set ? set->texels_dev : nullptr, set ? set->count : 0u, out, scratch, ticket, scratch + 2,
 	               ticket + 1););
 	return cudaGetLastError();

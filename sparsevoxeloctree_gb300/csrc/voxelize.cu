@@ -292,6 +292,7 @@ constexpr int kUnitTile = kTPB * kUnitIPT;
 //   unit_off[t]  = units of large triangles before t;    unit_off[n]  = unit total
 template <bool B, int IPT>
 __global__ void __launch_bounds__(kTPB) vox_classify_scan(VoxBatch vb, uint32_t n, VoxWorkspace w) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	constexpr int TILE = kTPB * IPT;
 	__shared__ uint32_t s_tile;
 	__shared__ uint32_t s_cnt[TILE];
@@ -371,6 +372,7 @@ __global__ void __launch_bounds__(kTPB) vox_classify_scan(VoxBatch vb, uint32_t 
 // region); unit_frag[units] = large total.  Persistent grid: tiles claimed in order by ticket.
 template <bool B>
 __global__ void __launch_bounds__(kTPB) vox_unit_scan(VoxBatch vb, uint32_t n, VoxWorkspace w) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	__shared__ uint32_t s_tile;
 	__shared__ unsigned long long s_warp[kTPB / 32 + 1];
 	__shared__ unsigned long long s_prefix;
@@ -450,6 +452,7 @@ struct SmallRec {
 template <bool B>
 __global__ void __launch_bounds__(kEmitTPB) vox_emit(VoxBatch vb, uint32_t n, VoxWorkspace w, uint64_t *__restrict__ frags,
                                                      uint64_t capacity) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	__shared__ SmallRec s_rec[kEmitTPB];
 	__shared__ uint8_t s_cum[kEmitTPB][kSmallArea + 1];
 	__shared__ int16_t s_lo[kEmitTPB][kSmallArea];
@@ -565,6 +568,7 @@ SVO_DEV uint32_t field_of(int axis, int which) { return (uint32_t)((axis + which
 template <bool B>
 __global__ void __launch_bounds__(kTPB, 4) vox_emit_units(VoxBatch vb, uint32_t n, VoxWorkspace w,
                                                        uint64_t *__restrict__ frags, uint64_t capacity) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	__shared__ UnitRec s_rec[kTPB];
 	__shared__ uint32_t s_incl[kTPB];
 	const uint32_t units = w.unit_off[n];
@@ -724,11 +728,11 @@ static cudaError_t clear_count_state(uint32_t n, const VoxWorkspace &w, cudaStre
 template <bool B> static void launch_count(const VoxBatch &vb, uint32_t n, const VoxWorkspace &w, cudaStream_t stream) {
 	if (n >= kBigCountTris)
 		SVO_LAUNCH("vox_classify_scan", stream,
-		           vox_classify_scan<B, 2 * kIPT><<<(n + 2 * kTile - 1) / (2 * kTile), kTPB, 0, stream>>>(vb, n, w););
+		           ::svo::launch_k(vox_classify_scan<B, 2 * kIPT>, (n + 2 * kTile - 1) / (2 * kTile), kTPB, 0, stream, vb, n, w););
 	else
-		SVO_LAUNCH("vox_classify_scan", stream, vox_classify_scan<B, kIPT><<<(n + kTile - 1) / kTile, kTPB, 0, stream>>>(vb, n, w););
+		SVO_LAUNCH("vox_classify_scan", stream, ::svo::launch_k(vox_classify_scan<B, kIPT>, (n + kTile - 1) / kTile, kTPB, 0, stream, vb, n, w););
 	const int sms = device_sm_count();
-	SVO_LAUNCH("vox_unit_scan", stream, vox_unit_scan<B><<<(uint32_t)sms * 4, kTPB, 0, stream>>>(vb, n, w););
+	SVO_LAUNCH("vox_unit_scan", stream, ::svo::launch_k(vox_unit_scan<B>, (uint32_t)sms * 4, kTPB, 0, stream, vb, n, w););
 }
 
 template <bool B>
@@ -737,9 +741,9 @@ static void launch_emit(const VoxBatch &vb, uint32_t n, uint32_t tune_level, con
 	const int sms = device_sm_count();
 	const uint32_t per_sm = (uint32_t)tune_value(kTuneEmitBlocks, tune_level, n);
 	SVO_LAUNCH("vox_emit", stream,
-	           vox_emit<B><<<(uint32_t)sms * per_sm * (kTPB / kEmitTPB), kEmitTPB, 0, stream>>>(vb, n, w, frags, capacity););
+	           ::svo::launch_k(vox_emit<B>, (uint32_t)sms * per_sm * (kTPB / kEmitTPB), kEmitTPB, 0, stream, vb, n, w, frags, capacity););
 	SVO_LAUNCH("vox_emit_units", stream,
-	           vox_emit_units<B><<<(uint32_t)sms * std::max(1u, per_sm / 2), kTPB, 0, stream>>>(vb, n, w, frags, capacity););
+	           ::svo::launch_k(vox_emit_units<B>, (uint32_t)sms * std::max(1u, per_sm / 2), kTPB, 0, stream, vb, n, w, frags, capacity););
 }
 
 cudaError_t vox_set_wait_fault(uint32_t limit, uint32_t withheld) { return set_wait_fault_here(limit, withheld); }
@@ -760,6 +764,7 @@ cudaError_t vox_launch_emit(const svo_triangle *tris, uint32_t n, uint32_t level
 }
 
 __global__ void vox_totals(VoxWorkspace w) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	const uint32_t units = w.unit_off[w.n];
 	const uint32_t status = w.counters[kCtrStatus];
 	w.totals[0] = w.small_off[w.n] + ((status & kStatusUnits) ? 0ull : w.unit_frag[units]);
@@ -768,7 +773,7 @@ __global__ void vox_totals(VoxWorkspace w) {
 }
 
 cudaError_t vox_launch_totals(const VoxWorkspace &w, cudaStream_t stream) {
-	SVO_LAUNCH("vox_totals", stream, vox_totals<<<1, 1, 0, stream>>>(w););
+	SVO_LAUNCH("vox_totals", stream, ::svo::launch_k(vox_totals, 1, 1, 0, stream, w););
 	return cudaGetLastError();
 }
 
@@ -791,6 +796,7 @@ cudaError_t vox_launch_emit_batch(const VoxBatch &vb, uint32_t n, const VoxWorks
 // fragments of earlier meshes sit before its small ones), large shift = small_off[T1] (every small
 // fragment up to the end of the mesh sits before its large ones).  Thread 0 also writes the totals.
 __global__ void vox_batch_totals(VoxBatch vb, VoxWorkspace w) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	const uint32_t status = w.counters[kCtrStatus];
 	const bool units_ok = !(status & kStatusUnits);
 	for (uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < vb.M; m += gridDim.x * blockDim.x) {
@@ -815,7 +821,7 @@ __global__ void vox_batch_totals(VoxBatch vb, VoxWorkspace w) {
 
 cudaError_t vox_launch_batch_totals(const VoxBatch &vb, uint32_t n, const VoxWorkspace &w, cudaStream_t stream) {
 	(void)n;
-	SVO_LAUNCH("vox_totals", stream, vox_batch_totals<<<(vb.M + 127) / 128, 128, 0, stream>>>(vb, w););
+	SVO_LAUNCH("vox_totals", stream, ::svo::launch_k(vox_batch_totals, (vb.M + 127) / 128, 128, 0, stream, vb, w););
 	return cudaGetLastError();
 }
 
