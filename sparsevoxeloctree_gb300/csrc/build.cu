@@ -114,6 +114,14 @@ template <typename T> SVO_DEV uint32_t mesh_search(const T *__restrict__ a, uint
 	return lo;
 }
 
+// The mesh of fragment f in a sweep pass whose fragments start at `first` (f >= first), given m0, the mesh
+// of `first` (searched once per pass: a pass covers a few runs of 32 consecutive fragments, which rarely
+// cross a mesh boundary).  a = frag_base, so a[M] is the batch total and the step ends there.
+SVO_DEV uint32_t mesh_from(const unsigned long long *__restrict__ a, uint32_t m0, unsigned long long f) {
+	while (__ldg(a + m0 + 1) <= f) ++m0;
+	return m0;
+}
+
 template <bool B> SVO_DEV BuildMesh mesh_at(const BuildBatch &bb, uint32_t m) {
 	if constexpr (B)
 		return bb.table[m];
@@ -193,6 +201,7 @@ __global__ void __launch_bounds__(kTPB) dense_mark(const uint64_t *__restrict__ 
 	const uint64_t runs = (n + 31ull) >> 5;
 	const uint32_t lane = lane_id();
 	for (uint64_t r = sweep_first_run<kSweepRuns>(); r < runs; r += sweep_run_stride<kSweepRuns>()) {
+		const uint32_t m0 = B ? mesh_search(bb.frag_base, bb.M, (unsigned long long)(r << 5)) : 0u;
 		uint64_t fr[kSweepRuns];
 #pragma unroll
 		for (uint32_t k = 0; k < kSweepRuns; ++k) {
@@ -204,7 +213,7 @@ __global__ void __launch_bounds__(kTPB) dense_mark(const uint64_t *__restrict__ 
 			const uint64_t f = ((r + k) << 5) + lane;
 			uint32_t word = 0xffffffffu, bit = 0, key = 0xffffffffu;
 			if (f < n) {
-				const uint32_t mi = B ? mesh_search(bb.frag_base, bb.M, (unsigned long long)f) : 0u;
+				const uint32_t mi = B ? mesh_from(bb.frag_base, m0, f) : 0u;
 				const BuildMesh md = mesh_at<B>(bb, mi);
 				uint32_t x, y, z;
 				frag_xyz(fr[k], x, y, z);
@@ -697,6 +706,7 @@ __global__ void __launch_bounds__(kTPB) bucket_scatter(const uint64_t *__restric
 	const uint64_t runs = (n + 31ull) >> 5;
 	const uint32_t lane = lane_id();
 	for (uint64_t r = sweep_first_run<kScatterRuns>(); r < runs; r += sweep_run_stride<kScatterRuns>()) {
+		const uint32_t m0 = B ? mesh_search(bb.frag_base, bb.M, (unsigned long long)(r << 5)) : 0u;
 		uint64_t out[kScatterRuns], send[kScatterRuns];
 		uint32_t key[kScatterRuns], pad[kScatterRuns], first[kScatterRuns], base[kScatterRuns];
 #pragma unroll
@@ -709,7 +719,7 @@ __global__ void __launch_bounds__(kTPB) bucket_scatter(const uint64_t *__restric
 			const uint64_t f = ((r + k) << 5) + lane;
 			key[k] = 0xffffffffu, pad[k] = 0, send[k] = 0;
 			if (f < n) {
-				const uint32_t mi = B ? mesh_search(bb.frag_base, bb.M, (unsigned long long)f) : 0u;
+				const uint32_t mi = B ? mesh_from(bb.frag_base, m0, f) : 0u;
 				const BuildMesh md = mesh_at<B>(bb, mi);
 				const uint32_t level = md.level;
 				const bool items = level == 1 || level - 1 <= md.dv.D;

@@ -503,11 +503,9 @@ __global__ void __launch_bounds__(kEmitTPB) vox_emit(VoxBatch vb, uint32_t n, Vo
 				s_cum[threadIdx.x][k] = (uint8_t)acc;
 				acc += len;
 			}
-			s_cum[threadIdx.x][rows] = (uint8_t)acc;
+			s_cum[threadIdx.x][rows] = (uint8_t)acc; // > every fragment index q < cnt: the span search stops
 			if (acc != cnt) cnt = 0; // cannot happen: the count pass walked the same spans
 			s_rec[threadIdx.x].cnt = cnt;
-			// spans past the last one read as "no more fragments"
-			for (uint32_t k = rows + 1; k <= (uint32_t)kSmallArea; ++k) s_cum[threadIdx.x][k] = 0xffu;
 		}
 		__syncwarp();
 		const uint32_t incl = warp_inclusive_sum(cnt);
