@@ -658,6 +658,7 @@ __global__ void __launch_bounds__(kTPB) bucket_scan(const uint32_t *__restrict__
 	__syncthreads();
 	const uint32_t tile = s_tile;
 	const uint32_t ntiles = (nb + kScanTile - 1) / kScanTile;
+	if (tile >= ntiles) return; // one tile per block: only an uncleared ticket goes past the grid
 	const uint32_t b0 = tile * kScanTile + threadIdx.x * kScanIPT;
 	uint32_t c[kScanIPT], local = 0, nonempty = 0;
 #pragma unroll

@@ -244,6 +244,7 @@ __global__ void __launch_bounds__(kTexTPB) vox_texture_compact(const uint64_t *_
 	__syncthreads();
 	const uint32_t tile = s_tile;
 	const uint64_t ntiles = (n_cand + kTexTile - 1) / kTexTile;
+	if (tile >= ntiles) return; // one tile per block: only an uncleared ticket goes past the grid
 	const uint64_t base = (uint64_t)tile * kTexTile + threadIdx.x;
 	uint64_t frag[kTexIPT];
 	uint32_t keep = 0, count = 0;

@@ -305,6 +305,8 @@ __global__ void __launch_bounds__(kTPB) vox_classify_scan(VoxBatch vb, uint32_t 
 	if (threadIdx.x == 0) s_tile = atomicAdd(&w.counters[kCtrTicketA], 1u);
 	__syncthreads();
 	const uint32_t tile = s_tile;
+	// one tile per block: only an uncleared ticket goes past the grid, and such a tile touches nothing
+	if ((uint64_t)tile * TILE >= (uint64_t)n) return;
 	const uint64_t base = (uint64_t)tile * TILE;
 #pragma unroll 1
 	for (int k = 0; k < IPT; ++k) {
