@@ -1,6 +1,7 @@
 // common.cuh — device helpers shared by the voxelize, build and march kernels (sm_103a).
 #pragma once
 
+#include <atomic>
 #include <cstdint>
 #include <utility>
 #include <cuda_runtime.h>
@@ -41,6 +42,25 @@ inline cudaError_t launch_k(void (*kernel)(KArgs...), dim3 grid, dim3 block, siz
 	cfg.attrs = attr;
 	cfg.numAttrs = 1;
 	return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
+// Grid of a persistent kernel: the blocks of `kernel` that are resident on the current device at once
+// (its occupancy at `threads` threads and `smem` bytes of dynamic shared memory, measured once per device).
+template <typename... KArgs>
+inline uint32_t resident_grid(void (*kernel)(KArgs...), int threads, size_t smem = 0) {
+	constexpr int kDevices = 16;
+	static std::atomic<int> per_sm[kDevices];
+	int dev = 0;
+	if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kDevices) dev = 0;
+	int b = per_sm[dev].load(std::memory_order_relaxed);
+	if (b == 0) {
+		if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, threads, smem) != cudaSuccess || b < 1) {
+			cudaGetLastError();
+			b = 1;
+		}
+		per_sm[dev].store(b, std::memory_order_relaxed);
+	}
+	return (uint32_t)(b * device_sm_count());
 }
 
 // Test hook of the bounded waits (svo_debug_wait_fault): `limit` bounds every wait's iterations, and the
@@ -141,17 +161,18 @@ SVO_DEV unsigned long long desc_load(const unsigned long long *d) {
 // and the returned prefix is a partial sum of published aggregates, never above the true prefix, so
 // offsets derived from it stay inside the buffers their totals size.  A tile with seg_start set begins a
 // new segment (a segmented scan): its prefix is 0, and the look-back of later tiles stops there.
+// published = true: the tile's aggregate was published earlier by tile_publish_aggregate.
 SVO_DEV unsigned long long tile_lookback_warp(unsigned long long *descs, uint32_t t, uint32_t epoch,
                                               unsigned long long aggregate, uint32_t *status,
-                                              bool seg_start = false) {
+                                              bool seg_start = false, bool published = false) {
 	const uint32_t lane = lane_id();
 	const WaitFault wf = c_wait_fault;
 	const bool publish = t != wf.withheld;
 	if (t == 0 || seg_start) {
-		if (lane == 0 && publish) desc_publish(&descs[t], epoch, 2, aggregate);
+		if (lane == 0 && publish && !published) desc_publish(&descs[t], epoch, 2, aggregate);
 		return 0;
 	}
-	if (lane == 0 && publish) desc_publish(&descs[t], epoch, 1, aggregate);
+	if (lane == 0 && publish && !published) desc_publish(&descs[t], epoch, 1, aggregate);
 	unsigned long long prefix = 0;
 	int64_t end = (int64_t)t - 1; // window: descriptors end, end-1, ..., end-31 (lane k reads end-k)
 	uint32_t spins = 0;
@@ -180,6 +201,14 @@ SVO_DEV unsigned long long tile_lookback_warp(unsigned long long *descs, uint32_
 	}
 	if (lane == 0 && publish) desc_publish(&descs[t], epoch, 2, prefix + aggregate);
 	return prefix;
+}
+
+// The first half of a deferred look-back (one thread): tile t publishes its aggregate (tile 0 or a
+// segment start: its inclusive prefix) as soon as it is known, and looks back later
+// (tile_lookback_warp(..., published = true)) after other work, when its predecessors have published.
+SVO_DEV void tile_publish_aggregate(unsigned long long *descs, uint32_t t, uint32_t epoch,
+                                    unsigned long long aggregate, bool seg_start = false) {
+	if (t != c_wait_fault.withheld) desc_publish(&descs[t], epoch, (t == 0 || seg_start) ? 2u : 1u, aggregate);
 }
 
 // ------------------------------------------------------------------------------- integer helpers

@@ -290,6 +290,9 @@ constexpr int kUnitTile = kTPB * kUnitIPT;
 // Per triangle: small fragment count and large unit count, both exclusive-scanned.
 //   small_off[t] = fragments of small triangles before t; small_off[n] = small total
 //   unit_off[t]  = units of large triangles before t;    unit_off[n]  = unit total
+// Persistent grid, tiles claimed in order by ticket, the two scans pipelined as in vox_unit_scan: a
+// tile's aggregates are published once its counts are known, its look-backs and output follow after the
+// block has counted its next tile.
 template <bool B, int IPT>
 __global__ void __launch_bounds__(kTPB) vox_classify_scan(VoxBatch vb, uint32_t n, VoxWorkspace w) {
 	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
@@ -302,76 +305,103 @@ __global__ void __launch_bounds__(kTPB) vox_classify_scan(VoxBatch vb, uint32_t 
 	__shared__ SpanSetup s_sp[kTPB];
 	__shared__ uint32_t s_rows[kTPB];
 	const uint32_t wb = threadIdx.x & ~31u;
-	if (threadIdx.x == 0) s_tile = atomicAdd(&w.counters[kCtrTicketA], 1u);
-	__syncthreads();
-	const uint32_t tile = s_tile;
-	// one tile per block: only an uncleared ticket goes past the grid, and such a tile touches nothing
-	if ((uint64_t)tile * TILE >= (uint64_t)n) return;
-	const uint64_t base = (uint64_t)tile * TILE;
+	const uint32_t ntiles = (uint32_t)(((uint64_t)n + TILE - 1) / TILE);
+	// the pending tile: its aggregates published, its offsets not yet written
+	uint32_t p_tile = 0xffffffffu, p_cnt[IPT], p_units[IPT];
+	unsigned long long p_ec = 0, p_eu = 0, p_tc = 0, p_tu = 0;
+	for (;;) {
+		if (threadIdx.x == 0) s_tile = atomicAdd(&w.counters[kCtrTicketA], 1u);
+		__syncthreads();
+		const uint32_t tile = s_tile;
+		__syncthreads();
+		uint32_t cnt[IPT], unt[IPT];
+		unsigned long long ec = 0, eu = 0, tc = 0, tu = 0;
+		if (tile < ntiles) {
+			const uint64_t base = (uint64_t)tile * TILE;
 #pragma unroll 1
-	for (int k = 0; k < IPT; ++k) {
-		const uint64_t t = base + (uint64_t)k * kTPB + threadIdx.x;
-		TriSetup s;
-		s.valid = 0;
-		if (t < n) {
-			const svo_triangle *tp;
-			uint32_t local, lvl, mi;
-			tri_of<B>(vb, (uint32_t)t, tp, local, lvl, mi);
-			tri_setup(tp, local, lvl, s);
-		}
-		const bool large = is_large(s);
-		// small triangles: fragments = the covered lengths of their spans, counted by the whole warp
-		const uint32_t rows = (s.valid && !large) ? (uint32_t)(s.v1 - s.v0 + 1) : 0u;
-		if (rows) span_setup(s, s_sp[threadIdx.x]);
-		const uint32_t rincl = warp_inclusive_sum(rows);
-		s_rows[threadIdx.x] = rincl;
-		s_cnt[k * kTPB + threadIdx.x] = 0u;
-		s_units[k * kTPB + threadIdx.x] = large ? unit_count(s) : 0u;
-		__syncwarp();
-		uint32_t *cnt = s_cnt + k * kTPB + wb;
-		warp_rows(s_rows + wb, s_sp + wb, __shfl_sync(kFullMask, rincl, 31),
-		          [&](uint32_t j, uint32_t, int32_t lo, int32_t hi) {
-			          if (hi >= lo) atomicAdd(cnt + j, (uint32_t)(hi - lo + 1));
-		          });
-		__syncwarp();
-	}
-	__syncthreads();
-	unsigned long long lc = 0, lu = 0;
+			for (int k = 0; k < IPT; ++k) {
+				const uint64_t t = base + (uint64_t)k * kTPB + threadIdx.x;
+				TriSetup s;
+				s.valid = 0;
+				if (t < n) {
+					const svo_triangle *tp;
+					uint32_t local, lvl, mi;
+					tri_of<B>(vb, (uint32_t)t, tp, local, lvl, mi);
+					tri_setup(tp, local, lvl, s);
+				}
+				const bool large = is_large(s);
+				// small triangles: fragments = the covered lengths of their spans, counted by the whole warp
+				const uint32_t rows = (s.valid && !large) ? (uint32_t)(s.v1 - s.v0 + 1) : 0u;
+				if (rows) span_setup(s, s_sp[threadIdx.x]);
+				const uint32_t rincl = warp_inclusive_sum(rows);
+				s_rows[threadIdx.x] = rincl;
+				s_cnt[k * kTPB + threadIdx.x] = 0u;
+				s_units[k * kTPB + threadIdx.x] = large ? unit_count(s) : 0u;
+				__syncwarp();
+				uint32_t *c = s_cnt + k * kTPB + wb;
+				warp_rows(s_rows + wb, s_sp + wb, __shfl_sync(kFullMask, rincl, 31),
+				          [&](uint32_t j, uint32_t, int32_t lo, int32_t hi) {
+					          if (hi >= lo) atomicAdd(c + j, (uint32_t)(hi - lo + 1));
+				          });
+				__syncwarp();
+			}
+			__syncthreads();
+			unsigned long long lc = 0, lu = 0;
 #pragma unroll
-	for (int k = 0; k < IPT; ++k) {
-		lc += s_cnt[threadIdx.x * IPT + k];
-		lu += s_units[threadIdx.x * IPT + k];
-	}
-	unsigned long long tc, tu;
-	const unsigned long long ec = block_exclusive_sum<unsigned long long, kTPB>(lc, s_warp, tc);
-	const unsigned long long eu = block_exclusive_sum<unsigned long long, kTPB>(lu, s_warp, tu);
-	if (threadIdx.x < 32) {
-		const unsigned long long pc = tile_lookback_warp(w.descs, tile, 1u, tc, &w.counters[kCtrStatus]);
-		const unsigned long long pu = tile_lookback_warp(w.descs2, tile, 1u, tu, &w.counters[kCtrStatus]);
-		if (threadIdx.x == 0) s_prefix[0] = pc, s_prefix[1] = pu;
-	}
-	__syncthreads();
-	unsigned long long rc = s_prefix[0] + ec, ru = s_prefix[1] + eu;
-#pragma unroll
-	for (int k = 0; k < IPT; ++k) {
-		const uint64_t t = base + (uint64_t)threadIdx.x * IPT + k;
-		if (t < n) {
-			w.small_off[t] = rc;
-			w.unit_off[t] = (uint32_t)ru;
+			for (int k = 0; k < IPT; ++k) {
+				cnt[k] = s_cnt[threadIdx.x * IPT + k];
+				unt[k] = s_units[threadIdx.x * IPT + k];
+				lc += cnt[k];
+				lu += unt[k];
+			}
+			ec = block_exclusive_sum<unsigned long long, kTPB>(lc, s_warp, tc);
+			eu = block_exclusive_sum<unsigned long long, kTPB>(lu, s_warp, tu);
+			if (threadIdx.x == 0) {
+				tile_publish_aggregate(w.descs, tile, 1u, tc);
+				tile_publish_aggregate(w.descs2, tile, 1u, tu);
+			}
 		}
-		rc += s_cnt[threadIdx.x * IPT + k];
-		ru += s_units[threadIdx.x * IPT + k];
-	}
-	if (base + TILE >= n && base <= n && threadIdx.x == 0) {
-		w.small_off[n] = s_prefix[0] + tc;
-		const unsigned long long units = s_prefix[1] + tu;
-		w.unit_off[n] = units > 0xffffffffull ? 0xffffffffu : (uint32_t)units;
-		if (units > w.unit_cap) atomicOr(&w.counters[kCtrStatus], kStatusUnits);
+		if (p_tile != 0xffffffffu) { // the previous tile: look back (its predecessors are done), write
+			if (threadIdx.x < 32) {
+				const unsigned long long pc =
+				    tile_lookback_warp(w.descs, p_tile, 1u, p_tc, &w.counters[kCtrStatus], false, true);
+				const unsigned long long pu =
+				    tile_lookback_warp(w.descs2, p_tile, 1u, p_tu, &w.counters[kCtrStatus], false, true);
+				if (threadIdx.x == 0) s_prefix[0] = pc, s_prefix[1] = pu;
+			}
+			__syncthreads();
+			const uint64_t base = (uint64_t)p_tile * TILE;
+			unsigned long long rc = s_prefix[0] + p_ec, ru = s_prefix[1] + p_eu;
+#pragma unroll
+			for (int k = 0; k < IPT; ++k) {
+				const uint64_t t = base + (uint64_t)threadIdx.x * IPT + k;
+				if (t < n) {
+					w.small_off[t] = rc;
+					w.unit_off[t] = (uint32_t)ru;
+				}
+				rc += p_cnt[k];
+				ru += p_units[k];
+			}
+			if (p_tile == ntiles - 1 && threadIdx.x == 0) {
+				w.small_off[n] = s_prefix[0] + p_tc;
+				const unsigned long long units = s_prefix[1] + p_tu;
+				w.unit_off[n] = units > 0xffffffffull ? 0xffffffffu : (uint32_t)units;
+				if (units > w.unit_cap) atomicOr(&w.counters[kCtrStatus], kStatusUnits);
+			}
+			__syncthreads();
+		}
+		if (tile >= ntiles) break;
+		p_tile = tile, p_ec = ec, p_eu = eu, p_tc = tc, p_tu = tu;
+#pragma unroll
+		for (int k = 0; k < IPT; ++k) p_cnt[k] = cnt[k], p_units[k] = unt[k];
 	}
 }
 
 // Per unit of a large triangle: covered length, scanned into unit_frag[u] (offset inside the large
-// region); unit_frag[units] = large total.  Persistent grid: tiles claimed in order by ticket.
+// region); unit_frag[units] = large total.  Persistent grid: tiles claimed in order by ticket.  The scan
+// is pipelined over a block's tiles: a tile publishes its aggregate as soon as its lengths are known,
+// and its look-back and output come one tile later, after the block has measured its next tile, so a
+// block does not idle at a barrier while its predecessors finish theirs.
 template <bool B>
 __global__ void __launch_bounds__(kTPB) vox_unit_scan(VoxBatch vb, uint32_t n, VoxWorkspace w) {
 	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
@@ -381,56 +411,67 @@ __global__ void __launch_bounds__(kTPB) vox_unit_scan(VoxBatch vb, uint32_t n, V
 	const uint32_t units = w.unit_off[n];
 	if (units > w.unit_cap) return; // the host re-runs with a workspace sized for `units`
 	const uint32_t ntiles = (units + kUnitTile - 1) / kUnitTile;
+	uint32_t p_tile = 0xffffffffu, p_len[kUnitIPT]; // the pending tile: aggregate published, output not
+	unsigned long long p_excl = 0, p_total = 0;
 	for (;;) {
 		if (threadIdx.x == 0) s_tile = atomicAdd(&w.counters[kCtrTicketB], 1u);
 		__syncthreads();
 		const uint32_t tile = s_tile;
 		__syncthreads();
-		if (tile >= ntiles) break;
 		uint32_t len[kUnitIPT];
-		unsigned long long local = 0;
-		// the warp's kUnitIPT * 32 consecutive units lie in triangles [t_first, t_last]
-		const uint32_t u_first = tile * kUnitTile + (threadIdx.x & ~31u) * kUnitIPT;
-		uint32_t t_first = 0, t_end = 0;
-		if (u_first < units) {
-			const uint32_t u_last = min(u_first + 32 * kUnitIPT - 1, units - 1);
-			t_first = warp_upper_index(w.unit_off, 0, n, u_first);
-			t_end = warp_upper_index(w.unit_off, t_first, n, u_last) + 1;
-		}
-#pragma unroll
-		for (int k = 0; k < kUnitIPT; ++k) {
-			const uint32_t u = tile * kUnitTile + threadIdx.x * kUnitIPT + k;
-			len[k] = 0;
-			if (u < units) {
-				const uint32_t t = upper_index_in(w.unit_off, t_first, t_end, u);
-				w.unit_tri[u] = t;
-				TriSetup s;
-				const svo_triangle *tp;
-				uint32_t local, lvl, mi;
-				tri_of<B>(vb, t, tp, local, lvl, mi);
-				tri_setup(tp, local, lvl, s);
-				int32_t v, lo, hi;
-				unit_interval(s, u - w.unit_off[t], v, lo, hi);
-				len[k] = hi >= lo ? (uint32_t)(hi - lo + 1) : 0u;
+		unsigned long long excl = 0, total = 0;
+		if (tile < ntiles) {
+			unsigned long long local = 0;
+			// the warp's kUnitIPT * 32 consecutive units lie in triangles [t_first, t_last]
+			const uint32_t u_first = tile * kUnitTile + (threadIdx.x & ~31u) * kUnitIPT;
+			uint32_t t_first = 0, t_end = 0;
+			if (u_first < units) {
+				const uint32_t u_last = min(u_first + 32 * kUnitIPT - 1, units - 1);
+				t_first = warp_upper_index(w.unit_off, 0, n, u_first);
+				t_end = warp_upper_index(w.unit_off, t_first, n, u_last) + 1;
 			}
-			local += len[k];
-		}
-		unsigned long long total;
-		const unsigned long long excl = block_exclusive_sum<unsigned long long, kTPB>(local, s_warp, total);
-		if (threadIdx.x < 32) {
-			const unsigned long long p = tile_lookback_warp(w.descs3, tile, 1u, total, &w.counters[kCtrStatus]);
-			if (threadIdx.x == 0) s_prefix = p;
-		}
-		__syncthreads();
-		unsigned long long run = s_prefix + excl;
 #pragma unroll
-		for (int k = 0; k < kUnitIPT; ++k) {
-			const uint32_t u = tile * kUnitTile + threadIdx.x * kUnitIPT + k;
-			if (u < units) w.unit_frag[u] = run;
-			run += len[k];
+			for (int k = 0; k < kUnitIPT; ++k) {
+				const uint32_t u = tile * kUnitTile + threadIdx.x * kUnitIPT + k;
+				len[k] = 0;
+				if (u < units) {
+					const uint32_t t = upper_index_in(w.unit_off, t_first, t_end, u);
+					w.unit_tri[u] = t;
+					TriSetup s;
+					const svo_triangle *tp;
+					uint32_t local_t, lvl, mi;
+					tri_of<B>(vb, t, tp, local_t, lvl, mi);
+					tri_setup(tp, local_t, lvl, s);
+					int32_t v, lo, hi;
+					unit_interval(s, u - w.unit_off[t], v, lo, hi);
+					len[k] = hi >= lo ? (uint32_t)(hi - lo + 1) : 0u;
+				}
+				local += len[k];
+			}
+			excl = block_exclusive_sum<unsigned long long, kTPB>(local, s_warp, total);
+			if (threadIdx.x == 0) tile_publish_aggregate(w.descs3, tile, 1u, total);
 		}
-		if (tile == ntiles - 1 && threadIdx.x == 0) w.unit_frag[units] = s_prefix + total;
-		__syncthreads();
+		if (p_tile != 0xffffffffu) { // the previous tile: look back (its predecessors are done), write
+			if (threadIdx.x < 32) {
+				const unsigned long long p =
+				    tile_lookback_warp(w.descs3, p_tile, 1u, p_total, &w.counters[kCtrStatus], false, true);
+				if (threadIdx.x == 0) s_prefix = p;
+			}
+			__syncthreads();
+			unsigned long long run = s_prefix + p_excl;
+#pragma unroll
+			for (int k = 0; k < kUnitIPT; ++k) {
+				const uint32_t u = p_tile * kUnitTile + threadIdx.x * kUnitIPT + k;
+				if (u < units) w.unit_frag[u] = run;
+				run += p_len[k];
+			}
+			if (p_tile == ntiles - 1 && threadIdx.x == 0) w.unit_frag[units] = s_prefix + p_total;
+			__syncthreads();
+		}
+		if (tile >= ntiles) break;
+		p_tile = tile, p_excl = excl, p_total = total;
+#pragma unroll
+		for (int k = 0; k < kUnitIPT; ++k) p_len[k] = len[k];
 	}
 	if (ntiles == 0 && blockIdx.x == 0 && threadIdx.x == 0) w.unit_frag[0] = 0;
 }
@@ -726,12 +767,17 @@ static cudaError_t clear_count_state(uint32_t n, const VoxWorkspace &w, cudaStre
 }
 
 template <bool B> static void launch_count(const VoxBatch &vb, uint32_t n, const VoxWorkspace &w, cudaStream_t stream) {
+	const int sms = device_sm_count();
 	if (n >= kBigCountTris)
 		SVO_LAUNCH("vox_classify_scan", stream,
-		           ::svo::launch_k(vox_classify_scan<B, 2 * kIPT>, (n + 2 * kTile - 1) / (2 * kTile), kTPB, 0, stream, vb, n, w););
+		           ::svo::launch_k(vox_classify_scan<B, 2 * kIPT>,
+		                           std::min((n + 2 * kTile - 1) / (2 * kTile), resident_grid(vox_classify_scan<B, 2 * kIPT>, kTPB)),
+		                           kTPB, 0, stream, vb, n, w););
 	else
-		SVO_LAUNCH("vox_classify_scan", stream, ::svo::launch_k(vox_classify_scan<B, kIPT>, (n + kTile - 1) / kTile, kTPB, 0, stream, vb, n, w););
-	const int sms = device_sm_count();
+		SVO_LAUNCH("vox_classify_scan", stream,
+		           ::svo::launch_k(vox_classify_scan<B, kIPT>,
+		                           std::min((n + kTile - 1) / kTile, resident_grid(vox_classify_scan<B, kIPT>, kTPB)), kTPB, 0,
+		                           stream, vb, n, w););
 	SVO_LAUNCH("vox_unit_scan", stream, ::svo::launch_k(vox_unit_scan<B>, (uint32_t)sms * 4, kTPB, 0, stream, vb, n, w););
 }
 
