@@ -350,44 +350,59 @@ __global__ void __launch_bounds__(kTPB) dense_scan(BuildBatch bb, uint32_t total
 	const uint32_t *bits = bb.dense_bits;
 	uint32_t *prefix = bb.dense_prefix;
 	const uint32_t ntiles = total_words / kDenseTile; // regions are whole tiles
+	// the pending tile (pipelined as the voxelize scans: aggregate published, look-back and prefixes one
+	// tile later); its word popcounts (at most 32 each) kept four to a register
+	uint32_t p_tile = 0xffffffffu, p_run = 0, p_total = 0, p_c[kDenseIPT / 4];
 	for (;;) {
 		if (threadIdx.x == 0) s_tile = atomicAdd(&gstate->tiles[0], 1u);
 		__syncthreads();
 		const uint32_t tile = s_tile;
 		__syncthreads();
+		uint32_t c[kDenseIPT / 4], run = 0, total = 0;
+		if (tile < ntiles) {
+			const uint32_t first = tile * kDenseTile;
+			bool seg_start = tile == 0;
+			if constexpr (B) seg_start = __ldg(bb.dense_base + mesh_search(bb.dense_base, bb.M, first)) == first;
+			const uint4 *src = reinterpret_cast<const uint4 *>(bits + first + threadIdx.x * kDenseIPT);
+			uint32_t local = 0;
+#pragma unroll
+			for (int k = 0; k < kDenseIPT / 4; ++k) {
+				const uint4 v = __ldcs(src + k);
+				const uint32_t a = __popc(v.x), b = __popc(v.y), d = __popc(v.z), e = __popc(v.w);
+				c[k] = a | (b << 8) | (d << 16) | (e << 24);
+				local += a + b + d + e;
+			}
+			run = block_exclusive_sum<uint32_t, kTPB>(local, s_warp, total);
+			if (threadIdx.x == 0) tile_publish_aggregate(descs, tile, 15u, total, seg_start);
+		}
+		if (p_tile != 0xffffffffu) {
+			if (threadIdx.x < 32) {
+				bool seg_start = p_tile == 0;
+				if constexpr (B) {
+					const uint32_t first = p_tile * kDenseTile;
+					seg_start = __ldg(bb.dense_base + mesh_search(bb.dense_base, bb.M, first)) == first;
+				}
+				const uint32_t p = (uint32_t)tile_lookback_warp(descs, p_tile, 15u, p_total, &gstate->status, seg_start, true);
+				if (threadIdx.x == 0) s_prefix = p;
+			}
+			__syncthreads();
+			uint32_t r = p_run + s_prefix;
+			uint4 *dst = reinterpret_cast<uint4 *>(prefix + p_tile * kDenseTile + threadIdx.x * kDenseIPT);
+#pragma unroll
+			for (int k = 0; k < kDenseIPT / 4; ++k) {
+				uint4 o;
+				o.x = r, r += p_c[k] & 0xffu;
+				o.y = r, r += (p_c[k] >> 8) & 0xffu;
+				o.z = r, r += (p_c[k] >> 16) & 0xffu;
+				o.w = r, r += p_c[k] >> 24;
+				dst[k] = o;
+			}
+			__syncthreads();
+		}
 		if (tile >= ntiles) break;
-		const uint32_t first = tile * kDenseTile;
-		bool seg_start = tile == 0;
-		if constexpr (B) seg_start = __ldg(bb.dense_base + mesh_search(bb.dense_base, bb.M, first)) == first;
-		const uint32_t w0 = first + threadIdx.x * kDenseIPT;
-		const uint4 *src = reinterpret_cast<const uint4 *>(bits + w0);
-		uint32_t c[kDenseIPT], local = 0;
+		p_tile = tile, p_run = run, p_total = total;
 #pragma unroll
-		for (int k = 0; k < kDenseIPT / 4; ++k) {
-			const uint4 v = __ldcs(src + k);
-			c[4 * k] = __popc(v.x), c[4 * k + 1] = __popc(v.y), c[4 * k + 2] = __popc(v.z), c[4 * k + 3] = __popc(v.w);
-		}
-#pragma unroll
-		for (int k = 0; k < kDenseIPT; ++k) local += c[k];
-		uint32_t total;
-		uint32_t run = block_exclusive_sum<uint32_t, kTPB>(local, s_warp, total);
-		if (threadIdx.x < 32) {
-			const uint32_t p = (uint32_t)tile_lookback_warp(descs, tile, 15u, total, &gstate->status, seg_start);
-			if (threadIdx.x == 0) s_prefix = p;
-		}
-		__syncthreads();
-		run += s_prefix;
-		uint4 *dst = reinterpret_cast<uint4 *>(prefix + w0);
-#pragma unroll
-		for (int k = 0; k < kDenseIPT / 4; ++k) {
-			uint4 o;
-			o.x = run, run += c[4 * k];
-			o.y = run, run += c[4 * k + 1];
-			o.z = run, run += c[4 * k + 2];
-			o.w = run, run += c[4 * k + 3];
-			dst[k] = o;
-		}
-		__syncthreads();
+		for (int k = 0; k < kDenseIPT / 4; ++k) p_c[k] = c[k];
 	}
 }
 
@@ -559,69 +574,82 @@ __global__ void __launch_bounds__(kTPB) build_alloc(uint32_t *__restrict__ pool,
 		}
 		return;
 	}
+	// pipelined as the voxelize scans: a tile's count is published at once, its look-back and its
+	// pointers follow after the block has counted its next tile.  The words of a sparse depth are 0 or
+	// the tag 0x80000000 until they are allocated, so a tile is kept as a mask of its tagged words.
+	uint32_t p_tile = 0xffffffffu, p_mask = 0, p_rank0 = 0, p_total = 0;
 	for (;;) {
 		if (threadIdx.x == 0) s_tile = atomicAdd(&state->tiles[depth], 1u);
 		__syncthreads();
 		const uint32_t tile = s_tile;
 		__syncthreads();
+		uint32_t mask = 0, rank0 = 0, total = 0;
+		if (tile < ntiles) {
+			const uint32_t w0 = tile * kAllocTile + threadIdx.x * kAllocIPT; // offset inside the level
+			if (w0 + kAllocIPT <= li.num) {
+				const uint4 *src = reinterpret_cast<const uint4 *>(pool + li.begin + w0);
+#pragma unroll
+				for (int k = 0; k < kAllocIPT / 4; ++k) {
+					const uint4 x = src[k];
+					mask |= ((x.x >> 31) << (4 * k)) | ((x.y >> 31) << (4 * k + 1)) | ((x.z >> 31) << (4 * k + 2)) |
+					        ((x.w >> 31) << (4 * k + 3));
+				}
+			} else {
+#pragma unroll
+				for (int k = 0; k < kAllocIPT; ++k)
+					if (w0 + k < li.num) mask |= (pool[li.begin + w0 + k] >> 31) << k;
+			}
+			rank0 = block_exclusive_sum<uint32_t, kTPB>((uint32_t)__popc(mask), s_warp, total);
+			if (threadIdx.x == 0) tile_publish_aggregate(descs, tile, depth, total);
+		}
+		if (p_tile != 0xffffffffu) {
+			if (threadIdx.x < 32) {
+				// a timeout goes to the batch-wide status, which every later stage of every mesh checks
+				const uint32_t p =
+				    (uint32_t)tile_lookback_warp(descs, p_tile, depth, p_total, &gstate->status, false, true);
+				if (threadIdx.x == 0) s_prefix = p;
+			}
+			__syncthreads();
+			const uint32_t prefix = s_prefix;
+			const uint32_t w0 = p_tile * kAllocTile + threadIdx.x * kAllocIPT;
+			uint32_t w[kAllocIPT], rank = p_rank0;
+#pragma unroll
+			for (int k = 0; k < kAllocIPT; ++k) {
+				w[k] = 0u;
+				if (!((p_mask >> k) & 1u)) continue;
+				const uint64_t b = (uint64_t)li.blocks_before + prefix + rank++; // 0-based child block number
+				const uint64_t ptr = (b + 1) * 8;
+				if (ptr + 8 > capacity || ptr + 8 > SVO_MAX_POOL_WORDS) {
+					atomicOr(&state->status, kStatusCapacity);
+					w[k] = 0x80000000u; // leave unallocated; the build reports SVO_ERR_CAPACITY
+					continue;
+				}
+				w[k] = (uint32_t)ptr | 0x80000000u;
+				if (!next_is_leaf) { // the next depth's init; leaf blocks are written whole by the leaf stage
+					uint4 *child = reinterpret_cast<uint4 *>(pool + ptr);
+					child[0] = make_uint4(0, 0, 0, 0);
+					child[1] = make_uint4(0, 0, 0, 0);
+				}
+			}
+			if (w0 + kAllocIPT <= li.num) {
+				uint4 *dst = reinterpret_cast<uint4 *>(pool + li.begin + w0);
+#pragma unroll
+				for (int k = 0; k < kAllocIPT / 4; ++k)
+					dst[k] = make_uint4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
+			} else {
+#pragma unroll
+				for (int k = 0; k < kAllocIPT; ++k)
+					if (w0 + k < li.num) pool[li.begin + w0 + k] = w[k];
+			}
+			if (p_tile == ntiles - 1 && threadIdx.x == 0) {
+				const uint32_t nodes = prefix + p_total;
+				state->lv[depth].nodes = nodes;
+				state->lv[depth + 1] = LevelInfo{next_begin, nodes * 8u, li.blocks_before + nodes, 0u};
+			}
+			__syncthreads();
+		}
 		if (tile >= ntiles) break;
-		const uint32_t w0 = tile * kAllocTile + threadIdx.x * kAllocIPT; // offset inside the level
-		uint32_t w[kAllocIPT];
-		if (w0 + kAllocIPT <= li.num) {
-			const uint4 *src = reinterpret_cast<const uint4 *>(pool + li.begin + w0);
-#pragma unroll
-			for (int k = 0; k < kAllocIPT / 4; ++k) {
-				const uint4 x = src[k];
-				w[4 * k] = x.x, w[4 * k + 1] = x.y, w[4 * k + 2] = x.z, w[4 * k + 3] = x.w;
-			}
-		} else {
-#pragma unroll
-			for (int k = 0; k < kAllocIPT; ++k) w[k] = w0 + k < li.num ? pool[li.begin + w0 + k] : 0u;
-		}
-		uint32_t cnt = 0;
-#pragma unroll
-		for (int k = 0; k < kAllocIPT; ++k) cnt += (w[k] >> 31);
-		uint32_t total;
-		const uint32_t rank0 = block_exclusive_sum<uint32_t, kTPB>(cnt, s_warp, total);
-		if (threadIdx.x < 32) {
-			// a timeout goes to the batch-wide status, which every later stage of every mesh checks
-			const uint32_t p = (uint32_t)tile_lookback_warp(descs, tile, depth, total, &gstate->status);
-			if (threadIdx.x == 0) s_prefix = p;
-		}
-		__syncthreads();
-		const uint32_t prefix = s_prefix;
-		uint32_t rank = rank0;
-#pragma unroll
-		for (int k = 0; k < kAllocIPT; ++k) {
-			if (!(w[k] >> 31)) continue;
-			const uint64_t b = (uint64_t)li.blocks_before + prefix + rank++; // 0-based child block number
-			const uint64_t ptr = (b + 1) * 8;
-			if (ptr + 8 > capacity || ptr + 8 > SVO_MAX_POOL_WORDS) {
-				atomicOr(&state->status, kStatusCapacity);
-				w[k] = 0x80000000u; // leave unallocated; the build reports SVO_ERR_CAPACITY
-				continue;
-			}
-			w[k] = (uint32_t)ptr | 0x80000000u;
-			if (!next_is_leaf) { // the next depth's init; leaf blocks are written whole by the leaf stage
-				uint4 *child = reinterpret_cast<uint4 *>(pool + ptr);
-				child[0] = make_uint4(0, 0, 0, 0);
-				child[1] = make_uint4(0, 0, 0, 0);
-			}
-		}
-		if (w0 + kAllocIPT <= li.num) {
-			uint4 *dst = reinterpret_cast<uint4 *>(pool + li.begin + w0);
-#pragma unroll
-			for (int k = 0; k < kAllocIPT / 4; ++k) dst[k] = make_uint4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
-		} else {
-#pragma unroll
-			for (int k = 0; k < kAllocIPT; ++k)
-				if (w0 + k < li.num) pool[li.begin + w0 + k] = w[k];
-		}
-		if (tile == ntiles - 1 && threadIdx.x == 0) {
-			const uint32_t nodes = prefix + total;
-			state->lv[depth].nodes = nodes;
-			state->lv[depth + 1] = LevelInfo{next_begin, nodes * 8u, li.blocks_before + nodes, 0u};
-		}
+		p_tile = tile, p_mask = mask, p_rank0 = rank0, p_total = total;
 	}
 }
 
