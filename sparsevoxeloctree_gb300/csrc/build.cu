@@ -11,12 +11,13 @@
 //     occupied depth-d cells whose Morton code is below m (breadth-first order = Morton order per depth);
 //   * that word sits at 8 * (1 + grank(d-1, m >> 3)) + (m & 7), i.e. in its parent's child block.
 // GB300 design, in four stages:
-//   dense   depths 1..D (D = min(L-1, 9); 8^9 bits = 16 MB stays in L2): one sweep over the fragments sets
+//   dense   depths 1..D (D = min(L-1, 9), or 10 for L >= 11 from 2^24 fragments; 8^9 bits = 16 MB stays in
+//           L2, 8^10 bits = 128 MB about fills it): one sweep over the fragments sets
 //           the occupancy bits of depth D (run-merged atomicOr), coarser depths are OR-reductions of
 //           8-bit groups, one single-pass look-back scan of popcounts over all depths gives every grank,
 //           and one pass writes all interior words of depths 1..D;
 //   buckets the same sweep counts fragments per bucket (16^3 voxels while the leaf parents are dense,
-//           L <= 10; 32^3 voxels deeper); a look-back scan and one scatter copy the fragments into bucket
+//           L - 1 <= D; 32^3 voxels otherwise); a look-back scan and one scatter copy the fragments into bucket
 //           order (8 B each: a leaf item, slot << 32 | rgb, when the leaf parents are dense, else the
 //           fragment), which every later sweep reads;
 //   sparse  depths D+1..L-1 (only when L > 10): the reference's tag / prefix-sum alloc per level with a
@@ -24,7 +25,7 @@
 //   leaf    one block per leaf window (4096 consecutive words of the leaf range) at a time: the window's
 //           items come from the run of buckets whose leaf spans meet it (each item is read at most
 //           twice), the block accumulates their colours in shared memory (r, g, b, n in 16-bit fields,
-//           one shared atomic per item) and writes every leaf word of the window,
+//           two 32-bit shared atomics per item) and writes every leaf word of the window,
 //           0xC0000000 | min(n,63)<<24 | floor(sum/n) (the channel-wise integer mean), with no
 //           accumulator array in device memory.  The packing is exact up to 257 fragments per voxel; a
 //           window where a voxel exceeds that is redone with exact 64-bit sums in the same block.
