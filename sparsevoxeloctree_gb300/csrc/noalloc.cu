@@ -115,7 +115,7 @@ extern "C" int svo_voxelize_static(const svo_triangle *tris, uint32_t n_tris, ui
 	// vox_launch_count clears the scan descriptors and counters the previous call left behind
 	e = vox_launch_count(tris, n_tris, level, w, s);
 	if (e == cudaSuccess) e = vox_launch_totals(w, s);
-	if (e == cudaSuccess) e = vox_launch_emit(tris, n_tris, level, w, frags, capacity, s);
+	if (e == cudaSuccess) e = vox_launch_emit(tris, n_tris, level, w, frags, capacity, s, false);
 	if (e == cudaSuccess) e = cudaMemcpyAsync(count_dev, w.totals, sizeof(uint64_t), cudaMemcpyDeviceToDevice, s);
 	if (e == cudaSuccess)
 		e = cudaMemcpyAsync(count_dev + 1, w.totals + 2, sizeof(uint64_t), cudaMemcpyDeviceToDevice, s);

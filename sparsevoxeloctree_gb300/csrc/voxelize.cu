@@ -783,13 +783,19 @@ template <bool B> static void launch_count(const VoxBatch &vb, uint32_t n, const
 
 template <bool B>
 static void launch_emit(const VoxBatch &vb, uint32_t n, uint32_t tune_level, const VoxWorkspace &w, uint64_t *frags,
-                        uint64_t capacity, cudaStream_t stream) {
+                        uint64_t capacity, cudaStream_t stream, bool two_streams = true) {
 	const int sms = device_sm_count();
 	const uint32_t per_sm = (uint32_t)tune_value(kTuneEmitBlocks, tune_level, n);
-	SVO_LAUNCH("vox_emit", stream,
-	           ::svo::launch_k(vox_emit<B>, (uint32_t)sms * per_sm * (kTPB / kEmitTPB), kEmitTPB, 0, stream, vb, n, w, frags, capacity););
+	// the small triangles' and the units' fragments go to disjoint ranges: the two emissions run on two
+	// streams, so each fills the SMs the other's tail leaves idle
+	SideFork fork(stream, two_streams);
+	cudaStream_t side = fork.side();
+	SVO_LAUNCH("vox_emit", side,
+	           ::svo::launch_k(vox_emit<B>, (uint32_t)sms * per_sm * (kTPB / kEmitTPB), kEmitTPB, 0, side, vb, n, w, frags, capacity););
+	fork.mark_side(0);
 	SVO_LAUNCH("vox_emit_units", stream,
 	           ::svo::launch_k(vox_emit_units<B>, (uint32_t)sms * std::max(1u, per_sm / 2), kTPB, 0, stream, vb, n, w, frags, capacity););
+	fork.main_waits(0);
 }
 
 cudaError_t vox_set_wait_fault(uint32_t limit, uint32_t withheld) { return set_wait_fault_here(limit, withheld); }
@@ -803,9 +809,9 @@ cudaError_t vox_launch_count(const svo_triangle *tris, uint32_t n, uint32_t leve
 }
 
 cudaError_t vox_launch_emit(const svo_triangle *tris, uint32_t n, uint32_t level, const VoxWorkspace &w,
-                            uint64_t *frags, uint64_t capacity, cudaStream_t stream) {
+                            uint64_t *frags, uint64_t capacity, cudaStream_t stream, bool two_streams) {
 	if (n == 0) return cudaSuccess;
-	launch_emit<false>(single_vox(tris, level), n, level, w, frags, capacity, stream);
+	launch_emit<false>(single_vox(tris, level), n, level, w, frags, capacity, stream, two_streams);
 	return cudaGetLastError();
 }
 
