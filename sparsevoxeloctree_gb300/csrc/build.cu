@@ -983,7 +983,7 @@ template <typename SlotFn, typename RgbFn>
 SVO_DEV uint32_t leaf_window(const uint64_t *__restrict__ sorted, uint32_t f0, uint32_t f1, uint32_t w0, uint32_t wn,
                              uint32_t *dst, unsigned long long *s_acc, uint32_t *s_over, SlotFn SLOT, RgbFn RGB) {
 	uint32_t *s_acc32 = reinterpret_cast<uint32_t *>(s_acc);
-	for (uint32_t i = threadIdx.x; i < wn; i += kTPB) s_acc[i] = 0ull;
+	// the accumulators are zero here: cleared once per block, then by each window's write-out
 	if (threadIdx.x == 0) *s_over = 0;
 	__syncthreads();
 	bool over = false;
@@ -1011,6 +1011,8 @@ SVO_DEV uint32_t leaf_window(const uint64_t *__restrict__ sorted, uint32_t f0, u
 		for (uint32_t i = 4 * threadIdx.x; i < wn; i += 4 * kTPB) {
 			const uint4 a = *reinterpret_cast<const uint4 *>(s_acc32 + 2 * i);
 			const uint4 c = *reinterpret_cast<const uint4 *>(s_acc32 + 2 * i + 4);
+			*reinterpret_cast<uint4 *>(s_acc32 + 2 * i) = make_uint4(0u, 0u, 0u, 0u); // ready for the next window
+			*reinterpret_cast<uint4 *>(s_acc32 + 2 * i + 4) = make_uint4(0u, 0u, 0u, 0u);
 			const uint32_t rg[4] = {a.x, a.z, c.x, c.z}, bn[4] = {a.y, a.w, c.y, c.w};
 			uint32_t word[4];
 #pragma unroll
@@ -1047,6 +1049,8 @@ SVO_DEV uint32_t leaf_window(const uint64_t *__restrict__ sorted, uint32_t f0, u
 				leaves += word != 0u;
 			}
 		}
+		__syncthreads();
+		for (uint32_t i = threadIdx.x; i < kLeafSlots; i += kTPB) s_acc[i] = 0ull; // the next window starts at zero
 	}
 	__syncthreads(); // the accumulators are reused by the next window
 	return leaves;
@@ -1068,6 +1072,8 @@ __global__ void __launch_bounds__(kTPB) build_leaf_windows(const uint64_t *__res
 	const uint32_t M = batch_size<B>(bb);
 	if (gstate->status & kStatusAbort) return; // no window bookkeeping was made (leaf_window_scan)
 	const uint32_t total = win_base[M], nbuckets = gstate->buckets;
+	for (uint32_t i = threadIdx.x; i < kLeafSlots; i += kTPB) s_acc[i] = 0ull; // leaf_window keeps them zero after
+	__syncthreads();
 	for (uint32_t gw = blockIdx.x; gw < total; gw += gridDim.x) {
 		const uint32_t mi = B ? mesh_search(win_base, M, gw) : 0u;
 		const BuildMesh md = mesh_at<B>(bb, mi);
