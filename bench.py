@@ -634,7 +634,7 @@ def batch_leg(args, device, meshes=None, workload: str | None = None, check_iden
 
 
 # ------------------------------------------------------------------------------------------ serving
-def serve_leg(args, device, rates=(100, 500, 1000, 2000, 5000), seconds=1.0) -> dict:
+def serve_leg(args, device, rates=(100, 200, 500, 1000, 2000, 5000), seconds=1.0) -> dict:
     """The serving workload: 16 resident octrees (levels 9..11, sphere + boxes + clutter meshes of 50k..2M
     triangles), trace requests with a uniform scene and a log-uniform ray count of 1k..2M (half primary
     camera rays, half diffuse-bounce rays), 2% rebuilds, admission under a 40 GB HBM budget.  Poisson
