@@ -399,7 +399,7 @@ def light_result(args, env, scene, F, T, n_rays, ms, stages, roofline, clocks, l
     cpu = parity = None
     if env.leader and env.world == 1 and not args.no_cpu_baseline:
         ref = {}
-        cpu = cpu_baseline(scene, per_step=False, outputs=ref)
+        cpu = cpu_baseline(scene, per_step=False, outputs=ref, repeats=0)  # one pass: seconds at 2^12
         torch.cuda.synchronize()
         parity = parity_vs_oracle(vox.GetVoxelFragmentList(), octree.words(), api.hits_numpy(hits),
                                   api.hits_numpy(bounce_hits) if scene.bounce else None, ref, device)
@@ -833,30 +833,64 @@ def serve_leg(args, device, rates=(100, 200, 500, 1000, 2000, 5000), seconds=1.0
 
 
 # ------------------------------------------------------------------------------------------ CPU arms
-def cpu_baseline(scene, per_step: bool, outputs: dict | None = None) -> dict:
-    """The oracle (CPU restatement of the reference's path) on the host cores, full workload.  With
-    `outputs` (a dict), the pass's fragment list, node pool and hits are stored there for the parity
-    comparison with the engine's outputs of the same workload."""
+def cpu_model() -> str:
+    """The host CPU as /proc/cpuinfo names it (x86: model name; Arm: implementer and part numbers)."""
+    try:
+        with open("/proc/cpuinfo") as f:
+            info = f.read().splitlines()
+    except OSError:
+        return "unknown"
+    fields = {}
+    for line in info:
+        if ":" in line:
+            k, v = (x.strip() for x in line.split(":", 1))
+            fields.setdefault(k, v)
+    if "model name" in fields:
+        return fields["model name"]
+    if "CPU part" in fields:
+        return f"Arm implementer {fields.get('CPU implementer', '?')} part {fields['CPU part']}"
+    return "unknown"
+
+
+def cpu_baseline(scene, per_step: bool, outputs: dict | None = None, repeats: int = 3) -> dict:
+    """The oracle (CPU restatement of the reference's path) on the host cores, full workload: one
+    warm-up pass, then the median of `repeats` timed passes per stage (repeats = 0: the one pass is the
+    measurement).  With `outputs` (a dict), the first pass's fragment list, node pool and hits are stored
+    there for the parity comparison with the engine's outputs of the same workload."""
+    import statistics
+
     import oracle
-    t0 = time.perf_counter()
-    frags = oracle.voxelize(scene.tris, scene.level)
-    t1 = time.perf_counter()
-    pool = oracle.build_octree(frags, scene.level)
-    t2 = time.perf_counter()
-    rays = oracle.camera_rays(scene.camera, scene.width, scene.height)
-    hits = oracle.raycast(pool, scene.level, rays)
-    bounce_hits = None
-    if scene.bounce:
-        bounce_hits = oracle.raycast(pool, scene.level, oracle.bounce_rays(hits, scene.seed))
-    t3 = time.perf_counter()
-    ms = (t3 - t0) * 1e3
+
+    def one_pass():
+        t0 = time.perf_counter()
+        frags = oracle.voxelize(scene.tris, scene.level)
+        t1 = time.perf_counter()
+        pool = oracle.build_octree(frags, scene.level)
+        t2 = time.perf_counter()
+        rays = oracle.camera_rays(scene.camera, scene.width, scene.height)
+        hits = oracle.raycast(pool, scene.level, rays)
+        bounce_hits = None
+        if scene.bounce:
+            bounce_hits = oracle.raycast(pool, scene.level, oracle.bounce_rays(hits, scene.seed))
+        t3 = time.perf_counter()
+        times = {"voxelize": (t1 - t0) * 1e3, "build": (t2 - t1) * 1e3, "march": (t3 - t2) * 1e3,
+                 "total": (t3 - t0) * 1e3}
+        return times, (frags, pool, hits, bounce_hits)
+
+    cold, (frags, pool, hits, bounce_hits) = one_pass()
     if outputs is not None:
         outputs.update(frags=frags, pool=pool, hits=hits, bounce_hits=bounce_hits)
-    return {"value": ms, "unit": "ms", "cores": oracle.threads(), "kind": "port",
-            "sample": f"full {scene.name} workload, one pass ({len(scene.tris)} tris, {len(frags)} fragments, "
-                      f"{scene.n_rays} rays)",
-            "fragments": int(len(frags)),
-            "stages_ms": {"voxelize": (t1 - t0) * 1e3, "build": (t2 - t1) * 1e3, "march": (t3 - t2) * 1e3}}
+    nfrags = int(len(frags))
+    del frags, pool, hits, bounce_hits
+    runs = [one_pass()[0] for _ in range(repeats)] or [cold]
+    med = {k: statistics.median(r[k] for r in runs) for k in ("voxelize", "build", "march", "total")}
+    how = f"one warm-up pass, then the median of {len(runs)} passes" if repeats else "one pass"
+    return {"value": med["total"], "unit": "ms", "cores": oracle.threads(), "kind": "port",
+            "cpu": cpu_model(), "hardware_threads": os.cpu_count(),
+            "sample": f"full {scene.name} workload ({len(scene.tris)} tris, {nfrags} fragments, {scene.n_rays} "
+                      f"rays): {how}",
+            "fragments": nfrags, "cold_ms": cold["total"],
+            "stages_ms": {k: med[k] for k in ("voxelize", "build", "march")}}
 
 
 def parity_vs_oracle(frags_dev, pool_dev, hits_np, bounce_np, ref: dict, device) -> dict:
@@ -900,8 +934,8 @@ def reference_arm(args, rank: int) -> dict | None:
     import oracle
     scene = make_scene(args.workload)
     for _ in range(args.warmup):
-        cpu_baseline(scene, True)
-    runs = [cpu_baseline(scene, True) for _ in range(args.steps)]
+        cpu_baseline(scene, True, repeats=0)
+    runs = [cpu_baseline(scene, True, repeats=0) for _ in range(args.steps)]
     ms = float(statistics.mean(r["value"] for r in runs))
     cpu = dict(runs[-1])
     cpu["value"] = ms
