@@ -586,16 +586,17 @@ SVO_DEV float ratio_f(int64_t num, int64_t den) {
 // [0, D); t = fr0 - k fb approximates (r0 - k NU) / D within 1e-4 (fr0, fb: the two ratios in float),
 // so floor(t) is exact unless t lies within kDepthEps of an integer, where the exact int64 division
 // decides.  The fragment words are base | u and z placed in their packed fields.
-struct UnitRec {
+// The fields a lane reloads when it moves to another unit come first, as four 16-byte groups.
+struct __align__(16) UnitRec {
 	float fr0, fb;
 	int32_t q0, lo;
-	int32_t excl, z0, z1;
-	uint32_t fields; // u shift | z shift << 8 | (u is the split z field) << 16 | (z is) << 17
+	int32_t z0, z1, excl, R;   // R: resolution of the unit's mesh
+	uint32_t ush, zsh;         // bit positions of u and z in the low fragment word
+	uint32_t usplit, zsplit;   // all ones when u (z) is the z field, whose top 4 bits sit in the high word
 	uint32_t base_lo, base_hi;
-	int32_t R;       // resolution of the unit's mesh
-	uint32_t pad;
-	int64_t num0, nu, d;
-	uint64_t shift;  // output position of the unit's mesh's large region
+	uint64_t shift;            // output position of the unit's mesh's large region
+	int64_t num0, nu, d;       // the exact division near integers
+	uint64_t pad;
 };
 constexpr float kDepthEps = 1.0f / 1024.0f;
 
@@ -651,7 +652,8 @@ __global__ void __launch_bounds__(kTPB, 4) vox_emit_units(VoxBatch vb, uint32_t 
 				// coordinate fields: i -> (axis+1)%3, j -> (axis+2)%3, depth -> axis (0 x, 1 y, 2 z)
 				const uint32_t fi = field_of(S.axis, 1), fj = field_of(S.axis, 2), fz = field_of(S.axis, 0);
 				const uint32_t fu = S.cols ? fj : fi, fv = S.cols ? fi : fj;
-				rec.fields = (12u * fu) | ((12u * fz) << 8) | ((fu == 2u) << 16) | ((fz == 2u) << 17);
+				rec.ush = 12u * fu, rec.zsh = 12u * fz;
+				rec.usplit = fu == 2u ? 0xffffffffu : 0u, rec.zsplit = fz == 2u ? 0xffffffffu : 0u;
 				const uint32_t vv = (uint32_t)v;
 				rec.base_lo = vv << (12u * fv);
 				rec.base_hi = (S.rgb & 0xffffffu) | (fv == 2u ? (vv >> 8) << 28 : 0u);
@@ -671,16 +673,16 @@ __global__ void __launch_bounds__(kTPB, 4) vox_emit_units(VoxBatch vb, uint32_t 
 #pragma unroll 2
 		for (uint32_t f = lane; f < total; f += 32) {
 			while (warp_incl[j] <= f) ++j;
-			if (j != have) {
-				const UnitRec &rec = warp_rec[j];
-				k = (int32_t)(f - (uint32_t)rec.excl);
+			if (j != have) { // the record's first 64 bytes in four vector loads
+				const uint4 *rr = reinterpret_cast<const uint4 *>(warp_rec + j);
+				const uint4 g0 = rr[0], g1 = rr[1], g2 = rr[2], g3 = rr[3];
+				fr0 = __uint_as_float(g0.x), fb = __uint_as_float(g0.y), q0 = (int32_t)g0.z, lo = (int32_t)g0.w;
+				z0 = (int32_t)g1.x, z1 = (int32_t)g1.y, R = (int32_t)g1.w;
+				k = (int32_t)(f - g1.z);
 				kf = (float)k;
-				fr0 = rec.fr0, fb = rec.fb, q0 = rec.q0, lo = rec.lo, z0 = rec.z0, z1 = rec.z1;
-				ush = rec.fields & 0xffu, zsh = (rec.fields >> 8) & 0xffu;
-				usplit = 0u - ((rec.fields >> 16) & 1u), zsplit = 0u - ((rec.fields >> 17) & 1u);
-				base_lo = rec.base_lo, base_hi = rec.base_hi;
-				R = rec.R;
-				out0 = rec.shift + first;
+				ush = g2.x, zsh = g2.y, usplit = g2.z, zsplit = g2.w;
+				base_lo = g3.x, base_hi = g3.y;
+				out0 = ((uint64_t)g3.z | ((uint64_t)g3.w << 32)) + first;
 				have = j;
 			} else {
 				k += 32;
