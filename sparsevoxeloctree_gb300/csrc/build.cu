@@ -236,10 +236,18 @@ __global__ void __launch_bounds__(kTPB) dense_mark(const uint64_t *__restrict__ 
 			uint32_t first, last;
 			lane_run(word, lane, first, last);
 			const uint32_t merged = run_or(bit, lane, last);
-			if (word != 0xffffffffu && lane == first) atomicOr(bb.dense_bits + word, merged);
-			// fragments per bucket, for the bucketed copy
-			lane_run(key, lane, first, last);
-			if (key != 0xffffffffu && lane == first) atomicAdd(bcount + key, last - first + 1u);
+			// fragments per bucket, for the bucketed copy: equal bitmap words have equal bucket keys (the key
+			// is a coarser prefix of the same Morton code, and both are numbered over the batch), so a
+			// word's run adds its length to its bucket; keys without a word (no dense depth) run alone
+			if (word != 0xffffffffu && lane == first) {
+				atomicOr(bb.dense_bits + word, merged);
+				if (key != 0xffffffffu) atomicAdd(bcount + key, last - first + 1u);
+			}
+			const bool loose = word == 0xffffffffu && key != 0xffffffffu;
+			if (__any_sync(kFullMask, loose)) {
+				lane_run(loose ? key : 0xffffffffu, lane, first, last);
+				if (loose && lane == first) atomicAdd(bcount + key, last - first + 1u);
+			}
 		}
 	}
 }
