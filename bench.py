@@ -373,6 +373,13 @@ def engine_arm(args, env, device, workload: str | None = None, light: bool = Fal
         stages["path_trace"] = path_trace_stats(api, octree, scene, stream)
 
     e2e = None if args.no_e2e else e2e_arm(args, scene, tris_host, device, env)
+    if e2e is not None:  # the host link bounds the copies of the end-to-end step
+        link = host_link_probe(device)
+        e2e["host_link"] = {**{k: link[k] for k in ("hit_store_gbs", "dma_d2h_gbs", "dma_h2d_gbs")},
+                            "floor_ms": e2e["h2d_bytes_per_step"] / link["dma_h2d_gbs"] / 1e6 +
+                                        e2e["d2h_bytes_per_step"] / link["hit_store_gbs"] / 1e6,
+                            "note": "triangle upload at the DMA rate plus the hits at the march's host-store "
+                                    "rate: the copies alone, before any voxelize or build work"}
     cpu = parity = None
     if env.leader and env.world == 1 and not args.no_cpu_baseline:
         # the timed steps' own outputs (the last step's fragment list, pool and hits), compared with the
@@ -480,6 +487,59 @@ def e2e_arm(args, scene, tris_host, device, env) -> dict:
             "d2h_bytes_per_step": int(hits_host.numel()) + 8 * 3 + 256,
             "path": "svo_voxelize -> svo_build_fraglist -> svo_raycast_camera_download with pinned host buffers",
             "timing": "host wall clock per step (includes the ABI's blocking readbacks)"}
+
+
+_HOST_LINK: dict = {}
+
+
+def host_link_probe(device, width: int = 4096, height: int = 2048) -> dict:
+    """GPU -> host bandwidth of this machine, the ceiling of every leg that delivers hits into host memory:
+    svo_raycast_camera_download on an empty octree (every ray ends at its first node, so the kernel is
+    ray set-up plus the 32 B hit store) into page-locked host memory, and a DMA copy of the same bytes
+    (median of 5 after a warm-up; measured once per process)."""
+    key = device.index if device.index is not None else 0
+    if key in _HOST_LINK:
+        return _HOST_LINK[key]
+    import numpy as np
+    import torch
+
+    from sparsevoxeloctree_gb300 import _lib, api, scenes
+    lib = _lib.load()
+    n = width * height
+    pool = torch.zeros(8, dtype=torch.int32, device=device)  # an empty root block
+    oc = _lib.OctreeC()
+    oc.words, oc.capacity, oc.range_words, oc.level, oc.owned = pool.data_ptr(), 8, 8, 3, 0
+    cam = api.camera_struct(scenes.camera_from_angles((1.5, 1.5, 0.2), 0.0, 0.0, aspect=width / height))
+    hits_dev = torch.empty(n * 32, dtype=torch.uint8, device=device)
+    hits_host = torch.empty(n * 32, dtype=torch.uint8).pin_memory()
+    st = torch.cuda.current_stream()
+    s = ctypes.c_void_p(st.cuda_stream)
+
+    def timed(fn, reps=5):
+        fn()
+        st.synchronize()
+        ts = []
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(st)
+            fn()
+            b.record(st)
+            st.synchronize()
+            ts.append(a.elapsed_time(b))
+        return float(np.median(ts))
+
+    store_ms = timed(lambda: _lib.check(lib.svo_raycast_camera_download(
+        ctypes.byref(oc), ctypes.byref(cam), width, height, ctypes.c_void_p(hits_dev.data_ptr()),
+        ctypes.c_void_p(hits_host.data_ptr()), None, s)))
+    dma_ms = timed(lambda: hits_host.copy_(hits_dev, non_blocking=True))
+    h2d_ms = timed(lambda: hits_dev.copy_(hits_host, non_blocking=True))
+    out = {"bytes": n * 32, "hit_store_gbs": n * 32 / store_ms / 1e6, "dma_d2h_gbs": n * 32 / dma_ms / 1e6,
+           "dma_h2d_gbs": n * 32 / h2d_ms / 1e6,
+           "method": f"{width}x{height} camera rays on an empty octree, hits stored into page-locked host memory "
+                     "by the march (svo_raycast_camera_download); DMA copies of the same bytes"}
+    del hits_dev, hits_host, pool
+    _HOST_LINK[key] = out
+    return out
 
 
 # ------------------------------------------------------------------------------------------ batched build
@@ -815,6 +875,12 @@ def serve_leg(args, device, rates=(100, 200, 500, 1000, 2000, 5000), seconds=1.0
             "formula": "saturated Grays/s x bytes per ray; bytes per ray = 32 B hit + 24 B ray for the bounce "
                        "half + 4 B x node words read (counted on the same 400 requests by a counting server)",
             "kernels": {k: {"ms": round(v["ms"], 3), "launches": v["launches"]} for k, v in prof.items()}}
+    # every served hit is delivered into the client's page-locked host memory: the GPU -> host link is the
+    # ceiling the delivered hit bytes are measured against
+    link = host_link_probe(device)
+    hit_gbs = saturated["grays_per_s"] * 32.0
+    roof["host_link"] = {"delivered_hit_gbs": hit_gbs, "hit_store_gbs": link["hit_store_gbs"],
+                         "frac": hit_gbs / link["hit_store_gbs"], "ceiling_grays_per_s": link["hit_store_gbs"] / 32.0}
     served_sat = summarize(one_reqs, run(one_reqs, None))
     st = server.stats()
     server.close()
@@ -952,7 +1018,9 @@ def summary_block(line: dict) -> dict:
     speed-ups with their roofline fractions, and served latency per arrival rate."""
     def r(x, n=4):
         return None if x is None else round(float(x), n)
+    e2e_link = (line.get("e2e") or {}).get("host_link") or {}
     out = {"step_ms": r(line.get("value")), "e2e_ms": r((line.get("e2e") or {}).get("value")),
+           "e2e_copy_floor_ms": r(e2e_link.get("floor_ms")),
            "march_frac": r(line["roofline"].get("frac"))}
     p = line.get("parity")
     if p:
@@ -971,6 +1039,8 @@ def summary_block(line: dict) -> dict:
         if sv.get("roofline"):
             out["served_frac"] = r(sv["roofline"]["frac"])
             out["served_march_launch_ms"] = r(sv["roofline"]["launch_ms"])
+            if "host_link" in sv["roofline"]:
+                out["served_host_link_frac"] = r(sv["roofline"]["host_link"]["frac"])
         out["served_p50_p99_ms"] = {k: [r(v["p50_ms"], 3), r(v["p99_ms"], 3)] for k, v in sv["poisson"].items()}
     for key in ("large", "large_batched"):
         if line.get(key):
