@@ -573,6 +573,116 @@ __global__ void __launch_bounds__(kEmitTPB) vox_emit(VoxBatch vb, uint32_t n, Vo
 	}
 }
 
+// The same emission with the warp's span tables in one pool of kRowPool rows instead of kSmallArea rows
+// per lane: a small triangle has 1 to 64 spans but few on average, so the pool (a quarter of the per-lane
+// tables' shared memory) holds the spans of all 32 triangles of a warp at once almost always; when it
+// does not, the warp takes its triangles in chunks of whole triangles whose spans fit.  The smaller
+// footprint lets more warps stay resident.
+constexpr uint32_t kRowPool = 256;
+
+template <bool B>
+__global__ void __launch_bounds__(kEmitTPB) vox_emit_pool(VoxBatch vb, uint32_t n, VoxWorkspace w,
+                                                          uint64_t *__restrict__ frags, uint64_t capacity) {
+	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
+	__shared__ SmallRec s_rec[kEmitTPB];
+	__shared__ SpanSetup s_sp[kEmitTPB];
+	__shared__ uint32_t s_incl[kEmitTPB];                   // span rows of lanes 0..j, inclusive
+	__shared__ int16_t s_lo[kEmitTPB / 32][kRowPool];        // first pixel of each pooled row
+	__shared__ uint16_t s_rcum[kEmitTPB / 32][kRowPool + 1]; // fragments of the chunk before each row
+	const uint32_t lane = lane_id(), wb = threadIdx.x & ~31u, wi = threadIdx.x >> 5;
+	int16_t *lo_of = s_lo[wi];
+	uint16_t *cum = s_rcum[wi];
+	const uint64_t warps = (uint64_t)gridDim.x * blockDim.x / 32;
+	for (uint64_t g = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32; g * 32 < n; g += warps) {
+		const uint64_t t = g * 32 + lane;
+		uint32_t cnt = 0, rows = 0;
+		if (t < n) {
+			uint64_t off = w.small_off[t];
+			cnt = (uint32_t)(w.small_off[t + 1] - off);
+			if (cnt) {
+				const svo_triangle *tp;
+				uint32_t local, lvl, mi;
+				tri_of<B>(vb, (uint32_t)t, tp, local, lvl, mi);
+				if (B) off += vb.shifts[2 * mi];
+				TriSetup S;
+				tri_setup(tp, local, lvl, S);
+				if (!S.valid || is_large(S) || off + cnt > capacity) {
+					cnt = 0;
+				} else {
+					SmallRec &r = s_rec[threadIdx.x];
+					r.K = S.K, r.NU = S.NU, r.NV = S.NV, r.D = S.D, r.off = off;
+					r.z0 = S.z0, r.z1 = S.z1, r.v0 = S.v0, r.level = S.level;
+					r.axis = (uint32_t)S.axis, r.cols = (uint32_t)S.cols, r.rgb = S.rgb, r.cnt = cnt;
+					rows = (uint32_t)(S.v1 - S.v0 + 1);
+					span_setup(S, s_sp[threadIdx.x]);
+				}
+			}
+		}
+		const uint32_t rincl = warp_inclusive_sum(rows);
+		s_incl[threadIdx.x] = rincl;
+		__syncwarp();
+		const uint32_t total_rows = __shfl_sync(kFullMask, rincl, 31);
+		uint32_t j0 = 0; // first lane of the chunk (warp-uniform)
+		for (uint32_t done = 0; done < total_rows;) {
+			// the chunk: lanes j0..j1-1, the most whose rows fit the pool (one triangle has at most 64)
+			const uint32_t fit = __ballot_sync(kFullMask, lane >= j0 && rincl - done <= kRowPool);
+			const uint32_t j1 = 32u - (uint32_t)__clz(fit);
+			const uint32_t chunk_rows = s_incl[wb + j1 - 1] - done;
+			// each pooled row's span: row r of the chunk belongs to lane j (the chunk's lanes in order)
+			uint32_t j = j0;
+			for (uint32_t r = lane; r < chunk_rows; r += 32) {
+				while (s_incl[wb + j] - done <= r) ++j;
+				const uint32_t k = r - ((j ? s_incl[wb + j - 1] : 0u) - done);
+				int32_t lo, hi;
+				span_interval(s_sp[wb + j], s_sp[wb + j].v0 + (int32_t)k, lo, hi);
+				lo_of[r] = (int16_t)lo;
+				cum[r + 1] = (uint16_t)(hi >= lo ? hi - lo + 1 : 0); // the row's length, scanned below
+			}
+			__syncwarp();
+			// row starts: an exclusive scan of the lengths over the chunk's rows (a chunk has at most
+			// 32 x 64 = 2048 fragments)
+			uint32_t carry = 0;
+			for (uint32_t r0 = 0; r0 < chunk_rows; r0 += 32) {
+				const uint32_t r = r0 + lane;
+				const uint32_t len = r < chunk_rows ? cum[r + 1] : 0u;
+				const uint32_t incl = warp_inclusive_sum(len) + carry;
+				__syncwarp();
+				if (r < chunk_rows) cum[r] = (uint16_t)(incl - len);
+				carry = __shfl_sync(kFullMask, incl, 31);
+				__syncwarp();
+			}
+			if (lane == 0) cum[chunk_rows] = (uint16_t)carry;
+			__syncwarp();
+			// lane j's fragments must be exactly its count (they are: the count pass walked the same spans)
+			bool ok = true;
+			if (lane >= j0 && lane < j1 && rows) {
+				const uint32_t r_first = rincl - rows - done;
+				ok = (uint32_t)(cum[r_first + rows] - cum[r_first]) == cnt;
+			}
+			if (__any_sync(kFullMask, !ok)) break; // cannot happen; emit nothing more for this group
+			// the chunk's fragments, lane-interleaved: fragment f -> its lane (triangle) -> its row
+			uint32_t jt = j0;
+			for (uint32_t f = lane; f < carry; f += 32) {
+				while (cum[(s_incl[wb + jt] - done)] <= f) ++jt; // first row after lane jt's rows
+				const uint32_t r_first = (jt ? s_incl[wb + jt - 1] : 0u) - done;
+				uint32_t r = r_first;
+				while (cum[r + 1] <= f) ++r; // the row holding fragment f (empty rows are skipped)
+				const SmallRec &rec = s_rec[wb + jt];
+				TriSetup S;
+				S.K = rec.K, S.NU = rec.NU, S.NV = rec.NV, S.D = rec.D;
+				S.z0 = rec.z0, S.z1 = rec.z1, S.level = rec.level, S.axis = (int32_t)rec.axis,
+				S.cols = (int32_t)rec.cols, S.rgb = rec.rgb;
+				const int32_t u = (int32_t)lo_of[r] + (int32_t)(f - cum[r]), v = rec.v0 + (int32_t)(r - r_first);
+				frags[rec.off + (f - cum[r_first])] = make_fragment(S, u, v);
+			}
+			__syncwarp();
+			done += chunk_rows;
+			j0 = j1;
+		}
+		__syncwarp();
+	}
+}
+
 // Float value of num / den (den > 0, |num| <= den here) from the top 31 bits of both: 32-bit
 // conversions only; relative error a few 2^-24.
 SVO_DEV float ratio_f(int64_t num, int64_t den) {
@@ -793,7 +903,7 @@ static void launch_emit(const VoxBatch &vb, uint32_t n, uint32_t tune_level, con
 	SideFork fork(stream, two_streams);
 	cudaStream_t side = fork.side();
 	SVO_LAUNCH("vox_emit", side,
-	           ::svo::launch_k(vox_emit<B>, (uint32_t)sms * per_sm * (kTPB / kEmitTPB), kEmitTPB, 0, side, vb, n, w, frags, capacity););
+	           ::svo::launch_k(vox_emit_pool<B>, (uint32_t)sms * per_sm * (kTPB / kEmitTPB), kEmitTPB, 0, side, vb, n, w, frags, capacity););
 	fork.mark_side(0);
 	SVO_LAUNCH("vox_emit_units", stream,
 	           ::svo::launch_k(vox_emit_units<B>, (uint32_t)sms * std::max(1u, per_sm / 2), kTPB, 0, stream, vb, n, w, frags, capacity););
