@@ -476,13 +476,17 @@ __global__ void __launch_bounds__(kTPB) vox_unit_scan(VoxBatch vb, uint32_t n, V
 	if (ntiles == 0 && blockIdx.x == 0 && threadIdx.x == 0) w.unit_frag[0] = 0;
 }
 
-// Emission of small triangles, 32 consecutive triangles per warp.  Each lane sets up its triangle
-// and records, in shared memory, the packing record and the start and covered length of each of its
-// spans (a small triangle has at most kSmallArea spans and fragments); then the warp writes the group's
-// fragments together: lane k takes fragments k, k+32, ... of the group (contiguous in the list: the
-// small fragments are in triangle order), finds its triangle and span and packs the fragment.  A lane
-// never waits for a large triangle's fragments, and every store instruction covers 256 contiguous bytes.
-// In a batch, mesh m's small fragments move up by its shift (the large fragments of earlier meshes).
+// Emission of small triangles, 32 consecutive triangles per warp.  Each lane sets up its triangle and
+// records its packing record in shared memory; the warp then evaluates the spans of all its triangles
+// together (one (triangle, row) pair per lane at a time) into one pool of kRowPool span rows (start
+// pixel and a running fragment count per row), and writes the group's fragments together: lane k takes
+// fragments k, k+32, ... of the group (contiguous in the list: the small fragments are in triangle
+// order), finds its triangle and span and packs the fragment, so every store instruction covers 256
+// contiguous bytes.  A small triangle has 1 to 64 spans, few on average: the pool holds all 32
+// triangles' spans almost always, and otherwise the warp takes its triangles in chunks of whole
+// triangles whose spans fit.  (Tables of 64 rows per lane took twice the shared memory and allowed 5
+// instead of 7 blocks per SM.)  In a batch, mesh m's small fragments move up by its shift (the large
+// fragments of earlier meshes).
 constexpr int kEmitTPB = 128;
 
 struct SmallRec {
@@ -492,97 +496,11 @@ struct SmallRec {
 	uint32_t axis, cols, rgb, cnt;
 };
 
-template <bool B>
-__global__ void __launch_bounds__(kEmitTPB) vox_emit(VoxBatch vb, uint32_t n, VoxWorkspace w, uint64_t *__restrict__ frags,
-                                                     uint64_t capacity) {
-	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
-	__shared__ SmallRec s_rec[kEmitTPB];
-	__shared__ uint8_t s_cum[kEmitTPB][kSmallArea + 1];
-	__shared__ int16_t s_lo[kEmitTPB][kSmallArea];
-	__shared__ uint32_t s_incl[kEmitTPB];
-	__shared__ SpanSetup s_sp[kEmitTPB];
-	const uint32_t lane = lane_id(), wb = threadIdx.x & ~31u;
-	const uint64_t warps = (uint64_t)gridDim.x * blockDim.x / 32;
-	for (uint64_t g = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32; g * 32 < n; g += warps) {
-		const uint64_t t = g * 32 + lane;
-		uint32_t cnt = 0, rows = 0;
-		if (t < n) {
-			uint64_t off = w.small_off[t];
-			cnt = (uint32_t)(w.small_off[t + 1] - off);
-			if (cnt) {
-				const svo_triangle *tp;
-				uint32_t local, lvl, mi;
-				tri_of<B>(vb, (uint32_t)t, tp, local, lvl, mi);
-				if (B) off += vb.shifts[2 * mi];
-				TriSetup S;
-				tri_setup(tp, local, lvl, S);
-				if (!S.valid || is_large(S) || off + cnt > capacity) {
-					cnt = 0;
-				} else {
-					SmallRec &r = s_rec[threadIdx.x];
-					r.K = S.K, r.NU = S.NU, r.NV = S.NV, r.D = S.D, r.off = off;
-					r.z0 = S.z0, r.z1 = S.z1, r.v0 = S.v0, r.level = S.level;
-					r.axis = (uint32_t)S.axis, r.cols = (uint32_t)S.cols, r.rgb = S.rgb, r.cnt = cnt;
-					rows = (uint32_t)(S.v1 - S.v0 + 1);
-					span_setup(S, s_sp[threadIdx.x]);
-				}
-			}
-		}
-		// the spans of the warp's triangles, evaluated by the whole warp: each row's first pixel and covered
-		// length (the length parked in s_cum), then each triangle's running sum over its rows
-		const uint32_t rincl = warp_inclusive_sum(rows);
-		s_incl[threadIdx.x] = rincl;
-		__syncwarp();
-		warp_rows(s_incl + wb, s_sp + wb, __shfl_sync(kFullMask, rincl, 31),
-		          [&](uint32_t j, uint32_t row, int32_t lo, int32_t hi) {
-			          s_lo[wb + j][row] = (int16_t)lo;
-			          s_cum[wb + j][row] = (uint8_t)(hi >= lo ? hi - lo + 1 : 0);
-		          });
-		__syncwarp();
-		if (rows) {
-			uint32_t acc = 0;
-			for (uint32_t k = 0; k < rows; ++k) {
-				const uint32_t len = s_cum[threadIdx.x][k];
-				s_cum[threadIdx.x][k] = (uint8_t)acc;
-				acc += len;
-			}
-			s_cum[threadIdx.x][rows] = (uint8_t)acc; // > every fragment index q < cnt: the span search stops
-			if (acc != cnt) cnt = 0; // cannot happen: the count pass walked the same spans
-			s_rec[threadIdx.x].cnt = cnt;
-		}
-		__syncwarp();
-		const uint32_t incl = warp_inclusive_sum(cnt);
-		const uint32_t total = __shfl_sync(kFullMask, incl, 31);
-		s_incl[threadIdx.x] = incl;
-		__syncwarp();
-		uint32_t j = 0;
-		for (uint32_t f = lane; f < total; f += 32) {
-			while (s_incl[wb + j] <= f) ++j;
-			const uint32_t tj = wb + j;
-			const SmallRec &r = s_rec[tj];
-			const uint32_t q = f - (s_incl[tj] - r.cnt);
-			uint32_t k = 0;
-			while (s_cum[tj][k + 1] <= q) ++k; // the span holding fragment q (empty spans are skipped)
-			TriSetup S;
-			S.K = r.K, S.NU = r.NU, S.NV = r.NV, S.D = r.D;
-			S.z0 = r.z0, S.z1 = r.z1, S.level = r.level, S.axis = (int32_t)r.axis, S.cols = (int32_t)r.cols, S.rgb = r.rgb;
-			const int32_t u = (int32_t)s_lo[tj][k] + (int32_t)(q - s_cum[tj][k]), v = r.v0 + (int32_t)k;
-			frags[r.off + q] = make_fragment(S, u, v);
-		}
-		__syncwarp();
-	}
-}
-
-// The same emission with the warp's span tables in one pool of kRowPool rows instead of kSmallArea rows
-// per lane: a small triangle has 1 to 64 spans but few on average, so the pool (a quarter of the per-lane
-// tables' shared memory) holds the spans of all 32 triangles of a warp at once almost always; when it
-// does not, the warp takes its triangles in chunks of whole triangles whose spans fit.  The smaller
-// footprint lets more warps stay resident.
-constexpr uint32_t kRowPool = 256;
+constexpr uint32_t kRowPool = 256; // span rows a warp keeps at a time (a small triangle has at most kSmallArea)
 
 template <bool B>
-__global__ void __launch_bounds__(kEmitTPB) vox_emit_pool(VoxBatch vb, uint32_t n, VoxWorkspace w,
-                                                          uint64_t *__restrict__ frags, uint64_t capacity) {
+__global__ void __launch_bounds__(kEmitTPB) vox_emit(VoxBatch vb, uint32_t n, VoxWorkspace w,
+                                                     uint64_t *__restrict__ frags, uint64_t capacity) {
 	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	__shared__ SmallRec s_rec[kEmitTPB];
 	__shared__ SpanSetup s_sp[kEmitTPB];
@@ -903,7 +821,7 @@ static void launch_emit(const VoxBatch &vb, uint32_t n, uint32_t tune_level, con
 	SideFork fork(stream, two_streams);
 	cudaStream_t side = fork.side();
 	SVO_LAUNCH("vox_emit", side,
-	           ::svo::launch_k(vox_emit_pool<B>, (uint32_t)sms * per_sm * (kTPB / kEmitTPB), kEmitTPB, 0, side, vb, n, w, frags, capacity););
+	           ::svo::launch_k(vox_emit<B>, (uint32_t)sms * per_sm * (kTPB / kEmitTPB), kEmitTPB, 0, side, vb, n, w, frags, capacity););
 	fork.mark_side(0);
 	SVO_LAUNCH("vox_emit_units", stream,
 	           ::svo::launch_k(vox_emit_units<B>, (uint32_t)sms * std::max(1u, per_sm / 2), kTPB, 0, stream, vb, n, w, frags, capacity););
