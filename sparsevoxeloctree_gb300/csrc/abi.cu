@@ -337,9 +337,21 @@ size_t svo_voxelize_workspace_size(uint32_t n_tris, uint64_t units) {
 
 // Count pass with a workspace from `mem`; retries once with exact unit arrays when the first guess is
 // short.  On success *ws_out (still owned by the caller) holds the counted workspace.
+// The most raster units a count of this process has met (a high-water mark).  The unit scratch of a
+// count's first attempt covers it, so a mesh with more large-triangle units than the default guess is
+// not counted twice on every call (the first attempt would overflow and report the exact number).  It
+// only sizes scratch: every call still runs its whole count.
+static std::atomic<uint64_t> g_units_seen{0};
+
+static void note_units(uint64_t units) {
+	uint64_t cur = g_units_seen.load(std::memory_order_relaxed);
+	while (units > cur && !g_units_seen.compare_exchange_weak(cur, units, std::memory_order_relaxed)) {
+	}
+}
+
 static int voxelize_count_pass(const svo_triangle *tris, uint32_t n_tris, uint32_t level, Mem &mem, void **ws_out,
                                VoxWorkspace &w, uint64_t &total, uint64_t &units) {
-	uint64_t cap = vox_default_unit_cap(n_tris);
+	uint64_t cap = std::max<uint64_t>(vox_default_unit_cap(n_tris), g_units_seen.load(std::memory_order_relaxed));
 	for (int attempt = 0; attempt < 2; ++attempt) {
 		void *ws = nullptr;
 		SVO_CK(mem.get(&ws, vox_workspace_bytes(n_tris, cap)), "voxelize workspace");
@@ -354,6 +366,7 @@ static int voxelize_count_pass(const svo_triangle *tris, uint32_t n_tris, uint32
 			return cuda_fail(e, "voxelize count");
 		}
 		const uint32_t status = (uint32_t)tot[2];
+		if (tot[1] < 0xffffffffull) note_units(tot[1]);
 		if (status & kStatusUnits) {
 			mem.put(ws);
 			if (tot[1] >= 0xffffffffull) return fail(SVO_ERR_CAPACITY, "too many raster units");
