@@ -482,9 +482,8 @@ __global__ void __launch_bounds__(kTPB) vox_unit_scan(VoxBatch vb, uint32_t n, V
 // pixel and a running fragment count per row), and writes the group's fragments together: lane k takes
 // fragments k, k+32, ... of the group (contiguous in the list: the small fragments are in triangle
 // order), finds its triangle and span and packs the fragment, so every store instruction covers 256
-// contiguous bytes.  A small triangle has 1 to 64 spans, few on average: the pool holds all 32
-// triangles' spans almost always, and otherwise the warp takes its triangles in chunks of whole
-// triangles whose spans fit.  (Tables of 64 rows per lane took twice the shared memory and allowed 5
+// contiguous bytes.  A small triangle has at most 8 spans (kMaxSmallSpans), so the pool holds every
+// span of the warp.  (Tables of kSmallArea rows per lane took twice the shared memory and allowed 5
 // instead of 7 blocks per SM.)  In a batch, mesh m's small fragments move up by its shift (the large
 // fragments of earlier meshes).
 constexpr int kEmitTPB = 128;
@@ -496,7 +495,13 @@ struct SmallRec {
 	uint32_t axis, cols, rgb, cnt;
 };
 
-constexpr uint32_t kRowPool = 256; // span rows a warp keeps at a time (a small triangle has at most kSmallArea)
+// Span rows of a warp's 32 small triangles.  A span runs along the longer side of a triangle's
+// bounding box (cols), so a small triangle (area <= kSmallArea pixels) has at most sqrt(kSmallArea) = 8
+// spans, and the pool holds every span of the warp.
+constexpr uint32_t kMaxSmallSpans = 8;
+constexpr uint32_t kRowPool = 32 * kMaxSmallSpans;
+static_assert(kMaxSmallSpans * kMaxSmallSpans >= (uint32_t)kSmallArea && (kMaxSmallSpans - 1) * (kMaxSmallSpans - 1) < (uint32_t)kSmallArea,
+              "kMaxSmallSpans is the integer square root of kSmallArea");
 
 template <bool B>
 __global__ void __launch_bounds__(kEmitTPB) vox_emit(VoxBatch vb, uint32_t n, VoxWorkspace w,
@@ -540,62 +545,47 @@ __global__ void __launch_bounds__(kEmitTPB) vox_emit(VoxBatch vb, uint32_t n, Vo
 		s_incl[threadIdx.x] = rincl;
 		__syncwarp();
 		const uint32_t total_rows = __shfl_sync(kFullMask, rincl, 31);
-		uint32_t j0 = 0; // first lane of the chunk (warp-uniform)
-		for (uint32_t done = 0; done < total_rows;) {
-			// the chunk: lanes j0..j1-1, the most whose rows fit the pool (one triangle has at most 64)
-			const uint32_t fit = __ballot_sync(kFullMask, lane >= j0 && rincl - done <= kRowPool);
-			const uint32_t j1 = 32u - (uint32_t)__clz(fit);
-			const uint32_t chunk_rows = s_incl[wb + j1 - 1] - done;
-			// each pooled row's span: row r of the chunk belongs to lane j (the chunk's lanes in order)
-			uint32_t j = j0;
-			for (uint32_t r = lane; r < chunk_rows; r += 32) {
-				while (s_incl[wb + j] - done <= r) ++j;
-				const uint32_t k = r - ((j ? s_incl[wb + j - 1] : 0u) - done);
-				int32_t lo, hi;
-				span_interval(s_sp[wb + j], s_sp[wb + j].v0 + (int32_t)k, lo, hi);
-				lo_of[r] = (int16_t)lo;
-				cum[r + 1] = (uint16_t)(hi >= lo ? hi - lo + 1 : 0); // the row's length, scanned below
-			}
+		// each pooled row's span: row r belongs to lane j (the lanes in order)
+		uint32_t j = 0;
+		for (uint32_t r = lane; r < total_rows; r += 32) {
+			while (s_incl[wb + j] <= r) ++j;
+			const uint32_t k = r - (j ? s_incl[wb + j - 1] : 0u);
+			int32_t lo, hi;
+			span_interval(s_sp[wb + j], s_sp[wb + j].v0 + (int32_t)k, lo, hi);
+			lo_of[r] = (int16_t)lo;
+			cum[r + 1] = (uint16_t)(hi >= lo ? hi - lo + 1 : 0); // the row's length, scanned below
+		}
+		__syncwarp();
+		// row starts: an exclusive scan of the lengths over the rows (at most 32 x kSmallArea fragments)
+		uint32_t carry = 0;
+		for (uint32_t r0 = 0; r0 < total_rows; r0 += 32) {
+			const uint32_t r = r0 + lane;
+			const uint32_t len = r < total_rows ? cum[r + 1] : 0u;
+			const uint32_t incl = warp_inclusive_sum(len) + carry;
 			__syncwarp();
-			// row starts: an exclusive scan of the lengths over the chunk's rows (a chunk has at most
-			// 32 x 64 = 2048 fragments)
-			uint32_t carry = 0;
-			for (uint32_t r0 = 0; r0 < chunk_rows; r0 += 32) {
-				const uint32_t r = r0 + lane;
-				const uint32_t len = r < chunk_rows ? cum[r + 1] : 0u;
-				const uint32_t incl = warp_inclusive_sum(len) + carry;
-				__syncwarp();
-				if (r < chunk_rows) cum[r] = (uint16_t)(incl - len);
-				carry = __shfl_sync(kFullMask, incl, 31);
-				__syncwarp();
-			}
-			if (lane == 0) cum[chunk_rows] = (uint16_t)carry;
+			if (r < total_rows) cum[r] = (uint16_t)(incl - len);
+			carry = __shfl_sync(kFullMask, incl, 31);
 			__syncwarp();
-			// lane j's fragments must be exactly its count (they are: the count pass walked the same spans)
-			bool ok = true;
-			if (lane >= j0 && lane < j1 && rows) {
-				const uint32_t r_first = rincl - rows - done;
-				ok = (uint32_t)(cum[r_first + rows] - cum[r_first]) == cnt;
-			}
-			if (__any_sync(kFullMask, !ok)) break; // cannot happen; emit nothing more for this group
-			// the chunk's fragments, lane-interleaved: fragment f -> its lane (triangle) -> its row
-			uint32_t jt = j0;
-			for (uint32_t f = lane; f < carry; f += 32) {
-				while (cum[(s_incl[wb + jt] - done)] <= f) ++jt; // first row after lane jt's rows
-				const uint32_t r_first = (jt ? s_incl[wb + jt - 1] : 0u) - done;
-				uint32_t r = r_first;
-				while (cum[r + 1] <= f) ++r; // the row holding fragment f (empty rows are skipped)
-				const SmallRec &rec = s_rec[wb + jt];
-				TriSetup S;
-				S.K = rec.K, S.NU = rec.NU, S.NV = rec.NV, S.D = rec.D;
-				S.z0 = rec.z0, S.z1 = rec.z1, S.level = rec.level, S.axis = (int32_t)rec.axis,
-				S.cols = (int32_t)rec.cols, S.rgb = rec.rgb;
-				const int32_t u = (int32_t)lo_of[r] + (int32_t)(f - cum[r]), v = rec.v0 + (int32_t)(r - r_first);
-				frags[rec.off + (f - cum[r_first])] = make_fragment(S, u, v);
-			}
-			__syncwarp();
-			done += chunk_rows;
-			j0 = j1;
+		}
+		if (lane == 0) cum[total_rows] = (uint16_t)carry;
+		__syncwarp();
+		// a lane's fragments must be exactly its count (they are: the count pass walked the same spans)
+		const bool ok = !rows || (uint32_t)(cum[rincl] - cum[rincl - rows]) == cnt;
+		if (__any_sync(kFullMask, !ok)) continue; // cannot happen; the group is left unwritten
+		// the group's fragments, lane-interleaved: fragment f -> its lane (triangle) -> its row
+		uint32_t jt = 0;
+		for (uint32_t f = lane; f < carry; f += 32) {
+			while (cum[s_incl[wb + jt]] <= f) ++jt; // cum at the first row after lane jt's rows
+			const uint32_t r_first = jt ? s_incl[wb + jt - 1] : 0u;
+			uint32_t r = r_first;
+			while (cum[r + 1] <= f) ++r; // the row holding fragment f (empty rows are skipped)
+			const SmallRec &rec = s_rec[wb + jt];
+			TriSetup S;
+			S.K = rec.K, S.NU = rec.NU, S.NV = rec.NV, S.D = rec.D;
+			S.z0 = rec.z0, S.z1 = rec.z1, S.level = rec.level, S.axis = (int32_t)rec.axis,
+			S.cols = (int32_t)rec.cols, S.rgb = rec.rgb;
+			const int32_t u = (int32_t)lo_of[r] + (int32_t)(f - cum[r]), v = rec.v0 + (int32_t)(r - r_first);
+			frags[rec.off + (f - cum[r_first])] = make_fragment(S, u, v);
 		}
 		__syncwarp();
 	}
