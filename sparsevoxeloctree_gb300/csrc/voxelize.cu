@@ -13,14 +13,16 @@
 // spans) from three exact interval bounds: a span costs three corrected float divisions whatever its
 // length.  Triangle sizes span five orders of magnitude (a room wall covers 5e5 pixels, clutter ~10), so
 // work is balanced at two granularities:
-//   * small triangles (AABB <= kSmallArea pixels) are handled whole by one lane;
+//   * small triangles (AABB <= kSmallArea pixels) are set up by one lane each; a warp evaluates its 32
+//     small triangles' spans together and writes their fragments together;
 //   * large triangles are cut into units = (span, piece of <= kPiece pixels); units are flat work items
 //     spread over the whole grid, so a wall becomes thousands of independent units.
 // Passes (all stream-ordered, sizes stay on the device):
 //   vox_classify_scan  per triangle: small -> fragment count, large -> unit count; both scanned with a
 //                      single-pass decoupled look-back (small fragment offsets, large unit offsets);
 //   vox_unit_scan      per unit: covered length, look-back scan -> fragment offset of every unit;
-//   vox_emit           small triangles by lane, then units by lane, at their offsets.
+//   vox_emit           small triangles by warp, at their offsets;
+//   vox_emit_units     units, 32 per warp, at their offsets (on a second stream beside vox_emit).
 // Fragment order is deterministic: small triangles in input order, then large triangles in input order
 // (spans, then pixels, in increasing order inside each).
 #include <cstring>
@@ -179,7 +181,9 @@ SVO_DEV uint64_t make_fragment(const TriSetup &s, int32_t u, int32_t v) {
 	return (uint64_t)fx | ((uint64_t)fy << 32);
 }
 
-constexpr int kSmallArea = 64;  // AABB pixels up to which one lane handles the whole triangle
+// AABB pixels up to which a triangle is small: set up once by one lane and emitted with its warp's other
+// small triangles (256 measured fastest of 64..1024: fewer raster units, whose set-up repeats per span)
+constexpr int kSmallArea = 256;
 constexpr int kPiece = 256;     // pixels of a span one unit covers at most
 
 SVO_DEV bool is_large(const TriSetup &s) {
@@ -482,7 +486,7 @@ __global__ void __launch_bounds__(kTPB) vox_unit_scan(VoxBatch vb, uint32_t n, V
 // pixel and a running fragment count per row), and writes the group's fragments together: lane k takes
 // fragments k, k+32, ... of the group (contiguous in the list: the small fragments are in triangle
 // order), finds its triangle and span and packs the fragment, so every store instruction covers 256
-// contiguous bytes.  A small triangle has at most 8 spans (kMaxSmallSpans), so the pool holds every
+// contiguous bytes.  A small triangle has at most 16 spans (kMaxSmallSpans), so the pool holds every
 // span of the warp.  (Tables of kSmallArea rows per lane took twice the shared memory and allowed 5
 // instead of 7 blocks per SM.)  In a batch, mesh m's small fragments move up by its shift (the large
 // fragments of earlier meshes).
@@ -496,9 +500,9 @@ struct SmallRec {
 };
 
 // Span rows of a warp's 32 small triangles.  A span runs along the longer side of a triangle's
-// bounding box (cols), so a small triangle (area <= kSmallArea pixels) has at most sqrt(kSmallArea) = 8
+// bounding box (cols), so a small triangle (area <= kSmallArea pixels) has at most sqrt(kSmallArea) = 16
 // spans, and the pool holds every span of the warp.
-constexpr uint32_t kMaxSmallSpans = 8;
+constexpr uint32_t kMaxSmallSpans = 16;
 constexpr uint32_t kRowPool = 32 * kMaxSmallSpans;
 static_assert(kMaxSmallSpans * kMaxSmallSpans >= (uint32_t)kSmallArea && (kMaxSmallSpans - 1) * (kMaxSmallSpans - 1) < (uint32_t)kSmallArea,
               "kMaxSmallSpans is the integer square root of kSmallArea");

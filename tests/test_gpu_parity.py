@@ -441,18 +441,23 @@ def _lib_reset_tune():
 
 
 def test_voxelizer_reemission_needs_exact_unit_scratch(cuda):
-    """The room scene's walls and cylinders need more raster units than the default guess: re-emission
-    (CmdVoxelize) must use the unit count from the first pass and reproduce every fragment."""
+    """A mesh that needs more raster units than the default scratch guess (three copies of the room's
+    walls at level 10: 36 triangles of 1024 spans x 4 pieces, 147,456 units against a guess of 65,608):
+    re-emission (CmdVoxelize) must size its scratch from the first pass's unit count and reproduce every
+    fragment, in order."""
     api = _api()
-    s = scenes.room_1024()
-    v = api.Voxelizer.Create(s.tris, s.level)
+    level = 10
+    walls = np.concatenate([scenes.room_shell(level)] * 3, 0)
+    tris = scenes._soup(walls, scenes.random_colors(scenes.rng(17), len(walls)))
+    v = api.Voxelizer.Create(tris, level)
     first = v.GetVoxelFragmentList().clone()
-    assert v.m_units > 2 * len(s.tris) + 65536  # more than the default guess
+    assert v.m_units > 2 * len(tris) + 65536  # more than the default guess
     v.GetVoxelFragmentList().fill_(0)
     v.CmdVoxelize()
     v.CheckEmission()
     import torch
     assert torch.equal(v.GetVoxelFragmentList(), first)
+    assert_same_fragments(first.cpu().numpy().view(np.uint64), oracle.voxelize(tris, level))
 
 
 # ------------------------------------------------------------------------------------------- beam / occlusion
