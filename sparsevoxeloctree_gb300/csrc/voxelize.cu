@@ -166,21 +166,6 @@ template <typename S> SVO_DEV void span_interval(const S &s, int32_t v, int32_t 
 	}
 }
 
-SVO_DEV uint64_t make_fragment(const TriSetup &s, int32_t u, int32_t v) {
-	const int32_t R = 1 << s.level;
-	const int64_t num = s.K - s.NU * u - s.NV * v;
-	int32_t z = clamp_i32(floor_div_window(num, s.D, 0, R - 1), 0, R - 1);
-	z = z < s.z0 ? s.z0 : (z > s.z1 ? s.z1 : z);
-	const uint32_t i = (uint32_t)(s.cols ? v : u), j = (uint32_t)(s.cols ? u : v), zz = (uint32_t)z;
-	// un-swizzle (shader/voxelizer.frag:24): axis 0 -> u.zxy, 1 -> u.yzx, 2 -> u.xyz
-	const uint32_t vx = s.axis == 0 ? zz : (s.axis == 1 ? j : i);
-	const uint32_t vy = s.axis == 0 ? i : (s.axis == 1 ? zz : j);
-	const uint32_t vz = s.axis == 0 ? j : (s.axis == 1 ? i : zz);
-	const uint32_t fx = vx | (vy << 12) | ((vz & 0xffu) << 24);
-	const uint32_t fy = ((vz >> 8) << 28) | (s.rgb & 0xffffffu);
-	return (uint64_t)fx | ((uint64_t)fy << 32);
-}
-
 // AABB pixels up to which a triangle is small: set up once by one lane and emitted with its warp's other
 // small triangles (256 measured fastest of 64..1024: fewer raster units, whose set-up repeats per span)
 constexpr int kSmallArea = 256;
@@ -480,24 +465,51 @@ __global__ void __launch_bounds__(kTPB) vox_unit_scan(VoxBatch vb, uint32_t n, V
 	if (ntiles == 0 && blockIdx.x == 0 && threadIdx.x == 0) w.unit_frag[0] = 0;
 }
 
+// Float value of num / den (den > 0, |num| <= den here) from the top 31 bits of both: 32-bit
+// conversions only; relative error a few 2^-24.
+SVO_DEV float ratio_f(int64_t num, int64_t den) {
+	const uint64_t mag = (uint64_t)(num < 0 ? -num : num) | (uint64_t)den;
+	const int sh = max(0, 33 - __clzll((long long)mag));
+	return (float)(int32_t)(num >> sh) / (float)(int32_t)(den >> sh);
+}
+
+// The plane depth of a fragment (both emissions).  Pixel u = lo + k of span v lies at plane depth
+// q0 + (r0 - k NU) / D, where num0 = K - NU lo - NV v, q0 = floor(num0 / D) and r0 = num0 - q0 D in
+// [0, D) are taken once at the span's first covered pixel lo.  t = fr0 - k fb (fr0 = r0 / D and
+// fb = NU / D in float; |NU| <= D by the dominant axis) approximates (r0 - k NU) / D within 1e-4 for
+// k < 256, so floor(t) is exact unless t lies within kDepthEps of an integer, where the exact int64
+// division decides.  Covered pixels lie within a voxel of the triangle's depth range, so q0 is exact.
+constexpr float kDepthEps = 1.0f / 1024.0f;
+
+SVO_DEV uint32_t field_of(int axis, int which) { return (uint32_t)((axis + which) % 3); } // 0 i, 1 j, 2 depth
+
 // Emission of small triangles, 32 consecutive triangles per warp.  Each lane sets up its triangle and
-// records its packing record in shared memory; the warp then evaluates the spans of all its triangles
-// together (one (triangle, row) pair per lane at a time) into one pool of kRowPool span rows (start
-// pixel and a running fragment count per row), and writes the group's fragments together: lane k takes
-// fragments k, k+32, ... of the group (contiguous in the list: the small fragments are in triangle
-// order), finds its triangle and span and packs the fragment, so every store instruction covers 256
+// records it in shared memory; the warp then evaluates the spans of all its triangles together (one
+// (triangle, row) pair per lane at a time) into one pool of kRowPool span rows: each row's first covered
+// pixel and length, and its plane depth there in the form above.  Then it writes the group's fragments
+// together: lane k takes fragments k, k+32, ... of the group (contiguous in the list: the small
+// fragments are in triangle order), finds its triangle and row, and packs the fragment from the row's
+// depth (no division, outside the rare near-integer case), so every store instruction covers 256
 // contiguous bytes.  A small triangle has at most 16 spans (kMaxSmallSpans), so the pool holds every
 // span of the warp.  (Tables of kSmallArea rows per lane took twice the shared memory and allowed 5
-// instead of 7 blocks per SM.)  In a batch, mesh m's small fragments move up by its shift (the large
-// fragments of earlier meshes).
+// instead of 7 blocks per SM; an int64 division per fragment instead of the row depths cost a third
+// more time on small-triangle scenes.)  In a batch, mesh m's small fragments move up by its shift (the
+// large fragments of earlier meshes).
 constexpr int kEmitTPB = 128;
 
-struct SmallRec {
-	int64_t K, NU, NV, D; // plane depth numerator / denominator (make_fragment)
-	uint64_t off;         // output position of the triangle's first fragment
-	int32_t z0, z1, v0, level;
-	uint32_t axis, cols, rgb, cnt;
+// A small triangle's record, as four 16-byte groups: the fragment loop reloads the first two when it
+// moves to the next triangle, and reads the last two (the exact plane) only near integer depths.
+struct __align__(16) SmallRec {
+	float fb;             // NU / D
+	uint32_t zr;          // z0 | z1 << 16: the depth range
+	uint32_t rgbf;        // rgb | axis << 24 | cols << 26
+	uint32_t rl;          // the triangle's first pooled row | level << 16
+	uint64_t out;         // output position of its first fragment, minus that fragment's index in the group
+	int32_t vadj;         // pooled row r is span v = r + vadj
+	uint32_t tend;        // one past its last fragment in the group
+	int64_t K, NU, NV, D; // plane depth (K - NU u - NV v) / D at the centre of pixel (u, v), D > 0
 };
+static_assert(sizeof(SmallRec) == 64, "four 16-byte groups");
 
 // Span rows of a warp's 32 small triangles.  A span runs along the longer side of a triangle's
 // bounding box (cols), so a small triangle (area <= kSmallArea pixels) has at most sqrt(kSmallArea) = 16
@@ -507,6 +519,18 @@ constexpr uint32_t kRowPool = 32 * kMaxSmallSpans;
 static_assert(kMaxSmallSpans * kMaxSmallSpans >= (uint32_t)kSmallArea && (kMaxSmallSpans - 1) * (kMaxSmallSpans - 1) < (uint32_t)kSmallArea,
               "kMaxSmallSpans is the integer square root of kSmallArea");
 
+// Fragment word of pixel (u, v), depth z of a triangle projected along `axis` with spans along `cols`
+// (shader/voxelizer.frag:24,40-42: un-swizzle axis 0 -> u.zxy, 1 -> u.yzx, 2 -> u.xyz, then pack).
+SVO_DEV uint64_t pack_fragment(uint32_t axis, uint32_t cols, uint32_t rgb, uint32_t u, uint32_t v, uint32_t z) {
+	const uint32_t i = cols ? v : u, j = cols ? u : v;
+	const uint32_t vx = axis == 0 ? z : (axis == 1 ? j : i);
+	const uint32_t vy = axis == 0 ? i : (axis == 1 ? z : j);
+	const uint32_t vz = axis == 0 ? j : (axis == 1 ? i : z);
+	const uint32_t fx = vx | (vy << 12) | ((vz & 0xffu) << 24);
+	const uint32_t fy = ((vz >> 8) << 28) | (rgb & 0xffffffu);
+	return (uint64_t)fx | ((uint64_t)fy << 32);
+}
+
 template <bool B>
 __global__ void __launch_bounds__(kEmitTPB) vox_emit(VoxBatch vb, uint32_t n, VoxWorkspace w,
                                                      uint64_t *__restrict__ frags, uint64_t capacity) {
@@ -514,11 +538,15 @@ __global__ void __launch_bounds__(kEmitTPB) vox_emit(VoxBatch vb, uint32_t n, Vo
 	__shared__ SmallRec s_rec[kEmitTPB];
 	__shared__ SpanSetup s_sp[kEmitTPB];
 	__shared__ uint32_t s_incl[kEmitTPB];                   // span rows of lanes 0..j, inclusive
-	__shared__ int16_t s_lo[kEmitTPB / 32][kRowPool];        // first pixel of each pooled row
-	__shared__ uint16_t s_rcum[kEmitTPB / 32][kRowPool + 1]; // fragments of the chunk before each row
+	__shared__ uint32_t s_lq[kEmitTPB / 32][kRowPool];       // per pooled row: first pixel lo | q0 << 16 (int16 each)
+	__shared__ float s_fr0[kEmitTPB / 32][kRowPool];         // per pooled row: fr0
+	__shared__ uint16_t s_rcum[kEmitTPB / 32][kRowPool + 1]; // fragments of the group before each row
 	const uint32_t lane = lane_id(), wb = threadIdx.x & ~31u, wi = threadIdx.x >> 5;
-	int16_t *lo_of = s_lo[wi];
+	uint32_t *lq_of = s_lq[wi];
+	float *fr0_of = s_fr0[wi];
 	uint16_t *cum = s_rcum[wi];
+	SmallRec *wrec = s_rec + wb;
+	const uint4 *wrec4 = reinterpret_cast<const uint4 *>(wrec);
 	const uint64_t warps = (uint64_t)gridDim.x * blockDim.x / 32;
 	for (uint64_t g = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32; g * 32 < n; g += warps) {
 		const uint64_t t = g * 32 + lane;
@@ -537,9 +565,13 @@ __global__ void __launch_bounds__(kEmitTPB) vox_emit(VoxBatch vb, uint32_t n, Vo
 					cnt = 0;
 				} else {
 					SmallRec &r = s_rec[threadIdx.x];
-					r.K = S.K, r.NU = S.NU, r.NV = S.NV, r.D = S.D, r.off = off;
-					r.z0 = S.z0, r.z1 = S.z1, r.v0 = S.v0, r.level = S.level;
-					r.axis = (uint32_t)S.axis, r.cols = (uint32_t)S.cols, r.rgb = S.rgb, r.cnt = cnt;
+					r.fb = ratio_f(S.NU, S.D);
+					r.zr = (uint32_t)S.z0 | ((uint32_t)S.z1 << 16);
+					r.rgbf = (S.rgb & 0xffffffu) | ((uint32_t)S.axis << 24) | ((uint32_t)S.cols << 26);
+					r.rl = (uint32_t)S.level << 16; // | first row, below
+					r.out = off;                    // - first fragment, below
+					r.vadj = S.v0;                  // - first row, below
+					r.K = S.K, r.NU = S.NU, r.NV = S.NV, r.D = S.D;
 					rows = (uint32_t)(S.v1 - S.v0 + 1);
 					span_setup(S, s_sp[threadIdx.x]);
 				}
@@ -549,15 +581,27 @@ __global__ void __launch_bounds__(kEmitTPB) vox_emit(VoxBatch vb, uint32_t n, Vo
 		s_incl[threadIdx.x] = rincl;
 		__syncwarp();
 		const uint32_t total_rows = __shfl_sync(kFullMask, rincl, 31);
-		// each pooled row's span: row r belongs to lane j (the lanes in order)
+		// each pooled row's span and depth at its first pixel: row r belongs to lane j (the lanes in order)
 		uint32_t j = 0;
 		for (uint32_t r = lane; r < total_rows; r += 32) {
 			while (s_incl[wb + j] <= r) ++j;
-			const uint32_t k = r - (j ? s_incl[wb + j - 1] : 0u);
+			const SpanSetup &sp = s_sp[wb + j];
+			const int32_t v = sp.v0 + (int32_t)(r - (j ? s_incl[wb + j - 1] : 0u));
 			int32_t lo, hi;
-			span_interval(s_sp[wb + j], s_sp[wb + j].v0 + (int32_t)k, lo, hi);
-			lo_of[r] = (int16_t)lo;
-			cum[r + 1] = (uint16_t)(hi >= lo ? hi - lo + 1 : 0); // the row's length, scanned below
+			span_interval(sp, v, lo, hi);
+			uint32_t len = 0;
+			int32_t q0 = 0;
+			float fr0 = 0.0f;
+			if (hi >= lo) {
+				len = (uint32_t)(hi - lo + 1);
+				const SmallRec &rec = wrec[j];
+				const int64_t num0 = rec.K - rec.NU * lo - rec.NV * v;
+				q0 = (int32_t)floor_div_window(num0, rec.D, -2, (1 << sp.level) + 2);
+				fr0 = ratio_f(num0 - (int64_t)q0 * rec.D, rec.D);
+			}
+			lq_of[r] = (uint32_t)(uint16_t)(int16_t)lo | ((uint32_t)q0 << 16);
+			fr0_of[r] = fr0;
+			cum[r + 1] = (uint16_t)len; // the row's length, scanned below
 		}
 		__syncwarp();
 		// row starts: an exclusive scan of the lengths over the rows (at most 32 x kSmallArea fragments)
@@ -574,40 +618,59 @@ __global__ void __launch_bounds__(kEmitTPB) vox_emit(VoxBatch vb, uint32_t n, Vo
 		if (lane == 0) cum[total_rows] = (uint16_t)carry;
 		__syncwarp();
 		// a lane's fragments must be exactly its count (they are: the count pass walked the same spans)
-		const bool ok = !rows || (uint32_t)(cum[rincl] - cum[rincl - rows]) == cnt;
+		const uint32_t rfirst = rincl - rows, tstart = cum[rfirst], tend = cum[rincl];
+		const bool ok = !rows || tend - tstart == cnt;
 		if (__any_sync(kFullMask, !ok)) continue; // cannot happen; the group is left unwritten
-		// the group's fragments, lane-interleaved: fragment f -> its lane (triangle) -> its row
-		uint32_t jt = 0;
+		s_rec[threadIdx.x].tend = tend; // also for a lane without rows: its triangle is passed over
+		if (rows) {
+			s_rec[threadIdx.x].rl |= rfirst;
+			s_rec[threadIdx.x].out -= tstart;
+			s_rec[threadIdx.x].vadj -= (int32_t)rfirst;
+		}
+		__syncwarp();
+		// the group's fragments, lane-interleaved: fragment f -> its triangle jt -> its row r
+		uint32_t jt = 0xffffffffu, fend = 0, r = 0, zr = 0, rgbf = 0, rl = 0;
+		float fb = 0.0f;
+		uint64_t out = 0;
+		int32_t vadj = 0;
 		for (uint32_t f = lane; f < carry; f += 32) {
-			while (cum[s_incl[wb + jt]] <= f) ++jt; // cum at the first row after lane jt's rows
-			const uint32_t r_first = jt ? s_incl[wb + jt - 1] : 0u;
-			uint32_t r = r_first;
+			if (f >= fend) { // the next triangle holding f (triangles without fragments are passed over)
+				do {
+					++jt;
+					fend = wrec[jt].tend;
+				} while (fend <= f);
+				const uint4 g0 = wrec4[4 * jt], g1 = wrec4[4 * jt + 1];
+				fb = __uint_as_float(g0.x), zr = g0.y, rgbf = g0.z, rl = g0.w;
+				out = (uint64_t)g1.x | ((uint64_t)g1.y << 32);
+				vadj = (int32_t)g1.z;
+				r = rl & 0xffffu;
+			}
 			while (cum[r + 1] <= f) ++r; // the row holding fragment f (empty rows are skipped)
-			const SmallRec &rec = s_rec[wb + jt];
-			TriSetup S;
-			S.K = rec.K, S.NU = rec.NU, S.NV = rec.NV, S.D = rec.D;
-			S.z0 = rec.z0, S.z1 = rec.z1, S.level = rec.level, S.axis = (int32_t)rec.axis,
-			S.cols = (int32_t)rec.cols, S.rgb = rec.rgb;
-			const int32_t u = (int32_t)lo_of[r] + (int32_t)(f - cum[r]), v = rec.v0 + (int32_t)(r - r_first);
-			frags[rec.off + (f - cum[r_first])] = make_fragment(S, u, v);
+			const uint32_t k = f - cum[r], lq = lq_of[r];
+			const int32_t lo = (int32_t)(int16_t)(lq & 0xffffu), v = (int32_t)r + vadj;
+			const float tf = fmaf(-(float)k, fb, fr0_of[r]);
+			const float fl = floorf(tf);
+			const float fr = tf - fl;
+			int32_t z;
+			if (fr >= kDepthEps && fr <= 1.0f - kDepthEps) {
+				z = ((int32_t)lq >> 16) + (int32_t)fl;
+			} else {
+				const SmallRec &rec = wrec[jt];
+				const int64_t num = rec.K - rec.NU * (lo + (int32_t)k) - rec.NV * v;
+				z = (int32_t)floor_div_window(num, rec.D, -2, (1 << (rl >> 16)) + 2);
+			}
+			const int32_t z0 = (int32_t)(zr & 0xffffu), z1 = (int32_t)(zr >> 16);
+			const uint32_t zz = (uint32_t)(z < z0 ? z0 : (z > z1 ? z1 : z));
+			frags[out + f] = pack_fragment((rgbf >> 24) & 3u, (rgbf >> 26) & 1u, rgbf, (uint32_t)(lo + (int32_t)k),
+			                               (uint32_t)v, zz);
 		}
 		__syncwarp();
 	}
 }
 
-// Float value of num / den (den > 0, |num| <= den here) from the top 31 bits of both: 32-bit
-// conversions only; relative error a few 2^-24.
-SVO_DEV float ratio_f(int64_t num, int64_t den) {
-	const uint64_t mag = (uint64_t)(num < 0 ? -num : num) | (uint64_t)den;
-	const int sh = max(0, 33 - __clzll((long long)mag));
-	return (float)(int32_t)(num >> sh) / (float)(int32_t)(den >> sh);
-}
-
 // One unit, prepared by the lane that owns it for the lanes that write its fragments.  Fragment k of
-// the unit is pixel u = lo + k of span v with plane depth q0 + (r0 - k NU) / D, r0 = num0 - q0 D in
-// [0, D); t = fr0 - k fb approximates (r0 - k NU) / D within 1e-4 (fr0, fb: the two ratios in float),
-// so floor(t) is exact unless t lies within kDepthEps of an integer, where the exact int64 division
-// decides.  The fragment words are base | u and z placed in their packed fields.
+// the unit is pixel u = lo + k of span v, its depth in the row form above (q0, fr0, fb at the unit's
+// first covered pixel).  The fragment words are base | u and z placed in their packed fields.
 // The fields a lane reloads when it moves to another unit come first, as four 16-byte groups.
 struct __align__(16) UnitRec {
 	float fr0, fb;
@@ -620,9 +683,6 @@ struct __align__(16) UnitRec {
 	int64_t num0, nu, d;       // the exact division near integers
 	uint64_t pad;
 };
-constexpr float kDepthEps = 1.0f / 1024.0f;
-
-SVO_DEV uint32_t field_of(int axis, int which) { return (uint32_t)((axis + which) % 3); } // 0 i, 1 j, 2 depth
 
 // Emission of large-triangle units, 32 consecutive units per warp.  Their fragments are contiguous in
 // the output, so the warp writes them together: lane k takes fragments k, k+32, ... of the group (each
