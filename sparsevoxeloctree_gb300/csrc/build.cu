@@ -17,11 +17,12 @@
 //           8-bit groups, one single-pass look-back scan of popcounts over all depths gives every grank,
 //           and one pass writes all interior words of depths 1..D;
 //   buckets the same sweep counts fragments per bucket (16^3 voxels while the leaf parents are dense,
-//           L - 1 <= D; 32^3 voxels otherwise); a look-back scan and one scatter copy the fragments into bucket
-//           order (8 B each: a leaf item, slot << 32 | rgb, when the leaf parents are dense, else the
-//           fragment), which every later sweep reads;
+//           L - 1 <= D; 32^3 voxels otherwise); a look-back scan and one scatter copy the fragments into
+//           bucket order (8 B each: a leaf item, slot << 32 | rgb, when the leaf parents are dense, else
+//           the fragment), which every later sweep reads;
 //   sparse  depths D+1..L-1 (only when L > 10): the reference's tag / prefix-sum alloc per level with a
-//           per-fragment cached node index (4 B per fragment), so tag reads one parent word;
+//           per-fragment cached node index (4 B per fragment), so tag reads one parent word; after the
+//           last depth, the pass that measures each bucket's leaf span turns its fragments into leaf items;
 //   leaf    one block per leaf window (4096 consecutive words of the leaf range) at a time: the window's
 //           items come from the run of buckets whose leaf spans meet it (each item is read at most
 //           twice), the block accumulates their colours in shared memory (r, g, b, n in 16-bit fields,
@@ -672,7 +673,9 @@ __global__ void __launch_bounds__(kTPB) build_alloc(uint32_t *__restrict__ pool,
 // places every mesh's bucketed copy after the previous mesh's.
 // Bucket edge: 16 voxels while the leaf parents are dense (level <= D + 1): a bucket then spans at most
 // one leaf window's worth of leaf words (8^3 parents x 8), which the windowed leaf stage relies on; 32
-// voxels when they are sparse, where 16-voxel buckets would need 8^8 bucket counters at level 12.
+// voxels when they are sparse, where 16-voxel buckets would need 8^8 bucket counters at level 12.  (A
+// 32-voxel bucket may meet more windows, each reading all its items; 16-voxel buckets at level 12 made
+// the leaf stage 3% faster and the bucket scan, scatter and span passes 0.4 ms slower on a 2^12 scene.)
 uint32_t bucket_shift(uint32_t level, uint32_t D) { return std::min<uint32_t>(level, level <= D + 1 ? 4u : 5u); }
 
 // Leaf windows a dense-parent mesh can need: its leaf range is at most 8 words per possible parent.
@@ -844,12 +847,12 @@ SVO_DEV uint32_t leaf_slot(uint64_t frag, uint64_t f, const uint32_t *__restrict
 constexpr uint32_t kLeafSlots = 4096;         // packed accumulators in shared memory (8 B each)
 constexpr uint32_t kWideSlots = kLeafSlots / 4; // exact accumulators (4 x 8 B each) of the overflow path
 
-// Leaf windows.  A mesh whose leaf parents are dense (level <= 10) has its leaf stage cut into windows of
-// kLeafSlots words of its leaf range; window k is built by one block from the buckets whose leaf spans
-// meet it.  Consecutive non-empty buckets of a mesh have adjacent spans (breadth-first order is Morton
-// order), so those buckets are one run of the bucket list and their items one range of the bucketed
-// copy; a 16^3-voxel bucket spans at most 512 parents = kLeafSlots words, so it meets at most two
-// windows and every item is read at most twice.
+// Leaf windows.  A mesh has its leaf stage cut into windows of kLeafSlots words of its leaf range;
+// window k is built by one block from the buckets whose leaf spans meet it.  Consecutive non-empty
+// buckets of a mesh have adjacent spans (breadth-first order is Morton order), so those buckets are one
+// run of the bucket list and their items one range of the bucketed copy; a 16^3-voxel bucket spans at
+// most 512 parents = kLeafSlots words, so it meets at most two windows and every item is read at most
+// twice (a 32^3-voxel bucket of a sparse-parent mesh spans at most 4096 parents, eight windows).
 constexpr uint32_t kWinBits = 12;
 static_assert((1u << kWinBits) == kLeafSlots, "a leaf window is one shared-memory accumulator window");
 
@@ -919,9 +922,11 @@ __global__ void bucket_meta(BuildBatch bb, const uint32_t *__restrict__ boff, co
 
 // Leaf span of each bucket of a sparse-parent mesh, one warp per bucket: the least and greatest leaf
 // slot of its fragments (through the node index the last sparse tag cached), widened to whole blocks.
-// A bucket holds all fragments of its parents, so its blocks are exactly those parents' blocks.
+// A bucket holds all fragments of its parents, so its blocks are exactly those parents' blocks.  Each
+// fragment of the bucketed copy is replaced by its leaf item (slot << 32 | rgb), the form the copy of a
+// dense-parent mesh has from the start, so the leaf stage reads no node words.
 template <bool B>
-__global__ void __launch_bounds__(kTPB) bucket_span_sparse(const uint64_t *__restrict__ sorted, BuildBatch bb,
+__global__ void __launch_bounds__(kTPB) bucket_span_sparse(uint64_t *__restrict__ sorted, BuildBatch bb,
                                                            const uint32_t *__restrict__ blist,
                                                            const uint32_t *__restrict__ cache,
                                                            const BuildState *gstate, uint4 *__restrict__ meta) {
@@ -938,8 +943,10 @@ __global__ void __launch_bounds__(kTPB) bucket_span_sparse(const uint64_t *__res
 		const uint32_t leaf_begin = md.state->lv[md.level].begin, leaf_num = md.state->lv[md.level].num;
 		uint32_t lo = 0xffffffffu, hi = 0u;
 		for (uint32_t f = m.x + lane; f < m.y; f += 32) {
-			const uint32_t sl = leaf_slot(__ldcs(sorted + f), f, md.pool, cache, leaf_begin);
+			const uint64_t frag = sorted[f];
+			const uint32_t sl = leaf_slot(frag, f, md.pool, cache, leaf_begin);
 			lo = min(lo, sl), hi = max(hi, sl);
+			sorted[f] = ((uint64_t)sl << 32) | ((frag >> 32) & 0xffffffu);
 		}
 		lo = __reduce_min_sync(kFullMask, lo), hi = __reduce_max_sync(kFullMask, hi);
 		if (lane == 0) {
@@ -1064,16 +1071,15 @@ SVO_DEV uint32_t leaf_window(const uint64_t *__restrict__ sorted, uint32_t f0, u
 	return leaves;
 }
 
-// Leaf stage: one leaf window per block at a time, windows of all meshes taken grid-stride.  For
-// dense-parent meshes the bucketed copy holds (slot << 32 | rgb) items; for sparse-parent meshes it holds
-// fragments, whose slot comes through the node index the last sparse tag cached.
+// Leaf stage: one leaf window per block at a time, windows of all meshes taken grid-stride.  The bucketed
+// copy holds (slot << 32 | rgb) items: from the scatter for dense-parent meshes, from bucket_span_sparse
+// for sparse-parent ones.
 template <bool B>
 __global__ void __launch_bounds__(kTPB) build_leaf_windows(const uint64_t *__restrict__ sorted, BuildBatch bb,
                                                            const uint4 *__restrict__ meta,
                                                            const uint32_t *__restrict__ win_base,
                                                            const uint32_t *__restrict__ wfirst,
-                                                           const uint32_t *__restrict__ wlast,
-                                                           const uint32_t *__restrict__ cache, BuildState *gstate) {
+                                                           const uint32_t *__restrict__ wlast, BuildState *gstate) {
 	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	extern __shared__ unsigned long long s_acc[];
 	__shared__ uint32_t s_over, s_leaves, s_skip;
@@ -1110,18 +1116,9 @@ __global__ void __launch_bounds__(kTPB) build_leaf_windows(const uint64_t *__res
 		}
 		const uint32_t f0 = meta[t0].x, f1 = meta[t1].y;
 		const uint32_t wn = min(kLeafSlots, leaf_num - w0);
-		uint32_t leaves;
-		if (dense_parents(md)) {
-			leaves = leaf_window(
-			    sorted, f0, f1, w0, wn, md.pool + leaf_begin + w0, s_acc, &s_over,
-			    [](uint64_t item, uint32_t) { return (uint32_t)(item >> 32); }, [](uint64_t item) { return (uint32_t)item; });
-		} else {
-			const uint32_t *pool_c = md.pool;
-			leaves = leaf_window(
-			    sorted, f0, f1, w0, wn, md.pool + leaf_begin + w0, s_acc, &s_over,
-			    [&](uint64_t item, uint32_t f) { return leaf_slot(item, f, pool_c, cache, leaf_begin); },
-			    [](uint64_t item) { return (uint32_t)(item >> 32); });
-		}
+		const uint32_t leaves = leaf_window(
+		    sorted, f0, f1, w0, wn, md.pool + leaf_begin + w0, s_acc, &s_over,
+		    [](uint64_t item, uint32_t) { return (uint32_t)(item >> 32); }, [](uint64_t item) { return (uint32_t)item; });
 		const uint32_t wl = warp_sum(leaves);
 		if (lane_id() == 0 && wl) atomicAdd(&s_leaves, wl);
 		__syncthreads();
@@ -1347,7 +1344,7 @@ template <bool B>
 static void launch_leaf_stage(const BuildBatch &bb, uint32_t M, uint32_t tune_level, uint64_t n, uint32_t nb_total,
                               const uint32_t *boff, const uint32_t *blist, const BuildState *gstate, uint4 *bmeta,
                               uint32_t *win_base, uint32_t *wfirst, uint32_t *wlast, bool any_sparse,
-                              const uint64_t *sorted, const uint32_t *cache, cudaStream_t stream) {
+                              uint64_t *sorted, const uint32_t *cache, cudaStream_t stream) {
 	const int sms = device_sm_count();
 	const size_t smem = kLeafSlots * sizeof(unsigned long long); // 32 KB: below the default dynamic limit
 	const uint32_t meta_items = std::max<uint32_t>(nb_total, M);
@@ -1361,7 +1358,7 @@ static void launch_leaf_stage(const BuildBatch &bb, uint32_t M, uint32_t tune_le
 	SVO_LAUNCH("bucket_windows", stream,
 	           ::svo::launch_k(bucket_windows<B>, grid_for(nb_total, kTPB, (uint32_t)sms * 4), kTPB, 0, stream, bb, blist, gstate, bmeta, win_base, wfirst, wlast););
 	SVO_LAUNCH("build_leaf_windows", stream,
-	           ::svo::launch_k(build_leaf_windows<B>, blocks, kTPB, smem, stream, sorted, bb, bmeta, win_base, wfirst, wlast, cache, const_cast<BuildState *>(gstate)););
+	           ::svo::launch_k(build_leaf_windows<B>, blocks, kTPB, smem, stream, sorted, bb, bmeta, win_base, wfirst, wlast, const_cast<BuildState *>(gstate)););
 }
 
 cudaError_t build_launch_interior(const uint64_t *frags, uint32_t count, uint32_t level, uint32_t *pool,
