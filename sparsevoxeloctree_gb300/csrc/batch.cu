@@ -276,7 +276,7 @@ static int batch_build(Batcher &b, const svo_batch_mesh *meshes, uint32_t M, cud
 	p.M = M;
 	p.frags_total = F;
 	p.max_level = 0, p.max_D = 0;
-	uint64_t pool_words = 0, sorted_total = 0, max_scan = 0;
+	uint64_t pool_words = 0, sorted_total = 0, max_scan = 0, max_sparse = 0;
 	uint32_t nb_total = 0, dense_total = 0, items_total = 0;
 	bool any_sparse = false;
 	uint64_t windows = 0;
@@ -323,8 +323,9 @@ static int batch_build(Batcher &b, const svo_batch_mesh *meshes, uint32_t M, cud
 		windows += leaf_window_bound(count, level);
 		if (level > bm.dv.D + 1) {
 			any_sparse = true;
-			max_scan = std::max<uint64_t>(max_scan, std::min<uint64_t>(max_sparse_level_words(count, level, bm.dv.D),
-			                                                          r.capacity));
+			const uint64_t sw = std::min<uint64_t>(max_sparse_level_words(count, level, bm.dv.D), r.capacity);
+			max_scan = std::max<uint64_t>(max_scan, sw);
+			max_sparse = std::max<uint64_t>(max_sparse, sw);
 		}
 	}
 	if (hfb[M] != F) return svo_fail(SVO_ERR_CUDA, "batch voxelize: per-mesh counts do not add up");
@@ -361,6 +362,8 @@ static int batch_build(Batcher &b, const svo_batch_mesh *meshes, uint32_t M, cud
 	const size_t o_wlast = take(windows * 4 + 4);
 	const size_t o_sorted = take(sorted_total * 8 + 32);
 	const size_t o_cache = take(any_sparse ? sorted_total * 4 + 16 : 16);
+	p.tag_words = any_sparse ? tag_bitmap_words(max_sparse) : 4;
+	const size_t o_tagbits = take(p.tag_words * 4);
 	SVO_BCK(b.build_ws.ensure(off), "batch build workspace allocation");
 	char *ws = (char *)b.build_ws.ptr;
 	p.gstate = (BuildState *)(ws + o_gstate);
@@ -380,6 +383,7 @@ static int batch_build(Batcher &b, const svo_batch_mesh *meshes, uint32_t M, cud
 	p.any_sparse = any_sparse;
 	p.sorted = (uint64_t *)(ws + o_sorted);
 	p.cache = (uint32_t *)(ws + o_cache);
+	p.tagbits = (uint32_t *)(ws + o_tagbits);
 	uint32_t *pool = (uint32_t *)b.pool.ptr;
 	for (uint32_t m = 0; m < M; ++m) {
 		BuildMesh &bm = hbm[m];

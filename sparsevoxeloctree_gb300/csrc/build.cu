@@ -40,6 +40,7 @@ namespace svo {
 
 constexpr int kTPB = 256;
 constexpr int kAllocIPT = 32; // words per thread of an alloc tile (large tiles: short look-back distances)
+static_assert(kAllocIPT == 32, "an alloc thread's words are one word of the tag bitmap");
 constexpr int kAllocTile = kTPB * kAllocIPT;
 constexpr int kScanIPT = 8;
 constexpr int kScanTile = kTPB * kScanIPT;
@@ -440,7 +441,7 @@ template <bool B> __global__ void dense_finish(BuildBatch bb) {
 
 // Writes the child blocks of every occupied cell of depths 0 (the root) .. D-1: the interior words of
 // depths 1..D.  The blocks of depth-D cells are the leaf stage's when depth D+1 is the leaf depth, and
-// zero_level's when sparse depths follow.  One bitmap word and one prefix word of the child depth serve
+// the first sparse alloc's when sparse depths follow.  One bitmap word and one prefix word of the child depth serve
 // all 8 children.
 template <bool B>
 __global__ void __launch_bounds__(kTPB) dense_write(BuildBatch bb, uint32_t total_items) {
@@ -490,49 +491,70 @@ __global__ void __launch_bounds__(kTPB) dense_write(BuildBatch bb, uint32_t tota
 	}
 }
 
-// Zeroes the word range of `depth` (the first sparse depth: the init of shader/octree_init_node.comp:7-11
-// for the blocks of the depth-D cells) with 16-byte stores, grid-stride.  The range is 8-word aligned.
-// A range beyond the pool is reported as a capacity overflow and not written.
-__global__ void __launch_bounds__(kTPB) zero_level(uint32_t *__restrict__ pool, uint64_t capacity, BuildState *state,
-                                                   uint32_t depth, const BuildState *gstate) {
+// Clears the tag bitmap of sparse depth `depth`: one bit per word of the depth's range, set by the tag
+// pass for every occupied node.  (The words themselves are written whole by the alloc, so the pool needs
+// no init pass, shader/octree_init_node.comp:7-11.)  A range beyond the pool or the bitmap is reported as
+// a capacity overflow and nothing is cleared.
+__global__ void __launch_bounds__(kTPB) tag_clear(uint32_t *__restrict__ tagbits, uint64_t tag_words,
+                                                  uint64_t capacity, BuildState *state, uint32_t depth,
+                                                  const BuildState *gstate) {
 	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
-	if (gstate->status & kStatusAbort) return; // the level range comes from an incomplete scan
+	if ((state->status & kStatusCapacity) || (gstate->status & kStatusAbort)) return;
 	const LevelInfo li = state->lv[depth];
-	const uint64_t begin = li.begin, end = begin + li.num;
-	if (end > capacity || end > SVO_MAX_POOL_WORDS) {
+	const uint64_t end = (uint64_t)li.begin + li.num, n4 = ((uint64_t)li.num + 127) / 128; // 4 words each
+	if (end > capacity || end > SVO_MAX_POOL_WORDS || 4 * n4 > tag_words) {
 		if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&state->status, kStatusCapacity);
 		return;
 	}
-	uint4 *dst = reinterpret_cast<uint4 *>(pool + begin);
-	const uint64_t n4 = (end - begin) / 4;
+	uint4 *dst = reinterpret_cast<uint4 *>(tagbits);
 	for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (uint64_t)gridDim.x * blockDim.x)
 		dst[i] = make_uint4(0u, 0u, 0u, 0u);
 }
 
 // ------------------------------------------------------------------------------------------ tag (sparse levels)
-// Marks the depth-`depth` node of every fragment (0x80000000), reading its parent through the node index
-// cached by the previous sparse depth (or the dense bitmaps when the parent depth is dense).
-SVO_DEV void tag_one(uint64_t frag, uint32_t &node, uint32_t level, uint32_t depth, bool parent_dense,
-                     const DenseView &dv, uint32_t *__restrict__ pool) {
+// The depth-`depth` node of a fragment, through its parent: the node index cached by the previous sparse
+// depth, or the dense bitmaps when the parent depth is dense.
+SVO_DEV uint32_t tag_node(uint64_t frag, uint32_t node, uint32_t level, uint32_t depth, bool parent_dense,
+                          const DenseView &dv, const uint32_t *__restrict__ pool) {
 	uint32_t x, y, z;
 	frag_xyz(frag, x, y, z);
-	uint32_t idx;
-	if (parent_dense)
-		idx = dense_child_word(dv, x, y, z, level, depth);
-	else
-		idx = (pool[node] & 0x3fffffffu) + octant_at(x, y, z, level - depth);
-	if ((pool[idx] & 0x80000000u) == 0u) pool[idx] = 0x80000000u;
-	node = idx;
+	if (parent_dense) return dense_child_word(dv, x, y, z, level, depth);
+	return (pool[node] & 0x3fffffffu) + octant_at(x, y, z, level - depth);
 }
 
-// One mesh's sparse depth (meshes of a batch with sparse depths run these one mesh at a time).
+// Sets the tag bits of nodes idx[0..3] (words of the depth's range [begin, begin + num)), one atomicOr per
+// run of equal bitmap words.
+SVO_DEV void tag_set(uint32_t *__restrict__ tagbits, uint32_t begin, uint32_t num, const uint32_t idx[4],
+                     BuildState *gstate) {
+	uint32_t word = 0xffffffffu, bits = 0u;
+#pragma unroll
+	for (int k = 0; k < 4; ++k) {
+		const uint32_t rel = idx[k] - begin;
+		if (rel >= num) { // a child of an allocated node lies in the range: cannot happen
+			SVO_CHECK_FAIL(10u, gstate);
+			continue;
+		}
+		if ((rel >> 5) != word) {
+			if (bits) atomicOr(tagbits + word, bits);
+			word = rel >> 5, bits = 0u;
+		}
+		bits |= 1u << (rel & 31u);
+	}
+	if (bits) atomicOr(tagbits + word, bits);
+	(void)gstate;
+}
+
+// Marks the depth-`depth` node of every fragment in the depth's tag bitmap (the tag of
+// shader/octree_tag_node.comp:33-60 for interior nodes) and caches the node index per fragment for the
+// next depth and the leaf stage.
 __global__ void __launch_bounds__(kTPB) build_tag(const uint64_t *__restrict__ frags, uint32_t n, uint32_t level,
-                                                  uint32_t depth, uint32_t *__restrict__ pool,
-                                                  uint32_t *__restrict__ cache, DenseView dv, BuildState *state,
-                                                  const BuildState *gstate) {
+                                                  uint32_t depth, const uint32_t *__restrict__ pool,
+                                                  uint32_t *__restrict__ tagbits, uint32_t *__restrict__ cache,
+                                                  DenseView dv, BuildState *state, BuildState *gstate) {
 	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	if ((state->status & kStatusCapacity) || (gstate->status & kStatusAbort)) return;
 	const bool parent_dense = depth == 1 || depth - 1 <= dv.D;
+	const uint32_t begin = state->lv[depth].begin, num = state->lv[depth].num;
 	const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
 	const uint64_t nq = (n + 3ull) / 4ull;
 	for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += stride) {
@@ -542,27 +564,29 @@ __global__ void __launch_bounds__(kTPB) build_tag(const uint64_t *__restrict__ f
 			const ulonglong2 b = __ldcs(reinterpret_cast<const ulonglong2 *>(frags + f0 + 2));
 			uint4 c = make_uint4(0, 0, 0, 0);
 			if (!parent_dense) c = __ldcs(reinterpret_cast<const uint4 *>(cache + f0));
-			tag_one(a.x, c.x, level, depth, parent_dense, dv, pool);
-			tag_one(a.y, c.y, level, depth, parent_dense, dv, pool);
-			tag_one(b.x, c.z, level, depth, parent_dense, dv, pool);
-			tag_one(b.y, c.w, level, depth, parent_dense, dv, pool);
-			__stcs(reinterpret_cast<uint4 *>(cache + f0), c);
+			const uint32_t idx[4] = {tag_node(a.x, c.x, level, depth, parent_dense, dv, pool),
+			                         tag_node(a.y, c.y, level, depth, parent_dense, dv, pool),
+			                         tag_node(b.x, c.z, level, depth, parent_dense, dv, pool),
+			                         tag_node(b.y, c.w, level, depth, parent_dense, dv, pool)};
+			tag_set(tagbits, begin, num, idx, gstate);
+			__stcs(reinterpret_cast<uint4 *>(cache + f0), make_uint4(idx[0], idx[1], idx[2], idx[3]));
 		} else {
 			for (uint64_t f = f0; f < n; ++f) {
-				uint32_t c = parent_dense ? 0u : cache[f];
-				tag_one(frags[f], c, level, depth, parent_dense, dv, pool);
-				cache[f] = c;
+				const uint32_t node = tag_node(frags[f], parent_dense ? 0u : cache[f], level, depth, parent_dense, dv, pool);
+				const uint32_t idx[4] = {node, node, node, node};
+				tag_set(tagbits, begin, num, idx, gstate);
+				cache[f] = node;
 			}
 		}
 	}
 }
 
-// Prefix-sum allocation of child blocks for the marked words of a sparse depth (persistent grid, tiles
-// claimed in order by ticket so the look-back always waits on a running or finished tile).  The block
-// of a node is zeroed (the next depth's init) unless the next depth is the leaf depth.
+// Prefix-sum allocation of child blocks for the tagged words of a sparse depth (persistent grid, tiles
+// claimed in order by ticket so the look-back always waits on a running or finished tile).  Every word of
+// the depth's range is written: a child pointer for a tagged word, 0 for the others.
 __global__ void __launch_bounds__(kTPB) build_alloc(uint32_t *__restrict__ pool, uint64_t capacity, uint32_t depth,
-                                                    uint32_t level, BuildState *state, unsigned long long *descs,
-                                                    BuildState *gstate) {
+                                                    const uint32_t *__restrict__ tagbits, BuildState *state,
+                                                    unsigned long long *descs, BuildState *gstate) {
 	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	__shared__ uint32_t s_tile;
 	__shared__ uint32_t s_warp[kTPB / 32 + 1];
@@ -575,7 +599,6 @@ __global__ void __launch_bounds__(kTPB) build_alloc(uint32_t *__restrict__ pool,
 	if (s_abort) return;
 	const LevelInfo li = state->lv[depth];
 	const uint32_t ntiles = (li.num + kAllocTile - 1) / kAllocTile;
-	const bool next_is_leaf = depth + 1 == level;
 	const uint32_t next_begin = li.begin + li.num;
 	if (ntiles == 0) {
 		if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -585,8 +608,8 @@ __global__ void __launch_bounds__(kTPB) build_alloc(uint32_t *__restrict__ pool,
 		return;
 	}
 	// pipelined as the voxelize scans: a tile's count is published at once, its look-back and its
-	// pointers follow after the block has counted its next tile.  The words of a sparse depth are 0 or
-	// the tag 0x80000000 until they are allocated, so a tile is kept as a mask of its tagged words.
+	// pointers follow after the block has counted its next tile.  A thread's kAllocIPT = 32 words are
+	// one word of the tag bitmap.
 	uint32_t p_tile = 0xffffffffu, p_mask = 0, p_rank0 = 0, p_total = 0;
 	for (;;) {
 		if (threadIdx.x == 0) s_tile = atomicAdd(&state->tiles[depth], 1u);
@@ -596,19 +619,7 @@ __global__ void __launch_bounds__(kTPB) build_alloc(uint32_t *__restrict__ pool,
 		uint32_t mask = 0, rank0 = 0, total = 0;
 		if (tile < ntiles) {
 			const uint32_t w0 = tile * kAllocTile + threadIdx.x * kAllocIPT; // offset inside the level
-			if (w0 + kAllocIPT <= li.num) {
-				const uint4 *src = reinterpret_cast<const uint4 *>(pool + li.begin + w0);
-#pragma unroll
-				for (int k = 0; k < kAllocIPT / 4; ++k) {
-					const uint4 x = src[k];
-					mask |= ((x.x >> 31) << (4 * k)) | ((x.y >> 31) << (4 * k + 1)) | ((x.z >> 31) << (4 * k + 2)) |
-					        ((x.w >> 31) << (4 * k + 3));
-				}
-			} else {
-#pragma unroll
-				for (int k = 0; k < kAllocIPT; ++k)
-					if (w0 + k < li.num) mask |= (pool[li.begin + w0 + k] >> 31) << k;
-			}
+			if (w0 < li.num) mask = tagbits[w0 / kAllocIPT]; // bits past the range are clear
 			rank0 = block_exclusive_sum<uint32_t, kTPB>((uint32_t)__popc(mask), s_warp, total);
 			if (threadIdx.x == 0) tile_publish_aggregate(descs, tile, depth, total);
 		}
@@ -635,11 +646,6 @@ __global__ void __launch_bounds__(kTPB) build_alloc(uint32_t *__restrict__ pool,
 					continue;
 				}
 				w[k] = (uint32_t)ptr | 0x80000000u;
-				if (!next_is_leaf) { // the next depth's init; leaf blocks are written whole by the leaf stage
-					uint4 *child = reinterpret_cast<uint4 *>(pool + ptr);
-					child[0] = make_uint4(0, 0, 0, 0);
-					child[1] = make_uint4(0, 0, 0, 0);
-				}
 			}
 			if (w0 + kAllocIPT <= li.num) {
 				uint4 *dst = reinterpret_cast<uint4 *>(pool + li.begin + w0);
@@ -1204,10 +1210,13 @@ uint64_t max_sparse_level_words(uint32_t count, uint32_t level, uint32_t D) {
 	return best;
 }
 
+// Words of a tag bitmap for a sparse depth of up to `level_words` words (whole 16-byte groups).
+uint64_t tag_bitmap_words(uint64_t level_words) { return (level_words + 127) / 128 * 4 + 4; }
+
 // Layout: state | dense-scan descriptors | dense bitmaps | dense prefix | bucket counts, offsets,
 // cursors, list and scan descriptors | bucketed fragment copy (8 B per fragment) | node cache (4 B per
-// fragment, sparse levels only).  The leaf stage needs nothing more: its accumulators live in shared
-// memory.
+// fragment) and tag bitmap (1 bit per word of the largest sparse depth), sparse levels only.  The leaf
+// stage needs nothing more: its accumulators live in shared memory.
 void build_workspace_layout(void *ws, uint32_t count, uint32_t level, uint64_t capacity, BuildWorkspace &w) {
 	char *p = (char *)ws;
 	size_t off = 0;
@@ -1243,6 +1252,8 @@ void build_workspace_layout(void *ws, uint32_t count, uint32_t level, uint64_t c
 	w.wlast = (uint32_t *)take(wins * 4 + 4);
 	w.sorted = (uint64_t *)take((size_t)count * 8 + 32);
 	w.cache = (uint32_t *)take(level > D + 1 ? (size_t)count * 4 + 16 : 16);
+	w.tag_words = level > D + 1 ? tag_bitmap_words(sparse_words) : 4;
+	w.tagbits = (uint32_t *)take(w.tag_words * 4);
 	w.total_bytes = off;
 }
 
@@ -1324,19 +1335,18 @@ static void launch_dense_and_scatter(const uint64_t *frags, uint64_t n, uint32_t
 }
 
 static void launch_sparse(const uint64_t *sorted, uint32_t count, uint32_t level, const DenseView &dv, uint32_t *pool,
-                          uint64_t capacity, uint32_t *cache, BuildState *state, unsigned long long *descs,
-                          BuildState *gstate, cudaStream_t stream) {
+                          uint64_t capacity, uint32_t *cache, uint32_t *tagbits, uint64_t tag_words, BuildState *state,
+                          unsigned long long *descs, BuildState *gstate, cudaStream_t stream) {
 	const int sms = device_sm_count();
 	const uint32_t tag_blocks =
 	    grid_for(((uint64_t)count + 3) / 4, kTPB, (uint32_t)sms * (uint32_t)tune_value(kTuneSweepBlocks, level, count));
-	// the first sparse depth's words start at zero (later depths' blocks are zeroed by the alloc before)
-	SVO_LAUNCH("zero_level", stream,
-	           ::svo::launch_k(zero_level, (uint32_t)sms * 8, kTPB, 0, stream, pool, capacity, state, dv.D + 1, gstate););
 	for (uint32_t depth = dv.D + 1; depth < level; ++depth) {
+		SVO_LAUNCH("tag_clear", stream,
+		           ::svo::launch_k(tag_clear, (uint32_t)sms * 4, kTPB, 0, stream, tagbits, tag_words, capacity, state, depth, gstate););
 		SVO_LAUNCH("build_tag", stream,
-		           ::svo::launch_k(build_tag, tag_blocks, kTPB, 0, stream, sorted, count, level, depth, pool, cache, dv, state, gstate););
+		           ::svo::launch_k(build_tag, tag_blocks, kTPB, 0, stream, sorted, count, level, depth, pool, tagbits, cache, dv, state, gstate););
 		SVO_LAUNCH("build_alloc", stream,
-		           ::svo::launch_k(build_alloc, (uint32_t)sms * 4, kTPB, 0, stream, pool, capacity, depth, level, state, descs, gstate););
+		           ::svo::launch_k(build_alloc, (uint32_t)sms * 4, kTPB, 0, stream, pool, capacity, depth, tagbits, state, descs, gstate););
 	}
 }
 
@@ -1374,7 +1384,8 @@ cudaError_t build_launch_interior(const uint64_t *frags, uint32_t count, uint32_
 	launch_dense_and_scatter<false>(frags, count, level, bb, 1, w.dv.D, w.dense_words, items, w.nb, w.state, w.descs, w.bcount,
 	                                w.boff, w.bfill, w.blist, w.bdescs, w.sorted, stream);
 	if (level > w.dv.D + 1)
-		launch_sparse(w.sorted, count, level, w.dv, pool, capacity, w.cache, w.state, w.descs, w.state, stream);
+		launch_sparse(w.sorted, count, level, w.dv, pool, capacity, w.cache, w.tagbits, w.tag_words, w.state, w.descs,
+		              w.state, stream);
 	return cudaGetLastError();
 }
 
@@ -1413,8 +1424,8 @@ cudaError_t build_launch_batch(const uint64_t *frags, const BuildBatchPlan &p, v
 		e = cudaMemsetAsync(p.descs, 0, p.desc_count * sizeof(unsigned long long), stream);
 		if (e != cudaSuccess) return e;
 		const uint64_t sb = md.frag_base + md.sorted_pad;
-		launch_sparse(p.sorted + sb, md.count, md.level, md.dv, md.pool, md.capacity, p.cache + sb, md.state, p.descs,
-		              p.gstate, stream);
+		launch_sparse(p.sorted + sb, md.count, md.level, md.dv, md.pool, md.capacity, p.cache + sb, p.tagbits, p.tag_words,
+		              md.state, p.descs, p.gstate, stream);
 	}
 	launch_leaf_stage<true>(p.bb, p.M, p.max_level, p.frags_total, p.nb_total, p.boff, p.blist, p.gstate, p.bmeta,
 	                        p.win_base, p.wfirst, p.wlast, p.any_sparse, p.sorted, p.cache, stream);

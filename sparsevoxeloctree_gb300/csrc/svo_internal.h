@@ -286,6 +286,8 @@ struct BuildWorkspace {
 	uint32_t *wfirst, *wlast;       // [leaf_window_bound] first and last listed bucket of each leaf window
 	uint64_t *sorted;               // [count] the fragments, bucketed
 	uint32_t *cache;                // [count] node index of the previous sparse depth, per sorted fragment
+	uint32_t *tagbits;              // [tag_words] tag bit per word of the sparse depth being built
+	uint64_t tag_words;
 	size_t total_bytes;
 };
 uint64_t build_pool_bound(uint32_t count, uint32_t level);
@@ -299,6 +301,7 @@ uint32_t dense_layout(uint32_t D, uint32_t off[kDenseMaxDepth + 2]);
 // dense_write items of a mesh (parent words of the depths whose child blocks it writes, plus the root).
 uint32_t dense_items(uint32_t level, uint32_t D, const uint32_t off[kDenseMaxDepth + 2]);
 uint64_t max_sparse_level_words(uint32_t count, uint32_t level, uint32_t D);
+uint64_t tag_bitmap_words(uint64_t level_words); // words of a sparse depth's tag bitmap
 void build_workspace_layout(void *ws, uint32_t count, uint32_t level, uint64_t capacity, BuildWorkspace &w);
 // Interior levels (dense bitmaps, then sparse tag/alloc); the leaf range ends up in state->lv[level].
 cudaError_t build_launch_interior(const uint64_t *frags, uint32_t count, uint32_t level, uint32_t *pool,
@@ -331,6 +334,8 @@ struct BuildBatchPlan {
 	uint32_t *dense_prefix;
 	uint64_t *sorted;
 	uint32_t *cache;                // only when a mesh has sparse levels (level > 10)
+	uint32_t *tagbits;              // tag bitmap of the sparse depth being built (one mesh at a time)
+	uint64_t tag_words;
 	uint32_t *win_base;             // [M+1] leaf windows before each mesh (leaf_window_scan)
 	uint32_t *wfirst, *wlast;       // [sum of leaf_window_bound] first and last listed bucket per window
 	bool any_sparse;                // a mesh's leaf parents are sparse (level > 10)
