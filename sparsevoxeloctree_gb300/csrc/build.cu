@@ -841,15 +841,6 @@ SVO_DEV uint32_t leaf_word(uint32_t n, uint32_t sr, uint32_t sg, uint32_t sb) {
 	return 0xC0000000u | (min(n, 63u) << 24) | (b << 16) | (g << 8) | r;
 }
 
-// Leaf word slot (index from the start of the leaf range) of fragment f of the bucketed copy, for a
-// mesh whose leaf parents are sparse: through the node index cached per fragment by the last sparse tag.
-SVO_DEV uint32_t leaf_slot(uint64_t frag, uint64_t f, const uint32_t *__restrict__ pool,
-                           const uint32_t *__restrict__ cache, uint32_t leaf_begin) {
-	uint32_t x, y, z;
-	frag_xyz(frag, x, y, z);
-	return (__ldg(pool + __ldg(cache + f)) & 0x3fffffffu) + octant_at(x, y, z, 0) - leaf_begin;
-}
-
 constexpr uint32_t kLeafSlots = 4096;         // packed accumulators in shared memory (8 B each)
 constexpr uint32_t kWideSlots = kLeafSlots / 4; // exact accumulators (4 x 8 B each) of the overflow path
 
@@ -948,11 +939,28 @@ __global__ void __launch_bounds__(kTPB) bucket_span_sparse(uint64_t *__restrict_
 		const uint4 m = meta[t];
 		const uint32_t leaf_begin = md.state->lv[md.level].begin, leaf_num = md.state->lv[md.level].num;
 		uint32_t lo = 0xffffffffu, hi = 0u;
-		for (uint32_t f = m.x + lane; f < m.y; f += 32) {
-			const uint64_t frag = sorted[f];
-			const uint32_t sl = leaf_slot(frag, f, md.pool, cache, leaf_begin);
-			lo = min(lo, sl), hi = max(hi, sl);
-			sorted[f] = ((uint64_t)sl << 32) | ((frag >> 32) & 0xffffffu);
+		// four fragments per lane and pass, their loads issued together (a fragment's slot is a chain of
+		// two dependent loads)
+		for (uint32_t f = m.x + lane; f < m.y; f += 4 * 32) {
+			uint64_t frag[4];
+			uint32_t node[4];
+#pragma unroll
+			for (uint32_t k = 0; k < 4; ++k) {
+				const uint32_t g = f + 32 * k;
+				frag[k] = g < m.y ? sorted[g] : 0ull;
+				node[k] = g < m.y ? __ldg(cache + g) : 0u;
+			}
+#pragma unroll
+			for (uint32_t k = 0; k < 4; ++k) {
+				const uint32_t g = f + 32 * k;
+				if (g < m.y) {
+					uint32_t x, y, z;
+					frag_xyz(frag[k], x, y, z);
+					const uint32_t sl = (__ldg(md.pool + node[k]) & 0x3fffffffu) + octant_at(x, y, z, 0) - leaf_begin;
+					lo = min(lo, sl), hi = max(hi, sl);
+					sorted[g] = ((uint64_t)sl << 32) | ((frag[k] >> 32) & 0xffffffu);
+				}
+			}
 		}
 		lo = __reduce_min_sync(kFullMask, lo), hi = __reduce_max_sync(kFullMask, hi);
 		if (lane == 0) {
