@@ -503,10 +503,10 @@ struct __align__(16) SmallRec {
 	float fb;             // NU / D
 	uint32_t zr;          // z0 | z1 << 16: the depth range
 	uint32_t rgbf;        // rgb | axis << 24 | cols << 26
-	uint32_t rl;          // the triangle's first pooled row | level << 16
+	uint32_t rl;          // level << 16
 	uint64_t out;         // output position of its first fragment, minus that fragment's index in the group
 	int32_t vadj;         // pooled row r is span v = r + vadj
-	uint32_t tend;        // one past its last fragment in the group
+	uint32_t spare;
 	int64_t K, NU, NV, D; // plane depth (K - NU u - NV v) / D at the centre of pixel (u, v), D > 0
 };
 static_assert(sizeof(SmallRec) == 64, "four 16-byte groups");
@@ -516,6 +516,7 @@ static_assert(sizeof(SmallRec) == 64, "four 16-byte groups");
 // spans, and the pool holds every span of the warp.
 constexpr uint32_t kMaxSmallSpans = 16;
 constexpr uint32_t kRowPool = 32 * kMaxSmallSpans;
+constexpr uint32_t kFragChunk = 256; // fragments per pass of the fragment loop: 8 map entries per lane
 static_assert(kMaxSmallSpans * kMaxSmallSpans >= (uint32_t)kSmallArea && (kMaxSmallSpans - 1) * (kMaxSmallSpans - 1) < (uint32_t)kSmallArea,
               "kMaxSmallSpans is the integer square root of kSmallArea");
 
@@ -531,12 +532,16 @@ SVO_DEV uint64_t pack_fragment(uint32_t axis, uint32_t cols, uint32_t rgb, uint3
 	return (uint64_t)fx | ((uint64_t)fy << 32);
 }
 
+static_assert(2 * kFragChunk + kRowPool <= 32 * sizeof(SpanSetup), "a warp's fragment map and row triangles fit its span set-ups");
+
 template <bool B>
 __global__ void __launch_bounds__(kEmitTPB) vox_emit(VoxBatch vb, uint32_t n, VoxWorkspace w,
                                                      uint64_t *__restrict__ frags, uint64_t capacity) {
 	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	__shared__ SmallRec s_rec[kEmitTPB];
-	__shared__ SpanSetup s_sp[kEmitTPB];
+	// the lanes' span set-ups; once the spans are evaluated, a warp's slice holds its fragment-to-row map
+	// (kFragChunk entries) and the triangle of each pooled row
+	__shared__ __align__(16) unsigned char s_span_raw[kEmitTPB * sizeof(SpanSetup)];
 	__shared__ uint32_t s_incl[kEmitTPB];                   // span rows of lanes 0..j, inclusive
 	__shared__ uint32_t s_lq[kEmitTPB / 32][kRowPool];       // per pooled row: first pixel lo | q0 << 16 (int16 each)
 	__shared__ float s_fr0[kEmitTPB / 32][kRowPool];         // per pooled row: fr0
@@ -547,6 +552,9 @@ __global__ void __launch_bounds__(kEmitTPB) vox_emit(VoxBatch vb, uint32_t n, Vo
 	uint16_t *cum = s_rcum[wi];
 	SmallRec *wrec = s_rec + wb;
 	const uint4 *wrec4 = reinterpret_cast<const uint4 *>(wrec);
+	SpanSetup *s_sp = reinterpret_cast<SpanSetup *>(s_span_raw);
+	uint16_t *fmap = reinterpret_cast<uint16_t *>(s_span_raw + wb * sizeof(SpanSetup));
+	uint8_t *rtri = reinterpret_cast<uint8_t *>(fmap + kFragChunk);
 	const uint64_t warps = (uint64_t)gridDim.x * blockDim.x / 32;
 	for (uint64_t g = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32; g * 32 < n; g += warps) {
 		const uint64_t t = g * 32 + lane;
@@ -568,7 +576,7 @@ __global__ void __launch_bounds__(kEmitTPB) vox_emit(VoxBatch vb, uint32_t n, Vo
 					r.fb = ratio_f(S.NU, S.D);
 					r.zr = (uint32_t)S.z0 | ((uint32_t)S.z1 << 16);
 					r.rgbf = (S.rgb & 0xffffffu) | ((uint32_t)S.axis << 24) | ((uint32_t)S.cols << 26);
-					r.rl = (uint32_t)S.level << 16; // | first row, below
+					r.rl = (uint32_t)S.level << 16;
 					r.out = off;                    // - first fragment, below
 					r.vadj = S.v0;                  // - first row, below
 					r.K = S.K, r.NU = S.NU, r.NV = S.NV, r.D = S.D;
@@ -621,50 +629,77 @@ __global__ void __launch_bounds__(kEmitTPB) vox_emit(VoxBatch vb, uint32_t n, Vo
 		const uint32_t rfirst = rincl - rows, tstart = cum[rfirst], tend = cum[rincl];
 		const bool ok = !rows || tend - tstart == cnt;
 		if (__any_sync(kFullMask, !ok)) continue; // cannot happen; the group is left unwritten
-		s_rec[threadIdx.x].tend = tend; // also for a lane without rows: its triangle is passed over
 		if (rows) {
-			s_rec[threadIdx.x].rl |= rfirst;
 			s_rec[threadIdx.x].out -= tstart;
 			s_rec[threadIdx.x].vadj -= (int32_t)rfirst;
 		}
 		__syncwarp();
-		// the group's fragments, lane-interleaved: fragment f -> its triangle jt -> its row r
-		uint32_t jt = 0xffffffffu, fend = 0, r = 0, zr = 0, rgbf = 0, rl = 0;
-		float fb = 0.0f;
-		uint64_t out = 0;
-		int32_t vadj = 0;
-		for (uint32_t f = lane; f < carry; f += 32) {
-			if (f >= fend) { // the next triangle holding f (triangles without fragments are passed over)
-				do {
-					++jt;
-					fend = wrec[jt].tend;
-				} while (fend <= f);
-				const uint4 g0 = wrec4[4 * jt], g1 = wrec4[4 * jt + 1];
-				fb = __uint_as_float(g0.x), zr = g0.y, rgbf = g0.z, rl = g0.w;
-				out = (uint64_t)g1.x | ((uint64_t)g1.y << 32);
-				vadj = (int32_t)g1.z;
-				r = rl & 0xffffu;
-			}
-			while (cum[r + 1] <= f) ++r; // the row holding fragment f (empty rows are skipped)
-			const uint32_t k = f - cum[r], lq = lq_of[r];
-			const int32_t lo = (int32_t)(int16_t)(lq & 0xffffu), v = (int32_t)r + vadj;
-			const float tf = fmaf(-(float)k, fb, fr0_of[r]);
-			const float fl = floorf(tf);
-			const float fr = tf - fl;
-			int32_t z;
-			if (fr >= kDepthEps && fr <= 1.0f - kDepthEps) {
-				z = ((int32_t)lq >> 16) + (int32_t)fl;
-			} else {
-				const SmallRec &rec = wrec[jt];
-				const int64_t num = rec.K - rec.NU * (lo + (int32_t)k) - rec.NV * v;
-				z = (int32_t)floor_div_window(num, rec.D, -2, (1 << (rl >> 16)) + 2);
-			}
-			const int32_t z0 = (int32_t)(zr & 0xffffu), z1 = (int32_t)(zr >> 16);
-			const uint32_t zz = (uint32_t)(z < z0 ? z0 : (z > z1 ? z1 : z));
-			frags[out + f] = pack_fragment((rgbf >> 24) & 3u, (rgbf >> 26) & 1u, rgbf, (uint32_t)(lo + (int32_t)k),
-			                               (uint32_t)v, zz);
+		// the triangle of each pooled row (the span set-ups are no longer read)
+		for (uint32_t r = lane, jr = 0; r < total_rows; r += 32) {
+			while (s_incl[wb + jr] <= r) ++jr;
+			rtri[r] = (uint8_t)jr;
 		}
-		__syncwarp();
+		// the group's fragments, kFragChunk at a time: each non-empty row marks its first fragment in the
+		// chunk's map, a max scan over the map gives every fragment its row, and lane k takes fragments
+		// k, k+32, ... of the chunk
+		uint32_t row_carry = 0; // 1 + the last non-empty row starting before the chunk
+		for (uint32_t c0 = 0; c0 < carry; c0 += kFragChunk) {
+			reinterpret_cast<uint4 *>(fmap)[lane] = make_uint4(0u, 0u, 0u, 0u);
+			__syncwarp();
+			for (uint32_t r = lane; r < total_rows; r += 32) {
+				const uint32_t st = cum[r];
+				if (st >= c0 && st < c0 + kFragChunk && cum[r + 1] > st) fmap[st - c0] = (uint16_t)(r + 1);
+			}
+			__syncwarp();
+			{ // inclusive max scan of the map: lane l holds entries 8l .. 8l+7
+				const uint4 e = reinterpret_cast<const uint4 *>(fmap)[lane];
+				uint32_t m8[8] = {e.x & 0xffffu, e.x >> 16, e.y & 0xffffu, e.y >> 16,
+				                  e.z & 0xffffu, e.z >> 16, e.w & 0xffffu, e.w >> 16};
+#pragma unroll
+				for (int i = 1; i < 8; ++i) m8[i] = max(m8[i], m8[i - 1]);
+				uint32_t m = m8[7];
+#pragma unroll
+				for (uint32_t d = 1; d < 32; d <<= 1) {
+					const uint32_t o = __shfl_up_sync(kFullMask, m, d);
+					if (lane >= d) m = max(m, o);
+				}
+				uint32_t before = __shfl_up_sync(kFullMask, m, 1);
+				before = max(lane ? before : 0u, row_carry);
+#pragma unroll
+				for (int i = 0; i < 8; ++i) m8[i] = max(m8[i], before);
+				reinterpret_cast<uint4 *>(fmap)[lane] = make_uint4(m8[0] | (m8[1] << 16), m8[2] | (m8[3] << 16),
+				                                                   m8[4] | (m8[5] << 16), m8[6] | (m8[7] << 16));
+				row_carry = max(row_carry, __shfl_sync(kFullMask, m, 31));
+			}
+			__syncwarp();
+			const uint32_t cn = min((uint32_t)kFragChunk, carry - c0);
+			for (uint32_t i = lane; i < cn; i += 32) {
+				const uint32_t f = c0 + i, r = fmap[i] - 1u, jt = rtri[r];
+				const uint4 g0 = wrec4[4 * jt], g1 = wrec4[4 * jt + 1];
+				const float fb = __uint_as_float(g0.x);
+				const uint32_t zr = g0.y, rgbf = g0.z, rl = g0.w;
+				const uint64_t out = (uint64_t)g1.x | ((uint64_t)g1.y << 32);
+				const int32_t vadj = (int32_t)g1.z;
+				const uint32_t k = f - cum[r], lq = lq_of[r];
+				const int32_t lo = (int32_t)(int16_t)(lq & 0xffffu), v = (int32_t)r + vadj;
+				const float tf = fmaf(-(float)k, fb, fr0_of[r]);
+				const float fl = floorf(tf);
+				const float fr = tf - fl;
+				int32_t z;
+				if (fr >= kDepthEps && fr <= 1.0f - kDepthEps) {
+					z = ((int32_t)lq >> 16) + (int32_t)fl;
+				} else {
+					const SmallRec &rec = wrec[jt];
+					const int64_t num = rec.K - rec.NU * (lo + (int32_t)k) - rec.NV * v;
+					z = (int32_t)floor_div_window(num, rec.D, -2, (1 << (rl >> 16)) + 2);
+				}
+				const int32_t z0 = (int32_t)(zr & 0xffffu), z1 = (int32_t)(zr >> 16);
+				const uint32_t zz = (uint32_t)(z < z0 ? z0 : (z > z1 ? z1 : z));
+				frags[out + f] = pack_fragment((rgbf >> 24) & 3u, (rgbf >> 26) & 1u, rgbf, (uint32_t)(lo + (int32_t)k),
+				                               (uint32_t)v, zz);
+			}
+			__syncwarp();
+		}
 	}
 }
 
