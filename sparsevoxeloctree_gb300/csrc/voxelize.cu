@@ -11,10 +11,10 @@
 //
 // GB300 design.  Coverage is computed per span (a row or column of the AABB, whichever makes fewer
 // spans) from three exact interval bounds: a span costs three corrected float divisions whatever its
-// length.  Triangle sizes span five orders of magnitude (a room wall covers 5e5 pixels, clutter ~10), so
+// length, or a few integer adds when the previous span of the same triangle is known (SpanWalk).  Triangle sizes span five orders of magnitude (a room wall covers 5e5 pixels, clutter ~10), so
 // work is balanced at two granularities:
-//   * small triangles (AABB <= kSmallArea pixels) are set up by one lane each; a warp evaluates its 32
-//     small triangles' spans together and writes their fragments together;
+//   * small triangles (AABB <= kSmallArea pixels) are set up by one lane each, which walks the
+//     triangle's spans; a warp writes its 32 small triangles' fragments together;
 //   * large triangles are cut into units = (span, piece of <= kPiece pixels); units are flat work items
 //     spread over the whole grid, so a wall becomes thousands of independent units.
 // Passes (all stream-ordered, sizes stay on the device):
@@ -130,21 +130,8 @@ SVO_DEV void tri_setup(const svo_triangle *__restrict__ tris, uint32_t t, uint32
 	s.D = 256 * nc;
 }
 
-// The fields of a triangle's set-up that span_interval reads, kept in shared memory so that the lanes
-// of a warp can evaluate the spans of each other's triangles.
-struct SpanSetup {
-	int32_t u0, u1, v0, level;
-	int32_t gu[3], gv[3], pu[3], pv[3];
-};
-
-SVO_DEV void span_setup(const TriSetup &s, SpanSetup &o) {
-	o.u0 = s.u0, o.u1 = s.u1, o.v0 = s.v0, o.level = s.level;
-#pragma unroll
-	for (int k = 0; k < 3; ++k) o.gu[k] = s.gu[k], o.gv[k] = s.gv[k], o.pu[k] = s.pu[k], o.pv[k] = s.pv[k];
-}
-
-// Covered interval [lo, hi] of span v (empty when lo > hi); S is TriSetup or SpanSetup.
-template <typename S> SVO_DEV void span_interval(const S &s, int32_t v, int32_t &lo, int32_t &hi) {
+// Covered interval [lo, hi] of span v (empty when lo > hi).
+SVO_DEV void span_interval(const TriSetup &s, int32_t v, int32_t &lo, int32_t &hi) {
 	const int32_t R = 1 << s.level;
 	lo = s.u0;
 	hi = s.u1;
@@ -166,6 +153,78 @@ template <typename S> SVO_DEV void span_interval(const S &s, int32_t v, int32_t 
 	}
 }
 
+// floor(num / den) exactly, for den > 0 and |num / den| < 2^31: a float estimate, a second one from its
+// remainder (within 1.001 of the remainder's quotient), and one final step.
+SVO_DEV int64_t floor_div_exact(int64_t num, int64_t den) {
+	const float fd = (float)den;
+	int64_t q = (int64_t)__fdividef((float)num, fd); // within |num / den| * 2^-21 + 1 of the quotient
+	int64_t r = num - q * den;
+	const int64_t q2 = (int64_t)floorf(__fdividef((float)r, fd));
+	q += q2;
+	r -= q2 * den; // in [-0.001 den, 1.001 den)
+	if (r < 0) {
+		r += den;
+		--q;
+	} else if (r >= den) {
+		r -= den;
+		++q;
+	}
+	return q;
+}
+
+// The spans of a small triangle row by row.  Edge k bounds span v by floor(Ck(v) / den) with
+// den = 256 |g| (span_interval), and Ck(v + 1) = Ck(v) + 256 h, so the quotient and remainder of row v + 1
+// follow from row v's by integer adds: a row costs a few adds instead of three divisions, and its
+// interval is span_interval's exactly.  An edge with g = 0 only empties rows on its outer side.  For a
+// small triangle every Ck(v) / den lies within 2^29 (|g|, |h| <= 2^16, coordinates < 2^20).
+struct SpanWalk {
+	int32_t q[3], rem[3], dq[3], drem[3], den[3];
+	int32_t kind[3]; // 1: lower bound -q, -1: upper bound q, 2 / -2 (g = 0): empty when q < 0 / q > 0
+	int32_t u0, u1, R;
+};
+
+SVO_DEV void span_walk_init(const TriSetup &s, SpanWalk &w) {
+	w.u0 = s.u0, w.u1 = s.u1, w.R = 1 << s.level;
+#pragma unroll
+	for (int k = 0; k < 3; ++k) {
+		const int32_t g = s.gu[k], h = s.gv[k];
+		if (g != 0) {
+			const int32_t ag = g > 0 ? g : -g;
+			const int64_t den = 256 * (int64_t)ag;
+			const int64_t Ck = (int64_t)g * ((g > 0 ? 256 : 0) - s.pu[k]) +
+			                   (int64_t)h * (256 * (int64_t)s.v0 + (h > 0 ? 256 : 0) - s.pv[k]);
+			const int64_t q = floor_div_exact(Ck, den);
+			int32_t dq = h / ag, dr = h - dq * ag; // floor(h / |g|) and 256 * (h mod |g|): the step 256 h
+			if (dr < 0) dr += ag, --dq;
+			w.kind[k] = g > 0 ? 1 : -1;
+			w.q[k] = (int32_t)q, w.rem[k] = (int32_t)(Ck - q * den);
+			w.dq[k] = dq, w.drem[k] = 256 * dr, w.den[k] = (int32_t)den;
+		} else { // Ck = h * x with x = 256 v + (h > 0 ? 256 : 0) - pv
+			w.kind[k] = h > 0 ? 2 : (h < 0 ? -2 : 0); // h = 0 too only for a degenerate (invalid) triangle
+			w.q[k] = 256 * s.v0 + (h > 0 ? 256 : 0) - s.pv[k];
+			w.rem[k] = 0, w.dq[k] = 256, w.drem[k] = 0, w.den[k] = 1;
+		}
+	}
+}
+
+// The interval [lo, hi] of the walk's current row (empty when lo > hi), then the walk moves to the next row.
+SVO_DEV void span_walk_next(SpanWalk &w, int32_t &lo, int32_t &hi) {
+	lo = w.u0, hi = w.u1;
+	bool empty = false;
+#pragma unroll
+	for (int k = 0; k < 3; ++k) {
+		const int32_t kd = w.kind[k], q = w.q[k];
+		const int32_t b = min(max(kd == 1 ? -q : q, -1), w.R);
+		if (kd == 1) lo = max(lo, b);
+		if (kd == -1) hi = min(hi, b);
+		empty |= (kd == 2 && q < 0) || (kd == -2 && q > 0);
+		w.q[k] = q + w.dq[k];
+		w.rem[k] += w.drem[k];
+		if (w.rem[k] >= w.den[k]) w.rem[k] -= w.den[k], ++w.q[k];
+	}
+	if (empty) hi = lo - 1;
+}
+
 // AABB pixels up to which a triangle is small: set up once by one lane and emitted with its warp's other
 // small triangles (256 measured fastest of 64..1024: fewer raster units, whose set-up repeats per span)
 constexpr int kSmallArea = 256;
@@ -178,22 +237,6 @@ SVO_DEV bool is_large(const TriSetup &s) {
 SVO_DEV uint32_t pieces_per_span(const TriSetup &s) { return (uint32_t)((s.u1 - s.u0) / kPiece + 1); }
 
 SVO_DEV uint32_t unit_count(const TriSetup &s) { return (uint32_t)(s.v1 - s.v0 + 1) * pieces_per_span(s); }
-
-// The spans of a warp's small triangles, evaluated by all 32 lanes together instead of by each
-// triangle's own lane (whose row counts differ, so most lanes would idle): lane j's triangle owns rows
-// [incl[j] - rows_j, incl[j]) of the warp's row list (incl: the inclusive prefix of the row counts, in
-// shared memory at `incl`, the setups at `sp`).  fn(j, row, lo, hi) is called once per row.
-template <typename Fn>
-SVO_DEV void warp_rows(const uint32_t *incl, const SpanSetup *sp, uint32_t total, Fn fn) {
-	uint32_t j = 0;
-	for (uint32_t r = lane_id(); r < total; r += 32) {
-		while (incl[j] <= r) ++j;
-		const uint32_t row = r - (j ? incl[j - 1] : 0u);
-		int32_t lo, hi;
-		span_interval(sp[j], sp[j].v0 + (int32_t)row, lo, hi);
-		fn(j, row, lo, hi);
-	}
-}
 
 // Unit `local` of a large triangle: its span v and the covered pixel interval [lo, hi] inside its piece.
 SVO_DEV void unit_interval(const TriSetup &s, uint32_t local, int32_t &v, int32_t &lo, int32_t &hi) {
@@ -291,9 +334,6 @@ __global__ void __launch_bounds__(kTPB) vox_classify_scan(VoxBatch vb, uint32_t 
 	__shared__ uint32_t s_units[TILE];
 	__shared__ unsigned long long s_warp[kTPB / 32 + 1];
 	__shared__ unsigned long long s_prefix[2];
-	__shared__ SpanSetup s_sp[kTPB];
-	__shared__ uint32_t s_rows[kTPB];
-	const uint32_t wb = threadIdx.x & ~31u;
 	const uint32_t ntiles = (uint32_t)(((uint64_t)n + TILE - 1) / TILE);
 	// the pending tile: its aggregates published, its offsets not yet written
 	uint32_t p_tile = 0xffffffffu, p_cnt[IPT], p_units[IPT];
@@ -319,20 +359,20 @@ __global__ void __launch_bounds__(kTPB) vox_classify_scan(VoxBatch vb, uint32_t 
 					tri_setup(tp, local, lvl, s);
 				}
 				const bool large = is_large(s);
-				// small triangles: fragments = the covered lengths of their spans, counted by the whole warp
-				const uint32_t rows = (s.valid && !large) ? (uint32_t)(s.v1 - s.v0 + 1) : 0u;
-				if (rows) span_setup(s, s_sp[threadIdx.x]);
-				const uint32_t rincl = warp_inclusive_sum(rows);
-				s_rows[threadIdx.x] = rincl;
-				s_cnt[k * kTPB + threadIdx.x] = 0u;
+				// small triangles: fragments = the covered lengths of their spans, walked row by row
+				uint32_t frags = 0;
+				if (s.valid && !large) {
+					SpanWalk sw;
+					span_walk_init(s, sw);
+#pragma unroll 1
+					for (int32_t v = s.v0; v <= s.v1; ++v) {
+						int32_t lo, hi;
+						span_walk_next(sw, lo, hi);
+						frags += hi >= lo ? (uint32_t)(hi - lo + 1) : 0u;
+					}
+				}
+				s_cnt[k * kTPB + threadIdx.x] = frags;
 				s_units[k * kTPB + threadIdx.x] = large ? unit_count(s) : 0u;
-				__syncwarp();
-				uint32_t *c = s_cnt + k * kTPB + wb;
-				warp_rows(s_rows + wb, s_sp + wb, __shfl_sync(kFullMask, rincl, 31),
-				          [&](uint32_t j, uint32_t, int32_t lo, int32_t hi) {
-					          if (hi >= lo) atomicAdd(c + j, (uint32_t)(hi - lo + 1));
-				          });
-				__syncwarp();
 			}
 			__syncthreads();
 			unsigned long long lc = 0, lu = 0;
@@ -473,28 +513,29 @@ SVO_DEV float ratio_f(int64_t num, int64_t den) {
 	return (float)(int32_t)(num >> sh) / (float)(int32_t)(den >> sh);
 }
 
-// The plane depth of a fragment (both emissions).  Pixel u = lo + k of span v lies at plane depth
-// q0 + (r0 - k NU) / D, where num0 = K - NU lo - NV v, q0 = floor(num0 / D) and r0 = num0 - q0 D in
-// [0, D) are taken once at the span's first covered pixel lo.  t = fr0 - k fb (fr0 = r0 / D and
-// fb = NU / D in float; |NU| <= D by the dominant axis) approximates (r0 - k NU) / D within 1e-4 for
-// k < 256, so floor(t) is exact unless t lies within kDepthEps of an integer, where the exact int64
-// division decides.  Covered pixels lie within a voxel of the triangle's depth range, so q0 is exact.
+// The plane depth of a fragment (both emissions).  Pixel u = ua + k of span v lies at plane depth
+// q0 + (r0 - k NU) / D, where num0 = K - NU ua - NV v, q0 = floor(num0 / D) and r0 = num0 - q0 D in
+// [0, D) are taken once per span at an anchor pixel ua: a unit's first covered pixel (covered pixels lie
+// within a voxel of the triangle's depth range, so the windowed division is exact there), or a small
+// triangle's first bounding-box pixel u0 (exact division, carried from row to row).  t = fr0 - k fb
+// (fr0 = r0 / D and fb = NU / D in float; |NU| <= D by the dominant axis) approximates (r0 - k NU) / D
+// within 1e-4 for k < 256, so floor(t) is exact unless t lies within kDepthEps of an integer, where the
+// exact int64 division decides.
 constexpr float kDepthEps = 1.0f / 1024.0f;
 
 SVO_DEV uint32_t field_of(int axis, int which) { return (uint32_t)((axis + which) % 3); } // 0 i, 1 j, 2 depth
 
-// Emission of small triangles, 32 consecutive triangles per warp.  Each lane sets up its triangle and
-// records it in shared memory; the warp then evaluates the spans of all its triangles together (one
-// (triangle, row) pair per lane at a time) into one pool of kRowPool span rows: each row's first covered
-// pixel and length, and its plane depth there in the form above.  Then it writes the group's fragments
-// together: lane k takes fragments k, k+32, ... of the group (contiguous in the list: the small
-// fragments are in triangle order), finds its triangle and row, and packs the fragment from the row's
-// depth (no division, outside the rare near-integer case), so every store instruction covers 256
-// contiguous bytes.  A small triangle has at most 16 spans (kMaxSmallSpans), so the pool holds every
-// span of the warp.  (Tables of kSmallArea rows per lane took twice the shared memory and allowed 5
-// instead of 7 blocks per SM; an int64 division per fragment instead of the row depths cost a third
-// more time on small-triangle scenes.)  In a batch, mesh m's small fragments move up by its shift (the
-// large fragments of earlier meshes).
+// Emission of small triangles, 32 consecutive triangles per warp.  Each lane sets up its triangle,
+// records it in shared memory and walks its rows (SpanWalk) into the warp's pool of kRowPool span rows:
+// each row's first covered pixel and length, and its plane depth at the bounding box's first pixel in
+// the form above.  Then the warp writes the group's fragments together: lane k takes fragments k, k+32,
+// ... of the group (contiguous in the list: the small fragments are in triangle order), finds its row
+// through the chunk's row map and packs the fragment from the row's depth (no division, outside the rare
+// near-integer case), so every store instruction covers 256 contiguous bytes.  A small triangle has at
+// most 16 spans (kMaxSmallSpans), so the pool holds every span of the warp.  (Evaluating the warp's rows
+// one (triangle, row) pair per lane, three divisions per row, took twice as long on small-triangle
+// scenes; so did an int64 division per fragment.)  In a batch, mesh m's small fragments move up by its
+// shift (the large fragments of earlier meshes).  Six blocks of four warps per SM: 80 registers.
 constexpr int kEmitTPB = 128;
 
 // A small triangle's record, as four 16-byte groups: the fragment loop reloads the first two when it
@@ -503,7 +544,7 @@ struct __align__(16) SmallRec {
 	float fb;             // NU / D
 	uint32_t zr;          // z0 | z1 << 16: the depth range
 	uint32_t rgbf;        // rgb | axis << 24 | cols << 26
-	uint32_t rl;          // level << 16
+	uint32_t rl;          // u0 | level << 16: the bounding box's first pixel along the spans
 	uint64_t out;         // output position of its first fragment, minus that fragment's index in the group
 	int32_t vadj;         // pooled row r is span v = r + vadj
 	uint32_t spare;
@@ -532,33 +573,33 @@ SVO_DEV uint64_t pack_fragment(uint32_t axis, uint32_t cols, uint32_t rgb, uint3
 	return (uint64_t)fx | ((uint64_t)fy << 32);
 }
 
-static_assert(2 * kFragChunk + kRowPool <= 32 * sizeof(SpanSetup), "a warp's fragment map and row triangles fit its span set-ups");
+static_assert(kFragChunk == 8 * 32, "a lane scans 8 map entries, one 16-byte group");
 
 template <bool B>
-__global__ void __launch_bounds__(kEmitTPB) vox_emit(VoxBatch vb, uint32_t n, VoxWorkspace w,
+__global__ void __launch_bounds__(kEmitTPB, 6) vox_emit(VoxBatch vb, uint32_t n, VoxWorkspace w,
                                                      uint64_t *__restrict__ frags, uint64_t capacity) {
 	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
 	__shared__ SmallRec s_rec[kEmitTPB];
-	// the lanes' span set-ups; once the spans are evaluated, a warp's slice holds its fragment-to-row map
-	// (kFragChunk entries) and the triangle of each pooled row
-	__shared__ __align__(16) unsigned char s_span_raw[kEmitTPB * sizeof(SpanSetup)];
-	__shared__ uint32_t s_incl[kEmitTPB];                   // span rows of lanes 0..j, inclusive
 	__shared__ uint32_t s_lq[kEmitTPB / 32][kRowPool];       // per pooled row: first pixel lo | q0 << 16 (int16 each)
 	__shared__ float s_fr0[kEmitTPB / 32][kRowPool];         // per pooled row: fr0
 	__shared__ uint16_t s_rcum[kEmitTPB / 32][kRowPool + 1]; // fragments of the group before each row
+	__shared__ uint8_t s_rtri[kEmitTPB / 32][kRowPool];      // per pooled row: its triangle (lane)
+	__shared__ __align__(16) uint16_t s_fmap[kEmitTPB / 32][kFragChunk]; // 1 + the row of each fragment of a chunk
 	const uint32_t lane = lane_id(), wb = threadIdx.x & ~31u, wi = threadIdx.x >> 5;
 	uint32_t *lq_of = s_lq[wi];
 	float *fr0_of = s_fr0[wi];
 	uint16_t *cum = s_rcum[wi];
+	uint8_t *rtri = s_rtri[wi];
+	uint16_t *fmap = s_fmap[wi];
 	SmallRec *wrec = s_rec + wb;
 	const uint4 *wrec4 = reinterpret_cast<const uint4 *>(wrec);
-	SpanSetup *s_sp = reinterpret_cast<SpanSetup *>(s_span_raw);
-	uint16_t *fmap = reinterpret_cast<uint16_t *>(s_span_raw + wb * sizeof(SpanSetup));
-	uint8_t *rtri = reinterpret_cast<uint8_t *>(fmap + kFragChunk);
 	const uint64_t warps = (uint64_t)gridDim.x * blockDim.x / 32;
 	for (uint64_t g = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32; g * 32 < n; g += warps) {
 		const uint64_t t = g * 32 + lane;
 		uint32_t cnt = 0, rows = 0;
+		SpanWalk sw;
+		int64_t rd = 0, nv = 0, dd = 1; // plane depth at the row's pixel u0: quotient qd, remainder rd in [0, D)
+		int32_t qd = 0;
 		if (t < n) {
 			uint64_t off = w.small_off[t];
 			cnt = (uint32_t)(w.small_off[t + 1] - off);
@@ -576,40 +617,36 @@ __global__ void __launch_bounds__(kEmitTPB) vox_emit(VoxBatch vb, uint32_t n, Vo
 					r.fb = ratio_f(S.NU, S.D);
 					r.zr = (uint32_t)S.z0 | ((uint32_t)S.z1 << 16);
 					r.rgbf = (S.rgb & 0xffffffu) | ((uint32_t)S.axis << 24) | ((uint32_t)S.cols << 26);
-					r.rl = (uint32_t)S.level << 16;
+					r.rl = (uint32_t)S.u0 | ((uint32_t)S.level << 16);
 					r.out = off;                    // - first fragment, below
 					r.vadj = S.v0;                  // - first row, below
 					r.K = S.K, r.NU = S.NU, r.NV = S.NV, r.D = S.D;
 					rows = (uint32_t)(S.v1 - S.v0 + 1);
-					span_setup(S, s_sp[threadIdx.x]);
+					span_walk_init(S, sw);
+					const int64_t num = S.K - S.NU * S.u0 - S.NV * S.v0;
+					qd = (int32_t)floor_div_exact(num, S.D);
+					rd = num - (int64_t)qd * S.D, nv = S.NV, dd = S.D;
 				}
 			}
 		}
-		const uint32_t rincl = warp_inclusive_sum(rows);
-		s_incl[threadIdx.x] = rincl;
-		__syncwarp();
+		const uint32_t rincl = warp_inclusive_sum(rows), rfirst = rincl - rows;
 		const uint32_t total_rows = __shfl_sync(kFullMask, rincl, 31);
-		// each pooled row's span and depth at its first pixel: row r belongs to lane j (the lanes in order)
-		uint32_t j = 0;
-		for (uint32_t r = lane; r < total_rows; r += 32) {
-			while (s_incl[wb + j] <= r) ++j;
-			const SpanSetup &sp = s_sp[wb + j];
-			const int32_t v = sp.v0 + (int32_t)(r - (j ? s_incl[wb + j - 1] : 0u));
+		// each lane walks its triangle's rows into the pool: span, plane depth at pixel u0 (|NV| <= D, so
+		// a row moves the quotient by at most one)
+#pragma unroll 1
+		for (uint32_t i = 0; i < rows; ++i) {
+			const uint32_t r = rfirst + i;
 			int32_t lo, hi;
-			span_interval(sp, v, lo, hi);
-			uint32_t len = 0;
-			int32_t q0 = 0;
-			float fr0 = 0.0f;
-			if (hi >= lo) {
-				len = (uint32_t)(hi - lo + 1);
-				const SmallRec &rec = wrec[j];
-				const int64_t num0 = rec.K - rec.NU * lo - rec.NV * v;
-				q0 = (int32_t)floor_div_window(num0, rec.D, -2, (1 << sp.level) + 2);
-				fr0 = ratio_f(num0 - (int64_t)q0 * rec.D, rec.D);
-			}
-			lq_of[r] = (uint32_t)(uint16_t)(int16_t)lo | ((uint32_t)q0 << 16);
-			fr0_of[r] = fr0;
-			cum[r + 1] = (uint16_t)len; // the row's length, scanned below
+			span_walk_next(sw, lo, hi);
+			lq_of[r] = (uint32_t)(uint16_t)(int16_t)lo | ((uint32_t)qd << 16);
+			fr0_of[r] = ratio_f(rd, dd);
+			cum[r + 1] = (uint16_t)(hi >= lo ? hi - lo + 1 : 0); // the row's length, scanned below
+			rtri[r] = (uint8_t)lane;
+			rd -= nv;
+			if (rd >= dd)
+				rd -= dd, ++qd;
+			else if (rd < 0)
+				rd += dd, --qd;
 		}
 		__syncwarp();
 		// row starts: an exclusive scan of the lengths over the rows (at most 32 x kSmallArea fragments)
@@ -626,7 +663,7 @@ __global__ void __launch_bounds__(kEmitTPB) vox_emit(VoxBatch vb, uint32_t n, Vo
 		if (lane == 0) cum[total_rows] = (uint16_t)carry;
 		__syncwarp();
 		// a lane's fragments must be exactly its count (they are: the count pass walked the same spans)
-		const uint32_t rfirst = rincl - rows, tstart = cum[rfirst], tend = cum[rincl];
+		const uint32_t tstart = cum[rfirst], tend = cum[rincl];
 		const bool ok = !rows || tend - tstart == cnt;
 		if (__any_sync(kFullMask, !ok)) continue; // cannot happen; the group is left unwritten
 		if (rows) {
@@ -634,11 +671,6 @@ __global__ void __launch_bounds__(kEmitTPB) vox_emit(VoxBatch vb, uint32_t n, Vo
 			s_rec[threadIdx.x].vadj -= (int32_t)rfirst;
 		}
 		__syncwarp();
-		// the triangle of each pooled row (the span set-ups are no longer read)
-		for (uint32_t r = lane, jr = 0; r < total_rows; r += 32) {
-			while (s_incl[wb + jr] <= r) ++jr;
-			rtri[r] = (uint8_t)jr;
-		}
 		// the group's fragments, kFragChunk at a time: each non-empty row marks its first fragment in the
 		// chunk's map, a max scan over the map gives every fragment its row, and lane k takes fragments
 		// k, k+32, ... of the chunk
@@ -680,9 +712,10 @@ __global__ void __launch_bounds__(kEmitTPB) vox_emit(VoxBatch vb, uint32_t n, Vo
 				const uint32_t zr = g0.y, rgbf = g0.z, rl = g0.w;
 				const uint64_t out = (uint64_t)g1.x | ((uint64_t)g1.y << 32);
 				const int32_t vadj = (int32_t)g1.z;
-				const uint32_t k = f - cum[r], lq = lq_of[r];
-				const int32_t lo = (int32_t)(int16_t)(lq & 0xffffu), v = (int32_t)r + vadj;
-				const float tf = fmaf(-(float)k, fb, fr0_of[r]);
+				const uint32_t lq = lq_of[r];
+				const int32_t u = (int32_t)(int16_t)(lq & 0xffffu) + (int32_t)(f - cum[r]), v = (int32_t)r + vadj;
+				// the row's depth is taken at pixel u0 of the bounding box: k = u - u0 < 256
+				const float tf = fmaf(-(float)(u - (int32_t)(rl & 0xffffu)), fb, fr0_of[r]);
 				const float fl = floorf(tf);
 				const float fr = tf - fl;
 				int32_t z;
@@ -690,13 +723,12 @@ __global__ void __launch_bounds__(kEmitTPB) vox_emit(VoxBatch vb, uint32_t n, Vo
 					z = ((int32_t)lq >> 16) + (int32_t)fl;
 				} else {
 					const SmallRec &rec = wrec[jt];
-					const int64_t num = rec.K - rec.NU * (lo + (int32_t)k) - rec.NV * v;
+					const int64_t num = rec.K - rec.NU * u - rec.NV * v;
 					z = (int32_t)floor_div_window(num, rec.D, -2, (1 << (rl >> 16)) + 2);
 				}
 				const int32_t z0 = (int32_t)(zr & 0xffffu), z1 = (int32_t)(zr >> 16);
 				const uint32_t zz = (uint32_t)(z < z0 ? z0 : (z > z1 ? z1 : z));
-				frags[out + f] = pack_fragment((rgbf >> 24) & 3u, (rgbf >> 26) & 1u, rgbf, (uint32_t)(lo + (int32_t)k),
-				                               (uint32_t)v, zz);
+				frags[out + f] = pack_fragment((rgbf >> 24) & 3u, (rgbf >> 26) & 1u, rgbf, (uint32_t)u, (uint32_t)v, zz);
 			}
 			__syncwarp();
 		}
