@@ -143,18 +143,41 @@ PROFILE_FILES = {"build_leaf_windows": "build_leaf_windows", "bucket_scatter": "
                  "march_camera": "march_kernel", "vox_emit_units": "vox_emit_units"}
 
 
-def profiled_traffic(label: str, workload: str) -> dict:
-    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the kernel, from its
-    committed ncu capture on this workload (profiles/<kernel>_<workload>.md), or null without one."""
+def profiled_value(label: str, workload: str, key: str):
+    """(value, path) of a `key: value` line of the kernel's committed ncu capture on this workload
+    (profiles/<kernel>_<workload>.md), or (None, None) without one."""
     name = PROFILE_FILES.get(label)
+    if name is None:
+        return None, None
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles", f"{name}_{workload}.md")
-    if name is None or not os.path.exists(path):
-        return {"traffic": None}
+    if not os.path.exists(path):
+        return None, None
     with open(path) as f:
         for line in f:
-            if line.startswith("dram_bytes_per_launch:"):
-                return {"traffic": int(line.split(":", 1)[1]), "traffic_source": os.path.relpath(path)}
-    return {"traffic": None}
+            if line.startswith(key + ":"):
+                return int(line.split(":", 1)[1]), os.path.relpath(path)
+    return None, None
+
+
+def profiled_traffic(label: str, workload: str) -> dict:
+    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the kernel, from its
+    committed ncu capture on this workload, or null without one."""
+    traffic, path = profiled_value(label, workload, "dram_bytes_per_launch")
+    return {"traffic": traffic, "traffic_source": path} if traffic is not None else {"traffic": None}
+
+
+def issue_roofline(label: str, workload: str, launch_ms: float, sms: int, sm_mhz) -> dict | None:
+    """The kernel's instruction-issue rate against what the SMs can issue (4 schedulers per SM, one warp
+    instruction each per clock, at the SM clock sampled during the timed region): the warp instructions
+    of one launch from its committed ncu capture on this workload, divided by the live launch time."""
+    wi, path = profiled_value(label, workload, "warp_instructions_per_launch")
+    if wi is None or not sm_mhz or not launch_ms:
+        return None
+    achieved = wi / (launch_ms * 1e-3) / 1e9
+    peak = sms * 4 * sm_mhz * 1e6 / 1e9
+    return {"unit": "G warp instructions/s", "achieved": achieved, "peak": peak, "frac": achieved / peak,
+            "warp_instructions_per_launch": wi, "source": path,
+            "peak_basis": f"{sms} SMs x 4 schedulers x 1 warp instruction per clock at {sm_mhz:.0f} MHz"}
 
 
 def engine_arm(args, env, device, workload: str | None = None, light: bool = False) -> dict:
@@ -337,6 +360,11 @@ def engine_arm(args, env, device, workload: str | None = None, light: bool = Fal
     if dom_name.startswith("march"):
         roofline["limiter"] = ("instruction issue: node words stay in L1/L2, DRAM idle (ncu, "
                                "profiles/march_kernel_room_1024.md); the HBM fraction is low by construction")
+        issue = issue_roofline(dom_name, workload, dom_launch_ms,
+                               torch.cuda.get_device_properties(device).multi_processor_count,
+                               clocks.get("sm_mhz") or clocks.get("sm_max_mhz"))
+        if issue:
+            roofline["issue"] = issue
 
     stages = {
         "voxelize_ms": vox_ms, "build_ms": build_ms, "march_ms": march_ms,
@@ -1048,6 +1076,8 @@ def summary_block(line: dict) -> dict:
     out = {"step_ms": r(line.get("value")), "e2e_ms": r((line.get("e2e") or {}).get("value")),
            "e2e_copy_floor_ms": r(e2e_link.get("floor_ms")),
            "march_frac": r(line["roofline"].get("frac"))}
+    if line["roofline"].get("issue"):
+        out["march_issue_frac"] = r(line["roofline"]["issue"]["frac"])
     p = line.get("parity")
     if p:
         out["parity"] = {"fragments": p["fragments"], "octree": p["octree"], "hits_equal_frac": r(p["hits_equal_frac"], 6)}

@@ -47,3 +47,17 @@ def test_summary_block_carries_the_headline_figures():
 def test_summary_block_without_the_optional_legs():
     out = bench.summary_block({"value": 2.0, "roofline": {"frac": 0.1}})
     assert out["step_ms"] == 2.0 and out["e2e_ms"] is None and out["e2e_copy_floor_ms"] is None
+
+
+def test_issue_roofline_of_the_march_from_its_committed_capture():
+    out = bench.issue_roofline("march_camera", "room_1024", launch_ms=0.4169, sms=152, sm_mhz=2050.6)
+    assert out is not None and out["warp_instructions_per_launch"] == 350298511
+    assert abs(out["peak"] - 152 * 4 * 2.0506) < 1e-6
+    assert 0.6 < out["frac"] < 0.75 and out["source"].endswith("march_kernel_room_1024.md")
+    assert bench.issue_roofline("march_camera", "no_such_workload", 0.4, 152, 2000.0) is None
+    assert bench.issue_roofline("dense_mark", "room_1024", 0.1, 152, 2000.0) is None
+
+
+def test_summary_block_carries_the_issue_fraction():
+    out = bench.summary_block({"value": 1.27, "roofline": {"frac": 0.18, "issue": {"frac": 0.674}}})
+    assert out["march_issue_frac"] == 0.674
