@@ -103,6 +103,31 @@ def test_voxelize_edge_cases(cuda):
         assert_same_fragments(gpu_voxelize(tris, level), oracle.voxelize(tris, level))
 
 
+@pytest.mark.parametrize("level", [3, 7, 10, 12])
+def test_voxelize_small_triangles_on_pixel_boundaries(cuda, level):
+    """Small triangles (bounding boxes around the 256-pixel bound) whose vertices sit on pixel corners,
+    pixel centres and sub-pixel steps, a third of them with an edge along an axis and many of them
+    slivers or steep: the spans walked row by row with integer steps give the oracle's intervals
+    exactly, on both sides of every edge."""
+    g = np.random.default_rng(100 + level)
+    R = 1 << level
+    n = 6000
+    base = g.integers(0, max(R - 17, 1), size=(n, 1, 3)).astype(np.float64)
+    step = g.integers(0, 17, size=(n, 3, 3)).astype(np.float64)
+    frac = g.choice([0.0, 0.5, 1 / 256, 255 / 256, 128 / 256], size=(n, 3, 3))
+    pts = (base + step + frac) / R
+    axis = g.integers(0, 3, size=n)
+    for i in np.nonzero(np.arange(n) % 3 == 0)[0]:  # vertices 0 and 1 differ along one axis only
+        others = [a for a in range(3) if a != axis[i]]
+        pts[i, 1, others] = pts[i, 0, others]
+    tris = np.zeros(n, TRIANGLE_DTYPE)
+    tris["v"] = np.clip(pts, 0.0, 1.0).reshape(n, 9).astype(np.float32)
+    tris["rgb"] = g.integers(0, 1 << 24, size=(n, 3))
+    ref = oracle.voxelize(tris, level)
+    assert len(ref) > n
+    assert_same_fragments(gpu_voxelize(tris, level), ref)
+
+
 def test_voxelize_empty(cuda):
     got = gpu_voxelize(np.zeros(0, TRIANGLE_DTYPE), 6)
     assert len(got) == 0
