@@ -510,9 +510,7 @@ int svo_voxelize_into(const svo_triangle *tris, uint32_t n_tris, uint32_t level,
 	const uint64_t cap = lo;
 	cudaStream_t s = (cudaStream_t)stream;
 	vox_workspace_layout(workspace, n_tris, cap, w);
-	SVO_CK(vox_launch_count(tris, n_tris, level, w, s), "voxelize count");
-	SVO_CK(vox_launch_totals(w, s), "voxelize totals");
-	SVO_CK(vox_launch_emit(tris, n_tris, level, w, frags, capacity, s), "voxelize emit");
+	SVO_CK(vox_launch_count_emit(tris, n_tris, level, w, frags, capacity, s), "voxelize count and emit");
 	// count_dev[0] = fragments, count_dev[1] = status bits (totals[2])
 	SVO_CK(cudaMemcpyAsync(count_dev, w.totals, sizeof(uint64_t), cudaMemcpyDeviceToDevice, s), "voxelize count copy");
 	SVO_CK(cudaMemcpyAsync(count_dev + 1, w.totals + 2, sizeof(uint64_t), cudaMemcpyDeviceToDevice, s),

@@ -167,6 +167,10 @@ size_t vox_workspace_layout(void *ws, uint32_t n, uint64_t unit_cap, VoxWorkspac
 cudaError_t vox_launch_count(const svo_triangle *tris, uint32_t n, uint32_t level, const VoxWorkspace &w,
                              cudaStream_t stream);
 cudaError_t vox_launch_totals(const VoxWorkspace &w, cudaStream_t stream);
+// Count, totals and emission into `frags` (capacity fragments) in one stream-ordered sequence; the
+// small-triangle emission overlaps the unit scan on a second stream.
+cudaError_t vox_launch_count_emit(const svo_triangle *tris, uint32_t n, uint32_t level, const VoxWorkspace &w,
+                                  uint64_t *frags, uint64_t capacity, cudaStream_t stream);
 // two_streams = false: every launch on `stream`, no side stream or event is made (svo_voxelize_static)
 cudaError_t vox_launch_emit(const svo_triangle *tris, uint32_t n, uint32_t level, const VoxWorkspace &w,
                             uint64_t *frags, uint64_t capacity, cudaStream_t stream,

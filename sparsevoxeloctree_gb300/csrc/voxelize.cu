@@ -951,6 +951,41 @@ static void launch_emit(const VoxBatch &vb, uint32_t n, uint32_t tune_level, con
 
 cudaError_t vox_set_wait_fault(uint32_t limit, uint32_t withheld) { return set_wait_fault_here(limit, withheld); }
 
+// Count, totals and emission of one mesh into an output buffer known in advance.  The small-triangle
+// emission needs only the count pass's triangle offsets, so it starts on a second stream as soon as the
+// count pass ends, beside the unit scan, the totals and the unit emission.
+cudaError_t vox_launch_count_emit(const svo_triangle *tris, uint32_t n, uint32_t level, const VoxWorkspace &w,
+                                  uint64_t *frags, uint64_t capacity, cudaStream_t stream) {
+	cudaError_t e = clear_count_state(n, w, stream);
+	if (e != cudaSuccess) return e;
+	if (n == 0) return vox_launch_totals(w, stream);
+	const VoxBatch vb = single_vox(tris, level);
+	const int sms = device_sm_count();
+	if (n >= kBigCountTris)
+		SVO_LAUNCH("vox_classify_scan", stream,
+		           ::svo::launch_k(vox_classify_scan<false, 2 * kIPT>,
+		                           std::min((n + 2 * kTile - 1) / (2 * kTile), resident_grid(vox_classify_scan<false, 2 * kIPT>, kTPB)),
+		                           kTPB, 0, stream, vb, n, w););
+	else
+		SVO_LAUNCH("vox_classify_scan", stream,
+		           ::svo::launch_k(vox_classify_scan<false, kIPT>,
+		                           std::min((n + kTile - 1) / kTile, resident_grid(vox_classify_scan<false, kIPT>, kTPB)), kTPB, 0,
+		                           stream, vb, n, w););
+	const uint32_t per_sm = (uint32_t)tune_value(kTuneEmitBlocks, level, n);
+	SideFork fork(stream, true);
+	cudaStream_t side = fork.side();
+	SVO_LAUNCH("vox_emit", side,
+	           ::svo::launch_k(vox_emit<false>, (uint32_t)sms * per_sm * (kTPB / kEmitTPB), kEmitTPB, 0, side, vb, n, w, frags, capacity););
+	fork.mark_side(0);
+	SVO_LAUNCH("vox_unit_scan", stream, ::svo::launch_k(vox_unit_scan<false>, (uint32_t)sms * 4, kTPB, 0, stream, vb, n, w););
+	e = vox_launch_totals(w, stream);
+	if (e != cudaSuccess) return e;
+	SVO_LAUNCH("vox_emit_units", stream,
+	           ::svo::launch_k(vox_emit_units<false>, (uint32_t)sms * std::max(1u, per_sm / 2), kTPB, 0, stream, vb, n, w, frags, capacity););
+	fork.main_waits(0);
+	return cudaGetLastError();
+}
+
 cudaError_t vox_launch_count(const svo_triangle *tris, uint32_t n, uint32_t level, const VoxWorkspace &w,
                              cudaStream_t stream) {
 	cudaError_t e = clear_count_state(n, w, stream);
