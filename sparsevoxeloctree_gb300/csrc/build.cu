@@ -1301,6 +1301,30 @@ static BuildBatch single_batch(const BuildWorkspace &w, uint32_t count, uint32_t
 	return bb;
 }
 
+// The leaf windows' bookkeeping: windows per mesh, each listed bucket's item range and leaf span, the
+// first and last bucket of every window.  Without sparse depths none of it reads the bucketed copy, so it
+// runs on the build's second stream beside the bucketed copy.
+struct LeafTables {
+	uint4 *bmeta;
+	uint32_t *win_base, *wfirst, *wlast;
+};
+
+template <bool B>
+static void launch_leaf_prep(const BuildBatch &bb, uint32_t M, uint32_t nb_total, const uint32_t *boff,
+                             const uint32_t *blist, const BuildState *gstate, const LeafTables &lt, bool any_sparse,
+                             uint64_t *sorted, const uint32_t *cache, cudaStream_t stream) {
+	const int sms = device_sm_count();
+	const uint32_t meta_items = std::max<uint32_t>(nb_total, M);
+	SVO_LAUNCH("leaf_window_scan", stream, ::svo::launch_k(leaf_window_scan<B>, 1, kTPB, 0, stream, bb, lt.win_base););
+	SVO_LAUNCH("bucket_meta", stream,
+	           ::svo::launch_k(bucket_meta<B>, grid_for(meta_items, kTPB, (uint32_t)sms * 4), kTPB, 0, stream, bb, boff, blist, gstate, lt.bmeta););
+	if (any_sparse)
+		SVO_LAUNCH("bucket_span_sparse", stream,
+		           ::svo::launch_k(bucket_span_sparse<B>, grid_for((uint64_t)nb_total * 32, kTPB, (uint32_t)sms * 8), kTPB, 0, stream, sorted, bb, blist, cache, gstate, lt.bmeta););
+	SVO_LAUNCH("bucket_windows", stream,
+	           ::svo::launch_k(bucket_windows<B>, grid_for(nb_total, kTPB, (uint32_t)sms * 4), kTPB, 0, stream, bb, blist, gstate, lt.bmeta, lt.win_base, lt.wfirst, lt.wlast););
+}
+
 // The stages shared by a single build and a batch.  `maxD` = deepest dense depth of any mesh.
 template <bool B>
 static void launch_dense_and_scatter(const uint64_t *frags, uint64_t n, uint32_t tune_level, const BuildBatch &bb,
@@ -1308,7 +1332,7 @@ static void launch_dense_and_scatter(const uint64_t *frags, uint64_t n, uint32_t
                                      uint32_t dense_words, uint32_t items_total, uint32_t nb_total, BuildState *gstate,
                                      unsigned long long *descs, uint32_t *bcount, uint32_t *boff, uint32_t *bfill,
                                      uint32_t *blist, unsigned long long *bdescs, uint64_t *sorted,
-                                     cudaStream_t stream) {
+                                     const LeafTables *early_leaf_prep, cudaStream_t stream) {
 	const int sms = device_sm_count();
 	const uint32_t sweep = (uint32_t)sms * (uint32_t)tune_value(kTuneSweepBlocks, tune_level, n);
 	SVO_LAUNCH("build_init", stream, ::svo::launch_k(build_init<B>, M, 256, 0, stream, bb, gstate););
@@ -1332,7 +1356,11 @@ static void launch_dense_and_scatter(const uint64_t *frags, uint64_t n, uint32_t
 		fork.side_waits_main();
 		SVO_LAUNCH("dense_write", aux,
 		           ::svo::launch_k(dense_write<B>, grid_for(items_total, kTPB, (uint32_t)sms * 16), kTPB, 0, aux, bb, items_total););
+	} else {
+		fork.side_waits_main(); // the leaf ranges of the level tables
 	}
+	if (early_leaf_prep) // no sparse depths: the leaf windows' bookkeeping beside the bucketed copy
+		launch_leaf_prep<B>(bb, M, nb_total, boff, blist, gstate, *early_leaf_prep, false, sorted, nullptr, aux);
 	fork.mark_side(1);
 	fork.main_waits(0); // bucket offsets
 	// the bucketed copy: leaf items when the leaf parents are dense (their bitmap is final now), fragments
@@ -1358,25 +1386,17 @@ static void launch_sparse(const uint64_t *sorted, uint32_t count, uint32_t level
 	}
 }
 
+// The leaf stage; `prepared`: the windows' bookkeeping already ran beside the bucketed copy.
 template <bool B>
 static void launch_leaf_stage(const BuildBatch &bb, uint32_t M, uint32_t tune_level, uint64_t n, uint32_t nb_total,
-                              const uint32_t *boff, const uint32_t *blist, const BuildState *gstate, uint4 *bmeta,
-                              uint32_t *win_base, uint32_t *wfirst, uint32_t *wlast, bool any_sparse,
-                              uint64_t *sorted, const uint32_t *cache, cudaStream_t stream) {
+                              const uint32_t *boff, const uint32_t *blist, const BuildState *gstate, const LeafTables &lt,
+                              bool any_sparse, bool prepared, uint64_t *sorted, const uint32_t *cache, cudaStream_t stream) {
 	const int sms = device_sm_count();
 	const size_t smem = kLeafSlots * sizeof(unsigned long long); // 32 KB: below the default dynamic limit
-	const uint32_t meta_items = std::max<uint32_t>(nb_total, M);
 	const uint32_t blocks = (uint32_t)sms * (uint32_t)tune_value(kTuneLeafBlocks, tune_level, n);
-	SVO_LAUNCH("leaf_window_scan", stream, ::svo::launch_k(leaf_window_scan<B>, 1, kTPB, 0, stream, bb, win_base););
-	SVO_LAUNCH("bucket_meta", stream,
-	           ::svo::launch_k(bucket_meta<B>, grid_for(meta_items, kTPB, (uint32_t)sms * 4), kTPB, 0, stream, bb, boff, blist, gstate, bmeta););
-	if (any_sparse)
-		SVO_LAUNCH("bucket_span_sparse", stream,
-		           ::svo::launch_k(bucket_span_sparse<B>, grid_for((uint64_t)nb_total * 32, kTPB, (uint32_t)sms * 8), kTPB, 0, stream, sorted, bb, blist, cache, gstate, bmeta););
-	SVO_LAUNCH("bucket_windows", stream,
-	           ::svo::launch_k(bucket_windows<B>, grid_for(nb_total, kTPB, (uint32_t)sms * 4), kTPB, 0, stream, bb, blist, gstate, bmeta, win_base, wfirst, wlast););
+	if (!prepared) launch_leaf_prep<B>(bb, M, nb_total, boff, blist, gstate, lt, any_sparse, sorted, cache, stream);
 	SVO_LAUNCH("build_leaf_windows", stream,
-	           ::svo::launch_k(build_leaf_windows<B>, blocks, kTPB, smem, stream, sorted, bb, bmeta, win_base, wfirst, wlast, const_cast<BuildState *>(gstate)););
+	           ::svo::launch_k(build_leaf_windows<B>, blocks, kTPB, smem, stream, sorted, bb, lt.bmeta, lt.win_base, lt.wfirst, lt.wlast, const_cast<BuildState *>(gstate)););
 }
 
 cudaError_t build_launch_interior(const uint64_t *frags, uint32_t count, uint32_t level, uint32_t *pool,
@@ -1389,9 +1409,11 @@ cudaError_t build_launch_interior(const uint64_t *frags, uint32_t count, uint32_
 	if (e != cudaSuccess) return e;
 	const BuildBatch bb = single_batch(w, count, level, pool, capacity);
 	const uint32_t items = dense_items(level, w.dv.D, w.dv.off);
+	const LeafTables lt{w.bmeta, w.win_base, w.wfirst, w.wlast};
+	const bool sparse = level > w.dv.D + 1;
 	launch_dense_and_scatter<false>(frags, count, level, bb, 1, w.dv.D, w.dense_words, items, w.nb, w.state, w.descs, w.bcount,
-	                                w.boff, w.bfill, w.blist, w.bdescs, w.sorted, stream);
-	if (level > w.dv.D + 1)
+	                                w.boff, w.bfill, w.blist, w.bdescs, w.sorted, sparse ? nullptr : &lt, stream);
+	if (sparse)
 		launch_sparse(w.sorted, count, level, w.dv, pool, capacity, w.cache, w.tagbits, w.tag_words, w.state, w.descs,
 		              w.state, stream);
 	return cudaGetLastError();
@@ -1400,8 +1422,10 @@ cudaError_t build_launch_interior(const uint64_t *frags, uint32_t count, uint32_
 cudaError_t build_launch_leaf(uint32_t count, uint32_t level, uint32_t *pool, uint64_t capacity,
                               const BuildWorkspace &w, cudaStream_t stream) {
 	const BuildBatch bb = single_batch(w, count, level, pool, capacity);
-	launch_leaf_stage<false>(bb, 1, level, count, w.nb, w.boff, w.blist, w.state, w.bmeta, w.win_base, w.wfirst,
-	                         w.wlast, level > w.dv.D + 1, w.sorted, w.cache, stream);
+	const LeafTables lt{w.bmeta, w.win_base, w.wfirst, w.wlast};
+	const bool sparse = level > w.dv.D + 1; // without sparse depths build_launch_interior prepared the windows
+	launch_leaf_stage<false>(bb, 1, level, count, w.nb, w.boff, w.blist, w.state, lt, sparse, !sparse, w.sorted, w.cache,
+	                         stream);
 	return cudaGetLastError();
 }
 
@@ -1423,9 +1447,10 @@ cudaError_t build_launch_batch(const uint64_t *frags, const BuildBatchPlan &p, v
 	if (e == cudaSuccess) e = cudaMemsetAsync(p.bfill, 0, (size_t)p.nb_total * 4, stream);
 	if (e == cudaSuccess) e = cudaMemsetAsync(p.bdescs, 0, p.bdesc_count * sizeof(unsigned long long), stream);
 	if (e != cudaSuccess) return e;
+	const LeafTables lt{p.bmeta, p.win_base, p.wfirst, p.wlast};
 	launch_dense_and_scatter<true>(frags, p.frags_total, p.max_level, p.bb, p.M, p.max_D, p.dense_total, p.items_total,
-	                               p.nb_total,
-	                               p.gstate, p.descs, p.bcount, p.boff, p.bfill, p.blist, p.bdescs, p.sorted, stream);
+	                               p.nb_total, p.gstate, p.descs, p.bcount, p.boff, p.bfill, p.blist, p.bdescs, p.sorted,
+	                               p.any_sparse ? nullptr : &lt, stream);
 	for (uint32_t m = 0; m < p.M; ++m) {
 		const BuildMesh &md = p.meshes[m];
 		if (md.level <= md.dv.D + 1) continue; // no sparse depths (an empty mesh still sets its leaf range)
@@ -1435,8 +1460,8 @@ cudaError_t build_launch_batch(const uint64_t *frags, const BuildBatchPlan &p, v
 		launch_sparse(p.sorted + sb, md.count, md.level, md.dv, md.pool, md.capacity, p.cache + sb, p.tagbits, p.tag_words,
 		              md.state, p.descs, p.gstate, stream);
 	}
-	launch_leaf_stage<true>(p.bb, p.M, p.max_level, p.frags_total, p.nb_total, p.boff, p.blist, p.gstate, p.bmeta,
-	                        p.win_base, p.wfirst, p.wlast, p.any_sparse, p.sorted, p.cache, stream);
+	launch_leaf_stage<true>(p.bb, p.M, p.max_level, p.frags_total, p.nb_total, p.boff, p.blist, p.gstate, lt,
+	                        p.any_sparse, !p.any_sparse, p.sorted, p.cache, stream);
 	SVO_LAUNCH("build_export", stream,
 	           ::svo::launch_k(build_export<true>, (p.M + 127) / 128, 128, 0, stream, p.bb, p.gstate, (uint32_t *)result_dev););
 	return cudaGetLastError();
