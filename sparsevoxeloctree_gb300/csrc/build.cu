@@ -164,9 +164,27 @@ SVO_DEV void flag_bad_fragment(BuildState *state, BuildState *g) {
 }
 
 // ------------------------------------------------------------------------------------------ init
-// Block m clears mesh m's state (and block 0 the batch-wide state of a batch).
-template <bool B> __global__ void build_init(BuildBatch bb, BuildState *gstate) {
+// The scratch a build zeroes before its first sweep (scan descriptors, dense bitmaps, bucket counters):
+// up to four 16-byte-aligned ranges whose sizes are multiples of 4 bytes.
+struct ClearList {
+	void *p[4];
+	size_t bytes[4];
+};
+
+// Zeroes the ranges (every block, grid-stride, 16-byte stores), and block m < M clears mesh m's state
+// (block 0 also the batch-wide state of a batch): one launch instead of a memset per range.
+template <bool B> __global__ void build_init(BuildBatch bb, BuildState *gstate, ClearList cl) {
 	griddep_wait(); // programmatic dependent launch: the predecessor's writes are visible after this
+	const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, nth = (uint64_t)gridDim.x * blockDim.x;
+#pragma unroll
+	for (int r = 0; r < 4; ++r) {
+		uint4 *d4 = reinterpret_cast<uint4 *>(cl.p[r]);
+		const uint64_t n4 = cl.bytes[r] / 16;
+		for (uint64_t i = tid; i < n4; i += nth) d4[i] = make_uint4(0u, 0u, 0u, 0u);
+		uint32_t *d = reinterpret_cast<uint32_t *>(cl.p[r]);
+		for (uint64_t i = 4 * n4 + tid; i < cl.bytes[r] / 4; i += nth) d[i] = 0u;
+	}
+	if (blockIdx.x >= batch_size<B>(bb)) return;
 	BuildState *state = mesh_at<B>(bb, blockIdx.x).state;
 	uint32_t *s = reinterpret_cast<uint32_t *>(state);
 	for (uint32_t k = threadIdx.x; k < sizeof(BuildState) / 4; k += blockDim.x) s[k] = 0u;
@@ -1332,10 +1350,11 @@ static void launch_dense_and_scatter(const uint64_t *frags, uint64_t n, uint32_t
                                      uint32_t dense_words, uint32_t items_total, uint32_t nb_total, BuildState *gstate,
                                      unsigned long long *descs, uint32_t *bcount, uint32_t *boff, uint32_t *bfill,
                                      uint32_t *blist, unsigned long long *bdescs, uint64_t *sorted,
-                                     const LeafTables *early_leaf_prep, cudaStream_t stream) {
+                                     const LeafTables *early_leaf_prep, const ClearList &clear, cudaStream_t stream) {
 	const int sms = device_sm_count();
 	const uint32_t sweep = (uint32_t)sms * (uint32_t)tune_value(kTuneSweepBlocks, tune_level, n);
-	SVO_LAUNCH("build_init", stream, ::svo::launch_k(build_init<B>, M, 256, 0, stream, bb, gstate););
+	SVO_LAUNCH("build_init", stream,
+	           ::svo::launch_k(build_init<B>, std::max<uint32_t>(M, (uint32_t)sms * 4), 256, 0, stream, bb, gstate, clear););
 	SVO_LAUNCH("dense_mark", stream,
 	           ::svo::launch_k(dense_mark<B>, grid_for(n, kTPB * kSweepRuns, sweep), kTPB, 0, stream, frags, n, bb, bcount););
 	// Two independent chains after the sweep: the bucket scan (then, once the dense prefix is final, the
@@ -1401,18 +1420,16 @@ static void launch_leaf_stage(const BuildBatch &bb, uint32_t M, uint32_t tune_le
 
 cudaError_t build_launch_interior(const uint64_t *frags, uint32_t count, uint32_t level, uint32_t *pool,
                                   uint64_t capacity, const BuildWorkspace &w, cudaStream_t stream) {
-	cudaError_t e = cudaMemsetAsync(w.descs, 0, w.desc_count * sizeof(unsigned long long), stream);
-	if (e == cudaSuccess && w.dense_words) e = cudaMemsetAsync(w.dv.bits, 0, (size_t)w.dense_words * 4, stream);
-	// bucket counts and cursors are adjacent: one memset
-	if (e == cudaSuccess) e = cudaMemsetAsync(w.bcount, 0, (char *)w.boff - (char *)w.bcount, stream);
-	if (e == cudaSuccess) e = cudaMemsetAsync(w.bdescs, 0, w.bdesc_count * sizeof(unsigned long long), stream);
-	if (e != cudaSuccess) return e;
+	// scan descriptors, dense bitmaps, bucket counts and cursors (adjacent), bucket-scan descriptors
+	const ClearList clear{{w.descs, w.dv.bits, w.bcount, w.bdescs},
+	                      {w.desc_count * sizeof(unsigned long long), (size_t)w.dense_words * 4,
+	                       (size_t)((char *)w.boff - (char *)w.bcount), w.bdesc_count * sizeof(unsigned long long)}};
 	const BuildBatch bb = single_batch(w, count, level, pool, capacity);
 	const uint32_t items = dense_items(level, w.dv.D, w.dv.off);
 	const LeafTables lt{w.bmeta, w.win_base, w.wfirst, w.wlast};
 	const bool sparse = level > w.dv.D + 1;
 	launch_dense_and_scatter<false>(frags, count, level, bb, 1, w.dv.D, w.dense_words, items, w.nb, w.state, w.descs, w.bcount,
-	                                w.boff, w.bfill, w.blist, w.bdescs, w.sorted, sparse ? nullptr : &lt, stream);
+	                                w.boff, w.bfill, w.blist, w.bdescs, w.sorted, sparse ? nullptr : &lt, clear, stream);
 	if (sparse)
 		launch_sparse(w.sorted, count, level, w.dv, pool, capacity, w.cache, w.tagbits, w.tag_words, w.state, w.descs,
 		              w.state, stream);
@@ -1440,17 +1457,15 @@ cudaError_t build_launch_export(const BuildWorkspace &w, uint32_t level, uint32_
 // meshes that have them (one mesh at a time), the leaf stage over all buckets, and one export record per
 // mesh to result_dev.
 cudaError_t build_launch_batch(const uint64_t *frags, const BuildBatchPlan &p, void *result_dev, cudaStream_t stream) {
-	cudaError_t e = cudaMemsetAsync(p.descs, 0, p.desc_count * sizeof(unsigned long long), stream);
-	if (e == cudaSuccess && p.dense_total)
-		e = cudaMemsetAsync(p.bb.dense_bits, 0, (size_t)p.dense_total * 4, stream);
-	if (e == cudaSuccess) e = cudaMemsetAsync(p.bcount, 0, (size_t)p.nb_total * 4, stream);
-	if (e == cudaSuccess) e = cudaMemsetAsync(p.bfill, 0, (size_t)p.nb_total * 4, stream);
-	if (e == cudaSuccess) e = cudaMemsetAsync(p.bdescs, 0, p.bdesc_count * sizeof(unsigned long long), stream);
-	if (e != cudaSuccess) return e;
+	// scan descriptors, dense bitmaps, bucket counts and cursors (adjacent), bucket-scan descriptors
+	const ClearList clear{{p.descs, p.bb.dense_bits, p.bcount, p.bdescs},
+	                      {p.desc_count * sizeof(unsigned long long), (size_t)p.dense_total * 4,
+	                       (size_t)((char *)p.boff - (char *)p.bcount), p.bdesc_count * sizeof(unsigned long long)}};
+	cudaError_t e = cudaSuccess;
 	const LeafTables lt{p.bmeta, p.win_base, p.wfirst, p.wlast};
 	launch_dense_and_scatter<true>(frags, p.frags_total, p.max_level, p.bb, p.M, p.max_D, p.dense_total, p.items_total,
 	                               p.nb_total, p.gstate, p.descs, p.bcount, p.boff, p.bfill, p.blist, p.bdescs, p.sorted,
-	                               p.any_sparse ? nullptr : &lt, stream);
+	                               p.any_sparse ? nullptr : &lt, clear, stream);
 	for (uint32_t m = 0; m < p.M; ++m) {
 		const BuildMesh &md = p.meshes[m];
 		if (md.level <= md.dv.D + 1) continue; // no sparse depths (an empty mesh still sets its leaf range)
