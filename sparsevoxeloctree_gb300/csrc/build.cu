@@ -796,7 +796,9 @@ __global__ void __launch_bounds__(kTPB) bucket_scatter(const uint64_t *__restric
 				} else if (items && level > 1) { // parent cell m (depth level-1); the bucket key is its prefix
 					const uint32_t *pbits = md.dv.bits + md.parent_off;
 					const uint32_t *pprefix = md.dv.prefix + md.parent_off;
-					const uint32_t leaf_begin = md.state->lv[level].begin;
+					// the leaf range starts after the blocks of every occupied cell above the parents'
+					// depth (dense_finish's level table, which may still be in flight on the other stream)
+					const uint32_t leaf_begin = 8u * (1u + __ldg(pprefix));
 					const uint32_t m = morton_tab(s_spread, x, y, z, 1), w = m >> 5;
 					key[k] = m >> (3 * (md.bshift - 1));
 					out[k] = ((uint64_t)(octant_at(x, y, z, 0) +
@@ -1371,8 +1373,10 @@ static void launch_dense_and_scatter(const uint64_t *frags, uint64_t n, uint32_t
 			           ::svo::launch_k(dense_reduce<B>, std::min<uint32_t>(bb.reduce_total, (uint32_t)sms * 8), 256, 0, stream, bb););
 		SVO_LAUNCH("dense_scan", stream,
 		           ::svo::launch_k(dense_scan<B>, grid_for(dense_words, kDenseTile, (uint32_t)sms * 4), kTPB, 0, stream, bb, dense_words, gstate, descs););
-		SVO_LAUNCH("dense_finish", stream, ::svo::launch_k(dense_finish<B>, (M + 127) / 128, 128, 0, stream, bb););
 		fork.side_waits_main();
+		// the level table, the interior words and (without sparse depths) the leaf bookkeeping on the
+		// second stream; the bucketed copy needs none of them
+		SVO_LAUNCH("dense_finish", aux, ::svo::launch_k(dense_finish<B>, (M + 127) / 128, 128, 0, aux, bb););
 		SVO_LAUNCH("dense_write", aux,
 		           ::svo::launch_k(dense_write<B>, grid_for(items_total, kTPB, (uint32_t)sms * 16), kTPB, 0, aux, bb, items_total););
 	} else {

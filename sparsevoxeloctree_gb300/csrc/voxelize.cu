@@ -905,9 +905,8 @@ static VoxBatch single_vox(const svo_triangle *tris, uint32_t level) {
 }
 
 static cudaError_t clear_count_state(uint32_t n, const VoxWorkspace &w, cudaStream_t stream) {
-	cudaError_t e = cudaMemsetAsync(w.descs, 0, w.desc_bytes, stream);
-	if (e != cudaSuccess) return e;
-	e = cudaMemsetAsync(w.counters, 0, kCtrCount * sizeof(uint32_t), stream);
+	// the scan descriptors and the counters are adjacent in the layout: one memset
+	cudaError_t e = cudaMemsetAsync(w.descs, 0, (size_t)((char *)(w.counters + kCtrCount) - (char *)w.descs), stream);
 	if (e != cudaSuccess) return e;
 	if (n == 0) {
 		e = cudaMemsetAsync(w.small_off, 0, sizeof(uint64_t), stream);
