@@ -952,7 +952,8 @@ cudaError_t vox_set_wait_fault(uint32_t limit, uint32_t withheld) { return set_w
 
 // Count, totals and emission of one mesh into an output buffer known in advance.  The small-triangle
 // emission needs only the count pass's triangle offsets, so it starts on a second stream as soon as the
-// count pass ends, beside the unit scan, the totals and the unit emission.
+// count pass ends, beside the unit scan and the unit emission; the totals (read only after the call)
+// follow it there once the unit scan is done.
 cudaError_t vox_launch_count_emit(const svo_triangle *tris, uint32_t n, uint32_t level, const VoxWorkspace &w,
                                   uint64_t *frags, uint64_t capacity, cudaStream_t stream) {
 	cudaError_t e = clear_count_state(n, w, stream);
@@ -975,10 +976,11 @@ cudaError_t vox_launch_count_emit(const svo_triangle *tris, uint32_t n, uint32_t
 	cudaStream_t side = fork.side();
 	SVO_LAUNCH("vox_emit", side,
 	           ::svo::launch_k(vox_emit<false>, (uint32_t)sms * per_sm * (kTPB / kEmitTPB), kEmitTPB, 0, side, vb, n, w, frags, capacity););
-	fork.mark_side(0);
 	SVO_LAUNCH("vox_unit_scan", stream, ::svo::launch_k(vox_unit_scan<false>, (uint32_t)sms * 4, kTPB, 0, stream, vb, n, w););
-	e = vox_launch_totals(w, stream);
+	fork.side_waits_main();
+	e = vox_launch_totals(w, side);
 	if (e != cudaSuccess) return e;
+	fork.mark_side(0);
 	SVO_LAUNCH("vox_emit_units", stream,
 	           ::svo::launch_k(vox_emit_units<false>, (uint32_t)sms * std::max(1u, per_sm / 2), kTPB, 0, stream, vb, n, w, frags, capacity););
 	fork.main_waits(0);
