@@ -1360,8 +1360,9 @@ static void launch_dense_and_scatter(const uint64_t *frags, uint64_t n, uint32_t
 	SVO_LAUNCH("dense_mark", stream,
 	           ::svo::launch_k(dense_mark<B>, grid_for(n, kTPB * kSweepRuns, sweep), kTPB, 0, stream, frags, n, bb, bcount););
 	// Two independent chains after the sweep: the bucket scan (then, once the dense prefix is final, the
-	// interior words) on a second stream, the dense reduce / scan on the caller's stream; the bucketed
-	// copy needs the bucket offsets and the dense prefix, and the caller's later work waits for both.
+	// level table, the interior words and, without sparse depths, the leaf windows' bookkeeping) on a
+	// second stream, the dense reduce / scan and then the bucketed copy on the caller's stream; the copy
+	// needs the bucket offsets and the dense prefix, and the caller's later work waits for both.
 	SideFork fork(stream, tune_value(kTuneBuildStreams, tune_level, n) == 2);
 	cudaStream_t aux = fork.side();
 	SVO_LAUNCH("bucket_scan", aux,
