@@ -206,8 +206,10 @@ void svo_tune_reset(void);
 /* ------------------------------------------------------------------ voxelize (Voxelizer) */
 
 /* Voxelizer::Create + CmdVoxelize (src/Voxelizer.cpp:5-26, 134-179): count pass, exact allocation,
- * emit pass.  `tris` (device) holds n_tris triangles.  On success *out owns a new device buffer with
- * exactly out->count fragments.  Blocks the calling thread once to read the fragment count, as the
+ * emit pass.  `tris` (device) holds n_tris triangles.  On success *out owns a new device buffer holding
+ * out->count fragments (out->capacity >= out->count: when the same triangle buffer, count and level
+ * were voxelized recently, the list is sized by that earlier count and the emission is queued before
+ * the count is read back).  Blocks the calling thread once to read the fragment count, as the
  * reference does (src/Voxelizer.cpp:151-155). */
 int svo_voxelize(const svo_triangle *tris, uint32_t n_tris, uint32_t level, svo_fraglist *out, void *stream);
 

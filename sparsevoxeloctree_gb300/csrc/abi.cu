@@ -386,6 +386,120 @@ static int voxelize_count_pass(const svo_triangle *tris, uint32_t n_tris, uint32
 	return fail(SVO_ERR_CAPACITY, "voxelize workspace retry failed");
 }
 
+// The fragment counts of the meshes this process voxelized last (their triangle buffer, triangle count and
+// level).  A repeated call with the library's own memory emits into a list of that size right after the
+// count pass, so the count's readback overlaps the emission instead of the device idling while the host
+// reads the count and launches it; a count that turns out larger is emitted again into an exact list.
+struct RecentVox {
+	const void *tris;
+	uint32_t n, level;
+	uint64_t total;
+};
+static std::mutex g_recent_mu;
+static RecentVox g_recent[8];
+static uint32_t g_recent_next = 0;
+
+static uint64_t recent_total(const void *tris, uint32_t n, uint32_t level) {
+	std::lock_guard<std::mutex> lock(g_recent_mu);
+	for (const RecentVox &r : g_recent)
+		if (r.tris == tris && r.n == n && r.level == level) return r.total;
+	return 0;
+}
+
+static void note_recent(const void *tris, uint32_t n, uint32_t level, uint64_t total) {
+	std::lock_guard<std::mutex> lock(g_recent_mu);
+	for (RecentVox &r : g_recent)
+		if (r.tris == tris && r.n == n && r.level == level) {
+			r.total = total;
+			return;
+		}
+	g_recent[g_recent_next++ % 8] = RecentVox{tris, n, level, total};
+}
+
+// svo_voxelize_ex's path for a mesh whose count is known from an earlier call (`guess` fragments, the
+// library's stream-ordered memory): count, emission into `guess` slots, then the count's readback.
+// Returns SVO_OK with *done = false when the count pass needs a larger unit scratch (the caller runs the
+// ordinary path, which counts again).
+static int voxelize_overlapped(const svo_triangle *tris, uint32_t n_tris, uint32_t level, uint64_t guess, Mem &mem,
+                               svo_fraglist *out, bool *done) {
+	*done = false;
+	thread_local unsigned long long *tot = nullptr; // page-locked, so the copy is asynchronous
+	thread_local cudaEvent_t ready = nullptr;
+	thread_local int ready_dev = -1; // the event belongs to the device current when it was made
+	int dev = 0;
+	if (cudaGetDevice(&dev) != cudaSuccess || (ready && ready_dev != dev)) return SVO_OK; // the ordinary path
+	if (!tot) {
+		note_allocation();
+		if (cudaHostAlloc((void **)&tot, 4 * sizeof(unsigned long long), cudaHostAllocDefault) != cudaSuccess) {
+			tot = nullptr;
+			return SVO_OK; // the ordinary path
+		}
+	}
+	if (!ready) {
+		if (cudaEventCreateWithFlags(&ready, cudaEventDisableTiming) != cudaSuccess) {
+			ready = nullptr;
+			return SVO_OK;
+		}
+		ready_dev = dev;
+	}
+	const uint64_t cap = std::max<uint64_t>(vox_default_unit_cap(n_tris), g_units_seen.load(std::memory_order_relaxed));
+	void *ws = nullptr, *frags = nullptr;
+	VoxWorkspace w;
+	SVO_CK(mem.get(&ws, vox_workspace_bytes(n_tris, cap)), "voxelize workspace");
+	vox_workspace_layout(ws, n_tris, cap, w);
+	cudaError_t e = vox_launch_count(tris, n_tris, level, w, mem.s);
+	if (e == cudaSuccess) e = vox_launch_totals(w, mem.s);
+	if (e == cudaSuccess) e = cudaMemcpyAsync(tot, w.totals, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, mem.s);
+	if (e == cudaSuccess) e = cudaEventRecord(ready, mem.s);
+	if (e == cudaSuccess) e = mem.get(&frags, guess * sizeof(uint64_t));
+	if (e == cudaSuccess) e = vox_launch_emit(tris, n_tris, level, w, (uint64_t *)frags, guess, mem.s);
+	if (e == cudaSuccess) e = cudaEventSynchronize(ready);
+	if (e != cudaSuccess) {
+		mem.put(frags);
+		mem.put(ws);
+		return cuda_fail(e, "voxelize");
+	}
+	const uint64_t total = tot[0], units = tot[1];
+	const uint32_t status = (uint32_t)tot[2];
+	if (units < 0xffffffffull) note_units(units);
+	if (status & kStatusUnits) { // the units did not fit the scratch: nothing of them was emitted
+		mem.put(frags);
+		mem.put(ws);
+		return SVO_OK;
+	}
+	int rc = status_to_error(status, "voxelize count");
+	if (!rc && total > 0xffffffffull)
+		rc = fail(SVO_ERR_CAPACITY, "%llu fragments exceed the 32-bit fragment count", (unsigned long long)total);
+	if (rc) {
+		mem.put(frags);
+		mem.put(ws);
+		return rc;
+	}
+	uint64_t capacity = guess;
+	if (total > guess) { // the list was short: emit again into an exact one (the scans are unchanged)
+		mem.put(frags);
+		frags = nullptr;
+		e = mem.get(&frags, total * sizeof(uint64_t));
+		if (e == cudaSuccess) e = vox_launch_emit(tris, n_tris, level, w, (uint64_t *)frags, total, mem.s);
+		if (e != cudaSuccess) {
+			mem.put(frags);
+			mem.put(ws);
+			return cuda_fail(e, "voxelize emit");
+		}
+		capacity = total;
+	}
+	mem.put(ws);
+	note_recent(tris, n_tris, level, total);
+	out->data = (uint64_t *)frags;
+	out->count = (uint32_t)total;
+	out->level = level;
+	out->capacity = capacity;
+	out->owned = mem.owned();
+	out->units = (uint32_t)units;
+	*done = true;
+	return SVO_OK;
+}
+
 int svo_voxelize_count(const svo_triangle *tris, uint32_t n_tris, uint32_t level, uint64_t *count_host,
                        void *stream) {
 	int rc;
@@ -408,6 +522,12 @@ int svo_voxelize_ex(const svo_triangle *tris, uint32_t n_tris, uint32_t level, c
 	if (!out) return fail(SVO_ERR_INVALID, "null output fragment list");
 	cudaStream_t s = (cudaStream_t)stream;
 	Mem mem{alloc, s};
+	if (!(alloc && alloc->alloc) && n_tris) { // a caller's allocator may reuse a released list at once
+		const uint64_t guess = recent_total(tris, n_tris, level);
+		bool done = false;
+		if (guess && (rc = voxelize_overlapped(tris, n_tris, level, guess, mem, out, &done))) return rc;
+		if (done) return SVO_OK;
+	}
 	void *ws = nullptr;
 	VoxWorkspace w;
 	uint64_t total = 0, units = 0;
@@ -428,6 +548,7 @@ int svo_voxelize_ex(const svo_triangle *tris, uint32_t n_tris, uint32_t level, c
 		mem.put(frags);
 		return cuda_fail(e, "voxelize emit");
 	}
+	if (!(alloc && alloc->alloc)) note_recent(tris, n_tris, level, total);
 	out->data = (uint64_t *)frags;
 	out->count = (uint32_t)total;
 	out->level = level;
