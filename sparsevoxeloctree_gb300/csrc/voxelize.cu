@@ -533,9 +533,10 @@ SVO_DEV uint32_t field_of(int axis, int which) { return (uint32_t)((axis + which
 // through the chunk's row map and packs the fragment from the row's depth (no division, outside the rare
 // near-integer case), so every store instruction covers 256 contiguous bytes.  A small triangle has at
 // most 16 spans (kMaxSmallSpans), so the pool holds every span of the warp.  (Evaluating the warp's rows
-// one (triangle, row) pair per lane, three divisions per row, took twice as long on small-triangle
-// scenes; so did an int64 division per fragment.)  In a batch, mesh m's small fragments move up by its
-// shift (the large fragments of earlier meshes).  Six blocks of four warps per SM: 80 registers.
+// one (triangle, row) pair per lane, three divisions per row, made this kernel 20-30% slower on
+// small-triangle scenes; an int64 division per fragment cost another 6%.)  In a batch, mesh m's small
+// fragments move up by its shift (the large fragments of earlier meshes).  Six blocks of four warps per
+// SM: 80 registers.
 constexpr int kEmitTPB = 128;
 
 // A small triangle's record, as four 16-byte groups: the fragment loop reloads the first two when it
