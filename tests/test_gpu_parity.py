@@ -128,6 +128,40 @@ def test_voxelize_small_triangles_on_pixel_boundaries(cuda, level):
     assert_same_fragments(gpu_voxelize(tris, level), ref)
 
 
+def test_voxelize_repeated_mesh_with_changed_triangles(cuda):
+    """svo_voxelize on the same triangle buffer again: the list is sized by the earlier count and the
+    emission queued before the count is read back.  The buffer's triangles then change so that the
+    count grows (the list is emitted again into an exact one) and then shrinks (the list keeps the
+    larger capacity); every call returns exactly the oracle's fragments."""
+    import ctypes
+
+    import torch
+    from sparsevoxeloctree_gb300 import _lib
+    lib = _lib.load()
+    s = scenes.plain_256()
+    base = np.asarray(s.tris, TRIANGLE_DTYPE)
+    bigger = base.copy()
+    bigger["v"] = np.clip(0.5 + (bigger["v"] - 0.5) * 1.3, 0.0, 1.0)  # larger triangles: more fragments
+    smaller = np.zeros(len(base), TRIANGLE_DTYPE)  # same triangle count: half of them, the rest degenerate
+    smaller[: len(base) // 2] = base[: len(base) // 2]
+    dev = torch.empty(base.nbytes, dtype=torch.uint8, device="cuda")
+    counts, capacities = [], []
+    for tris in (base, base, bigger, bigger, smaller):
+        dev.copy_(torch.from_numpy(np.ascontiguousarray(tris).view(np.uint8).reshape(-1)))
+        fl = _lib.Fraglist()
+        _lib.check(lib.svo_voxelize(ctypes.c_void_p(dev.data_ptr()), len(tris), s.level, ctypes.byref(fl), None))
+        got = np.empty(fl.count, np.uint64)
+        if fl.count:
+            _lib.check(lib.svo_download(ctypes.c_void_p(got.ctypes.data), ctypes.c_void_p(fl.data),
+                                        fl.count * 8, 1, None))
+        assert_same_fragments(got, oracle.voxelize(tris, s.level))
+        counts.append(fl.count)
+        capacities.append(fl.capacity)
+        lib.svo_fraglist_destroy(ctypes.byref(fl), None)
+    assert counts[2] > counts[1] and counts[4] < counts[3]
+    assert capacities[4] >= counts[4] and all(c >= n for c, n in zip(capacities, counts))
+
+
 def test_voxelize_empty(cuda):
     got = gpu_voxelize(np.zeros(0, TRIANGLE_DTYPE), 6)
     assert len(got) == 0
